@@ -1,0 +1,599 @@
+// api.cu — the extern "C" boundary declared in include/cpq.h.
+//
+// Handles own device memory; arrays passed in are caller-owned.  Every entry
+// point catches its own failures and returns a cp_status with a message in a
+// thread-local string; nothing here exits the process (the reference's die()
+// does, src/lib/log.h:46-49).  Workspaces that the caller does not provide
+// come from a per-device stream-ordered memory pool, so a query allocates
+// nothing synchronously and stays on its stream.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/cpq.h"
+#include "bvh.cuh"
+
+using namespace cpq;
+
+struct cp_mesh {
+    Bvh bvh;
+};
+
+struct cp_batch {
+    Bvh bvh;
+    int64_t* d_qoff = nullptr;
+    std::vector<int64_t> h_qoff;
+    // CUDA-graph cache of the last captured query launch sequence
+    cudaGraphExec_t exec = nullptr;
+    std::vector<uintptr_t> graph_key;
+};
+
+namespace {
+
+thread_local std::string g_last_error;
+
+cp_status fail(cp_status s, const std::string& msg) {
+    g_last_error = msg;
+    return s;
+}
+
+cp_status cuda_fail(cudaError_t e, const char* where) {
+    if (e == cudaErrorMemoryAllocation) {
+        cudaGetLastError();
+        return fail(CP_ERROR_OUT_OF_MEMORY, std::string(where) + ": " + cudaGetErrorString(e));
+    }
+    return fail(CP_ERROR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CP_CUDA(call, where)                          \
+    do {                                              \
+        cudaError_t e_ = (call);                      \
+        if (e_ != cudaSuccess) return cuda_fail(e_, where); \
+    } while (0)
+
+cp_status require_gpu() {
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) {
+        cudaGetLastError();
+        return fail(CP_ERROR_NOT_SUPPORTED, "no CUDA device is available");
+    }
+    return CP_SUCCESS;
+}
+
+// Per-device pool for stream-ordered workspaces that stays warm between calls.
+std::mutex g_pool_mu;
+std::vector<cudaMemPool_t> g_pools;
+
+cudaError_t get_pool(cudaMemPool_t* out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    std::lock_guard<std::mutex> lock(g_pool_mu);
+    if ((int)g_pools.size() <= dev) g_pools.resize(dev + 1, nullptr);
+    if (!g_pools[dev]) {
+        cudaMemPoolProps props = {};
+        props.allocType = cudaMemAllocationTypePinned;
+        props.handleTypes = cudaMemHandleTypeNone;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        cudaMemPool_t pool;
+        e = cudaMemPoolCreate(&pool, &props);
+        if (e != cudaSuccess) return e;
+        uint64_t threshold = UINT64_MAX;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+        g_pools[dev] = pool;
+    }
+    *out = g_pools[dev];
+    return cudaSuccess;
+}
+
+cudaError_t ws_alloc(void** p, size_t bytes, cudaStream_t st) {
+    cudaMemPool_t pool;
+    cudaError_t e = get_pool(&pool);
+    if (e != cudaSuccess) return e;
+    return cudaMallocFromPoolAsync(p, bytes ? bytes : 256, pool, st);
+}
+
+cp_status to_build_params(const cp_build_opts* o, BuildParams* p) {
+    cp_build_opts d;
+    cp_build_opts_default(&d);
+    if (!o) o = &d;
+    if (o->branching != 2 && o->branching != 4 && o->branching != 8)
+        return fail(CP_ERROR_INVALID_VALUE, "branching must be 2, 4 or 8");
+    if (o->leaf_size < 1 || o->leaf_size > kMaxLeafSize)
+        return fail(CP_ERROR_INVALID_VALUE, "leaf_size must be in 1..15");
+    if (o->collapse != CP_COLLAPSE_COUNT && o->collapse != CP_COLLAPSE_SAH)
+        return fail(CP_ERROR_INVALID_VALUE, "collapse must be CP_COLLAPSE_COUNT or CP_COLLAPSE_SAH");
+    if (o->collapse == CP_COLLAPSE_SAH &&
+        !(o->sah_node_cost >= 0.0f && o->sah_tri_cost > 0.0f && std::isfinite(o->sah_node_cost) &&
+          std::isfinite(o->sah_tri_cost)))
+        return fail(CP_ERROR_INVALID_VALUE, "SAH costs must be finite, node >= 0, triangle > 0");
+    p->K = o->branching;
+    p->leaf_size = o->leaf_size;
+    p->collapse = o->collapse;
+    p->c_node = o->sah_node_cost;
+    p->c_tri = o->sah_tri_cost;
+    return CP_SUCCESS;
+}
+
+cp_status to_query_params(const cp_query_opts* o, QueryParams* q) {
+    cp_query_opts d;
+    cp_query_opts_default(&d);
+    if (!o) o = &d;
+    int block = o->block_size ? o->block_size : d.block_size;
+    if (block < 32 || block > 256 || block % 32)
+        return fail(CP_ERROR_INVALID_VALUE, "block_size must be a multiple of 32 in 32..256");
+    int ss = o->short_stack ? o->short_stack : d.short_stack;
+    if (ss != 4 && ss != 8 && ss != 16)
+        return fail(CP_ERROR_INVALID_VALUE, "short_stack must be 4, 8 or 16");
+    if (o->blocks_per_sm < 0 || o->blocks_per_sm > 64)
+        return fail(CP_ERROR_INVALID_VALUE, "blocks_per_sm must be in 0..64");
+    q->block = block;
+    q->sort = o->sort_queries ? 1 : 0;
+    q->blocks_per_sm = o->blocks_per_sm;
+    q->short_stack = ss;
+    return CP_SUCCESS;
+}
+
+cp_status build_common(Bvh& b, const float* verts, int64_t vstride_bytes, const int32_t* tris,
+                       const std::vector<int64_t>& voff, const std::vector<int64_t>& toff,
+                       const cp_build_opts* opts, cp_stream_t stream) {
+    BuildParams p;
+    cp_status s = to_build_params(opts, &p);
+    if (s != CP_SUCCESS) return s;
+    if (vstride_bytes < 12 || vstride_bytes % 4)
+        return fail(CP_ERROR_INVALID_VALUE, "vertex stride must be a multiple of 4 bytes and >= 12");
+    bool bad = false;
+    std::string why;
+    cudaError_t e = bvh_build(b, verts, vstride_bytes / 4, tris, voff, toff, p,
+                              reinterpret_cast<cudaStream_t>(stream), &bad, &why);
+    if (e != cudaSuccess) {
+        bvh_free(b);
+        return cuda_fail(e, "BVH build");
+    }
+    if (bad) {
+        bvh_free(b);
+        return fail(CP_ERROR_INVALID_VALUE, "BVH build: " + why);
+    }
+    if (b.stack_bound > 256) {
+        bvh_free(b);
+        return fail(CP_ERROR_NOT_SUPPORTED, "BVH deeper than the traversal stack supports");
+    }
+    return CP_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+CP_API void cp_build_opts_default(cp_build_opts* o) {
+    if (!o) return;
+    o->branching = 2;
+    o->leaf_size = 4;
+    o->collapse = CP_COLLAPSE_COUNT;
+    o->sah_node_cost = 1.0f;
+    o->sah_tri_cost = 1.0f;
+}
+
+CP_API void cp_query_opts_default(cp_query_opts* o) {
+    if (!o) return;
+    o->block_size = 256;
+    o->sort_queries = 1;
+    o->blocks_per_sm = 0;
+    o->short_stack = 8;
+}
+
+CP_API const char* cp_last_error_string(void) { return g_last_error.c_str(); }
+
+CP_API const char* cp_status_string(cp_status s) {
+    switch (s) {
+        case CP_SUCCESS: return "success";
+        case CP_ERROR_INVALID_VALUE: return "invalid value";
+        case CP_ERROR_OUT_OF_MEMORY: return "out of memory";
+        case CP_ERROR_CUDA: return "CUDA error";
+        case CP_ERROR_DEVICE_FAULT: return "device fault";
+        case CP_ERROR_NOT_SUPPORTED: return "not supported";
+        case CP_ERROR_SCRATCH_TOO_SMALL: return "scratch too small";
+    }
+    return "unknown status";
+}
+
+CP_API int32_t cp_version(void) { return 100; }
+
+CP_API int32_t cp_size_class(int64_t nt) {
+    int32_t c = 0;
+    while (nt > 1) {
+        nt >>= 1;
+        ++c;
+    }
+    return c;
+}
+
+CP_API cp_status cp_mesh_create(const float* verts, int64_t nv, int64_t vstride, const int32_t* tris,
+                                int64_t nt, const cp_build_opts* opts, cp_stream_t stream,
+                                cp_mesh** out) {
+    if (!out) return fail(CP_ERROR_INVALID_VALUE, "out is NULL");
+    *out = nullptr;
+    if (!verts || !tris) return fail(CP_ERROR_INVALID_VALUE, "verts or tris is NULL");
+    if (nv <= 0 || nt <= 0) return fail(CP_ERROR_INVALID_VALUE, "mesh needs at least one vertex and one triangle");
+    if (nt > kMaxTriangles) return fail(CP_ERROR_NOT_SUPPORTED, "more than 2^27 - 1 triangles");
+    if (nv > INT32_MAX) return fail(CP_ERROR_INVALID_VALUE, "more than 2^31 - 1 vertices");
+    cp_status s = require_gpu();
+    if (s != CP_SUCCESS) return s;
+    cp_mesh* m = new (std::nothrow) cp_mesh();
+    if (!m) return fail(CP_ERROR_OUT_OF_MEMORY, "host allocation of the handle failed");
+    s = build_common(m->bvh, verts, vstride, tris, {0, nv}, {0, nt}, opts, stream);
+    if (s != CP_SUCCESS) {
+        delete m;
+        return s;
+    }
+    *out = m;
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_mesh_refit(cp_mesh* m, const float* verts, int64_t vstride, cp_stream_t stream) {
+    if (!m || !verts) return fail(CP_ERROR_INVALID_VALUE, "mesh or verts is NULL");
+    if (vstride < 12 || vstride % 4)
+        return fail(CP_ERROR_INVALID_VALUE, "vertex stride must be a multiple of 4 bytes and >= 12");
+    CP_CUDA(bvh_refit(m->bvh, verts, vstride / 4, reinterpret_cast<cudaStream_t>(stream)), "refit");
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_mesh_destroy(cp_mesh* m) {
+    if (!m) return CP_SUCCESS;
+    bvh_free(m->bvh);
+    delete m;
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_mesh_info(const cp_mesh* m, cp_mesh_info_t* o) {
+    if (!m || !o) return fail(CP_ERROR_INVALID_VALUE, "mesh or out is NULL");
+    const Bvh& b = m->bvh;
+    o->num_vertices = b.nv;
+    o->num_triangles = b.nt;
+    o->num_binary_nodes = 2 * b.nt - 1;
+    o->num_wide_nodes = b.num_wide;
+    o->num_leaves = b.num_leaves;
+    o->branching = b.p.K;
+    o->leaf_size = b.p.leaf_size;
+    o->max_wide_depth = b.max_wide_depth;
+    o->stack_bound = b.stack_bound;
+    o->device_bytes = (int64_t)b.device_bytes;
+    o->build_ms = b.build_ms;
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_mesh_device_status(cp_mesh* m, cp_stream_t stream, uint32_t* bits) {
+    if (!m || !bits) return fail(CP_ERROR_INVALID_VALUE, "mesh or bits is NULL");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    uint32_t h = 0;
+    CP_CUDA(cudaMemcpyAsync(&h, m->bvh.status, sizeof(uint32_t), cudaMemcpyDeviceToHost, st), "status read");
+    CP_CUDA(cudaStreamSynchronize(st), "status read");
+    CP_CUDA(cudaMemsetAsync(m->bvh.status, 0, sizeof(uint32_t), st), "status clear");
+    *bits = h;
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_query_workspace_size(const cp_mesh* m, int64_t nq, const cp_query_opts* opts,
+                                         size_t* bytes) {
+    if (!m || !bytes) return fail(CP_ERROR_INVALID_VALUE, "mesh or bytes is NULL");
+    if (nq < 0) return fail(CP_ERROR_INVALID_VALUE, "negative query count");
+    QueryParams qp;
+    cp_status s = to_query_params(opts, &qp);
+    if (s != CP_SUCCESS) return s;
+    *bytes = query_workspace_bytes(m->bvh, nq, qp);
+    return CP_SUCCESS;
+}
+
+static cp_status query_impl(const Bvh& b, const float* q, int64_t nq, const int64_t* d_qoff,
+                            const QueryParams& qp, float* op, float* od, int32_t* ot, float* ob,
+                            void* ws, size_t ws_bytes, cudaStream_t st) {
+    const size_t need = query_workspace_bytes(b, nq, qp);
+    void* own = nullptr;
+    if (!ws) {
+        CP_CUDA(ws_alloc(&own, need, st), "workspace allocation");
+        ws = own;
+        ws_bytes = need;
+    } else if (ws_bytes < need) {
+        return fail(CP_ERROR_SCRATCH_TOO_SMALL, "workspace smaller than cp_query_workspace_size()");
+    }
+    cudaError_t e = bvh_query(b, q, nq, d_qoff, qp, op, od, ot, ob, ws, ws_bytes, st);
+    if (own) cudaFreeAsync(own, st);
+    if (e != cudaSuccess) return cuda_fail(e, "query");
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_query(const cp_mesh* m, const float* queries, int64_t nq,
+                          const cp_query_opts* opts, float* out_point, float* out_dist,
+                          int32_t* out_tri, float* out_bary, void* workspace, size_t ws_bytes,
+                          cp_stream_t stream) {
+    if (!m) return fail(CP_ERROR_INVALID_VALUE, "mesh is NULL");
+    if (nq < 0) return fail(CP_ERROR_INVALID_VALUE, "negative query count");
+    if (nq > INT32_MAX) return fail(CP_ERROR_NOT_SUPPORTED, "more than 2^31 - 1 queries in one call");
+    if (nq == 0) return CP_SUCCESS;
+    if (!queries) return fail(CP_ERROR_INVALID_VALUE, "queries is NULL");
+    QueryParams qp;
+    cp_status s = to_query_params(opts, &qp);
+    if (s != CP_SUCCESS) return s;
+    return query_impl(m->bvh, queries, nq, nullptr, qp, out_point, out_dist, out_tri, out_bary,
+                      workspace, ws_bytes, reinterpret_cast<cudaStream_t>(stream));
+}
+
+CP_API cp_status cp_query_host(const cp_mesh* m, const float* queries, int64_t nq,
+                               const cp_query_opts* opts, float* out_point, float* out_dist,
+                               int32_t* out_tri, float* out_bary, cp_stream_t stream) {
+    if (!m) return fail(CP_ERROR_INVALID_VALUE, "mesh is NULL");
+    if (nq < 0) return fail(CP_ERROR_INVALID_VALUE, "negative query count");
+    if (nq == 0) return CP_SUCCESS;
+    if (!queries) return fail(CP_ERROR_INVALID_VALUE, "queries is NULL");
+    QueryParams qp;
+    cp_status s = to_query_params(opts, &qp);
+    if (s != CP_SUCCESS) return s;
+    const Bvh& b = m->bvh;
+    cudaStream_t user = reinterpret_cast<cudaStream_t>(stream);
+    const int64_t chunk = nq < (int64_t(1) << 22) ? nq : (int64_t(1) << 22);
+    const int64_t nchunks = (nq + chunk - 1) / chunk;
+    const int nslots = nchunks > 1 ? 2 : 1;
+    cudaStream_t st[2] = {nullptr, nullptr};
+    cudaEvent_t start = nullptr, done[2] = {nullptr, nullptr};
+    struct Slot {
+        float *q, *p, *d, *b;
+        int32_t* t;
+        void* ws;
+    } slot[2] = {};
+    const size_t wsb = query_workspace_bytes(b, chunk, qp);
+    cp_status result = CP_SUCCESS;
+    auto check = [&](cudaError_t e, const char* where) {
+        if (e != cudaSuccess && result == CP_SUCCESS) result = cuda_fail(e, where);
+        return e == cudaSuccess;
+    };
+    check(cudaEventCreateWithFlags(&start, cudaEventDisableTiming), "event");
+    check(cudaEventRecord(start, user), "event");
+    for (int k = 0; k < nslots && result == CP_SUCCESS; ++k) {
+        check(cudaStreamCreateWithFlags(&st[k], cudaStreamNonBlocking), "stream");
+        check(cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming), "event");
+        check(cudaStreamWaitEvent(st[k], start, 0), "stream wait");
+        check(ws_alloc(reinterpret_cast<void**>(&slot[k].q), sizeof(float) * 3 * chunk, st[k]), "alloc");
+        if (out_point) check(ws_alloc(reinterpret_cast<void**>(&slot[k].p), sizeof(float) * 3 * chunk, st[k]), "alloc");
+        if (out_dist) check(ws_alloc(reinterpret_cast<void**>(&slot[k].d), sizeof(float) * chunk, st[k]), "alloc");
+        if (out_tri) check(ws_alloc(reinterpret_cast<void**>(&slot[k].t), sizeof(int32_t) * chunk, st[k]), "alloc");
+        if (out_bary) check(ws_alloc(reinterpret_cast<void**>(&slot[k].b), sizeof(float) * 2 * chunk, st[k]), "alloc");
+        check(ws_alloc(&slot[k].ws, wsb, st[k]), "alloc");
+    }
+    for (int64_t c = 0; c < nchunks && result == CP_SUCCESS; ++c) {
+        const int k = (int)(c % nslots);
+        const int64_t off = c * chunk;
+        const int64_t cnt = (nq - off) < chunk ? (nq - off) : chunk;
+        Slot& sl = slot[k];
+        check(cudaMemcpyAsync(sl.q, queries + 3 * off, sizeof(float) * 3 * cnt, cudaMemcpyHostToDevice, st[k]), "H2D");
+        if (result != CP_SUCCESS) break;
+        cudaError_t e = bvh_query(b, sl.q, cnt, nullptr, qp, sl.p, sl.d, sl.t, sl.b, sl.ws, wsb, st[k]);
+        if (!check(e, "query")) break;
+        if (out_point) check(cudaMemcpyAsync(out_point + 3 * off, sl.p, sizeof(float) * 3 * cnt, cudaMemcpyDeviceToHost, st[k]), "D2H");
+        if (out_dist) check(cudaMemcpyAsync(out_dist + off, sl.d, sizeof(float) * cnt, cudaMemcpyDeviceToHost, st[k]), "D2H");
+        if (out_tri) check(cudaMemcpyAsync(out_tri + off, sl.t, sizeof(int32_t) * cnt, cudaMemcpyDeviceToHost, st[k]), "D2H");
+        if (out_bary) check(cudaMemcpyAsync(out_bary + 2 * off, sl.b, sizeof(float) * 2 * cnt, cudaMemcpyDeviceToHost, st[k]), "D2H");
+    }
+    for (int k = 0; k < nslots; ++k) {
+        if (!st[k]) continue;
+        void* ptrs[6] = {slot[k].q, slot[k].p, slot[k].d, slot[k].t, slot[k].b, slot[k].ws};
+        for (void* p : ptrs)
+            if (p) cudaFreeAsync(p, st[k]);
+        if (done[k]) {
+            cudaEventRecord(done[k], st[k]);
+            cudaStreamWaitEvent(user, done[k], 0);
+        }
+    }
+    check(cudaStreamSynchronize(user), "synchronise");
+    for (int k = 0; k < nslots; ++k) {
+        if (st[k]) cudaStreamDestroy(st[k]);
+        if (done[k]) cudaEventDestroy(done[k]);
+    }
+    if (start) cudaEventDestroy(start);
+    return result;
+}
+
+CP_API cp_status cp_backward(const cp_mesh* m, const float* queries, const int32_t* tri,
+                             const float* bary, const float* grad_dist, int64_t nq,
+                             float* grad_queries, float* grad_verts, cp_stream_t stream) {
+    if (!m) return fail(CP_ERROR_INVALID_VALUE, "mesh is NULL");
+    if (nq < 0) return fail(CP_ERROR_INVALID_VALUE, "negative query count");
+    if (nq == 0) return CP_SUCCESS;
+    if (!queries || !tri || !bary || !grad_dist)
+        return fail(CP_ERROR_INVALID_VALUE, "queries, tri, bary and grad_dist are required");
+    CP_CUDA(bvh_backward(m->bvh, queries, tri, bary, grad_dist, nq, grad_queries, grad_verts,
+                         reinterpret_cast<cudaStream_t>(stream)),
+            "backward");
+    return CP_SUCCESS;
+}
+
+// ---- batches ---------------------------------------------------------------
+
+CP_API cp_status cp_batch_create(const float* verts, const int64_t* vert_offsets, const int32_t* tris,
+                                 const int64_t* tri_offsets, int32_t nmeshes,
+                                 const cp_build_opts* opts, cp_stream_t stream, cp_batch** out) {
+    if (!out) return fail(CP_ERROR_INVALID_VALUE, "out is NULL");
+    *out = nullptr;
+    if (!verts || !tris || !vert_offsets || !tri_offsets)
+        return fail(CP_ERROR_INVALID_VALUE, "NULL array");
+    if (nmeshes <= 0) return fail(CP_ERROR_INVALID_VALUE, "nmeshes must be positive");
+    if (nmeshes > (1 << 20)) return fail(CP_ERROR_NOT_SUPPORTED, "more than 2^20 meshes");
+    std::vector<int64_t> voff(vert_offsets, vert_offsets + nmeshes + 1);
+    std::vector<int64_t> toff(tri_offsets, tri_offsets + nmeshes + 1);
+    if (voff[0] != 0 || toff[0] != 0) return fail(CP_ERROR_INVALID_VALUE, "offsets must start at 0");
+    for (int32_t i = 0; i < nmeshes; ++i) {
+        if (toff[i + 1] <= toff[i]) return fail(CP_ERROR_INVALID_VALUE, "every mesh needs at least one triangle");
+        if (voff[i + 1] <= voff[i]) return fail(CP_ERROR_INVALID_VALUE, "every mesh needs at least one vertex");
+    }
+    if (toff.back() > kMaxTriangles) return fail(CP_ERROR_NOT_SUPPORTED, "more than 2^27 - 1 triangles");
+    cp_status s = require_gpu();
+    if (s != CP_SUCCESS) return s;
+    cp_batch* bt = new (std::nothrow) cp_batch();
+    if (!bt) return fail(CP_ERROR_OUT_OF_MEMORY, "host allocation of the handle failed");
+    s = build_common(bt->bvh, verts, 12, tris, voff, toff, opts, stream);
+    if (s != CP_SUCCESS) {
+        delete bt;
+        return s;
+    }
+    if (cudaMalloc(&bt->d_qoff, sizeof(int64_t) * (nmeshes + 1)) != cudaSuccess) {
+        bvh_free(bt->bvh);
+        delete bt;
+        return fail(CP_ERROR_OUT_OF_MEMORY, "query offsets");
+    }
+    *out = bt;
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_batch_destroy(cp_batch* bt) {
+    if (!bt) return CP_SUCCESS;
+    if (bt->exec) cudaGraphExecDestroy(bt->exec);
+    if (bt->d_qoff) cudaFree(bt->d_qoff);
+    bvh_free(bt->bvh);
+    delete bt;
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_batch_info(const cp_batch* bt, int32_t* nmeshes, int64_t* num_wide,
+                               int64_t* num_tris, int32_t* stack_bound) {
+    if (!bt) return fail(CP_ERROR_INVALID_VALUE, "batch is NULL");
+    if (nmeshes) *nmeshes = bt->bvh.nmeshes;
+    if (num_wide) *num_wide = bt->bvh.num_wide;
+    if (num_tris) *num_tris = bt->bvh.nt;
+    if (stack_bound) *stack_bound = bt->bvh.stack_bound;
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_batch_query_workspace_size(const cp_batch* bt, int64_t nq,
+                                               const cp_query_opts* opts, size_t* bytes) {
+    if (!bt || !bytes) return fail(CP_ERROR_INVALID_VALUE, "batch or bytes is NULL");
+    QueryParams qp;
+    cp_status s = to_query_params(opts, &qp);
+    if (s != CP_SUCCESS) return s;
+    *bytes = query_workspace_bytes(bt->bvh, nq, qp);
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_batch_query(cp_batch* bt, const float* queries, const int64_t* q_offsets,
+                                const cp_query_opts* opts, float* out_point, float* out_dist,
+                                int32_t* out_tri, float* out_bary, void* workspace,
+                                size_t ws_bytes, int32_t use_graph, cp_stream_t stream) {
+    if (!bt || !q_offsets) return fail(CP_ERROR_INVALID_VALUE, "batch or q_offsets is NULL");
+    const int nm = bt->bvh.nmeshes;
+    if (q_offsets[0] != 0) return fail(CP_ERROR_INVALID_VALUE, "q_offsets must start at 0");
+    for (int i = 0; i < nm; ++i)
+        if (q_offsets[i + 1] < q_offsets[i]) return fail(CP_ERROR_INVALID_VALUE, "q_offsets must not decrease");
+    const int64_t nq = q_offsets[nm];
+    if (nq > INT32_MAX) return fail(CP_ERROR_NOT_SUPPORTED, "more than 2^31 - 1 queries in one call");
+    if (nq == 0) return CP_SUCCESS;
+    if (!queries) return fail(CP_ERROR_INVALID_VALUE, "queries is NULL");
+    QueryParams qp;
+    cp_status s = to_query_params(opts, &qp);
+    if (s != CP_SUCCESS) return s;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const bool changed = bt->h_qoff.size() != (size_t)(nm + 1) ||
+                         std::memcmp(bt->h_qoff.data(), q_offsets, sizeof(int64_t) * (nm + 1)) != 0;
+    if (changed) {
+        bt->h_qoff.assign(q_offsets, q_offsets + nm + 1);
+        CP_CUDA(cudaMemcpyAsync(bt->d_qoff, bt->h_qoff.data(), sizeof(int64_t) * (nm + 1),
+                                cudaMemcpyHostToDevice, st),
+                "query offsets upload");
+        CP_CUDA(cudaStreamSynchronize(st), "query offsets upload");
+    }
+    if (!use_graph)
+        return query_impl(bt->bvh, queries, nq, bt->d_qoff, qp, out_point, out_dist, out_tri,
+                          out_bary, workspace, ws_bytes, st);
+    if (!workspace) return fail(CP_ERROR_INVALID_VALUE, "graph mode needs a caller workspace");
+    const size_t need = query_workspace_bytes(bt->bvh, nq, qp);
+    if (ws_bytes < need) return fail(CP_ERROR_SCRATCH_TOO_SMALL, "workspace smaller than cp_batch_query_workspace_size()");
+    std::vector<uintptr_t> key = {(uintptr_t)queries, (uintptr_t)out_point, (uintptr_t)out_dist,
+                                  (uintptr_t)out_tri, (uintptr_t)out_bary, (uintptr_t)workspace,
+                                  (uintptr_t)qp.block, (uintptr_t)qp.sort, (uintptr_t)qp.blocks_per_sm,
+                                  (uintptr_t)qp.short_stack, (uintptr_t)nq};
+    for (int i = 0; i <= nm; ++i) key.push_back((uintptr_t)q_offsets[i]);
+    if (!bt->exec || key != bt->graph_key) {
+        if (bt->exec) {
+            cudaGraphExecDestroy(bt->exec);
+            bt->exec = nullptr;
+        }
+        CP_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed), "graph capture");
+        cudaError_t e = bvh_query(bt->bvh, queries, nq, bt->d_qoff, qp, out_point, out_dist, out_tri,
+                                  out_bary, workspace, ws_bytes, st);
+        cudaGraph_t graph = nullptr;
+        cudaError_t e2 = cudaStreamEndCapture(st, &graph);
+        if (e != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return cuda_fail(e, "graph capture");
+        }
+        if (e2 != cudaSuccess) return cuda_fail(e2, "graph capture");
+        e = cudaGraphInstantiate(&bt->exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            bt->exec = nullptr;
+            return cuda_fail(e, "graph instantiate");
+        }
+        bt->graph_key = key;
+    }
+    CP_CUDA(cudaGraphLaunch(bt->exec, st), "graph launch");
+    return CP_SUCCESS;
+}
+
+// ---- inspection ------------------------------------------------------------
+
+CP_API cp_status cp_mesh_export_build(const cp_mesh* m, uint64_t* keys, int32_t* order, int32_t* left,
+                                      int32_t* right, int32_t* parent, uint8_t* cluster,
+                                      int32_t* wide_src) {
+    if (!m) return fail(CP_ERROR_INVALID_VALUE, "mesh is NULL");
+    const Bvh& b = m->bvh;
+    const int64_t n = b.nt, nn = 2 * n - 1;
+    CP_CUDA(cudaDeviceSynchronize(), "export");
+    if (keys) CP_CUDA(cudaMemcpy(keys, b.keys, 8 * n, cudaMemcpyDeviceToHost), "export");
+    if (order) CP_CUDA(cudaMemcpy(order, b.order, 4 * n, cudaMemcpyDeviceToHost), "export");
+    if (n > 1 && left) CP_CUDA(cudaMemcpy(left, b.left, 4 * (n - 1), cudaMemcpyDeviceToHost), "export");
+    if (n > 1 && right) CP_CUDA(cudaMemcpy(right, b.right, 4 * (n - 1), cudaMemcpyDeviceToHost), "export");
+    if (parent) CP_CUDA(cudaMemcpy(parent, b.parent, 4 * nn, cudaMemcpyDeviceToHost), "export");
+    if (cluster) CP_CUDA(cudaMemcpy(cluster, b.cluster, nn, cudaMemcpyDeviceToHost), "export");
+    if (wide_src) CP_CUDA(cudaMemcpy(wide_src, b.wide_src, 4 * b.num_wide, cudaMemcpyDeviceToHost), "export");
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_mesh_export_wide(const cp_mesh* m, float* boxes, int32_t* refs, int32_t* counts) {
+    if (!m) return fail(CP_ERROR_INVALID_VALUE, "mesh is NULL");
+    const Bvh& b = m->bvh;
+    const int K = b.p.K;
+    const size_t node_bytes = (size_t)32 * K;
+    std::vector<unsigned char> h(node_bytes * (size_t)b.num_wide);
+    CP_CUDA(cudaDeviceSynchronize(), "export");
+    CP_CUDA(cudaMemcpy(h.data(), b.nodes, h.size(), cudaMemcpyDeviceToHost), "export");
+    for (int64_t w = 0; w < b.num_wide; ++w) {
+        const float* rows = reinterpret_cast<const float*>(h.data() + node_bytes * w);
+        const int32_t* child = reinterpret_cast<const int32_t*>(rows + 6 * K);
+        for (int s = 0; s < K; ++s) {
+            if (boxes)
+                for (int r = 0; r < 6; ++r) boxes[(w * 6 + r) * K + s] = rows[r * K + s];
+            const bool empty = std::isinf(rows[s]) && rows[s] > 0 && std::isinf(rows[K + s]) && rows[K + s] < 0;
+            int32_t ref, cnt;
+            if (empty) {
+                ref = 0;
+                cnt = -1;
+            } else if (ref_is_leaf(child[s])) {
+                ref = leaf_first(child[s]);
+                cnt = leaf_count(child[s]);
+            } else {
+                ref = child[s];
+                cnt = 0;
+            }
+            if (refs) refs[w * K + s] = ref;
+            if (counts) counts[w * K + s] = cnt;
+        }
+    }
+    return CP_SUCCESS;
+}
+
+}  // extern "C"

@@ -1,0 +1,99 @@
+// bvh.cuh — the device-resident BVH shared by single meshes and batches.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+
+namespace cpq {
+
+struct BuildParams {
+    int K = 2;              // branching
+    int leaf_size = 4;      // max triangles per leaf
+    int collapse = 0;       // 0 count, 1 SAH
+    float c_node = 1.0f;    // SAH node-visit cost
+    float c_tri = 1.0f;     // SAH triangle-test cost
+};
+
+// Everything a build leaves on the device.  A single mesh is a batch of one.
+struct Bvh {
+    BuildParams p;
+    int32_t nmeshes = 0;
+    int64_t nt = 0, nv = 0;
+    int mesh_bits = 0;          // high key bits holding the mesh id
+    int morton_bits = 21;       // bits per axis of the build's Morton codes
+    int64_t num_wide = 0, num_leaves = 0;
+    int32_t max_wide_depth = 0, stack_bound = 0;
+    float build_ms = 0.0f;
+    int device = 0;
+
+    // traversal data
+    void* nodes = nullptr;          // WideNode<K>[num_wide]
+    TriRec* recs = nullptr;         // nt triangle records in leaf order
+    int32_t* wide_root = nullptr;   // nmeshes
+    float* frame = nullptr;         // nmeshes x 6: query Morton frame (lo xyz, scale xyz)
+
+    // kept for refit and inspection
+    int32_t* tris = nullptr;        // nt x 3 local indices
+    int64_t* d_voff = nullptr;      // nmeshes + 1
+    int64_t* d_toff = nullptr;      // nmeshes + 1
+    std::vector<int64_t> h_voff, h_toff;
+    uint64_t* keys = nullptr;       // nt sorted
+    int32_t* order = nullptr;       // nt: sorted position -> global triangle
+    int32_t* inv_order = nullptr;   // nt: global triangle -> sorted position
+    int32_t* left = nullptr;        // nt - 1
+    int32_t* right = nullptr;       // nt - 1
+    int32_t* parent = nullptr;      // 2nt - 1
+    int32_t* first = nullptr;       // 2nt - 1
+    int32_t* last = nullptr;        // 2nt - 1
+    float* box = nullptr;           // (2nt - 1) x 6: lo xyz, hi xyz
+    float* cost = nullptr;          // 2nt - 1
+    uint8_t* leaf_flag = nullptr;   // 2nt - 1
+    uint8_t* cluster = nullptr;     // 2nt - 1
+    uint32_t* arrive = nullptr;     // 2nt - 1 refit counters
+    int32_t* mesh_root = nullptr;   // nmeshes: binary root per mesh
+    int32_t* wide_src = nullptr;    // num_wide
+    int32_t* slot_src = nullptr;    // num_wide x K: binary node per child slot (-1 empty)
+    uint32_t* status = nullptr;     // device status word (CP_DEVICE_* bits)
+
+    std::vector<void*> allocations;
+    size_t device_bytes = 0;
+};
+
+// Build.  verts: nv points at vert_stride floats; tris: local indices;
+// h_voff/h_toff: host offsets (nmeshes + 1).  Synchronises the stream.
+// On failure returns a CUDA error or sets *bad_input (invalid index /
+// non-finite vertex) and leaves the Bvh to be released by bvh_free.
+cudaError_t bvh_build(Bvh& b, const float* verts, int64_t vert_stride, const int32_t* tris,
+                      const std::vector<int64_t>& h_voff, const std::vector<int64_t>& h_toff,
+                      const BuildParams& p, cudaStream_t st, bool* bad_input, std::string* why);
+
+// Move the vertices and refit every box; topology unchanged.  Asynchronous.
+cudaError_t bvh_refit(Bvh& b, const float* verts, int64_t vert_stride, cudaStream_t st);
+
+void bvh_free(Bvh& b);
+
+// Query workspace and launch (query.cu).
+struct QueryParams {
+    int block = 256;
+    int sort = 1;
+    int blocks_per_sm = 0;
+    int short_stack = 8;
+};
+
+size_t query_workspace_bytes(const Bvh& b, int64_t nq, const QueryParams& qp);
+
+// q_off: device array of nmeshes + 1 query offsets (nullptr for one mesh).
+cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int64_t* d_qoff,
+                      const QueryParams& qp, float* out_point, float* out_dist, int32_t* out_tri,
+                      float* out_bary, void* ws, size_t ws_bytes, cudaStream_t st);
+
+cudaError_t bvh_backward(const Bvh& b, const float* queries, const int32_t* tri, const float* bary,
+                         const float* grad_dist, int64_t nq, float* grad_q, float* grad_verts,
+                         cudaStream_t st);
+
+}  // namespace cpq

@@ -1,0 +1,621 @@
+// query.cu — closest-point traversal, query ordering and the adjoint kernel.
+//
+// Replaces the reference's per-pixel traceRayEXT over its TLAS
+// (src/shaders/rt/rt.rgen:257-270) and the slab test hit_bbox
+// (src/shaders/rt/rtcommon.glsl:242-251) with a closest-first descent: a
+// child box is visited only while its squared distance lower bound is below
+// the best squared distance found so far.  Point-triangle distance follows
+// the Voronoi-region method (Ericson 2005, section 5.1.5).
+//
+// Kernel shape (GB300, 152 SMs): a persistent grid of SMs x resident blocks;
+// each warp takes 32 consecutive (Morton-ordered) queries from a global
+// counter, one query per lane, and leaves when the counter runs past the end
+// (warp-uniform exit).  Each thread keeps the top `S` entries of its stack in
+// shared memory (a ring in a per-warp slice, [slot][thread] so a warp's
+// accesses hit 32 distinct banks) and spills older entries to local memory.
+// Node rows and triangle records are read with 128-bit read-only loads.
+#include <cfloat>
+#include <climits>
+
+#include "bvh.cuh"
+#include "sort.cuh"
+
+namespace cpq {
+
+namespace {
+
+constexpr int kStackTotal = 256;   // >= (K-1)(depth+1) for any 64+32-bit-key LBVH
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ int mesh_of(const int64_t* __restrict__ off, int nmeshes, int64_t i) {
+    int lo = 0, hi = nmeshes - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+template <int K>
+__device__ __forceinline__ void load_row(const float* __restrict__ p, float (&r)[K]) {
+    if constexpr (K == 2) {
+        float2 v = __ldg(reinterpret_cast<const float2*>(p));
+        r[0] = v.x; r[1] = v.y;
+    } else if constexpr (K == 4) {
+        float4 v = __ldg(reinterpret_cast<const float4*>(p));
+        r[0] = v.x; r[1] = v.y; r[2] = v.z; r[3] = v.w;
+    } else {
+        float4 v = __ldg(reinterpret_cast<const float4*>(p));
+        float4 u = __ldg(reinterpret_cast<const float4*>(p) + 1);
+        r[0] = v.x; r[1] = v.y; r[2] = v.z; r[3] = v.w;
+        r[4] = u.x; r[5] = u.y; r[6] = u.z; r[7] = u.w;
+    }
+}
+template <int K>
+__device__ __forceinline__ void load_row_i(const int32_t* __restrict__ p, int32_t (&r)[K]) {
+    if constexpr (K == 2) {
+        int2 v = __ldg(reinterpret_cast<const int2*>(p));
+        r[0] = v.x; r[1] = v.y;
+    } else if constexpr (K == 4) {
+        int4 v = __ldg(reinterpret_cast<const int4*>(p));
+        r[0] = v.x; r[1] = v.y; r[2] = v.z; r[3] = v.w;
+    } else {
+        int4 v = __ldg(reinterpret_cast<const int4*>(p));
+        int4 u = __ldg(reinterpret_cast<const int4*>(p) + 1);
+        r[0] = v.x; r[1] = v.y; r[2] = v.z; r[3] = v.w;
+        r[4] = u.x; r[5] = u.y; r[6] = u.z; r[7] = u.w;
+    }
+}
+
+__device__ __forceinline__ void cswap(float& a, float& b, int& x, int& y) {
+    if (b < a) {
+        float t = a; a = b; b = t;
+        int u = x; x = y; y = u;
+    }
+}
+
+// Ascending sorting networks (2: 1 exchange, 4: 5, 8: 19).
+template <int K>
+__device__ __forceinline__ void sort_children(float (&d)[K], int (&c)[K]) {
+    if constexpr (K == 2) {
+        cswap(d[0], d[1], c[0], c[1]);
+    } else if constexpr (K == 4) {
+        cswap(d[0], d[1], c[0], c[1]); cswap(d[2], d[3], c[2], c[3]);
+        cswap(d[0], d[2], c[0], c[2]); cswap(d[1], d[3], c[1], c[3]);
+        cswap(d[1], d[2], c[1], c[2]);
+    } else {
+        cswap(d[0], d[1], c[0], c[1]); cswap(d[2], d[3], c[2], c[3]);
+        cswap(d[4], d[5], c[4], c[5]); cswap(d[6], d[7], c[6], c[7]);
+        cswap(d[0], d[2], c[0], c[2]); cswap(d[1], d[3], c[1], c[3]);
+        cswap(d[4], d[6], c[4], c[6]); cswap(d[5], d[7], c[5], c[7]);
+        cswap(d[1], d[2], c[1], c[2]); cswap(d[5], d[6], c[5], c[6]);
+        cswap(d[0], d[4], c[0], c[4]); cswap(d[3], d[7], c[3], c[7]);
+        cswap(d[1], d[5], c[1], c[5]); cswap(d[2], d[6], c[2], c[6]);
+        cswap(d[1], d[4], c[1], c[4]); cswap(d[3], d[6], c[3], c[6]);
+        cswap(d[2], d[4], c[2], c[4]); cswap(d[3], d[5], c[3], c[5]);
+        cswap(d[3], d[4], c[3], c[4]);
+    }
+}
+
+__device__ __forceinline__ float box_lb2(float qx, float qy, float qz, float lox, float hix,
+                                         float loy, float hiy, float loz, float hiz) {
+    float dx = fmaxf(fmaxf(lox - qx, qx - hix), 0.0f);
+    float dy = fmaxf(fmaxf(loy - qy, qy - hiy), 0.0f);
+    float dz = fmaxf(fmaxf(loz - qz, qz - hiz), 0.0f);
+    return dx * dx + dy * dy + dz * dz;
+}
+
+// FP32 squared distance to a triangle record (traversal test).  Voronoi
+// regions; the difference vector is measured from the vertex owning the
+// region so near-surface queries keep their small distances accurate.
+__device__ __forceinline__ float tri_d2(float qx, float qy, float qz, const TriRec& r) {
+    const float ax = r.p0.x, ay = r.p0.y, az = r.p0.z;
+    const float bx = r.p0.w, by = r.p1.x, bz = r.p1.y;
+    const float cx = r.p1.z, cy = r.p1.w, cz = r.p2.x;
+    const float abx = bx - ax, aby = by - ay, abz = bz - az;
+    const float acx = cx - ax, acy = cy - ay, acz = cz - az;
+    const float apx = qx - ax, apy = qy - ay, apz = qz - az;
+    float rx, ry, rz;
+    if (__float_as_uint(r.p2.z) & kTriDegenerate) {
+        // closest of the three edges
+        float best = FLT_MAX;
+        const float px[3] = {ax, bx, ax}, py[3] = {ay, by, ay}, pz[3] = {az, bz, az};
+        const float ex[3] = {abx, cx - bx, acx}, ey[3] = {aby, cy - by, acy}, ez[3] = {abz, cz - bz, acz};
+#pragma unroll
+        for (int e = 0; e < 3; ++e) {
+            float wx = qx - px[e], wy = qy - py[e], wz = qz - pz[e];
+            float l = ex[e] * ex[e] + ey[e] * ey[e] + ez[e] * ez[e];
+            float t = l > 0.0f ? __saturatef((wx * ex[e] + wy * ey[e] + wz * ez[e]) / l) : 0.0f;
+            wx -= t * ex[e]; wy -= t * ey[e]; wz -= t * ez[e];
+            best = fminf(best, wx * wx + wy * wy + wz * wz);
+        }
+        return best;
+    }
+    const float d1 = abx * apx + aby * apy + abz * apz;
+    const float d2 = acx * apx + acy * apy + acz * apz;
+    if (d1 <= 0.0f && d2 <= 0.0f) {
+        rx = apx; ry = apy; rz = apz;
+    } else {
+        const float bpx = qx - bx, bpy = qy - by, bpz = qz - bz;
+        const float d3 = abx * bpx + aby * bpy + abz * bpz;
+        const float d4 = acx * bpx + acy * bpy + acz * bpz;
+        const float cpx = qx - cx, cpy = qy - cy, cpz = qz - cz;
+        const float d5 = abx * cpx + aby * cpy + abz * cpz;
+        const float d6 = acx * cpx + acy * cpy + acz * cpz;
+        const float vc = d1 * d4 - d3 * d2;
+        const float vb = d5 * d2 - d1 * d6;
+        const float va = d3 * d6 - d5 * d4;
+        if (d3 >= 0.0f && d4 <= d3) {
+            rx = bpx; ry = bpy; rz = bpz;
+        } else if (vc <= 0.0f && d1 >= 0.0f && d3 <= 0.0f) {
+            const float v = __fdividef(d1, d1 - d3);
+            rx = apx - v * abx; ry = apy - v * aby; rz = apz - v * abz;
+        } else if (d6 >= 0.0f && d5 <= d6) {
+            rx = cpx; ry = cpy; rz = cpz;
+        } else if (vb <= 0.0f && d2 >= 0.0f && d6 <= 0.0f) {
+            const float w = __fdividef(d2, d2 - d6);
+            rx = apx - w * acx; ry = apy - w * acy; rz = apz - w * acz;
+        } else if (va <= 0.0f && (d4 - d3) >= 0.0f && (d5 - d6) >= 0.0f) {
+            const float w = __fdividef(d4 - d3, (d4 - d3) + (d5 - d6));
+            rx = bpx - w * (cx - bx); ry = bpy - w * (cy - by); rz = bpz - w * (cz - bz);
+        } else {
+            const float inv = __fdividef(1.0f, va + vb + vc);
+            const float v = vb * inv, w = vc * inv;
+            rx = apx - (v * abx + w * acx);
+            ry = apy - (v * aby + w * acy);
+            rz = apz - (v * abz + w * acz);
+        }
+    }
+    return rx * rx + ry * ry + rz * rz;
+}
+
+// Degenerate triangle in FP32 with barycentrics (weights of b and c).
+__device__ void degenerate_bary(float qx, float qy, float qz, const TriRec& r, float& ov, float& ow) {
+    const float ax = r.p0.x, ay = r.p0.y, az = r.p0.z;
+    const float bx = r.p0.w, by = r.p1.x, bz = r.p1.y;
+    const float cx = r.p1.z, cy = r.p1.w, cz = r.p2.x;
+    const float px[3] = {ax, bx, ax}, py[3] = {ay, by, ay}, pz[3] = {az, bz, az};
+    const float ex[3] = {bx - ax, cx - bx, cx - ax}, ey[3] = {by - ay, cy - by, cy - ay},
+                ez[3] = {bz - az, cz - bz, cz - az};
+    float best = FLT_MAX;
+    ov = 0.0f;
+    ow = 0.0f;
+    for (int e = 0; e < 3; ++e) {
+        float wx = qx - px[e], wy = qy - py[e], wz = qz - pz[e];
+        float l = ex[e] * ex[e] + ey[e] * ey[e] + ez[e] * ez[e];
+        float t = l > 0.0f ? __saturatef((wx * ex[e] + wy * ey[e] + wz * ez[e]) / l) : 0.0f;
+        wx -= t * ex[e]; wy -= t * ey[e]; wz -= t * ez[e];
+        float d2 = wx * wx + wy * wy + wz * wz;
+        if (d2 < best) {
+            best = d2;
+            if (e == 0) { ov = t; ow = 0.0f; }
+            else if (e == 1) { ov = 1.0f - t; ow = t; }
+            else { ov = 0.0f; ow = t; }
+        }
+    }
+}
+
+// Final answer for the winning triangle in float-float arithmetic: the same
+// region logic as tri_d2 on exact differences, then |q - p| to ~2^-44.
+__device__ void precise_closest(float qx, float qy, float qz, const TriRec& r, float& dist,
+                                float& px, float& py, float& pz, float& ov, float& ow) {
+    const ff3 A = ff3_from(r.p0.x, r.p0.y, r.p0.z);
+    const ff3 B = ff3_from(r.p0.w, r.p1.x, r.p1.y);
+    const ff3 C = ff3_from(r.p1.z, r.p1.w, r.p2.x);
+    const ff3 Q = ff3_from(qx, qy, qz);
+    const ff3 ab = ff3_sub(B, A), ac = ff3_sub(C, A), ap = ff3_sub(Q, A);
+    ff v = ff_from(0.0f), w = ff_from(0.0f);
+    if (__float_as_uint(r.p2.z) & kTriDegenerate) {
+        float fv, fw;
+        degenerate_bary(qx, qy, qz, r, fv, fw);
+        v = ff_from(fv);
+        w = ff_from(fw);
+    } else {
+        const ff d1 = ff3_dot(ab, ap), d2 = ff3_dot(ac, ap);
+        if (ff_le0(d1) && ff_le0(d2)) {
+            // vertex a
+        } else {
+            const ff3 bp = ff3_sub(Q, B), cp = ff3_sub(Q, C);
+            const ff d3 = ff3_dot(ab, bp), d4 = ff3_dot(ac, bp);
+            const ff d5 = ff3_dot(ab, cp), d6 = ff3_dot(ac, cp);
+            const ff vc = ff_sub(ff_mul(d1, d4), ff_mul(d3, d2));
+            const ff vb = ff_sub(ff_mul(d5, d2), ff_mul(d1, d6));
+            const ff va = ff_sub(ff_mul(d3, d6), ff_mul(d5, d4));
+            const ff d43 = ff_sub(d4, d3), d56 = ff_sub(d5, d6);
+            if (ff_ge0(d3) && ff_le(d4, d3)) {
+                v = ff_from(1.0f);
+            } else if (ff_le0(vc) && ff_ge0(d1) && ff_le0(d3)) {
+                v = ff_div(d1, ff_sub(d1, d3));
+            } else if (ff_ge0(d6) && ff_le(d5, d6)) {
+                w = ff_from(1.0f);
+            } else if (ff_le0(vb) && ff_ge0(d2) && ff_le0(d6)) {
+                w = ff_div(d2, ff_sub(d2, d6));
+            } else if (ff_le0(va) && ff_ge0(d43) && ff_ge0(d56)) {
+                w = ff_div(d43, ff_add(d43, d56));
+                v = ff_sub(ff_from(1.0f), w);
+            } else {
+                const ff den = ff_add(ff_add(va, vb), vc);
+                v = ff_div(vb, den);
+                w = ff_div(vc, den);
+            }
+        }
+    }
+    // r = ap - v ab - w ac; p = a + v ab + w ac
+    const ff3 off = {ff_add(ff_mul(v, ab.x), ff_mul(w, ac.x)), ff_add(ff_mul(v, ab.y), ff_mul(w, ac.y)),
+                     ff_add(ff_mul(v, ab.z), ff_mul(w, ac.z))};
+    const ff3 rr = ff3_sub(ap, off);
+    const ff d2 = ff3_dot(rr, rr);
+    dist = ff_to_float(ff_sqrt(d2));
+    px = ff_to_float(ff_add(A.x, off.x));
+    py = ff_to_float(ff_add(A.y, off.y));
+    pz = ff_to_float(ff_add(A.z, off.z));
+    ov = ff_to_float(v);
+    ow = ff_to_float(w);
+}
+
+struct TraverseArgs {
+    const void* nodes;
+    const TriRec* recs;
+    const int32_t* wide_root;
+    const int64_t* qoff;
+    int nmeshes;
+    const float* queries;
+    const int32_t* perm;
+    int64_t nq;
+    float* out_point;
+    float* out_dist;
+    int32_t* out_tri;
+    float* out_bary;
+    unsigned long long* counter;
+    uint32_t* status;
+};
+
+template <int K, int S>
+__global__ void __launch_bounds__(256) k_traverse(TraverseArgs a) {
+    extern __shared__ float2 s_stack[];
+    const int lane = threadIdx.x & 31;
+    const int nth = blockDim.x;
+    float2* my = s_stack + threadIdx.x;
+    float2 spill[kStackTotal - S];
+    const WideNode<K>* __restrict__ nodes = static_cast<const WideNode<K>*>(a.nodes);
+
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(a.counter, 32ull);
+        base = __shfl_sync(kFull, base, 0);
+        if (base >= (unsigned long long)a.nq) break;  // warp-uniform exit
+        const int64_t i = (int64_t)base + lane;
+        if (i >= a.nq) continue;
+        const int64_t qi = a.perm ? (int64_t)a.perm[i] : i;
+        const float qx = a.queries[3 * qi], qy = a.queries[3 * qi + 1], qz = a.queries[3 * qi + 2];
+        const int m = a.nmeshes > 1 ? mesh_of(a.qoff, a.nmeshes, qi) : 0;
+
+        float best = INFINITY;
+        int best_rec = -1;
+        int best_idx = INT_MAX;
+        int sp = 0;
+        int cur = a.wide_root[m];
+        bool have = true;
+        while (have) {
+            if (cur >= 0) {
+                const WideNode<K>* nd = nodes + cur;
+                float lox[K], hix[K], loy[K], hiy[K], loz[K], hiz[K];
+                int32_t ch[K];
+                load_row<K>(nd->lox, lox);
+                load_row<K>(nd->hix, hix);
+                load_row<K>(nd->loy, loy);
+                load_row<K>(nd->hiy, hiy);
+                load_row<K>(nd->loz, loz);
+                load_row<K>(nd->hiz, hiz);
+                load_row_i<K>(nd->child, ch);
+                float lb[K];
+#pragma unroll
+                for (int s = 0; s < K; ++s) {
+                    float d = box_lb2(qx, qy, qz, lox[s], hix[s], loy[s], hiy[s], loz[s], hiz[s]);
+                    lb[s] = d < best ? d : INFINITY;
+                }
+                sort_children<K>(lb, ch);
+#pragma unroll
+                for (int s = K - 1; s >= 1; --s) {
+                    if (lb[s] < INFINITY) {
+                        // push (far children first so the nearest is on top)
+                        const int slot = (sp & (S - 1)) * nth;
+                        if (sp >= S) {
+                            const int ov = sp - S;
+                            if (ov < kStackTotal - S) spill[ov] = my[slot];
+                            else atomicOr(a.status, 1u);
+                        }
+                        my[slot] = make_float2(lb[s], __int_as_float(ch[s]));
+                        ++sp;
+                    }
+                }
+                if (lb[0] < INFINITY) {
+                    cur = ch[0];
+                    continue;
+                }
+            } else {
+                const int first = leaf_first(cur), cnt = leaf_count(cur);
+                for (int k = 0; k < cnt; ++k) {
+                    const float4* rp = reinterpret_cast<const float4*>(a.recs + first + k);
+                    TriRec r;
+                    r.p0 = __ldg(rp);
+                    r.p1 = __ldg(rp + 1);
+                    r.p2 = __ldg(rp + 2);
+                    const float d2 = tri_d2(qx, qy, qz, r);
+                    const int idx = __float_as_int(r.p2.y);
+                    if (d2 < best || (d2 == best && idx < best_idx)) {
+                        best = d2;
+                        best_rec = first + k;
+                        best_idx = idx;
+                    }
+                }
+            }
+            // pop the nearest entry that can still hold a closer triangle
+            have = false;
+            while (sp > 0) {
+                --sp;
+                const int slot = (sp & (S - 1)) * nth;
+                const float2 e = my[slot];
+                if (sp >= S) my[slot] = spill[sp - S];
+                if (e.x < best) {
+                    cur = __float_as_int(e.y);
+                    have = true;
+                    break;
+                }
+            }
+        }
+
+        float dist = __int_as_float(0x7fc00000), px = dist, py = dist, pz = dist, bv = dist, bw = dist;
+        if (best_rec >= 0) {
+            const float4* rp = reinterpret_cast<const float4*>(a.recs + best_rec);
+            TriRec r;
+            r.p0 = __ldg(rp);
+            r.p1 = __ldg(rp + 1);
+            r.p2 = __ldg(rp + 2);
+            precise_closest(qx, qy, qz, r, dist, px, py, pz, bv, bw);
+        } else {
+            atomicOr(a.status, 4u);
+        }
+        if (a.out_dist) a.out_dist[qi] = dist;
+        if (a.out_tri) a.out_tri[qi] = best_rec >= 0 ? best_idx : -1;
+        if (a.out_point) {
+            a.out_point[3 * qi] = px;
+            a.out_point[3 * qi + 1] = py;
+            a.out_point[3 * qi + 2] = pz;
+        }
+        if (a.out_bary) {
+            a.out_bary[2 * qi] = bv;
+            a.out_bary[2 * qi + 1] = bw;
+        }
+    }
+}
+
+__global__ void k_query_keys(const float* __restrict__ q, int64_t nq, const int64_t* __restrict__ qoff,
+                             int nmeshes, const float* __restrict__ frame, int qbits,
+                             uint64_t* __restrict__ keys, int32_t* __restrict__ vals) {
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nq) return;
+    const int m = nmeshes > 1 ? mesh_of(qoff, nmeshes, i) : 0;
+    const float* f = frame + 6 * m;
+    const float maxcell = (float)((1u << qbits) - 1u);
+    uint64_t code = 0;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float t = (q[3 * i + k] - f[k]) * f[3 + k];
+        t = fminf(fmaxf(t, 0.0f), maxcell);  // NaN -> 0
+        code |= spread3((uint32_t)t) << (2 - k);
+    }
+    keys[i] = ((uint64_t)m << (3 * qbits)) | code;
+    vals[i] = (int32_t)i;
+}
+
+// Adjoint: recompute p from (tri, bary), scatter -b_k g (q - p)/d to the
+// triangle's vertices.  Lanes that hit the same vertex are summed inside the
+// warp first (match_any + an ordered shuffle loop) and one lane adds.
+__device__ __forceinline__ void warp_add3(float* __restrict__ base, int vid, float x, float y, float z) {
+    const int lane = threadIdx.x & 31;
+    const unsigned peers = __match_any_sync(kFull, vid);
+    const bool shared = __any_sync(kFull, vid >= 0 && __popc(peers) > 1);
+    if (!shared) {
+        if (vid >= 0) {
+            atomicAdd(base + 3 * (int64_t)vid, x);
+            atomicAdd(base + 3 * (int64_t)vid + 1, y);
+            atomicAdd(base + 3 * (int64_t)vid + 2, z);
+        }
+        return;
+    }
+    float sx = 0.0f, sy = 0.0f, sz = 0.0f;
+#pragma unroll 1
+    for (int src = 0; src < 32; ++src) {
+        const float vx = __shfl_sync(kFull, x, src);
+        const float vy = __shfl_sync(kFull, y, src);
+        const float vz = __shfl_sync(kFull, z, src);
+        if ((peers >> src) & 1u) {
+            sx += vx;
+            sy += vy;
+            sz += vz;
+        }
+    }
+    if (vid >= 0 && (__ffs(peers) - 1) == lane) {
+        atomicAdd(base + 3 * (int64_t)vid, sx);
+        atomicAdd(base + 3 * (int64_t)vid + 1, sy);
+        atomicAdd(base + 3 * (int64_t)vid + 2, sz);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_backward(const TriRec* __restrict__ recs,
+                                                   const int32_t* __restrict__ inv_order,
+                                                   const int32_t* __restrict__ tris, int64_t nt,
+                                                   const float* __restrict__ q,
+                                                   const int32_t* __restrict__ tri,
+                                                   const float* __restrict__ bary,
+                                                   const float* __restrict__ grad, int64_t nq,
+                                                   float* __restrict__ grad_q,
+                                                   float* __restrict__ grad_v,
+                                                   uint32_t* __restrict__ status) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int32_t t = -1;
+    float gx = 0.f, gy = 0.f, gz = 0.f, u = 0.f, v = 0.f, w = 0.f;
+    if (i < nq) {
+        t = tri[i];
+        if (t >= nt) {
+            atomicOr(status, 2u);
+            t = -1;
+        }
+        if (t >= 0) {
+            const float4* rp = reinterpret_cast<const float4*>(recs + inv_order[t]);
+            const float4 p0 = __ldg(rp), p1 = __ldg(rp + 1), p2 = __ldg(rp + 2);
+            v = bary[2 * i];
+            w = bary[2 * i + 1];
+            u = 1.0f - v - w;
+            const float px = p0.x + v * (p0.w - p0.x) + w * (p1.z - p0.x);
+            const float py = p0.y + v * (p1.x - p0.y) + w * (p1.w - p0.y);
+            const float pz = p0.z + v * (p1.y - p0.z) + w * (p2.x - p0.z);
+            const float rx = q[3 * i] - px, ry = q[3 * i + 1] - py, rz = q[3 * i + 2] - pz;
+            const float d = sqrtf(rx * rx + ry * ry + rz * rz);
+            const float s = d > 0.0f ? grad[i] / d : 0.0f;
+            gx = s * rx;
+            gy = s * ry;
+            gz = s * rz;
+        }
+        if (grad_q) {
+            grad_q[3 * i] = gx;
+            grad_q[3 * i + 1] = gy;
+            grad_q[3 * i + 2] = gz;
+        }
+    }
+    if (grad_v == nullptr) return;  // uniform across the grid
+    int v0 = -1, v1 = -1, v2 = -1;
+    if (t >= 0) {
+        v0 = tris[3 * (int64_t)t];
+        v1 = tris[3 * (int64_t)t + 1];
+        v2 = tris[3 * (int64_t)t + 2];
+    }
+    warp_add3(grad_v, v0, -u * gx, -u * gy, -u * gz);
+    warp_add3(grad_v, v1, -v * gx, -v * gy, -v * gz);
+    warp_add3(grad_v, v2, -w * gx, -w * gy, -w * gz);
+}
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+struct QueryLayout {
+    size_t keys = 0, vals = 0, keys_alt = 0, vals_alt = 0, sort_ws = 0, counter = 0, total = 0;
+    size_t sort_ws_bytes = 0;
+};
+
+QueryLayout layout(int64_t nq, bool sort) {
+    QueryLayout L;
+    size_t off = 0;
+    L.counter = off;
+    off += 256;
+    if (sort && nq > 1) {
+        L.keys = off; off += align256(sizeof(uint64_t) * nq);
+        L.vals = off; off += align256(sizeof(int32_t) * nq);
+        L.keys_alt = off; off += align256(sizeof(uint64_t) * nq);
+        L.vals_alt = off; off += align256(sizeof(int32_t) * nq);
+        L.sort_ws = off;
+        L.sort_ws_bytes = radix_sort_workspace_bytes(nq);
+        off += align256(L.sort_ws_bytes);
+    }
+    L.total = off;
+    return L;
+}
+
+template <int K, int S>
+cudaError_t launch_traverse(const TraverseArgs& args, int block, int blocks_per_sm, cudaStream_t st) {
+    const size_t smem = (size_t)S * block * sizeof(float2);
+    auto kern = k_traverse<K, S>;
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    if (blocks_per_sm <= 0) {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, block, smem);
+        if (e != cudaSuccess) return e;
+        if (blocks_per_sm < 1) blocks_per_sm = 1;
+    }
+    int64_t grid = (int64_t)sms * blocks_per_sm;
+    const int64_t need = (args.nq + 31) / 32 * 32 / block + 1;
+    if (grid > need) grid = need;
+    kern<<<(unsigned)grid, block, smem, st>>>(args);
+    return cudaGetLastError();
+}
+
+template <int K>
+cudaError_t launch_k(const TraverseArgs& args, const QueryParams& qp, cudaStream_t st) {
+    switch (qp.short_stack) {
+        case 4: return launch_traverse<K, 4>(args, qp.block, qp.blocks_per_sm, st);
+        case 16: return launch_traverse<K, 16>(args, qp.block, qp.blocks_per_sm, st);
+        default: return launch_traverse<K, 8>(args, qp.block, qp.blocks_per_sm, st);
+    }
+}
+
+}  // namespace
+
+size_t query_workspace_bytes(const Bvh& b, int64_t nq, const QueryParams& qp) {
+    (void)b;
+    return layout(nq, qp.sort != 0).total;
+}
+
+cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int64_t* d_qoff,
+                      const QueryParams& qp, float* out_point, float* out_dist, int32_t* out_tri,
+                      float* out_bary, void* ws, size_t ws_bytes, cudaStream_t st) {
+    if (nq <= 0) return cudaSuccess;
+    const QueryLayout L = layout(nq, qp.sort != 0);
+    if (ws_bytes < L.total) return cudaErrorInvalidValue;
+    unsigned char* w = static_cast<unsigned char*>(ws);
+    unsigned long long* counter = reinterpret_cast<unsigned long long*>(w + L.counter);
+    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
+    if (e != cudaSuccess) return e;
+    const int32_t* perm = nullptr;
+    if (qp.sort && nq > 1) {
+        uint64_t* keys = reinterpret_cast<uint64_t*>(w + L.keys);
+        int32_t* vals = reinterpret_cast<int32_t*>(w + L.vals);
+        uint64_t* keys_alt = reinterpret_cast<uint64_t*>(w + L.keys_alt);
+        int32_t* vals_alt = reinterpret_cast<int32_t*>(w + L.vals_alt);
+        const int qbits = (64 - b.mesh_bits) / 3 < 10 ? (64 - b.mesh_bits) / 3 : 10;
+        k_query_keys<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(queries, nq, d_qoff, b.nmeshes,
+                                                                   b.frame, qbits, keys, vals);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        bool in_alt = false;
+        e = radix_sort_pairs<uint64_t>(keys, vals, keys_alt, vals_alt, nq, 0, 3 * qbits + b.mesh_bits,
+                                       w + L.sort_ws, L.sort_ws_bytes, st, &in_alt);
+        if (e != cudaSuccess) return e;
+        perm = in_alt ? vals_alt : vals;
+    }
+    TraverseArgs args;
+    args.nodes = b.nodes;
+    args.recs = b.recs;
+    args.wide_root = b.wide_root;
+    args.qoff = d_qoff;
+    args.nmeshes = b.nmeshes;
+    args.queries = queries;
+    args.perm = perm;
+    args.nq = nq;
+    args.out_point = out_point;
+    args.out_dist = out_dist;
+    args.out_tri = out_tri;
+    args.out_bary = out_bary;
+    args.counter = counter;
+    args.status = b.status;
+    switch (b.p.K) {
+        case 2: return launch_k<2>(args, qp, st);
+        case 4: return launch_k<4>(args, qp, st);
+        default: return launch_k<8>(args, qp, st);
+    }
+}
+
+cudaError_t bvh_backward(const Bvh& b, const float* queries, const int32_t* tri, const float* bary,
+                         const float* grad_dist, int64_t nq, float* grad_q, float* grad_verts,
+                         cudaStream_t st) {
+    if (nq <= 0) return cudaSuccess;
+    k_backward<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(b.recs, b.inv_order, b.tris, b.nt,
+                                                             queries, tri, bary, grad_dist, nq,
+                                                             grad_q, grad_verts, b.status);
+    return cudaGetLastError();
+}
+
+}  // namespace cpq

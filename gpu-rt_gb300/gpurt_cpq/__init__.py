@@ -1,0 +1,12 @@
+"""GB300 closest-point engine (Python binding of include/cpq.h).
+
+Mesh in, BVH built on the GPU, a batch of points in; closest point, unsigned
+distance and triangle index out.  See :class:`Mesh`, :class:`Batch` and
+:func:`closest_distance`.
+"""
+from ._lib import CpError, LIB_PATH, lib  # noqa: F401  (raises if the library is missing)
+from .mesh import (Batch, Mesh, QueryResult, autotune, build_opts, closest_distance,  # noqa: F401
+                   query_opts)
+
+__all__ = ["Mesh", "Batch", "QueryResult", "closest_distance", "autotune", "build_opts",
+           "query_opts", "CpError", "lib", "LIB_PATH"]

@@ -1,0 +1,340 @@
+"""Host-side mirror of the closest-point query surface.
+
+A :class:`Mesh` plays the role of the reference's ``VK::Mesh`` + ``VK::Accel``
+pair (src/vk/mesh.h:14-58, src/vk/vulkan.h:256-284): it is built once from
+vertices and triangles and then queried; :meth:`Mesh.query` takes the place of
+``trace_ray`` (src/shaders/rt/rt.rgen:257-270) with a closest-point query, and
+:class:`Batch` the place of the TLAS over many BLASes
+(src/vk/vulkan.cpp:777-856).  Every method is a thin call into the C ABI
+(include/cpq.h); device tensors are passed as raw pointers on torch's current
+CUDA stream.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import byref, c_int32, c_int64, c_size_t, c_uint32, c_void_p
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from ._lib import (CP_COLLAPSE_COUNT, CP_COLLAPSE_SAH, BuildOpts, MeshInfo, QueryOpts, check, lib)
+
+
+def _stream(stream=None) -> c_void_p:
+    if stream is None:
+        stream = torch.cuda.current_stream()
+    return c_void_p(stream.cuda_stream)
+
+
+def _ptr(t: torch.Tensor | None) -> c_void_p:
+    return c_void_p(t.data_ptr()) if t is not None else c_void_p(None)
+
+
+def _check_dev(t: torch.Tensor, name: str, dtype, cols: int | None) -> None:
+    if not t.is_cuda:
+        raise ValueError(f"{name} must be a CUDA tensor")
+    if t.dtype != dtype:
+        raise ValueError(f"{name} must be {dtype}, got {t.dtype}")
+    if cols is not None and (t.dim() != 2 or t.shape[1] != cols):
+        raise ValueError(f"{name} must have shape (N, {cols})")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+
+
+def build_opts(branching: int = 2, leaf_size: int = 4, collapse: str = "count",
+               sah_node_cost: float = 1.0, sah_tri_cost: float = 1.0) -> BuildOpts:
+    o = BuildOpts()
+    lib.cp_build_opts_default(byref(o))
+    o.branching = branching
+    o.leaf_size = leaf_size
+    o.collapse = {"count": CP_COLLAPSE_COUNT, "sah": CP_COLLAPSE_SAH}[collapse]
+    o.sah_node_cost = sah_node_cost
+    o.sah_tri_cost = sah_tri_cost
+    return o
+
+
+def query_opts(block_size: int = 0, sort_queries: bool = True, blocks_per_sm: int = 0,
+               short_stack: int = 0) -> QueryOpts:
+    o = QueryOpts()
+    lib.cp_query_opts_default(byref(o))
+    if block_size:
+        o.block_size = block_size
+    o.sort_queries = 1 if sort_queries else 0
+    o.blocks_per_sm = blocks_per_sm
+    if short_stack:
+        o.short_stack = short_stack
+    return o
+
+
+@dataclass
+class QueryResult:
+    point: torch.Tensor | None   # (N, 3) float32
+    dist: torch.Tensor           # (N,) float32
+    tri: torch.Tensor            # (N,) int32
+    bary: torch.Tensor | None    # (N, 2) float32, weights of vertices 1 and 2
+
+
+class Mesh:
+    """A triangle mesh with a GPU-built BVH (see include/cpq.h, cp_mesh_create)."""
+
+    def __init__(self, verts: torch.Tensor, tris: torch.Tensor, *, branching: int = 2,
+                 leaf_size: int = 4, collapse: str = "count", sah_node_cost: float = 1.0,
+                 sah_tri_cost: float = 1.0, stream=None):
+        if verts.dim() != 2 or verts.shape[1] < 3:
+            raise ValueError("verts must have shape (V, >=3)")
+        if not verts.is_cuda or verts.dtype != torch.float32 or verts.stride(1) != 1:
+            raise ValueError("verts must be a CUDA float32 tensor with unit column stride")
+        _check_dev(tris, "tris", torch.int32, 3)
+        self.num_vertices = int(verts.shape[0])
+        self.num_triangles = int(tris.shape[0])
+        self.opts = build_opts(branching, leaf_size, collapse, sah_node_cost, sah_tri_cost)
+        h = c_void_p()
+        check(lib.cp_mesh_create(_ptr(verts), self.num_vertices, verts.stride(0) * 4, _ptr(tris),
+                                 self.num_triangles, byref(self.opts), _stream(stream), byref(h)),
+              "cp_mesh_create")
+        self._h = h
+        self.device = verts.device
+
+    # -- lifetime ------------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            lib.cp_mesh_destroy(self._h)
+            self._h = c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> c_void_p:
+        return self._h
+
+    def info(self) -> MeshInfo:
+        out = MeshInfo()
+        check(lib.cp_mesh_info(self._h, byref(out)), "cp_mesh_info")
+        return out
+
+    def device_status(self, stream=None) -> int:
+        bits = c_uint32(0)
+        check(lib.cp_mesh_device_status(self._h, _stream(stream), byref(bits)), "cp_mesh_device_status")
+        return bits.value
+
+    # -- queries -------------------------------------------------------------
+    def workspace_size(self, nq: int, opts: QueryOpts | None = None) -> int:
+        b = c_size_t(0)
+        o = opts or query_opts()
+        check(lib.cp_query_workspace_size(self._h, nq, byref(o), byref(b)), "cp_query_workspace_size")
+        return b.value
+
+    def query(self, points: torch.Tensor, *, want_point: bool = True, want_bary: bool = False,
+              opts: QueryOpts | None = None, workspace: torch.Tensor | None = None,
+              out: QueryResult | None = None, stream=None) -> QueryResult:
+        _check_dev(points, "points", torch.float32, 3)
+        n = int(points.shape[0])
+        o = opts or query_opts()
+        if out is None:
+            dev = points.device
+            out = QueryResult(
+                point=torch.empty((n, 3), dtype=torch.float32, device=dev) if want_point else None,
+                dist=torch.empty((n,), dtype=torch.float32, device=dev),
+                tri=torch.empty((n,), dtype=torch.int32, device=dev),
+                bary=torch.empty((n, 2), dtype=torch.float32, device=dev) if want_bary else None)
+        ws_ptr, ws_bytes = c_void_p(None), 0
+        if workspace is not None:
+            ws_ptr, ws_bytes = c_void_p(workspace.data_ptr()), workspace.numel() * workspace.element_size()
+        check(lib.cp_query(self._h, _ptr(points), n, byref(o), _ptr(out.point), _ptr(out.dist),
+                           _ptr(out.tri), _ptr(out.bary), ws_ptr, ws_bytes, _stream(stream)),
+              "cp_query")
+        return out
+
+    def query_host(self, points: np.ndarray | torch.Tensor, *, want_point: bool = True,
+                   want_bary: bool = False, opts: QueryOpts | None = None,
+                   out: dict | None = None) -> dict:
+        """Host arrays in and out (pinned torch CPU tensors give full copy speed)."""
+        if isinstance(points, np.ndarray):
+            points = torch.from_numpy(np.ascontiguousarray(points, dtype=np.float32))
+        if points.is_cuda or points.dtype != torch.float32 or not points.is_contiguous():
+            raise ValueError("points must be a contiguous float32 CPU tensor")
+        n = int(points.shape[0])
+        pin = points.is_pinned()
+        if out is None:
+            out = {"dist": torch.empty((n,), dtype=torch.float32, pin_memory=pin),
+                   "tri": torch.empty((n,), dtype=torch.int32, pin_memory=pin)}
+            if want_point:
+                out["point"] = torch.empty((n, 3), dtype=torch.float32, pin_memory=pin)
+            if want_bary:
+                out["bary"] = torch.empty((n, 2), dtype=torch.float32, pin_memory=pin)
+        o = opts or query_opts()
+        check(lib.cp_query_host(self._h, _ptr(points), n, byref(o), _ptr(out.get("point")),
+                                _ptr(out["dist"]), _ptr(out["tri"]), _ptr(out.get("bary")),
+                                _stream()), "cp_query_host")
+        return out
+
+    def refit(self, verts: torch.Tensor, stream=None) -> None:
+        if not verts.is_cuda or verts.dtype != torch.float32 or verts.shape[0] != self.num_vertices:
+            raise ValueError("verts must be a CUDA float32 tensor with the mesh's vertex count")
+        check(lib.cp_mesh_refit(self._h, _ptr(verts), verts.stride(0) * 4, _stream(stream)),
+              "cp_mesh_refit")
+
+    def backward(self, points: torch.Tensor, tri: torch.Tensor, bary: torch.Tensor,
+                 grad_dist: torch.Tensor, *, need_points: bool = True, need_verts: bool = True,
+                 grad_verts: torch.Tensor | None = None, stream=None):
+        _check_dev(points, "points", torch.float32, 3)
+        n = int(points.shape[0])
+        grad_dist = grad_dist.contiguous().to(torch.float32)
+        gq = torch.empty((n, 3), dtype=torch.float32, device=points.device) if need_points else None
+        if need_verts and grad_verts is None:
+            grad_verts = torch.zeros((self.num_vertices, 3), dtype=torch.float32, device=points.device)
+        check(lib.cp_backward(self._h, _ptr(points), _ptr(tri.contiguous()), _ptr(bary.contiguous()),
+                              _ptr(grad_dist), n, _ptr(gq), _ptr(grad_verts if need_verts else None),
+                              _stream(stream)), "cp_backward")
+        return gq, (grad_verts if need_verts else None)
+
+    # -- inspection ----------------------------------------------------------
+    def export_build(self) -> dict:
+        n = self.num_triangles
+        info = self.info()
+        out = {"keys": np.empty(n, np.uint64), "order": np.empty(n, np.int32),
+               "left": np.empty(max(n - 1, 1), np.int32), "right": np.empty(max(n - 1, 1), np.int32),
+               "parent": np.empty(2 * n - 1, np.int32), "cluster": np.empty(2 * n - 1, np.uint8),
+               "wide_src": np.empty(info.num_wide_nodes, np.int32)}
+        check(lib.cp_mesh_export_build(self._h, *(c_void_p(out[k].ctypes.data) for k in
+                                                  ("keys", "order", "left", "right", "parent",
+                                                   "cluster", "wide_src"))), "export")
+        if n == 1:
+            out["left"] = out["left"][:0]
+            out["right"] = out["right"][:0]
+        return out
+
+    def export_wide(self) -> dict:
+        info = self.info()
+        K, w = info.branching, info.num_wide_nodes
+        out = {"boxes": np.empty(w * 6 * K, np.float32), "refs": np.empty(w * K, np.int32),
+               "counts": np.empty(w * K, np.int32)}
+        check(lib.cp_mesh_export_wide(self._h, c_void_p(out["boxes"].ctypes.data),
+                                      c_void_p(out["refs"].ctypes.data),
+                                      c_void_p(out["counts"].ctypes.data)), "export")
+        return out
+
+
+class Batch:
+    """Many meshes with one batched build and one persistent query launch."""
+
+    def __init__(self, verts: torch.Tensor, vert_offsets, tris: torch.Tensor, tri_offsets, *,
+                 branching: int = 2, leaf_size: int = 4, collapse: str = "count", stream=None):
+        _check_dev(verts, "verts", torch.float32, 3)
+        _check_dev(tris, "tris", torch.int32, 3)
+        self.vert_offsets = np.ascontiguousarray(vert_offsets, dtype=np.int64)
+        self.tri_offsets = np.ascontiguousarray(tri_offsets, dtype=np.int64)
+        self.nmeshes = len(self.tri_offsets) - 1
+        self.opts = build_opts(branching, leaf_size, collapse)
+        h = c_void_p()
+        check(lib.cp_batch_create(_ptr(verts), c_void_p(self.vert_offsets.ctypes.data), _ptr(tris),
+                                  c_void_p(self.tri_offsets.ctypes.data), self.nmeshes,
+                                  byref(self.opts), _stream(stream), byref(h)), "cp_batch_create")
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            lib.cp_batch_destroy(self._h)
+            self._h = c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self) -> dict:
+        nm, nw, ntri, sb = c_int32(), c_int64(), c_int64(), c_int32()
+        check(lib.cp_batch_info(self._h, byref(nm), byref(nw), byref(ntri), byref(sb)), "cp_batch_info")
+        return {"nmeshes": nm.value, "num_wide_nodes": nw.value, "num_triangles": ntri.value,
+                "stack_bound": sb.value}
+
+    def workspace_size(self, nq: int, opts: QueryOpts | None = None) -> int:
+        b = c_size_t(0)
+        o = opts or query_opts()
+        check(lib.cp_batch_query_workspace_size(self._h, nq, byref(o), byref(b)), "workspace")
+        return b.value
+
+    def query(self, points: torch.Tensor, q_offsets, *, want_point: bool = True,
+              want_bary: bool = False, opts: QueryOpts | None = None,
+              workspace: torch.Tensor | None = None, use_graph: bool = False,
+              out: QueryResult | None = None, stream=None) -> QueryResult:
+        _check_dev(points, "points", torch.float32, 3)
+        qoff = np.ascontiguousarray(q_offsets, dtype=np.int64)
+        n = int(points.shape[0])
+        if int(qoff[-1]) != n:
+            raise ValueError("q_offsets[-1] must equal the number of points")
+        o = opts or query_opts()
+        if out is None:
+            dev = points.device
+            out = QueryResult(
+                point=torch.empty((n, 3), dtype=torch.float32, device=dev) if want_point else None,
+                dist=torch.empty((n,), dtype=torch.float32, device=dev),
+                tri=torch.empty((n,), dtype=torch.int32, device=dev),
+                bary=torch.empty((n, 2), dtype=torch.float32, device=dev) if want_bary else None)
+        ws_ptr, ws_bytes = c_void_p(None), 0
+        if workspace is not None:
+            ws_ptr, ws_bytes = c_void_p(workspace.data_ptr()), workspace.numel() * workspace.element_size()
+        check(lib.cp_batch_query(self._h, _ptr(points), c_void_p(qoff.ctypes.data), byref(o),
+                                 _ptr(out.point), _ptr(out.dist), _ptr(out.tri), _ptr(out.bary),
+                                 ws_ptr, ws_bytes, 1 if use_graph else 0, _stream(stream)),
+              "cp_batch_query")
+        return out
+
+
+def autotune(verts: torch.Tensor, tris: torch.Tensor, sample: torch.Tensor,
+             cache_path: str | None = None):
+    """Run cp_autotune; returns (BuildOpts, QueryOpts)."""
+    _check_dev(verts, "verts", torch.float32, 3)
+    _check_dev(tris, "tris", torch.int32, 3)
+    _check_dev(sample, "sample", torch.float32, 3)
+    bo, qo = BuildOpts(), QueryOpts()
+    torch.cuda.synchronize()
+    check(lib.cp_autotune(_ptr(verts), verts.shape[0], _ptr(tris), tris.shape[0], _ptr(sample),
+                          sample.shape[0], cache_path.encode() if cache_path else None, byref(bo),
+                          byref(qo)), "cp_autotune")
+    return bo, qo
+
+
+class _ClosestDistance(torch.autograd.Function):
+    """Unsigned distance with a hand-written adjoint (cp_backward).
+
+    The forward keeps only the winning triangle index and its barycentrics;
+    the backward recomputes the closest point from them instead of storing
+    traversal state.
+    """
+
+    @staticmethod
+    def forward(ctx, points, verts, mesh: Mesh):
+        res = mesh.query(points.detach().contiguous(), want_point=False, want_bary=True)
+        ctx.mesh = mesh
+        ctx.save_for_backward(points.detach().contiguous(), res.tri, res.bary)
+        ctx.mark_non_differentiable(res.tri)
+        return res.dist, res.tri
+
+    @staticmethod
+    def backward(ctx, grad_dist, _grad_tri):
+        points, tri, bary = ctx.saved_tensors
+        need_q, need_v = ctx.needs_input_grad[0], ctx.needs_input_grad[1]
+        if grad_dist is None or not (need_q or need_v):
+            return None, None, None
+        gq, gv = ctx.mesh.backward(points, tri, bary, grad_dist, need_points=need_q,
+                                   need_verts=need_v)
+        return gq, gv, None
+
+
+def closest_distance(points: torch.Tensor, mesh: Mesh, verts: torch.Tensor | None = None):
+    """Differentiable unsigned distance from each point to the mesh.
+
+    ``verts`` is the (V, 3) tensor the mesh was built from (or refitted to);
+    pass it with ``requires_grad`` to receive d(distance)/d(vertices).
+    Returns (dist, tri).
+    """
+    if verts is None:
+        verts = torch.empty((mesh.num_vertices, 3), device=points.device)
+    return _ClosestDistance.apply(points, verts, mesh)

@@ -1,0 +1,302 @@
+/*
+ * cpq.h — C ABI of the GB300 closest-point engine.
+ *
+ * Query surface: a triangle mesh goes in, a BVH is built on the GPU, a batch
+ * of query points goes in, and for every point the closest point on the mesh,
+ * the unsigned distance and the index of the closest triangle come out.
+ *
+ * The reference (TheNumbat/GPU-RT, main branch) has no library target and no
+ * FFI: it is one SDL executable (CMakeLists.txt:66-70).  Its closest-point
+ * work lives on a branch that is not available, so every entry point below
+ * names the reference interface whose role it takes over:
+ *   - mesh in + BVH built  ->  VK::Mesh (src/vk/mesh.h:14-58) and
+ *                              VK::Accel(const Mesh&) (src/vk/vulkan.h:259,
+ *                              src/vk/vulkan.cpp:881-936);
+ *   - query                ->  trace_ray / traceRayEXT over the TLAS
+ *                              (src/shaders/rt/rt.rgen:257-270), issued by
+ *                              RTPipe::trace (src/vk/rt.cpp:346-394);
+ *   - many meshes at once  ->  the TLAS over per-mesh BLASes
+ *                              (src/vk/vulkan.cpp:777-856, src/gpurt.cpp:220-241);
+ *   - destroy              ->  Drop<T> / Accel::destroy (src/vk/vulkan.h:305-336).
+ *
+ * Conventions
+ *   - Every array argument is caller-owned DEVICE memory unless the entry
+ *     point's name ends in _host.  Handles own their BVH memory.
+ *   - Every call returns a cp_status and never exits the process (the
+ *     reference's die() calls std::exit, src/lib/log.h:46-49).
+ *     cp_last_error_string() describes the last failure of the calling thread.
+ *   - Calls are asynchronous on the given stream unless documented otherwise.
+ *     A NULL stream is the legacy default stream.
+ *   - A built mesh is read-only for cp_query / cp_backward, so concurrent
+ *     queries on different streams are safe.  cp_mesh_refit and
+ *     cp_mesh_destroy need exclusive access.
+ *   - Triangle indices are int32 triples into the mesh's own vertex array.
+ *     Vertices are float xyz triples with a byte stride >= 12 (48 reads the
+ *     reference's VK::Mesh::Vertex layout, src/vk/mesh.h:16-22, directly).
+ *   - Tie rule: among triangles at exactly the same computed distance, the one
+ *     with the smallest index wins.
+ */
+#ifndef GPURT_CPQ_H
+#define GPURT_CPQ_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define CP_API __declspec(dllexport)
+#else
+#define CP_API __attribute__((visibility("default")))
+#endif
+
+/* Same type as cudaStream_t; declared here so the header needs no CUDA headers. */
+typedef struct CUstream_st* cp_stream_t;
+
+typedef enum cp_status {
+    CP_SUCCESS = 0,
+    CP_ERROR_INVALID_VALUE = 1,   /* bad pointer, size, option or index */
+    CP_ERROR_OUT_OF_MEMORY = 2,   /* a device or host allocation failed */
+    CP_ERROR_CUDA = 3,            /* a CUDA runtime call failed */
+    CP_ERROR_DEVICE_FAULT = 4,    /* a kernel reported an error through its status word */
+    CP_ERROR_NOT_SUPPORTED = 5,   /* no GPU, or an option this build does not support */
+    CP_ERROR_SCRATCH_TOO_SMALL = 6 /* a workspace or fixed scratch area is too small */
+} cp_status;
+
+/* Device status-word bits, reported by cp_mesh_device_status(). */
+#define CP_DEVICE_STACK_OVERFLOW 0x1u
+#define CP_DEVICE_BAD_INDEX      0x2u
+#define CP_DEVICE_NONFINITE      0x4u
+
+typedef enum cp_collapse {
+    CP_COLLAPSE_COUNT = 0,  /* a subtree becomes a leaf when it holds <= leaf_size triangles */
+    CP_COLLAPSE_SAH = 1     /* ... and the surface-area heuristic says a leaf is cheaper */
+} cp_collapse;
+
+typedef struct cp_build_opts {
+    int32_t branching;      /* BVH width: 2, 4 or 8 */
+    int32_t leaf_size;      /* maximum triangles per leaf, 1..15 */
+    int32_t collapse;       /* cp_collapse */
+    float sah_node_cost;    /* SAH cost of one node visit (CP_COLLAPSE_SAH) */
+    float sah_tri_cost;     /* SAH cost of one point-triangle test (CP_COLLAPSE_SAH) */
+} cp_build_opts;
+
+typedef struct cp_query_opts {
+    int32_t block_size;     /* traversal threads per block: 64..1024, multiple of 32; 0 = default */
+    int32_t sort_queries;   /* 1: walk the queries in Morton order of their position (outputs keep input order) */
+    int32_t blocks_per_sm;  /* persistent grid = SM count x this; 0 = from occupancy */
+    int32_t short_stack;    /* per-thread stack entries kept in shared memory: 4, 8 or 16; 0 = default */
+} cp_query_opts;
+
+/* Statistics of a built mesh (cp_mesh_info). */
+typedef struct cp_mesh_info_t {
+    int64_t num_vertices;
+    int64_t num_triangles;
+    int64_t num_binary_nodes;   /* 2*T - 1 */
+    int64_t num_wide_nodes;
+    int64_t num_leaves;         /* leaf clusters */
+    int32_t branching;
+    int32_t leaf_size;
+    int32_t max_wide_depth;     /* edges on the longest root-to-leaf path of the wide BVH */
+    int32_t stack_bound;        /* stack entries the traversal can need at most */
+    int64_t device_bytes;       /* BVH + triangle memory held by the handle */
+    float build_ms;             /* device time of the last build or refit (0 if not timed) */
+} cp_mesh_info_t;
+
+typedef struct cp_mesh cp_mesh;
+typedef struct cp_batch cp_batch;
+
+/* ---- options ---------------------------------------------------------------- */
+
+/* Binary BVH, leaf size 4, count collapse: the canonical configuration. */
+CP_API void cp_build_opts_default(cp_build_opts* opts);
+CP_API void cp_query_opts_default(cp_query_opts* opts);
+
+/* ---- errors ----------------------------------------------------------------- */
+
+/* Message of the last failed call on this thread ("" if none). */
+CP_API const char* cp_last_error_string(void);
+CP_API const char* cp_status_string(cp_status status);
+/* Library version as an integer (major * 10000 + minor * 100 + patch). */
+CP_API int32_t cp_version(void);
+
+/* ---- single mesh -------------------------------------------------------------- */
+
+/*
+ * Build a BVH over a triangle mesh.  Replaces VK::Accel(const Mesh&)
+ * (src/vk/vulkan.h:259; src/vk/vulkan.cpp:881-936), which hands the mesh to
+ * the Vulkan driver's closed BVH builder.  Here the build is a Morton-code
+ * LBVH (63-bit codes, stable radix sort, Karras 2012 hierarchy), a bottom-up
+ * bounding-box refit, a leaf collapse (count or SAH) and a collapse to
+ * `branching`-wide nodes.  `verts` holds nv points of 3 floats at
+ * `vert_stride_bytes` (a multiple of 4, >= 12); `tris` holds nt int32 triples.
+ * opts may be NULL (defaults).  Synchronises `stream` before returning.
+ */
+CP_API cp_status cp_mesh_create(const float* verts, int64_t nv, int64_t vert_stride_bytes,
+                                const int32_t* tris, int64_t nt, const cp_build_opts* opts,
+                                cp_stream_t stream, cp_mesh** out);
+
+/*
+ * Move the vertices of a built mesh (same count, same triangles) and refit
+ * every box bottom-up; the tree topology is kept.  Takes the role of the
+ * reference's rebuild-on-change of its BLAS (src/gpurt.cpp:220-241).
+ * Asynchronous on `stream`; no host synchronisation, so it can be captured
+ * in a CUDA graph.
+ */
+CP_API cp_status cp_mesh_refit(cp_mesh* mesh, const float* verts, int64_t vert_stride_bytes,
+                               cp_stream_t stream);
+
+/* Free the handle and its device memory (Accel::destroy, src/vk/vulkan.h:268). */
+CP_API cp_status cp_mesh_destroy(cp_mesh* mesh);
+
+CP_API cp_status cp_mesh_info(const cp_mesh* mesh, cp_mesh_info_t* out);
+
+/*
+ * Synchronise `stream`, return the device status bits the kernels set on this
+ * mesh since the last call (CP_DEVICE_*), and clear them.
+ */
+CP_API cp_status cp_mesh_device_status(cp_mesh* mesh, cp_stream_t stream, uint32_t* bits);
+
+/*
+ * Bytes of device workspace cp_query needs for nq queries with these options.
+ */
+CP_API cp_status cp_query_workspace_size(const cp_mesh* mesh, int64_t nq, const cp_query_opts* opts,
+                                         size_t* bytes);
+
+/*
+ * Closest-point query.  Replaces the per-pixel traceRayEXT over the
+ * acceleration structure (src/shaders/rt/rt.rgen:257-270) with a closest-first
+ * BVH descent and an exact point-triangle distance at the leaves; the
+ * hit payload {barycentrics, primitive id} (src/shaders/rt/rtcommon.glsl:55-60,
+ * src/shaders/rt/rt.rchit:11-16) becomes {closest point, distance, triangle,
+ * barycentrics}.
+ *   queries    nq x 3 floats
+ *   out_point  nq x 3 floats (closest point), may be NULL
+ *   out_dist   nq floats (unsigned distance), may be NULL
+ *   out_tri    nq int32 (closest triangle), may be NULL
+ *   out_bary   nq x 2 floats (barycentric weights of vertices 1 and 2 of the
+ *              closest triangle; vertex 0 has 1 - u - v), may be NULL
+ *   workspace  device memory of cp_query_workspace_size() bytes, or NULL to
+ *              allocate it stream-ordered inside the call.
+ * nq == 0 is a no-op.  Asynchronous on `stream`.
+ */
+CP_API cp_status cp_query(const cp_mesh* mesh, const float* queries, int64_t nq,
+                          const cp_query_opts* opts, float* out_point, float* out_dist,
+                          int32_t* out_tri, float* out_bary, void* workspace,
+                          size_t workspace_bytes, cp_stream_t stream);
+
+/*
+ * cp_query with HOST arrays: copies the queries to the device in chunks,
+ * queries each chunk and copies the results back, overlapping the copies of
+ * one chunk with the traversal of the previous one.  Host arrays should be
+ * pinned (cudaHostAlloc / cudaHostRegister) for full copy speed.  Synchronous:
+ * the outputs are ready when it returns.
+ */
+CP_API cp_status cp_query_host(const cp_mesh* mesh, const float* queries, int64_t nq,
+                               const cp_query_opts* opts, float* out_point, float* out_dist,
+                               int32_t* out_tri, float* out_bary, cp_stream_t stream);
+
+/*
+ * Adjoint of the unsigned distance.  For each query i with upstream gradient
+ * g_i = grad_dist[i], closest triangle t = tri[i] and barycentrics b = bary[i]:
+ *   grad_queries[i]  = g_i (q_i - p_i) / d_i           (written; may be NULL)
+ *   grad_verts[v_k] += -g_i b_k (q_i - p_i) / d_i      (accumulated atomically
+ *                      for the three vertices of t; may be NULL)
+ * with p_i = sum_k b_k v_k recomputed from the mesh and d_i = |q_i - p_i|;
+ * d_i == 0 contributes zero.  The gradient with respect to the vertices
+ * follows from the envelope theorem (the barycentrics are optimal, so their
+ * own derivative drops out).  grad_verts is nv x 3 floats and is NOT cleared.
+ * No counterpart in the reference, which has no differentiable path.
+ */
+CP_API cp_status cp_backward(const cp_mesh* mesh, const float* queries, const int32_t* tri,
+                             const float* bary, const float* grad_dist, int64_t nq,
+                             float* grad_queries, float* grad_verts, cp_stream_t stream);
+
+/* ---- many meshes, one launch ---------------------------------------------- */
+
+/*
+ * Build one BVH per mesh for a set of meshes in one batched build: one sort
+ * over (mesh id, Morton code) keys, one hierarchy and refit pass, one collapse.
+ * Takes the role of the reference's BLAS-per-mesh plus TLAS build
+ * (src/vk/vulkan.cpp:777-856; src/gpurt.cpp:220-241).
+ *   verts          all meshes' vertices back to back, total_v x 3 floats
+ *   vert_offsets   HOST array of nmeshes + 1 int64 vertex offsets
+ *   tris           all meshes' triangles back to back, indices LOCAL to each mesh
+ *   tri_offsets    HOST array of nmeshes + 1 int64 triangle offsets
+ * Every mesh needs at least one triangle.  Synchronises `stream`.
+ */
+CP_API cp_status cp_batch_create(const float* verts, const int64_t* vert_offsets,
+                                 const int32_t* tris, const int64_t* tri_offsets, int32_t nmeshes,
+                                 const cp_build_opts* opts, cp_stream_t stream, cp_batch** out);
+
+CP_API cp_status cp_batch_destroy(cp_batch* batch);
+
+/* Per-mesh root info: number of meshes and wide-node count of the whole batch. */
+CP_API cp_status cp_batch_info(const cp_batch* batch, int32_t* nmeshes, int64_t* num_wide_nodes,
+                               int64_t* num_triangles, int32_t* stack_bound);
+
+CP_API cp_status cp_batch_query_workspace_size(const cp_batch* batch, int64_t nq,
+                                               const cp_query_opts* opts, size_t* bytes);
+
+/*
+ * Query every mesh of a batch in one persistent, work-stealing launch.
+ * Queries of mesh m are queries[q_offsets[m] .. q_offsets[m+1]) (q_offsets is a
+ * HOST array of nmeshes + 1 int64).  out_tri holds triangle indices local to
+ * each mesh.  Outputs as in cp_query.  With use_graph != 0 the launch sequence
+ * is captured into a CUDA graph on first use with these pointers and sizes
+ * and replayed on later calls (the workspace must then be given and stay the
+ * same).
+ */
+CP_API cp_status cp_batch_query(cp_batch* batch, const float* queries, const int64_t* q_offsets,
+                                const cp_query_opts* opts, float* out_point, float* out_dist,
+                                int32_t* out_tri, float* out_bary, void* workspace,
+                                size_t workspace_bytes, int32_t use_graph, cp_stream_t stream);
+
+/* ---- autotuner ------------------------------------------------------------ */
+
+/*
+ * Pick branching, leaf size, block size and short-stack depth for a mesh's
+ * size class by timing candidate builds and queries on the given mesh and a
+ * sample of queries (device arrays).  The winner is written to *best_build /
+ * *best_query and, when cache_path is not NULL, stored in that text file
+ * under the size class (one "class branching leaf block stack ms" line per
+ * class); a cached class is returned without timing.  Synchronous.
+ */
+CP_API cp_status cp_autotune(const float* verts, int64_t nv, const int32_t* tris, int64_t nt,
+                             const float* queries, int64_t nq, const char* cache_path,
+                             cp_build_opts* best_build, cp_query_opts* best_query);
+
+/* Size class used by the autotuner cache: floor(log2(num_triangles)). */
+CP_API int32_t cp_size_class(int64_t num_triangles);
+
+/* ---- inspection (tests compare these with the CPU restatement bit for bit) -- */
+
+/*
+ * Copy the build's intermediate arrays to HOST memory (any pointer may be
+ * NULL): sorted 64-bit Morton keys and triangle order (nt each), the binary
+ * hierarchy's left/right children (nt-1 each; ids >= nt-1 are leaves
+ * nt-1+k for sorted position k), parent (2nt-1), the leaf-cluster flag per
+ * binary node (2nt-1 bytes) and, per wide node, the binary node it was made
+ * from.  Synchronous.
+ */
+CP_API cp_status cp_mesh_export_build(const cp_mesh* mesh, uint64_t* keys, int32_t* order,
+                                      int32_t* left, int32_t* right, int32_t* parent,
+                                      uint8_t* cluster, int32_t* wide_src);
+
+/*
+ * Copy the wide nodes to HOST memory: num_wide_nodes * branching * 6 floats of
+ * child boxes (lo x, hi x, lo y, hi y, lo z, hi z per child), child refs and
+ * child counts (num_wide_nodes * branching int32 each; count 0 = inner child,
+ * count > 0 = leaf of `count` triangles starting at sorted position `ref`,
+ * count -1 = empty slot).  Synchronous.
+ */
+CP_API cp_status cp_mesh_export_wide(const cp_mesh* mesh, float* boxes, int32_t* refs,
+                                     int32_t* counts);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPURT_CPQ_H */

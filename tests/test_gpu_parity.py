@@ -1,0 +1,361 @@
+"""GPU parity: the CUDA build must equal the CPU restatement bit for bit, and
+queries must match the FP64 oracle (distances within 1e-6 relative; indices
+equal except at FP64-confirmed ties within 1e-6).  All calls go through the
+C ABI (gpurt_cpq is a ctypes binding of include/cpq.h)."""
+from __future__ import annotations
+
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+REL_TOL = 1e-6      # distance tolerance against FP64 (relative)
+ABS_TOL = 1e-7      # for exact zero distances (query on the surface)
+
+
+def dev(a, cuda):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+
+
+def rel_err(d, ref):
+    d = np.asarray(d, np.float64)
+    out = np.abs(d - ref)
+    nz = ref > 0
+    out[nz] /= ref[nz]
+    return out
+
+
+def check_against_fp64(orc, v, t, q, res, ref=None, rel=REL_TOL):
+    """Distances, indices (ties confirmed in FP64), points; returns stats."""
+    if ref is None:
+        ref = orc.brute_f64(v, t, q) if t.shape[0] * q.shape[0] <= 4e8 else orc.exact_f64(v, t, q)
+    d = res.dist.cpu().numpy()
+    tri = res.tri.cpu().numpy()
+    err = rel_err(d, ref["dist"])
+    zero = ref["dist"] == 0
+    assert np.all(np.abs(d[zero]) <= ABS_TOL), "zero distances"
+    assert err[~zero].max(initial=0) <= rel, f"max rel err {err[~zero].max()}"
+    mm = np.nonzero(tri != ref["tri"])[0]
+    if len(mm):
+        assert np.all(tri[mm] >= 0)
+        dt = orc.dist_to_tri_f64(v, t, q[mm], tri[mm])
+        gap = (dt - ref["dist"][mm]) / np.maximum(ref["dist"][mm], 1e-30)
+        assert np.all(gap <= 1e-6), f"{len(mm)} index mismatches, worst FP64 gap {gap.max()}"
+    if res.point is not None:
+        p = res.point.cpu().numpy().astype(np.float64)
+        scale = np.maximum(1.0, np.abs(ref["point"]).max(axis=1))
+        perr = np.linalg.norm(p - ref["point"], axis=1) / scale
+        # a tie may legitimately move the closest point along the shared feature
+        ok = (perr <= 1e-6) | (tri != ref["tri"])
+        assert ok.all(), f"point error {perr[~ok].max()}"
+    return {"max_rel": float(err[~zero].max(initial=0)),
+            "p99_rel": float(np.percentile(err[~zero], 99)) if (~zero).any() else 0.0,
+            "mismatch": int(len(mm))}
+
+
+# ---------------------------------------------------------------- known answers
+
+def test_kat_gpu(cpq, cuda):
+    cases = json.loads((GOLDEN / "kat_point_triangle.json").read_text())
+    for c in cases["cases"]:
+        v = np.array([c["a"], c["b"], c["c"]], np.float32)
+        t = np.array([[0, 1, 2]], np.int32)
+        q = np.array([c["q"]], np.float32)
+        m = cpq.Mesh(dev(v, cuda), dev(t, cuda))
+        r = m.query(dev(q, cuda), want_bary=True)
+        d = float(r.dist.cpu()[0])
+        if c["dist"] == 0:
+            assert abs(d) <= ABS_TOL, c
+        else:
+            assert abs(d - c["dist"]) <= REL_TOL * c["dist"], (c, d)
+        np.testing.assert_allclose(r.point.cpu().numpy()[0], c["point"], atol=1e-5, rtol=1e-6)
+        if c["bary"] is not None:
+            b = r.bary.cpu().numpy()[0]
+            np.testing.assert_allclose([1 - b[0] - b[1], b[0], b[1]], c["bary"], atol=1e-6)
+        assert int(r.tri.cpu()[0]) == 0
+    tm = cases["tie_mesh"]
+    m = cpq.Mesh(dev(np.array(tm["verts"], np.float32), cuda), dev(np.array(tm["tris"], np.int32), cuda))
+    r = m.query(dev(np.array(tm["queries"], np.float32), cuda))
+    np.testing.assert_array_equal(r.tri.cpu().numpy(), tm["tri"])
+
+
+# ---------------------------------------------------------------- bit-exact build
+
+def meshes_for_build():
+    from gpurt_cpq import workloads as W
+
+    rng = np.random.default_rng(5)
+    ico = W.icosphere(4)
+    hf = W.heightfield(64, seed=9)
+    rv = rng.normal(size=(500, 3)).astype(np.float32)
+    rt = rng.integers(0, 500, (2000, 3)).astype(np.int32)
+    rt[:50] = rt[0]  # duplicated triangles: equal keys
+    tiny = (np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [1, 1, 0]], np.float32),
+            np.array([[0, 1, 2], [1, 3, 2]], np.int32))
+    one = (tiny[0], tiny[1][:1])
+    return {"icosphere4": ico, "heightfield64": hf, "random_dup": (rv, rt), "two": tiny, "one": one}
+
+
+BUILDS = [(2, 4, 0), (4, 4, 0), (8, 4, 0), (4, 1, 0), (4, 8, 1), (8, 15, 0), (2, 2, 1)]
+
+
+@pytest.mark.parametrize("name", ["icosphere4", "heightfield64", "random_dup", "two", "one"])
+@pytest.mark.parametrize("K,leaf,collapse", BUILDS)
+def test_build_bit_exact(orc, cpq, cuda, name, K, leaf, collapse):
+    v, t = meshes_for_build()[name]
+    ref = orc.Tree(v, t, K, leaf, collapse, 1.0, 1.0)
+    m = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=K, leaf_size=leaf,
+                 collapse="sah" if collapse else "count")
+    info = m.info()
+    assert info.num_wide_nodes == ref.num_wide
+    assert info.max_wide_depth == ref.max_wide_depth
+    assert info.stack_bound == ref.stack_bound
+    assert info.num_leaves == ref.num_leaves
+    b = m.export_build()
+    np.testing.assert_array_equal(b["keys"], ref.keys)
+    np.testing.assert_array_equal(b["order"], ref.order)
+    np.testing.assert_array_equal(b["left"], ref.left)
+    np.testing.assert_array_equal(b["right"], ref.right)
+    np.testing.assert_array_equal(b["parent"], ref.parent)
+    np.testing.assert_array_equal(b["cluster"], ref.cluster)
+    np.testing.assert_array_equal(b["wide_src"], ref.wide_src)
+    w = m.export_wide()
+    np.testing.assert_array_equal(w["boxes"].view(np.uint32), ref.wide_box.view(np.uint32))
+    np.testing.assert_array_equal(w["refs"], ref.wide_ref)
+    np.testing.assert_array_equal(w["counts"], ref.wide_count)
+
+
+def test_vertex_stride_48(orc, cpq, cuda):
+    """The reference's VK::Mesh::Vertex layout (pos, norm, tang as Vec4) builds the same tree."""
+    import torch
+
+    from gpurt_cpq import workloads as W
+
+    v, t = W.icosphere(3)
+    fat = np.zeros((v.shape[0], 12), np.float32)
+    fat[:, :3] = v
+    fat[:, 4:7] = v  # normal slot
+    m12 = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=4)
+    m48 = cpq.Mesh(dev(fat, cuda), dev(t, cuda), branching=4)
+    a, b = m12.export_wide(), m48.export_wide()
+    for k in a:
+        np.testing.assert_array_equal(a[k], b[k])
+    q = dev(W.uniform_queries(4096, -2, 2, 1), cuda)
+    r1, r2 = m12.query(q), m48.query(q)
+    assert torch.equal(r1.dist, r2.dist) and torch.equal(r1.tri, r2.tri)
+
+
+# ---------------------------------------------------------------- queries
+
+@pytest.mark.parametrize("K", [2, 4, 8])
+def test_query_small_config(orc, cpq, cuda, K):
+    from gpurt_cpq import workloads as W
+
+    v, t, q = W.small()
+    m = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=K, leaf_size=4)
+    r = m.query(dev(q, cuda), want_bary=True)
+    stats = check_against_fp64(orc, v, t, q, r)
+    print(f"small K={K}: {stats}")
+    b = r.bary.cpu().numpy()
+    assert np.all(b >= -1e-6) and np.all(b.sum(1) <= 1 + 1e-6)
+    assert m.device_status() == 0
+
+
+def test_query_options_do_not_change_results(cpq, cuda):
+    import torch
+
+    from gpurt_cpq import workloads as W
+
+    v, t = W.heightfield(128, seed=3)
+    q = W.heightfield_queries(v, t, 50000, seed=4)
+    m = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=4, leaf_size=4)
+    qd = dev(q, cuda)
+    base = m.query(qd, want_bary=True)
+    for kw in [dict(sort_queries=False), dict(block_size=128), dict(block_size=64, short_stack=4),
+               dict(short_stack=16), dict(blocks_per_sm=1)]:
+        r = m.query(qd, want_bary=True, opts=cpq.query_opts(**kw))
+        assert torch.equal(r.dist, base.dist), kw
+        assert torch.equal(r.tri, base.tri), kw
+        assert torch.equal(r.point, base.point), kw
+
+
+def test_query_heightfield_sampled(orc, cpq, cuda):
+    """The large workload's mesh at full size; FP64 checked on a seeded sample."""
+    from gpurt_cpq import workloads as W
+
+    v, t = W.heightfield(1024, seed=1)
+    q = W.heightfield_queries(v, t, 1 << 20, seed=2)
+    m = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=4, leaf_size=4)
+    r = m.query(dev(q, cuda))
+    idx = np.random.default_rng(0).choice(q.shape[0], 65536, replace=False)
+    ref = orc.exact_f64(v, t, q[idx])
+
+    class Sub:
+        pass
+
+    s = Sub()
+    s.dist, s.tri, s.point = r.dist[idx], r.tri[idx], r.point[idx]
+    stats = check_against_fp64(orc, v, t, q[idx], s, ref=ref)
+    print(f"heightfield 1024^2 sample: {stats}")
+
+
+def test_full_size_properties(cpq, cuda):
+    """Size-independent checks on every query of the 16M-query large workload:
+    p lies on the reported triangle at the reported barycentrics, |q - p| is
+    the reported distance, and the answer is no farther than a probe triangle."""
+    import torch
+
+    from gpurt_cpq import workloads as W
+
+    v, t, q = W.large()
+    vd, td, qd = dev(v, cuda), dev(t, cuda), dev(q, cuda)
+    m = cpq.Mesh(vd, td, branching=4, leaf_size=4)
+    r = m.query(qd, want_bary=True)
+    assert int((r.tri < 0).sum()) == 0
+    tri = td[r.tri.long()].long()
+    a, b, c = vd[tri[:, 0]].double(), vd[tri[:, 1]].double(), vd[tri[:, 2]].double()
+    bv, bw = r.bary[:, 0:1].double(), r.bary[:, 1:2].double()
+    p = a + bv * (b - a) + bw * (c - a)
+    assert float((p - r.point.double()).norm(dim=1).max()) < 1e-5
+    d = (qd.double() - r.point.double()).norm(dim=1)
+    # the FP32 rounding of the reported point bounds the difference
+    assert float(((d - r.dist.double()).abs() - 1e-6 * d).max()) < 5e-7
+    # the distance to triangle 0 bounds every answer from above
+    probe = (qd.double() - vd[td[0, 0].long()].double()).norm(dim=1)
+    assert bool((r.dist.double() <= probe + 1e-6).all())
+    assert m.device_status() == 0
+    del tri, a, b, c, p, d, probe
+    torch.cuda.empty_cache()
+
+
+def test_reference_meshes(orc, cpq, cuda):
+    g = np.load(GOLDEN / "ref_meshes.npz")
+    vo, to, qo = g["vert_offsets"], g["tri_offsets"], g["q_offsets"]
+    for mi in range(len(to) - 1):
+        v = g["verts"][vo[mi]:vo[mi + 1]]
+        t = g["tris"][to[mi]:to[mi + 1]]
+        q = g["queries"][qo[mi]:qo[mi + 1]]
+        ref = {"dist": g["dist"][qo[mi]:qo[mi + 1]], "tri": g["tri"][qo[mi]:qo[mi + 1]]}
+        ref.update({k: orc.brute_f64(v, t, q)[k] for k in ("point",)})
+        m = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=4)
+        check_against_fp64(orc, v, t, q, m.query(dev(q, cuda)), ref=ref)
+
+
+def test_degenerate_triangles(orc, cpq, cuda):
+    rng = np.random.default_rng(2)
+    v = rng.normal(size=(300, 3)).astype(np.float32)
+    t = rng.integers(0, 300, (1000, 3)).astype(np.int32)
+    v[:3] = [[0, 0, 0], [1, 0, 0], [2, 0, 0]]
+    t[:20] = [0, 1, 2]           # collinear
+    t[20:40] = [[5, 5, 6]]       # repeated vertex
+    t[40:60] = [[7, 7, 7]]       # a point
+    q = (rng.normal(size=(20000, 3)) * 1.5).astype(np.float32)
+    m = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=4)
+    check_against_fp64(orc, v, t, q, m.query(dev(q, cuda)))
+
+
+def test_queries_on_surface_and_far(orc, cpq, cuda):
+    from gpurt_cpq import workloads as W
+
+    v, t = W.icosphere(4)
+    far = np.array([[1e4, 0, 0], [0, -3e4, 1e4], [123.5, 77.25, -1000]], np.float32)
+    q = np.concatenate([v[:500], far]).astype(np.float32)   # exactly on vertices, then far away
+    m = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=8)
+    check_against_fp64(orc, v, t, q, m.query(dev(q, cuda)))
+
+
+def test_edge_cases(cpq, cuda):
+    import torch
+
+    from gpurt_cpq._lib import CP_ERROR_INVALID_VALUE, CP_ERROR_SCRATCH_TOO_SMALL, CpError
+    from gpurt_cpq import workloads as W
+
+    v, t = W.icosphere(2)
+    m = cpq.Mesh(dev(v, cuda), dev(t, cuda))
+    empty = torch.empty((0, 3), dtype=torch.float32, device=cuda)
+    r = m.query(empty)
+    assert r.dist.numel() == 0
+    one = m.query(dev(np.array([[0, 0, 2]], np.float32), cuda))
+    assert abs(float(one.dist.cpu()[0]) - 1.0) < 1e-3
+    # a NaN query finds nothing: tri -1, NaN distance, and the status bit
+    nan = m.query(dev(np.array([[np.nan, 0, 0], [0, 0, 3]], np.float32), cuda))
+    assert int(nan.tri.cpu()[0]) == -1 and np.isnan(float(nan.dist.cpu()[0]))
+    assert int(nan.tri.cpu()[1]) >= 0
+    assert m.device_status() & 0x4
+    assert m.device_status() == 0
+    # too small a workspace is refused before any launch
+    q = dev(W.uniform_queries(1000, -1, 1, 0), cuda)
+    ws = torch.empty(16, dtype=torch.uint8, device=cuda)
+    with pytest.raises(CpError) as e:
+        m.query(q, workspace=ws)
+    assert e.value.status == CP_ERROR_SCRATCH_TOO_SMALL
+    # caller-provided workspace of the reported size works
+    ws = torch.empty(m.workspace_size(1000), dtype=torch.uint8, device=cuda)
+    assert torch.equal(m.query(q, workspace=ws).dist, m.query(q).dist)
+    # invalid meshes are refused with a status, not a fault
+    bad = t.copy()
+    bad[3, 1] = v.shape[0] + 5
+    with pytest.raises(CpError) as e:
+        cpq.Mesh(dev(v, cuda), dev(bad, cuda))
+    assert e.value.status == CP_ERROR_INVALID_VALUE
+    bad[3, 1] = -1
+    with pytest.raises(CpError):
+        cpq.Mesh(dev(v, cuda), dev(bad, cuda))
+    vn = v.copy()
+    vn[7, 2] = np.inf
+    with pytest.raises(CpError) as e:
+        cpq.Mesh(dev(vn, cuda), dev(t, cuda))
+    assert e.value.status == CP_ERROR_INVALID_VALUE
+    with pytest.raises(CpError):
+        cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=3)
+    with pytest.raises(CpError):
+        cpq.Mesh(dev(v, cuda), dev(t, cuda), leaf_size=16)
+
+
+def test_host_buffers_match_device(cpq, cuda):
+    import torch
+
+    from gpurt_cpq import workloads as W
+
+    v, t = W.torus(100, 40)
+    q = W.uniform_queries(200000, -1.5, 1.5, 8)
+    m = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=4)
+    d = m.query(dev(q, cuda), want_bary=True)
+    h = m.query_host(torch.from_numpy(q).pin_memory(), want_bary=True)
+    assert torch.equal(h["dist"], d.dist.cpu())
+    assert torch.equal(h["tri"], d.tri.cpu())
+    assert torch.equal(h["point"], d.point.cpu())
+    assert torch.equal(h["bary"], d.bary.cpu())
+
+
+def test_refit_moves_vertices(orc, cpq, cuda):
+    from gpurt_cpq import workloads as W
+
+    v, t = W.icosphere(4)
+    rng = np.random.default_rng(1)
+    m = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=4)
+    before = m.export_build()
+    v2 = (v * 1.3 + rng.normal(0, 0.02, v.shape)).astype(np.float32)
+    m.refit(dev(v2, cuda))
+    q = W.uniform_queries(30000, -2.5, 2.5, 3)
+    check_against_fp64(orc, v2, t, q, m.query(dev(q, cuda)))
+    after = m.export_build()
+    np.testing.assert_array_equal(before["order"], after["order"])
+    # every wide box still contains the triangles below it
+    w = m.export_wide()
+    K = 4
+    boxes = w["boxes"].reshape(-1, 6, K)
+    order = after["order"]
+    for node in range(0, boxes.shape[0], 7):
+        for s in range(K):
+            c = w["counts"][node * K + s]
+            if c > 0:
+                f = w["refs"][node * K + s]
+                pts = v2[t[order[f:f + c]]].reshape(-1, 3)
+                lo, hi = boxes[node, 0::2, s], boxes[node, 1::2, s]
+                assert np.all(pts >= lo) and np.all(pts <= hi)
