@@ -1,0 +1,391 @@
+#!/usr/bin/env python
+"""Closest-point queries/s on one GB300: the large heightfield workload.
+
+Workload (seeded, synthetic; no dataset involved): a 1024 x 1024-vertex
+heightfield over [0,1]^2 (2,093,058 triangles; z = 8 sinusoids, frequencies
+U[1,32], amplitude 0.05/f, + N(0,1e-3)), 16,777,216 queries (half within
+N(0, 0.01^2) of random surface points, half uniform in [-0.1,1.1]^2 x
+[-0.5,0.5]); 4-wide BVH, leaf size autotuned (cp_autotune, branching fixed).
+
+A step is one cp_query over all 16M queries with the inputs resident in HBM
+(Morton ordering of the queries + persistent traversal + exact re-evaluation
+of each winner).  `value` is queries/s over K timed steps (CUDA events on the
+launching stream).  `e2e` is the same metric through cp_query_host: pinned
+host queries in, closest point / distance / triangle out, copies included.
+
+Roofline (dominant kernel = the traversal): algorithmic bytes per query are
+B_io = 32 (query 12 + point 12 + distance 4 + index 4) plus
+B_trav = 32 V_node + 36 V_tri, with V_node / V_tri the mean binary-node visits
+and triangle tests of the canonical algorithm (binary Morton LBVH, leaf <= 4,
+closest-first), measured by the CPU restatement on a seeded 65,536-query
+sample of this workload.  t_roof = B_io / BW_HBM + B_trav / BW_L2 with BW_HBM
+from MEASURED_PEAKS.json and BW_L2 measured here; frac = t_roof / t_kernel.
+
+Multi-GPU: the path needs no exchange; each rank runs the same workload on its
+own GPU (replicas, weak scaling), barrier + max-over-ranks timing.
+
+--impl reference: the reference's closest-point code is not in its mounted
+tree (its FCPW-GPU branch is absent), so the reference arm times the CPU
+restatement of the same algorithm (the oracle port) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "gpu-rt_gb300"
+for p in (str(ROOT), str(PKG)):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+import numpy as np  # noqa: E402
+
+METRIC = "closest-point queries/s (large heightfield, 2.09M tris, 16M queries)"
+UNIT = "queries/s"
+N_QUERIES = 16 * (1 << 20)
+B_IO = 32.0
+# canonical visit counts (binary LBVH, leaf 4) of this seeded workload, from the
+# CPU restatement on the first 65,536 queries; re-measured in the CPU leg
+CANON_V_NODE = 114.635
+CANON_V_TRI = 61.954
+# dram bytes per traversal launch from the committed ncu capture (null until measured)
+NCU_TRAFFIC_PER_QUERY = None
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-sample", type=int, default=1 << 21,
+                    help="queries timed on the host cores for the CPU baseline")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--leaf", type=int, default=0)
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def host_cores() -> int:
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+
+
+def cpu_model() -> str:
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.lines: list[str] = []
+        self.proc = None
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[4:8]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text())
+    return {"hbm_gbs": 6800.0, "fallback": True}
+
+
+def measure_l2_gbs(torch, dev) -> float:
+    """Read bandwidth of a 48 MB L2-resident buffer (torch sum, best of 20)."""
+    x = torch.ones(12 * (1 << 20), dtype=torch.float32, device=dev)
+    for _ in range(3):
+        x.sum()
+    best = 0.0
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    for _ in range(20):
+        e0.record()
+        for _ in range(10):
+            x.sum()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / 10
+        best = max(best, x.numel() * 4 / (ms * 1e-3) / 1e9)
+    del x
+    return best
+
+
+def workload():
+    from gpurt_cpq import workloads as W
+
+    return W.large()
+
+
+def cpu_leg(v, t, q, sample: int) -> dict:
+    """CPU restatement (oracle port) on all host cores: canonical tree, bounded sample."""
+    from oracle import oracle as O
+
+    O.build()
+    threads = host_cores()
+    t0 = time.perf_counter()
+    tree = O.Tree(v, t, 2, 4, 0)
+    build_s = time.perf_counter() - t0
+    stat = tree.query(q[:65536], threads=threads, stats=True)
+    s = q[:sample]
+    r = tree.query(s, threads=threads)
+    return {"value": s.shape[0] / r["seconds"], "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"first {s.shape[0]} of the {q.shape[0]} queries, canonical binary LBVH "
+                      f"(leaf 4) built on the host in {build_s:.2f} s, {cpu_model()}",
+            "build_s": build_s,
+            "v_node": float(stat["node_visits"].mean()), "v_tri": float(stat["tri_tests"].mean())}
+
+
+def emit(obj):
+    print(json.dumps(obj), flush=True)
+
+
+def reference_arm(args):
+    rank, world, _ = dist_env()
+    if world > 1:
+        import torch.distributed as td
+
+        td.init_process_group("gloo")
+        td.barrier()
+        if rank != 0:
+            td.destroy_process_group()
+            return
+    from oracle import oracle as O
+
+    O.build()
+    v, t, q = workload()
+    threads = host_cores()
+    t0 = time.perf_counter()
+    tree = O.Tree(v, t, 2, 4, 0)
+    build_s = time.perf_counter() - t0
+    per_step = min(args.cpu_sample, q.shape[0])
+    for w in range(args.warmup):
+        tree.query(q[w * per_step % q.shape[0]:][:per_step], threads=threads)
+    secs = 0.0
+    done = 0
+    for k in range(args.steps):
+        off = (k * per_step) % (q.shape[0] - per_step + 1)
+        r = tree.query(q[off:off + per_step], threads=threads)
+        secs += r["seconds"]
+        done += per_step
+    value = done / secs
+    emit({"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+          "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+          "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+          "data": "synthetic (seeded heightfield + queries)",
+          "config": {"workload": "large heightfield: 1024x1024 vertices (2,093,058 tris), 16,777,216 "
+                                 "queries; each step a bounded sample", "sample_per_step": per_step},
+          "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                           "sample": f"{per_step} queries per step, canonical binary LBVH leaf 4 "
+                                     f"(built in {build_s:.2f} s), {cpu_model()}; the reference's "
+                                     "own closest-point code is absent from its tree"},
+          "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+    if world > 1:
+        import torch.distributed as td
+
+        td.destroy_process_group()
+
+
+def our_arm(args):
+    import torch
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as td
+
+        torch.cuda.set_device(local)
+        td.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    import gpurt_cpq as cpq
+    from gpurt_cpq._lib import lib
+
+    v, t, q = workload()
+    vd = torch.from_numpy(v).to(dev)
+    td_ = torch.from_numpy(t).to(dev)
+    qd = torch.from_numpy(q).to(dev)
+    nq = q.shape[0]
+
+    # 4-wide BVH, leaf size (and block / short stack) autotuned on a 1M-query sample
+    leaf, qopts = 4, cpq.query_opts()
+    tuned = None
+    if args.leaf:
+        leaf = args.leaf
+    elif not args.no_autotune:
+        bo, qo = cpq.autotune(vd, td_, qd[: 1 << 20].contiguous(), cache_path=None, branching=4)
+        leaf, qopts = bo.leaf_size, qo
+        tuned = {"leaf_size": bo.leaf_size, "block_size": qo.block_size, "short_stack": qo.short_stack}
+    mesh = cpq.Mesh(vd, td_, branching=4, leaf_size=leaf)
+    info = mesh.info()
+    ws = torch.empty(mesh.workspace_size(nq, qopts), dtype=torch.uint8, device=dev)
+    out = mesh.query(qd, workspace=ws, opts=qopts)
+    l2_gbs = measure_l2_gbs(torch, dev)
+    for _ in range(args.warmup):
+        mesh.query(qd, workspace=ws, opts=qopts, out=out)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    lib.cp_timing_enable(1)
+    from ctypes import byref, c_double, c_int64
+
+    tms, tl = c_double(), c_int64()
+    lib.cp_timing_read(byref(tms), byref(tl), 1)
+    launches0 = lib.cp_kernel_launches()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        mesh.query(qd, workspace=ws, opts=qopts, out=out)
+    e1.record()
+    torch.cuda.synchronize()
+    launches = lib.cp_kernel_launches() - launches0
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    lib.cp_timing_read(byref(tms), byref(tl), 1)
+    lib.cp_timing_enable(0)
+    trav_ms = tms.value / max(tl.value, 1)
+    if world > 1:
+        m = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(m, op=torch.distributed.ReduceOp.MAX)
+        ms = float(m.item())
+    value = world * nq * args.steps / (ms * 1e-3)
+    assert mesh.device_status() == 0
+
+    # end to end through the host entry point: pinned buffers, copies inside
+    qh = torch.from_numpy(q).pin_memory()
+    hout = {"dist": torch.empty(nq, dtype=torch.float32).pin_memory(),
+            "tri": torch.empty(nq, dtype=torch.int32).pin_memory(),
+            "point": torch.empty((nq, 3), dtype=torch.float32).pin_memory()}
+    e2e_steps = max(1, min(args.steps, 5))
+    mesh.query_host(qh, opts=qopts, out=hout)
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        mesh.query_host(qh, opts=qopts, out=hout)
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        m = torch.tensor([e2e_s], device=dev)
+        torch.distributed.all_reduce(m, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(m.item())
+    e2e = {"value": world * nq * e2e_steps / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": nq * 12, "d2h_bytes_per_step": nq * (12 + 4 + 4),
+           "steps": e2e_steps, "path": "cp_query_host, pinned host buffers"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_leg(v, t, q, min(args.cpu_sample, nq))
+    v_node = cpu["v_node"] if cpu else CANON_V_NODE
+    v_tri = cpu["v_tri"] if cpu else CANON_V_TRI
+    peaks = measured_peaks()
+    hbm = float(peaks["hbm_gbs"])
+    b_trav = 32.0 * v_node + 36.0 * v_tri
+    t_roof = B_IO / (hbm * 1e9) + b_trav / (l2_gbs * 1e9)          # s per query
+    t_kernel = trav_ms * 1e-3 / nq                                  # s per query
+    achieved = (B_IO + b_trav) / t_kernel / 1e9
+    peak_eff = (B_IO + b_trav) / t_roof / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak_eff, "unit": "GB/s",
+                "frac": achieved / peak_eff, "of": "measured",
+                "traffic": None if NCU_TRAFFIC_PER_QUERY is None else NCU_TRAFFIC_PER_QUERY * nq,
+                "kernel": "k_traverse", "kernel_ms_per_launch": trav_ms,
+                "model": "t_roof = B_io/BW_HBM + B_trav/BW_L2 (algorithmic bytes of the canonical "
+                         "binary LBVH); peak = (B_io + B_trav)/t_roof",
+                "bytes_per_query": {"io": B_IO, "trav": b_trav, "v_node": v_node, "v_tri": v_tri},
+                "hbm_gbs": hbm, "l2_gbs_measured": l2_gbs,
+                "hbm_only_frac": B_IO / t_kernel / 1e9 / hbm}
+    if rank == 0:
+        res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+               "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+               "data": "synthetic (seeded heightfield + queries, generated on the host)",
+               "config": {"workload": "large heightfield: 1024x1024 vertices (2,093,058 tris), "
+                                      "16,777,216 queries (50% near-surface sigma 0.01, 50% box)",
+                          "branching": 4, "leaf_size": leaf, "autotuned": tuned,
+                          "block_size": qopts.block_size, "short_stack": qopts.short_stack,
+                          "sort_queries": bool(qopts.sort_queries),
+                          "wide_nodes": info.num_wide_nodes, "build_ms": info.build_ms,
+                          "l2": "inputs larger than L2 (201 MB queries + 335 MB outputs + 151 MB "
+                                "BVH per step); no flush",
+                          "parallelism": f"replicas x{world}"},
+               "e2e": e2e, "roofline": roofline, "gpu_launches": int(launches),
+               "clocks": clk}
+        if cpu is not None:
+            res["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        emit(res)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        our_arm(args)
+
+
+if __name__ == "__main__":
+    main()

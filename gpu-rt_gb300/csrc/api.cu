@@ -8,6 +8,7 @@
 // nothing synchronously and stays on its stream.
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -21,6 +22,11 @@
 
 using namespace cpq;
 
+namespace cpq {
+static std::atomic<uint64_t> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+}  // namespace cpq
+
 struct cp_mesh {
     Bvh bvh;
 };
@@ -32,6 +38,7 @@ struct cp_batch {
     // CUDA-graph cache of the last captured query launch sequence
     cudaGraphExec_t exec = nullptr;
     std::vector<uintptr_t> graph_key;
+    cudaStream_t capture_stream = nullptr;
 };
 
 namespace {
@@ -206,6 +213,18 @@ CP_API const char* cp_status_string(cp_status s) {
 }
 
 CP_API int32_t cp_version(void) { return 100; }
+
+CP_API uint64_t cp_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
+
+CP_API cp_status cp_timing_enable(int32_t on) {
+    timing_enable(on != 0);
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_timing_read(double* traverse_ms, int64_t* launches, int32_t reset) {
+    CP_CUDA(timing_read(traverse_ms, launches, reset != 0), "timing read");
+    return CP_SUCCESS;
+}
 
 CP_API int32_t cp_size_class(int64_t nt) {
     int32_t c = 0;
@@ -406,8 +425,8 @@ CP_API cp_status cp_backward(const cp_mesh* m, const float* queries, const int32
     if (!m) return fail(CP_ERROR_INVALID_VALUE, "mesh is NULL");
     if (nq < 0) return fail(CP_ERROR_INVALID_VALUE, "negative query count");
     if (nq == 0) return CP_SUCCESS;
-    if (!queries || !tri || !bary || !grad_dist)
-        return fail(CP_ERROR_INVALID_VALUE, "queries, tri, bary and grad_dist are required");
+    if (!queries || !tri || !grad_dist)
+        return fail(CP_ERROR_INVALID_VALUE, "queries, tri and grad_dist are required");
     CP_CUDA(bvh_backward(m->bvh, queries, tri, bary, grad_dist, nq, grad_queries, grad_verts,
                          reinterpret_cast<cudaStream_t>(stream)),
             "backward");
@@ -454,6 +473,7 @@ CP_API cp_status cp_batch_create(const float* verts, const int64_t* vert_offsets
 CP_API cp_status cp_batch_destroy(cp_batch* bt) {
     if (!bt) return CP_SUCCESS;
     if (bt->exec) cudaGraphExecDestroy(bt->exec);
+    if (bt->capture_stream) cudaStreamDestroy(bt->capture_stream);
     if (bt->d_qoff) cudaFree(bt->d_qoff);
     bvh_free(bt->bvh);
     delete bt;
@@ -522,11 +542,17 @@ CP_API cp_status cp_batch_query(cp_batch* bt, const float* queries, const int64_
             cudaGraphExecDestroy(bt->exec);
             bt->exec = nullptr;
         }
-        CP_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed), "graph capture");
+        // Capture on a private stream: the caller's stream may be the legacy
+        // default stream, which cannot be captured.  Captured work does not
+        // run, so the private stream needs no ordering with the caller's.
+        if (!bt->capture_stream)
+            CP_CUDA(cudaStreamCreateWithFlags(&bt->capture_stream, cudaStreamNonBlocking), "graph capture");
+        cudaStream_t cs = bt->capture_stream;
+        CP_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "graph capture");
         cudaError_t e = bvh_query(bt->bvh, queries, nq, bt->d_qoff, qp, out_point, out_dist, out_tri,
-                                  out_bary, workspace, ws_bytes, st);
+                                  out_bary, workspace, ws_bytes, cs);
         cudaGraph_t graph = nullptr;
-        cudaError_t e2 = cudaStreamEndCapture(st, &graph);
+        cudaError_t e2 = cudaStreamEndCapture(cs, &graph);
         if (e != cudaSuccess) {
             if (graph) cudaGraphDestroy(graph);
             return cuda_fail(e, "graph capture");

@@ -52,11 +52,14 @@ extern "C" CP_API cp_status cp_autotune(const float* verts, int64_t nv, const in
     if (!verts || !tris || !queries || !best_build || !best_query || nv <= 0 || nt <= 0 || nq <= 0)
         return CP_ERROR_INVALID_VALUE;
     const int cls = cp_size_class(nt);
+    // a branching already set on entry (2, 4 or 8) restricts the search to it
+    const int fixed_K = (best_build->branching == 2 || best_build->branching == 4 ||
+                         best_build->branching == 8) ? best_build->branching : 0;
     std::vector<Entry> cache = read_cache(cache_path);
     cp_build_opts_default(best_build);
     cp_query_opts_default(best_query);
     for (const Entry& e : cache)
-        if (e.cls == cls) {
+        if (e.cls == cls && (fixed_K == 0 || e.K == fixed_K)) {
             best_build->branching = e.K;
             best_build->leaf_size = e.leaf;
             best_query->block_size = e.block;
@@ -82,6 +85,7 @@ extern "C" CP_API cp_status cp_autotune(const float* verts, int64_t nv, const in
     const int stacks[3] = {4, 8, 16};
     for (int ki = 0; ki < 3 && result == CP_SUCCESS; ++ki)
         for (int li = 0; li < 4 && result == CP_SUCCESS; ++li) {
+            if (fixed_K && Ks[ki] != fixed_K) continue;
             cp_build_opts bo;
             cp_build_opts_default(&bo);
             bo.branching = Ks[ki];
@@ -137,7 +141,7 @@ extern "C" CP_API cp_status cp_autotune(const float* verts, int64_t nv, const in
     if (cache_path) {
         std::vector<Entry> out;
         for (const Entry& e : cache)
-            if (e.cls != cls) out.push_back(e);
+            if (e.cls != cls || e.K != best.K) out.push_back(e);
         out.push_back(best);
         write_cache(cache_path, out);
     }

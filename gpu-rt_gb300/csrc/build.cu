@@ -620,7 +620,7 @@ cudaError_t bvh_build(Bvh& b, const float* verts, int64_t vstride, const int32_t
 
     // validate indices and coordinates before any kernel reads a vertex by index
     k_validate<<<grid_for(n), kThreads, 0, st>>>(verts, vstride, b.tris, n, b.d_voff, b.d_toff, nm,
-                                                scratch);
+                                                scratch); note_launch();
     CK(cudaGetLastError());
     uint32_t h_scr[16];
     CK(cudaMemcpyAsync(h_scr, scratch, sizeof(h_scr), cudaMemcpyDeviceToHost, st));
@@ -630,15 +630,15 @@ cudaError_t bvh_build(Bvh& b, const float* verts, int64_t vstride, const int32_t
         if (why) *why = (h_scr[0] & 2u) ? "triangle index out of range" : "non-finite vertex coordinate";
         return cudaSuccess;
     }
-    k_init_boxes<<<grid_for(6 * nm), kThreads, 0, st>>>(mbox, 6 * nm);
+    k_init_boxes<<<grid_for(6 * nm), kThreads, 0, st>>>(mbox, 6 * nm); note_launch();
     k_centroid_bounds<<<grid_for(n), kThreads, 0, st>>>(verts, vstride, b.tris, n, b.d_voff,
-                                                       b.d_toff, nm, csum, mbox);
+                                                       b.d_toff, nm, csum, mbox); note_launch();
     CK(cudaGetLastError());
-    k_build_frames<<<grid_for(nm), kThreads, 0, st>>>(mbox, nm, (float)(1u << bits), lo_scale);
-    k_morton<<<grid_for(n), kThreads, 0, st>>>(csum, n, b.d_toff, nm, lo_scale, bits, b.keys, vals);
+    k_build_frames<<<grid_for(nm), kThreads, 0, st>>>(mbox, nm, (float)(1u << bits), lo_scale); note_launch();
+    k_morton<<<grid_for(n), kThreads, 0, st>>>(csum, n, b.d_toff, nm, lo_scale, bits, b.keys, vals); note_launch();
     CK(cudaGetLastError());
     // sort only the digits whose bits vary
-    k_key_and_or<<<256, kThreads, 0, st>>>(b.keys, n, reinterpret_cast<unsigned long long*>(scratch + 4));
+    k_key_and_or<<<256, kThreads, 0, st>>>(b.keys, n, reinterpret_cast<unsigned long long*>(scratch + 4)); note_launch();
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(h_scr, scratch, sizeof(h_scr), cudaMemcpyDeviceToHost, st));
     CK(cudaStreamSynchronize(st));
@@ -662,25 +662,25 @@ cudaError_t bvh_build(Bvh& b, const float* verts, int64_t vstride, const int32_t
         CK(cudaMemcpyAsync(b.order, vals, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, st));
     }
 
-    k_leaf_init<<<grid_for(n), kThreads, 0, st>>>(n, b.first, b.last, b.parent);
+    k_leaf_init<<<grid_for(n), kThreads, 0, st>>>(n, b.first, b.last, b.parent); note_launch();
     CK(cudaGetLastError());
     if (n > 1) {
         k_karras<<<grid_for(n - 1), kThreads, 0, st>>>(b.keys, n, bits, nm, b.d_toff, b.left,
                                                        b.right, b.parent, b.first, b.last,
-                                                       b.mesh_root);
+                                                       b.mesh_root); note_launch();
         CK(cudaGetLastError());
     }
-    k_single_tri_roots<<<grid_for(nm), kThreads, 0, st>>>(b.d_toff, nm, n, b.mesh_root);
+    k_single_tri_roots<<<grid_for(nm), kThreads, 0, st>>>(b.d_toff, nm, n, b.mesh_root); note_launch();
     CK(cudaMemsetAsync(b.arrive, 0, sizeof(uint32_t) * nn, st));
     k_refit<true><<<grid_for(n), kThreads, 0, st>>>(
         verts, vstride, b.tris, b.order, b.keys, n, b.d_voff, b.d_toff, nm, key_shift, b.left,
         b.right, b.parent, b.first, b.last, b.box, b.cost, b.leaf_flag, b.arrive, b.recs,
-        b.inv_order, p.leaf_size, p.collapse, p.c_node, p.c_tri);
+        b.inv_order, p.leaf_size, p.collapse, p.c_node, p.c_tri); note_launch();
     CK(cudaGetLastError());
     int32_t* max_depth = reinterpret_cast<int32_t*>(scratch + 1);
     k_wide_flags<<<grid_for(nn), kThreads, 0, st>>>(n, b.keys, nm, key_shift, b.parent, b.first,
                                                    b.last, b.leaf_flag, b.mesh_root, k_levels,
-                                                   b.cluster, wide_id, max_depth);
+                                                   b.cluster, wide_id, max_depth); note_launch();
     CK(cudaGetLastError());
     uint32_t* wide_flag;
     CK(tmp.get(&wide_flag, (size_t)nn));
@@ -707,25 +707,25 @@ cudaError_t bvh_build(Bvh& b, const float* verts, int64_t vstride, const int32_t
             k_wide_emit<2><<<grid_for(nn), kThreads, 0, st>>>(
                 n, k_levels, wide_flag, wide_id, b.keys, nm, key_shift, b.left, b.right, b.first,
                 b.last, b.box, b.cluster, b.mesh_root, static_cast<WideNode<2>*>(b.nodes),
-                b.wide_src, b.slot_src, b.wide_root, scratch + 3);
+                b.wide_src, b.slot_src, b.wide_root, scratch + 3); note_launch();
             break;
         case 4:
             k_wide_emit<4><<<grid_for(nn), kThreads, 0, st>>>(
                 n, k_levels, wide_flag, wide_id, b.keys, nm, key_shift, b.left, b.right, b.first,
                 b.last, b.box, b.cluster, b.mesh_root, static_cast<WideNode<4>*>(b.nodes),
-                b.wide_src, b.slot_src, b.wide_root, scratch + 3);
+                b.wide_src, b.slot_src, b.wide_root, scratch + 3); note_launch();
             break;
         default:
             k_wide_emit<8><<<grid_for(nn), kThreads, 0, st>>>(
                 n, k_levels, wide_flag, wide_id, b.keys, nm, key_shift, b.left, b.right, b.first,
                 b.last, b.box, b.cluster, b.mesh_root, static_cast<WideNode<8>*>(b.nodes),
-                b.wide_src, b.slot_src, b.wide_root, scratch + 3);
+                b.wide_src, b.slot_src, b.wide_root, scratch + 3); note_launch();
             break;
     }
     CK(cudaGetLastError());
     const int qbits = (64 - b.mesh_bits) / 3 < 10 ? (64 - b.mesh_bits) / 3 : 10;
     k_query_frames<<<grid_for(nm), kThreads, 0, st>>>(b.box, b.mesh_root, nm, (float)(1u << qbits),
-                                                     b.frame);
+                                                     b.frame); note_launch();
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(h_scr, scratch, sizeof(h_scr), cudaMemcpyDeviceToHost, st));
     CK(cudaEventRecord(ev1, st));
@@ -744,27 +744,27 @@ cudaError_t bvh_refit(Bvh& b, const float* verts, int64_t vstride, cudaStream_t 
     k_refit<false><<<grid_for(n), kThreads, 0, st>>>(
         verts, vstride, b.tris, b.order, b.keys, n, b.d_voff, b.d_toff, b.nmeshes, key_shift,
         b.left, b.right, b.parent, b.first, b.last, b.box, b.cost, b.leaf_flag, b.arrive, b.recs,
-        b.inv_order, b.p.leaf_size, b.p.collapse, b.p.c_node, b.p.c_tri);
+        b.inv_order, b.p.leaf_size, b.p.collapse, b.p.c_node, b.p.c_tri); note_launch();
     CK(cudaGetLastError());
     const int64_t slots = b.num_wide * b.p.K;
     switch (b.p.K) {
         case 2:
             k_wide_boxes<2><<<grid_for(slots), kThreads, 0, st>>>(b.num_wide, b.slot_src, b.box,
-                                                                 static_cast<WideNode<2>*>(b.nodes));
+                                                                 static_cast<WideNode<2>*>(b.nodes)); note_launch();
             break;
         case 4:
             k_wide_boxes<4><<<grid_for(slots), kThreads, 0, st>>>(b.num_wide, b.slot_src, b.box,
-                                                                 static_cast<WideNode<4>*>(b.nodes));
+                                                                 static_cast<WideNode<4>*>(b.nodes)); note_launch();
             break;
         default:
             k_wide_boxes<8><<<grid_for(slots), kThreads, 0, st>>>(b.num_wide, b.slot_src, b.box,
-                                                                 static_cast<WideNode<8>*>(b.nodes));
+                                                                 static_cast<WideNode<8>*>(b.nodes)); note_launch();
             break;
     }
     CK(cudaGetLastError());
     const int qbits = (64 - b.mesh_bits) / 3 < 10 ? (64 - b.mesh_bits) / 3 : 10;
     k_query_frames<<<grid_for(b.nmeshes), kThreads, 0, st>>>(b.box, b.mesh_root, b.nmeshes,
-                                                            (float)(1u << qbits), b.frame);
+                                                            (float)(1u << qbits), b.frame); note_launch();
     return cudaGetLastError();
 }
 

@@ -25,6 +25,9 @@ constexpr int64_t kMaxTriangles = (int64_t(1) << 27) - 1;  // first must fit in 
 
 constexpr uint32_t kTriDegenerate = 1u;   // TriRec flags: zero-area triangle
 
+// Host side: count one kernel launch of this library (cp_kernel_launches).
+void note_launch();
+
 template <int K>
 struct alignas(16) WideNode {
     float lox[K], hix[K], loy[K], hiy[K], loz[K], hiz[K];

@@ -16,6 +16,9 @@
 // Node rows and triangle records are read with 128-bit read-only loads.
 #include <cfloat>
 #include <climits>
+#include <mutex>
+#include <utility>
+#include <vector>
 
 #include "bvh.cuh"
 #include "sort.cuh"
@@ -196,60 +199,77 @@ __device__ void degenerate_bary(float qx, float qy, float qz, const TriRec& r, f
     }
 }
 
-// Final answer for the winning triangle in float-float arithmetic: the same
-// region logic as tri_d2 on exact differences, then |q - p| to ~2^-44.
-__device__ void precise_closest(float qx, float qy, float qz, const TriRec& r, float& dist,
-                                float& px, float& py, float& pz, float& ov, float& ow) {
-    const ff3 A = ff3_from(r.p0.x, r.p0.y, r.p0.z);
-    const ff3 B = ff3_from(r.p0.w, r.p1.x, r.p1.y);
-    const ff3 C = ff3_from(r.p1.z, r.p1.w, r.p2.x);
-    const ff3 Q = ff3_from(qx, qy, qz);
-    const ff3 ab = ff3_sub(B, A), ac = ff3_sub(C, A), ap = ff3_sub(Q, A);
-    ff v = ff_from(0.0f), w = ff_from(0.0f);
+// Barycentric weights (of b and c) of the closest point on the triangle, by
+// the region logic of tri_d2 evaluated in float-float on exact differences.
+__device__ void precise_bary(float qx, float qy, float qz, const TriRec& r, ff& v, ff& w) {
+    v = ff_from(0.0f);
+    w = ff_from(0.0f);
     if (__float_as_uint(r.p2.z) & kTriDegenerate) {
         float fv, fw;
         degenerate_bary(qx, qy, qz, r, fv, fw);
         v = ff_from(fv);
         w = ff_from(fw);
-    } else {
-        const ff d1 = ff3_dot(ab, ap), d2 = ff3_dot(ac, ap);
-        if (ff_le0(d1) && ff_le0(d2)) {
-            // vertex a
-        } else {
-            const ff3 bp = ff3_sub(Q, B), cp = ff3_sub(Q, C);
-            const ff d3 = ff3_dot(ab, bp), d4 = ff3_dot(ac, bp);
-            const ff d5 = ff3_dot(ab, cp), d6 = ff3_dot(ac, cp);
-            const ff vc = ff_sub(ff_mul(d1, d4), ff_mul(d3, d2));
-            const ff vb = ff_sub(ff_mul(d5, d2), ff_mul(d1, d6));
-            const ff va = ff_sub(ff_mul(d3, d6), ff_mul(d5, d4));
-            const ff d43 = ff_sub(d4, d3), d56 = ff_sub(d5, d6);
-            if (ff_ge0(d3) && ff_le(d4, d3)) {
-                v = ff_from(1.0f);
-            } else if (ff_le0(vc) && ff_ge0(d1) && ff_le0(d3)) {
-                v = ff_div(d1, ff_sub(d1, d3));
-            } else if (ff_ge0(d6) && ff_le(d5, d6)) {
-                w = ff_from(1.0f);
-            } else if (ff_le0(vb) && ff_ge0(d2) && ff_le0(d6)) {
-                w = ff_div(d2, ff_sub(d2, d6));
-            } else if (ff_le0(va) && ff_ge0(d43) && ff_ge0(d56)) {
-                w = ff_div(d43, ff_add(d43, d56));
-                v = ff_sub(ff_from(1.0f), w);
-            } else {
-                const ff den = ff_add(ff_add(va, vb), vc);
-                v = ff_div(vb, den);
-                w = ff_div(vc, den);
-            }
-        }
+        return;
     }
-    // r = ap - v ab - w ac; p = a + v ab + w ac
-    const ff3 off = {ff_add(ff_mul(v, ab.x), ff_mul(w, ac.x)), ff_add(ff_mul(v, ab.y), ff_mul(w, ac.y)),
-                     ff_add(ff_mul(v, ab.z), ff_mul(w, ac.z))};
-    const ff3 rr = ff3_sub(ap, off);
-    const ff d2 = ff3_dot(rr, rr);
-    dist = ff_to_float(ff_sqrt(d2));
-    px = ff_to_float(ff_add(A.x, off.x));
-    py = ff_to_float(ff_add(A.y, off.y));
-    pz = ff_to_float(ff_add(A.z, off.z));
+    const ff3 A = ff3_from(r.p0.x, r.p0.y, r.p0.z);
+    const ff3 B = ff3_from(r.p0.w, r.p1.x, r.p1.y);
+    const ff3 C = ff3_from(r.p1.z, r.p1.w, r.p2.x);
+    const ff3 Q = ff3_from(qx, qy, qz);
+    const ff3 ab = ff3_sub(B, A), ac = ff3_sub(C, A), ap = ff3_sub(Q, A);
+    const ff d1 = ff3_dot(ab, ap), d2 = ff3_dot(ac, ap);
+    if (ff_le0(d1) && ff_le0(d2)) return;  // vertex a
+    const ff3 bp = ff3_sub(Q, B), cp = ff3_sub(Q, C);
+    const ff d3 = ff3_dot(ab, bp), d4 = ff3_dot(ac, bp);
+    const ff d5 = ff3_dot(ab, cp), d6 = ff3_dot(ac, cp);
+    const ff vc = ff_sub(ff_mul(d1, d4), ff_mul(d3, d2));
+    const ff vb = ff_sub(ff_mul(d5, d2), ff_mul(d1, d6));
+    const ff va = ff_sub(ff_mul(d3, d6), ff_mul(d5, d4));
+    const ff d43 = ff_sub(d4, d3), d56 = ff_sub(d5, d6);
+    if (ff_ge0(d3) && ff_le(d4, d3)) {
+        v = ff_from(1.0f);
+    } else if (ff_le0(vc) && ff_ge0(d1) && ff_le0(d3)) {
+        v = ff_div(d1, ff_sub(d1, d3));
+    } else if (ff_ge0(d6) && ff_le(d5, d6)) {
+        w = ff_from(1.0f);
+    } else if (ff_le0(vb) && ff_ge0(d2) && ff_le0(d6)) {
+        w = ff_div(d2, ff_sub(d2, d6));
+    } else if (ff_le0(va) && ff_ge0(d43) && ff_ge0(d56)) {
+        w = ff_div(d43, ff_add(d43, d56));
+        v = ff_sub(ff_from(1.0f), w);
+    } else {
+        const ff den = ff_add(ff_add(va, vb), vc);
+        v = ff_div(vb, den);
+        w = ff_div(vc, den);
+    }
+}
+
+// Residual q - p and offset p - a for p = a + v (b - a) + w (c - a), in
+// float-float: the differences of FP32 inputs are exact, so the residual of a
+// query very close to the surface keeps its relative accuracy.
+__device__ __forceinline__ void precise_residual(float qx, float qy, float qz, const TriRec& r,
+                                                 ff v, ff w, ff3& res, ff3& off) {
+    const ff3 A = ff3_from(r.p0.x, r.p0.y, r.p0.z);
+    const ff3 B = ff3_from(r.p0.w, r.p1.x, r.p1.y);
+    const ff3 C = ff3_from(r.p1.z, r.p1.w, r.p2.x);
+    const ff3 Q = ff3_from(qx, qy, qz);
+    const ff3 ab = ff3_sub(B, A), ac = ff3_sub(C, A), ap = ff3_sub(Q, A);
+    off = {ff_add(ff_mul(v, ab.x), ff_mul(w, ac.x)), ff_add(ff_mul(v, ab.y), ff_mul(w, ac.y)),
+           ff_add(ff_mul(v, ab.z), ff_mul(w, ac.z))};
+    res = ff3_sub(ap, off);
+}
+
+// Final answer for the winning triangle: distance to ~2^-44 relative, the
+// closest point and its barycentric weights rounded once to FP32.
+__device__ void precise_closest(float qx, float qy, float qz, const TriRec& r, float& dist,
+                                float& px, float& py, float& pz, float& ov, float& ow) {
+    ff v, w;
+    precise_bary(qx, qy, qz, r, v, w);
+    ff3 res, off;
+    precise_residual(qx, qy, qz, r, v, w, res, off);
+    dist = ff_to_float(ff_sqrt(ff3_dot(res, res)));
+    px = ff_to_float(ff_add(ff_from(r.p0.x), off.x));
+    py = ff_to_float(ff_add(ff_from(r.p0.y), off.y));
+    pz = ff_to_float(ff_add(ff_from(r.p0.z), off.z));
     ov = ff_to_float(v);
     ow = ff_to_float(w);
 }
@@ -465,19 +485,28 @@ __global__ void __launch_bounds__(256) k_backward(const TriRec* __restrict__ rec
         }
         if (t >= 0) {
             const float4* rp = reinterpret_cast<const float4*>(recs + inv_order[t]);
-            const float4 p0 = __ldg(rp), p1 = __ldg(rp + 1), p2 = __ldg(rp + 2);
-            v = bary[2 * i];
-            w = bary[2 * i + 1];
-            u = 1.0f - v - w;
-            const float px = p0.x + v * (p0.w - p0.x) + w * (p1.z - p0.x);
-            const float py = p0.y + v * (p1.x - p0.y) + w * (p1.w - p0.y);
-            const float pz = p0.z + v * (p1.y - p0.z) + w * (p2.x - p0.z);
-            const float rx = q[3 * i] - px, ry = q[3 * i + 1] - py, rz = q[3 * i + 2] - pz;
-            const float d = sqrtf(rx * rx + ry * ry + rz * rz);
+            TriRec r;
+            r.p0 = __ldg(rp);
+            r.p1 = __ldg(rp + 1);
+            r.p2 = __ldg(rp + 2);
+            const float qx = q[3 * i], qy = q[3 * i + 1], qz = q[3 * i + 2];
+            ff fv, fw;
+            if (bary) {
+                fv = ff_from(bary[2 * i]);
+                fw = ff_from(bary[2 * i + 1]);
+            } else {
+                precise_bary(qx, qy, qz, r, fv, fw);
+            }
+            ff3 res, off;
+            precise_residual(qx, qy, qz, r, fv, fw, res, off);
+            const float d = ff_to_float(ff_sqrt(ff3_dot(res, res)));
+            v = ff_to_float(fv);
+            w = ff_to_float(fw);
+            u = ff_to_float(ff_sub(ff_sub(ff_from(1.0f), fv), fw));
             const float s = d > 0.0f ? grad[i] / d : 0.0f;
-            gx = s * rx;
-            gy = s * ry;
-            gz = s * rz;
+            gx = s * ff_to_float(res.x);
+            gy = s * ff_to_float(res.y);
+            gz = s * ff_to_float(res.z);
         }
         if (grad_q) {
             grad_q[3 * i] = gx;
@@ -522,6 +551,16 @@ QueryLayout layout(int64_t nq, bool sort) {
     return L;
 }
 
+// Opt-in CUDA-event timing of every traversal launch (cp_timing_*).
+struct TraverseTiming {
+    std::mutex mu;
+    bool on = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+    double ms = 0.0;
+    int64_t launches = 0;
+};
+TraverseTiming g_timing;
+
 template <int K, int S>
 cudaError_t launch_traverse(const TraverseArgs& args, int block, int blocks_per_sm, cudaStream_t st) {
     const size_t smem = (size_t)S * block * sizeof(float2);
@@ -539,8 +578,29 @@ cudaError_t launch_traverse(const TraverseArgs& args, int block, int blocks_per_
     int64_t grid = (int64_t)sms * blocks_per_sm;
     const int64_t need = (args.nq + 31) / 32 * 32 / block + 1;
     if (grid > need) grid = need;
-    kern<<<(unsigned)grid, block, smem, st>>>(args);
-    return cudaGetLastError();
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    bool timed = false;
+    {
+        std::lock_guard<std::mutex> lock(g_timing.mu);
+        timed = g_timing.on;
+    }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(st, &cap);
+    if (timed && cap == cudaStreamCaptureStatusNone) {
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, st);
+    } else {
+        timed = false;
+    }
+    kern<<<(unsigned)grid, block, smem, st>>>(args); note_launch();
+    e = cudaGetLastError();
+    if (timed) {
+        cudaEventRecord(e1, st);
+        std::lock_guard<std::mutex> lock(g_timing.mu);
+        g_timing.pending.emplace_back(e0, e1);
+    }
+    return e;
 }
 
 template <int K>
@@ -553,6 +613,34 @@ cudaError_t launch_k(const TraverseArgs& args, const QueryParams& qp, cudaStream
 }
 
 }  // namespace
+
+void timing_enable(bool on) {
+    std::lock_guard<std::mutex> lock(g_timing.mu);
+    g_timing.on = on;
+}
+
+cudaError_t timing_read(double* ms, int64_t* launches, bool reset) {
+    std::lock_guard<std::mutex> lock(g_timing.mu);
+    cudaError_t err = cudaSuccess;
+    for (auto& pr : g_timing.pending) {
+        float t = 0.0f;
+        cudaError_t e = cudaEventSynchronize(pr.second);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&t, pr.first, pr.second);
+        if (e != cudaSuccess) err = e;
+        g_timing.ms += t;
+        g_timing.launches += 1;
+        cudaEventDestroy(pr.first);
+        cudaEventDestroy(pr.second);
+    }
+    g_timing.pending.clear();
+    if (ms) *ms = g_timing.ms;
+    if (launches) *launches = g_timing.launches;
+    if (reset) {
+        g_timing.ms = 0.0;
+        g_timing.launches = 0;
+    }
+    return err;
+}
 
 size_t query_workspace_bytes(const Bvh& b, int64_t nq, const QueryParams& qp) {
     (void)b;
@@ -577,7 +665,7 @@ cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int6
         int32_t* vals_alt = reinterpret_cast<int32_t*>(w + L.vals_alt);
         const int qbits = (64 - b.mesh_bits) / 3 < 10 ? (64 - b.mesh_bits) / 3 : 10;
         k_query_keys<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(queries, nq, d_qoff, b.nmeshes,
-                                                                   b.frame, qbits, keys, vals);
+                                                                   b.frame, qbits, keys, vals); note_launch();
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         bool in_alt = false;
@@ -614,7 +702,7 @@ cudaError_t bvh_backward(const Bvh& b, const float* queries, const int32_t* tri,
     if (nq <= 0) return cudaSuccess;
     k_backward<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(b.recs, b.inv_order, b.tris, b.nt,
                                                              queries, tri, bary, grad_dist, nq,
-                                                             grad_q, grad_verts, b.status);
+                                                             grad_q, grad_verts, b.status); note_launch();
     return cudaGetLastError();
 }
 

@@ -245,16 +245,16 @@ size_t scan_workspace_bytes(int64_t m) {
 static cudaError_t scan_rec(uint32_t* data, int64_t m, unsigned char* ws, cudaStream_t st) {
     int64_t chunks = ceil_div(m, kScanChunk);
     if (chunks <= 1) {
-        k_scan_chunk<<<1, kScanThreads, 0, st>>>(data, m, nullptr);
+        k_scan_chunk<<<1, kScanThreads, 0, st>>>(data, m, nullptr); note_launch();
         return cudaGetLastError();
     }
     uint32_t* sums = reinterpret_cast<uint32_t*>(ws);
-    k_scan_chunk<<<(unsigned)chunks, kScanThreads, 0, st>>>(data, m, sums);
+    k_scan_chunk<<<(unsigned)chunks, kScanThreads, 0, st>>>(data, m, sums); note_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     e = scan_rec(sums, chunks, ws + align256((size_t)chunks * sizeof(uint32_t)), st);
     if (e != cudaSuccess) return e;
-    k_scan_add<<<(unsigned)ceil_div(m, 256), 256, 0, st>>>(data, m, sums);
+    k_scan_add<<<(unsigned)ceil_div(m, 256), 256, 0, st>>>(data, m, sums); note_launch();
     return cudaGetLastError();
 }
 
@@ -268,12 +268,12 @@ cudaError_t exclusive_scan_u32(uint32_t* data, int64_t m, uint32_t* total, void*
     unsigned char* ws = static_cast<unsigned char*>(workspace);
     uint32_t* last = reinterpret_cast<uint32_t*>(ws);
     if (total) {
-        k_save_last<<<1, 1, 0, stream>>>(data, m, last);
+        k_save_last<<<1, 1, 0, stream>>>(data, m, last); note_launch();
     }
     cudaError_t e = scan_rec(data, m, ws + 256, stream);
     if (e != cudaSuccess) return e;
     if (total) {
-        k_scan_total<<<1, 1, 0, stream>>>(data, last, m, total);
+        k_scan_total<<<1, 1, 0, stream>>>(data, last, m, total); note_launch();
         e = cudaGetLastError();
     }
     return e;
@@ -310,12 +310,12 @@ cudaError_t radix_sort_pairs(KeyT* keys, int32_t* vals, KeyT* keys_alt, int32_t*
     int32_t *vi = vals, *vo = vals_alt;
     bool alt = false;
     for (int shift = begin_bit; shift < end_bit; shift += 8) {
-        k_digit_hist<KeyT><<<tiles, kSortThreads, 0, stream>>>(ki, n, shift, counts, tiles);
+        k_digit_hist<KeyT><<<tiles, kSortThreads, 0, stream>>>(ki, n, shift, counts, tiles); note_launch();
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         e = exclusive_scan_u32(counts, m, nullptr, scan_ws, scan_bytes, stream);
         if (e != cudaSuccess) return e;
-        k_scatter<KeyT><<<tiles, kSortThreads, smem, stream>>>(ki, vi, ko, vo, n, shift, counts, tiles);
+        k_scatter<KeyT><<<tiles, kSortThreads, smem, stream>>>(ki, vi, ko, vo, n, shift, counts, tiles); note_launch();
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         std::swap(ki, ko);

@@ -9,6 +9,9 @@
 
 namespace cpq {
 
+// Host side: count one kernel launch of this library (defined in api.cu).
+void note_launch();
+
 // Bytes of workspace radix_sort_pairs needs for n keys.
 size_t radix_sort_workspace_bytes(int64_t n);
 

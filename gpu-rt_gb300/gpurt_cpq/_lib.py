@@ -8,7 +8,7 @@ path in its place.
 from __future__ import annotations
 
 import ctypes
-from ctypes import (POINTER, Structure, c_char_p, c_float, c_int32, c_int64, c_size_t, c_uint8,
+from ctypes import (POINTER, Structure, c_char_p, c_double, c_float, c_int32, c_int64, c_size_t,
                     c_uint32, c_uint64, c_void_p)
 from pathlib import Path
 
@@ -55,6 +55,9 @@ SIGNATURES = {
     "cp_last_error_string": (c_char_p, []),
     "cp_status_string": (c_char_p, [c_int32]),
     "cp_version": (c_int32, []),
+    "cp_kernel_launches": (c_uint64, []),
+    "cp_timing_enable": (c_int32, [c_int32]),
+    "cp_timing_read": (c_int32, [POINTER(c_double), POINTER(c_int64), c_int32]),
     "cp_mesh_create": (c_int32, [c_void_p, c_int64, c_int64, c_void_p, c_int64, POINTER(BuildOpts),
                                  c_void_p, POINTER(c_void_p)]),
     "cp_mesh_refit": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p]),

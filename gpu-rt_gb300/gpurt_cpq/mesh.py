@@ -179,16 +179,18 @@ class Mesh:
         check(lib.cp_mesh_refit(self._h, _ptr(verts), verts.stride(0) * 4, _stream(stream)),
               "cp_mesh_refit")
 
-    def backward(self, points: torch.Tensor, tri: torch.Tensor, bary: torch.Tensor,
+    def backward(self, points: torch.Tensor, tri: torch.Tensor, bary: torch.Tensor | None,
                  grad_dist: torch.Tensor, *, need_points: bool = True, need_verts: bool = True,
                  grad_verts: torch.Tensor | None = None, stream=None):
+        """Adjoint (cp_backward).  bary=None recomputes the exact barycentrics."""
         _check_dev(points, "points", torch.float32, 3)
         n = int(points.shape[0])
         grad_dist = grad_dist.contiguous().to(torch.float32)
         gq = torch.empty((n, 3), dtype=torch.float32, device=points.device) if need_points else None
         if need_verts and grad_verts is None:
             grad_verts = torch.zeros((self.num_vertices, 3), dtype=torch.float32, device=points.device)
-        check(lib.cp_backward(self._h, _ptr(points), _ptr(tri.contiguous()), _ptr(bary.contiguous()),
+        bary = bary.contiguous() if bary is not None else None
+        check(lib.cp_backward(self._h, _ptr(points), _ptr(tri.contiguous()), _ptr(bary),
                               _ptr(grad_dist), n, _ptr(gq), _ptr(grad_verts if need_verts else None),
                               _stream(stream)), "cp_backward")
         return gq, (grad_verts if need_verts else None)
@@ -288,12 +290,13 @@ class Batch:
 
 
 def autotune(verts: torch.Tensor, tris: torch.Tensor, sample: torch.Tensor,
-             cache_path: str | None = None):
-    """Run cp_autotune; returns (BuildOpts, QueryOpts)."""
+             cache_path: str | None = None, branching: int = 0):
+    """Run cp_autotune; returns (BuildOpts, QueryOpts).  branching=2/4/8 fixes the width."""
     _check_dev(verts, "verts", torch.float32, 3)
     _check_dev(tris, "tris", torch.int32, 3)
     _check_dev(sample, "sample", torch.float32, 3)
     bo, qo = BuildOpts(), QueryOpts()
+    bo.branching = branching
     torch.cuda.synchronize()
     check(lib.cp_autotune(_ptr(verts), verts.shape[0], _ptr(tris), tris.shape[0], _ptr(sample),
                           sample.shape[0], cache_path.encode() if cache_path else None, byref(bo),

@@ -122,6 +122,19 @@ CP_API const char* cp_status_string(cp_status status);
 /* Library version as an integer (major * 10000 + minor * 100 + patch). */
 CP_API int32_t cp_version(void);
 
+/* Kernels this library has launched in the process so far (all devices).
+ * A diagnostic: the difference across a region counts its launches.  No
+ * counterpart in the reference. */
+CP_API uint64_t cp_kernel_launches(void);
+
+/* Diagnostic timing: while enabled, every traversal-kernel launch outside a
+ * stream capture is bracketed by CUDA events on its own stream.
+ * cp_timing_read waits for those events and returns the summed device time
+ * (ms) and the number of launches since the last reset.  No counterpart in
+ * the reference (its only timing is an FPS readout, src/gpurt.cpp:275). */
+CP_API cp_status cp_timing_enable(int32_t on);
+CP_API cp_status cp_timing_read(double* traverse_ms, int64_t* launches, int32_t reset);
+
 /* ---- single mesh -------------------------------------------------------------- */
 
 /*
@@ -205,7 +218,11 @@ CP_API cp_status cp_query_host(const cp_mesh* mesh, const float* queries, int64_
  *   grad_verts[v_k] += -g_i b_k (q_i - p_i) / d_i      (accumulated atomically
  *                      for the three vertices of t; may be NULL)
  * with p_i = sum_k b_k v_k recomputed from the mesh and d_i = |q_i - p_i|;
- * d_i == 0 contributes zero.  The gradient with respect to the vertices
+ * d_i == 0 contributes zero.  The residual q_i - p_i is formed in float-float
+ * from the triangle's vertices, so queries very close to the surface keep an
+ * accurate direction.  bary may be NULL: the barycentrics of the closest point
+ * on tri[i] are then recomputed exactly (float-float Voronoi regions) from
+ * the query, which removes the FP32 rounding of cached weights.  The gradient with respect to the vertices
  * follows from the envelope theorem (the barycentrics are optimal, so their
  * own derivative drops out).  grad_verts is nv x 3 floats and is NOT cleared.
  * No counterpart in the reference, which has no differentiable path.
@@ -262,7 +279,9 @@ CP_API cp_status cp_batch_query(cp_batch* batch, const float* queries, const int
  * sample of queries (device arrays).  The winner is written to *best_build /
  * *best_query and, when cache_path is not NULL, stored in that text file
  * under the size class (one "class branching leaf block stack ms" line per
- * class); a cached class is returned without timing.  Synchronous.
+ * class and branching); a cached class is returned without timing.  If
+ * best_build->branching is 2, 4 or 8 on entry, only that branching is tried.
+ * Synchronous.
  */
 CP_API cp_status cp_autotune(const float* verts, int64_t nv, const int32_t* tris, int64_t nt,
                              const float* queries, int64_t nq, const char* cache_path,

@@ -246,12 +246,12 @@ void orc_brute_f64(const float* verts, int64_t nv, const int32_t* tris, int64_t 
 }
 
 void orc_point_tri_batch_f64(const float* verts, const int32_t* tris, const float* q,
-                             const int32_t* tri, int64_t nq, double* out_d2) {
+                             const int32_t* tri, int64_t nq, double* out_d2, double* out_bary) {
     for (int64_t i = 0; i < nq; ++i) {
         double p[3] = {q[3 * i], q[3 * i + 1], q[3 * i + 2]};
         double A[3], B[3], C[3];
         load_tri_f64(verts, tris, tri[i], A, B, C);
-        out_d2[i] = orc_point_tri_f64(p, A, B, C, NULL, NULL);
+        out_d2[i] = orc_point_tri_f64(p, A, B, C, NULL, out_bary ? out_bary + 3 * i : NULL);
     }
 }
 

@@ -53,9 +53,10 @@ int orc_exact_f64_dq(const float* verts, int64_t nv, const int32_t* tris, int64_
                      const double* q, int64_t nq, double* out_d2, int32_t* out_tri, int nthreads);
 
 /* FP64 squared distance from query i to the given triangle tri[i] (used to
- * confirm that a differing triangle index is a tie). */
+ * confirm that a differing triangle index is a tie), and optionally the
+ * barycentrics (nq x 3) of the closest point on that triangle. */
 void orc_point_tri_batch_f64(const float* verts, const int32_t* tris, const float* q,
-                             const int32_t* tri, int64_t nq, double* out_d2);
+                             const int32_t* tri, int64_t nq, double* out_d2, double* out_bary);
 
 /* ---- FP32 restatement of the LBVH build and traversal ------------------------ */
 

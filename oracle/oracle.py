@@ -68,7 +68,8 @@ def lib():
         L.orc_exact_f64_dq.argtypes = [c_void_p, c_int64, c_void_p, c_int64, c_void_p, c_int64,
                                        c_void_p, c_void_p, c_int]
         L.orc_point_tri_batch_f64.restype = None
-        L.orc_point_tri_batch_f64.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p]
+        L.orc_point_tri_batch_f64.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p,
+                                              c_void_p]
         L.orc_build.restype = c_int
         L.orc_build.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_int64, c_int64,
                                 c_int32, c_int32, c_int32, c_float, c_float, POINTER(POINTER(OrcTree))]
@@ -149,11 +150,14 @@ def exact_f64_dq(verts, tris, q64, threads: int | None = None):
     return np.sqrt(d2), tri
 
 
-def dist_to_tri_f64(verts, tris, q, tri_idx):
+def dist_to_tri_f64(verts, tris, q, tri_idx, want_bary: bool = False):
+    """FP64 distance from each query to the given triangle (and its barycentrics)."""
     verts, tris, q, tri_idx = _f32(verts), _i32(tris), _f32(q), _i32(tri_idx)
     out = np.empty(q.shape[0])
-    lib().orc_point_tri_batch_f64(_p(verts), _p(tris), _p(q), _p(tri_idx), q.shape[0], _p(out))
-    return np.sqrt(out)
+    bary = np.empty((q.shape[0], 3)) if want_bary else None
+    lib().orc_point_tri_batch_f64(_p(verts), _p(tris), _p(q), _p(tri_idx), q.shape[0], _p(out),
+                                  _p(bary))
+    return (np.sqrt(out), bary) if want_bary else np.sqrt(out)
 
 
 class Tree:

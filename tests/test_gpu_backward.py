@@ -29,21 +29,31 @@ def test_backward_torus(orc, cpq, cuda):
     v, t, q, g = W.torus_workload(nq=1 << 20)
     m = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=4)
     qd, gd = dev(q, cuda), dev(g, cuda)
-    r = m.query(qd, want_point=False, want_bary=True)
+    r = m.query(qd, want_point=True, want_bary=True)
     gq, gv = m.backward(qd, r.tri, r.bary, gd)
     gq, gv = gq.cpu().numpy(), gv.cpu().numpy()
     tri, b2 = r.tri.cpu().numpy(), r.bary.cpu().numpy()
-    # analytic FP64 gradient at the GPU's (tri, bary)
+    # 1. the FP64 analytic gradient at the GPU's own (tri, bary)
     rq, rv = orc.backward_f64(v, t, q, tri, bary3(b2), g.astype(np.float64))
     assert np.abs(gq - rq).max() <= GRAD_ATOL
     scale = np.maximum(1.0, np.abs(rv))
     assert (np.abs(gv - rv) / scale).max() <= 1e-4
-    # analytic FP64 gradient at the FP64 optimum on a sample
+    # 2. with bary = NULL the adjoint recomputes the exact closest point on the
+    #    forward's triangle: it matches the FP64 analytic gradient at the FP64
+    #    closest point of that triangle.  (Where the forward's triangle differs
+    #    from the FP64 optimum, FP64 confirms a distance tie within 1e-6, but
+    #    far from a finely tessellated surface the tied closest points can sit
+    #    ~1e-4 apart, so the gradient is compared per selected triangle.)
+    gq_x, _ = m.backward(qd, r.tri, None, gd, need_verts=False)
+    gq_x = gq_x.cpu().numpy()
     idx = np.random.default_rng(1).choice(q.shape[0], 10000, replace=False)
+    d_sel, b_sel = orc.dist_to_tri_f64(v, t, q[idx], tri[idx], want_bary=True)
+    rq2, _ = orc.backward_f64(v, t, q[idx], tri[idx], b_sel, g[idx].astype(np.float64))
+    err2 = np.abs(gq_x[idx] - rq2).max(axis=1)
+    assert err2.max() <= GRAD_ATOL, np.sort(err2)[-10:]
     e = orc.exact_f64(v, t, q[idx])
-    rq2, _ = orc.backward_f64(v, t, q[idx], e["tri"], e["bary"], g[idx].astype(np.float64))
-    assert np.abs(gq[idx] - rq2).max() <= 1e-4
-    # central finite differences in FP64 on the same 10k queries
+    assert np.all((d_sel - e["dist"]) / e["dist"] <= 1e-6)
+    # 3. central finite differences in FP64 on the same 10k queries
     q64 = q[idx].astype(np.float64)
     fd = np.zeros((len(idx), 3))
     for k in range(3):
@@ -53,13 +63,16 @@ def test_backward_torus(orc, cpq, cuda):
         dp, _ = orc.exact_f64_dq(v, t, qp)
         dm, _ = orc.exact_f64_dq(v, t, qm)
         fd[:, k] = g[idx] * (dp - dm) / (2 * FD_H)
-    err = np.abs(gq[idx] - fd).max(axis=1)
-    # the distance is not differentiable where the closest feature switches
-    # (medial axis); those few queries show O(1) differences
+    # finite differences follow the FP64 optimum: compare where the forward's
+    # closest point is that optimum (tied closest points elsewhere, see 2.)
+    same = np.linalg.norm(r.point.cpu().numpy()[idx] - e["point"], axis=1) <= 1e-6 \
+        if r.point is not None else (tri[idx] == e["tri"])
+    assert same.mean() >= 0.95
+    err = np.abs(gq[idx] - fd).max(axis=1)[same]
     frac_bad = float((err > 1e-3).mean())
-    print(f"FD check: median {np.median(err):.2e}, p99 {np.percentile(err, 99):.2e}, "
-          f"non-smooth fraction {frac_bad:.2e}")
-    assert np.percentile(err, 99) <= 1e-3
+    print(f"FD check on {same.sum()} queries: median {np.median(err):.2e}, "
+          f"p99 {np.percentile(err, 99):.2e}, non-smooth fraction {frac_bad:.2e}")
+    assert np.percentile(err, 99) <= 1e-4
     assert frac_bad <= 5e-3
 
 
