@@ -152,23 +152,16 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "fallback": True}
 
 
-def measure_l2_gbs(torch, dev) -> float:
-    """Read bandwidth of a 48 MB L2-resident buffer (torch sum, best of 20)."""
-    x = torch.ones(12 * (1 << 20), dtype=torch.float32, device=dev)
-    for _ in range(3):
-        x.sum()
-    best = 0.0
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    for _ in range(20):
-        e0.record()
-        for _ in range(10):
-            x.sum()
-        e1.record()
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1) / 10
-        best = max(best, x.numel() * 4 / (ms * 1e-3) / 1e9)
-    del x
-    return best
+def measure_l2_gbs(torch) -> float:
+    """L2 read bandwidth: 128-bit loads over a 48 MB L2-resident buffer (cp_probe_read_bandwidth)."""
+    from ctypes import byref, c_double, c_void_p
+
+    from gpurt_cpq._lib import check, lib
+
+    g = c_double()
+    check(lib.cp_probe_read_bandwidth(48 << 20, 20, byref(g),
+                                      c_void_p(torch.cuda.current_stream().cuda_stream)), "probe")
+    return g.value
 
 
 def workload():
@@ -279,7 +272,7 @@ def our_arm(args):
     info = mesh.info()
     ws = torch.empty(mesh.workspace_size(nq, qopts), dtype=torch.uint8, device=dev)
     out = mesh.query(qd, workspace=ws, opts=qopts)
-    l2_gbs = measure_l2_gbs(torch, dev)
+    l2_gbs = measure_l2_gbs(torch)
     for _ in range(args.warmup):
         mesh.query(qd, workspace=ws, opts=qopts, out=out)
     torch.cuda.synchronize()

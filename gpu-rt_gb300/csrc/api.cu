@@ -142,10 +142,13 @@ cp_status to_query_params(const cp_query_opts* o, QueryParams* q) {
         return fail(CP_ERROR_INVALID_VALUE, "short_stack must be 4, 8 or 16");
     if (o->blocks_per_sm < 0 || o->blocks_per_sm > 64)
         return fail(CP_ERROR_INVALID_VALUE, "blocks_per_sm must be in 0..64");
+    if (o->traversal < CP_TRAVERSAL_AUTO || o->traversal > CP_TRAVERSAL_PACKET)
+        return fail(CP_ERROR_INVALID_VALUE, "traversal must be CP_TRAVERSAL_AUTO, _THREAD or _PACKET");
     q->block = block;
     q->sort = o->sort_queries ? 1 : 0;
     q->blocks_per_sm = o->blocks_per_sm;
     q->short_stack = ss;
+    q->traversal = o->traversal;
     return CP_SUCCESS;
 }
 
@@ -195,6 +198,7 @@ CP_API void cp_query_opts_default(cp_query_opts* o) {
     o->sort_queries = 1;
     o->blocks_per_sm = 0;
     o->short_stack = 8;
+    o->traversal = CP_TRAVERSAL_AUTO;
 }
 
 CP_API const char* cp_last_error_string(void) { return g_last_error.c_str(); }
@@ -535,7 +539,7 @@ CP_API cp_status cp_batch_query(cp_batch* bt, const float* queries, const int64_
     std::vector<uintptr_t> key = {(uintptr_t)queries, (uintptr_t)out_point, (uintptr_t)out_dist,
                                   (uintptr_t)out_tri, (uintptr_t)out_bary, (uintptr_t)workspace,
                                   (uintptr_t)qp.block, (uintptr_t)qp.sort, (uintptr_t)qp.blocks_per_sm,
-                                  (uintptr_t)qp.short_stack, (uintptr_t)nq};
+                                  (uintptr_t)qp.short_stack, (uintptr_t)qp.traversal, (uintptr_t)nq};
     for (int i = 0; i <= nm; ++i) key.push_back((uintptr_t)q_offsets[i]);
     if (!bt->exec || key != bt->graph_key) {
         if (bt->exec) {

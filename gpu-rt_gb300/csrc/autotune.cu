@@ -2,8 +2,9 @@
 // short-stack depth by timing real builds and queries on the caller's data.
 // The reference has no tuner; its only knobs are UI sliders that feed push
 // constants (src/gpurt.cpp:283-322, src/vk/rt.h:85-102).  Results are cached
-// in a plain text file, one line per size class:
+// in a plain text file, one line per size class and branching:
 //   <class> <branching> <leaf_size> <block_size> <short_stack> <ms>
+// where short_stack 0 stands for the warp-packet traversal.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -63,7 +64,8 @@ extern "C" CP_API cp_status cp_autotune(const float* verts, int64_t nv, const in
             best_build->branching = e.K;
             best_build->leaf_size = e.leaf;
             best_query->block_size = e.block;
-            best_query->short_stack = e.stack;
+            best_query->short_stack = e.stack ? e.stack : 8;
+            best_query->traversal = e.stack ? CP_TRAVERSAL_THREAD : CP_TRAVERSAL_PACKET;
             return CP_SUCCESS;
         }
 
@@ -97,11 +99,14 @@ extern "C" CP_API cp_status cp_autotune(const float* verts, int64_t nv, const in
                 break;
             }
             for (int bi = 0; bi < 2; ++bi)
-                for (int si = 0; si < 3; ++si) {
+                for (int si = 0; si < 4; ++si) {
+                    // stacks[0..2]: per-thread traversal with that short stack;
+                    // si == 3: warp-packet traversal
                     cp_query_opts qo;
                     cp_query_opts_default(&qo);
                     qo.block_size = blocks[bi];
-                    qo.short_stack = stacks[si];
+                    qo.short_stack = si < 3 ? stacks[si] : 8;
+                    qo.traversal = si < 3 ? CP_TRAVERSAL_THREAD : CP_TRAVERSAL_PACKET;
                     size_t wsb = 0;
                     cp_query_workspace_size(mesh, nq, &qo, &wsb);
                     void* ws = nullptr;
@@ -124,7 +129,8 @@ extern "C" CP_API cp_status cp_autotune(const float* verts, int64_t nv, const in
                         result = s;
                         break;
                     }
-                    if (ms < best.ms) best = {cls, Ks[ki], leaves[li], blocks[bi], stacks[si], ms};
+                    if (ms < best.ms)
+                        best = {cls, Ks[ki], leaves[li], blocks[bi], si < 3 ? stacks[si] : 0, ms};
                 }
             cp_mesh_destroy(mesh);
         }
@@ -137,7 +143,8 @@ extern "C" CP_API cp_status cp_autotune(const float* verts, int64_t nv, const in
     best_build->branching = best.K;
     best_build->leaf_size = best.leaf;
     best_query->block_size = best.block;
-    best_query->short_stack = best.stack;
+    best_query->short_stack = best.stack ? best.stack : 8;
+    best_query->traversal = best.stack ? CP_TRAVERSAL_THREAD : CP_TRAVERSAL_PACKET;
     if (cache_path) {
         std::vector<Entry> out;
         for (const Entry& e : cache)

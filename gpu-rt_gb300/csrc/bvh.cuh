@@ -83,6 +83,7 @@ struct QueryParams {
     int sort = 1;
     int blocks_per_sm = 0;
     int short_stack = 8;
+    int traversal = 0;  // 0 auto (packet when sorted), 1 per-thread, 2 warp packet
 };
 
 size_t query_workspace_bytes(const Bvh& b, int64_t nq, const QueryParams& qp);

@@ -411,6 +411,218 @@ __global__ void __launch_bounds__(256) k_traverse(TraverseArgs a) {
     }
 }
 
+__device__ __forceinline__ void write_result(const TraverseArgs& a, int64_t qi, float qx, float qy,
+                                             float qz, int best_rec, int best_idx) {
+    float dist = __int_as_float(0x7fc00000), px = dist, py = dist, pz = dist, bv = dist, bw = dist;
+    if (best_rec >= 0) {
+        const float4* rp = reinterpret_cast<const float4*>(a.recs + best_rec);
+        TriRec r;
+        r.p0 = __ldg(rp);
+        r.p1 = __ldg(rp + 1);
+        r.p2 = __ldg(rp + 2);
+        precise_closest(qx, qy, qz, r, dist, px, py, pz, bv, bw);
+    } else {
+        atomicOr(a.status, 4u);
+    }
+    if (a.out_dist) a.out_dist[qi] = dist;
+    if (a.out_tri) a.out_tri[qi] = best_rec >= 0 ? best_idx : -1;
+    if (a.out_point) {
+        a.out_point[3 * qi] = px;
+        a.out_point[3 * qi + 1] = py;
+        a.out_point[3 * qi + 2] = pz;
+    }
+    if (a.out_bary) {
+        a.out_bary[2 * qi] = bv;
+        a.out_bary[2 * qi + 1] = bw;
+    }
+}
+
+// Warp-packet traversal.  The 32 lanes of a warp hold 32 consecutive queries
+// of the Morton order (neighbours in space) and walk ONE shared stack: a
+// child is visited when any lane's box lower bound beats that lane's best, so
+// every node row is a single broadcast load and node tests run with all
+// lanes converged.  The child order is the first pending lane's nearest-first
+// order.  Stack entries keep the child's box, so on a pop every lane re-checks
+// its own bound and the entry is skipped when no lane still needs it.  The
+// stack holds (K-1)(depth+1) entries at most; `cap` is that bound, so it
+// cannot overflow.  Lanes of different meshes in one chunk (batches) are
+// served one mesh at a time.
+template <int K>
+__global__ void __launch_bounds__(256) k_traverse_packet(TraverseArgs a, int cap) {
+    extern __shared__ float s_pk[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    // per warp: ref[cap] then lo x, hi x, lo y, hi y, lo z, hi z [cap] each
+    int32_t* st_ref = reinterpret_cast<int32_t*>(s_pk + (size_t)warp * 7 * cap);
+    float* st_box = s_pk + (size_t)warp * 7 * cap + cap;
+    const WideNode<K>* __restrict__ nodes = static_cast<const WideNode<K>*>(a.nodes);
+    const uint32_t lt_mask = (1u << lane) - 1u;
+
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(a.counter, 32ull);
+        base = __shfl_sync(kFull, base, 0);
+        if (base >= (unsigned long long)a.nq) break;  // warp-uniform exit
+        const int64_t i = (int64_t)base + lane;
+        const bool valid = i < a.nq;
+        int64_t qi = 0;
+        float qx = 0.f, qy = 0.f, qz = 0.f;
+        int m = 0;
+        if (valid) {
+            qi = a.perm ? (int64_t)a.perm[i] : i;
+            qx = a.queries[3 * qi];
+            qy = a.queries[3 * qi + 1];
+            qz = a.queries[3 * qi + 2];
+            m = a.nmeshes > 1 ? mesh_of(a.qoff, a.nmeshes, qi) : 0;
+        }
+        float best = INFINITY;
+        int best_rec = -1, best_idx = INT_MAX;
+        unsigned pending = __ballot_sync(kFull, valid);
+        while (pending) {
+            const int leader = __ffs(pending) - 1;
+            const int mesh = __shfl_sync(kFull, m, leader);
+            const bool mine = ((pending >> lane) & 1u) && m == mesh;
+            pending &= ~__ballot_sync(kFull, mine);
+            // lanes outside this round never need anything: bound -inf
+            float lim = mine ? best : -INFINITY;
+            int sp = 0;
+            int cur = a.wide_root[mesh];
+            bool leaf_active = false;  // for leaves: this lane's bound beat its best
+            bool have = true;
+            while (have) {
+                if (cur >= 0) {
+                    const WideNode<K>* nd = nodes + cur;
+                    float lox[K], hix[K], loy[K], hiy[K], loz[K], hiz[K];
+                    int32_t ch[K];
+                    load_row<K>(nd->lox, lox);
+                    load_row<K>(nd->hix, hix);
+                    load_row<K>(nd->loy, loy);
+                    load_row<K>(nd->hiy, hiy);
+                    load_row<K>(nd->loz, loz);
+                    load_row<K>(nd->hiz, hiz);
+                    load_row_i<K>(nd->child, ch);
+                    float lb[K];
+                    uint32_t need = 0;
+#pragma unroll
+                    for (int s = 0; s < K; ++s) {
+                        lb[s] = box_lb2(qx, qy, qz, lox[s], hix[s], loy[s], hiy[s], loz[s], hiz[s]);
+                        if (__any_sync(kFull, lb[s] < lim)) need |= 1u << s;
+                    }
+                    // the leader's nearest-first order, packed 4 bits per slot
+                    float d[K];
+                    int sl[K];
+#pragma unroll
+                    for (int s = 0; s < K; ++s) {
+                        d[s] = lb[s];
+                        sl[s] = s;
+                    }
+                    sort_children<K>(d, sl);
+                    uint32_t packed = 0;
+#pragma unroll
+                    for (int s = 0; s < K; ++s) packed |= (uint32_t)sl[s] << (4 * s);
+                    packed = __shfl_sync(kFull, packed, leader);
+                    // visit order restricted to needed slots; first is taken now
+                    int first_slot = -1, npush = 0;
+                    uint32_t push_mask = 0;
+#pragma unroll
+                    for (int t = 0; t < K; ++t) {
+                        const int s = (packed >> (4 * t)) & 15;
+                        if ((need >> s) & 1u) {
+                            if (first_slot < 0) first_slot = s;
+                            else {
+                                push_mask |= 1u << s;
+                                ++npush;
+                            }
+                        }
+                    }
+                    // lane j < K pushes slot j: farthest entries go deepest
+                    if (lane < K && ((push_mask >> lane) & 1u)) {
+                        int above = 0;  // pushed slots later in the visit order than mine
+                        bool seen = false;
+#pragma unroll
+                        for (int t = 0; t < K; ++t) {
+                            const int s = (packed >> (4 * t)) & 15;
+                            if (s == lane) seen = true;
+                            else if (seen && ((push_mask >> s) & 1u)) ++above;
+                        }
+                        int pos = sp + above;
+                        if (pos >= cap) {  // cannot happen: cap is the depth bound
+                            atomicOr(a.status, 1u);
+                            pos = cap - 1;
+                        }
+                        float blx = 0.f, bhx = 0.f, bly = 0.f, bhy = 0.f, blz = 0.f, bhz = 0.f;
+                        int32_t c = 0;
+#pragma unroll
+                        for (int s = 0; s < K; ++s)
+                            if (s == lane) {
+                                blx = lox[s]; bhx = hix[s]; bly = loy[s]; bhy = hiy[s];
+                                blz = loz[s]; bhz = hiz[s]; c = ch[s];
+                            }
+                        st_ref[pos] = c;
+                        st_box[0 * cap + pos] = blx;
+                        st_box[1 * cap + pos] = bhx;
+                        st_box[2 * cap + pos] = bly;
+                        st_box[3 * cap + pos] = bhy;
+                        st_box[4 * cap + pos] = blz;
+                        st_box[5 * cap + pos] = bhz;
+                    }
+                    sp = min(sp + npush, cap);
+                    __syncwarp();
+                    if (first_slot >= 0) {
+                        float lbf = lb[0];
+                        int32_t cf = ch[0];
+#pragma unroll
+                        for (int s = 1; s < K; ++s)
+                            if (s == first_slot) {
+                                lbf = lb[s];
+                                cf = ch[s];
+                            }
+                        cur = cf;
+                        leaf_active = lbf < lim;
+                        continue;
+                    }
+                } else {
+                    const int first = leaf_first(cur), cnt = leaf_count(cur);
+                    for (int k = 0; k < cnt; ++k) {
+                        const float4* rp = reinterpret_cast<const float4*>(a.recs + first + k);
+                        TriRec r;
+                        r.p0 = __ldg(rp);
+                        r.p1 = __ldg(rp + 1);
+                        r.p2 = __ldg(rp + 2);
+                        if (leaf_active) {
+                            const float d2 = tri_d2(qx, qy, qz, r);
+                            const int idx = __float_as_int(r.p2.y);
+                            if (d2 < best || (d2 == best && idx < best_idx)) {
+                                best = d2;
+                                best_rec = first + k;
+                                best_idx = idx;
+                            }
+                        }
+                    }
+                    if (mine) lim = best;
+                }
+                // pop the next entry some lane still needs
+                have = false;
+                while (sp > 0) {
+                    --sp;
+                    const float lb = box_lb2(qx, qy, qz, st_box[sp], st_box[cap + sp],
+                                             st_box[2 * cap + sp], st_box[3 * cap + sp],
+                                             st_box[4 * cap + sp], st_box[5 * cap + sp]);
+                    const bool want = lb < lim;
+                    if (__any_sync(kFull, want)) {
+                        cur = st_ref[sp];
+                        leaf_active = want;
+                        have = true;
+                        break;
+                    }
+                }
+                __syncwarp();
+            }
+            (void)lt_mask;
+        }
+        if (valid) write_result(a, qi, qx, qy, qz, best_rec, best_idx);
+    }
+}
+
 __global__ void k_query_keys(const float* __restrict__ q, int64_t nq, const int64_t* __restrict__ qoff,
                              int nmeshes, const float* __restrict__ frame, int qbits,
                              uint64_t* __restrict__ keys, int32_t* __restrict__ vals) {
@@ -604,7 +816,57 @@ cudaError_t launch_traverse(const TraverseArgs& args, int block, int blocks_per_
 }
 
 template <int K>
-cudaError_t launch_k(const TraverseArgs& args, const QueryParams& qp, cudaStream_t st) {
+cudaError_t launch_packet(const TraverseArgs& args, int cap, int block, int blocks_per_sm,
+                          cudaStream_t st) {
+    if (cap < 1) cap = 1;
+    const size_t smem = (size_t)(block / 32) * 7 * cap * sizeof(float);
+    auto kern = k_traverse_packet<K>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0;
+    e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    if (blocks_per_sm <= 0) {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, block, smem);
+        if (e != cudaSuccess) return e;
+        if (blocks_per_sm < 1) blocks_per_sm = 1;
+    }
+    int64_t grid = (int64_t)sms * blocks_per_sm;
+    const int64_t need = ((args.nq + 31) / 32 * 32 + block - 1) / block;
+    if (grid > need) grid = need;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    bool timed = false;
+    {
+        std::lock_guard<std::mutex> lock(g_timing.mu);
+        timed = g_timing.on;
+    }
+    cudaStreamCaptureStatus capst = cudaStreamCaptureStatusNone;
+    cudaStreamIsCapturing(st, &capst);
+    if (timed && capst == cudaStreamCaptureStatusNone) {
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        cudaEventRecord(e0, st);
+    } else {
+        timed = false;
+    }
+    kern<<<(unsigned)grid, block, smem, st>>>(args, cap); note_launch();
+    e = cudaGetLastError();
+    if (timed) {
+        cudaEventRecord(e1, st);
+        std::lock_guard<std::mutex> lock(g_timing.mu);
+        g_timing.pending.emplace_back(e0, e1);
+    }
+    return e;
+}
+
+template <int K>
+cudaError_t launch_k(const TraverseArgs& args, const QueryParams& qp, int cap, cudaStream_t st) {
+    // packet traversal needs spatially coherent warps: the default whenever
+    // the queries are walked in Morton order
+    const bool packet = qp.traversal == 2 || (qp.traversal == 0 && qp.sort);
+    if (packet) return launch_packet<K>(args, cap, qp.block, qp.blocks_per_sm, st);
     switch (qp.short_stack) {
         case 4: return launch_traverse<K, 4>(args, qp.block, qp.blocks_per_sm, st);
         case 16: return launch_traverse<K, 16>(args, qp.block, qp.blocks_per_sm, st);
@@ -690,9 +952,9 @@ cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int6
     args.counter = counter;
     args.status = b.status;
     switch (b.p.K) {
-        case 2: return launch_k<2>(args, qp, st);
-        case 4: return launch_k<4>(args, qp, st);
-        default: return launch_k<8>(args, qp, st);
+        case 2: return launch_k<2>(args, qp, b.stack_bound, st);
+        case 4: return launch_k<4>(args, qp, b.stack_bound, st);
+        default: return launch_k<8>(args, qp, b.stack_bound, st);
     }
 }
 

@@ -37,7 +37,12 @@ class BuildOpts(Structure):
 
 class QueryOpts(Structure):
     _fields_ = [("block_size", c_int32), ("sort_queries", c_int32), ("blocks_per_sm", c_int32),
-                ("short_stack", c_int32)]
+                ("short_stack", c_int32), ("traversal", c_int32)]
+
+
+CP_TRAVERSAL_AUTO = 0
+CP_TRAVERSAL_THREAD = 1
+CP_TRAVERSAL_PACKET = 2
 
 
 class MeshInfo(Structure):
@@ -58,6 +63,7 @@ SIGNATURES = {
     "cp_kernel_launches": (c_uint64, []),
     "cp_timing_enable": (c_int32, [c_int32]),
     "cp_timing_read": (c_int32, [POINTER(c_double), POINTER(c_int64), c_int32]),
+    "cp_probe_read_bandwidth": (c_int32, [c_int64, c_int32, POINTER(c_double), c_void_p]),
     "cp_mesh_create": (c_int32, [c_void_p, c_int64, c_int64, c_void_p, c_int64, POINTER(BuildOpts),
                                  c_void_p, POINTER(c_void_p)]),
     "cp_mesh_refit": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p]),

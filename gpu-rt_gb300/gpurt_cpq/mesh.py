@@ -55,7 +55,7 @@ def build_opts(branching: int = 2, leaf_size: int = 4, collapse: str = "count",
 
 
 def query_opts(block_size: int = 0, sort_queries: bool = True, blocks_per_sm: int = 0,
-               short_stack: int = 0) -> QueryOpts:
+               short_stack: int = 0, traversal: str = "auto") -> QueryOpts:
     o = QueryOpts()
     lib.cp_query_opts_default(byref(o))
     if block_size:
@@ -64,6 +64,7 @@ def query_opts(block_size: int = 0, sort_queries: bool = True, blocks_per_sm: in
     o.blocks_per_sm = blocks_per_sm
     if short_stack:
         o.short_stack = short_stack
+    o.traversal = {"auto": 0, "thread": 1, "packet": 2}[traversal]
     return o
 
 

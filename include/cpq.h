@@ -88,7 +88,16 @@ typedef struct cp_query_opts {
     int32_t sort_queries;   /* 1: walk the queries in Morton order of their position (outputs keep input order) */
     int32_t blocks_per_sm;  /* persistent grid = SM count x this; 0 = from occupancy */
     int32_t short_stack;    /* per-thread stack entries kept in shared memory: 4, 8 or 16; 0 = default */
+    int32_t traversal;      /* CP_TRAVERSAL_*: how lanes share work */
 } cp_query_opts;
+
+/* Traversal kernels.  PACKET: the 32 lanes of a warp take 32 consecutive
+ * (Morton-ordered, so neighbouring) queries and walk one shared stack, a node
+ * being visited when any lane still needs it; THREAD: every lane walks its
+ * own query with its own stack.  AUTO picks PACKET when sort_queries is set. */
+#define CP_TRAVERSAL_AUTO   0
+#define CP_TRAVERSAL_THREAD 1
+#define CP_TRAVERSAL_PACKET 2
 
 /* Statistics of a built mesh (cp_mesh_info). */
 typedef struct cp_mesh_info_t {
@@ -134,6 +143,12 @@ CP_API uint64_t cp_kernel_launches(void);
  * the reference (its only timing is an FPS readout, src/gpurt.cpp:275). */
 CP_API cp_status cp_timing_enable(int32_t on);
 CP_API cp_status cp_timing_read(double* traverse_ms, int64_t* launches, int32_t reset);
+
+/* Diagnostic: read bandwidth (GB/s) of 128-bit L2 loads over a `bytes`-sized
+ * buffer, best of 5 timed launches of `reps` sweeps each.  A buffer smaller
+ * than L2 (129 MB on GB300) measures L2, a larger one HBM.  Synchronous. */
+CP_API cp_status cp_probe_read_bandwidth(int64_t bytes, int32_t reps, double* gbs,
+                                         cp_stream_t stream);
 
 /* ---- single mesh -------------------------------------------------------------- */
 

@@ -64,16 +64,21 @@ def test_backward_torus(orc, cpq, cuda):
         dm, _ = orc.exact_f64_dq(v, t, qm)
         fd[:, k] = g[idx] * (dp - dm) / (2 * FD_H)
     # finite differences follow the FP64 optimum: compare where the forward's
-    # closest point is that optimum (tied closest points elsewhere, see 2.)
-    same = np.linalg.norm(r.point.cpu().numpy()[idx] - e["point"], axis=1) <= 1e-6 \
-        if r.point is not None else (tri[idx] == e["tri"])
+    # closest point is that optimum (tied closest points elsewhere, see 2.),
+    # and where the central difference is accurate: its truncation error near
+    # an edge or vertex feature is ~h^2/(6 d^2), so queries with d >= 0.01
+    same = np.linalg.norm(r.point.cpu().numpy()[idx] - e["point"], axis=1) <= 1e-6
     assert same.mean() >= 0.95
-    err = np.abs(gq[idx] - fd).max(axis=1)[same]
+    use = same & (e["dist"] >= 0.01)
+    err = np.abs(gq[idx] - fd).max(axis=1)[use]
     frac_bad = float((err > 1e-3).mean())
-    print(f"FD check on {same.sum()} queries: median {np.median(err):.2e}, "
-          f"p99 {np.percentile(err, 99):.2e}, non-smooth fraction {frac_bad:.2e}")
+    print(f"FD check on {use.sum()} queries: median {np.median(err):.2e}, "
+          f"p99 {np.percentile(err, 99):.2e}, max {err.max():.2e}, "
+          f"medial-axis fraction {frac_bad:.2e}")
+    assert np.median(err) <= 1e-6
     assert np.percentile(err, 99) <= 1e-4
-    assert frac_bad <= 5e-3
+    # a central difference across the medial axis (two equidistant features) is O(1)
+    assert frac_bad <= 2e-3
 
 
 def test_backward_zero_distance_and_invalid(cpq, cuda):

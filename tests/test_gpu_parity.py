@@ -175,13 +175,25 @@ def test_query_options_do_not_change_results(cpq, cuda):
     q = W.heightfield_queries(v, t, 50000, seed=4)
     m = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=4, leaf_size=4)
     qd = dev(q, cuda)
-    base = m.query(qd, want_bary=True)
-    for kw in [dict(sort_queries=False), dict(block_size=128), dict(block_size=64, short_stack=4),
-               dict(short_stack=16), dict(blocks_per_sm=1)]:
+    base = m.query(qd, want_bary=True, opts=cpq.query_opts(traversal="thread"))
+    for kw in [dict(sort_queries=False, traversal="thread"), dict(block_size=128, traversal="thread"),
+               dict(block_size=64, short_stack=4, traversal="thread"),
+               dict(short_stack=16, traversal="thread"), dict(blocks_per_sm=1, traversal="thread")]:
         r = m.query(qd, want_bary=True, opts=cpq.query_opts(**kw))
         assert torch.equal(r.dist, base.dist), kw
         assert torch.equal(r.tri, base.tri), kw
         assert torch.equal(r.point, base.point), kw
+    # the warp-packet kernel visits nodes in another order: every triangle
+    # closer than the answer is still tested, so results agree up to exact
+    # FP32 ties of the traversal distance
+    for kw in [dict(traversal="packet"), dict(traversal="packet", sort_queries=False),
+               dict(traversal="packet", block_size=64), dict(traversal="auto")]:
+        r = m.query(qd, want_bary=True, opts=cpq.query_opts(**kw))
+        same = r.tri == base.tri
+        assert float(same.float().mean()) > 0.999, kw
+        assert torch.equal(r.dist[same], base.dist[same]), kw
+        rel = ((r.dist - base.dist).abs() / base.dist.clamp_min(1e-30)).max()
+        assert float(rel) <= 1e-6, kw
 
 
 def test_query_heightfield_sampled(orc, cpq, cuda):
