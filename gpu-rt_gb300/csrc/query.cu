@@ -642,6 +642,78 @@ __global__ void k_query_keys(const float* __restrict__ q, int64_t nq, const int6
     vals[i] = (int32_t)i;
 }
 
+__device__ __forceinline__ void atomic_min_pos(float* addr, float v) {
+    if (v >= 0.0f) atomicMin(reinterpret_cast<int*>(addr), __float_as_int(v));
+    else atomicMax(reinterpret_cast<unsigned*>(addr), __float_as_uint(v));
+}
+__device__ __forceinline__ void atomic_max_pos(float* addr, float v) {
+    if (v >= 0.0f) atomicMax(reinterpret_cast<int*>(addr), __float_as_int(v));
+    else atomicMin(reinterpret_cast<unsigned*>(addr), __float_as_uint(v));
+}
+
+__global__ void k_init_qbounds(float* __restrict__ qb, int nmeshes) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 6 * nmeshes) qb[i] = (i % 6) < 3 ? INFINITY : -INFINITY;
+}
+
+// Per-mesh bounding box of the finite query points (warp-reduced atomics).
+__global__ void k_query_bounds(const float* __restrict__ q, int64_t nq,
+                               const int64_t* __restrict__ qoff, int nmeshes,
+                               float* __restrict__ qb) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < nq;
+    float p[3] = {0.f, 0.f, 0.f};
+    bool fin = false;
+    int m = 0;
+    if (valid) {
+        p[0] = q[3 * i];
+        p[1] = q[3 * i + 1];
+        p[2] = q[3 * i + 2];
+        fin = isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]);
+        m = nmeshes > 1 ? mesh_of(qoff, nmeshes, i) : 0;
+    }
+    const int m0 = __shfl_sync(kFull, m, 0);
+    if (__all_sync(kFull, valid && fin && m == m0)) {
+        float lo[3] = {p[0], p[1], p[2]}, hi[3] = {p[0], p[1], p[2]};
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                lo[k] = fminf(lo[k], __shfl_xor_sync(kFull, lo[k], o));
+                hi[k] = fmaxf(hi[k], __shfl_xor_sync(kFull, hi[k], o));
+            }
+        if ((threadIdx.x & 31) == 0)
+            for (int k = 0; k < 3; ++k) {
+                atomic_min_pos(&qb[6 * m + k], lo[k]);
+                atomic_max_pos(&qb[6 * m + 3 + k], hi[k]);
+            }
+    } else if (valid && fin) {
+        for (int k = 0; k < 3; ++k) {
+            atomic_min_pos(&qb[6 * m + k], p[k]);
+            atomic_max_pos(&qb[6 * m + 3 + k], p[k]);
+        }
+    }
+}
+
+// Isotropic Morton frame over each mesh's query box: the same cell size on
+// every axis, so 32 consecutive codes are a compact cluster of queries (with
+// the mesh's box instead, queries above or below a flat mesh collapse into
+// one clamped layer of cells and a warp's queries spread far apart).
+__global__ void k_query_frame(float* __restrict__ qb, int nmeshes, float cells) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= nmeshes) return;
+    float ext = 0.0f;
+    for (int k = 0; k < 3; ++k) {
+        const float e = qb[6 * m + 3 + k] - qb[6 * m + k];
+        if (e > ext) ext = e;  // NaN / empty boxes leave ext at 0
+    }
+    const float scale = ext > 0.0f && ext < INFINITY ? cells / ext : 0.0f;
+    for (int k = 0; k < 3; ++k) {
+        if (!(qb[6 * m + k] > -INFINITY && qb[6 * m + k] < INFINITY)) qb[6 * m + k] = 0.0f;
+        qb[6 * m + 3 + k] = scale;
+    }
+}
+
 // Adjoint: recompute p from (tri, bary), scatter -b_k g (q - p)/d to the
 // triangle's vertices.  Lanes that hit the same vertex are summed inside the
 // warp first (match_any + an ordered shuffle loop) and one lane adds.
@@ -742,15 +814,16 @@ size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 struct QueryLayout {
     size_t keys = 0, vals = 0, keys_alt = 0, vals_alt = 0, sort_ws = 0, counter = 0, total = 0;
-    size_t sort_ws_bytes = 0;
+    size_t sort_ws_bytes = 0, frame = 0;
 };
 
-QueryLayout layout(int64_t nq, bool sort) {
+QueryLayout layout(int64_t nq, int nmeshes, bool sort) {
     QueryLayout L;
     size_t off = 0;
     L.counter = off;
     off += 256;
     if (sort && nq > 1) {
+        L.frame = off; off += align256(sizeof(float) * 6 * nmeshes);
         L.keys = off; off += align256(sizeof(uint64_t) * nq);
         L.vals = off; off += align256(sizeof(int32_t) * nq);
         L.keys_alt = off; off += align256(sizeof(uint64_t) * nq);
@@ -905,15 +978,14 @@ cudaError_t timing_read(double* ms, int64_t* launches, bool reset) {
 }
 
 size_t query_workspace_bytes(const Bvh& b, int64_t nq, const QueryParams& qp) {
-    (void)b;
-    return layout(nq, qp.sort != 0).total;
+    return layout(nq, b.nmeshes, qp.sort != 0).total;
 }
 
 cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int64_t* d_qoff,
                       const QueryParams& qp, float* out_point, float* out_dist, int32_t* out_tri,
                       float* out_bary, void* ws, size_t ws_bytes, cudaStream_t st) {
     if (nq <= 0) return cudaSuccess;
-    const QueryLayout L = layout(nq, qp.sort != 0);
+    const QueryLayout L = layout(nq, b.nmeshes, qp.sort != 0);
     if (ws_bytes < L.total) return cudaErrorInvalidValue;
     unsigned char* w = static_cast<unsigned char*>(ws);
     unsigned long long* counter = reinterpret_cast<unsigned long long*>(w + L.counter);
@@ -926,8 +998,14 @@ cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int6
         uint64_t* keys_alt = reinterpret_cast<uint64_t*>(w + L.keys_alt);
         int32_t* vals_alt = reinterpret_cast<int32_t*>(w + L.vals_alt);
         const int qbits = (64 - b.mesh_bits) / 3 < 10 ? (64 - b.mesh_bits) / 3 : 10;
+        float* frame = reinterpret_cast<float*>(w + L.frame);
+        k_init_qbounds<<<(unsigned)((6 * b.nmeshes + 255) / 256), 256, 0, st>>>(frame, b.nmeshes); note_launch();
+        k_query_bounds<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(queries, nq, d_qoff, b.nmeshes,
+                                                                     frame); note_launch();
+        k_query_frame<<<(unsigned)((b.nmeshes + 255) / 256), 256, 0, st>>>(frame, b.nmeshes,
+                                                                           (float)(1u << qbits)); note_launch();
         k_query_keys<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(queries, nq, d_qoff, b.nmeshes,
-                                                                   b.frame, qbits, keys, vals); note_launch();
+                                                                   frame, qbits, keys, vals); note_launch();
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
         bool in_alt = false;

@@ -56,29 +56,32 @@ def test_backward_torus(orc, cpq, cuda):
     # 3. central finite differences in FP64 on the same 10k queries
     q64 = q[idx].astype(np.float64)
     fd = np.zeros((len(idx), 3))
+    smooth = np.ones(len(idx), bool)
     for k in range(3):
         qp, qm = q64.copy(), q64.copy()
         qp[:, k] += FD_H
         qm[:, k] -= FD_H
-        dp, _ = orc.exact_f64_dq(v, t, qp)
-        dm, _ = orc.exact_f64_dq(v, t, qm)
+        dp, tp = orc.exact_f64_dq(v, t, qp)
+        dm, tm = orc.exact_f64_dq(v, t, qm)
         fd[:, k] = g[idx] * (dp - dm) / (2 * FD_H)
-    # finite differences follow the FP64 optimum: compare where the forward's
-    # closest point is that optimum (tied closest points elsewhere, see 2.),
-    # and where the central difference is accurate: its truncation error near
-    # an edge or vertex feature is ~h^2/(6 d^2), so queries with d >= 0.01
+        smooth &= (tp == e["tri"]) & (tm == e["tri"])
+    # A central difference measures the gradient only where the distance is
+    # smooth across the stencil: the FP64 closest triangle is the same at q and
+    # at q +- h on every axis (a stencil across a medial sheet of the
+    # polyhedral surface straddles a jump in the gradient), and the
+    # truncation error ~h^2/(6 d^2) near an edge or vertex feature is small
+    # (d >= 0.01).  Compare there, at queries whose forward closest point is
+    # the FP64 optimum's (tied closest points elsewhere, see 2.).
     same = np.linalg.norm(r.point.cpu().numpy()[idx] - e["point"], axis=1) <= 1e-6
     assert same.mean() >= 0.95
-    use = same & (e["dist"] >= 0.01)
+    use = same & smooth & (e["dist"] >= 0.01)
+    assert use.mean() >= 0.8
     err = np.abs(gq[idx] - fd).max(axis=1)[use]
-    frac_bad = float((err > 1e-3).mean())
-    print(f"FD check on {use.sum()} queries: median {np.median(err):.2e}, "
-          f"p99 {np.percentile(err, 99):.2e}, max {err.max():.2e}, "
-          f"medial-axis fraction {frac_bad:.2e}")
+    print(f"FD check on {use.sum()} smooth queries: median {np.median(err):.2e}, "
+          f"p99 {np.percentile(err, 99):.2e}, max {err.max():.2e}")
     assert np.median(err) <= 1e-6
     assert np.percentile(err, 99) <= 1e-4
-    # a central difference across the medial axis (two equidistant features) is O(1)
-    assert frac_bad <= 2e-3
+    assert err.max() <= 1e-3
 
 
 def test_backward_zero_distance_and_invalid(cpq, cuda):
