@@ -259,15 +259,18 @@ def our_arm(args):
     qd = torch.from_numpy(q).to(dev)
     nq = q.shape[0]
 
-    # 4-wide BVH, leaf size (and block / short stack) autotuned on a 1M-query sample
+    # 4-wide BVH; leaf size, block size and traversal kernel autotuned on the
+    # workload's own query set (warp coherence depends on the query density)
     leaf, qopts = 4, cpq.query_opts()
     tuned = None
     if args.leaf:
         leaf = args.leaf
     elif not args.no_autotune:
-        bo, qo = cpq.autotune(vd, td_, qd[: 1 << 20].contiguous(), cache_path=None, branching=4)
+        bo, qo = cpq.autotune(vd, td_, qd, cache_path=None, branching=4)
         leaf, qopts = bo.leaf_size, qo
-        tuned = {"leaf_size": bo.leaf_size, "block_size": qo.block_size, "short_stack": qo.short_stack}
+        tuned = {"leaf_size": bo.leaf_size, "block_size": qo.block_size,
+                 "traversal": ["auto", "thread", "packet"][qo.traversal],
+                 "short_stack": qo.short_stack}
     mesh = cpq.Mesh(vd, td_, branching=4, leaf_size=leaf)
     info = mesh.info()
     ws = torch.empty(mesh.workspace_size(nq, qopts), dtype=torch.uint8, device=dev)
@@ -281,10 +284,12 @@ def our_arm(args):
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     lib.cp_timing_enable(1)
-    from ctypes import byref, c_double, c_int64
+    from ctypes import byref, c_double, c_int64, c_uint64
 
     tms, tl = c_double(), c_int64()
     lib.cp_timing_read(byref(tms), byref(tl), 1)
+    counts = (c_uint64 * 4)()
+    lib.cp_traversal_stats(counts, 1)
     launches0 = lib.cp_kernel_launches()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
@@ -298,8 +303,16 @@ def our_arm(args):
         torch.distributed.barrier()
     clk = clocks.stop()
     lib.cp_timing_read(byref(tms), byref(tl), 1)
+    lib.cp_traversal_stats(counts, 1)
     lib.cp_timing_enable(0)
     trav_ms = tms.value / max(tl.value, 1)
+    # packet kernel: per-warp node visits / triangle tests, per query of the step
+    per_q = float(nq * args.steps)
+    packet_visits = {"node_visits_per_query": counts[0] * 32 / per_q / 32,
+                     "warp_node_visits_per_32_queries": counts[0] * 32 / per_q,
+                     "warp_tri_tests_per_32_queries": counts[1] * 32 / per_q,
+                     "warp_pops_per_32_queries": counts[2] * 32 / per_q,
+                     "warp_skipped_pops_per_32_queries": counts[3] * 32 / per_q} if counts[0] else None
     if world > 1:
         m = torch.tensor([ms], device=dev)
         torch.distributed.all_reduce(m, op=torch.distributed.ReduceOp.MAX)
@@ -348,7 +361,8 @@ def our_arm(args):
                          "binary LBVH); peak = (B_io + B_trav)/t_roof",
                 "bytes_per_query": {"io": B_IO, "trav": b_trav, "v_node": v_node, "v_tri": v_tri},
                 "hbm_gbs": hbm, "l2_gbs_measured": l2_gbs,
-                "hbm_only_frac": B_IO / t_kernel / 1e9 / hbm}
+                "hbm_only_frac": B_IO / t_kernel / 1e9 / hbm,
+                "packet_counters": packet_visits}
     if rank == 0:
         res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,

@@ -230,6 +230,14 @@ CP_API cp_status cp_timing_read(double* traverse_ms, int64_t* launches, int32_t 
     return CP_SUCCESS;
 }
 
+CP_API cp_status cp_traversal_stats(uint64_t* counts4, int32_t reset) {
+    if (!counts4) return fail(CP_ERROR_INVALID_VALUE, "counts4 is NULL");
+    unsigned long long c[4];
+    CP_CUDA(traversal_stats(c, reset != 0), "traversal stats");
+    for (int k = 0; k < 4; ++k) counts4[k] = c[k];
+    return CP_SUCCESS;
+}
+
 CP_API int32_t cp_size_class(int64_t nt) {
     int32_t c = 0;
     while (nt > 1) {

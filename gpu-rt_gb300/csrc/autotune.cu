@@ -2,9 +2,10 @@
 // short-stack depth by timing real builds and queries on the caller's data.
 // The reference has no tuner; its only knobs are UI sliders that feed push
 // constants (src/gpurt.cpp:283-322, src/vk/rt.h:85-102).  Results are cached
-// in a plain text file, one line per size class and branching:
-//   <class> <branching> <leaf_size> <block_size> <short_stack> <ms>
-// where short_stack 0 stands for the warp-packet traversal.
+// in a plain text file, one line per (triangle class, query class, branching):
+//   <tri_class> <query_class> <branching> <leaf_size> <block_size> <short_stack> <ms>
+// where a class is floor(log2(count)) and short_stack 0 stands for the
+// warp-packet traversal.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -19,7 +20,7 @@
 namespace {
 
 struct Entry {
-    int cls, K, leaf, block, stack;
+    int cls, qcls, K, leaf, block, stack;
     float ms;
 };
 
@@ -31,7 +32,7 @@ std::vector<Entry> read_cache(const char* path) {
     while (std::getline(f, line)) {
         std::istringstream is(line);
         Entry e;
-        if (is >> e.cls >> e.K >> e.leaf >> e.block >> e.stack >> e.ms) out.push_back(e);
+        if (is >> e.cls >> e.qcls >> e.K >> e.leaf >> e.block >> e.stack >> e.ms) out.push_back(e);
     }
     return out;
 }
@@ -40,8 +41,8 @@ void write_cache(const char* path, const std::vector<Entry>& es) {
     if (!path) return;
     std::ofstream f(path, std::ios::trunc);
     for (const Entry& e : es)
-        f << e.cls << ' ' << e.K << ' ' << e.leaf << ' ' << e.block << ' ' << e.stack << ' ' << e.ms
-          << '\n';
+        f << e.cls << ' ' << e.qcls << ' ' << e.K << ' ' << e.leaf << ' ' << e.block << ' ' << e.stack
+          << ' ' << e.ms << '\n';
 }
 
 }  // namespace
@@ -53,6 +54,9 @@ extern "C" CP_API cp_status cp_autotune(const float* verts, int64_t nv, const in
     if (!verts || !tris || !queries || !best_build || !best_query || nv <= 0 || nt <= 0 || nq <= 0)
         return CP_ERROR_INVALID_VALUE;
     const int cls = cp_size_class(nt);
+    // query density decides how coherent a warp's queries are, so the query
+    // count is part of the size class
+    const int qcls = cp_size_class(nq);
     // a branching already set on entry (2, 4 or 8) restricts the search to it
     const int fixed_K = (best_build->branching == 2 || best_build->branching == 4 ||
                          best_build->branching == 8) ? best_build->branching : 0;
@@ -60,7 +64,7 @@ extern "C" CP_API cp_status cp_autotune(const float* verts, int64_t nv, const in
     cp_build_opts_default(best_build);
     cp_query_opts_default(best_query);
     for (const Entry& e : cache)
-        if (e.cls == cls && (fixed_K == 0 || e.K == fixed_K)) {
+        if (e.cls == cls && e.qcls == qcls && (fixed_K == 0 || e.K == fixed_K)) {
             best_build->branching = e.K;
             best_build->leaf_size = e.leaf;
             best_query->block_size = e.block;
@@ -80,7 +84,7 @@ extern "C" CP_API cp_status cp_autotune(const float* verts, int64_t nv, const in
     if (cudaMalloc(&dist, sizeof(float) * nq) != cudaSuccess ||
         cudaMalloc(&tri, sizeof(int32_t) * nq) != cudaSuccess)
         result = CP_ERROR_OUT_OF_MEMORY;
-    Entry best = {cls, 2, 4, 256, 8, 1e30f};
+    Entry best = {cls, qcls, fixed_K ? fixed_K : 2, 4, 256, 0, 1e30f};
     const int Ks[3] = {2, 4, 8};
     const int leaves[4] = {1, 2, 4, 8};
     const int blocks[2] = {128, 256};
@@ -130,7 +134,7 @@ extern "C" CP_API cp_status cp_autotune(const float* verts, int64_t nv, const in
                         break;
                     }
                     if (ms < best.ms)
-                        best = {cls, Ks[ki], leaves[li], blocks[bi], si < 3 ? stacks[si] : 0, ms};
+                        best = {cls, qcls, Ks[ki], leaves[li], blocks[bi], si < 3 ? stacks[si] : 0, ms};
                 }
             cp_mesh_destroy(mesh);
         }
@@ -148,7 +152,7 @@ extern "C" CP_API cp_status cp_autotune(const float* verts, int64_t nv, const in
     if (cache_path) {
         std::vector<Entry> out;
         for (const Entry& e : cache)
-            if (e.cls != cls || e.K != best.K) out.push_back(e);
+            if (e.cls != cls || e.qcls != qcls || e.K != best.K) out.push_back(e);
         out.push_back(best);
         write_cache(cache_path, out);
     }

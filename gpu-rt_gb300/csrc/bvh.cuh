@@ -96,6 +96,7 @@ cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int6
 // CUDA-event timing of traversal launches (diagnostic; see cp_timing_enable).
 void timing_enable(bool on);
 cudaError_t timing_read(double* ms, int64_t* launches, bool reset);
+cudaError_t traversal_stats(unsigned long long* out4, bool reset);
 
 cudaError_t bvh_backward(const Bvh& b, const float* queries, const int32_t* tri, const float* bary,
                          const float* grad_dist, int64_t nq, float* grad_q, float* grad_verts,

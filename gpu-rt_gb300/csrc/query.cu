@@ -101,11 +101,18 @@ __device__ __forceinline__ void sort_children(float (&d)[K], int (&c)[K]) {
     }
 }
 
+// max(a, b, c) in one instruction (three-input max.f32, sm_100 and later).
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 __device__ __forceinline__ float box_lb2(float qx, float qy, float qz, float lox, float hix,
                                          float loy, float hiy, float loz, float hiz) {
-    float dx = fmaxf(fmaxf(lox - qx, qx - hix), 0.0f);
-    float dy = fmaxf(fmaxf(loy - qy, qy - hiy), 0.0f);
-    float dz = fmaxf(fmaxf(loz - qz, qz - hiz), 0.0f);
+    const float dx = max3f(lox - qx, qx - hix, 0.0f);
+    const float dy = max3f(loy - qy, qy - hiy, 0.0f);
+    const float dz = max3f(loz - qz, qz - hiz, 0.0f);
     return dx * dx + dy * dy + dz * dz;
 }
 
@@ -289,6 +296,7 @@ struct TraverseArgs {
     float* out_bary;
     unsigned long long* counter;
     uint32_t* status;
+    unsigned long long* stats;  // optional: node visits, leaf triangle tests, pops, skipped pops
 };
 
 template <int K, int S>
@@ -455,7 +463,7 @@ __global__ void __launch_bounds__(256) k_traverse_packet(TraverseArgs a, int cap
     int32_t* st_ref = reinterpret_cast<int32_t*>(s_pk + (size_t)warp * 7 * cap);
     float* st_box = s_pk + (size_t)warp * 7 * cap + cap;
     const WideNode<K>* __restrict__ nodes = static_cast<const WideNode<K>*>(a.nodes);
-    const uint32_t lt_mask = (1u << lane) - 1u;
+    unsigned long long n_nodes = 0, n_tris = 0, n_pops = 0, n_skips = 0;
 
     for (;;) {
         unsigned long long base = 0;
@@ -490,6 +498,7 @@ __global__ void __launch_bounds__(256) k_traverse_packet(TraverseArgs a, int cap
             bool have = true;
             while (have) {
                 if (cur >= 0) {
+                    ++n_nodes;
                     const WideNode<K>* nd = nodes + cur;
                     float lox[K], hix[K], loy[K], hiy[K], loz[K], hiz[K];
                     int32_t ch[K];
@@ -501,13 +510,14 @@ __global__ void __launch_bounds__(256) k_traverse_packet(TraverseArgs a, int cap
                     load_row<K>(nd->hiz, hiz);
                     load_row_i<K>(nd->child, ch);
                     float lb[K];
-                    uint32_t need = 0;
+                    uint32_t mine_need = 0;
 #pragma unroll
                     for (int s = 0; s < K; ++s) {
                         lb[s] = box_lb2(qx, qy, qz, lox[s], hix[s], loy[s], hiy[s], loz[s], hiz[s]);
-                        if (__any_sync(kFull, lb[s] < lim)) need |= 1u << s;
+                        mine_need |= (lb[s] < lim ? 1u : 0u) << s;
                     }
-                    // the leader's nearest-first order, packed 4 bits per slot
+                    const uint32_t need = __reduce_or_sync(kFull, mine_need);
+                    // the leader's nearest-first order, packed 4 bits per position
                     float d[K];
                     int sl[K];
 #pragma unroll
@@ -518,63 +528,51 @@ __global__ void __launch_bounds__(256) k_traverse_packet(TraverseArgs a, int cap
                     sort_children<K>(d, sl);
                     uint32_t packed = 0;
 #pragma unroll
-                    for (int s = 0; s < K; ++s) packed |= (uint32_t)sl[s] << (4 * s);
+                    for (int t = 0; t < K; ++t) packed |= (uint32_t)sl[t] << (4 * t);
                     packed = __shfl_sync(kFull, packed, leader);
-                    // visit order restricted to needed slots; first is taken now
-                    int first_slot = -1, npush = 0;
-                    uint32_t push_mask = 0;
+                    // needed slots as a mask over visit positions
+                    uint32_t npos = 0;
 #pragma unroll
-                    for (int t = 0; t < K; ++t) {
-                        const int s = (packed >> (4 * t)) & 15;
-                        if ((need >> s) & 1u) {
-                            if (first_slot < 0) first_slot = s;
-                            else {
-                                push_mask |= 1u << s;
-                                ++npush;
+                    for (int t = 0; t < K; ++t) npos |= ((need >> ((packed >> (4 * t)) & 15)) & 1u) << t;
+                    if (npos == 0) goto pop;
+                    {
+                        const int t0 = __ffs(npos) - 1;
+                        const uint32_t pm = npos & (npos - 1);  // pushed: all but the first
+                        // lane t < K pushes visit position t; later positions go deeper
+                        if (lane < K && ((pm >> lane) & 1u)) {
+                            const int s = (packed >> (4 * lane)) & 15;
+                            int pos = sp + __popc(pm >> (lane + 1));
+                            if (pos >= cap) {  // cannot happen: cap is the depth bound
+                                atomicOr(a.status, 1u);
+                                pos = cap - 1;
                             }
-                        }
-                    }
-                    // lane j < K pushes slot j: farthest entries go deepest
-                    if (lane < K && ((push_mask >> lane) & 1u)) {
-                        int above = 0;  // pushed slots later in the visit order than mine
-                        bool seen = false;
+                            float blx = lox[0], bhx = hix[0], bly = loy[0], bhy = hiy[0];
+                            float blz = loz[0], bhz = hiz[0];
+                            int32_t c = ch[0];
 #pragma unroll
-                        for (int t = 0; t < K; ++t) {
-                            const int s = (packed >> (4 * t)) & 15;
-                            if (s == lane) seen = true;
-                            else if (seen && ((push_mask >> s) & 1u)) ++above;
+                            for (int u = 1; u < K; ++u)
+                                if (u == s) {
+                                    blx = lox[u]; bhx = hix[u]; bly = loy[u]; bhy = hiy[u];
+                                    blz = loz[u]; bhz = hiz[u]; c = ch[u];
+                                }
+                            st_ref[pos] = c;
+                            st_box[0 * cap + pos] = blx;
+                            st_box[1 * cap + pos] = bhx;
+                            st_box[2 * cap + pos] = bly;
+                            st_box[3 * cap + pos] = bhy;
+                            st_box[4 * cap + pos] = blz;
+                            st_box[5 * cap + pos] = bhz;
                         }
-                        int pos = sp + above;
-                        if (pos >= cap) {  // cannot happen: cap is the depth bound
-                            atomicOr(a.status, 1u);
-                            pos = cap - 1;
-                        }
-                        float blx = 0.f, bhx = 0.f, bly = 0.f, bhy = 0.f, blz = 0.f, bhz = 0.f;
-                        int32_t c = 0;
-#pragma unroll
-                        for (int s = 0; s < K; ++s)
-                            if (s == lane) {
-                                blx = lox[s]; bhx = hix[s]; bly = loy[s]; bhy = hiy[s];
-                                blz = loz[s]; bhz = hiz[s]; c = ch[s];
-                            }
-                        st_ref[pos] = c;
-                        st_box[0 * cap + pos] = blx;
-                        st_box[1 * cap + pos] = bhx;
-                        st_box[2 * cap + pos] = bly;
-                        st_box[3 * cap + pos] = bhy;
-                        st_box[4 * cap + pos] = blz;
-                        st_box[5 * cap + pos] = bhz;
-                    }
-                    sp = min(sp + npush, cap);
-                    __syncwarp();
-                    if (first_slot >= 0) {
+                        sp = min(sp + __popc(pm), cap);
+                        __syncwarp();
+                        const int s0 = (packed >> (4 * t0)) & 15;
                         float lbf = lb[0];
                         int32_t cf = ch[0];
 #pragma unroll
-                        for (int s = 1; s < K; ++s)
-                            if (s == first_slot) {
-                                lbf = lb[s];
-                                cf = ch[s];
+                        for (int u = 1; u < K; ++u)
+                            if (u == s0) {
+                                lbf = lb[u];
+                                cf = ch[u];
                             }
                         cur = cf;
                         leaf_active = lbf < lim;
@@ -582,6 +580,7 @@ __global__ void __launch_bounds__(256) k_traverse_packet(TraverseArgs a, int cap
                     }
                 } else {
                     const int first = leaf_first(cur), cnt = leaf_count(cur);
+                    n_tris += cnt;
                     for (int k = 0; k < cnt; ++k) {
                         const float4* rp = reinterpret_cast<const float4*>(a.recs + first + k);
                         TriRec r;
@@ -600,10 +599,12 @@ __global__ void __launch_bounds__(256) k_traverse_packet(TraverseArgs a, int cap
                     }
                     if (mine) lim = best;
                 }
+            pop:
                 // pop the next entry some lane still needs
                 have = false;
                 while (sp > 0) {
                     --sp;
+                    ++n_pops;
                     const float lb = box_lb2(qx, qy, qz, st_box[sp], st_box[cap + sp],
                                              st_box[2 * cap + sp], st_box[3 * cap + sp],
                                              st_box[4 * cap + sp], st_box[5 * cap + sp]);
@@ -614,12 +615,18 @@ __global__ void __launch_bounds__(256) k_traverse_packet(TraverseArgs a, int cap
                         have = true;
                         break;
                     }
+                    ++n_skips;
                 }
                 __syncwarp();
             }
-            (void)lt_mask;
         }
         if (valid) write_result(a, qi, qx, qy, qz, best_rec, best_idx);
+    }
+    if (a.stats && lane == 0) {
+        atomicAdd(&a.stats[0], n_nodes);
+        atomicAdd(&a.stats[1], n_tris);
+        atomicAdd(&a.stats[2], n_pops);
+        atomicAdd(&a.stats[3], n_skips);
     }
 }
 
@@ -843,6 +850,7 @@ struct TraverseTiming {
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
     double ms = 0.0;
     int64_t launches = 0;
+    unsigned long long* stats = nullptr;  // device: packet visit counters while timing is on
 };
 TraverseTiming g_timing;
 
@@ -952,6 +960,23 @@ cudaError_t launch_k(const TraverseArgs& args, const QueryParams& qp, int cap, c
 void timing_enable(bool on) {
     std::lock_guard<std::mutex> lock(g_timing.mu);
     g_timing.on = on;
+    if (on && !g_timing.stats) {
+        if (cudaMalloc(&g_timing.stats, 4 * sizeof(unsigned long long)) == cudaSuccess)
+            cudaMemset(g_timing.stats, 0, 4 * sizeof(unsigned long long));
+        else
+            g_timing.stats = nullptr;
+    }
+}
+
+cudaError_t traversal_stats(unsigned long long* out4, bool reset) {
+    std::lock_guard<std::mutex> lock(g_timing.mu);
+    for (int k = 0; k < 4; ++k) out4[k] = 0;
+    if (!g_timing.stats) return cudaSuccess;
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return e;
+    e = cudaMemcpy(out4, g_timing.stats, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && reset) e = cudaMemset(g_timing.stats, 0, 4 * sizeof(unsigned long long));
+    return e;
 }
 
 cudaError_t timing_read(double* ms, int64_t* launches, bool reset) {
@@ -1029,6 +1054,13 @@ cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int6
     args.out_bary = out_bary;
     args.counter = counter;
     args.status = b.status;
+    args.stats = nullptr;
+    {
+        cudaStreamCaptureStatus capst = cudaStreamCaptureStatusNone;
+        cudaStreamIsCapturing(st, &capst);
+        std::lock_guard<std::mutex> lock(g_timing.mu);
+        if (g_timing.on && capst == cudaStreamCaptureStatusNone) args.stats = g_timing.stats;
+    }
     switch (b.p.K) {
         case 2: return launch_k<2>(args, qp, b.stack_bound, st);
         case 4: return launch_k<4>(args, qp, b.stack_bound, st);

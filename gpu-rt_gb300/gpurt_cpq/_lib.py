@@ -64,6 +64,7 @@ SIGNATURES = {
     "cp_timing_enable": (c_int32, [c_int32]),
     "cp_timing_read": (c_int32, [POINTER(c_double), POINTER(c_int64), c_int32]),
     "cp_probe_read_bandwidth": (c_int32, [c_int64, c_int32, POINTER(c_double), c_void_p]),
+    "cp_traversal_stats": (c_int32, [POINTER(c_uint64), c_int32]),
     "cp_mesh_create": (c_int32, [c_void_p, c_int64, c_int64, c_void_p, c_int64, POINTER(BuildOpts),
                                  c_void_p, POINTER(c_void_p)]),
     "cp_mesh_refit": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p]),

@@ -144,6 +144,11 @@ CP_API uint64_t cp_kernel_launches(void);
 CP_API cp_status cp_timing_enable(int32_t on);
 CP_API cp_status cp_timing_read(double* traverse_ms, int64_t* launches, int32_t reset);
 
+/* While timing is enabled, packet traversals also count, per warp, the node
+ * visits, leaf triangle tests, stack pops and skipped pops (counts4[0..3],
+ * summed over warps).  Synchronises the device. */
+CP_API cp_status cp_traversal_stats(uint64_t* counts4, int32_t reset);
+
 /* Diagnostic: read bandwidth (GB/s) of 128-bit L2 loads over a `bytes`-sized
  * buffer, best of 5 timed launches of `reps` sweeps each.  A buffer smaller
  * than L2 (129 MB on GB300) measures L2, a larger one HBM.  Synchronous. */
@@ -289,14 +294,16 @@ CP_API cp_status cp_batch_query(cp_batch* batch, const float* queries, const int
 /* ---- autotuner ------------------------------------------------------------ */
 
 /*
- * Pick branching, leaf size, block size and short-stack depth for a mesh's
- * size class by timing candidate builds and queries on the given mesh and a
- * sample of queries (device arrays).  The winner is written to *best_build /
- * *best_query and, when cache_path is not NULL, stored in that text file
- * under the size class (one "class branching leaf block stack ms" line per
- * class and branching); a cached class is returned without timing.  If
- * best_build->branching is 2, 4 or 8 on entry, only that branching is tried.
- * Synchronous.
+ * Pick branching, leaf size, block size and traversal kernel (warp packet, or
+ * per-thread with a short-stack depth) for a size class by timing candidate
+ * builds and queries on the given mesh and queries (device arrays; pass the
+ * real query set or one of the same density: packet coherence depends on
+ * it).  The size class is (floor(log2(nt)), floor(log2(nq))).  The winner is
+ * written to *best_build / *best_query and, when cache_path is not NULL,
+ * stored in that text file (one "tri_class query_class branching leaf block
+ * stack ms" line per class pair and branching, stack 0 = packet); a cached
+ * class is returned without timing.  If best_build->branching is 2, 4 or 8 on
+ * entry, only that branching is tried.  Synchronous.
  */
 CP_API cp_status cp_autotune(const float* verts, int64_t nv, const int32_t* tris, int64_t nt,
                              const float* queries, int64_t nq, const char* cache_path,
