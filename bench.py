@@ -53,8 +53,8 @@ N_QUERIES = 16 * (1 << 20)
 B_IO = 32.0
 # canonical visit counts (binary LBVH, leaf 4) of this seeded workload, from the
 # CPU restatement on the first 65,536 queries; re-measured in the CPU leg
-CANON_V_NODE = 114.635
-CANON_V_TRI = 61.954
+CANON_V_NODE = 84.273
+CANON_V_TRI = 44.413
 # dram bytes per traversal launch from the committed ncu capture (null until measured)
 NCU_TRAFFIC_PER_QUERY = None
 

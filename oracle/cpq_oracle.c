@@ -622,10 +622,15 @@ int orc_build(const float* verts, const int64_t* vert_offsets, const int32_t* tr
                 lo[k] = s < lo[k] ? s : lo[k];
                 hi[k] = s > hi[k] ? s : hi[k];
             }
+        /* isotropic frame: one cell size, from the largest extent */
+        float emax = 0.0f;
         for (int k = 0; k < 3; ++k) {
-            float ext = hi[k] - lo[k];
-            float scale = ext > 0.0f ? cells / ext : 0.0f;
-            if (!(scale <= FLT_MAX)) scale = 0.0f;
+            float e = hi[k] - lo[k];
+            if (e > emax) emax = e;
+        }
+        float scale = emax > 0.0f ? cells / emax : 0.0f;
+        if (!(scale <= FLT_MAX)) scale = 0.0f;
+        for (int k = 0; k < 3; ++k) {
             mlo[3 * m + k] = lo[k];
             mscale[3 * m + k] = scale;
         }
