@@ -70,6 +70,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--leaf", type=int, default=0)
+    ap.add_argument("--workload", default="large",
+                    choices=["large", "torus", "batched", "dynamic", "small"],
+                    help="large is the headline; the others measure the other forms")
     return ap.parse_args()
 
 
@@ -386,12 +389,225 @@ def our_arm(args):
         torch.distributed.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# The other forms of the path (one GPU each).  These print their own JSON line;
+# the default workload above is the headline.
+
+
+def _timed(torch, fn, steps, warmup):
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def _line(metric, value, unit, ms, args, config, extra):
+    res = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)", "config": config}
+    res.update(extra)
+    emit(res)
+
+
+def torus_arm(args):
+    """Forward + adjoint on the differentiable workload vs forward alone."""
+    import torch
+
+    import gpurt_cpq as cpq
+    from gpurt_cpq import workloads as W
+
+    dev = torch.device("cuda", 0)
+    v, t, q, g = W.torus_workload()
+    vd, td, qd, gd = (torch.from_numpy(x).to(dev) for x in (v, t, q, g))
+    nq = qd.shape[0]
+    mesh = cpq.Mesh(vd, td, branching=4, leaf_size=2)
+    o = cpq.query_opts()
+    ws = torch.empty(mesh.workspace_size(nq, o), dtype=torch.uint8, device=dev)
+    out = mesh.query(qd, want_point=False, want_bary=True, workspace=ws, opts=o)
+    gv = torch.zeros_like(vd)
+
+    def fwd():
+        mesh.query(qd, want_point=False, want_bary=True, workspace=ws, opts=o, out=out)
+
+    def fwd_bwd():
+        fwd()
+        gv.zero_()
+        mesh.backward(qd, out.tri, out.bary, gd, grad_verts=gv)
+
+    ms_f = _timed(torch, fwd, args.steps, args.warmup)
+    ms_fb = _timed(torch, fwd_bwd, args.steps, args.warmup)
+    _line("closest-point fwd+bwd queries/s (torus 200k tris, 4M queries)", nq / (ms_fb * 1e-3),
+          "queries/s", ms_fb, args,
+          {"workload": "torus R=1 r=0.3 500x200 (200,000 tris), 4,194,304 queries U[-1.5,1.5]^3, "
+                       "upstream gradient N(0,1); forward caches (tri, bary), adjoint recomputes",
+           "branching": 4, "leaf_size": 2},
+          {"forward_only": {"value": nq / (ms_f * 1e-3), "ms_per_step": ms_f},
+           "fwd_bwd_over_fwd": ms_fb / ms_f, "target_fwd_bwd_over_fwd": 2.5})
+
+
+def batched_arm(args):
+    """256 uneven meshes: one batched build + one persistent graph-captured
+    launch, against plain per-mesh builds and launches on the same GPU."""
+    import torch
+
+    import gpurt_cpq as cpq
+    from gpurt_cpq import workloads as W
+
+    dev = torch.device("cuda", 0)
+    meshes, queries = W.batched()
+    V, voff, T, toff, Q, qoff = W.concat_batch(meshes, queries)
+    Vd, Td, Qd = (torch.from_numpy(x).to(dev) for x in (V, T, Q))
+    nq = Qd.shape[0]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    batch = cpq.Batch(Vd, voff, Td, toff, branching=4, leaf_size=2)
+    torch.cuda.synchronize()
+    build_batch_ms = (time.perf_counter() - t0) * 1e3
+    o = cpq.query_opts()
+    ws = torch.empty(batch.workspace_size(nq, o), dtype=torch.uint8, device=dev)
+    out = cpq.QueryResult(point=torch.empty((nq, 3), device=dev), dist=torch.empty(nq, device=dev),
+                          tri=torch.empty(nq, dtype=torch.int32, device=dev), bary=None)
+
+    def batched_step():
+        batch.query(Qd, qoff, workspace=ws, opts=o, use_graph=True, out=out)
+
+    ms_b = _timed(torch, batched_step, args.steps, args.warmup)
+    d_batched = out.dist.clone()
+    # plain per-mesh: one build and one launch sequence per mesh
+    vparts = [Vd[voff[i]:voff[i + 1]] for i in range(len(meshes))]
+    tparts = [Td[toff[i]:toff[i + 1]] for i in range(len(meshes))]
+    qparts = [Qd[qoff[i]:qoff[i + 1]] for i in range(len(meshes))]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain = [cpq.Mesh(vparts[i], tparts[i].contiguous(), branching=4, leaf_size=2)
+             for i in range(len(meshes))]
+    torch.cuda.synchronize()
+    build_plain_ms = (time.perf_counter() - t0) * 1e3
+    wss = [torch.empty(plain[i].workspace_size(qparts[i].shape[0], o), dtype=torch.uint8, device=dev)
+           for i in range(len(meshes))]
+    outs = [cpq.QueryResult(point=out.point[qoff[i]:qoff[i + 1]], dist=out.dist[qoff[i]:qoff[i + 1]],
+                            tri=out.tri[qoff[i]:qoff[i + 1]], bary=None) for i in range(len(meshes))]
+
+    def plain_step():
+        for i in range(len(meshes)):
+            plain[i].query(qparts[i], workspace=wss[i], opts=o, out=outs[i])
+
+    ms_p = _timed(torch, plain_step, args.steps, args.warmup)
+    rel = float(((out.dist - d_batched).abs() / d_batched.clamp_min(1e-30)).max())
+    tri_counts = [int(toff[i + 1] - toff[i]) for i in range(len(meshes))]
+    _line("closest-point queries/s (batched: 256 uneven meshes, one launch)", nq / (ms_b * 1e-3),
+          "queries/s", ms_b, args,
+          {"workload": f"256 deformed icospheres/tori, {int(toff[-1])} tris "
+                       f"({min(tri_counts)}..{max(tri_counts)} per mesh), {nq} queries "
+                       f"({int(np.diff(qoff).min())}..{int(np.diff(qoff).max())} per mesh)",
+           "branching": 4, "leaf_size": 2, "graph": True},
+          {"per_mesh_launches": {"value": nq / (ms_p * 1e-3), "ms_per_step": ms_p},
+           "speedup_vs_per_mesh": ms_p / ms_b, "target_speedup": 3.0,
+           "max_rel_diff_batched_vs_per_mesh": rel,
+           "build_ms": {"batched": build_batch_ms, "per_mesh_total": build_plain_ms}})
+
+
+def dynamic_arm(args):
+    """8M-triangle soup: per iteration perturb the vertices, refit, query 64M
+    fixed points and 1M moving points, adjoint on the moving points, and a
+    gradient step on their squared distance."""
+    import torch
+
+    import gpurt_cpq as cpq
+    from gpurt_cpq import workloads as W
+
+    dev = torch.device("cuda", 0)
+    v, t = W.soup()
+    vd, td = torch.from_numpy(v).to(dev), torch.from_numpy(t).to(dev)
+    qfix = torch.from_numpy(W.uniform_queries(64 * (1 << 20), 0.0, 1.0, 11)).to(dev)
+    pts = torch.from_numpy(W.uniform_queries(1 << 20, 0.0, 1.0, 12)).to(dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    mesh = cpq.Mesh(vd, td, branching=4, leaf_size=2)
+    torch.cuda.synchronize()
+    build_ms = (time.perf_counter() - t0) * 1e3
+    o = cpq.query_opts()
+    wsf = torch.empty(mesh.workspace_size(qfix.shape[0], o), dtype=torch.uint8, device=dev)
+    wsp = torch.empty(mesh.workspace_size(pts.shape[0], o), dtype=torch.uint8, device=dev)
+    outf = mesh.query(qfix, want_point=False, workspace=wsf, opts=o)
+    outp = mesh.query(pts, want_point=False, want_bary=True, workspace=wsp, opts=o)
+    gen = torch.Generator(device=dev).manual_seed(13)
+    noise = torch.empty_like(vd)
+    lr = 0.25
+
+    def iteration():
+        noise.normal_(0.0, 1e-4, generator=gen)
+        vd.add_(noise)
+        mesh.refit(vd)
+        mesh.query(qfix, want_point=False, workspace=wsf, opts=o, out=outf)
+        mesh.query(pts, want_point=False, want_bary=True, workspace=wsp, opts=o, out=outp)
+        # d(d^2)/dq = 2 d * d(d)/dq
+        gq, _ = mesh.backward(pts, outp.tri, outp.bary, 2.0 * outp.dist, need_verts=False)
+        pts.sub_(lr * gq)
+
+    iters = 50
+    for _ in range(max(1, args.warmup)):
+        iteration()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(iters):
+        iteration()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / iters
+    t0 = time.perf_counter()
+    rebuilt = cpq.Mesh(vd, td, branching=4, leaf_size=2)
+    torch.cuda.synchronize()
+    rebuild_ms = (time.perf_counter() - t0) * 1e3
+    del rebuilt
+    nq = qfix.shape[0] + pts.shape[0]
+    _line("closest-point queries/s (dynamic soup loop: refit + fwd + bwd per iteration)",
+          nq / (ms * 1e-3), "queries/s", ms, args,
+          {"workload": "4,096 Gaussian clusters x 2,048 tris (8,388,608-tri soup), vertices "
+                       "perturbed N(0,1e-4) per iteration, 67,108,864 fixed + 1,048,576 moving "
+                       "queries, 50 iterations of refit + forward + adjoint + step",
+           "branching": 4, "leaf_size": 2, "iterations": iters},
+          {"build_ms": build_ms, "rebuild_ms": rebuild_ms, "final_mean_dist":
+           float(outp.dist.mean())})
+
+
+def small_arm(args):
+    """The small CPU-runnable configuration on the GPU (binary BVH, leaf 4)."""
+    import torch
+
+    import gpurt_cpq as cpq
+    from gpurt_cpq import workloads as W
+
+    dev = torch.device("cuda", 0)
+    v, t, q = W.small()
+    vd, td, qd = (torch.from_numpy(x).to(dev) for x in (v, t, q))
+    mesh = cpq.Mesh(vd, td, branching=2, leaf_size=4)
+    o = cpq.query_opts()
+    ws = torch.empty(mesh.workspace_size(qd.shape[0], o), dtype=torch.uint8, device=dev)
+    out = mesh.query(qd, workspace=ws, opts=o)
+    ms = _timed(torch, lambda: mesh.query(qd, workspace=ws, opts=o, out=out), args.steps, args.warmup)
+    _line("closest-point queries/s (small: icosphere 5,120 tris, 65,536 queries)",
+          qd.shape[0] / (ms * 1e-3), "queries/s", ms, args,
+          {"workload": "icosphere level 4, 65,536 queries U[-2,2]^3", "branching": 2, "leaf_size": 4},
+          {})
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         reference_arm(args)
-    else:
+    elif args.workload == "large":
         our_arm(args)
+    else:
+        {"torus": torus_arm, "batched": batched_arm, "dynamic": dynamic_arm,
+         "small": small_arm}[args.workload](args)
 
 
 if __name__ == "__main__":

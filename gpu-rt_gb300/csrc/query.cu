@@ -456,7 +456,7 @@ __device__ __forceinline__ void write_result(const TraverseArgs& a, int64_t qi, 
 // cannot overflow.  Lanes of different meshes in one chunk (batches) are
 // served one mesh at a time.
 template <int K>
-__global__ void __launch_bounds__(256, 4) k_traverse_packet(TraverseArgs a, int cap) {
+__global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(TraverseArgs a, int cap) {
     extern __shared__ float s_pk[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     // per warp: ref[cap] then lo x, hi x, lo y, hi y, lo z, hi z [cap] each

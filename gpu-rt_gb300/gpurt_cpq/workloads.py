@@ -238,7 +238,9 @@ def concat_batch(meshes, queries):
 def soup(seed: int = 5, clusters: int = 4096, per: int = 2048, sigma: float = 0.01):
     """Triangle soup: each triangle has 3 own vertices drawn around its cluster centre."""
     rng = np.random.default_rng(seed)
-    centres = rng.random((clusters, 3))
-    v = np.repeat(centres, per * 3, axis=0) + rng.normal(0.0, sigma, (clusters * per * 3, 3))
+    centres = rng.random((clusters, 3)).astype(np.float32)
+    v = rng.standard_normal((clusters, per * 3, 3), dtype=np.float32)
+    v *= np.float32(sigma)
+    v += centres[:, None, :]
     tris = np.arange(clusters * per * 3, dtype=np.int32).reshape(-1, 3)
-    return v.astype(np.float32), tris
+    return v.reshape(-1, 3), tris
