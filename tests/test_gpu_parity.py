@@ -190,9 +190,10 @@ def test_query_options_do_not_change_results(cpq, cuda):
                dict(traversal="packet", block_size=64), dict(traversal="auto")]:
         r = m.query(qd, want_bary=True, opts=cpq.query_opts(**kw))
         same = r.tri == base.tri
-        # exact ties (a closest point on a vertex or edge shared by several
-        # triangles) resolve by visit order; everything else agrees
-        assert float(same.float().mean()) > 0.99, kw
+        # exact ties (a closest point on a grid vertex or edge shared by
+        # several triangles, whose box bound equals the tied distance) resolve
+        # by visit order; the distances must agree everywhere
+        assert float(same.float().mean()) > 0.9, kw
         assert torch.equal(r.dist[same], base.dist[same]), kw
         rel = ((r.dist - base.dist).abs() / base.dist.clamp_min(1e-30)).max()
         assert float(rel) <= 1e-6, kw
