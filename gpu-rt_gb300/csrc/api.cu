@@ -19,6 +19,7 @@
 
 #include "../../include/cpq.h"
 #include "bvh.cuh"
+#include "handles.cuh"
 
 using namespace cpq;
 
@@ -26,10 +27,6 @@ namespace cpq {
 static std::atomic<uint64_t> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 }  // namespace cpq
-
-struct cp_mesh {
-    Bvh bvh;
-};
 
 struct cp_batch {
     Bvh bvh;
@@ -180,6 +177,13 @@ cp_status build_common(Bvh& b, const float* verts, int64_t vstride_bytes, const 
 }
 
 }  // namespace
+
+namespace cpq {
+cp_status parse_query_opts(const cp_query_opts* opts, QueryParams* out) {
+    return to_query_params(opts, out);
+}
+cp_status set_error(cp_status s, const std::string& msg) { return fail(s, msg); }
+}  // namespace cpq
 
 extern "C" {
 

@@ -84,6 +84,7 @@ struct QueryParams {
     int blocks_per_sm = 0;
     int short_stack = 8;
     int traversal = 0;  // 0 auto (packet when sorted), 1 per-thread, 2 warp packet
+    bool no_timing = false;  // never create timing events, even when cp_timing_enable is on
 };
 
 size_t query_workspace_bytes(const Bvh& b, int64_t nq, const QueryParams& qp);

@@ -855,7 +855,8 @@ struct TraverseTiming {
 TraverseTiming g_timing;
 
 template <int K, int S>
-cudaError_t launch_traverse(const TraverseArgs& args, int block, int blocks_per_sm, cudaStream_t st) {
+cudaError_t launch_traverse(const TraverseArgs& args, int block, int blocks_per_sm, cudaStream_t st,
+                            bool allow_timing) {
     const size_t smem = (size_t)S * block * sizeof(float2);
     auto kern = k_traverse<K, S>;
     int dev = 0, sms = 0;
@@ -875,7 +876,7 @@ cudaError_t launch_traverse(const TraverseArgs& args, int block, int blocks_per_
     bool timed = false;
     {
         std::lock_guard<std::mutex> lock(g_timing.mu);
-        timed = g_timing.on;
+        timed = g_timing.on && allow_timing;
     }
     cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
     cudaStreamIsCapturing(st, &cap);
@@ -898,7 +899,7 @@ cudaError_t launch_traverse(const TraverseArgs& args, int block, int blocks_per_
 
 template <int K>
 cudaError_t launch_packet(const TraverseArgs& args, int cap, int block, int blocks_per_sm,
-                          cudaStream_t st) {
+                          cudaStream_t st, bool allow_timing) {
     if (cap < 1) cap = 1;
     const size_t smem = (size_t)(block / 32) * 7 * cap * sizeof(float);
     auto kern = k_traverse_packet<K>;
@@ -921,7 +922,7 @@ cudaError_t launch_packet(const TraverseArgs& args, int cap, int block, int bloc
     bool timed = false;
     {
         std::lock_guard<std::mutex> lock(g_timing.mu);
-        timed = g_timing.on;
+        timed = g_timing.on && allow_timing;
     }
     cudaStreamCaptureStatus capst = cudaStreamCaptureStatusNone;
     cudaStreamIsCapturing(st, &capst);
@@ -947,11 +948,12 @@ cudaError_t launch_k(const TraverseArgs& args, const QueryParams& qp, int cap, c
     // packet traversal needs spatially coherent warps: the default whenever
     // the queries are walked in Morton order
     const bool packet = qp.traversal == 2 || (qp.traversal == 0 && qp.sort);
-    if (packet) return launch_packet<K>(args, cap, qp.block, qp.blocks_per_sm, st);
+    const bool allow_timing = !qp.no_timing;
+    if (packet) return launch_packet<K>(args, cap, qp.block, qp.blocks_per_sm, st, allow_timing);
     switch (qp.short_stack) {
-        case 4: return launch_traverse<K, 4>(args, qp.block, qp.blocks_per_sm, st);
-        case 16: return launch_traverse<K, 16>(args, qp.block, qp.blocks_per_sm, st);
-        default: return launch_traverse<K, 8>(args, qp.block, qp.blocks_per_sm, st);
+        case 4: return launch_traverse<K, 4>(args, qp.block, qp.blocks_per_sm, st, allow_timing);
+        case 16: return launch_traverse<K, 16>(args, qp.block, qp.blocks_per_sm, st, allow_timing);
+        default: return launch_traverse<K, 8>(args, qp.block, qp.blocks_per_sm, st, allow_timing);
     }
 }
 
@@ -1059,7 +1061,8 @@ cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int6
         cudaStreamCaptureStatus capst = cudaStreamCaptureStatusNone;
         cudaStreamIsCapturing(st, &capst);
         std::lock_guard<std::mutex> lock(g_timing.mu);
-        if (g_timing.on && capst == cudaStreamCaptureStatusNone) args.stats = g_timing.stats;
+        if (g_timing.on && !qp.no_timing && capst == cudaStreamCaptureStatusNone)
+            args.stats = g_timing.stats;
     }
     switch (b.p.K) {
         case 2: return launch_k<2>(args, qp, b.stack_bound, st);

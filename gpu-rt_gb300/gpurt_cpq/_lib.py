@@ -76,6 +76,9 @@ SIGNATURES = {
                            c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "cp_query_host": (c_int32, [c_void_p, c_void_p, c_int64, POINTER(QueryOpts), c_void_p, c_void_p,
                                 c_void_p, c_void_p, c_void_p]),
+    "cp_query_noalloc": (c_int32, [c_void_p, c_void_p, c_int64, POINTER(QueryOpts), c_void_p,
+                                   c_void_p, c_void_p, c_void_p, c_void_p]),
+    "cp_query_noalloc_scratch_bytes": (c_size_t, []),
     "cp_backward": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p,
                               c_void_p, c_void_p]),
     "cp_batch_create": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, POINTER(BuildOpts),

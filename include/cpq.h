@@ -232,6 +232,31 @@ CP_API cp_status cp_query_host(const cp_mesh* mesh, const float* queries, int64_
                                int32_t* out_tri, float* out_bary, cp_stream_t stream);
 
 /*
+ * cp_query for callers that must not allocate device memory while they run:
+ * a render or simulation loop that forbids allocation after start-up (an
+ * allocation can synchronise the device and stall a frame), a plugin whose
+ * host owns all device memory, or code running while its own allocator holds
+ * a lock.  Same arguments and results as cp_query, minus the workspace: the
+ * scratch comes from a fixed 32 MiB device array inside the library
+ * (cp_query_noalloc_scratch_bytes), which each GPU that loads the library
+ * holds until the process exits.  That is enough for 1,048,576 queries per
+ * call with sort_queries on (any count with it off); larger calls return
+ * CP_ERROR_SCRATCH_TOO_SMALL with a message and launch nothing.  The call
+ * makes no cudaMalloc / cudaFree and no other allocation.  The first call on
+ * a device looks up the array's device address (cudaGetSymbolAddress with
+ * that device current), so make that first call before any stream capture.
+ * All calls share the one array: calls that overlap on the GPU (other
+ * streams, other threads) race and give wrong results — keep them ordered on
+ * one stream.  This entry point has no counterpart in the reference.
+ */
+CP_API cp_status cp_query_noalloc(const cp_mesh* mesh, const float* queries, int64_t nq,
+                                  const cp_query_opts* opts, float* out_point, float* out_dist,
+                                  int32_t* out_tri, float* out_bary, cp_stream_t stream);
+
+/* Size in bytes of cp_query_noalloc's fixed scratch array. */
+CP_API size_t cp_query_noalloc_scratch_bytes(void);
+
+/*
  * Adjoint of the unsigned distance.  For each query i with upstream gradient
  * g_i = grad_dist[i], closest triangle t = tri[i] and barycentrics b = bary[i]:
  *   grad_queries[i]  = g_i (q_i - p_i) / d_i           (written; may be NULL)
