@@ -9,6 +9,7 @@
 // (MacDonald and Booth 1990).  The reference's counterpart is the closed
 // driver build behind VK::Accel::recreate (src/vk/vulkan.cpp:881-936); its
 // only box vocabulary is BBox::enclose / surface_area (src/lib/bbox.h:35-59).
+#include <algorithm>
 #include <cfloat>
 #include <cstring>
 
@@ -77,29 +78,44 @@ __global__ void k_centroid_bounds(const float* __restrict__ verts, int64_t strid
                                   const int64_t* __restrict__ voff,
                                   const int64_t* __restrict__ toff, int nmeshes,
                                   float* __restrict__ csum, float* __restrict__ mbox) {
-    int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    bool valid = t < nt;
-    int m = 0;
-    float s[3] = {0.f, 0.f, 0.f};
-    if (valid) {
-        m = nmeshes > 1 ? mesh_of(toff, nmeshes, t) : 0;
-        int64_t vb = voff[m];
-        float3 a = load_vert(verts, stride, vb + tris[3 * t + 0]);
-        float3 b = load_vert(verts, stride, vb + tris[3 * t + 1]);
-        float3 c = load_vert(verts, stride, vb + tris[3 * t + 2]);
-        s[0] = __fadd_rn(__fadd_rn(a.x, b.x), c.x);
-        s[1] = __fadd_rn(__fadd_rn(a.y, b.y), c.y);
-        s[2] = __fadd_rn(__fadd_rn(a.z, b.z), c.z);
+    // Each block owns a contiguous chunk; a thread keeps a running box and
+    // flushes it with atomics only when the mesh changes and at the end (min
+    // and max are exact, so any reduction order gives the same bounds).
+    const int64_t per_block = (nt + gridDim.x - 1) / gridDim.x;
+    const int64_t b0 = (int64_t)blockIdx.x * per_block;
+    const int64_t b1 = min(nt, b0 + per_block);
+    int cur = -1;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int64_t t = b0 + threadIdx.x; t < b1; t += blockDim.x) {
+        const int m = nmeshes > 1 ? mesh_of(toff, nmeshes, t) : 0;
+        const int64_t vb = voff[m];
+        const float3 a = load_vert(verts, stride, vb + tris[3 * t + 0]);
+        const float3 b = load_vert(verts, stride, vb + tris[3 * t + 1]);
+        const float3 c = load_vert(verts, stride, vb + tris[3 * t + 2]);
+        const float s[3] = {__fadd_rn(__fadd_rn(a.x, b.x), c.x), __fadd_rn(__fadd_rn(a.y, b.y), c.y),
+                            __fadd_rn(__fadd_rn(a.z, b.z), c.z)};
         csum[3 * t + 0] = s[0];
         csum[3 * t + 1] = s[1];
         csum[3 * t + 2] = s[2];
+        if (m != cur) {
+            if (cur >= 0)
+                for (int k = 0; k < 3; ++k) {
+                    atomic_min_f(&mbox[6 * cur + k], lo[k]);
+                    atomic_max_f(&mbox[6 * cur + 3 + k], hi[k]);
+                }
+            cur = m;
+            lo[0] = lo[1] = lo[2] = INFINITY;
+            hi[0] = hi[1] = hi[2] = -INFINITY;
+        }
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = fminf(lo[k], s[k]);
+            hi[k] = fmaxf(hi[k], s[k]);
+        }
     }
-    // min/max are exact, so any reduction order gives the same bounds
     const unsigned full = 0xffffffffu;
-    int m0 = __shfl_sync(full, m, 0);
-    bool uniform = __all_sync(full, valid && m == m0);
-    if (uniform) {
-        float lo[3] = {s[0], s[1], s[2]}, hi[3] = {s[0], s[1], s[2]};
+    const int c0 = __shfl_sync(full, cur, 0);
+    if (__all_sync(full, cur == c0)) {
+        if (c0 < 0) return;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
@@ -109,13 +125,13 @@ __global__ void k_centroid_bounds(const float* __restrict__ verts, int64_t strid
             }
         if ((threadIdx.x & 31) == 0)
             for (int k = 0; k < 3; ++k) {
-                atomic_min_f(&mbox[6 * m + k], lo[k]);
-                atomic_max_f(&mbox[6 * m + 3 + k], hi[k]);
+                atomic_min_f(&mbox[6 * c0 + k], lo[k]);
+                atomic_max_f(&mbox[6 * c0 + 3 + k], hi[k]);
             }
-    } else if (valid) {
+    } else if (cur >= 0) {
         for (int k = 0; k < 3; ++k) {
-            atomic_min_f(&mbox[6 * m + k], s[k]);
-            atomic_max_f(&mbox[6 * m + 3 + k], s[k]);
+            atomic_min_f(&mbox[6 * cur + k], lo[k]);
+            atomic_max_f(&mbox[6 * cur + 3 + k], hi[k]);
         }
     }
 }
@@ -639,7 +655,8 @@ cudaError_t bvh_build(Bvh& b, const float* verts, int64_t vstride, const int32_t
         return cudaSuccess;
     }
     k_init_boxes<<<grid_for(6 * nm), kThreads, 0, st>>>(mbox, 6 * nm); note_launch();
-    k_centroid_bounds<<<grid_for(n), kThreads, 0, st>>>(verts, vstride, b.tris, n, b.d_voff,
+    k_centroid_bounds<<<(unsigned)std::min<int64_t>((n + 2047) / 2048, 1216), kThreads, 0, st>>>(
+        verts, vstride, b.tris, n, b.d_voff,
                                                        b.d_toff, nm, csum, mbox); note_launch();
     CK(cudaGetLastError());
     k_build_frames<<<grid_for(nm), kThreads, 0, st>>>(mbox, nm, (float)(1u << bits), lo_scale); note_launch();

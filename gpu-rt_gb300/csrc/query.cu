@@ -19,6 +19,7 @@
 #include <mutex>
 #include <utility>
 #include <vector>
+#include <algorithm>
 
 #include "bvh.cuh"
 #include "sort.cuh"
@@ -663,25 +664,43 @@ __global__ void k_init_qbounds(float* __restrict__ qb, int nmeshes) {
     if (i < 6 * nmeshes) qb[i] = (i % 6) < 3 ? INFINITY : -INFINITY;
 }
 
-// Per-mesh bounding box of the finite query points (warp-reduced atomics).
-__global__ void k_query_bounds(const float* __restrict__ q, int64_t nq,
-                               const int64_t* __restrict__ qoff, int nmeshes,
-                               float* __restrict__ qb) {
-    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = i < nq;
-    float p[3] = {0.f, 0.f, 0.f};
-    bool fin = false;
-    int m = 0;
-    if (valid) {
-        p[0] = q[3 * i];
-        p[1] = q[3 * i + 1];
-        p[2] = q[3 * i + 2];
-        fin = isfinite(p[0]) && isfinite(p[1]) && isfinite(p[2]);
-        m = nmeshes > 1 ? mesh_of(qoff, nmeshes, i) : 0;
+// Per-mesh bounding box of the finite query points.  Each block reduces one
+// contiguous chunk; a thread keeps a running box and flushes it with atomics
+// only when the mesh changes and at the end (warp-reduced when the warp's
+// lanes agree on the mesh), so a 16M-query call issues a few thousand atomics
+// rather than one set per warp of queries.
+__device__ __forceinline__ void flush_box(float* __restrict__ qb, int m, const float* lo,
+                                          const float* hi) {
+    for (int k = 0; k < 3; ++k) {
+        atomic_min_pos(&qb[6 * m + k], lo[k]);
+        atomic_max_pos(&qb[6 * m + 3 + k], hi[k]);
     }
-    const int m0 = __shfl_sync(kFull, m, 0);
-    if (__all_sync(kFull, valid && fin && m == m0)) {
-        float lo[3] = {p[0], p[1], p[2]}, hi[3] = {p[0], p[1], p[2]};
+}
+
+__global__ void __launch_bounds__(256) k_query_bounds(const float* __restrict__ q, int64_t nq,
+                                                      const int64_t* __restrict__ qoff, int nmeshes,
+                                                      float* __restrict__ qb) {
+    const int64_t per_block = (nq + gridDim.x - 1) / gridDim.x;
+    const int64_t b0 = (int64_t)blockIdx.x * per_block;
+    const int64_t b1 = min(nq, b0 + per_block);
+    int cur = -1;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int64_t i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
+        const float x = q[3 * i], y = q[3 * i + 1], z = q[3 * i + 2];
+        if (!(isfinite(x) && isfinite(y) && isfinite(z))) continue;
+        const int m = nmeshes > 1 ? mesh_of(qoff, nmeshes, i) : 0;
+        if (m != cur) {
+            if (cur >= 0) flush_box(qb, cur, lo, hi);
+            cur = m;
+            lo[0] = lo[1] = lo[2] = INFINITY;
+            hi[0] = hi[1] = hi[2] = -INFINITY;
+        }
+        lo[0] = fminf(lo[0], x); lo[1] = fminf(lo[1], y); lo[2] = fminf(lo[2], z);
+        hi[0] = fmaxf(hi[0], x); hi[1] = fmaxf(hi[1], y); hi[2] = fmaxf(hi[2], z);
+    }
+    const int c0 = __shfl_sync(kFull, cur, 0);
+    if (__all_sync(kFull, cur == c0)) {
+        if (c0 < 0) return;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
@@ -689,16 +708,9 @@ __global__ void k_query_bounds(const float* __restrict__ q, int64_t nq,
                 lo[k] = fminf(lo[k], __shfl_xor_sync(kFull, lo[k], o));
                 hi[k] = fmaxf(hi[k], __shfl_xor_sync(kFull, hi[k], o));
             }
-        if ((threadIdx.x & 31) == 0)
-            for (int k = 0; k < 3; ++k) {
-                atomic_min_pos(&qb[6 * m + k], lo[k]);
-                atomic_max_pos(&qb[6 * m + 3 + k], hi[k]);
-            }
-    } else if (valid && fin) {
-        for (int k = 0; k < 3; ++k) {
-            atomic_min_pos(&qb[6 * m + k], p[k]);
-            atomic_max_pos(&qb[6 * m + 3 + k], p[k]);
-        }
+        if ((threadIdx.x & 31) == 0) flush_box(qb, c0, lo, hi);
+    } else if (cur >= 0) {
+        flush_box(qb, cur, lo, hi);
     }
 }
 
@@ -1027,7 +1039,9 @@ cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int6
         const int qbits = (64 - b.mesh_bits) / 3 < 10 ? (64 - b.mesh_bits) / 3 : 10;
         float* frame = reinterpret_cast<float*>(w + L.frame);
         k_init_qbounds<<<(unsigned)((6 * b.nmeshes + 255) / 256), 256, 0, st>>>(frame, b.nmeshes); note_launch();
-        k_query_bounds<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(queries, nq, d_qoff, b.nmeshes,
+        // ~8 blocks per SM of 152, each over a contiguous chunk of >= 4096 queries
+        const unsigned bgrid = (unsigned)std::min<int64_t>((nq + 4095) / 4096, 1216);
+        k_query_bounds<<<bgrid, 256, 0, st>>>(queries, nq, d_qoff, b.nmeshes,
                                                                      frame); note_launch();
         k_query_frame<<<(unsigned)((b.nmeshes + 255) / 256), 256, 0, st>>>(frame, b.nmeshes,
                                                                            (float)(1u << qbits)); note_launch();
