@@ -8,7 +8,7 @@
 // the Voronoi-region method (Ericson 2005, section 5.1.5).
 //
 // Kernel shape (GB300, 152 SMs): a persistent grid of SMs x resident blocks;
-// each warp takes 32 consecutive (Morton-ordered) queries from a global
+// each warp takes 32 consecutive (Hilbert-ordered) queries from a global
 // counter, one query per lane, and leaves when the counter runs past the end
 // (warp-uniform exit).  Each thread keeps the top `S` entries of its stack in
 // shared memory (a ring in a per-warp slice, [slot][thread] so a warp's
@@ -447,7 +447,7 @@ __device__ __forceinline__ void write_result(const TraverseArgs& a, int64_t qi, 
 }
 
 // Warp-packet traversal.  The 32 lanes of a warp hold 32 consecutive queries
-// of the Morton order (neighbours in space) and walk ONE shared stack: a
+// of the Hilbert order (neighbours in space) and walk ONE shared stack: a
 // child is visited when any lane's box lower bound beats that lane's best, so
 // every node row is a single broadcast load and node tests run with all
 // lanes converged.  The child order is the first pending lane's nearest-first
@@ -631,22 +631,59 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
     }
 }
 
+// Index of cell (x, y, z) along the 3D Hilbert curve of 2^bits cells per axis
+// (Skilling 2004, "Programming the Hilbert curve": undo the excess rotations
+// and reflections level by level, Gray-encode, then read the transposed
+// coordinates out bit-interleaved).  Consecutive indices are face-adjacent
+// cells, unlike Morton order, which jumps at every octant boundary; a warp
+// of 32 consecutive queries is therefore a tighter cluster, and the next
+// warp's cluster lies next to it.
+__device__ __forceinline__ uint64_t hilbert3(uint32_t x, uint32_t y, uint32_t z, int bits) {
+    uint32_t X[3] = {x, y, z};
+    const uint32_t top = 1u << (bits - 1);
+    for (uint32_t Q = top; Q > 1; Q >>= 1) {
+        const uint32_t P = Q - 1;
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            if (X[i] & Q) {
+                X[0] ^= P;
+            } else {
+                const uint32_t t = (X[0] ^ X[i]) & P;
+                X[0] ^= t;
+                X[i] ^= t;
+            }
+        }
+    }
+    X[1] ^= X[0];
+    X[2] ^= X[1];
+    uint32_t t = 0;
+    for (uint32_t Q = top; Q > 1; Q >>= 1)
+        if (X[2] & Q) t ^= Q - 1;
+    X[0] ^= t;
+    X[1] ^= t;
+    X[2] ^= t;
+    return (spread3(X[0]) << 2) | (spread3(X[1]) << 1) | spread3(X[2]);
+}
+
+// Ordering key of each query: its mesh in the high bits, then the Hilbert
+// index of its cell in the mesh's isotropic query frame.
+template <typename KeyT>
 __global__ void k_query_keys(const float* __restrict__ q, int64_t nq, const int64_t* __restrict__ qoff,
                              int nmeshes, const float* __restrict__ frame, int qbits,
-                             uint64_t* __restrict__ keys, int32_t* __restrict__ vals) {
+                             KeyT* __restrict__ keys, int32_t* __restrict__ vals) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nq) return;
     const int m = nmeshes > 1 ? mesh_of(qoff, nmeshes, i) : 0;
     const float* f = frame + 6 * m;
     const float maxcell = (float)((1u << qbits) - 1u);
-    uint64_t code = 0;
+    uint32_t c[3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
         float t = (q[3 * i + k] - f[k]) * f[3 + k];
         t = fminf(fmaxf(t, 0.0f), maxcell);  // NaN -> 0
-        code |= spread3((uint32_t)t) << (2 - k);
+        c[k] = (uint32_t)t;
     }
-    keys[i] = ((uint64_t)m << (3 * qbits)) | code;
+    keys[i] = (KeyT)(((uint64_t)m << (3 * qbits)) | hilbert3(c[0], c[1], c[2], qbits));
     vals[i] = (int32_t)i;
 }
 
@@ -958,7 +995,7 @@ cudaError_t launch_packet(const TraverseArgs& args, int cap, int block, int bloc
 template <int K>
 cudaError_t launch_k(const TraverseArgs& args, const QueryParams& qp, int cap, cudaStream_t st) {
     // packet traversal needs spatially coherent warps: the default whenever
-    // the queries are walked in Morton order
+    // the queries are walked in Hilbert order
     const bool packet = qp.traversal == 2 || (qp.traversal == 0 && qp.sort);
     const bool allow_timing = !qp.no_timing;
     if (packet) return launch_packet<K>(args, cap, qp.block, qp.blocks_per_sm, st, allow_timing);
@@ -1045,13 +1082,27 @@ cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int6
                                                                      frame); note_launch();
         k_query_frame<<<(unsigned)((b.nmeshes + 255) / 256), 256, 0, st>>>(frame, b.nmeshes,
                                                                            (float)(1u << qbits)); note_launch();
-        k_query_keys<<<(unsigned)((nq + 255) / 256), 256, 0, st>>>(queries, nq, d_qoff, b.nmeshes,
-                                                                   frame, qbits, keys, vals); note_launch();
-        e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
+        const int key_bits = 3 * qbits + b.mesh_bits;
+        const unsigned kgrid = (unsigned)((nq + 255) / 256);
         bool in_alt = false;
-        e = radix_sort_pairs<uint64_t>(keys, vals, keys_alt, vals_alt, nq, 0, 3 * qbits + b.mesh_bits,
-                                       w + L.sort_ws, L.sort_ws_bytes, st, &in_alt);
+        if (key_bits <= 32) {
+            // 32-bit keys (a single mesh: 30 bits) move a third less data per sort pass
+            uint32_t* k32 = reinterpret_cast<uint32_t*>(keys);
+            uint32_t* k32_alt = reinterpret_cast<uint32_t*>(keys_alt);
+            k_query_keys<uint32_t><<<kgrid, 256, 0, st>>>(queries, nq, d_qoff, b.nmeshes, frame, qbits,
+                                                          k32, vals); note_launch();
+            e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+            e = radix_sort_pairs<uint32_t>(k32, vals, k32_alt, vals_alt, nq, 0, key_bits,
+                                           w + L.sort_ws, L.sort_ws_bytes, st, &in_alt);
+        } else {
+            k_query_keys<uint64_t><<<kgrid, 256, 0, st>>>(queries, nq, d_qoff, b.nmeshes, frame, qbits,
+                                                          keys, vals); note_launch();
+            e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+            e = radix_sort_pairs<uint64_t>(keys, vals, keys_alt, vals_alt, nq, 0, key_bits,
+                                           w + L.sort_ws, L.sort_ws_bytes, st, &in_alt);
+        }
         if (e != cudaSuccess) return e;
         perm = in_alt ? vals_alt : vals;
     }

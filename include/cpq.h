@@ -85,14 +85,14 @@ typedef struct cp_build_opts {
 
 typedef struct cp_query_opts {
     int32_t block_size;     /* traversal threads per block: 64..1024, multiple of 32; 0 = default */
-    int32_t sort_queries;   /* 1: walk the queries in Morton order of their position (outputs keep input order) */
+    int32_t sort_queries;   /* 1: walk the queries along a Hilbert curve through their positions (outputs keep input order) */
     int32_t blocks_per_sm;  /* persistent grid = SM count x this; 0 = from occupancy */
     int32_t short_stack;    /* per-thread stack entries kept in shared memory: 4, 8 or 16; 0 = default */
     int32_t traversal;      /* CP_TRAVERSAL_*: how lanes share work */
 } cp_query_opts;
 
 /* Traversal kernels.  PACKET: the 32 lanes of a warp take 32 consecutive
- * (Morton-ordered, so neighbouring) queries and walk one shared stack, a node
+ * (Hilbert-ordered, so neighbouring) queries and walk one shared stack, a node
  * being visited when any lane still needs it; THREAD: every lane walks its
  * own query with its own stack.  AUTO picks PACKET when sort_queries is set. */
 #define CP_TRAVERSAL_AUTO   0
