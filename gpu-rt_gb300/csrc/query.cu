@@ -79,6 +79,33 @@ __device__ __forceinline__ void cswap(float& a, float& b, int& x, int& y) {
     }
 }
 
+// Ascending sorting networks on packed unsigned keys: an exchange is one
+// integer min and one max.
+__device__ __forceinline__ void kswap(uint32_t& a, uint32_t& b) {
+    const uint32_t lo = min(a, b), hi = max(a, b);
+    a = lo;
+    b = hi;
+}
+template <int K>
+__device__ __forceinline__ void sort_keys(uint32_t (&k)[K]) {
+    if constexpr (K == 2) {
+        kswap(k[0], k[1]);
+    } else if constexpr (K == 4) {
+        kswap(k[0], k[1]); kswap(k[2], k[3]);
+        kswap(k[0], k[2]); kswap(k[1], k[3]);
+        kswap(k[1], k[2]);
+    } else {
+        kswap(k[0], k[1]); kswap(k[2], k[3]); kswap(k[4], k[5]); kswap(k[6], k[7]);
+        kswap(k[0], k[2]); kswap(k[1], k[3]); kswap(k[4], k[6]); kswap(k[5], k[7]);
+        kswap(k[1], k[2]); kswap(k[5], k[6]);
+        kswap(k[0], k[4]); kswap(k[3], k[7]);
+        kswap(k[1], k[5]); kswap(k[2], k[6]);
+        kswap(k[1], k[4]); kswap(k[3], k[6]);
+        kswap(k[2], k[4]); kswap(k[3], k[5]);
+        kswap(k[3], k[4]);
+    }
+}
+
 // Ascending sorting networks (2: 1 exchange, 4: 5, 8: 19).
 template <int K>
 __device__ __forceinline__ void sort_children(float (&d)[K], int (&c)[K]) {
@@ -460,9 +487,10 @@ template <int K>
 __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(TraverseArgs a, int cap) {
     extern __shared__ float s_pk[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    // per warp: ref[cap] then lo x, hi x, lo y, hi y, lo z, hi z [cap] each
-    int32_t* st_ref = reinterpret_cast<int32_t*>(s_pk + (size_t)warp * 7 * cap);
-    float* st_box = s_pk + (size_t)warp * 7 * cap + cap;
+    // per warp: ref[cap], then every lane's own box bound of each entry,
+    // [entry][lane] so a warp's access is one conflict-free row
+    int32_t* st_ref = reinterpret_cast<int32_t*>(s_pk + (size_t)warp * 33 * cap);
+    float* st_lb = s_pk + (size_t)warp * 33 * cap + cap + lane;
     const WideNode<K>* __restrict__ nodes = static_cast<const WideNode<K>*>(a.nodes);
     unsigned long long n_nodes = 0, n_tris = 0, n_pops = 0, n_skips = 0;
 
@@ -518,18 +546,16 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                         mine_need |= (lb[s] < lim ? 1u : 0u) << s;
                     }
                     const uint32_t need = __reduce_or_sync(kFull, mine_need);
-                    // the leader's nearest-first order, packed 4 bits per position
-                    float d[K];
-                    int sl[K];
+                    // the leader's nearest-first order: sort (bound bits | slot)
+                    // as unsigned keys (non-negative floats order as their bit
+                    // patterns), then pack the slots 4 bits per position
+                    uint32_t key[K];
 #pragma unroll
-                    for (int s = 0; s < K; ++s) {
-                        d[s] = lb[s];
-                        sl[s] = s;
-                    }
-                    sort_children<K>(d, sl);
+                    for (int s = 0; s < K; ++s) key[s] = (__float_as_uint(lb[s]) & ~7u) | (uint32_t)s;
+                    sort_keys<K>(key);
                     uint32_t packed = 0;
 #pragma unroll
-                    for (int t = 0; t < K; ++t) packed |= (uint32_t)sl[t] << (4 * t);
+                    for (int t = 0; t < K; ++t) packed |= (key[t] & 7u) << (4 * t);
                     packed = __shfl_sync(kFull, packed, leader);
                     // needed slots as a mask over visit positions
                     uint32_t npos = 0;
@@ -539,30 +565,28 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                     {
                         const int t0 = __ffs(npos) - 1;
                         const uint32_t pm = npos & (npos - 1);  // pushed: all but the first
-                        // lane t < K pushes visit position t; later positions go deeper
-                        if (lane < K && ((pm >> lane) & 1u)) {
-                            const int s = (packed >> (4 * lane)) & 15;
-                            int pos = sp + __popc(pm >> (lane + 1));
-                            if (pos >= cap) {  // cannot happen: cap is the depth bound
-                                atomicOr(a.status, 1u);
-                                pos = cap - 1;
-                            }
-                            float blx = lox[0], bhx = hix[0], bly = loy[0], bhy = hiy[0];
-                            float blz = loz[0], bhz = hiz[0];
-                            int32_t c = ch[0];
+                        // every lane stores its own bound of each pushed child;
+                        // later visit positions go deeper
 #pragma unroll
-                            for (int u = 1; u < K; ++u)
-                                if (u == s) {
-                                    blx = lox[u]; bhx = hix[u]; bly = loy[u]; bhy = hiy[u];
-                                    blz = loz[u]; bhz = hiz[u]; c = ch[u];
+                        for (int t = 0; t < K; ++t) {
+                            if ((pm >> t) & 1u) {
+                                const int s = (packed >> (4 * t)) & 15;
+                                int pos = sp + __popc(pm >> (t + 1));
+                                if (pos >= cap) {  // cannot happen: cap is the depth bound
+                                    atomicOr(a.status, 1u);
+                                    pos = cap - 1;
                                 }
-                            st_ref[pos] = c;
-                            st_box[0 * cap + pos] = blx;
-                            st_box[1 * cap + pos] = bhx;
-                            st_box[2 * cap + pos] = bly;
-                            st_box[3 * cap + pos] = bhy;
-                            st_box[4 * cap + pos] = blz;
-                            st_box[5 * cap + pos] = bhz;
+                                float ls = lb[0];
+                                int32_t c = ch[0];
+#pragma unroll
+                                for (int u = 1; u < K; ++u)
+                                    if (u == s) {
+                                        ls = lb[u];
+                                        c = ch[u];
+                                    }
+                                st_lb[pos * 32] = ls;
+                                if (lane == 0) st_ref[pos] = c;
+                            }
                         }
                         sp = min(sp + __popc(pm), cap);
                         __syncwarp();
@@ -606,10 +630,7 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                 while (sp > 0) {
                     --sp;
                     ++n_pops;
-                    const float lb = box_lb2(qx, qy, qz, st_box[sp], st_box[cap + sp],
-                                             st_box[2 * cap + sp], st_box[3 * cap + sp],
-                                             st_box[4 * cap + sp], st_box[5 * cap + sp]);
-                    const bool want = lb < lim;
+                    const bool want = st_lb[sp * 32] < lim;
                     if (__any_sync(kFull, want)) {
                         cur = st_ref[sp];
                         leaf_active = want;
@@ -950,7 +971,7 @@ template <int K>
 cudaError_t launch_packet(const TraverseArgs& args, int cap, int block, int blocks_per_sm,
                           cudaStream_t st, bool allow_timing) {
     if (cap < 1) cap = 1;
-    const size_t smem = (size_t)(block / 32) * 7 * cap * sizeof(float);
+    const size_t smem = (size_t)(block / 32) * 33 * cap * sizeof(float);
     auto kern = k_traverse_packet<K>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
