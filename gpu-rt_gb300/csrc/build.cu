@@ -278,6 +278,31 @@ __device__ __forceinline__ uint32_t degenerate_flag(float3 a, float3 b, float3 c
     return (nn > __fmul_rn(1e-10f, __fmul_rn(lab, lac))) ? 0u : kTriDegenerate;
 }
 
+__device__ __forceinline__ FastTri make_fast_tri(float3 a, float3 b, float3 c, int32_t local,
+                                                 bool degenerate) {
+    const float abx = b.x - a.x, aby = b.y - a.y, abz = b.z - a.z;
+    const float acx = c.x - a.x, acy = c.y - a.y, acz = c.z - a.z;
+    const float bcx = c.x - b.x, bcy = c.y - b.y, bcz = c.z - b.z;
+    const float aa = abx * abx + aby * aby + abz * abz;
+    const float cc = acx * acx + acy * acy + acz * acz;
+    const float bb = abx * acx + aby * acy + abz * acz;
+    const float ee = bcx * bcx + bcy * bcy + bcz * bcz;
+    float g0 = __int_as_float(0x7fc00000), g1 = g0, g2 = g0;  // NaN: never inside
+    if (!degenerate) {
+        const float inv_det = 1.0f / (aa * cc - bb * bb);
+        g0 = cc * inv_det;
+        g1 = bb * inv_det;
+        g2 = aa * inv_det;
+    }
+    FastTri f;
+    f.p0 = make_float4(a.x, a.y, a.z, abx);
+    f.p1 = make_float4(aby, abz, acx, acy);
+    f.p2 = make_float4(acz, g0, g1, g2);
+    f.p3 = make_float4(aa > 0.0f ? 1.0f / aa : 0.0f, cc > 0.0f ? 1.0f / cc : 0.0f,
+                       ee > 0.0f ? 1.0f / ee : 0.0f, __int_as_float(local));
+    return f;
+}
+
 // Leaf boxes + triangle records, then the bottom-up walk: the second thread
 // to reach a node merges its children (min/max are order-free; SAH costs use
 // only the children's values), so the result does not depend on scheduling.
@@ -291,8 +316,8 @@ __global__ void k_refit(const float* __restrict__ verts, int64_t stride,
                         const int32_t* __restrict__ first, const int32_t* __restrict__ last,
                         float* box, float* cost, uint8_t* __restrict__ leaf_flag,
                         uint32_t* __restrict__ arrive, TriRec* __restrict__ recs,
-                        int32_t* __restrict__ inv_order, int leaf_size, int collapse,
-                        float c_node, float c_tri) {
+                        FastTri* __restrict__ fast, int32_t* __restrict__ inv_order,
+                        int leaf_size, int collapse, float c_node, float c_tri) {
     int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int32_t t = order[k];
@@ -306,8 +331,10 @@ __global__ void k_refit(const float* __restrict__ verts, int64_t stride,
     TriRec r;
     r.p0 = make_float4(a.x, a.y, a.z, b.x);
     r.p1 = make_float4(b.y, b.z, c.x, c.y);
-    r.p2 = make_float4(c.z, __int_as_float(local), __uint_as_float(degenerate_flag(a, b, c)), 0.0f);
+    const uint32_t degenerate = degenerate_flag(a, b, c);
+    r.p2 = make_float4(c.z, __int_as_float(local), __uint_as_float(degenerate), 0.0f);
     recs[k] = r;
+    fast[k] = make_fast_tri(a, b, c, local, degenerate != 0);
     if (kBuild) inv_order[t] = (int32_t)k;
 
     const int64_t node = n - 1 + k;
@@ -609,6 +636,7 @@ cudaError_t bvh_build(Bvh& b, const float* verts, int64_t vstride, const int32_t
     CK(dalloc(b, &b.wide_root, (size_t)nm));
     CK(dalloc(b, &b.frame, (size_t)6 * nm));
     CK(dalloc(b, &b.recs, (size_t)n));
+    CK(dalloc(b, &b.fast, (size_t)n));
     CK(dalloc(b, &b.status, (size_t)64));
 
     CK(cudaMemcpyAsync(b.tris, tris, sizeof(int32_t) * 3 * n, cudaMemcpyDeviceToDevice, st));
@@ -700,7 +728,7 @@ cudaError_t bvh_build(Bvh& b, const float* verts, int64_t vstride, const int32_t
     k_refit<true><<<grid_for(n), kThreads, 0, st>>>(
         verts, vstride, b.tris, b.order, b.keys, n, b.d_voff, b.d_toff, nm, key_shift, b.left,
         b.right, b.parent, b.first, b.last, b.box, b.cost, b.leaf_flag, b.arrive, b.recs,
-        b.inv_order, p.leaf_size, p.collapse, p.c_node, p.c_tri); note_launch();
+        b.fast, b.inv_order, p.leaf_size, p.collapse, p.c_node, p.c_tri); note_launch();
     CK(cudaGetLastError());
     int32_t* max_depth = reinterpret_cast<int32_t*>(scratch + 1);
     k_wide_flags<<<grid_for(nn), kThreads, 0, st>>>(n, b.keys, nm, key_shift, b.parent, b.first,
@@ -769,7 +797,7 @@ cudaError_t bvh_refit(Bvh& b, const float* verts, int64_t vstride, cudaStream_t 
     k_refit<false><<<grid_for(n), kThreads, 0, st>>>(
         verts, vstride, b.tris, b.order, b.keys, n, b.d_voff, b.d_toff, b.nmeshes, key_shift,
         b.left, b.right, b.parent, b.first, b.last, b.box, b.cost, b.leaf_flag, b.arrive, b.recs,
-        b.inv_order, b.p.leaf_size, b.p.collapse, b.p.c_node, b.p.c_tri); note_launch();
+        b.fast, b.inv_order, b.p.leaf_size, b.p.collapse, b.p.c_node, b.p.c_tri); note_launch();
     CK(cudaGetLastError());
     const int64_t slots = b.num_wide * b.p.K;
     switch (b.p.K) {

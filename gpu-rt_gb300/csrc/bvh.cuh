@@ -33,7 +33,8 @@ struct Bvh {
 
     // traversal data
     void* nodes = nullptr;          // WideNode<K>[num_wide]
-    TriRec* recs = nullptr;         // nt triangle records in leaf order
+    TriRec* recs = nullptr;         // nt triangle records in leaf order (exact vertices)
+    FastTri* fast = nullptr;        // nt distance-test records in leaf order
     int32_t* wide_root = nullptr;   // nmeshes
     float* frame = nullptr;         // nmeshes x 6: query Morton frame (lo xyz, scale xyz)
 

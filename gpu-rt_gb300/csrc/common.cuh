@@ -42,6 +42,16 @@ struct alignas(16) TriRec {
     float4 p0, p1, p2;
 };
 
+// 64-byte record for the traversal's distance test, in the same (leaf) order
+// as TriRec: {a.xyz ab.x} {ab.yz ac.xy} {ac.z G0 G1 G2} {1/|ab|^2 1/|ac|^2
+// 1/|bc|^2 idx}.  (G0, G1, G2) is the inverse Gram matrix of (ab, ac) up to
+// the shared determinant, so the plane projection's barycentrics are
+// v = G0 (ab.ap) - G1 (ac.ap), w = G2 (ac.ap) - G1 (ab.ap); zero-area
+// triangles store NaN there (never "inside").  Zero-length edges store 0.
+struct alignas(16) FastTri {
+    float4 p0, p1, p2, p3;
+};
+
 __host__ __device__ inline int32_t pack_leaf(int32_t first, int32_t count) {
     return ~((first << kLeafShift) | (count - 1));
 }

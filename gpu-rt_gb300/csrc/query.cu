@@ -144,68 +144,45 @@ __device__ __forceinline__ float box_lb2(float qx, float qy, float qz, float lox
     return dx * dx + dy * dy + dz * dz;
 }
 
-// FP32 squared distance to a triangle record (traversal test).  Voronoi
-// regions; the difference vector is measured from the vertex owning the
-// region so near-surface queries keep their small distances accurate.
-__device__ __forceinline__ float tri_d2(float qx, float qy, float qz, const TriRec& r) {
-    const float ax = r.p0.x, ay = r.p0.y, az = r.p0.z;
-    const float bx = r.p0.w, by = r.p1.x, bz = r.p1.y;
-    const float cx = r.p1.z, cy = r.p1.w, cz = r.p2.x;
-    const float abx = bx - ax, aby = by - ay, abz = bz - az;
-    const float acx = cx - ax, acy = cy - ay, acz = cz - az;
-    const float apx = qx - ax, apy = qy - ay, apz = qz - az;
-    float rx, ry, rz;
-    if (__float_as_uint(r.p2.z) & kTriDegenerate) {
-        // closest of the three edges
-        float best = FLT_MAX;
-        const float px[3] = {ax, bx, ax}, py[3] = {ay, by, ay}, pz[3] = {az, bz, az};
-        const float ex[3] = {abx, cx - bx, acx}, ey[3] = {aby, cy - by, acy}, ez[3] = {abz, cz - bz, acz};
-#pragma unroll
-        for (int e = 0; e < 3; ++e) {
-            float wx = qx - px[e], wy = qy - py[e], wz = qz - pz[e];
-            float l = ex[e] * ex[e] + ey[e] * ey[e] + ez[e] * ez[e];
-            float t = l > 0.0f ? __saturatef((wx * ex[e] + wy * ey[e] + wz * ez[e]) / l) : 0.0f;
-            wx -= t * ex[e]; wy -= t * ey[e]; wz -= t * ez[e];
-            best = fminf(best, wx * wx + wy * wy + wz * wz);
-        }
-        return best;
-    }
-    const float d1 = abx * apx + aby * apy + abz * apz;
-    const float d2 = acx * apx + acy * apy + acz * apz;
-    if (d1 <= 0.0f && d2 <= 0.0f) {
-        rx = apx; ry = apy; rz = apz;
-    } else {
-        const float bpx = qx - bx, bpy = qy - by, bpz = qz - bz;
-        const float d3 = abx * bpx + aby * bpy + abz * bpz;
-        const float d4 = acx * bpx + acy * bpy + acz * bpz;
-        const float cpx = qx - cx, cpy = qy - cy, cpz = qz - cz;
-        const float d5 = abx * cpx + aby * cpy + abz * cpz;
-        const float d6 = acx * cpx + acy * cpy + acz * cpz;
-        const float vc = d1 * d4 - d3 * d2;
-        const float vb = d5 * d2 - d1 * d6;
-        const float va = d3 * d6 - d5 * d4;
-        if (d3 >= 0.0f && d4 <= d3) {
-            rx = bpx; ry = bpy; rz = bpz;
-        } else if (vc <= 0.0f && d1 >= 0.0f && d3 <= 0.0f) {
-            const float v = __fdividef(d1, d1 - d3);
-            rx = apx - v * abx; ry = apy - v * aby; rz = apz - v * abz;
-        } else if (d6 >= 0.0f && d5 <= d6) {
-            rx = cpx; ry = cpy; rz = cpz;
-        } else if (vb <= 0.0f && d2 >= 0.0f && d6 <= 0.0f) {
-            const float w = __fdividef(d2, d2 - d6);
-            rx = apx - w * acx; ry = apy - w * acy; rz = apz - w * acz;
-        } else if (va <= 0.0f && (d4 - d3) >= 0.0f && (d5 - d6) >= 0.0f) {
-            const float w = __fdividef(d4 - d3, (d4 - d3) + (d5 - d6));
-            rx = bpx - w * (cx - bx); ry = bpy - w * (cy - by); rz = bpz - w * (cz - bz);
-        } else {
-            const float inv = __fdividef(1.0f, va + vb + vc);
-            const float v = vb * inv, w = vc * inv;
-            rx = apx - (v * abx + w * acx);
-            ry = apy - (v * aby + w * acy);
-            rz = apz - (v * abz + w * acz);
-        }
-    }
-    return rx * rx + ry * ry + rz * rz;
+// Branch-free squared distance for the traversal, on a FastTri record.  If
+// the plane projection's barycentrics lie inside the triangle the answer is
+// the plane residual; otherwise the closest point is on the boundary, so it
+// is the nearest of the three edge segments (each clamped with a saturating
+// multiply).  Nearly all work is FMA-pipe arithmetic, and lanes that test the
+// same triangle from different Voronoi regions do not diverge.
+__device__ __forceinline__ float tri_d2_fast(float qx, float qy, float qz, const FastTri& f) {
+    const float apx = qx - f.p0.x, apy = qy - f.p0.y, apz = qz - f.p0.z;
+    const float abx = f.p0.w, aby = f.p1.x, abz = f.p1.y;
+    const float acx = f.p1.z, acy = f.p1.w, acz = f.p2.x;
+    const float dab = abx * apx + aby * apy + abz * apz;
+    const float dac = acx * apx + acy * apy + acz * apz;
+    // edge ab
+    const float tab = __saturatef(dab * f.p3.x);
+    float rx = apx - tab * abx, ry = apy - tab * aby, rz = apz - tab * abz;
+    float d2 = rx * rx + ry * ry + rz * rz;
+    // edge ac
+    const float tac = __saturatef(dac * f.p3.y);
+    rx = apx - tac * acx;
+    ry = apy - tac * acy;
+    rz = apz - tac * acz;
+    d2 = fminf(d2, rx * rx + ry * ry + rz * rz);
+    // edge bc, from b
+    const float bpx = apx - abx, bpy = apy - aby, bpz = apz - abz;
+    const float bcx = acx - abx, bcy = acy - aby, bcz = acz - abz;
+    const float tbc = __saturatef((bcx * bpx + bcy * bpy + bcz * bpz) * f.p3.z);
+    rx = bpx - tbc * bcx;
+    ry = bpy - tbc * bcy;
+    rz = bpz - tbc * bcz;
+    d2 = fminf(d2, rx * rx + ry * ry + rz * rz);
+    // face: barycentrics of the plane projection
+    const float v = f.p2.y * dab - f.p2.z * dac;
+    const float w = f.p2.w * dac - f.p2.z * dab;
+    rx = apx - (v * abx + w * acx);
+    ry = apy - (v * aby + w * acy);
+    rz = apz - (v * abz + w * acz);
+    const float d2f = rx * rx + ry * ry + rz * rz;
+    const bool inside = v >= 0.0f && w >= 0.0f && v + w <= 1.0f;  // false for NaN
+    return inside ? d2f : d2;
 }
 
 // Degenerate triangle in FP32 with barycentrics (weights of b and c).
@@ -311,7 +288,8 @@ __device__ void precise_closest(float qx, float qy, float qz, const TriRec& r, f
 
 struct TraverseArgs {
     const void* nodes;
-    const TriRec* recs;
+    const TriRec* recs;   // exact vertices: the winner's re-evaluation
+    const FastTri* fast;  // distance-test records, same order
     const int32_t* wide_root;
     const int64_t* qoff;
     int nmeshes;
@@ -393,13 +371,14 @@ __global__ void __launch_bounds__(256) k_traverse(TraverseArgs a) {
             } else {
                 const int first = leaf_first(cur), cnt = leaf_count(cur);
                 for (int k = 0; k < cnt; ++k) {
-                    const float4* rp = reinterpret_cast<const float4*>(a.recs + first + k);
-                    TriRec r;
-                    r.p0 = __ldg(rp);
-                    r.p1 = __ldg(rp + 1);
-                    r.p2 = __ldg(rp + 2);
-                    const float d2 = tri_d2(qx, qy, qz, r);
-                    const int idx = __float_as_int(r.p2.y);
+                    const float4* fp = reinterpret_cast<const float4*>(a.fast + first + k);
+                    FastTri f;
+                    f.p0 = __ldg(fp);
+                    f.p1 = __ldg(fp + 1);
+                    f.p2 = __ldg(fp + 2);
+                    f.p3 = __ldg(fp + 3);
+                    const float d2 = tri_d2_fast(qx, qy, qz, f);
+                    const int idx = __float_as_int(f.p3.w);
                     if (d2 < best || (d2 == best && idx < best_idx)) {
                         best = d2;
                         best_rec = first + k;
@@ -607,14 +586,15 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                     const int first = leaf_first(cur), cnt = leaf_count(cur);
                     n_tris += cnt;
                     for (int k = 0; k < cnt; ++k) {
-                        const float4* rp = reinterpret_cast<const float4*>(a.recs + first + k);
-                        TriRec r;
-                        r.p0 = __ldg(rp);
-                        r.p1 = __ldg(rp + 1);
-                        r.p2 = __ldg(rp + 2);
+                        const float4* fp = reinterpret_cast<const float4*>(a.fast + first + k);
+                        FastTri f;
+                        f.p0 = __ldg(fp);
+                        f.p1 = __ldg(fp + 1);
+                        f.p2 = __ldg(fp + 2);
+                        f.p3 = __ldg(fp + 3);
                         if (leaf_active) {
-                            const float d2 = tri_d2(qx, qy, qz, r);
-                            const int idx = __float_as_int(r.p2.y);
+                            const float d2 = tri_d2_fast(qx, qy, qz, f);
+                            const int idx = __float_as_int(f.p3.w);
                             if (d2 < best || (d2 == best && idx < best_idx)) {
                                 best = d2;
                                 best_rec = first + k;
@@ -1130,6 +1110,7 @@ cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int6
     TraverseArgs args;
     args.nodes = b.nodes;
     args.recs = b.recs;
+    args.fast = b.fast;
     args.wide_root = b.wide_root;
     args.qoff = d_qoff;
     args.nmeshes = b.nmeshes;
