@@ -525,59 +525,49 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                         mine_need |= (lb[s] < lim ? 1u : 0u) << s;
                     }
                     const uint32_t need = __reduce_or_sync(kFull, mine_need);
-                    // the leader's nearest-first order: sort (bound bits | slot)
-                    // as unsigned keys (non-negative floats order as their bit
-                    // patterns), then pack the slots 4 bits per position
-                    uint32_t key[K];
-#pragma unroll
-                    for (int s = 0; s < K; ++s) key[s] = (__float_as_uint(lb[s]) & ~7u) | (uint32_t)s;
-                    sort_keys<K>(key);
-                    uint32_t packed = 0;
-#pragma unroll
-                    for (int t = 0; t < K; ++t) packed |= (key[t] & 7u) << (4 * t);
-                    packed = __shfl_sync(kFull, packed, leader);
-                    // needed slots as a mask over visit positions
-                    uint32_t npos = 0;
-#pragma unroll
-                    for (int t = 0; t < K; ++t) npos |= ((need >> ((packed >> (4 * t)) & 15)) & 1u) << t;
-                    if (npos == 0) goto pop;
+                    if (need == 0) goto pop;
                     {
-                        const int t0 = __ffs(npos) - 1;
-                        const uint32_t pm = npos & (npos - 1);  // pushed: all but the first
-                        // every lane stores its own bound of each pushed child;
-                        // later visit positions go deeper
+                        // The leader's nearest-first order of the needed
+                        // children: sort (bound bits | slot) as unsigned keys
+                        // (non-negative floats order as their bit patterns),
+                        // unneeded children last, so the needed ones take
+                        // positions 0 .. cnt-1.  Broadcast each slot's position
+                        // (4 bits per slot).
+                        const int cnt = __popc(need);
+                        uint32_t key[K];
 #pragma unroll
-                        for (int t = 0; t < K; ++t) {
-                            if ((pm >> t) & 1u) {
-                                const int s = (packed >> (4 * t)) & 15;
-                                int pos = sp + __popc(pm >> (t + 1));
-                                if (pos >= cap) {  // cannot happen: cap is the depth bound
-                                    atomicOr(a.status, 1u);
-                                    pos = cap - 1;
-                                }
-                                float ls = lb[0];
-                                int32_t c = ch[0];
+                        for (int s = 0; s < K; ++s)
+                            key[s] = ((need >> s) & 1u) ? ((__float_as_uint(lb[s]) & ~7u) | (uint32_t)s)
+                                                        : (0xFFFFFFF8u | (uint32_t)s);
+                        sort_keys<K>(key);
+                        uint32_t inv = 0;
 #pragma unroll
-                                for (int u = 1; u < K; ++u)
-                                    if (u == s) {
-                                        ls = lb[u];
-                                        c = ch[u];
-                                    }
-                                st_lb[pos * 32] = ls;
-                                if (lane == 0) st_ref[pos] = c;
-                            }
-                        }
-                        sp = min(sp + __popc(pm), cap);
-                        __syncwarp();
-                        const int s0 = (packed >> (4 * t0)) & 15;
+                        for (int t = 0; t < K; ++t) inv |= (uint32_t)t << (4 * (key[t] & 7u));
+                        inv = __shfl_sync(kFull, inv, leader);
+                        // position 0 is taken now; every lane stores its own
+                        // bound of the others, the farthest deepest
                         float lbf = lb[0];
                         int32_t cf = ch[0];
+                        const int top = min(sp + cnt - 1, cap);  // cap is the depth bound
 #pragma unroll
-                        for (int u = 1; u < K; ++u)
-                            if (u == s0) {
-                                lbf = lb[u];
-                                cf = ch[u];
+                        for (int s = 0; s < K; ++s) {
+                            if ((need >> s) & 1u) {
+                                const int pos = (int)((inv >> (4 * s)) & 15u);
+                                if (pos == 0) {
+                                    lbf = lb[s];
+                                    cf = ch[s];
+                                } else {
+                                    const int at = top - pos;
+                                    if (at >= 0) {
+                                        st_lb[at * 32] = lb[s];
+                                        if (lane == 0) st_ref[at] = ch[s];
+                                    }
+                                }
                             }
+                        }
+                        if (sp + cnt - 1 > cap) atomicOr(a.status, 1u);  // cannot happen
+                        sp = top;
+                        __syncwarp();
                         cur = cf;
                         leaf_active = lbf < lim;
                         continue;
