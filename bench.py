@@ -55,14 +55,16 @@ B_IO = 32.0
 # CPU restatement on the first 65,536 queries; re-measured in the CPU leg
 CANON_V_NODE = 84.273
 CANON_V_TRI = 44.413
-# dram bytes per traversal launch from the committed ncu capture (null until measured)
-NCU_TRAFFIC_PER_QUERY = None
+# DRAM bytes (read + write) per query of one traversal launch, from the ncu
+# capture summarised in profiles/k_traverse_packet_large_heightfield.md
+# (5.914 GB for 16,777,216 queries, leaf 2)
+NCU_TRAFFIC_PER_QUERY = 352.5
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=60)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=1 << 21,
@@ -97,7 +99,7 @@ def cpu_model() -> str:
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+    """nvidia-smi clocks / throttle reasons sampled every 100 ms while running."""
 
     FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -109,7 +111,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(gpu_index), f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
