@@ -12,7 +12,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <tuple>
 #include <new>
 #include <string>
 #include <vector>
@@ -26,6 +28,67 @@ using namespace cpq;
 namespace cpq {
 static std::atomic<uint64_t> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+namespace {
+struct KernelCache {
+    std::mutex mu;
+    std::map<std::pair<const void*, int>, size_t> smem_limit;                   // (kernel, device)
+    std::map<std::tuple<const void*, int, int, size_t>, int> occupancy;  // + block, smem
+    std::map<int, int> sms;
+};
+KernelCache& kernel_cache() {
+    static KernelCache c;
+    return c;
+}
+}  // namespace
+
+cudaError_t sm_count(int* out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    KernelCache& c = kernel_cache();
+    std::lock_guard<std::mutex> lock(c.mu);
+    auto it = c.sms.find(dev);
+    if (it == c.sms.end()) {
+        int n = 0;
+        e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
+        it = c.sms.emplace(dev, n).first;
+    }
+    *out = it->second;
+    return cudaSuccess;
+}
+
+cudaError_t ensure_smem_limit(const void* kernel, size_t smem) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    KernelCache& c = kernel_cache();
+    std::lock_guard<std::mutex> lock(c.mu);
+    size_t& have = c.smem_limit[{kernel, dev}];
+    if (have >= smem) return cudaSuccess;
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) have = smem;
+    return e;
+}
+
+cudaError_t blocks_per_sm(const void* kernel, int block, size_t smem, int* out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    KernelCache& c = kernel_cache();
+    std::lock_guard<std::mutex> lock(c.mu);
+    auto key = std::make_tuple(kernel, dev, block, smem);
+    auto it = c.occupancy.find(key);
+    if (it == c.occupancy.end()) {
+        int n = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, block, smem);
+        if (e != cudaSuccess) return e;
+        it = c.occupancy.emplace(key, n < 1 ? 1 : n).first;
+    }
+    *out = it->second;
+    return cudaSuccess;
+}
 }  // namespace cpq
 
 struct cp_batch {

@@ -28,6 +28,15 @@ constexpr uint32_t kTriDegenerate = 1u;   // TriRec flags: zero-area triangle
 // Host side: count one kernel launch of this library (cp_kernel_launches).
 void note_launch();
 
+// Host side, cached per device and kernel: raise the kernel's dynamic
+// shared-memory limit to at least `smem` (the runtime call is made only when
+// the cached limit is lower), and the kernel's resident blocks per SM for a
+// block size and shared-memory size.  Keeps per-query host work free of
+// runtime calls that could wait for the device.
+cudaError_t ensure_smem_limit(const void* kernel, size_t smem);
+cudaError_t blocks_per_sm(const void* kernel, int block, size_t smem, int* out);
+cudaError_t sm_count(int* out);
+
 template <int K>
 struct alignas(16) WideNode {
     float lox[K], hix[K], loy[K], hiy[K], loz[K], hiz[K];

@@ -9,14 +9,23 @@
 
 namespace {
 
+// Four independent 128-bit loads in flight per thread per iteration.
 __global__ void __launch_bounds__(256) k_probe_read(const float4* __restrict__ buf, int64_t n4,
                                                     int reps, float* __restrict__ sink) {
     float acc = 0.0f;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     for (int r = 0; r < reps; ++r) {
-        for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += stride) {
-            const float4 v = __ldcg(buf + i);  // L2, not L1
-            acc += v.x + v.y + v.z + v.w;
+        int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+        for (; i + 3 * stride < n4; i += 4 * stride) {
+            const float4 v0 = __ldcg(buf + i);  // L2, not L1
+            const float4 v1 = __ldcg(buf + i + stride);
+            const float4 v2 = __ldcg(buf + i + 2 * stride);
+            const float4 v3 = __ldcg(buf + i + 3 * stride);
+            acc += (v0.x + v1.y) + (v2.z + v3.w);
+        }
+        for (; i < n4; i += stride) {
+            const float4 v = __ldcg(buf + i);
+            acc += v.x;
         }
     }
     if (acc == 1234.5f) sink[0] = acc;  // keeps the loads alive
@@ -40,22 +49,25 @@ extern "C" CP_API cp_status cp_probe_read_bandwidth(int64_t bytes, int32_t reps,
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaMemsetAsync(buf, 0, n4 * 16, st);
-    const unsigned grid = (unsigned)sms * 8;
-    k_probe_read<<<grid, 256, 0, st>>>(buf, n4, 2, sink);  // warm: brings the buffer into L2
-    cpq::note_launch();
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
+    // best over 4, 8 and 16 resident blocks per SM, 5 timed launches each
     float best_ms = 1e30f;
-    for (int t = 0; t < 5; ++t) {
-        cudaEventRecord(e0, st);
-        k_probe_read<<<grid, 256, 0, st>>>(buf, n4, reps, sink);
+    for (int per_sm = 4; per_sm <= 16; per_sm *= 2) {
+        const unsigned grid = (unsigned)sms * per_sm;
+        k_probe_read<<<grid, 256, 0, st>>>(buf, n4, 2, sink);  // warm: brings the buffer into L2
         cpq::note_launch();
-        cudaEventRecord(e1, st);
-        cudaEventSynchronize(e1);
-        float ms = 0.0f;
-        cudaEventElapsedTime(&ms, e0, e1);
-        if (ms < best_ms) best_ms = ms;
+        for (int t = 0; t < 5; ++t) {
+            cudaEventRecord(e0, st);
+            k_probe_read<<<grid, 256, 0, st>>>(buf, n4, reps, sink);
+            cpq::note_launch();
+            cudaEventRecord(e1, st);
+            cudaEventSynchronize(e1);
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best_ms) best_ms = ms;
+        }
     }
     cudaError_t e = cudaGetLastError();
     cudaEventDestroy(e0);

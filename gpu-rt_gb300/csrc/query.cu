@@ -899,15 +899,12 @@ cudaError_t launch_traverse(const TraverseArgs& args, int block, int blocks_per_
                             bool allow_timing) {
     const size_t smem = (size_t)S * block * sizeof(float2);
     auto kern = k_traverse<K, S>;
-    int dev = 0, sms = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int sms = 0;
+    cudaError_t e = sm_count(&sms);
     if (e != cudaSuccess) return e;
     if (blocks_per_sm <= 0) {
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, block, smem);
+        e = cpq::blocks_per_sm(reinterpret_cast<const void*>(kern), block, smem, &blocks_per_sm);
         if (e != cudaSuccess) return e;
-        if (blocks_per_sm < 1) blocks_per_sm = 1;
     }
     int64_t grid = (int64_t)sms * blocks_per_sm;
     const int64_t need = (args.nq + 31) / 32 * 32 / block + 1;
@@ -943,17 +940,14 @@ cudaError_t launch_packet(const TraverseArgs& args, int cap, int block, int bloc
     if (cap < 1) cap = 1;
     const size_t smem = (size_t)(block / 32) * 33 * cap * sizeof(float);
     auto kern = k_traverse_packet<K>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaError_t e = ensure_smem_limit(reinterpret_cast<const void*>(kern), smem);
     if (e != cudaSuccess) return e;
-    int dev = 0, sms = 0;
-    e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return e;
-    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int sms = 0;
+    e = sm_count(&sms);
     if (e != cudaSuccess) return e;
     if (blocks_per_sm <= 0) {
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, block, smem);
+        e = cpq::blocks_per_sm(reinterpret_cast<const void*>(kern), block, smem, &blocks_per_sm);
         if (e != cudaSuccess) return e;
-        if (blocks_per_sm < 1) blocks_per_sm = 1;
     }
     int64_t grid = (int64_t)sms * blocks_per_sm;
     const int64_t need = ((args.nq + 31) / 32 * 32 + block - 1) / block;

@@ -294,9 +294,7 @@ cudaError_t radix_sort_pairs(KeyT* keys, int32_t* vals, KeyT* keys_alt, int32_t*
     if (workspace_bytes < radix_sort_workspace_bytes(n)) return cudaErrorInvalidValue;
     const size_t smem = scatter_smem_bytes<KeyT>();
     {
-        // per-context function attribute; cheap, and legal while a stream captures
-        cudaError_t e = cudaFuncSetAttribute(k_scatter<KeyT>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e = ensure_smem_limit(reinterpret_cast<const void*>(k_scatter<KeyT>), smem);
         if (e != cudaSuccess) return e;
     }
     const int tiles = (int)ceil_div(n, kTile);

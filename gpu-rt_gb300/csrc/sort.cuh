@@ -12,6 +12,10 @@ namespace cpq {
 // Host side: count one kernel launch of this library (defined in api.cu).
 void note_launch();
 
+// Host side: raise a kernel's dynamic shared-memory limit once per device
+// (defined in api.cu).
+cudaError_t ensure_smem_limit(const void* kernel, size_t smem);
+
 // Bytes of workspace radix_sort_pairs needs for n keys.
 size_t radix_sort_workspace_bytes(int64_t n);
 
