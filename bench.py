@@ -259,7 +259,7 @@ def our_arm(args):
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
     import gpurt_cpq as cpq
-    from gpurt_cpq._lib import lib
+    from gpurt_cpq._lib import CP_TIMING_COUNTERS, CP_TIMING_EVENTS, lib
 
     v, t, q = workload()
     vd = torch.from_numpy(v).to(dev)
@@ -291,13 +291,11 @@ def our_arm(args):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
-    lib.cp_timing_enable(1)
+    lib.cp_timing_enable(CP_TIMING_EVENTS)
     from ctypes import byref, c_double, c_int64, c_uint64
 
     tms, tl = c_double(), c_int64()
     lib.cp_timing_read(byref(tms), byref(tl), 1)
-    counts = (c_uint64 * 4)()
-    lib.cp_traversal_stats(counts, 1)
     launches0 = lib.cp_kernel_launches()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
@@ -311,11 +309,16 @@ def our_arm(args):
         torch.distributed.barrier()
     clk = clocks.stop()
     lib.cp_timing_read(byref(tms), byref(tl), 1)
+    trav_ms = tms.value / max(tl.value, 1)
+    # packet kernel: per-warp node visits / triangle tests, from one more
+    # (untimed) query through the counting build of the kernel
+    counts = (c_uint64 * 4)()
+    lib.cp_timing_enable(CP_TIMING_COUNTERS)
+    lib.cp_traversal_stats(counts, 1)
+    mesh.query(qd, workspace=ws, opts=qopts, out=out)
     lib.cp_traversal_stats(counts, 1)
     lib.cp_timing_enable(0)
-    trav_ms = tms.value / max(tl.value, 1)
-    # packet kernel: per-warp node visits / triangle tests, per query of the step
-    per_q = float(nq * args.steps)
+    per_q = float(nq)
     packet_visits = {"node_visits_per_query": counts[0] * 32 / per_q / 32,
                      "warp_node_visits_per_32_queries": counts[0] * 32 / per_q,
                      "warp_tri_tests_per_32_queries": counts[1] * 32 / per_q,

@@ -287,8 +287,10 @@ CP_API int32_t cp_version(void) { return 100; }
 
 CP_API uint64_t cp_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
 
-CP_API cp_status cp_timing_enable(int32_t on) {
-    timing_enable(on != 0);
+CP_API cp_status cp_timing_enable(int32_t flags) {
+    if (flags & ~(CP_TIMING_EVENTS | CP_TIMING_COUNTERS))
+        return fail(CP_ERROR_INVALID_VALUE, "cp_timing_enable: unknown flag bits");
+    timing_enable((flags & CP_TIMING_EVENTS) != 0, (flags & CP_TIMING_COUNTERS) != 0);
     return CP_SUCCESS;
 }
 

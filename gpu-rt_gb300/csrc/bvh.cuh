@@ -96,7 +96,7 @@ cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int6
                       float* out_bary, void* ws, size_t ws_bytes, cudaStream_t st);
 
 // CUDA-event timing of traversal launches (diagnostic; see cp_timing_enable).
-void timing_enable(bool on);
+void timing_enable(bool events, bool counters);
 cudaError_t timing_read(double* ms, int64_t* launches, bool reset);
 cudaError_t traversal_stats(unsigned long long* out4, bool reset);
 

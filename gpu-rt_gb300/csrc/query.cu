@@ -79,33 +79,6 @@ __device__ __forceinline__ void cswap(float& a, float& b, int& x, int& y) {
     }
 }
 
-// Ascending sorting networks on packed unsigned keys: an exchange is one
-// integer min and one max.
-__device__ __forceinline__ void kswap(uint32_t& a, uint32_t& b) {
-    const uint32_t lo = min(a, b), hi = max(a, b);
-    a = lo;
-    b = hi;
-}
-template <int K>
-__device__ __forceinline__ void sort_keys(uint32_t (&k)[K]) {
-    if constexpr (K == 2) {
-        kswap(k[0], k[1]);
-    } else if constexpr (K == 4) {
-        kswap(k[0], k[1]); kswap(k[2], k[3]);
-        kswap(k[0], k[2]); kswap(k[1], k[3]);
-        kswap(k[1], k[2]);
-    } else {
-        kswap(k[0], k[1]); kswap(k[2], k[3]); kswap(k[4], k[5]); kswap(k[6], k[7]);
-        kswap(k[0], k[2]); kswap(k[1], k[3]); kswap(k[4], k[6]); kswap(k[5], k[7]);
-        kswap(k[1], k[2]); kswap(k[5], k[6]);
-        kswap(k[0], k[4]); kswap(k[3], k[7]);
-        kswap(k[1], k[5]); kswap(k[2], k[6]);
-        kswap(k[1], k[4]); kswap(k[3], k[6]);
-        kswap(k[2], k[4]); kswap(k[3], k[5]);
-        kswap(k[3], k[4]);
-    }
-}
-
 // Ascending sorting networks (2: 1 exchange, 4: 5, 8: 19).
 template <int K>
 __device__ __forceinline__ void sort_children(float (&d)[K], int (&c)[K]) {
@@ -452,24 +425,71 @@ __device__ __forceinline__ void write_result(const TraverseArgs& a, int64_t qi, 
     }
 }
 
+// Slot lists of the packet stack: entry m lists the set bits of m, lowest
+// first, one per nibble (m < 256 covers nodes up to 8 wide).
+struct SlotLists {
+    uint32_t v[256];
+};
+constexpr SlotLists make_slot_lists() {
+    SlotLists t{};
+    for (int m = 0; m < 256; ++m) {
+        uint32_t l = 0;
+        int p = 0;
+        for (int s = 0; s < 8; ++s)
+            if ((m >> s) & 1) l |= (uint32_t)s << (4 * p++);
+        t.v[m] = l;
+    }
+    return t;
+}
+__constant__ SlotLists c_slot_lists = make_slot_lists();
+
+// Store K consecutive 4-byte values with vector stores (dst 8- or 16-byte
+// aligned as K is 2 or more).
+template <int K, typename T>
+__device__ __forceinline__ void store_row(T* dst, const T (&v)[K]) {
+    static_assert(sizeof(T) == 4, "4-byte elements");
+    if constexpr (K == 2) {
+        *reinterpret_cast<uint2*>(dst) = make_uint2(__builtin_bit_cast(uint32_t, v[0]),
+                                                    __builtin_bit_cast(uint32_t, v[1]));
+    } else {
+#pragma unroll
+        for (int j = 0; j < K; j += 4)
+            *reinterpret_cast<uint4*>(dst + j) =
+                make_uint4(__builtin_bit_cast(uint32_t, v[j]), __builtin_bit_cast(uint32_t, v[j + 1]),
+                           __builtin_bit_cast(uint32_t, v[j + 2]), __builtin_bit_cast(uint32_t, v[j + 3]));
+    }
+}
+
+// Shared memory of one warp's packet stack of `cap` entries: every lane's K
+// bounds [entry][lane][slot], the K child refs [entry][slot], the (slot list,
+// count) of entries below the top [entry]; rounded to 16 bytes.
+__host__ __device__ constexpr size_t packet_warp_bytes(int K, int cap) {
+    return ((size_t)cap * (128 * K + 4 * K + 8) + 15) & ~size_t(15);
+}
+
 // Warp-packet traversal.  The 32 lanes of a warp hold 32 consecutive queries
 // of the Hilbert order (neighbours in space) and walk ONE shared stack: a
 // child is visited when any lane's box lower bound beats that lane's best, so
 // every node row is a single broadcast load and node tests run with all
-// lanes converged.  The child order is the first pending lane's nearest-first
-// order.  Stack entries keep the child's box, so on a pop every lane re-checks
-// its own bound and the entry is skipped when no lane still needs it.  The
-// stack holds (K-1)(depth+1) entries at most; `cap` is that bound, so it
-// cannot overflow.  Lanes of different meshes in one chunk (batches) are
-// served one mesh at a time.
-template <int K>
+// lanes converged.  A visit goes on at once to the first pending lane's
+// nearest needed child; if other children are needed the node becomes ONE
+// stack entry holding every lane's K bounds, the K child refs and the list of
+// the needed slots still to visit (in slot order).  On a pop the
+// top entry's next slot is re-checked against every lane's current best and
+// skipped when no lane still needs it.  Only the top entry can be used up,
+// and a push reuses it, so the stack holds one entry per wide level at most;
+// `cap` (max wide depth + 1) is that bound, so it cannot overflow.  Lanes of
+// different meshes in one chunk (batches) are served one mesh at a time.
+// kStats adds per-warp visit counters (a diagnostic build of the kernel).
+template <int K, bool kStats>
 __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(TraverseArgs a, int cap) {
-    extern __shared__ float s_pk[];
+    extern __shared__ __align__(16) unsigned char s_pk[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    // per warp: ref[cap], then every lane's own box bound of each entry,
-    // [entry][lane] so a warp's access is one conflict-free row
-    int32_t* st_ref = reinterpret_cast<int32_t*>(s_pk + (size_t)warp * 33 * cap);
-    float* st_lb = s_pk + (size_t)warp * 33 * cap + cap + lane;
+    const bool lane0 = lane == 0;
+    unsigned char* wbase = s_pk + (size_t)warp * packet_warp_bytes(K, cap);
+    float* st_bnd = reinterpret_cast<float*>(wbase) + lane * K;  // entry e, slot s at [e * 32 * K + s]
+    int32_t* st_ch = reinterpret_cast<int32_t*>(wbase + (size_t)cap * 128 * K);
+    uint2* st_state = reinterpret_cast<uint2*>(wbase + (size_t)cap * 132 * K);
     const WideNode<K>* __restrict__ nodes = static_cast<const WideNode<K>*>(a.nodes);
     unsigned long long n_nodes = 0, n_tris = 0, n_pops = 0, n_skips = 0;
 
@@ -500,13 +520,14 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
             pending &= ~__ballot_sync(kFull, mine);
             // lanes outside this round never need anything: bound -inf
             float lim = mine ? best : -INFINITY;
-            int sp = 0;
+            int sp = 0;            // stack entries; only the top one can be used up
+            uint32_t t_order = 0;  // the top entry's slots still to visit, next in the low nibble
+            int t_cnt = 0;         // and their number
             int cur = a.wide_root[mesh];
             bool leaf_active = false;  // for leaves: this lane's bound beat its best
-            bool have = true;
-            while (have) {
+            for (;;) {
                 if (cur >= 0) {
-                    ++n_nodes;
+                    if (kStats) ++n_nodes;
                     const WideNode<K>* nd = nodes + cur;
                     float lox[K], hix[K], loy[K], hiy[K], loz[K], hiz[K];
                     int32_t ch[K];
@@ -525,56 +546,47 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                         mine_need |= (lb[s] < lim ? 1u : 0u) << s;
                     }
                     const uint32_t need = __reduce_or_sync(kFull, mine_need);
-                    if (need == 0) goto pop;
-                    {
-                        // The leader's nearest-first order of the needed
-                        // children: sort (bound bits | slot) as unsigned keys
-                        // (non-negative floats order as their bit patterns),
-                        // unneeded children last, so the needed ones take
-                        // positions 0 .. cnt-1.  Broadcast each slot's position
-                        // (4 bits per slot).
-                        const int cnt = __popc(need);
-                        uint32_t key[K];
+                    if (need != 0) {
+                        // the leader's nearest needed child: the least of
+                        // (bound bits | slot) as unsigned keys (non-negative
+                        // floats order as their bit patterns; the sign bit is
+                        // cleared so every needed key beats the sentinel)
+                        uint32_t kmin = 0xFFFFFFFFu;
 #pragma unroll
                         for (int s = 0; s < K; ++s)
-                            key[s] = ((need >> s) & 1u) ? ((__float_as_uint(lb[s]) & ~7u) | (uint32_t)s)
-                                                        : (0xFFFFFFF8u | (uint32_t)s);
-                        sort_keys<K>(key);
-                        uint32_t inv = 0;
-#pragma unroll
-                        for (int t = 0; t < K; ++t) inv |= (uint32_t)t << (4 * (key[t] & 7u));
-                        inv = __shfl_sync(kFull, inv, leader);
-                        // position 0 is taken now; every lane stores its own
-                        // bound of the others, the farthest deepest
-                        float lbf = lb[0];
-                        int32_t cf = ch[0];
-                        const int top = min(sp + cnt - 1, cap);  // cap is the depth bound
-#pragma unroll
-                        for (int s = 0; s < K; ++s) {
-                            if ((need >> s) & 1u) {
-                                const int pos = (int)((inv >> (4 * s)) & 15u);
-                                if (pos == 0) {
-                                    lbf = lb[s];
-                                    cf = ch[s];
-                                } else {
-                                    const int at = top - pos;
-                                    if (at >= 0) {
-                                        st_lb[at * 32] = lb[s];
-                                        if (lane == 0) st_ref[at] = ch[s];
-                                    }
-                                }
+                            kmin = min(kmin, ((need >> s) & 1u)
+                                                 ? ((__float_as_uint(lb[s]) & 0x7FFFFFF8u) | (uint32_t)s)
+                                                 : 0xFFFFFFFFu);
+                        const int f = (int)(__shfl_sync(kFull, kmin, leader) & 7u);
+                        const uint32_t rest = need & ~(1u << f);
+                        if (rest != 0) {
+                            // the node becomes the top entry; a used-up top
+                            // entry is overwritten, a live one keeps its list
+                            if (sp > 0) {
+                                if (t_cnt == 0) --sp;
+                                else if (lane0) st_state[sp - 1] = make_uint2(t_order, (uint32_t)t_cnt);
                             }
+                            if (sp >= cap) {  // cannot happen: cap bounds the depth
+                                atomicOr(a.status, 1u);
+                                sp = cap - 1;
+                            }
+                            store_row<K>(st_bnd + sp * 32 * K, lb);
+                            if (lane0) store_row<K>(st_ch + sp * K, ch);
+                            t_order = c_slot_lists.v[rest];
+                            t_cnt = __popc(rest);
+                            ++sp;
+                            __syncwarp();
                         }
-                        if (sp + cnt - 1 > cap) atomicOr(a.status, 1u);  // cannot happen
-                        sp = top;
-                        __syncwarp();
+                        int32_t cf = ch[0];
+#pragma unroll
+                        for (int s = 1; s < K; ++s) cf = f == s ? ch[s] : cf;
                         cur = cf;
-                        leaf_active = lbf < lim;
+                        leaf_active = (mine_need >> f) & 1u;
                         continue;
                     }
                 } else {
                     const int first = leaf_first(cur), cnt = leaf_count(cur);
-                    n_tris += cnt;
+                    if (kStats) n_tris += cnt;
                     for (int k = 0; k < cnt; ++k) {
                         const float4* fp = reinterpret_cast<const float4*>(a.fast + first + k);
                         FastTri f;
@@ -594,27 +606,38 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                     }
                     if (mine) lim = best;
                 }
-            pop:
-                // pop the next entry some lane still needs
-                have = false;
-                while (sp > 0) {
-                    --sp;
-                    ++n_pops;
-                    const bool want = st_lb[sp * 32] < lim;
+                // pop: the top entry's next slot that some lane still needs
+                bool found = false;
+                for (;;) {
+                    if (t_cnt == 0) {
+                        if (sp <= 1) break;
+                        --sp;
+                        const uint2 s2 = st_state[sp - 1];
+                        t_order = s2.x;
+                        t_cnt = (int)s2.y;
+                        continue;
+                    }
+                    const int s = (int)(t_order & 15u);
+                    t_order >>= 4;
+                    --t_cnt;
+                    const int e = sp - 1;
+                    const bool want = st_bnd[e * 32 * K + s] < lim;
+                    if (kStats) ++n_pops;
                     if (__any_sync(kFull, want)) {
-                        cur = st_ref[sp];
+                        cur = st_ch[e * K + s];
                         leaf_active = want;
-                        have = true;
+                        found = true;
                         break;
                     }
-                    ++n_skips;
+                    if (kStats) ++n_skips;
                 }
-                __syncwarp();
+                __syncwarp();  // the reads above come before a push's writes
+                if (!found) break;
             }
         }
         if (valid) write_result(a, qi, qx, qy, qz, best_rec, best_idx);
     }
-    if (a.stats && lane == 0) {
+    if (kStats && a.stats && lane == 0) {
         atomicAdd(&a.stats[0], n_nodes);
         atomicAdd(&a.stats[1], n_tris);
         atomicAdd(&a.stats[2], n_pops);
@@ -886,11 +909,12 @@ QueryLayout layout(int64_t nq, int nmeshes, bool sort) {
 // Opt-in CUDA-event timing of every traversal launch (cp_timing_*).
 struct TraverseTiming {
     std::mutex mu;
-    bool on = false;
+    bool on = false;        // events around each traversal launch
+    bool counters = false;  // packet traversals run their counting build
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
     double ms = 0.0;
     int64_t launches = 0;
-    unsigned long long* stats = nullptr;  // device: packet visit counters while timing is on
+    unsigned long long* stats = nullptr;  // device: packet visit counters
 };
 TraverseTiming g_timing;
 
@@ -938,9 +962,21 @@ template <int K>
 cudaError_t launch_packet(const TraverseArgs& args, int cap, int block, int blocks_per_sm,
                           cudaStream_t st, bool allow_timing) {
     if (cap < 1) cap = 1;
-    const size_t smem = (size_t)(block / 32) * 33 * cap * sizeof(float);
-    auto kern = k_traverse_packet<K>;
-    cudaError_t e = ensure_smem_limit(reinterpret_cast<const void*>(kern), smem);
+    size_t smem = (size_t)(block / 32) * packet_warp_bytes(K, cap);
+    cudaError_t e;
+    if (smem > 48 * 1024) {
+        // very deep trees: fewer warps per block until the stacks fit
+        int dev = 0, optin = 0;
+        e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+        if (e != cudaSuccess) return e;
+        while (block > 32 && smem > (size_t)optin) {
+            block /= 2;
+            smem = (size_t)(block / 32) * packet_warp_bytes(K, cap);
+        }
+    }
+    auto kern = args.stats ? k_traverse_packet<K, true> : k_traverse_packet<K, false>;
+    e = ensure_smem_limit(reinterpret_cast<const void*>(kern), smem);
     if (e != cudaSuccess) return e;
     int sms = 0;
     e = sm_count(&sms);
@@ -993,10 +1029,11 @@ cudaError_t launch_k(const TraverseArgs& args, const QueryParams& qp, int cap, c
 
 }  // namespace
 
-void timing_enable(bool on) {
+void timing_enable(bool events, bool counters) {
     std::lock_guard<std::mutex> lock(g_timing.mu);
-    g_timing.on = on;
-    if (on && !g_timing.stats) {
+    g_timing.on = events;
+    g_timing.counters = counters;
+    if (counters && !g_timing.stats) {
         if (cudaMalloc(&g_timing.stats, 4 * sizeof(unsigned long long)) == cudaSuccess)
             cudaMemset(g_timing.stats, 0, 4 * sizeof(unsigned long long));
         else
@@ -1112,13 +1149,15 @@ cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int6
         cudaStreamCaptureStatus capst = cudaStreamCaptureStatusNone;
         cudaStreamIsCapturing(st, &capst);
         std::lock_guard<std::mutex> lock(g_timing.mu);
-        if (g_timing.on && !qp.no_timing && capst == cudaStreamCaptureStatusNone)
+        if (g_timing.counters && !qp.no_timing && capst == cudaStreamCaptureStatusNone)
             args.stats = g_timing.stats;
     }
+    // the packet stack holds one entry per wide level at most
+    const int packet_cap = b.max_wide_depth + 1;
     switch (b.p.K) {
-        case 2: return launch_k<2>(args, qp, b.stack_bound, st);
-        case 4: return launch_k<4>(args, qp, b.stack_bound, st);
-        default: return launch_k<8>(args, qp, b.stack_bound, st);
+        case 2: return launch_k<2>(args, qp, packet_cap, st);
+        case 4: return launch_k<4>(args, qp, packet_cap, st);
+        default: return launch_k<8>(args, qp, packet_cap, st);
     }
 }
 

@@ -26,6 +26,9 @@ CP_DEVICE_STACK_OVERFLOW = 0x1
 CP_DEVICE_BAD_INDEX = 0x2
 CP_DEVICE_NONFINITE = 0x4
 
+CP_TIMING_EVENTS = 1
+CP_TIMING_COUNTERS = 2
+
 CP_COLLAPSE_COUNT = 0
 CP_COLLAPSE_SAH = 1
 

@@ -136,17 +136,20 @@ CP_API int32_t cp_version(void);
  * counterpart in the reference. */
 CP_API uint64_t cp_kernel_launches(void);
 
-/* Diagnostic timing: while enabled, every traversal-kernel launch outside a
- * stream capture is bracketed by CUDA events on its own stream.
- * cp_timing_read waits for those events and returns the summed device time
- * (ms) and the number of launches since the last reset.  No counterpart in
- * the reference (its only timing is an FPS readout, src/gpurt.cpp:275). */
-CP_API cp_status cp_timing_enable(int32_t on);
-CP_API cp_status cp_timing_read(double* traverse_ms, int64_t* launches, int32_t reset);
-
-/* While timing is enabled, packet traversals also count, per warp, the node
+/* Diagnostic timing, flags of cp_timing_enable (0 turns both off).
+ * CP_TIMING_EVENTS: every traversal-kernel launch outside a stream capture
+ * is bracketed by CUDA events on its own stream; cp_timing_read waits for
+ * them and returns the summed device time (ms) and the number of launches
+ * since the last reset.  CP_TIMING_COUNTERS: packet traversals run a
+ * counting build of the kernel (a few percent slower) whose per-warp node
  * visits, leaf triangle tests, stack pops and skipped pops (counts4[0..3],
- * summed over warps).  Synchronises the device. */
+ * summed over warps) cp_traversal_stats returns; it synchronises the device.
+ * No counterpart in the reference (its only timing is an FPS readout,
+ * src/gpurt.cpp:275). */
+#define CP_TIMING_EVENTS 1
+#define CP_TIMING_COUNTERS 2
+CP_API cp_status cp_timing_enable(int32_t flags);
+CP_API cp_status cp_timing_read(double* traverse_ms, int64_t* launches, int32_t reset);
 CP_API cp_status cp_traversal_stats(uint64_t* counts4, int32_t reset);
 
 /* Diagnostic: read bandwidth (GB/s) of 128-bit L2 loads over a `bytes`-sized
