@@ -117,6 +117,60 @@ __device__ __forceinline__ float box_lb2(float qx, float qy, float qz, float lox
     return dx * dx + dy * dy + dz * dz;
 }
 
+// Packed f32x2 arithmetic (sm_100 and later): one instruction applies the
+// same IEEE single-precision operation, rounded to nearest even, to both
+// halves of a 64-bit register pair, so two children's box tests issue as
+// one.  Half .x is the low word.  (Triangle tests stay scalar: paired, their
+// unpacking and per-half selects cost as many ALU instructions as the packing
+// saved on the FMA pipe.)
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 f2_pack(float x, float y) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(x), "f"(y));
+    return r;
+}
+__device__ __forceinline__ void f2_unpack(f32x2 v, float& x, float& y) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(x), "=f"(y) : "l"(v));
+}
+__device__ __forceinline__ f32x2 f2_sub(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 f2_mul(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 f2_fma(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+// Box distance along one axis for two children: max(lo - q, q - hi, 0).
+__device__ __forceinline__ f32x2 box_axis2(f32x2 q, f32x2 lo, f32x2 hi) {
+    float a0, a1, b0, b1;
+    f2_unpack(f2_sub(lo, q), a0, a1);
+    f2_unpack(f2_sub(q, hi), b0, b1);
+    return f2_pack(max3f(a0, b0, 0.0f), max3f(a1, b1, 0.0f));
+}
+
+// A node row of K floats as K/2 pairs (children 2j, 2j+1), 16-byte loads.
+template <int K>
+__device__ __forceinline__ void load_row2(const float* __restrict__ p, f32x2 (&r)[K / 2]) {
+    if constexpr (K == 2) {
+        r[0] = __ldg(reinterpret_cast<const unsigned long long*>(p));
+    } else {
+#pragma unroll
+        for (int j = 0; j < K / 2; j += 2) {
+            const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(p) + j / 2);
+            r[j] = v.x;
+            r[j + 1] = v.y;
+        }
+    }
+}
+
 // Branch-free squared distance for the traversal, on a FastTri record.  If
 // the plane projection's barycentrics lie inside the triangle the answer is
 // the plane residual; otherwise the closest point is on the boundary, so it
@@ -471,8 +525,9 @@ __host__ __device__ constexpr size_t packet_warp_bytes(int K, int cap) {
 // of the Hilbert order (neighbours in space) and walk ONE shared stack: a
 // child is visited when any lane's box lower bound beats that lane's best, so
 // every node row is a single broadcast load and node tests run with all
-// lanes converged.  A visit goes on at once to the first pending lane's
-// nearest needed child; if other children are needed the node becomes ONE
+// lanes converged; child bounds are computed two children per packed f32x2
+// operation.  A visit goes on at once to the needed child nearest to any
+// lane (one warp min); if other children are needed the node becomes ONE
 // stack entry holding every lane's K bounds, the K child refs and the list of
 // the needed slots still to visit (in slot order).  On a pop the
 // top entry's next slot is re-checked against every lane's current best and
@@ -510,6 +565,7 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
             qz = a.queries[3 * qi + 2];
             m = a.nmeshes > 1 ? mesh_of(a.qoff, a.nmeshes, qi) : 0;
         }
+        const f32x2 qx2 = f2_pack(qx, qx), qy2 = f2_pack(qy, qy), qz2 = f2_pack(qz, qz);
         float best = INFINITY;
         int best_rec = -1, best_idx = INT_MAX;
         unsigned pending = __ballot_sync(kFull, valid);
@@ -529,35 +585,40 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                 if (cur >= 0) {
                     if (kStats) ++n_nodes;
                     const WideNode<K>* nd = nodes + cur;
-                    float lox[K], hix[K], loy[K], hiy[K], loz[K], hiz[K];
+                    f32x2 lox[K / 2], hix[K / 2], loy[K / 2], hiy[K / 2], loz[K / 2], hiz[K / 2];
                     int32_t ch[K];
-                    load_row<K>(nd->lox, lox);
-                    load_row<K>(nd->hix, hix);
-                    load_row<K>(nd->loy, loy);
-                    load_row<K>(nd->hiy, hiy);
-                    load_row<K>(nd->loz, loz);
-                    load_row<K>(nd->hiz, hiz);
+                    load_row2<K>(nd->lox, lox);
+                    load_row2<K>(nd->hix, hix);
+                    load_row2<K>(nd->loy, loy);
+                    load_row2<K>(nd->hiy, hiy);
+                    load_row2<K>(nd->loz, loz);
+                    load_row2<K>(nd->hiz, hiz);
                     load_row_i<K>(nd->child, ch);
+                    // box lower bounds, two children per packed operation
                     float lb[K];
-                    uint32_t mine_need = 0;
+#pragma unroll
+                    for (int j = 0; j < K / 2; ++j) {
+                        const f32x2 dx = box_axis2(qx2, lox[j], hix[j]);
+                        const f32x2 dy = box_axis2(qy2, loy[j], hiy[j]);
+                        const f32x2 dz = box_axis2(qz2, loz[j], hiz[j]);
+                        f2_unpack(f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx))), lb[2 * j], lb[2 * j + 1]);
+                    }
+                    // each lane's needed children, and its nearest as the least
+                    // (bound bits | slot) unsigned key: non-negative floats
+                    // order as their bit patterns, and the cleared sign bit
+                    // keeps every needed key below the sentinel
+                    uint32_t mine_need = 0, kmine = 0xFFFFFFFFu;
 #pragma unroll
                     for (int s = 0; s < K; ++s) {
-                        lb[s] = box_lb2(qx, qy, qz, lox[s], hix[s], loy[s], hiy[s], loz[s], hiz[s]);
-                        mine_need |= (lb[s] < lim ? 1u : 0u) << s;
+                        const bool want = lb[s] < lim;
+                        mine_need |= (want ? 1u : 0u) << s;
+                        kmine = min(kmine, want ? ((__float_as_uint(lb[s]) & 0x7FFFFFF8u) | (uint32_t)s)
+                                                : 0xFFFFFFFFu);
                     }
                     const uint32_t need = __reduce_or_sync(kFull, mine_need);
                     if (need != 0) {
-                        // the leader's nearest needed child: the least of
-                        // (bound bits | slot) as unsigned keys (non-negative
-                        // floats order as their bit patterns; the sign bit is
-                        // cleared so every needed key beats the sentinel)
-                        uint32_t kmin = 0xFFFFFFFFu;
-#pragma unroll
-                        for (int s = 0; s < K; ++s)
-                            kmin = min(kmin, ((need >> s) & 1u)
-                                                 ? ((__float_as_uint(lb[s]) & 0x7FFFFFF8u) | (uint32_t)s)
-                                                 : 0xFFFFFFFFu);
-                        const int f = (int)(__shfl_sync(kFull, kmin, leader) & 7u);
+                        // go first to the child nearest to any lane
+                        const int f = (int)(__reduce_min_sync(kFull, kmine) & 7u);
                         const uint32_t rest = need & ~(1u << f);
                         if (rest != 0) {
                             // the node becomes the top entry; a used-up top

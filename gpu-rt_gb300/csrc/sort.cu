@@ -1,14 +1,20 @@
 // sort.cu — stable LSD radix sort and exclusive scan (see sort.cuh).
 //
-// One 8-bit pass = three launches:
+// One pass over B digit bits (B = 8 or 10, D = 2^B buckets) = three launches:
 //   k_digit_hist   per-tile digit counts, written digit-major
 //                  (counts[d * tiles + tile]);
 //   exclusive scan of that array: the global start of (digit d, tile t);
-//   k_scatter      each tile ranks its keys stably (warp match_any + a
-//                  per-round prefix over warps), stages them in shared memory
-//                  in digit order and writes digit runs out contiguously.
-// A tile is 256 threads x 16 keys.  Stability comes from ranking the tile's
-// keys in input order: round r holds keys r*256 .. r*256+255, lanes in order.
+//   k_scatter      ranks the tile's keys, stages them in shared memory in
+//                  digit order and writes digit runs out contiguously.
+// A tile is 256 threads x IT keys (IT = 16 for 32-bit keys, 8 for 64-bit).
+// Ranking needs no block-wide barrier per round: warp w owns the tile's keys
+// [w*32*IT, (w+1)*32*IT) and ranks them round by round (32 consecutive keys,
+// lanes in order) against its own digit counters — match_any groups equal
+// digits, the group's first lane reads and advances the warp counter.  One
+// block-wide pass then turns the warp counters into per-warp offsets and the
+// tile's digit starts.  Keys are ranked in (warp, round, lane) order, which is
+// input order, so every pass is stable.  Ten-bit digits are used when they
+// save a pass (30-bit Hilbert keys: 3 passes; 63-bit build keys: 7).
 #include "sort.cuh"
 
 #include <algorithm>
@@ -18,12 +24,20 @@ namespace cpq {
 namespace {
 
 constexpr int kSortThreads = 256;
-constexpr int kSortItems = 16;
-constexpr int kTile = kSortThreads * kSortItems;
 constexpr int kWarps = kSortThreads / 32;
+constexpr int kMaxDigits = 1024;
 constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4;
 constexpr int kScanChunk = kScanThreads * kScanItems;
+
+template <typename KeyT>
+constexpr int items_per_thread() {
+    return sizeof(KeyT) == 4 ? 16 : 8;
+}
+template <typename KeyT>
+constexpr int tile_keys() {
+    return kSortThreads * items_per_thread<KeyT>();
+}
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
     uint32_t m;
@@ -32,24 +46,31 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
 }
 
 template <typename KeyT>
+__device__ __forceinline__ uint32_t digit_of(KeyT k, int shift, uint32_t mask) {
+    return (uint32_t)(k >> shift) & mask;
+}
+
+template <typename KeyT, int B>
 __global__ void __launch_bounds__(kSortThreads) k_digit_hist(const KeyT* __restrict__ keys,
-                                                              int64_t n, int shift,
+                                                              int64_t n, int shift, uint32_t mask,
                                                               uint32_t* __restrict__ counts,
                                                               int tiles) {
-    __shared__ uint32_t hist[256];
-    hist[threadIdx.x] = 0;
+    constexpr int D = 1 << B, IT = items_per_thread<KeyT>(), TILE = tile_keys<KeyT>();
+    __shared__ uint32_t hist[D];
+    for (int d = threadIdx.x; d < D; d += kSortThreads) hist[d] = 0;
     __syncthreads();
-    const int64_t base = (int64_t)blockIdx.x * kTile;
+    const int64_t base = (int64_t)blockIdx.x * TILE;
+    const int lane = threadIdx.x & 31;
 #pragma unroll
-    for (int r = 0; r < kSortItems; ++r) {
-        int64_t i = base + r * kSortThreads + threadIdx.x;
-        bool valid = i < n;
-        uint32_t d = valid ? (uint32_t)((keys[i] >> shift) & 255u) : 256u + (threadIdx.x & 31);
-        uint32_t peers = __match_any_sync(0xffffffffu, d);
+    for (int r = 0; r < IT; ++r) {
+        const int64_t i = base + r * kSortThreads + threadIdx.x;
+        const bool valid = i < n;
+        const uint32_t d = valid ? digit_of(keys[i], shift, mask) : (uint32_t)D + lane;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
         if (valid && (peers & lanemask_lt()) == 0) atomicAdd(&hist[d], (uint32_t)__popc(peers));
     }
     __syncthreads();
-    counts[(int64_t)threadIdx.x * tiles + blockIdx.x] = hist[threadIdx.x];
+    for (int d = threadIdx.x; d < D; d += kSortThreads) counts[(int64_t)d * tiles + blockIdx.x] = hist[d];
 }
 
 // Exclusive scan of one value per thread over a block of 256 threads.
@@ -70,101 +91,116 @@ __device__ __forceinline__ uint32_t block_scan_256(uint32_t v, uint32_t* warp_to
     return off + x - v;
 }
 
-template <typename KeyT>
+template <typename KeyT, int B>
+constexpr size_t scatter_smem_bytes() {
+    constexpr int D = 1 << B, TILE = tile_keys<KeyT>();
+    return (size_t)TILE * sizeof(KeyT) + (size_t)TILE * sizeof(int32_t) +
+           (size_t)(kWarps * D + D + D + kWarps) * sizeof(uint32_t);
+}
+
+template <typename KeyT, int B>
 __global__ void __launch_bounds__(kSortThreads) k_scatter(const KeyT* __restrict__ keys_in,
                                                            const int32_t* __restrict__ vals_in,
                                                            KeyT* __restrict__ keys_out,
                                                            int32_t* __restrict__ vals_out,
-                                                           int64_t n, int shift,
+                                                           int64_t n, int shift, uint32_t mask,
                                                            const uint32_t* __restrict__ offsets,
                                                            int tiles) {
+    constexpr int D = 1 << B, IT = items_per_thread<KeyT>(), TILE = tile_keys<KeyT>();
+    constexpr int DPT = D / kSortThreads;  // digits per thread in the block-wide passes
     extern __shared__ __align__(16) unsigned char smem_raw[];
     KeyT* skeys = reinterpret_cast<KeyT*>(smem_raw);
-    int32_t* svals = reinterpret_cast<int32_t*>(skeys + kTile);
-    uint32_t* tile_base = reinterpret_cast<uint32_t*>(svals + kTile);  // 256
-    uint32_t* run = tile_base + 256;                                   // 256
-    uint32_t* warp_cnt = run + 256;                                    // kWarps * 256
-    uint32_t* warp_tot = warp_cnt + kWarps * 256;                      // kWarps
-    uint32_t* global_base = warp_tot + kWarps;                         // 256
+    int32_t* svals = reinterpret_cast<int32_t*>(skeys + TILE);
+    uint32_t* wcnt = reinterpret_cast<uint32_t*>(svals + TILE);  // [warp][digit]
+    uint32_t* tile_base = wcnt + kWarps * D;                     // D
+    uint32_t* global_base = tile_base + D;                       // D
+    uint32_t* warp_tot = global_base + D;                        // kWarps
 
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int64_t base = (int64_t)blockIdx.x * kTile;
-    const int tile_n = (int)((n - base) < (int64_t)kTile ? (n - base) : (int64_t)kTile);
+    const int64_t base = (int64_t)blockIdx.x * TILE;
+    const int tile_n = (int)((n - base) < (int64_t)TILE ? (n - base) : (int64_t)TILE);
+    const int wbase = warp * 32 * IT;  // this warp's keys within the tile
 
-    KeyT k[kSortItems];
-    int32_t v[kSortItems];
+    KeyT k[IT];
+    int32_t v[IT];
 #pragma unroll
-    for (int r = 0; r < kSortItems; ++r) {
-        int64_t i = base + r * kSortThreads + tid;
-        if (i < n) {
-            k[r] = keys_in[i];
-            v[r] = vals_in[i];
+    for (int r = 0; r < IT; ++r) {
+        const int j = wbase + r * 32 + lane;
+        if (j < tile_n) {
+            k[r] = keys_in[base + j];
+            v[r] = vals_in[base + j];
         } else {
             k[r] = 0;
             v[r] = 0;
         }
     }
-    // tile histogram (reuse run[] as the counter array)
-    run[tid] = 0;
-    global_base[tid] = offsets[(int64_t)tid * tiles + blockIdx.x];
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < kSortItems; ++r) {
-        bool valid = r * kSortThreads + tid < tile_n;
-        uint32_t d = valid ? (uint32_t)((k[r] >> shift) & 255u) : 256u + lane;
-        uint32_t peers = __match_any_sync(0xffffffffu, d);
-        if (valid && (peers & lanemask_lt()) == 0) atomicAdd(&run[d], (uint32_t)__popc(peers));
-    }
-    __syncthreads();
-    uint32_t cnt = run[tid];
-    uint32_t b = block_scan_256(cnt, warp_tot);
-    tile_base[tid] = b;
-    run[tid] = 0;
+    for (int j = tid; j < kWarps * D; j += kSortThreads) wcnt[j] = 0;
+    for (int d = tid; d < D; d += kSortThreads) global_base[d] = offsets[(int64_t)d * tiles + blockIdx.x];
     __syncthreads();
 
+    // rank within the warp, round by round; the counters are this warp's own
+    uint32_t* my = wcnt + warp * D;
     const uint32_t lt = lanemask_lt();
-#pragma unroll 1
-    for (int r = 0; r < kSortItems; ++r) {
+    uint32_t rank[IT];
 #pragma unroll
-        for (int w = 0; w < kWarps; ++w) warp_cnt[w * 256 + tid] = 0;
-        __syncthreads();
-        bool valid = r * kSortThreads + tid < tile_n;
-        uint32_t d = valid ? (uint32_t)((k[r] >> shift) & 255u) : 256u + lane;
-        uint32_t peers = __match_any_sync(0xffffffffu, d);
-        uint32_t rank = __popc(peers & lt);
-        if (valid && rank == 0) warp_cnt[warp * 256 + d] = __popc(peers);
-        __syncthreads();
-        {
-            uint32_t acc = run[tid];
-#pragma unroll
-            for (int w = 0; w < kWarps; ++w) {
-                uint32_t c = warp_cnt[w * 256 + tid];
-                warp_cnt[w * 256 + tid] = acc;
-                acc += c;
-            }
-            run[tid] = acc;
+    for (int r = 0; r < IT; ++r) {
+        const bool valid = wbase + r * 32 + lane < tile_n;
+        const uint32_t d = valid ? digit_of(k[r], shift, mask) : (uint32_t)D + lane;
+        const uint32_t peers = __match_any_sync(0xffffffffu, d);
+        const int leader = __ffs(peers) - 1;
+        uint32_t old = 0;
+        if (valid && lane == leader) {
+            old = my[d];
+            my[d] = old + (uint32_t)__popc(peers);
         }
-        __syncthreads();
-        if (valid) {
-            uint32_t pos = tile_base[d] + warp_cnt[warp * 256 + d] + rank;
+        old = __shfl_sync(0xffffffffu, old, leader);
+        rank[r] = old + (uint32_t)__popc(peers & lt);
+        __syncwarp();
+    }
+    __syncthreads();
+
+    // per digit: exclusive prefix over warps, then the tile's digit starts
+    uint32_t tot[DPT];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int j = 0; j < DPT; ++j) {
+        const int d = tid * DPT + j;
+        uint32_t acc = 0;
+#pragma unroll
+        for (int w = 0; w < kWarps; ++w) {
+            const uint32_t c = wcnt[w * D + d];
+            wcnt[w * D + d] = acc;
+            acc += c;
+        }
+        tot[j] = acc;
+        sum += acc;
+    }
+    uint32_t run = block_scan_256(sum, warp_tot);
+#pragma unroll
+    for (int j = 0; j < DPT; ++j) {
+        tile_base[tid * DPT + j] = run;
+        run += tot[j];
+    }
+    __syncthreads();
+
+    // stage in digit order
+#pragma unroll
+    for (int r = 0; r < IT; ++r) {
+        if (wbase + r * 32 + lane < tile_n) {
+            const uint32_t d = digit_of(k[r], shift, mask);
+            const uint32_t pos = tile_base[d] + wcnt[warp * D + d] + rank[r];
             skeys[pos] = k[r];
             svals[pos] = v[r];
         }
-        __syncthreads();
     }
+    __syncthreads();
     for (int j = tid; j < tile_n; j += kSortThreads) {
-        KeyT key = skeys[j];
-        uint32_t d = (uint32_t)((key >> shift) & 255u);
-        uint32_t dst = global_base[d] + (uint32_t)j - tile_base[d];
+        const KeyT key = skeys[j];
+        const uint32_t d = digit_of(key, shift, mask);
+        const uint32_t dst = global_base[d] + (uint32_t)j - tile_base[d];
         keys_out[dst] = key;
         vals_out[dst] = svals[j];
     }
-}
-
-template <typename KeyT>
-size_t scatter_smem_bytes() {
-    return (size_t)kTile * sizeof(KeyT) + (size_t)kTile * sizeof(int32_t) +
-           (256 + 256 + kWarps * 256 + kWarps + 256) * sizeof(uint32_t);
 }
 
 // ---- exclusive scan ------------------------------------------------------
@@ -280,10 +316,37 @@ cudaError_t exclusive_scan_u32(uint32_t* data, int64_t m, uint32_t* total, void*
 }
 
 size_t radix_sort_workspace_bytes(int64_t n) {
-    int64_t tiles = std::max<int64_t>(1, ceil_div(n, kTile));
-    int64_t m = tiles * 256;
+    // the largest per-pass count array: the smaller (64-bit key) tile and
+    // ten-bit digits
+    int64_t tiles = std::max<int64_t>(1, ceil_div(n, tile_keys<uint64_t>()));
+    int64_t m = tiles * kMaxDigits;
     return align256((size_t)m * sizeof(uint32_t)) + scan_workspace_bytes(m);
 }
+
+namespace {
+
+template <typename KeyT, int B>
+cudaError_t sort_pass(const KeyT* ki, const int32_t* vi, KeyT* ko, int32_t* vo, int64_t n,
+                      int shift, int bits, uint32_t* counts, unsigned char* scan_ws,
+                      size_t scan_bytes, cudaStream_t stream) {
+    constexpr int D = 1 << B;
+    const int tiles = (int)ceil_div(n, tile_keys<KeyT>());
+    const int64_t m = (int64_t)tiles * D;
+    const uint32_t mask = (bits >= 32 ? 0xffffffffu : ((1u << bits) - 1u));
+    const size_t smem = scatter_smem_bytes<KeyT, B>();
+    cudaError_t e = ensure_smem_limit(reinterpret_cast<const void*>(k_scatter<KeyT, B>), smem);
+    if (e != cudaSuccess) return e;
+    k_digit_hist<KeyT, B><<<tiles, kSortThreads, 0, stream>>>(ki, n, shift, mask, counts, tiles); note_launch();
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    e = exclusive_scan_u32(counts, m, nullptr, scan_ws, scan_bytes, stream);
+    if (e != cudaSuccess) return e;
+    k_scatter<KeyT, B><<<tiles, kSortThreads, smem, stream>>>(ki, vi, ko, vo, n, shift, mask, counts,
+                                                             tiles); note_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace
 
 template <typename KeyT>
 cudaError_t radix_sort_pairs(KeyT* keys, int32_t* vals, KeyT* keys_alt, int32_t* vals_alt,
@@ -292,29 +355,23 @@ cudaError_t radix_sort_pairs(KeyT* keys, int32_t* vals, KeyT* keys_alt, int32_t*
     *in_alt = false;
     if (n <= 1 || end_bit <= begin_bit) return cudaSuccess;
     if (workspace_bytes < radix_sort_workspace_bytes(n)) return cudaErrorInvalidValue;
-    const size_t smem = scatter_smem_bytes<KeyT>();
-    {
-        cudaError_t e = ensure_smem_limit(reinterpret_cast<const void*>(k_scatter<KeyT>), smem);
-        if (e != cudaSuccess) return e;
-    }
-    const int tiles = (int)ceil_div(n, kTile);
-    const int64_t m = (int64_t)tiles * 256;
+    const int nbits = end_bit - begin_bit;
+    // ten-bit digits when they take fewer passes than eight-bit ones
+    const int digit_bits = (nbits + 9) / 10 < (nbits + 7) / 8 ? 10 : 8;
     unsigned char* ws = static_cast<unsigned char*>(workspace);
+    const int64_t max_m = std::max<int64_t>(1, ceil_div(n, tile_keys<uint64_t>())) * kMaxDigits;
     uint32_t* counts = reinterpret_cast<uint32_t*>(ws);
-    unsigned char* scan_ws = ws + align256((size_t)m * sizeof(uint32_t));
-    const size_t scan_bytes = workspace_bytes - align256((size_t)m * sizeof(uint32_t));
+    unsigned char* scan_ws = ws + align256((size_t)max_m * sizeof(uint32_t));
+    const size_t scan_bytes = workspace_bytes - align256((size_t)max_m * sizeof(uint32_t));
 
     KeyT *ki = keys, *ko = keys_alt;
     int32_t *vi = vals, *vo = vals_alt;
     bool alt = false;
-    for (int shift = begin_bit; shift < end_bit; shift += 8) {
-        k_digit_hist<KeyT><<<tiles, kSortThreads, 0, stream>>>(ki, n, shift, counts, tiles); note_launch();
-        cudaError_t e = cudaGetLastError();
-        if (e != cudaSuccess) return e;
-        e = exclusive_scan_u32(counts, m, nullptr, scan_ws, scan_bytes, stream);
-        if (e != cudaSuccess) return e;
-        k_scatter<KeyT><<<tiles, kSortThreads, smem, stream>>>(ki, vi, ko, vo, n, shift, counts, tiles); note_launch();
-        e = cudaGetLastError();
+    for (int shift = begin_bit; shift < end_bit; shift += digit_bits) {
+        const int bits = std::min(digit_bits, end_bit - shift);
+        cudaError_t e = digit_bits == 10
+                            ? sort_pass<KeyT, 10>(ki, vi, ko, vo, n, shift, bits, counts, scan_ws, scan_bytes, stream)
+                            : sort_pass<KeyT, 8>(ki, vi, ko, vo, n, shift, bits, counts, scan_ws, scan_bytes, stream);
         if (e != cudaSuccess) return e;
         std::swap(ki, ko);
         std::swap(vi, vo);
