@@ -317,6 +317,8 @@ struct TraverseArgs {
     const void* nodes;
     const TriRec* recs;   // exact vertices: the winner's re-evaluation
     const FastTri* fast;  // distance-test records, same order
+    const int32_t* inv_order;  // triangle (mesh offset + local index) -> record
+    const int64_t* toff;       // per-mesh triangle offsets
     const int32_t* wide_root;
     const int64_t* qoff;
     int nmeshes;
@@ -514,12 +516,33 @@ __device__ __forceinline__ void store_row(T* dst, const T (&v)[K]) {
     }
 }
 
-// Shared memory of one warp's packet stack of `cap` entries: every lane's K
-// bounds [entry][lane][slot], the K child refs [entry][slot], the (slot list,
-// count) of entries below the top [entry]; rounded to 16 bytes.
-__host__ __device__ constexpr size_t packet_warp_bytes(int K, int cap) {
+// Shared memory of one warp: the packet stack of `cap` entries (every lane's
+// K bounds [entry][lane][slot], the K child refs [entry][slot], the (slot
+// list, count) of entries below the top [entry]; rounded to 16 bytes), then
+// the leaf-compaction slots (32 query points) when the kernel compacts.
+__host__ __device__ constexpr size_t packet_stack_bytes(int K, int cap) {
     return ((size_t)cap * (128 * K + 4 * K + 8) + 15) & ~size_t(15);
 }
+__host__ __device__ constexpr size_t packet_warp_bytes(int K, int cap, bool compact) {
+    return packet_stack_bytes(K, cap) + (compact ? 32 * sizeof(float4) : 0);
+}
+
+__device__ __forceinline__ uint32_t lanemask_lt() {
+    uint32_t m;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+    return m;
+}
+
+// A lane's best candidate as one unsigned key: the squared distance's bits
+// (non-negative floats order as their bit patterns) over the triangle index,
+// so the unsigned minimum is the nearest triangle, ties to the smallest index.
+__device__ __forceinline__ unsigned long long best_key(float d2, int idx) {
+    return ((unsigned long long)__float_as_uint(d2) << 32) | (uint32_t)idx;
+}
+__device__ __forceinline__ float key_d2(unsigned long long k) {
+    return __uint_as_float((uint32_t)(k >> 32));
+}
+constexpr unsigned long long kNoKey = 0x7f8000007fffffffull;  // (+inf, INT_MAX): nothing found
 
 // Warp-packet traversal.  The 32 lanes of a warp hold 32 consecutive queries
 // of the Hilbert order (neighbours in space) and walk ONE shared stack: a
@@ -535,16 +558,22 @@ __host__ __device__ constexpr size_t packet_warp_bytes(int K, int cap) {
 // and a push reuses it, so the stack holds one entry per wide level at most;
 // `cap` (max wide depth + 1) is that bound, so it cannot overflow.  Lanes of
 // different meshes in one chunk (batches) are served one mesh at a time.
-// kStats adds per-warp visit counters (a diagnostic build of the kernel).
-template <int K, bool kStats>
+// kCompact (trees whose leaves hold 3 or more triangles) spreads a leaf's
+// (query, triangle) pairs over the warp when few lanes need the leaf; it
+// costs 512 bytes of shared memory per warp, which with 2-triangle leaves
+// is better spent on resident warps.  kStats adds per-warp visit counters (a
+// diagnostic build of the kernel).
+template <int K, bool kCompact, bool kStats>
 __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(TraverseArgs a, int cap) {
     extern __shared__ __align__(16) unsigned char s_pk[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const bool lane0 = lane == 0;
-    unsigned char* wbase = s_pk + (size_t)warp * packet_warp_bytes(K, cap);
+    unsigned char* wbase = s_pk + (size_t)warp * packet_warp_bytes(K, cap, kCompact);
     float* st_bnd = reinterpret_cast<float*>(wbase) + lane * K;  // entry e, slot s at [e * 32 * K + s]
     int32_t* st_ch = reinterpret_cast<int32_t*>(wbase + (size_t)cap * 128 * K);
     uint2* st_state = reinterpret_cast<uint2*>(wbase + (size_t)cap * 132 * K);
+    float4* st_q = reinterpret_cast<float4*>(wbase + packet_stack_bytes(K, cap));
+    const uint32_t lt_mask = lanemask_lt();
     const WideNode<K>* __restrict__ nodes = static_cast<const WideNode<K>*>(a.nodes);
     unsigned long long n_nodes = 0, n_tris = 0, n_pops = 0, n_skips = 0;
 
@@ -566,8 +595,7 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
             m = a.nmeshes > 1 ? mesh_of(a.qoff, a.nmeshes, qi) : 0;
         }
         const f32x2 qx2 = f2_pack(qx, qx), qy2 = f2_pack(qy, qy), qz2 = f2_pack(qz, qz);
-        float best = INFINITY;
-        int best_rec = -1, best_idx = INT_MAX;
+        unsigned long long best = kNoKey;
         unsigned pending = __ballot_sync(kFull, valid);
         while (pending) {
             const int leader = __ffs(pending) - 1;
@@ -575,7 +603,7 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
             const bool mine = ((pending >> lane) & 1u) && m == mesh;
             pending &= ~__ballot_sync(kFull, mine);
             // lanes outside this round never need anything: bound -inf
-            float lim = mine ? best : -INFINITY;
+            float lim = mine ? key_d2(best) : -INFINITY;
             int sp = 0;            // stack entries; only the top one can be used up
             uint32_t t_order = 0;  // the top entry's slots still to visit, next in the low nibble
             int t_cnt = 0;         // and their number
@@ -648,24 +676,47 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                 } else {
                     const int first = leaf_first(cur), cnt = leaf_count(cur);
                     if (kStats) n_tris += cnt;
-                    for (int k = 0; k < cnt; ++k) {
-                        const float4* fp = reinterpret_cast<const float4*>(a.fast + first + k);
-                        FastTri f;
-                        f.p0 = __ldg(fp);
-                        f.p1 = __ldg(fp + 1);
-                        f.p2 = __ldg(fp + 2);
-                        f.p3 = __ldg(fp + 3);
-                        if (leaf_active) {
-                            const float d2 = tri_d2_fast(qx, qy, qz, f);
-                            const int idx = __float_as_int(f.p3.w);
-                            if (d2 < best || (d2 == best && idx < best_idx)) {
-                                best = d2;
-                                best_rec = first + k;
-                                best_idx = idx;
-                            }
+                    const uint32_t act = __ballot_sync(kFull, leaf_active);
+                    const int na = __popc(act);
+                    if (kCompact && cnt >= 2 && na * cnt <= 32) {
+                        // Few lanes need this leaf: spread its (query, triangle)
+                        // pairs over the warp, lane w testing triangle w / na
+                        // against the (w % na)-th active lane's query; each
+                        // active lane then takes the minimum of its cnt keys
+                        // (order-free, so the result is the same).
+                        const int r = __popc(act & lt_mask);
+                        if (leaf_active) st_q[r] = make_float4(qx, qy, qz, 0.0f);
+                        __syncwarp();
+                        unsigned long long key = kNoKey;
+                        if (lane < na * cnt) {
+                            int k = 0;
+                            for (int j = 1; j < cnt; ++j) k += lane >= j * na ? 1 : 0;
+                            const float4 qq = st_q[lane - k * na];
+                            const float4* fp = reinterpret_cast<const float4*>(a.fast + first + k);
+                            FastTri f;
+                            f.p0 = __ldg(fp);
+                            f.p1 = __ldg(fp + 1);
+                            f.p2 = __ldg(fp + 2);
+                            f.p3 = __ldg(fp + 3);
+                            key = best_key(tri_d2_fast(qq.x, qq.y, qq.z, f), __float_as_int(f.p3.w));
+                        }
+                        for (int j = 0; j < cnt; ++j) {
+                            const unsigned long long got = __shfl_sync(kFull, key, (r + j * na) & 31);
+                            if (leaf_active) best = min(best, got);
+                        }
+                    } else {
+                        for (int k = 0; k < cnt; ++k) {
+                            const float4* fp = reinterpret_cast<const float4*>(a.fast + first + k);
+                            FastTri f;
+                            f.p0 = __ldg(fp);
+                            f.p1 = __ldg(fp + 1);
+                            f.p2 = __ldg(fp + 2);
+                            f.p3 = __ldg(fp + 3);
+                            if (leaf_active)
+                                best = min(best, best_key(tri_d2_fast(qx, qy, qz, f), __float_as_int(f.p3.w)));
                         }
                     }
-                    if (mine) lim = best;
+                    if (mine) lim = key_d2(best);
                 }
                 // pop: the top entry's next slot that some lane still needs
                 bool found = false;
@@ -696,7 +747,12 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                 if (!found) break;
             }
         }
-        if (valid) write_result(a, qi, qx, qy, qz, best_rec, best_idx);
+        if (valid) {
+            // the winner's record: its triangle through the build's inverse order
+            const int idx = (int)(uint32_t)best;
+            const int rec = best == kNoKey ? -1 : a.inv_order[a.toff[m] + idx];
+            write_result(a, qi, qx, qy, qz, rec, idx);
+        }
     }
     if (kStats && a.stats && lane == 0) {
         atomicAdd(&a.stats[0], n_nodes);
@@ -1020,10 +1076,10 @@ cudaError_t launch_traverse(const TraverseArgs& args, int block, int blocks_per_
 }
 
 template <int K>
-cudaError_t launch_packet(const TraverseArgs& args, int cap, int block, int blocks_per_sm,
-                          cudaStream_t st, bool allow_timing) {
+cudaError_t launch_packet(const TraverseArgs& args, int cap, bool compact, int block,
+                          int blocks_per_sm, cudaStream_t st, bool allow_timing) {
     if (cap < 1) cap = 1;
-    size_t smem = (size_t)(block / 32) * packet_warp_bytes(K, cap);
+    size_t smem = (size_t)(block / 32) * packet_warp_bytes(K, cap, compact);
     cudaError_t e;
     if (smem > 48 * 1024) {
         // very deep trees: fewer warps per block until the stacks fit
@@ -1033,10 +1089,11 @@ cudaError_t launch_packet(const TraverseArgs& args, int cap, int block, int bloc
         if (e != cudaSuccess) return e;
         while (block > 32 && smem > (size_t)optin) {
             block /= 2;
-            smem = (size_t)(block / 32) * packet_warp_bytes(K, cap);
+            smem = (size_t)(block / 32) * packet_warp_bytes(K, cap, compact);
         }
     }
-    auto kern = args.stats ? k_traverse_packet<K, true> : k_traverse_packet<K, false>;
+    auto kern = compact ? (args.stats ? k_traverse_packet<K, true, true> : k_traverse_packet<K, true, false>)
+                        : (args.stats ? k_traverse_packet<K, false, true> : k_traverse_packet<K, false, false>);
     e = ensure_smem_limit(reinterpret_cast<const void*>(kern), smem);
     if (e != cudaSuccess) return e;
     int sms = 0;
@@ -1075,12 +1132,13 @@ cudaError_t launch_packet(const TraverseArgs& args, int cap, int block, int bloc
 }
 
 template <int K>
-cudaError_t launch_k(const TraverseArgs& args, const QueryParams& qp, int cap, cudaStream_t st) {
+cudaError_t launch_k(const TraverseArgs& args, const QueryParams& qp, int cap, bool compact,
+                     cudaStream_t st) {
     // packet traversal needs spatially coherent warps: the default whenever
     // the queries are walked in Hilbert order
     const bool packet = qp.traversal == 2 || (qp.traversal == 0 && qp.sort);
     const bool allow_timing = !qp.no_timing;
-    if (packet) return launch_packet<K>(args, cap, qp.block, qp.blocks_per_sm, st, allow_timing);
+    if (packet) return launch_packet<K>(args, cap, compact, qp.block, qp.blocks_per_sm, st, allow_timing);
     switch (qp.short_stack) {
         case 4: return launch_traverse<K, 4>(args, qp.block, qp.blocks_per_sm, st, allow_timing);
         case 16: return launch_traverse<K, 16>(args, qp.block, qp.blocks_per_sm, st, allow_timing);
@@ -1193,6 +1251,8 @@ cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int6
     args.nodes = b.nodes;
     args.recs = b.recs;
     args.fast = b.fast;
+    args.inv_order = b.inv_order;
+    args.toff = b.d_toff;
     args.wide_root = b.wide_root;
     args.qoff = d_qoff;
     args.nmeshes = b.nmeshes;
@@ -1215,10 +1275,12 @@ cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int6
     }
     // the packet stack holds one entry per wide level at most
     const int packet_cap = b.max_wide_depth + 1;
+    // leaf compaction pays once leaves can hold 3 or more triangles
+    const bool compact = b.p.leaf_size >= 3;
     switch (b.p.K) {
-        case 2: return launch_k<2>(args, qp, packet_cap, st);
-        case 4: return launch_k<4>(args, qp, packet_cap, st);
-        default: return launch_k<8>(args, qp, packet_cap, st);
+        case 2: return launch_k<2>(args, qp, packet_cap, compact, st);
+        case 4: return launch_k<4>(args, qp, packet_cap, compact, st);
+        default: return launch_k<8>(args, qp, packet_cap, compact, st);
     }
 }
 
