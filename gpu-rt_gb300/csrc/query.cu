@@ -544,6 +544,22 @@ __device__ __forceinline__ float key_d2(unsigned long long k) {
 }
 constexpr unsigned long long kNoKey = 0x7f8000007fffffffull;  // (+inf, INT_MAX): nothing found
 
+// Leaf compaction with na active lanes (1..16): kpr = 32 / na triangles per
+// round and 1 / na.
+struct LeafSplit {
+    int kpr;
+    float inv;
+};
+struct LeafSplits {
+    LeafSplit v[17];
+};
+constexpr LeafSplits make_leaf_splits() {
+    LeafSplits t{};
+    for (int na = 1; na <= 16; ++na) t.v[na] = {32 / na, 1.0f / (float)na};
+    return t;
+}
+__constant__ LeafSplits c_leaf_splits = make_leaf_splits();
+
 // Warp-packet traversal.  The 32 lanes of a warp hold 32 consecutive queries
 // of the Hilbert order (neighbours in space) and walk ONE shared stack: a
 // child is visited when any lane's box lower bound beats that lane's best, so
@@ -678,31 +694,38 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                     if (kStats) n_tris += cnt;
                     const uint32_t act = __ballot_sync(kFull, leaf_active);
                     const int na = __popc(act);
-                    if (kCompact && cnt >= 2 && na * cnt <= 32) {
+                    if (kCompact && cnt >= 2 && na >= 1 && na <= 16) {
                         // Few lanes need this leaf: spread its (query, triangle)
-                        // pairs over the warp, lane w testing triangle w / na
-                        // against the (w % na)-th active lane's query; each
-                        // active lane then takes the minimum of its cnt keys
-                        // (order-free, so the result is the same).
+                        // pairs over the warp.  A round covers kpr = 32 / na
+                        // triangles: lane w tests triangle k0 + w / na against
+                        // the (w % na)-th active lane's query, and each active
+                        // lane takes the minimum of its keys (order-free, so
+                        // the result is the same).
+                        const LeafSplit sp2 = c_leaf_splits.v[na];
                         const int r = __popc(act & lt_mask);
                         if (leaf_active) st_q[r] = make_float4(qx, qy, qz, 0.0f);
                         __syncwarp();
-                        unsigned long long key = kNoKey;
-                        if (lane < na * cnt) {
-                            int k = 0;
-                            for (int j = 1; j < cnt; ++j) k += lane >= j * na ? 1 : 0;
-                            const float4 qq = st_q[lane - k * na];
-                            const float4* fp = reinterpret_cast<const float4*>(a.fast + first + k);
-                            FastTri f;
-                            f.p0 = __ldg(fp);
-                            f.p1 = __ldg(fp + 1);
-                            f.p2 = __ldg(fp + 2);
-                            f.p3 = __ldg(fp + 3);
-                            key = best_key(tri_d2_fast(qq.x, qq.y, qq.z, f), __float_as_int(f.p3.w));
-                        }
-                        for (int j = 0; j < cnt; ++j) {
-                            const unsigned long long got = __shfl_sync(kFull, key, (r + j * na) & 31);
-                            if (leaf_active) best = min(best, got);
+                        // w / na, exact: (w + 1/2) / na is at least 1/32 from an integer
+                        const int kk = (int)(((float)lane + 0.5f) * sp2.inv);
+                        const bool worker = lane < sp2.kpr * na;
+                        const float4 qq = st_q[worker ? lane - kk * na : 0];
+                        for (int k0 = 0; k0 < cnt; k0 += sp2.kpr) {
+                            unsigned long long key = kNoKey;
+                            const int k = k0 + kk;
+                            if (worker && k < cnt) {
+                                const float4* fp = reinterpret_cast<const float4*>(a.fast + first + k);
+                                FastTri f;
+                                f.p0 = __ldg(fp);
+                                f.p1 = __ldg(fp + 1);
+                                f.p2 = __ldg(fp + 2);
+                                f.p3 = __ldg(fp + 3);
+                                key = best_key(tri_d2_fast(qq.x, qq.y, qq.z, f), __float_as_int(f.p3.w));
+                            }
+                            const int nk = min(sp2.kpr, cnt - k0);
+                            for (int j = 0; j < nk; ++j) {
+                                const unsigned long long got = __shfl_sync(kFull, key, (r + j * na) & 31);
+                                if (leaf_active) best = min(best, got);
+                            }
                         }
                     } else {
                         for (int k = 0; k < cnt; ++k) {
