@@ -57,8 +57,8 @@ CANON_V_NODE = 84.273
 CANON_V_TRI = 44.413
 # DRAM bytes (read + write) per query of one traversal launch, from the ncu
 # capture summarised in profiles/k_traverse_packet_large_heightfield.md
-# (5.914 GB for 16,777,216 queries, leaf 2)
-NCU_TRAFFIC_PER_QUERY = 352.5
+# (4.154 + 1.714 GB for 16,777,216 queries, leaf 4)
+NCU_TRAFFIC_PER_QUERY = 349.7
 
 
 def parse():
@@ -367,13 +367,16 @@ def our_arm(args):
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak_eff, "unit": "GB/s",
                 "frac": achieved / peak_eff, "of": "measured",
                 "traffic": None if NCU_TRAFFIC_PER_QUERY is None else NCU_TRAFFIC_PER_QUERY * nq,
-                "kernel": "k_traverse", "kernel_ms_per_launch": trav_ms,
+                "kernel": "k_traverse_packet" if packet_visits else "k_traverse",
+                "kernel_ms_per_launch": trav_ms,
                 "model": "t_roof = B_io/BW_HBM + B_trav/BW_L2 (algorithmic bytes of the canonical "
                          "binary LBVH); peak = (B_io + B_trav)/t_roof",
                 "bytes_per_query": {"io": B_IO, "trav": b_trav, "v_node": v_node, "v_tri": v_tri},
                 "hbm_gbs": hbm, "l2_gbs_measured": l2_gbs,
                 "hbm_only_frac": B_IO / t_kernel / 1e9 / hbm,
                 "packet_counters": packet_visits}
+    # read by the traversal: K-wide nodes (32K B), 48-B exact and 64-B test records
+    traversal_mb = (info.num_wide_nodes * 32 * 4 + info.num_triangles * (48 + 64)) / 1e6
     if rank == 0:
         res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
@@ -385,8 +388,9 @@ def our_arm(args):
                           "block_size": qopts.block_size, "short_stack": qopts.short_stack,
                           "sort_queries": bool(qopts.sort_queries),
                           "wide_nodes": info.num_wide_nodes, "build_ms": info.build_ms,
-                          "l2": "inputs larger than L2 (201 MB queries + 335 MB outputs + 151 MB "
-                                "BVH per step); no flush",
+                          "l2": f"inputs larger than L2 ({nq * 12 / 1e6:.0f} MB queries + "
+                                f"{nq * 20 / 1e6:.0f} MB outputs + {traversal_mb:.0f} MB of nodes and "
+                                "triangle records per step); no flush",
                           "parallelism": f"replicas x{world}"},
                "e2e": e2e, "roofline": roofline, "gpu_launches": int(launches),
                "clocks": clk}

@@ -166,6 +166,26 @@ def test_query_small_config(orc, cpq, cuda, K):
     assert m.device_status() == 0
 
 
+@pytest.mark.parametrize("K", [2, 4, 8])
+@pytest.mark.parametrize("leaf", [3, 8, 15])
+def test_query_leaf_compaction(orc, cpq, cuda, K, leaf):
+    """Leaves of 3 or more triangles: the packet kernel spreads a leaf's
+    (query, triangle) pairs over the warp when few lanes need it, in one or
+    several rounds.  Queries near the surface and far from it give both few
+    and many active lanes per leaf; every answer is checked in FP64."""
+    from gpurt_cpq import workloads as W
+
+    v, t = W.torus(120, 48)
+    near = W.surface_points(v, t, 20000, np.random.default_rng(11))
+    near += np.random.default_rng(12).normal(0.0, 0.02, near.shape)
+    q = np.concatenate([near.astype(np.float32), W.uniform_queries(20000, -1.6, 1.6, 13)])
+    m = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=K, leaf_size=leaf)
+    r = m.query(dev(q, cuda), opts=cpq.query_opts(traversal="packet"))
+    stats = check_against_fp64(orc, v, t, q, r)
+    print(f"leaf compaction K={K} leaf={leaf}: {stats}")
+    assert m.device_status() == 0
+
+
 def test_query_options_do_not_change_results(cpq, cuda):
     import torch
 
