@@ -150,6 +150,25 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(x: float, world: int, device) -> float:
+    """The largest of each rank's x (x itself on one rank): the job's time is
+    its slowest replica's."""
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as td
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank: float, world: int, seconds: float) -> float:
+    """Units all replicas processed per second (weak scaling: each rank runs
+    the same per-rank workload)."""
+    return world * units_per_rank / seconds
+
+
 def measured_peaks() -> dict:
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -324,11 +343,8 @@ def our_arm(args):
                      "warp_tri_tests_per_32_queries": counts[1] * 32 / per_q,
                      "warp_pops_per_32_queries": counts[2] * 32 / per_q,
                      "warp_skipped_pops_per_32_queries": counts[3] * 32 / per_q} if counts[0] else None
-    if world > 1:
-        m = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(m, op=torch.distributed.ReduceOp.MAX)
-        ms = float(m.item())
-    value = world * nq * args.steps / (ms * 1e-3)
+    ms = max_over_ranks(ms, world, dev)
+    value = whole_job_rate(nq * args.steps, world, ms * 1e-3)
     assert mesh.device_status() == 0
 
     # end to end through the host entry point: pinned buffers, copies inside
@@ -343,12 +359,8 @@ def our_arm(args):
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         mesh.query_host(qh, opts=qopts, out=hout)
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        m = torch.tensor([e2e_s], device=dev)
-        torch.distributed.all_reduce(m, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(m.item())
-    e2e = {"value": world * nq * e2e_steps / e2e_s, "unit": UNIT,
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
+    e2e = {"value": whole_job_rate(nq * e2e_steps, world, e2e_s), "unit": UNIT,
            "h2d_bytes_per_step": nq * 12, "d2h_bytes_per_step": nq * (12 + 4 + 4),
            "steps": e2e_steps, "path": "cp_query_host, pinned host buffers"}
 
