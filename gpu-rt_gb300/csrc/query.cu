@@ -209,7 +209,12 @@ __device__ __forceinline__ float tri_d2_fast(float qx, float qy, float qz, const
     rz = apz - (v * abz + w * acz);
     const float d2f = rx * rx + ry * ry + rz * rz;
     const bool inside = v >= 0.0f && w >= 0.0f && v + w <= 1.0f;  // false for NaN
-    return inside ? d2f : d2;
+    // Every candidate is the distance to a point of the triangle, so each is
+    // an upper bound; the face one is taken only when it is the smallest.
+    // For a sliver the FP32 barycentrics carry errors of eps / sin^2 of its
+    // angle and may place an "inside" point far from the foot: the edges then
+    // bound the answer by half the sliver's width above the true distance.
+    return inside ? fminf(d2f, d2) : d2;
 }
 
 // Degenerate triangle in FP32 with barycentrics (weights of b and c).
