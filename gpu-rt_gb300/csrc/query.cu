@@ -243,11 +243,47 @@ __device__ void degenerate_bary(float qx, float qy, float qz, const TriRec& r, f
     }
 }
 
-// Barycentric weights (of b and c) of the closest point on the triangle, by
-// the region logic of tri_d2 evaluated in float-float on exact differences.
-__device__ void precise_bary(float qx, float qy, float qz, const TriRec& r, ff& v, ff& w) {
-    v = ff_from(0.0f);
-    w = ff_from(0.0f);
+// Exact float-float differences of FP32 values (one two-sum each).
+__device__ __forceinline__ ff ff_diff(float a, float b) { return ff_two_sum(a, -b); }
+__device__ __forceinline__ ff3 ff3_diff(float ax, float ay, float az, float bx, float by, float bz) {
+    return {ff_diff(ax, bx), ff_diff(ay, by), ff_diff(az, bz)};
+}
+// Float-float sum whose error is ~2^-48 of the larger operand (the low parts
+// added once): enough for the region tests, which only need signs and ratios.
+__device__ __forceinline__ ff ff_add_fast(ff a, ff b) {
+    ff s = ff_two_sum(a.hi, b.hi);
+    s.lo = __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo));
+    return ff_fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ ff ff3_dot_fast(const ff3& a, const ff3& b) {
+    return ff_add_fast(ff_add_fast(ff_mul(a.x, b.x), ff_mul(a.y, b.y)), ff_mul(a.z, b.z));
+}
+// 1 / b to float-float precision: an FP32 quotient and one correction step.
+__device__ __forceinline__ ff ff_recip(ff b) {
+    const float q1 = __fdiv_rn(1.0f, b.hi);
+    const ff r = ff_sub(ff_from(1.0f), ff_mul(b, ff_from(q1)));
+    return ff_fast_two_sum(q1, __fmul_rn(r.hi, q1));
+}
+__device__ __forceinline__ ff ff_select(bool c, ff a, ff b) { return c ? a : b; }
+
+// The triangle's exact edge vectors and the query's offset from a.
+struct TriDiff {
+    ff3 ab, ac, ap;
+};
+__device__ __forceinline__ TriDiff tri_diff(float qx, float qy, float qz, const TriRec& r) {
+    return {ff3_diff(r.p0.w, r.p1.x, r.p1.y, r.p0.x, r.p0.y, r.p0.z),
+            ff3_diff(r.p1.z, r.p1.w, r.p2.x, r.p0.x, r.p0.y, r.p0.z),
+            ff3_diff(qx, qy, qz, r.p0.x, r.p0.y, r.p0.z)};
+}
+
+// Barycentric weights (of b and c) of the closest point on the triangle:
+// the Voronoi-region logic (Ericson 2005, 5.1.5) in float-float on exact
+// differences, evaluated branch-free — every region's weights are a
+// (numerator v, numerator w, denominator) triple, the one of the region
+// found is kept, and one reciprocal finishes it — so lanes of a warp in
+// different regions do not serialise.
+__device__ void precise_bary_d(float qx, float qy, float qz, const TriRec& r, const TriDiff& t, ff& v,
+                               ff& w) {
     if (__float_as_uint(r.p2.z) & kTriDegenerate) {
         float fv, fw;
         degenerate_bary(qx, qy, qz, r, fv, fw);
@@ -255,61 +291,73 @@ __device__ void precise_bary(float qx, float qy, float qz, const TriRec& r, ff& 
         w = ff_from(fw);
         return;
     }
-    const ff3 A = ff3_from(r.p0.x, r.p0.y, r.p0.z);
-    const ff3 B = ff3_from(r.p0.w, r.p1.x, r.p1.y);
-    const ff3 C = ff3_from(r.p1.z, r.p1.w, r.p2.x);
-    const ff3 Q = ff3_from(qx, qy, qz);
-    const ff3 ab = ff3_sub(B, A), ac = ff3_sub(C, A), ap = ff3_sub(Q, A);
-    const ff d1 = ff3_dot(ab, ap), d2 = ff3_dot(ac, ap);
-    if (ff_le0(d1) && ff_le0(d2)) return;  // vertex a
-    const ff3 bp = ff3_sub(Q, B), cp = ff3_sub(Q, C);
-    const ff d3 = ff3_dot(ab, bp), d4 = ff3_dot(ac, bp);
-    const ff d5 = ff3_dot(ab, cp), d6 = ff3_dot(ac, cp);
+    const ff3 bp = ff3_diff(qx, qy, qz, r.p0.w, r.p1.x, r.p1.y);
+    const ff3 cp = ff3_diff(qx, qy, qz, r.p1.z, r.p1.w, r.p2.x);
+    const ff d1 = ff3_dot_fast(t.ab, t.ap), d2 = ff3_dot_fast(t.ac, t.ap);
+    const ff d3 = ff3_dot_fast(t.ab, bp), d4 = ff3_dot_fast(t.ac, bp);
+    const ff d5 = ff3_dot_fast(t.ab, cp), d6 = ff3_dot_fast(t.ac, cp);
     const ff vc = ff_sub(ff_mul(d1, d4), ff_mul(d3, d2));
     const ff vb = ff_sub(ff_mul(d5, d2), ff_mul(d1, d6));
     const ff va = ff_sub(ff_mul(d3, d6), ff_mul(d5, d4));
     const ff d43 = ff_sub(d4, d3), d56 = ff_sub(d5, d6);
-    if (ff_ge0(d3) && ff_le(d4, d3)) {
-        v = ff_from(1.0f);
-    } else if (ff_le0(vc) && ff_ge0(d1) && ff_le0(d3)) {
-        v = ff_div(d1, ff_sub(d1, d3));
-    } else if (ff_ge0(d6) && ff_le(d5, d6)) {
-        w = ff_from(1.0f);
-    } else if (ff_le0(vb) && ff_ge0(d2) && ff_le0(d6)) {
-        w = ff_div(d2, ff_sub(d2, d6));
-    } else if (ff_le0(va) && ff_ge0(d43) && ff_ge0(d56)) {
-        w = ff_div(d43, ff_add(d43, d56));
-        v = ff_sub(ff_from(1.0f), w);
-    } else {
-        const ff den = ff_add(ff_add(va, vb), vc);
-        v = ff_div(vb, den);
-        w = ff_div(vc, den);
-    }
+    const ff zero = ff_from(0.0f), one = ff_from(1.0f);
+    // face, then the regions that take precedence over it, last one wins
+    ff nv = vb, nw = vc, dn = ff_add(ff_add(va, vb), vc);
+    bool c = ff_le0(va) && ff_ge0(d43) && ff_ge0(d56);  // edge bc
+    nv = ff_select(c, d56, nv);
+    nw = ff_select(c, d43, nw);
+    dn = ff_select(c, ff_add(d43, d56), dn);
+    c = ff_le0(vb) && ff_ge0(d2) && ff_le0(d6);  // edge ac
+    nv = ff_select(c, zero, nv);
+    nw = ff_select(c, d2, nw);
+    dn = ff_select(c, ff_sub(d2, d6), dn);
+    c = ff_ge0(d6) && ff_le(d5, d6);  // vertex c
+    nv = ff_select(c, zero, nv);
+    nw = ff_select(c, one, nw);
+    dn = ff_select(c, one, dn);
+    c = ff_le0(vc) && ff_ge0(d1) && ff_le0(d3);  // edge ab
+    nv = ff_select(c, d1, nv);
+    nw = ff_select(c, zero, nw);
+    dn = ff_select(c, ff_sub(d1, d3), dn);
+    c = ff_ge0(d3) && ff_le(d4, d3);  // vertex b
+    nv = ff_select(c, one, nv);
+    nw = ff_select(c, zero, nw);
+    dn = ff_select(c, one, dn);
+    c = ff_le0(d1) && ff_le0(d2);  // vertex a
+    nv = ff_select(c, zero, nv);
+    nw = ff_select(c, zero, nw);
+    dn = ff_select(c, one, dn);
+    const ff rd = ff_recip(dn);
+    v = ff_mul(nv, rd);
+    w = ff_mul(nw, rd);
+}
+
+__device__ void precise_bary(float qx, float qy, float qz, const TriRec& r, ff& v, ff& w) {
+    precise_bary_d(qx, qy, qz, r, tri_diff(qx, qy, qz, r), v, w);
 }
 
 // Residual q - p and offset p - a for p = a + v (b - a) + w (c - a), in
 // float-float: the differences of FP32 inputs are exact, so the residual of a
 // query very close to the surface keeps its relative accuracy.
+__device__ __forceinline__ void precise_residual_d(const TriDiff& t, ff v, ff w, ff3& res, ff3& off) {
+    off = {ff_add(ff_mul(v, t.ab.x), ff_mul(w, t.ac.x)), ff_add(ff_mul(v, t.ab.y), ff_mul(w, t.ac.y)),
+           ff_add(ff_mul(v, t.ab.z), ff_mul(w, t.ac.z))};
+    res = ff3_sub(t.ap, off);
+}
 __device__ __forceinline__ void precise_residual(float qx, float qy, float qz, const TriRec& r,
                                                  ff v, ff w, ff3& res, ff3& off) {
-    const ff3 A = ff3_from(r.p0.x, r.p0.y, r.p0.z);
-    const ff3 B = ff3_from(r.p0.w, r.p1.x, r.p1.y);
-    const ff3 C = ff3_from(r.p1.z, r.p1.w, r.p2.x);
-    const ff3 Q = ff3_from(qx, qy, qz);
-    const ff3 ab = ff3_sub(B, A), ac = ff3_sub(C, A), ap = ff3_sub(Q, A);
-    off = {ff_add(ff_mul(v, ab.x), ff_mul(w, ac.x)), ff_add(ff_mul(v, ab.y), ff_mul(w, ac.y)),
-           ff_add(ff_mul(v, ab.z), ff_mul(w, ac.z))};
-    res = ff3_sub(ap, off);
+    precise_residual_d(tri_diff(qx, qy, qz, r), v, w, res, off);
 }
 
 // Final answer for the winning triangle: distance to ~2^-44 relative, the
 // closest point and its barycentric weights rounded once to FP32.
 __device__ void precise_closest(float qx, float qy, float qz, const TriRec& r, float& dist,
                                 float& px, float& py, float& pz, float& ov, float& ow) {
+    const TriDiff t = tri_diff(qx, qy, qz, r);
     ff v, w;
-    precise_bary(qx, qy, qz, r, v, w);
+    precise_bary_d(qx, qy, qz, r, t, v, w);
     ff3 res, off;
-    precise_residual(qx, qy, qz, r, v, w, res, off);
+    precise_residual_d(t, v, w, res, off);
     dist = ff_to_float(ff_sqrt(ff3_dot(res, res)));
     px = ff_to_float(ff_add(ff_from(r.p0.x), off.x));
     py = ff_to_float(ff_add(ff_from(r.p0.y), off.y));
