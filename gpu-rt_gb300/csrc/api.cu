@@ -22,6 +22,7 @@
 #include "../../include/cpq.h"
 #include "bvh.cuh"
 #include "handles.cuh"
+#include "ray.cuh"
 
 using namespace cpq;
 
@@ -511,6 +512,82 @@ CP_API cp_status cp_backward(const cp_mesh* m, const float* queries, const int32
     CP_CUDA(bvh_backward(m->bvh, queries, tri, bary, grad_dist, nq, grad_queries, grad_verts,
                          reinterpret_cast<cudaStream_t>(stream)),
             "backward");
+    return CP_SUCCESS;
+}
+
+// ---- rays ------------------------------------------------------------------
+
+CP_API void cp_ray_opts_default(cp_ray_opts* o) {
+    if (!o) return;
+    o->tmin = 0.0f;
+    o->tmax = INFINITY;
+    o->det_epsilon = 0.0f;
+    o->any_hit = 0;
+    o->sort_rays = 1;
+    o->block_size = 256;
+}
+
+static cp_status to_ray_params(const cp_ray_opts* o, RayParams* r) {
+    cp_ray_opts d;
+    cp_ray_opts_default(&d);
+    if (!o) o = &d;
+    const int block = o->block_size ? o->block_size : d.block_size;
+    if (block < 32 || block > 256 || block % 32)
+        return fail(CP_ERROR_INVALID_VALUE, "block_size must be a multiple of 32 in 32..256");
+    if (std::isnan(o->tmin) || std::isnan(o->tmax) || !(o->tmin <= o->tmax))
+        return fail(CP_ERROR_INVALID_VALUE, "tmin and tmax must satisfy tmin <= tmax");
+    if (!(o->det_epsilon >= 0.0f) || std::isinf(o->det_epsilon))
+        return fail(CP_ERROR_INVALID_VALUE, "det_epsilon must be finite and >= 0");
+    r->tmin = o->tmin;
+    r->tmax = o->tmax;
+    r->det_eps = o->det_epsilon;
+    r->any_hit = o->any_hit ? 1 : 0;
+    r->sort = o->sort_rays ? 1 : 0;
+    r->block = block;
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_ray_workspace_size(const cp_mesh* m, int64_t n, const cp_ray_opts* opts,
+                                       size_t* bytes) {
+    if (!m || !bytes) return fail(CP_ERROR_INVALID_VALUE, "mesh or bytes is NULL");
+    if (n < 0) return fail(CP_ERROR_INVALID_VALUE, "negative ray count");
+    RayParams rp;
+    cp_status s = to_ray_params(opts, &rp);
+    if (s != CP_SUCCESS) return s;
+    QueryParams qp;
+    qp.sort = rp.sort;
+    *bytes = query_workspace_bytes(m->bvh, n, qp);
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_ray_query(const cp_mesh* m, const float* origins, const float* directions,
+                              const float* tmax_per_ray, int64_t n, const cp_ray_opts* opts,
+                              float* out_t, int32_t* out_tri, float* out_uv, void* workspace,
+                              size_t ws_bytes, cp_stream_t stream) {
+    if (!m) return fail(CP_ERROR_INVALID_VALUE, "mesh is NULL");
+    if (n < 0) return fail(CP_ERROR_INVALID_VALUE, "negative ray count");
+    if (n > INT32_MAX) return fail(CP_ERROR_NOT_SUPPORTED, "more than 2^31 - 1 rays in one call");
+    if (n == 0) return CP_SUCCESS;
+    if (!origins || !directions) return fail(CP_ERROR_INVALID_VALUE, "origins and directions are required");
+    RayParams rp;
+    cp_status s = to_ray_params(opts, &rp);
+    if (s != CP_SUCCESS) return s;
+    QueryParams qp;
+    qp.sort = rp.sort;
+    const size_t need = query_workspace_bytes(m->bvh, n, qp);
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    void* own = nullptr;
+    if (!workspace) {
+        CP_CUDA(ws_alloc(&own, need, st), "workspace allocation");
+        workspace = own;
+        ws_bytes = need;
+    } else if (ws_bytes < need) {
+        return fail(CP_ERROR_SCRATCH_TOO_SMALL, "workspace smaller than cp_ray_workspace_size()");
+    }
+    cudaError_t e = bvh_ray_query(m->bvh, origins, directions, tmax_per_ray, n, nullptr, rp, out_t,
+                                  out_tri, out_uv, workspace, ws_bytes, st);
+    if (own) cudaFreeAsync(own, st);
+    if (e != cudaSuccess) return cuda_fail(e, "ray query");
     return CP_SUCCESS;
 }
 

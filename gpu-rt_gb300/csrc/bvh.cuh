@@ -90,6 +90,14 @@ struct QueryParams {
 
 size_t query_workspace_bytes(const Bvh& b, int64_t nq, const QueryParams& qp);
 
+// The visiting order of nq points (queries or ray origins): their Hilbert
+// order when `sort` (else nullptr), in a workspace of
+// query_workspace_bytes(b, nq, {sort}) bytes, plus the zeroed work counter of
+// a persistent traversal.  Stream-ordered; no host synchronisation.
+cudaError_t order_points(const Bvh& b, const float* points, int64_t nq, const int64_t* d_qoff,
+                         bool sort, void* ws, size_t ws_bytes, cudaStream_t st, const int32_t** perm,
+                         unsigned long long** counter);
+
 // q_off: device array of nmeshes + 1 query offsets (nullptr for one mesh).
 cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int64_t* d_qoff,
                       const QueryParams& qp, float* out_point, float* out_dist, int32_t* out_tri,

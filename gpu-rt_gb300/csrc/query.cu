@@ -1274,18 +1274,19 @@ size_t query_workspace_bytes(const Bvh& b, int64_t nq, const QueryParams& qp) {
     return layout(nq, b.nmeshes, qp.sort != 0).total;
 }
 
-cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int64_t* d_qoff,
-                      const QueryParams& qp, float* out_point, float* out_dist, int32_t* out_tri,
-                      float* out_bary, void* ws, size_t ws_bytes, cudaStream_t st) {
-    if (nq <= 0) return cudaSuccess;
-    const QueryLayout L = layout(nq, b.nmeshes, qp.sort != 0);
+cudaError_t order_points(const Bvh& b, const float* queries, int64_t nq, const int64_t* d_qoff,
+                         bool sort, void* ws, size_t ws_bytes, cudaStream_t st, const int32_t** perm_out,
+                         unsigned long long** counter_out) {
+    const QueryLayout L = layout(nq, b.nmeshes, sort);
     if (ws_bytes < L.total) return cudaErrorInvalidValue;
     unsigned char* w = static_cast<unsigned char*>(ws);
     unsigned long long* counter = reinterpret_cast<unsigned long long*>(w + L.counter);
+    *counter_out = counter;
+    *perm_out = nullptr;
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
     if (e != cudaSuccess) return e;
     const int32_t* perm = nullptr;
-    if (qp.sort && nq > 1) {
+    if (sort && nq > 1) {
         uint64_t* keys = reinterpret_cast<uint64_t*>(w + L.keys);
         int32_t* vals = reinterpret_cast<int32_t*>(w + L.vals);
         uint64_t* keys_alt = reinterpret_cast<uint64_t*>(w + L.keys_alt);
@@ -1323,6 +1324,18 @@ cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int6
         if (e != cudaSuccess) return e;
         perm = in_alt ? vals_alt : vals;
     }
+    *perm_out = perm;
+    return cudaSuccess;
+}
+
+cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int64_t* d_qoff,
+                      const QueryParams& qp, float* out_point, float* out_dist, int32_t* out_tri,
+                      float* out_bary, void* ws, size_t ws_bytes, cudaStream_t st) {
+    if (nq <= 0) return cudaSuccess;
+    const int32_t* perm = nullptr;
+    unsigned long long* counter = nullptr;
+    cudaError_t e = order_points(b, queries, nq, d_qoff, qp.sort != 0, ws, ws_bytes, st, &perm, &counter);
+    if (e != cudaSuccess) return e;
     TraverseArgs args;
     args.nodes = b.nodes;
     args.recs = b.recs;

@@ -1,0 +1,283 @@
+// ray.cu — ray queries through the closest-point BVH.
+//
+// The reference's own GPU query is a ray: `trace_ray` (closest hit over
+// [EPS, LARGE_DIST], src/shaders/rt/rt.rgen:257-270) and `visibility`
+// (terminate on the first hit of a segment, rt.rgen:272-291), answered by the
+// driver's hardware traversal, with the payload {barycentrics, obj_id,
+// prim_id, hit} (src/shaders/rt/rtcommon.glsl:55-60, rt.rchit:11-16).  Here
+// the same wide BVH that serves closest-point queries is walked by one thread
+// per ray: a slab test per child box (the reference's hit_bbox,
+// rtcommon.glsl:242-251, made conservative), children visited nearest entry
+// first, and at the leaves the Möller–Trumbore test of the reference's
+// triangle_hit (rtcommon.glsl:181-202) in FP32.
+//
+// The triangle test is written with round-to-nearest intrinsics in
+// triangle_hit's own evaluation order (dot = (x + y) + z, cross
+// components as differences of products), so it is the same FP32 function
+// as the CPU restatement; the closest hit is the least (t, triangle index)
+// over every triangle the test accepts, and the slab test never rejects a box
+// a ray enters, so the answer does not depend on the traversal order and
+// equals the restatement's brute force bit for bit.
+#include <cfloat>
+#include <climits>
+
+#include "bvh.cuh"
+#include "ray.cuh"
+
+namespace cpq {
+
+namespace {
+
+constexpr int kRayStack = 264;  // > (K-1)(depth+1) + 1: cp_mesh_create refuses (K-1)(depth+1) > 256
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ int mesh_of(const int64_t* __restrict__ off, int nmeshes, int64_t i) {
+    int lo = 0, hi = nmeshes - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (off[mid] <= i) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__device__ __forceinline__ float dot_rn(float ax, float ay, float az, float bx, float by, float bz) {
+    return __fadd_rn(__fadd_rn(__fmul_rn(ax, bx), __fmul_rn(ay, by)), __fmul_rn(az, bz));
+}
+
+// triangle_hit of the reference: t, and the weights u (of b) and v (of c).
+// |det| <= det_eps (and det = 0 always) is a miss.
+__device__ __forceinline__ bool mt_hit(float ox, float oy, float oz, float dx, float dy, float dz,
+                                       const TriRec& r, float det_eps, float& t, float& u, float& v) {
+    const float ax = r.p0.x, ay = r.p0.y, az = r.p0.z;
+    const float v1x = __fsub_rn(r.p0.w, ax), v1y = __fsub_rn(r.p1.x, ay), v1z = __fsub_rn(r.p1.y, az);
+    const float v2x = __fsub_rn(r.p1.z, ax), v2y = __fsub_rn(r.p1.w, ay), v2z = __fsub_rn(r.p2.x, az);
+    // p = cross(d, v2)
+    const float px = __fsub_rn(__fmul_rn(dy, v2z), __fmul_rn(dz, v2y));
+    const float py = __fsub_rn(__fmul_rn(dz, v2x), __fmul_rn(dx, v2z));
+    const float pz = __fsub_rn(__fmul_rn(dx, v2y), __fmul_rn(dy, v2x));
+    const float det = dot_rn(v1x, v1y, v1z, px, py, pz);
+    if (!(fabsf(det) > det_eps)) return false;
+    const float inv = __fdiv_rn(1.0f, det);
+    const float sx = __fsub_rn(ox, ax), sy = __fsub_rn(oy, ay), sz = __fsub_rn(oz, az);
+    u = __fmul_rn(dot_rn(sx, sy, sz, px, py, pz), inv);
+    if (u < 0.0f || u > 1.0f) return false;
+    // q = cross(s, v1)
+    const float qx = __fsub_rn(__fmul_rn(sy, v1z), __fmul_rn(sz, v1y));
+    const float qy = __fsub_rn(__fmul_rn(sz, v1x), __fmul_rn(sx, v1z));
+    const float qz = __fsub_rn(__fmul_rn(sx, v1y), __fmul_rn(sy, v1x));
+    v = __fmul_rn(dot_rn(dx, dy, dz, qx, qy, qz), inv);
+    if (v < 0.0f || __fadd_rn(u, v) > 1.0f) return false;
+    t = __fmul_rn(dot_rn(v2x, v2y, v2z, qx, qy, qz), inv);
+    return true;
+}
+
+struct RayArgs {
+    const void* nodes;
+    const TriRec* recs;
+    const int32_t* wide_root;
+    const int64_t* qoff;
+    int nmeshes;
+    const float* orig;
+    const float* dir;
+    const float* tmax_per_ray;  // optional
+    int64_t n;
+    float tmin, tmax, det_eps;
+    int any_hit;
+    const int32_t* perm;
+    float* out_t;
+    int32_t* out_tri;
+    float* out_uv;
+    unsigned long long* counter;
+    uint32_t* status;
+};
+
+template <int K>
+__device__ __forceinline__ void load_row(const float* __restrict__ p, float (&r)[K]) {
+    if constexpr (K == 2) {
+        const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+        r[0] = v.x; r[1] = v.y;
+    } else {
+#pragma unroll
+        for (int j = 0; j < K; j += 4) {
+            const float4 v = __ldg(reinterpret_cast<const float4*>(p) + j / 4);
+            r[j] = v.x; r[j + 1] = v.y; r[j + 2] = v.z; r[j + 3] = v.w;
+        }
+    }
+}
+template <int K>
+__device__ __forceinline__ void load_row_i(const int32_t* __restrict__ p, int32_t (&r)[K]) {
+    if constexpr (K == 2) {
+        const int2 v = __ldg(reinterpret_cast<const int2*>(p));
+        r[0] = v.x; r[1] = v.y;
+    } else {
+#pragma unroll
+        for (int j = 0; j < K; j += 4) {
+            const int4 v = __ldg(reinterpret_cast<const int4*>(p) + j / 4);
+            r[j] = v.x; r[j + 1] = v.y; r[j + 2] = v.z; r[j + 3] = v.w;
+        }
+    }
+}
+
+// One thread per ray, persistent over an atomic counter (32 rays per warp
+// grab).  Per node: slab entry/exit of every child box against the current
+// hit distance; entered children are pushed farthest first.  The exit
+// distance is widened by 2^-20 of its magnitude (four times the rounding of
+// a subtraction and a product on each side), so a box the ray enters is
+// never rejected.  The slab test divides by the direction with zero
+// components replaced by a signed 1e-30, so an origin lying on a slab plane
+// gives 0 rather than the NaN of 0 * inf; the triangle test uses the ray as
+// given.
+template <int K>
+__global__ void __launch_bounds__(256) k_ray(RayArgs a) {
+    const int lane = threadIdx.x & 31;
+    const WideNode<K>* __restrict__ nodes = static_cast<const WideNode<K>*>(a.nodes);
+    int32_t stack[kRayStack];
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(a.counter, 32ull);
+        base = __shfl_sync(kFull, base, 0);
+        if (base >= (unsigned long long)a.n) break;
+        const int64_t i = (int64_t)base + lane;
+        if (i >= a.n) continue;
+        const int64_t qi = a.perm ? (int64_t)a.perm[i] : i;
+        const float ox = a.orig[3 * qi], oy = a.orig[3 * qi + 1], oz = a.orig[3 * qi + 2];
+        const float dx = a.dir[3 * qi], dy = a.dir[3 * qi + 1], dz = a.dir[3 * qi + 2];
+        const float ix = __fdiv_rn(1.0f, fabsf(dx) < 1e-30f ? copysignf(1e-30f, dx) : dx);
+        const float iy = __fdiv_rn(1.0f, fabsf(dy) < 1e-30f ? copysignf(1e-30f, dy) : dy);
+        const float iz = __fdiv_rn(1.0f, fabsf(dz) < 1e-30f ? copysignf(1e-30f, dz) : dz);
+        float tmax = a.tmax;
+        if (a.tmax_per_ray) tmax = fminf(tmax, a.tmax_per_ray[qi]);
+        const float tmin = a.tmin;
+        const int m = a.nmeshes > 1 ? mesh_of(a.qoff, a.nmeshes, qi) : 0;
+        float bt = INFINITY, bu = 0.0f, bv = 0.0f;
+        int bidx = INT_MAX;
+        bool found = false;
+        int sp = 0;
+        stack[sp++] = a.wide_root[m];
+        while (sp > 0) {
+            const int cur = stack[--sp];
+            if (cur >= 0) {
+                const WideNode<K>* nd = nodes + cur;
+                float lox[K], hix[K], loy[K], hiy[K], loz[K], hiz[K];
+                int32_t ch[K];
+                load_row<K>(nd->lox, lox);
+                load_row<K>(nd->hix, hix);
+                load_row<K>(nd->loy, loy);
+                load_row<K>(nd->hiy, hiy);
+                load_row<K>(nd->loz, loz);
+                load_row<K>(nd->hiz, hiz);
+                load_row_i<K>(nd->child, ch);
+                const float limit = fminf(bt, tmax);
+                float tn[K];
+#pragma unroll
+                for (int s = 0; s < K; ++s) {
+                    const float x0 = (lox[s] - ox) * ix, x1 = (hix[s] - ox) * ix;
+                    const float y0 = (loy[s] - oy) * iy, y1 = (hiy[s] - oy) * iy;
+                    const float z0 = (loz[s] - oz) * iz, z1 = (hiz[s] - oz) * iz;
+                    const float tnear = fmaxf(fmaxf(fminf(x0, x1), fminf(y0, y1)), fmaxf(fminf(z0, z1), tmin));
+                    float tfar = fminf(fminf(fmaxf(x0, x1), fmaxf(y0, y1)), fminf(fmaxf(z0, z1), limit));
+                    tfar += fabsf(tfar) * 9.5367432e-7f;
+                    // empty slots (lo = +inf) give tnear = +inf or NaN: never entered
+                    tn[s] = (tnear <= tfar && lox[s] <= hix[s]) ? tnear : INFINITY;
+                }
+                // push entered children, farthest first (insertion order by tn)
+#pragma unroll
+                for (int pass = 0; pass < K; ++pass) {
+                    int pick = -1;
+                    float far = -1.0f;
+#pragma unroll
+                    for (int s = 0; s < K; ++s)
+                        if (tn[s] < INFINITY && tn[s] > far) {
+                            far = tn[s];
+                            pick = s;
+                        }
+                    if (pick < 0) break;
+                    if (sp < kRayStack) stack[sp++] = ch[pick];
+                    else atomicOr(a.status, 1u);
+#pragma unroll
+                    for (int s = 0; s < K; ++s)
+                        if (s == pick) tn[s] = INFINITY;
+                }
+            } else {
+                const int first = leaf_first(cur), cnt = leaf_count(cur);
+                for (int k = 0; k < cnt; ++k) {
+                    const float4* rp = reinterpret_cast<const float4*>(a.recs + first + k);
+                    TriRec r;
+                    r.p0 = __ldg(rp);
+                    r.p1 = __ldg(rp + 1);
+                    r.p2 = __ldg(rp + 2);
+                    float t, u, v;
+                    if (!mt_hit(ox, oy, oz, dx, dy, dz, r, a.det_eps, t, u, v)) continue;
+                    if (!(t >= tmin && t <= tmax)) continue;
+                    const int idx = __float_as_int(r.p2.y);
+                    if (t < bt || (t == bt && idx < bidx)) {
+                        bt = t;
+                        bu = u;
+                        bv = v;
+                        bidx = idx;
+                        found = true;
+                    }
+                }
+                if (found && a.any_hit) break;
+            }
+        }
+        if (a.out_t) a.out_t[qi] = found ? bt : INFINITY;
+        if (a.out_tri) a.out_tri[qi] = found ? bidx : -1;
+        if (a.out_uv) {
+            a.out_uv[2 * qi] = found ? bu : 0.0f;
+            a.out_uv[2 * qi + 1] = found ? bv : 0.0f;
+        }
+    }
+}
+
+template <int K>
+cudaError_t launch_ray(const RayArgs& args, int block, cudaStream_t st) {
+    auto kern = k_ray<K>;
+    int sms = 0;
+    cudaError_t e = sm_count(&sms);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = blocks_per_sm(reinterpret_cast<const void*>(kern), block, 0, &per_sm);
+    if (e != cudaSuccess) return e;
+    int64_t grid = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
+    const int64_t need = ((args.n + 31) / 32 * 32 + block - 1) / block;
+    if (grid > need) grid = need;
+    kern<<<(unsigned)grid, block, 0, st>>>(args); note_launch();
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t bvh_ray_query(const Bvh& b, const float* orig, const float* dir, const float* tmax_per_ray,
+                          int64_t n, const int64_t* d_off, const RayParams& rp, float* out_t,
+                          int32_t* out_tri, float* out_uv, void* ws, size_t ws_bytes, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    RayArgs args;
+    cudaError_t e = order_points(b, orig, n, d_off, rp.sort != 0, ws, ws_bytes, st, &args.perm, &args.counter);
+    if (e != cudaSuccess) return e;
+    args.nodes = b.nodes;
+    args.recs = b.recs;
+    args.wide_root = b.wide_root;
+    args.qoff = d_off;
+    args.nmeshes = b.nmeshes;
+    args.orig = orig;
+    args.dir = dir;
+    args.tmax_per_ray = tmax_per_ray;
+    args.n = n;
+    args.tmin = rp.tmin;
+    args.tmax = rp.tmax;
+    args.det_eps = rp.det_eps;
+    args.any_hit = rp.any_hit;
+    args.out_t = out_t;
+    args.out_tri = out_tri;
+    args.out_uv = out_uv;
+    args.status = b.status;
+    switch (b.p.K) {
+        case 2: return launch_ray<2>(args, rp.block, st);
+        case 4: return launch_ray<4>(args, rp.block, st);
+        default: return launch_ray<8>(args, rp.block, st);
+    }
+}
+
+}  // namespace cpq

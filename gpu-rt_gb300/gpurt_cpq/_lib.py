@@ -43,6 +43,11 @@ class QueryOpts(Structure):
                 ("short_stack", c_int32), ("traversal", c_int32)]
 
 
+class RayOpts(Structure):
+    _fields_ = [("tmin", c_float), ("tmax", c_float), ("det_epsilon", c_float), ("any_hit", c_int32),
+                ("sort_rays", c_int32), ("block_size", c_int32)]
+
+
 CP_TRAVERSAL_AUTO = 0
 CP_TRAVERSAL_THREAD = 1
 CP_TRAVERSAL_PACKET = 2
@@ -84,6 +89,10 @@ SIGNATURES = {
     "cp_query_noalloc_scratch_bytes": (c_size_t, []),
     "cp_backward": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p,
                               c_void_p, c_void_p]),
+    "cp_ray_opts_default": (None, [POINTER(RayOpts)]),
+    "cp_ray_workspace_size": (c_int32, [c_void_p, c_int64, POINTER(RayOpts), POINTER(c_size_t)]),
+    "cp_ray_query": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, POINTER(RayOpts),
+                               c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "cp_batch_create": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, POINTER(BuildOpts),
                                   c_void_p, POINTER(c_void_p)]),
     "cp_batch_destroy": (c_int32, [c_void_p]),

@@ -18,7 +18,8 @@ from dataclasses import dataclass
 import numpy as np
 import torch
 
-from ._lib import (CP_COLLAPSE_COUNT, CP_COLLAPSE_SAH, BuildOpts, MeshInfo, QueryOpts, check, lib)
+from ._lib import (CP_COLLAPSE_COUNT, CP_COLLAPSE_SAH, BuildOpts, MeshInfo, QueryOpts, RayOpts, check,
+                   lib)
 
 
 def _stream(stream=None) -> c_void_p:
@@ -66,6 +67,27 @@ def query_opts(block_size: int = 0, sort_queries: bool = True, blocks_per_sm: in
         o.short_stack = short_stack
     o.traversal = {"auto": 0, "thread": 1, "packet": 2}[traversal]
     return o
+
+
+def ray_opts(tmin: float = 0.0, tmax: float = float("inf"), det_epsilon: float = 0.0,
+             any_hit: bool = False, sort_rays: bool = True, block_size: int = 0) -> RayOpts:
+    """cp_ray_opts: hits count for t in [tmin, tmax]; det_epsilon as the reference's
+    triangle_hit (1e-5 there); any_hit stops at the first hit (its visibility())."""
+    o = RayOpts()
+    lib.cp_ray_opts_default(byref(o))
+    o.tmin, o.tmax, o.det_epsilon = tmin, tmax, det_epsilon
+    o.any_hit = 1 if any_hit else 0
+    o.sort_rays = 1 if sort_rays else 0
+    if block_size:
+        o.block_size = block_size
+    return o
+
+
+@dataclass
+class RayResult:
+    t: torch.Tensor     # (N,) float32, +inf on a miss
+    tri: torch.Tensor   # (N,) int32, -1 on a miss
+    uv: torch.Tensor | None  # (N, 2) float32: weights of vertices 1 and 2 at the hit
 
 
 @dataclass
@@ -149,6 +171,29 @@ class Mesh:
         check(lib.cp_query(self._h, _ptr(points), n, byref(o), _ptr(out.point), _ptr(out.dist),
                            _ptr(out.tri), _ptr(out.bary), ws_ptr, ws_bytes, _stream(stream)),
               "cp_query")
+        return out
+
+    def ray_query(self, origins: torch.Tensor, directions: torch.Tensor, *,
+                  tmax_per_ray: torch.Tensor | None = None, opts: RayOpts | None = None,
+                  want_uv: bool = True, stream=None) -> RayResult:
+        """Closest (or, with opts.any_hit, some) hit of each ray (cp_ray_query)."""
+        _check_dev(origins, "origins", torch.float32, 3)
+        _check_dev(directions, "directions", torch.float32, 3)
+        n = int(origins.shape[0])
+        if directions.shape[0] != n:
+            raise ValueError("origins and directions must have the same length")
+        if tmax_per_ray is not None and (not tmax_per_ray.is_cuda or tmax_per_ray.dtype != torch.float32
+                                         or tmax_per_ray.numel() != n):
+            raise ValueError("tmax_per_ray must be a CUDA float32 tensor of one value per ray")
+        o = opts or ray_opts()
+        dev = origins.device
+        out = RayResult(t=torch.empty((n,), dtype=torch.float32, device=dev),
+                        tri=torch.empty((n,), dtype=torch.int32, device=dev),
+                        uv=torch.empty((n, 2), dtype=torch.float32, device=dev) if want_uv else None)
+        tm = tmax_per_ray.contiguous() if tmax_per_ray is not None else None
+        check(lib.cp_ray_query(self._h, _ptr(origins), _ptr(directions), _ptr(tm), n, byref(o),
+                               _ptr(out.t), _ptr(out.tri), _ptr(out.uv), c_void_p(None), 0, _stream(stream)),
+              "cp_ray_query")
         return out
 
     def query_host(self, points: np.ndarray | torch.Tensor, *, want_point: bool = True,

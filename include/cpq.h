@@ -234,6 +234,48 @@ CP_API cp_status cp_query_host(const cp_mesh* mesh, const float* queries, int64_
                                const cp_query_opts* opts, float* out_point, float* out_dist,
                                int32_t* out_tri, float* out_bary, cp_stream_t stream);
 
+/* ---- ray queries ----------------------------------------------------------- */
+
+/*
+ * Rays through the same BVH: the reference's own GPU query, `trace_ray`
+ * (closest hit, src/shaders/rt/rt.rgen:257-270) and `visibility` (stop at the
+ * first hit of a segment, rt.rgen:272-291), whose payload is the barycentrics,
+ * the object and the primitive index (rtcommon.glsl:55-60, rt.rchit:11-16).
+ * Boxes are tested by slabs (hit_bbox, rtcommon.glsl:242-251, made
+ * conservative), triangles by Möller–Trumbore exactly as triangle_hit
+ * (rtcommon.glsl:181-202) evaluates it in FP32.  The closest hit is the least
+ * (t, triangle index) over every triangle the test accepts with t in
+ * [tmin, tmax], so it does not depend on the traversal.
+ */
+typedef struct cp_ray_opts {
+    float tmin;          /* hits count for t in [tmin, tmax] (the reference: [1e-5, 1e7]) */
+    float tmax;          /* +inf allowed */
+    float det_epsilon;   /* |det| <= det_epsilon is a miss; 0: only det == 0 (triangle_hit: 1e-5,
+                            a scene-scale constant that rejects every triangle below ~3e-3 in size) */
+    int32_t any_hit;     /* 1: stop at the first accepted hit (visibility); t and triangle are that hit's */
+    int32_t sort_rays;   /* 1: walk the rays in the Hilbert order of their origins (outputs keep input order) */
+    int32_t block_size;  /* threads per block: 32..256, multiple of 32; 0 = default */
+} cp_ray_opts;
+
+CP_API void cp_ray_opts_default(cp_ray_opts* opts);  /* [0, +inf], exact det test, closest hit, sorted, 256 */
+
+CP_API cp_status cp_ray_workspace_size(const cp_mesh* mesh, int64_t n, const cp_ray_opts* opts,
+                                       size_t* bytes);
+
+/*
+ * n rays (origins and directions: n x 3 floats, device; directions need not
+ * be unit, t is in units of the direction's length).  tmax_per_ray (n floats,
+ * may be NULL) lowers tmax per ray: segment ends, as visibility(a, b) uses.
+ * Outputs (device, each may be NULL): out_t (n; +inf on a miss), out_tri (n;
+ * -1 on a miss), out_uv (n x 2: weights u of vertex 1 and v of vertex 2; the
+ * reference's barycentrics are (1 - u - v, u, v)).  workspace as cp_query.
+ * n == 0 is a no-op.  Asynchronous on `stream`.
+ */
+CP_API cp_status cp_ray_query(const cp_mesh* mesh, const float* origins, const float* directions,
+                              const float* tmax_per_ray, int64_t n, const cp_ray_opts* opts,
+                              float* out_t, int32_t* out_tri, float* out_uv, void* workspace,
+                              size_t workspace_bytes, cp_stream_t stream);
+
 /*
  * cp_query for callers that must not allocate device memory while they run:
  * a render or simulation loop that forbids allocation after start-up (an

@@ -1126,3 +1126,170 @@ void orc_backward_f64(const float* verts, int64_t nv, const int32_t* tris, const
         }
     }
 }
+
+/* ===================================================================== */
+/* Rays: brute force in FP32 (the GPU's arithmetic) and FP64             */
+/* ===================================================================== */
+
+/* triangle_hit (src/shaders/rt/rtcommon.glsl:181-202) in FP32, in its own
+ * evaluation order (dot = (x + y) + z; cross components as differences of
+ * products); compiled without contraction, so each step rounds once. */
+static int mt_f32(const float o[3], const float d[3], const float a[3], const float b[3],
+                  const float c[3], float det_eps, float* t, float* u, float* v) {
+    float v1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+    float v2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+    float p[3] = {d[1] * v2[2] - d[2] * v2[1], d[2] * v2[0] - d[0] * v2[2], d[0] * v2[1] - d[1] * v2[0]};
+    float det = (v1[0] * p[0] + v1[1] * p[1]) + v1[2] * p[2];
+    if (!(fabsf(det) > det_eps)) return 0;
+    float inv = 1.0f / det;
+    float s[3] = {o[0] - a[0], o[1] - a[1], o[2] - a[2]};
+    float uu = ((s[0] * p[0] + s[1] * p[1]) + s[2] * p[2]) * inv;
+    if (uu < 0.0f || uu > 1.0f) return 0;
+    float q[3] = {s[1] * v1[2] - s[2] * v1[1], s[2] * v1[0] - s[0] * v1[2], s[0] * v1[1] - s[1] * v1[0]};
+    float vv = ((d[0] * q[0] + d[1] * q[1]) + d[2] * q[2]) * inv;
+    if (vv < 0.0f || uu + vv > 1.0f) return 0;
+    *t = ((v2[0] * q[0] + v2[1] * q[1]) + v2[2] * q[2]) * inv;
+    *u = uu;
+    *v = vv;
+    return 1;
+}
+
+static int mt_f64(const double o[3], const double d[3], const double a[3], const double b[3],
+                  const double c[3], double det_eps, double* t, double* u, double* v) {
+    double v1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+    double v2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+    double p[3] = {d[1] * v2[2] - d[2] * v2[1], d[2] * v2[0] - d[0] * v2[2], d[0] * v2[1] - d[1] * v2[0]};
+    double det = (v1[0] * p[0] + v1[1] * p[1]) + v1[2] * p[2];
+    if (!(fabs(det) > det_eps)) return 0;
+    double inv = 1.0 / det;
+    double s[3] = {o[0] - a[0], o[1] - a[1], o[2] - a[2]};
+    double uu = ((s[0] * p[0] + s[1] * p[1]) + s[2] * p[2]) * inv;
+    if (uu < 0.0 || uu > 1.0) return 0;
+    double q[3] = {s[1] * v1[2] - s[2] * v1[1], s[2] * v1[0] - s[0] * v1[2], s[0] * v1[1] - s[1] * v1[0]};
+    double vv = ((d[0] * q[0] + d[1] * q[1]) + d[2] * q[2]) * inv;
+    if (vv < 0.0 || uu + vv > 1.0) return 0;
+    *t = ((v2[0] * q[0] + v2[1] * q[1]) + v2[2] * q[2]) * inv;
+    *u = uu;
+    *v = vv;
+    return 1;
+}
+
+typedef struct {
+    const float *verts, *orig, *dir, *tmax_per;
+    const int32_t* tris;
+    int64_t nt;
+    float tmin, tmax, eps;
+    double tmin64, tmax64, eps64;
+    float *t32, *uv32;
+    double *t64, *uv64;
+    int32_t* tri;
+} ray_ctx;
+
+static void ray32_range(void* vctx, int64_t b, int64_t e) {
+    ray_ctx* c = (ray_ctx*)vctx;
+    for (int64_t i = b; i < e; ++i) {
+        const float* o = c->orig + 3 * i;
+        const float* d = c->dir + 3 * i;
+        float tmax = c->tmax;
+        if (c->tmax_per && c->tmax_per[i] < tmax) tmax = c->tmax_per[i];
+        float bt = INFINITY, bu = 0.0f, bv = 0.0f;
+        int32_t bi = -1;
+        for (int64_t k = 0; k < c->nt; ++k) {
+            const int32_t* ix = c->tris + 3 * k;
+            float t, u, v;
+            if (!mt_f32(o, d, c->verts + 3 * (int64_t)ix[0], c->verts + 3 * (int64_t)ix[1],
+                        c->verts + 3 * (int64_t)ix[2], c->eps, &t, &u, &v))
+                continue;
+            if (!(t >= c->tmin && t <= tmax)) continue;
+            if (t < bt) {  /* triangles in index order: the first of equal t is the least index */
+                bt = t;
+                bu = u;
+                bv = v;
+                bi = (int32_t)k;
+            }
+        }
+        c->t32[i] = bt;
+        c->tri[i] = bi;
+        if (c->uv32) {
+            c->uv32[2 * i] = bu;
+            c->uv32[2 * i + 1] = bv;
+        }
+    }
+}
+
+static void ray64_range(void* vctx, int64_t b, int64_t e) {
+    ray_ctx* c = (ray_ctx*)vctx;
+    for (int64_t i = b; i < e; ++i) {
+        const double o[3] = {c->orig[3 * i], c->orig[3 * i + 1], c->orig[3 * i + 2]};
+        const double d[3] = {c->dir[3 * i], c->dir[3 * i + 1], c->dir[3 * i + 2]};
+        double tmax = c->tmax64;
+        if (c->tmax_per && c->tmax_per[i] < tmax) tmax = c->tmax_per[i];
+        double bt = INFINITY, bu = 0.0, bv = 0.0;
+        int32_t bi = -1;
+        for (int64_t k = 0; k < c->nt; ++k) {
+            double A[3], B[3], C[3];
+            load_tri_f64(c->verts, c->tris, k, A, B, C);
+            double t, u, v;
+            if (!mt_f64(o, d, A, B, C, c->eps64, &t, &u, &v)) continue;
+            if (!(t >= c->tmin64 && t <= tmax)) continue;
+            if (t < bt) {
+                bt = t;
+                bu = u;
+                bv = v;
+                bi = (int32_t)k;
+            }
+        }
+        c->t64[i] = bt;
+        c->tri[i] = bi;
+        if (c->uv64) {
+            c->uv64[2 * i] = bu;
+            c->uv64[2 * i + 1] = bv;
+        }
+    }
+}
+
+double orc_ray_brute_f32(const float* verts, const int32_t* tris, int64_t nt, const float* orig,
+                         const float* dir, const float* tmax_per_ray, int64_t n, float tmin,
+                         float tmax, float det_eps, float* out_t, int32_t* out_tri, float* out_uv,
+                         int nthreads) {
+    ray_ctx c;
+    memset(&c, 0, sizeof c);
+    c.verts = verts;
+    c.tris = tris;
+    c.nt = nt;
+    c.orig = orig;
+    c.dir = dir;
+    c.tmax_per = tmax_per_ray;
+    c.tmin = tmin;
+    c.tmax = tmax;
+    c.eps = det_eps;
+    c.t32 = out_t;
+    c.uv32 = out_uv;
+    c.tri = out_tri;
+    double t0 = now_s();
+    parallel_for(n, 16, nthreads, ray32_range, &c);
+    return now_s() - t0;
+}
+
+double orc_ray_brute_f64(const float* verts, const int32_t* tris, int64_t nt, const float* orig,
+                         const float* dir, const float* tmax_per_ray, int64_t n, double tmin,
+                         double tmax, double det_eps, double* out_t, int32_t* out_tri,
+                         double* out_uv, int nthreads) {
+    ray_ctx c;
+    memset(&c, 0, sizeof c);
+    c.verts = verts;
+    c.tris = tris;
+    c.nt = nt;
+    c.orig = orig;
+    c.dir = dir;
+    c.tmax_per = tmax_per_ray;
+    c.tmin64 = tmin;
+    c.tmax64 = tmax;
+    c.eps64 = det_eps;
+    c.t64 = out_t;
+    c.uv64 = out_uv;
+    c.tri = out_tri;
+    double t0 = now_s();
+    parallel_for(n, 16, nthreads, ray64_range, &c);
+    return now_s() - t0;
+}

@@ -117,6 +117,22 @@ void orc_backward_f64(const float* verts, int64_t nv, const int32_t* tris, const
                       const int32_t* tri, const double* bary, const double* grad_d, int64_t nq,
                       double* grad_q, double* grad_verts);
 
+/* Rays, brute force over every triangle.  The hit test is the reference's
+ * triangle_hit (Möller–Trumbore, src/shaders/rt/rtcommon.glsl:181-202): in
+ * FP32 (orc_ray_brute_f32) operation for operation as the GPU evaluates it,
+ * or in FP64 (orc_ray_brute_f64).  |det| <= det_eps is a miss; a hit counts
+ * for t in [tmin, min(tmax, tmax_per_ray[i])] (tmax_per_ray may be NULL); the
+ * answer is the least (t, triangle index).  Misses give t = +inf, tri = -1,
+ * uv = (0, 0).  Returns elapsed wall seconds. */
+double orc_ray_brute_f32(const float* verts, const int32_t* tris, int64_t nt, const float* orig,
+                         const float* dir, const float* tmax_per_ray, int64_t n, float tmin,
+                         float tmax, float det_eps, float* out_t, int32_t* out_tri, float* out_uv,
+                         int nthreads);
+double orc_ray_brute_f64(const float* verts, const int32_t* tris, int64_t nt, const float* orig,
+                         const float* dir, const float* tmax_per_ray, int64_t n, double tmin,
+                         double tmax, double det_eps, double* out_t, int32_t* out_tri,
+                         double* out_uv, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -81,6 +81,12 @@ def lib():
         L.orc_backward_f64.restype = None
         L.orc_backward_f64.argtypes = [c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
                                        c_void_p, c_int64, c_void_p, c_void_p]
+        L.orc_ray_brute_f32.restype = c_double
+        L.orc_ray_brute_f32.argtypes = [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_int64,
+                                        c_float, c_float, c_float, c_void_p, c_void_p, c_void_p, c_int]
+        L.orc_ray_brute_f64.restype = c_double
+        L.orc_ray_brute_f64.argtypes = [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_int64,
+                                        c_double, c_double, c_double, c_void_p, c_void_p, c_void_p, c_int]
         _lib = L
     return _lib
 
@@ -240,3 +246,21 @@ def backward_f64(verts, tris, q, tri, bary3, grad):
     lib().orc_backward_f64(_p(verts), verts.shape[0], _p(tris), _p(q), _p(tri), _p(bary3), _p(grad),
                            n, _p(gq), _p(gv))
     return gq, gv
+
+
+def ray_brute(verts, tris, orig, dirs, tmin=0.0, tmax=float("inf"), det_eps=0.0, tmax_per_ray=None,
+              fp64=False, threads: int | None = None):
+    """Closest hit of every ray over every triangle (Möller–Trumbore of the
+    reference's triangle_hit): FP32 as the GPU evaluates it, or FP64."""
+    v, t = _f32(verts), _i32(tris)
+    o, d = _f32(orig), _f32(dirs)
+    n = o.shape[0]
+    tm = None if tmax_per_ray is None else _f32(tmax_per_ray)
+    dt = np.float64 if fp64 else np.float32
+    out_t = np.empty(n, dt)
+    out_tri = np.empty(n, np.int32)
+    out_uv = np.empty((n, 2), dt)
+    fn = lib().orc_ray_brute_f64 if fp64 else lib().orc_ray_brute_f32
+    secs = fn(_p(v), _p(t), t.shape[0], _p(o), _p(d), _p(tm), n, tmin, tmax, det_eps, _p(out_t),
+              _p(out_tri), _p(out_uv), threads or nthreads())
+    return {"t": out_t, "tri": out_tri, "uv": out_uv, "seconds": secs}

@@ -212,3 +212,50 @@ def test_backward_f64_matches_finite_differences(orc):
                        for x in qm[:20]])
         fd = g[:20] * (dp - dm) / (2 * h)
         np.testing.assert_allclose(gq[:20, k], fd, atol=1e-5, rtol=1e-4)
+
+
+# ---------------------------------------------------------------- rays
+
+def test_ray_known_answers(orc):
+    """Hand-computed hits on the unit right triangle (0,0,0), (1,0,0), (0,1,0)."""
+    v = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0]], np.float32)
+    t = np.array([[0, 1, 2]], np.int32)
+    o = np.array([[0.25, 0.25, 1], [0.25, 0.25, 1], [2, 2, 1], [0.25, 0.25, -1], [0.5, 0.25, 3],
+                  [-1, 0.25, 0]], np.float32)
+    d = np.array([[0, 0, -1], [0, 0, 1], [0, 0, -1], [0, 0, 2], [0, 0, -0.5], [1, 0, 0]], np.float32)
+    for fp64 in (False, True):
+        r = orc.ray_brute(v, t, o, d, fp64=fp64)
+        np.testing.assert_array_equal(r["tri"], [0, -1, -1, 0, 0, -1])  # last: in the plane, det = 0
+        np.testing.assert_allclose(r["t"][[0, 3, 4]], [1.0, 0.5, 6.0])
+        np.testing.assert_allclose(r["uv"][[0, 3, 4]], [[0.25, 0.25], [0.25, 0.25], [0.5, 0.25]])
+        # [tmin, tmax] and per-ray ends
+        r = orc.ray_brute(v, t, o, d, tmin=0.0, tmax=0.9, fp64=fp64)
+        np.testing.assert_array_equal(r["tri"], [-1, -1, -1, 0, -1, -1])
+        r = orc.ray_brute(v, t, o, d, tmax_per_ray=np.full(6, 5.0, np.float32), fp64=fp64)
+        np.testing.assert_array_equal(r["tri"], [0, -1, -1, 0, -1, -1])
+
+
+def test_ray_reference_epsilon_rejects_small_triangles(orc):
+    """triangle_hit's |det| < 1e-5 (a scene-scale constant): a triangle of
+    size 1e-3 is missed with it and hit without it."""
+    v = np.array([[0, 0, 0], [1e-3, 0, 0], [0, 1e-3, 0]], np.float32)
+    t = np.array([[0, 1, 2]], np.int32)
+    o = np.array([[2.5e-4, 2.5e-4, 1]], np.float32)
+    d = np.array([[0, 0, -1]], np.float32)
+    assert orc.ray_brute(v, t, o, d)["tri"][0] == 0
+    assert orc.ray_brute(v, t, o, d, det_eps=1e-5)["tri"][0] == -1
+
+
+def test_ray_f32_agrees_with_f64(orc):
+    from gpurt_cpq import workloads as W
+
+    v, t = W.icosphere(2)
+    rng = np.random.default_rng(4)
+    o = rng.uniform(-2, 2, (3000, 3)).astype(np.float32)
+    d = rng.normal(size=(3000, 3)).astype(np.float32)
+    a = orc.ray_brute(v, t, o, d)
+    b = orc.ray_brute(v, t, o, d, fp64=True)
+    same = a["tri"] == b["tri"]
+    assert same.mean() > 0.99
+    both = same & (a["tri"] >= 0)
+    np.testing.assert_allclose(a["t"][both], b["t"][both], rtol=1e-5, atol=1e-6)
