@@ -73,7 +73,7 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--leaf", type=int, default=0)
     ap.add_argument("--workload", default="large",
-                    choices=["large", "torus", "batched", "dynamic", "small"],
+                    choices=["large", "torus", "batched", "dynamic", "small", "rays"],
                     help="large is the headline; the others measure the other forms")
     return ap.parse_args()
 
@@ -475,6 +475,35 @@ def torus_arm(args):
            "fwd_bwd_over_fwd": ms_fb / ms_f, "target_fwd_bwd_over_fwd": 2.5})
 
 
+def rays_arm(args):
+    """Ray queries (cp_ray_query) through the large workload's BVH: 16M rays
+    from the workload's query points in seeded random directions, closest hit
+    (trace_ray) and any hit (visibility)."""
+    import torch
+
+    import gpurt_cpq as cpq
+
+    dev = torch.device("cuda", 0)
+    v, t, q = workload()
+    rng = np.random.default_rng(17)
+    d = rng.normal(size=q.shape).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    vd, td, od, dd = (torch.from_numpy(x).to(dev) for x in (v, t, q, d))
+    n = od.shape[0]
+    mesh = cpq.Mesh(vd, td, branching=4, leaf_size=4)
+    closest, anyhit = cpq.ray_opts(), cpq.ray_opts(any_hit=True)
+    r = mesh.ray_query(od, dd, opts=closest)
+    ms_c = _timed(torch, lambda: mesh.ray_query(od, dd, opts=closest), args.steps, args.warmup)
+    ms_a = _timed(torch, lambda: mesh.ray_query(od, dd, opts=anyhit), args.steps, args.warmup)
+    _line("ray queries/s, closest hit (large heightfield, 2.09M tris, 16M rays)", n / (ms_c * 1e-3),
+          "rays/s", ms_c, args,
+          {"workload": "large heightfield mesh; origins = the 16,777,216 closest-point queries, "
+                       "directions uniform on the sphere (seed 17); t in [0, inf)",
+           "branching": 4, "leaf_size": 4, "sort_rays": True},
+          {"any_hit": {"value": n / (ms_a * 1e-3), "ms_per_step": ms_a},
+           "hit_fraction": float((r.tri >= 0).float().mean())})
+
+
 def batched_arm(args):
     """256 uneven meshes: one batched build + one persistent graph-captured
     launch, against plain per-mesh builds and launches on the same GPU."""
@@ -634,7 +663,7 @@ def main():
         our_arm(args)
     else:
         {"torus": torus_arm, "batched": batched_arm, "dynamic": dynamic_arm,
-         "small": small_arm}[args.workload](args)
+         "small": small_arm, "rays": rays_arm}[args.workload](args)
 
 
 if __name__ == "__main__":
