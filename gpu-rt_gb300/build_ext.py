@@ -1,7 +1,8 @@
 """Build the closest-point engine's shared library for sm_103a.
 
-Compiles every translation unit of ``csrc/`` in parallel with nvcc
-(``-gencode arch=compute_103a,code=sm_103a -lineinfo -O3``) and links
+Compiles every CUDA translation unit of ``csrc/`` in parallel with nvcc
+(``-gencode arch=compute_103a,code=sm_103a -lineinfo -O3``) and the host-only
+C++ ones (``*.cpp``: the glTF reader) with the host compiler, and links
 ``gpurt_cpq/libgpurt_cpq.so`` in-tree.  No CMake, no torch extension machinery:
 the library has a plain C ABI (``include/cpq.h``) and links only the CUDA
 runtime.  Run as ``python gpu-rt_gb300/build_ext.py`` or call :func:`build`.
@@ -24,6 +25,7 @@ BUILD_DIR = PKG_ROOT / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
               "--expt-relaxed-constexpr", "-Werror", "all-warnings"]
+CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-Wall", "-Wextra", "-Werror"]
 
 
 def _nvcc() -> str:
@@ -44,16 +46,21 @@ def build(verbose: bool = False, force: bool = False) -> Path:
     """Compile csrc/*.cu and link the shared library; returns its path."""
     nvcc = _nvcc()
     BUILD_DIR.mkdir(exist_ok=True)
-    sources = sorted(CSRC.glob("*.cu"))
-    headers = sorted(CSRC.glob("*.cuh")) + [PKG_ROOT.parent / "include" / "cpq.h"]
+    sources = sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp"))
+    headers = (sorted(CSRC.glob("*.cuh")) + sorted(CSRC.glob("*.h")) +
+               [PKG_ROOT.parent / "include" / "cpq.h"])
+    cxx = os.environ.get("CXX") or shutil.which("g++") or "c++"
     objs = []
     jobs = []
     for src in sources:
-        obj = BUILD_DIR / (src.stem + ".o")
+        obj = BUILD_DIR / (src.stem + ("_host" if src.suffix == ".cpp" else "") + ".o")
         objs.append(obj)
         if force or _needs_rebuild(obj, [src] + headers):
-            cmd = [nvcc, *ARCH, *NVCC_FLAGS, "-I", str(PKG_ROOT.parent / "include"), "-c", str(src),
-                   "-o", str(obj)]
+            inc = ["-I", str(PKG_ROOT.parent / "include")]
+            if src.suffix == ".cpp":
+                cmd = [cxx, *CXX_FLAGS, *inc, "-c", str(src), "-o", str(obj)]
+            else:
+                cmd = [nvcc, *ARCH, *NVCC_FLAGS, *inc, "-c", str(src), "-o", str(obj)]
             jobs.append(cmd)
 
     def run(cmd):
@@ -61,7 +68,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
-            raise RuntimeError(f"nvcc failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+            raise RuntimeError(f"compile failed:\n{' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
         return r
 
     if jobs:

@@ -89,6 +89,11 @@ SIGNATURES = {
     "cp_query_noalloc_scratch_bytes": (c_size_t, []),
     "cp_backward": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_int64, c_void_p,
                               c_void_p, c_void_p]),
+    "cp_gltf_load": (c_int32, [c_char_p, POINTER(c_void_p)]),
+    "cp_gltf_free": (None, [c_void_p]),
+    "cp_gltf_primitives": (c_int32, [c_void_p, POINTER(c_int32), POINTER(c_void_p), POINTER(c_void_p),
+                                     POINTER(c_void_p), POINTER(c_void_p)]),
+    "cp_gltf_instances": (c_int32, [c_void_p, POINTER(c_int32), POINTER(c_void_p), POINTER(c_void_p)]),
     "cp_ray_opts_default": (None, [POINTER(RayOpts)]),
     "cp_ray_workspace_size": (c_int32, [c_void_p, c_int64, POINTER(RayOpts), POINTER(c_size_t)]),
     "cp_ray_query": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, POINTER(RayOpts),

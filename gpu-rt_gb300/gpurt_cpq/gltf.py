@@ -1,0 +1,68 @@
+"""glTF 2.0 ingest (cp_gltf_*): triangle primitives and their placement.
+
+``load_gltf`` copies what the library read into numpy arrays; ``world_mesh``
+flattens the instances into one world-space triangle soup for
+:class:`~gpurt_cpq.Mesh`, and the per-primitive arrays feed
+:class:`~gpurt_cpq.Batch` (object space) directly.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import byref, c_int32, c_void_p
+from dataclasses import dataclass
+
+import numpy as np
+
+from ._lib import check, lib
+
+
+@dataclass
+class GltfScene:
+    verts: np.ndarray          # (V, 3) float32, object space, all primitives
+    tris: np.ndarray           # (T, 3) int32, local to each primitive
+    vert_offsets: np.ndarray   # (P + 1,) int64
+    tri_offsets: np.ndarray    # (P + 1,) int64
+    instance_primitive: np.ndarray  # (I,) int32
+    instance_world: np.ndarray      # (I, 4, 4) float32, row-major
+
+    def world_mesh(self) -> tuple[np.ndarray, np.ndarray]:
+        """All instances in world space as one mesh (vertices, triangles)."""
+        vs, ts, base = [], [], 0
+        for p, w in zip(self.instance_primitive, self.instance_world):
+            v = self.verts[self.vert_offsets[p]:self.vert_offsets[p + 1]].astype(np.float64)
+            t = self.tris[self.tri_offsets[p]:self.tri_offsets[p + 1]]
+            vs.append((v @ w[:3, :3].T.astype(np.float64) + w[:3, 3]).astype(np.float32))
+            ts.append(t + base)
+            base += v.shape[0]
+        if not vs:
+            return np.zeros((0, 3), np.float32), np.zeros((0, 3), np.int32)
+        return np.concatenate(vs), np.concatenate(ts).astype(np.int32)
+
+
+def _array(ptr, count, dtype):
+    if count == 0:
+        return np.zeros(0, dtype)
+    ct = np.ctypeslib.as_ctypes_type(dtype)
+    return np.ctypeslib.as_array(ctypes.cast(ptr, ctypes.POINTER(ct)), shape=(count,)).copy()
+
+
+def load_gltf(path: str) -> GltfScene:
+    h = c_void_p()
+    check(lib.cp_gltf_load(str(path).encode(), byref(h)), "cp_gltf_load")
+    try:
+        n = c_int32()
+        pv, pt, pvo, pto = c_void_p(), c_void_p(), c_void_p(), c_void_p()
+        check(lib.cp_gltf_primitives(h, byref(n), byref(pv), byref(pt), byref(pvo), byref(pto)),
+              "cp_gltf_primitives")
+        voff = _array(pvo, n.value + 1, np.int64)
+        toff = _array(pto, n.value + 1, np.int64)
+        verts = _array(pv, int(voff[-1]) * 3, np.float32).reshape(-1, 3)
+        tris = _array(pt, int(toff[-1]) * 3, np.int32).reshape(-1, 3)
+        ni = c_int32()
+        ip, iw = c_void_p(), c_void_p()
+        check(lib.cp_gltf_instances(h, byref(ni), byref(ip), byref(iw)), "cp_gltf_instances")
+        prim = _array(ip, ni.value, np.int32)
+        world = _array(iw, ni.value * 16, np.float32).reshape(-1, 4, 4)
+        return GltfScene(verts, tris, voff, toff, prim, world)
+    finally:
+        lib.cp_gltf_free(h)

@@ -234,6 +234,43 @@ CP_API cp_status cp_query_host(const cp_mesh* mesh, const float* queries, int64_
                                const cp_query_opts* opts, float* out_point, float* out_dist,
                                int32_t* out_tri, float* out_bary, cp_stream_t stream);
 
+/* ---- glTF ingest (host) ---------------------------------------------------- */
+
+/*
+ * Reads a glTF 2.0 scene (.gltf with external or base64 "data:" buffers, or
+ * .glb) on the host, as the reference's Scene::load / Scene::parse_mesh do
+ * with tinygltf (src/scene/scene.cpp:48-315, 317-391), keeping what the
+ * closest-point path needs: triangle geometry and where it is placed.
+ *
+ * Primitives: every meshes[i].primitives[j] in file order whose mode is
+ * TRIANGLES, TRIANGLE_STRIP (triangles (k-2, k-1, k)) or TRIANGLE_FAN
+ * ((0, k-1, k)), as parse_mesh converts them; other modes are skipped.
+ * POSITION must be FLOAT VEC3; indices may be (U)BYTE, (U)SHORT or UINT, or
+ * absent (0..count-1).  Vertices are in the mesh's own (object) space,
+ * indices local to the primitive; vert_offsets / tri_offsets have
+ * num_primitives + 1 entries, so the arrays feed cp_batch_create directly.
+ *
+ * Instances: every scene's root nodes, depth first, one instance per
+ * primitive of each node's mesh, in the order Scene::load adds objects; world = parent * local with local the node's
+ * "matrix" or T * R * S of its translation / rotation / scale.  (The
+ * reference reads only "matrix", so it places TRS-only nodes at identity.)
+ * Matrices are 4 x 4 row-major floats.
+ *
+ * Arrays returned by cp_gltf_* are owned by the handle and live until
+ * cp_gltf_free.  Errors (unreadable file, malformed JSON, an accessor out of
+ * its buffer, an index past its vertices) return CP_ERROR_INVALID_VALUE with
+ * the reason in cp_last_error_string().  No CUDA device is needed.
+ */
+typedef struct cp_gltf cp_gltf;
+
+CP_API cp_status cp_gltf_load(const char* path, cp_gltf** out);
+CP_API void cp_gltf_free(cp_gltf* scene);
+CP_API cp_status cp_gltf_primitives(const cp_gltf* scene, int32_t* num_primitives,
+                                    const float** verts, const int32_t** tris,
+                                    const int64_t** vert_offsets, const int64_t** tri_offsets);
+CP_API cp_status cp_gltf_instances(const cp_gltf* scene, int32_t* num_instances,
+                                   const int32_t** primitive, const float** world);
+
 /* ---- ray queries ----------------------------------------------------------- */
 
 /*
