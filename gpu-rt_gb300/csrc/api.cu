@@ -728,6 +728,219 @@ CP_API cp_status cp_batch_query(cp_batch* bt, const float* queries, const int64_
     return CP_SUCCESS;
 }
 
+}  // extern "C"
+
+// ---- instanced scenes ------------------------------------------------------
+
+struct cp_scene {
+    Bvh top;                    // over the instances' proxies, one per instance
+    const cp_batch* batch = nullptr;
+    int32_t n = 0;
+    int32_t* d_inst_mesh = nullptr;
+    float* d_fwd = nullptr;     // n x 12 world <- object
+    float* d_inv = nullptr;     // n x 12 object <- world
+    float* d_s2 = nullptr;      // n x 2: squared scale, lower bound of the squared stretch
+};
+
+namespace {
+
+// Per instance: the matrix as given, its inverse (in double, rounded once),
+// the squared scale s^2 = tr(M^T M) / 3 and a lower bound of M^T M's smallest
+// eigenvalue (Gershgorin).  Refuses non-finite and non-similarity matrices.
+cp_status instance_frames(const float* T, int32_t n, std::vector<float>& fwd, std::vector<float>& inv,
+                          std::vector<float>& s2) {
+    fwd.assign(T, T + (size_t)12 * n);
+    inv.resize((size_t)12 * n);
+    s2.resize((size_t)2 * n);
+    for (int32_t i = 0; i < n; ++i) {
+        const float* t = T + (size_t)12 * i;
+        for (int k = 0; k < 12; ++k)
+            if (!std::isfinite(t[k]))
+                return fail(CP_ERROR_INVALID_VALUE, "instance " + std::to_string(i) + ": non-finite transform");
+        double M[3][3], tr[3];
+        for (int r = 0; r < 3; ++r) {
+            for (int c = 0; c < 3; ++c) M[r][c] = t[4 * r + c];
+            tr[r] = t[4 * r + 3];
+        }
+        double G[3][3];
+        for (int j = 0; j < 3; ++j)
+            for (int k = 0; k < 3; ++k) G[j][k] = M[0][j] * M[0][k] + M[1][j] * M[1][k] + M[2][j] * M[2][k];
+        const double s = (G[0][0] + G[1][1] + G[2][2]) / 3.0;
+        if (!(s > 1e-30) || !std::isfinite(s))
+            return fail(CP_ERROR_INVALID_VALUE, "instance " + std::to_string(i) + ": singular transform");
+        double dev = 0.0, lo = INFINITY;
+        for (int j = 0; j < 3; ++j) {
+            double off = 0.0;
+            for (int k = 0; k < 3; ++k) {
+                dev = std::max(dev, std::fabs(G[j][k] - (j == k ? s : 0.0)));
+                if (k != j) off += std::fabs(G[j][k]);
+            }
+            lo = std::min(lo, G[j][j] - off);
+        }
+        if (dev > 1e-5 * s)
+            return fail(CP_ERROR_INVALID_VALUE,
+                        "instance " + std::to_string(i) +
+                            ": transform is not a similarity (rotation or reflection, uniform scale, translation)");
+        const double det = M[0][0] * (M[1][1] * M[2][2] - M[1][2] * M[2][1]) -
+                           M[0][1] * (M[1][0] * M[2][2] - M[1][2] * M[2][0]) +
+                           M[0][2] * (M[1][0] * M[2][1] - M[1][1] * M[2][0]);
+        double A[3][3];  // inverse by the adjugate
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) {
+                const int r1 = (c + 1) % 3, r2 = (c + 2) % 3, c1 = (r + 1) % 3, c2 = (r + 2) % 3;
+                A[r][c] = (M[r1][c1] * M[r2][c2] - M[r1][c2] * M[r2][c1]) / det;
+            }
+        float* o = inv.data() + (size_t)12 * i;
+        for (int r = 0; r < 3; ++r) {
+            for (int c = 0; c < 3; ++c) o[4 * r + c] = (float)A[r][c];
+            o[4 * r + 3] = (float)-(A[r][0] * tr[0] + A[r][1] * tr[1] + A[r][2] * tr[2]);
+        }
+        s2[2 * i] = (float)s;
+        s2[2 * i + 1] = (float)(lo * (1.0 - 1e-6));
+    }
+    return CP_SUCCESS;
+}
+
+// Frames to the device, proxies, top-level build.  The top level has the
+// batch's branching factor and one instance per leaf.
+cp_status scene_build(cp_scene* sc, const float* T, cudaStream_t st) {
+    std::vector<float> fwd, inv, s2;
+    cp_status s = instance_frames(T, sc->n, fwd, inv, s2);
+    if (s != CP_SUCCESS) return s;
+    const size_t n = (size_t)sc->n;
+    CP_CUDA(cudaMemcpyAsync(sc->d_fwd, fwd.data(), sizeof(float) * 12 * n, cudaMemcpyHostToDevice, st), "scene upload");
+    CP_CUDA(cudaMemcpyAsync(sc->d_inv, inv.data(), sizeof(float) * 12 * n, cudaMemcpyHostToDevice, st), "scene upload");
+    CP_CUDA(cudaMemcpyAsync(sc->d_s2, s2.data(), sizeof(float) * 2 * n, cudaMemcpyHostToDevice, st), "scene upload");
+    float* verts = nullptr;
+    int32_t* tris = nullptr;
+    if (cudaMalloc(&verts, sizeof(float) * 6 * n) != cudaSuccess ||
+        cudaMalloc(&tris, sizeof(int32_t) * 3 * n) != cudaSuccess) {
+        cudaFree(verts);
+        return fail(CP_ERROR_OUT_OF_MEMORY, "scene proxies");
+    }
+    cudaError_t e = instance_proxies(sc->batch->bvh, sc->d_inst_mesh, sc->d_fwd, sc->n, verts, tris, st);
+    if (e == cudaSuccess) {
+        bvh_free(sc->top);
+        sc->top = Bvh();
+        cp_build_opts bo;
+        cp_build_opts_default(&bo);
+        bo.branching = sc->batch->bvh.p.K;
+        bo.leaf_size = 1;
+        s = build_common(sc->top, verts, 12, tris, {0, (int64_t)(2 * n)}, {0, (int64_t)n}, &bo, st);
+    }
+    cudaError_t e2 = cudaStreamSynchronize(st);
+    cudaFree(verts);
+    cudaFree(tris);
+    if (e != cudaSuccess) return cuda_fail(e, "scene proxies");
+    if (s != CP_SUCCESS) return s;
+    if (e2 != cudaSuccess) return cuda_fail(e2, "scene build");
+    return CP_SUCCESS;
+}
+
+void scene_free(cp_scene* sc) {
+    cudaFree(sc->d_inst_mesh);
+    cudaFree(sc->d_fwd);
+    cudaFree(sc->d_inv);
+    cudaFree(sc->d_s2);
+    bvh_free(sc->top);
+    delete sc;
+}
+
+}  // namespace
+
+extern "C" {
+
+CP_API cp_status cp_scene_create(const cp_batch* batch, const int32_t* instance_mesh,
+                                 const float* instance_transform, int32_t n_instances,
+                                 cp_stream_t stream, cp_scene** out) {
+    if (!out) return fail(CP_ERROR_INVALID_VALUE, "out is NULL");
+    *out = nullptr;
+    if (!batch || !instance_mesh || !instance_transform) return fail(CP_ERROR_INVALID_VALUE, "NULL argument");
+    if (n_instances <= 0) return fail(CP_ERROR_INVALID_VALUE, "a scene needs at least one instance");
+    if (n_instances > kMaxTriangles) return fail(CP_ERROR_NOT_SUPPORTED, "more than 2^27 - 1 instances");
+    for (int32_t i = 0; i < n_instances; ++i)
+        if (instance_mesh[i] < 0 || instance_mesh[i] >= batch->bvh.nmeshes)
+            return fail(CP_ERROR_INVALID_VALUE, "instance " + std::to_string(i) + ": mesh id out of range");
+    cp_status s = require_gpu();
+    if (s != CP_SUCCESS) return s;
+    cp_scene* sc = new (std::nothrow) cp_scene();
+    if (!sc) return fail(CP_ERROR_OUT_OF_MEMORY, "host allocation of the handle failed");
+    sc->batch = batch;
+    sc->n = n_instances;
+    const size_t n = (size_t)n_instances;
+    if (cudaMalloc(&sc->d_inst_mesh, sizeof(int32_t) * n) != cudaSuccess ||
+        cudaMalloc(&sc->d_fwd, sizeof(float) * 12 * n) != cudaSuccess ||
+        cudaMalloc(&sc->d_inv, sizeof(float) * 12 * n) != cudaSuccess ||
+        cudaMalloc(&sc->d_s2, sizeof(float) * 2 * n) != cudaSuccess) {
+        scene_free(sc);
+        return fail(CP_ERROR_OUT_OF_MEMORY, "scene instance arrays");
+    }
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    cudaError_t e = cudaMemcpyAsync(sc->d_inst_mesh, instance_mesh, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) {
+        scene_free(sc);
+        return cuda_fail(e, "scene upload");
+    }
+    s = scene_build(sc, instance_transform, st);
+    if (s != CP_SUCCESS) {
+        scene_free(sc);
+        return s;
+    }
+    *out = sc;
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_scene_update(cp_scene* scene, const float* instance_transform, cp_stream_t stream) {
+    if (!scene || !instance_transform) return fail(CP_ERROR_INVALID_VALUE, "scene or transforms is NULL");
+    return scene_build(scene, instance_transform, reinterpret_cast<cudaStream_t>(stream));
+}
+
+CP_API cp_status cp_scene_destroy(cp_scene* scene) {
+    if (scene) scene_free(scene);
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_scene_query_workspace_size(const cp_scene* scene, int64_t nq,
+                                               const cp_query_opts* opts, size_t* bytes) {
+    if (!scene || !bytes) return fail(CP_ERROR_INVALID_VALUE, "scene or bytes is NULL");
+    if (nq < 0) return fail(CP_ERROR_INVALID_VALUE, "negative query count");
+    QueryParams qp;
+    cp_status s = to_query_params(opts, &qp);
+    if (s != CP_SUCCESS) return s;
+    *bytes = query_workspace_bytes(scene->top, nq, qp);
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_scene_query(const cp_scene* scene, const float* queries, int64_t nq,
+                                const cp_query_opts* opts, float* out_point, float* out_dist,
+                                int32_t* out_instance, int32_t* out_tri, float* out_bary,
+                                void* workspace, size_t ws_bytes, cp_stream_t stream) {
+    if (!scene) return fail(CP_ERROR_INVALID_VALUE, "scene is NULL");
+    if (nq < 0) return fail(CP_ERROR_INVALID_VALUE, "negative query count");
+    if (nq > INT32_MAX) return fail(CP_ERROR_NOT_SUPPORTED, "more than 2^31 - 1 queries in one call");
+    if (nq == 0) return CP_SUCCESS;
+    if (!queries) return fail(CP_ERROR_INVALID_VALUE, "queries is NULL");
+    QueryParams qp;
+    cp_status s = to_query_params(opts, &qp);
+    if (s != CP_SUCCESS) return s;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const size_t need = query_workspace_bytes(scene->top, nq, qp);
+    void* own = nullptr;
+    if (!workspace) {
+        CP_CUDA(ws_alloc(&own, need, st), "workspace allocation");
+        workspace = own;
+        ws_bytes = need;
+    } else if (ws_bytes < need) {
+        return fail(CP_ERROR_SCRATCH_TOO_SMALL, "workspace smaller than cp_scene_query_workspace_size()");
+    }
+    cudaError_t e = bvh_instance_query(scene->top, scene->batch->bvh, scene->d_inst_mesh, scene->d_inv,
+                                       scene->d_fwd, scene->d_s2, queries, nq, qp.sort != 0, out_point,
+                                       out_dist, out_instance, out_tri, out_bary, workspace, ws_bytes, st);
+    if (own) cudaFreeAsync(own, st);
+    if (e != cudaSuccess) return cuda_fail(e, "scene query");
+    return CP_SUCCESS;
+}
+
 // ---- inspection ------------------------------------------------------------
 
 CP_API cp_status cp_mesh_export_build(const cp_mesh* m, uint64_t* keys, int32_t* order, int32_t* left,

@@ -108,6 +108,23 @@ void timing_enable(bool events, bool counters);
 cudaError_t timing_read(double* ms, int64_t* launches, bool reset);
 cudaError_t traversal_stats(unsigned long long* out4, bool reset);
 
+// Proxy triangles for the top level of an instanced scene: per instance the
+// world box of its mesh in `bottom` as (lo, hi, hi); verts 2n x 3, tris n x 3.
+cudaError_t instance_proxies(const Bvh& bottom, const int32_t* inst_mesh, const float* inst_fwd,
+                             int32_t n, float* verts, int32_t* tris, cudaStream_t st);
+
+// Closest points over instances (similarity transforms) of a batch's meshes:
+// `top` is a BVH over the instances' proxies (local index = instance),
+// `bottom` the batch.  inst_inv / inst_fwd: 12 floats per instance (object <-
+// world, world <- object, row-major 3 x 4); inst_s2: 2 per instance, the
+// squared scale and a lower bound of the smallest squared stretch.
+// Workspace: query_workspace_bytes(top, nq, ...) with the same sort flag.
+cudaError_t bvh_instance_query(const Bvh& top, const Bvh& bottom, const int32_t* inst_mesh,
+                               const float* inst_inv, const float* inst_fwd, const float* inst_s2,
+                               const float* queries, int64_t nq, bool sort, float* out_point,
+                               float* out_dist, int32_t* out_inst, int32_t* out_tri, float* out_bary,
+                               void* ws, size_t ws_bytes, cudaStream_t st);
+
 cudaError_t bvh_backward(const Bvh& b, const float* queries, const int32_t* tri, const float* bary,
                          const float* grad_dist, int64_t nq, float* grad_q, float* grad_verts,
                          cudaStream_t st);

@@ -282,17 +282,9 @@ __device__ __forceinline__ TriDiff tri_diff(float qx, float qy, float qz, const 
 // (numerator v, numerator w, denominator) triple, the one of the region
 // found is kept, and one reciprocal finishes it — so lanes of a warp in
 // different regions do not serialise.
-__device__ void precise_bary_d(float qx, float qy, float qz, const TriRec& r, const TriDiff& t, ff& v,
-                               ff& w) {
-    if (__float_as_uint(r.p2.z) & kTriDegenerate) {
-        float fv, fw;
-        degenerate_bary(qx, qy, qz, r, fv, fw);
-        v = ff_from(fv);
-        w = ff_from(fw);
-        return;
-    }
-    const ff3 bp = ff3_diff(qx, qy, qz, r.p0.w, r.p1.x, r.p1.y);
-    const ff3 cp = ff3_diff(qx, qy, qz, r.p1.z, r.p1.w, r.p2.x);
+// The region logic on float-float edge vectors ab, ac and offsets ap, bp, cp
+// of the query from a, b and c.
+__device__ void precise_bary_core(const TriDiff& t, const ff3& bp, const ff3& cp, ff& v, ff& w) {
     const ff d1 = ff3_dot_fast(t.ab, t.ap), d2 = ff3_dot_fast(t.ac, t.ap);
     const ff d3 = ff3_dot_fast(t.ab, bp), d4 = ff3_dot_fast(t.ac, bp);
     const ff d5 = ff3_dot_fast(t.ab, cp), d6 = ff3_dot_fast(t.ac, cp);
@@ -330,6 +322,19 @@ __device__ void precise_bary_d(float qx, float qy, float qz, const TriRec& r, co
     const ff rd = ff_recip(dn);
     v = ff_mul(nv, rd);
     w = ff_mul(nw, rd);
+}
+
+__device__ void precise_bary_d(float qx, float qy, float qz, const TriRec& r, const TriDiff& t, ff& v,
+                               ff& w) {
+    if (__float_as_uint(r.p2.z) & kTriDegenerate) {
+        float fv, fw;
+        degenerate_bary(qx, qy, qz, r, fv, fw);
+        v = ff_from(fv);
+        w = ff_from(fw);
+        return;
+    }
+    precise_bary_core(t, ff3_diff(qx, qy, qz, r.p0.w, r.p1.x, r.p1.y),
+                      ff3_diff(qx, qy, qz, r.p1.z, r.p1.w, r.p2.x), v, w);
 }
 
 __device__ void precise_bary(float qx, float qy, float qz, const TriRec& r, ff& v, ff& w) {
@@ -1222,6 +1227,311 @@ cudaError_t launch_k(const TraverseArgs& args, const QueryParams& qp, int cap, b
     }
 }
 
+// ---- instances: two-level traversal ------------------------------------------
+//
+// The reference places meshes with a TLAS of transformed BLAS instances
+// (Accel::recreate(blas, T), src/vk/vulkan.cpp:777-856; per-object model
+// matrices, src/rt/rt.cpp:31-45).  Here a top-level wide BVH over the
+// instances' world boxes is walked closest first in world space; at an
+// instance the query is taken to the mesh's object space and the mesh's own
+// BVH (a batch's) is walked with the world bound divided by the instance's
+// squared scale — instances are similarity transforms, under which distances
+// scale by s.  The winner is re-evaluated in float-float in WORLD space: its
+// object-space barycentrics give the point, the instance's 3x4 matrix takes
+// it to world space in float-float, and the residual to the query is formed
+// there, so the distance keeps the accuracy of the plain path.
+
+struct InstArgs {
+    const void* tnodes;        // top level: wide BVH over the instances' world boxes
+    const TriRec* trecs;       // its leaf records; p2.y = instance index
+    const int32_t* troot;      // device: its root reference
+    const void* bnodes;        // bottom level: the batch's meshes
+    const FastTri* bfast;
+    const TriRec* brecs;
+    const int32_t* broot;      // per mesh
+    const int32_t* inst_mesh;  // per instance
+    const float* inst_inv;     // 12 per instance: object <- world, row-major 3 x 4
+    const float* inst_fwd;     // 12 per instance: world <- object
+    const float* inst_s2;      // 2 per instance: squared scale (ranking), its lower bound (pruning)
+    const float* queries;
+    const int32_t* perm;
+    int64_t nq;
+    float* out_point;
+    float* out_dist;
+    int32_t* out_inst;
+    int32_t* out_tri;
+    float* out_bary;
+    unsigned long long* counter;
+    uint32_t* status;
+};
+
+__device__ __forceinline__ void affine(const float* m, float x, float y, float z, float& ox, float& oy,
+                                       float& oz) {
+    ox = fmaf(m[0], x, fmaf(m[1], y, fmaf(m[2], z, m[3])));
+    oy = fmaf(m[4], x, fmaf(m[5], y, fmaf(m[6], z, m[7])));
+    oz = fmaf(m[8], x, fmaf(m[9], y, fmaf(m[10], z, m[11])));
+}
+
+// Closest-first walk of one mesh's BVH from `root` for one point: nodes whose
+// box bound is below `lim` are visited nearest first; on return `lim` is the
+// best squared distance found (unchanged if none), with its record and index.
+// The stack holds at most (K-1)(depth+1) <= kStackTotal entries.
+template <int K>
+__device__ void walk_mesh(const WideNode<K>* __restrict__ nodes, const FastTri* __restrict__ fast,
+                     const TriRec* __restrict__ recs, int32_t root, float qx, float qy, float qz,
+                     float& lim, int& rec, int& idx, float2* stack, uint32_t* status) {
+    int sp = 0;
+    stack[sp++] = make_float2(0.0f, __int_as_float(root));
+    while (sp > 0) {
+        const float2 e = stack[--sp];
+        if (!(e.x < lim)) continue;
+        const int cur = __float_as_int(e.y);
+        if (cur >= 0) {
+            const WideNode<K>* nd = nodes + cur;
+            float lox[K], hix[K], loy[K], hiy[K], loz[K], hiz[K];
+            int32_t ch[K];
+            load_row<K>(nd->lox, lox);
+            load_row<K>(nd->hix, hix);
+            load_row<K>(nd->loy, loy);
+            load_row<K>(nd->hiy, hiy);
+            load_row<K>(nd->loz, loz);
+            load_row<K>(nd->hiz, hiz);
+            load_row_i<K>(nd->child, ch);
+            float lb[K];
+#pragma unroll
+            for (int s = 0; s < K; ++s) {
+                const float d = box_lb2(qx, qy, qz, lox[s], hix[s], loy[s], hiy[s], loz[s], hiz[s]);
+                lb[s] = d < lim ? d : INFINITY;
+            }
+            sort_children<K>(lb, ch);
+#pragma unroll
+            for (int s = K - 1; s >= 0; --s) {
+                if (lb[s] < INFINITY) {
+                    if (sp < kStackTotal) stack[sp++] = make_float2(lb[s], __int_as_float(ch[s]));
+                    else atomicOr(status, 1u);
+                }
+            }
+        } else {
+            const int first = leaf_first(cur), cnt = leaf_count(cur);
+            for (int k = 0; k < cnt; ++k) {
+                const float4* fp = reinterpret_cast<const float4*>(fast + first + k);
+                FastTri f;
+                f.p0 = __ldg(fp);
+                f.p1 = __ldg(fp + 1);
+                f.p2 = __ldg(fp + 2);
+                f.p3 = __ldg(fp + 3);
+                const float d2 = tri_d2_fast(qx, qy, qz, f);
+                const int i = __float_as_int(f.p3.w);
+                if (d2 < lim || (d2 == lim && rec >= 0 && i < idx)) {
+                    lim = d2;
+                    rec = first + k;
+                    idx = i;
+                }
+            }
+        }
+    }
+}
+
+// One query of the two-level walk (index i in the work order).
+template <int K>
+__device__ void instance_point(const InstArgs& a, const WideNode<K>* __restrict__ tnodes,
+                               const WideNode<K>* __restrict__ bnodes, int32_t troot, int64_t i,
+                               float2* tstack, float2* bstack) {
+    const int64_t qi = a.perm ? (int64_t)a.perm[i] : i;
+    const float qx = a.queries[3 * qi], qy = a.queries[3 * qi + 1], qz = a.queries[3 * qi + 2];
+    float best = INFINITY;
+    int binst = -1, brec = -1, bidx = INT_MAX;
+    // top level: closest first over instance boxes, instances walked as found
+    int tsp = 0;
+    tstack[tsp++] = make_float2(0.0f, __int_as_float(troot));
+    while (tsp > 0) {
+        const float2 e = tstack[--tsp];
+        if (!(e.x < best)) continue;
+        const int cur = __float_as_int(e.y);
+        if (cur >= 0) {
+            const WideNode<K>* nd = tnodes + cur;
+            float lox[K], hix[K], loy[K], hiy[K], loz[K], hiz[K];
+            int32_t ch[K];
+            load_row<K>(nd->lox, lox);
+            load_row<K>(nd->hix, hix);
+            load_row<K>(nd->loy, loy);
+            load_row<K>(nd->hiy, hiy);
+            load_row<K>(nd->loz, loz);
+            load_row<K>(nd->hiz, hiz);
+            load_row_i<K>(nd->child, ch);
+            float lb[K];
+#pragma unroll
+            for (int s = 0; s < K; ++s) {
+                const float d = box_lb2(qx, qy, qz, lox[s], hix[s], loy[s], hiy[s], loz[s], hiz[s]);
+                lb[s] = d < best ? d : INFINITY;
+            }
+            sort_children<K>(lb, ch);
+#pragma unroll
+            for (int s = K - 1; s >= 0; --s) {
+                if (lb[s] < INFINITY) {
+                    if (tsp < kStackTotal) tstack[tsp++] = make_float2(lb[s], __int_as_float(ch[s]));
+                    else atomicOr(a.status, 1u);
+                }
+            }
+            continue;
+        }
+        const int first = leaf_first(cur), cnt = leaf_count(cur);
+        for (int k = 0; k < cnt; ++k) {
+            const int inst = __float_as_int(__ldg(&a.trecs[first + k].p2.y));
+            const float* inv = a.inst_inv + 12 * inst;
+            float ox, oy, oz;
+            affine(inv, qx, qy, qz, ox, oy, oz);
+            const float s2 = a.inst_s2[2 * inst], s2lo = a.inst_s2[2 * inst + 1];
+            // object-space bound: below it lies every triangle whose world
+            // distance can beat `best` (s2lo bounds the transform's
+            // smallest squared stretch), widened for the FP32 rounding
+            float lim = best < INFINITY ? best / s2lo * (1.0f + 1e-5f) : INFINITY;
+            int rec = -1, idx = INT_MAX;
+            walk_mesh<K>(bnodes, a.bfast, a.brecs, a.broot[a.inst_mesh[inst]], ox, oy, oz, lim, rec,
+                           idx, bstack, a.status);
+            if (rec < 0) continue;
+            const float d2w = lim * s2;
+            if (d2w < best || (d2w == best && (inst < binst || (inst == binst && idx < bidx)))) {
+                best = d2w;
+                binst = inst;
+                brec = rec;
+                bidx = idx;
+            }
+        }
+    }
+    float dist = __int_as_float(0x7fc00000), px = dist, py = dist, pz = dist, bv = dist, bw = dist;
+    if (brec >= 0) {
+        const float4* rp = reinterpret_cast<const float4*>(a.brecs + brec);
+        TriRec r;
+        r.p0 = __ldg(rp);
+        r.p1 = __ldg(rp + 1);
+        r.p2 = __ldg(rp + 2);
+        // the world triangle: the instance matrix applied to the FP32
+        // vertices in float-float (products exact, sums to ~2^-44)
+        const float* f = a.inst_fwd + 12 * binst;
+        const float ov[3][3] = {{r.p0.x, r.p0.y, r.p0.z}, {r.p0.w, r.p1.x, r.p1.y}, {r.p1.z, r.p1.w, r.p2.x}};
+        ff3 wv[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+            ff c[3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+                c[j] = ff_add(ff_add(ff_two_prod(f[4 * j], ov[k][0]), ff_two_prod(f[4 * j + 1], ov[k][1])),
+                              ff_add(ff_two_prod(f[4 * j + 2], ov[k][2]), ff_from(f[4 * j + 3])));
+            wv[k] = {c[0], c[1], c[2]};
+        }
+        const ff3 q3 = ff3_from(qx, qy, qz);
+        TriDiff t;
+        t.ab = ff3_sub(wv[1], wv[0]);
+        t.ac = ff3_sub(wv[2], wv[0]);
+        t.ap = ff3_sub(q3, wv[0]);
+        ff v, w;
+        if (__float_as_uint(r.p2.z) & kTriDegenerate) {
+            TriRec rw = r;  // degenerate: the FP32 edge search on the rounded world vertices
+            rw.p0 = make_float4(ff_to_float(wv[0].x), ff_to_float(wv[0].y), ff_to_float(wv[0].z),
+                                ff_to_float(wv[1].x));
+            rw.p1 = make_float4(ff_to_float(wv[1].y), ff_to_float(wv[1].z), ff_to_float(wv[2].x),
+                                ff_to_float(wv[2].y));
+            rw.p2.x = ff_to_float(wv[2].z);
+            float fv, fw;
+            degenerate_bary(qx, qy, qz, rw, fv, fw);
+            v = ff_from(fv);
+            w = ff_from(fw);
+        } else {
+            precise_bary_core(t, ff3_sub(q3, wv[1]), ff3_sub(q3, wv[2]), v, w);
+        }
+        ff3 res, off;
+        precise_residual_d(t, v, w, res, off);
+        dist = ff_to_float(ff_sqrt(ff3_dot(res, res)));
+        px = ff_to_float(ff_add(wv[0].x, off.x));
+        py = ff_to_float(ff_add(wv[0].y, off.y));
+        pz = ff_to_float(ff_add(wv[0].z, off.z));
+        bv = ff_to_float(v);
+        bw = ff_to_float(w);
+    } else {
+        atomicOr(a.status, 4u);
+    }
+    if (a.out_dist) a.out_dist[qi] = dist;
+    if (a.out_inst) a.out_inst[qi] = binst;
+    if (a.out_tri) a.out_tri[qi] = brec >= 0 ? bidx : -1;
+    if (a.out_point) {
+        a.out_point[3 * qi] = px;
+        a.out_point[3 * qi + 1] = py;
+        a.out_point[3 * qi + 2] = pz;
+    }
+    if (a.out_bary) {
+        a.out_bary[2 * qi] = bv;
+        a.out_bary[2 * qi + 1] = bw;
+    }
+}
+
+template <int K>
+__global__ void __launch_bounds__(128) k_instances(InstArgs a) {
+    const int lane = threadIdx.x & 31;
+    const WideNode<K>* __restrict__ tnodes = static_cast<const WideNode<K>*>(a.tnodes);
+    const WideNode<K>* __restrict__ bnodes = static_cast<const WideNode<K>*>(a.bnodes);
+    float2 tstack[kStackTotal];
+    float2 bstack[kStackTotal];
+    const int32_t troot = __ldg(a.troot);
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(a.counter, 32ull);
+        base = __shfl_sync(kFull, base, 0);
+        if (base >= (unsigned long long)a.nq) break;
+        const int64_t i = (int64_t)base + lane;
+        if (i < a.nq) instance_point<K>(a, tnodes, bnodes, troot, i, tstack, bstack);
+    }
+}
+
+// One proxy triangle (lo, hi, hi) per instance: the world box of its mesh's
+// root box (the 8 corners through the instance matrix), padded by 2^-20 of
+// the terms' magnitude so that FP32 rounding cannot shrink it.
+__global__ void k_instance_proxies(const float* __restrict__ box, const int32_t* __restrict__ mesh_root,
+                                   const int32_t* __restrict__ inst_mesh, const float* __restrict__ fwd,
+                                   int32_t n, float* __restrict__ verts, int32_t* __restrict__ tris) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* bx = box + 6 * (int64_t)mesh_root[inst_mesh[i]];
+    const float* m = fwd + 12 * i;
+    float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (int c = 0; c < 8; ++c) {
+        float w[3];
+        affine(m, bx[(c & 1) ? 3 : 0], bx[(c & 2) ? 4 : 1], bx[(c & 4) ? 5 : 2], w[0], w[1], w[2]);
+        for (int k = 0; k < 3; ++k) {
+            lo[k] = fminf(lo[k], w[k]);
+            hi[k] = fmaxf(hi[k], w[k]);
+        }
+    }
+    const float ax = fmaxf(fabsf(bx[0]), fabsf(bx[3])), ay = fmaxf(fabsf(bx[1]), fabsf(bx[4])),
+                az = fmaxf(fabsf(bx[2]), fabsf(bx[5]));
+    for (int k = 0; k < 3; ++k) {
+        const float mag = fabsf(m[4 * k]) * ax + fabsf(m[4 * k + 1]) * ay + fabsf(m[4 * k + 2]) * az +
+                          fabsf(m[4 * k + 3]);
+        const float pad = mag * 0x1p-20f + 1e-30f;
+        verts[6 * (int64_t)i + k] = lo[k] - pad;
+        verts[6 * (int64_t)i + 3 + k] = hi[k] + pad;
+    }
+    tris[3 * (int64_t)i] = 2 * i;
+    tris[3 * (int64_t)i + 1] = 2 * i + 1;
+    tris[3 * (int64_t)i + 2] = 2 * i + 1;
+}
+
+template <int K>
+cudaError_t launch_instances(const InstArgs& args, cudaStream_t st) {
+    auto kern = k_instances<K>;
+    int sms = 0;
+    cudaError_t e = sm_count(&sms);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cpq::blocks_per_sm(reinterpret_cast<const void*>(kern), 128, 0, &per_sm);
+    if (e != cudaSuccess) return e;
+    int64_t grid = (int64_t)sms * per_sm;
+    const int64_t need = ((args.nq + 31) / 32 * 32 + 127) / 128;
+    if (grid > need) grid = need;
+    kern<<<(unsigned)grid, 128, 0, st>>>(args); note_launch();
+    return cudaGetLastError();
+}
+
 }  // namespace
 
 void timing_enable(bool events, bool counters) {
@@ -1381,6 +1691,51 @@ cudaError_t bvh_backward(const Bvh& b, const float* queries, const int32_t* tri,
                                                              queries, tri, bary, grad_dist, nq,
                                                              grad_q, grad_verts, b.status); note_launch();
     return cudaGetLastError();
+}
+
+cudaError_t instance_proxies(const Bvh& bottom, const int32_t* inst_mesh, const float* inst_fwd,
+                             int32_t n, float* verts, int32_t* tris, cudaStream_t st) {
+    if (n <= 0) return cudaSuccess;
+    k_instance_proxies<<<(n + 127) / 128, 128, 0, st>>>(bottom.box, bottom.mesh_root, inst_mesh, inst_fwd, n,
+                                                        verts, tris);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t bvh_instance_query(const Bvh& top, const Bvh& bottom, const int32_t* inst_mesh,
+                               const float* inst_inv, const float* inst_fwd, const float* inst_s2,
+                               const float* queries, int64_t nq, bool sort, float* out_point,
+                               float* out_dist, int32_t* out_inst, int32_t* out_tri, float* out_bary,
+                               void* ws, size_t ws_bytes, cudaStream_t st) {
+    if (nq <= 0) return cudaSuccess;
+    if (top.p.K != bottom.p.K) return cudaErrorInvalidValue;
+    InstArgs a;
+    cudaError_t e = order_points(top, queries, nq, nullptr, sort, ws, ws_bytes, st, &a.perm, &a.counter);
+    if (e != cudaSuccess) return e;
+    a.tnodes = top.nodes;
+    a.trecs = top.recs;
+    a.troot = top.wide_root;
+    a.bnodes = bottom.nodes;
+    a.bfast = bottom.fast;
+    a.brecs = bottom.recs;
+    a.broot = bottom.wide_root;
+    a.inst_mesh = inst_mesh;
+    a.inst_inv = inst_inv;
+    a.inst_fwd = inst_fwd;
+    a.inst_s2 = inst_s2;
+    a.queries = queries;
+    a.nq = nq;
+    a.out_point = out_point;
+    a.out_dist = out_dist;
+    a.out_inst = out_inst;
+    a.out_tri = out_tri;
+    a.out_bary = out_bary;
+    a.status = bottom.status;
+    switch (top.p.K) {
+        case 2: return launch_instances<2>(a, st);
+        case 4: return launch_instances<4>(a, st);
+        default: return launch_instances<8>(a, st);
+    }
 }
 
 }  // namespace cpq

@@ -2,12 +2,12 @@
 
 Mesh in, BVH built on the GPU, a batch of points in; closest point, unsigned
 distance and triangle index out.  See :class:`Mesh`, :class:`Batch` and
-:func:`closest_distance`.
+:class:`Scene` (instances) and :func:`closest_distance`.
 """
 from ._lib import CpError, LIB_PATH, lib  # noqa: F401  (raises if the library is missing)
 from .gltf import GltfScene, load_gltf  # noqa: F401
-from .mesh import (Batch, Mesh, QueryResult, RayResult, autotune, build_opts,  # noqa: F401
-                   closest_distance, query_opts, ray_opts)
+from .mesh import (Batch, Mesh, QueryResult, RayResult, Scene, SceneResult, autotune,  # noqa: F401
+                   build_opts, closest_distance, query_opts, ray_opts)
 
-__all__ = ["Mesh", "Batch", "QueryResult", "RayResult", "closest_distance", "autotune", "build_opts",
+__all__ = ["Mesh", "Batch", "Scene", "SceneResult", "QueryResult", "RayResult", "closest_distance", "autotune", "build_opts",
            "query_opts", "ray_opts", "load_gltf", "GltfScene", "CpError", "lib", "LIB_PATH"]

@@ -108,6 +108,12 @@ SIGNATURES = {
     "cp_batch_query": (c_int32, [c_void_p, c_void_p, c_void_p, POINTER(QueryOpts), c_void_p,
                                  c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_int32,
                                  c_void_p]),
+    "cp_scene_create": (c_int32, [c_void_p, c_void_p, c_void_p, c_int32, c_void_p, POINTER(c_void_p)]),
+    "cp_scene_update": (c_int32, [c_void_p, c_void_p, c_void_p]),
+    "cp_scene_destroy": (c_int32, [c_void_p]),
+    "cp_scene_query_workspace_size": (c_int32, [c_void_p, c_int64, POINTER(QueryOpts), POINTER(c_size_t)]),
+    "cp_scene_query": (c_int32, [c_void_p, c_void_p, c_int64, POINTER(QueryOpts), c_void_p, c_void_p,
+                                 c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
     "cp_autotune": (c_int32, [c_void_p, c_int64, c_void_p, c_int64, c_void_p, c_int64, c_char_p,
                               POINTER(BuildOpts), POINTER(QueryOpts)]),
     "cp_size_class": (c_int32, [c_int64]),

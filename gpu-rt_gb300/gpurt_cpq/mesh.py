@@ -335,6 +335,84 @@ class Batch:
         return out
 
 
+@dataclass
+class SceneResult:
+    point: torch.Tensor | None   # (N, 3) float32, world space
+    dist: torch.Tensor           # (N,) float32, world units
+    instance: torch.Tensor       # (N,) int32
+    tri: torch.Tensor            # (N,) int32, local to the instance's mesh
+    bary: torch.Tensor | None    # (N, 2) float32
+
+
+def _transforms(transforms) -> np.ndarray:
+    """(n, 3, 4) or (n, 4, 4) object-to-world matrices -> (n, 12) float32 row-major 3 x 4."""
+    t = np.asarray(transforms.cpu() if isinstance(transforms, torch.Tensor) else transforms)
+    if t.ndim != 3 or t.shape[1:] not in ((3, 4), (4, 4)):
+        raise ValueError("transforms must be (n, 3, 4) or (n, 4, 4)")
+    return np.ascontiguousarray(t[:, :3, :4].reshape(-1, 12), dtype=np.float32)
+
+
+class Scene:
+    """Instances of a batch's meshes placed by similarity transforms
+    (cp_scene_create); queries are in world space.  Keeps the batch alive."""
+
+    def __init__(self, batch: Batch, instance_mesh, transforms, *, stream=None):
+        self.batch = batch
+        self.instance_mesh = np.ascontiguousarray(instance_mesh, dtype=np.int32)
+        t = _transforms(transforms)
+        if len(t) != len(self.instance_mesh):
+            raise ValueError("one transform per instance")
+        self.n = len(t)
+        h = c_void_p()
+        check(lib.cp_scene_create(batch._h, c_void_p(self.instance_mesh.ctypes.data), c_void_p(t.ctypes.data),
+                                  self.n, _stream(stream), byref(h)), "cp_scene_create")
+        self._h = h
+
+    def update(self, transforms, *, stream=None) -> None:
+        t = _transforms(transforms)
+        if len(t) != self.n:
+            raise ValueError("one transform per instance")
+        check(lib.cp_scene_update(self._h, c_void_p(t.ctypes.data), _stream(stream)), "cp_scene_update")
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            lib.cp_scene_destroy(self._h)
+            self._h = c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def workspace_size(self, nq: int, opts: QueryOpts | None = None) -> int:
+        b = c_size_t(0)
+        o = opts or query_opts()
+        check(lib.cp_scene_query_workspace_size(self._h, nq, byref(o), byref(b)), "workspace")
+        return b.value
+
+    def query(self, points: torch.Tensor, *, want_point: bool = True, want_bary: bool = False,
+              opts: QueryOpts | None = None, workspace: torch.Tensor | None = None,
+              stream=None) -> SceneResult:
+        _check_dev(points, "points", torch.float32, 3)
+        n = int(points.shape[0])
+        dev = points.device
+        out = SceneResult(
+            point=torch.empty((n, 3), dtype=torch.float32, device=dev) if want_point else None,
+            dist=torch.empty((n,), dtype=torch.float32, device=dev),
+            instance=torch.empty((n,), dtype=torch.int32, device=dev),
+            tri=torch.empty((n,), dtype=torch.int32, device=dev),
+            bary=torch.empty((n, 2), dtype=torch.float32, device=dev) if want_bary else None)
+        o = opts or query_opts()
+        ws_ptr, ws_bytes = c_void_p(None), 0
+        if workspace is not None:
+            ws_ptr, ws_bytes = c_void_p(workspace.data_ptr()), workspace.numel() * workspace.element_size()
+        check(lib.cp_scene_query(self._h, _ptr(points), n, byref(o), _ptr(out.point), _ptr(out.dist),
+                                 _ptr(out.instance), _ptr(out.tri), _ptr(out.bary), ws_ptr, ws_bytes,
+                                 _stream(stream)), "cp_scene_query")
+        return out
+
+
 def autotune(verts: torch.Tensor, tris: torch.Tensor, sample: torch.Tensor,
              cache_path: str | None = None, branching: int = 0):
     """Run cp_autotune; returns (BuildOpts, QueryOpts).  branching=2/4/8 fixes the width."""

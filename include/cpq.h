@@ -116,6 +116,7 @@ typedef struct cp_mesh_info_t {
 
 typedef struct cp_mesh cp_mesh;
 typedef struct cp_batch cp_batch;
+typedef struct cp_scene cp_scene;
 
 /* ---- options ---------------------------------------------------------------- */
 
@@ -397,6 +398,56 @@ CP_API cp_status cp_batch_query(cp_batch* batch, const float* queries, const int
                                 const cp_query_opts* opts, float* out_point, float* out_dist,
                                 int32_t* out_tri, float* out_bary, void* workspace,
                                 size_t workspace_bytes, int32_t use_graph, cp_stream_t stream);
+
+/* ---- instanced scenes ------------------------------------------------------ */
+
+/*
+ * A scene of instances of a batch's meshes, each placed by its own 3 x 4
+ * object-to-world matrix: the reference's TLAS over transformed BLAS instances
+ * (Accel::recreate(blas, T), src/vk/vulkan.cpp:777-856; one model matrix per
+ * object, src/rt/rt.cpp:31-45).  A top-level BVH over the instances' world
+ * boxes is built on the device; a query walks it closest first and each
+ * instance's mesh BVH in object space, and the winner is re-evaluated in
+ * float-float in world space.
+ *   batch               the meshes; it must outlive the scene
+ *   instance_mesh       HOST array, n_instances mesh ids in [0, nmeshes)
+ *   instance_transform  HOST array, n_instances x 12 floats, row-major 3 x 4
+ *                       [R | t] taking object to world coordinates
+ * Transforms must be similarities (rotation or reflection, uniform scale,
+ * translation): M^T M = s^2 I within 1e-5 s^2 per entry, else
+ * CP_ERROR_INVALID_VALUE.  Distances and points are in world units; the
+ * accuracy bound of cp_query holds for transforms that are similarities to
+ * FP32 rounding; a deviation d from one adds up to about d/2 of the distance.
+ * Synchronises `stream`.
+ */
+CP_API cp_status cp_scene_create(const cp_batch* batch, const int32_t* instance_mesh,
+                                 const float* instance_transform, int32_t n_instances,
+                                 cp_stream_t stream, cp_scene** out);
+
+/*
+ * New transforms for every instance (same meshes), or the same ones after the
+ * batch's vertices changed: re-derives the instance frames and rebuilds the
+ * top level.  Synchronises `stream`.
+ */
+CP_API cp_status cp_scene_update(cp_scene* scene, const float* instance_transform, cp_stream_t stream);
+
+CP_API cp_status cp_scene_destroy(cp_scene* scene);
+
+CP_API cp_status cp_scene_query_workspace_size(const cp_scene* scene, int64_t nq,
+                                               const cp_query_opts* opts, size_t* bytes);
+
+/*
+ * Closest point on the scene for each world-space query.  out_instance is the
+ * instance, out_tri the triangle local to that instance's mesh, out_bary the
+ * weights of its b and c vertices; any output may be NULL.  Options as in
+ * cp_query (sort_queries orders the queries along a Morton curve of the
+ * scene's world box; the traversal options are ignored).  Workspace as in
+ * cp_query (NULL = stream-ordered pool).
+ */
+CP_API cp_status cp_scene_query(const cp_scene* scene, const float* queries, int64_t nq,
+                                const cp_query_opts* opts, float* out_point, float* out_dist,
+                                int32_t* out_instance, int32_t* out_tri, float* out_bary,
+                                void* workspace, size_t workspace_bytes, cp_stream_t stream);
 
 /* ---- autotuner ------------------------------------------------------------ */
 

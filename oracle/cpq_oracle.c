@@ -1293,3 +1293,45 @@ double orc_ray_brute_f64(const float* verts, const int32_t* tris, int64_t nt, co
     parallel_for(n, 16, nthreads, ray64_range, &c);
     return now_s() - t0;
 }
+
+/* ===================================================================== */
+/* FP64 brute force over FP64 vertices                                    */
+/* ===================================================================== */
+
+typedef struct {
+    const double* verts;
+    const int32_t* tris;
+    int64_t nt;
+    const float* q;
+    double *d2, *p;
+    int32_t* tri;
+} brute_dv_ctx;
+
+static void brute_dv_range(void* vctx, int64_t b, int64_t e) {
+    brute_dv_ctx* c = (brute_dv_ctx*)vctx;
+    for (int64_t i = b; i < e; ++i) {
+        double q[3] = {c->q[3 * i], c->q[3 * i + 1], c->q[3 * i + 2]};
+        double best = INFINITY, bp[3] = {0, 0, 0};
+        int32_t bt = -1;
+        for (int64_t t = 0; t < c->nt; ++t) {
+            const int32_t* ix = c->tris + 3 * t;
+            double cp[3], w[3];
+            double d2 = orc_point_tri_f64(q, c->verts + 3 * (int64_t)ix[0], c->verts + 3 * (int64_t)ix[1],
+                                          c->verts + 3 * (int64_t)ix[2], cp, w);
+            if (d2 < best) {
+                best = d2;
+                bt = (int32_t)t;
+                memcpy(bp, cp, sizeof bp);
+            }
+        }
+        c->d2[i] = best;
+        c->tri[i] = bt;
+        if (c->p) memcpy(c->p + 3 * i, bp, sizeof bp);
+    }
+}
+
+void orc_brute_f64_dv(const double* verts, const int32_t* tris, int64_t nt, const float* q, int64_t nq,
+                      double* out_d2, int32_t* out_tri, double* out_p, int nthreads) {
+    brute_dv_ctx c = {verts, tris, nt, q, out_d2, out_p, out_tri};
+    parallel_for(nq, 16, nthreads, brute_dv_range, &c);
+}

@@ -117,6 +117,11 @@ void orc_backward_f64(const float* verts, int64_t nv, const int32_t* tris, const
                       const int32_t* tri, const double* bary, const double* grad_d, int64_t nq,
                       double* grad_q, double* grad_verts);
 
+/* FP64 brute force over triangles given by FP64 vertices (geometry placed by
+ * an FP64 transform, e.g. instances): out_d2, out_tri, out_p (3 per query). */
+void orc_brute_f64_dv(const double* verts, const int32_t* tris, int64_t nt, const float* q, int64_t nq,
+                      double* out_d2, int32_t* out_tri, double* out_p, int nthreads);
+
 /* Rays, brute force over every triangle.  The hit test is the reference's
  * triangle_hit (Möller–Trumbore, src/shaders/rt/rtcommon.glsl:181-202): in
  * FP32 (orc_ray_brute_f32) operation for operation as the GPU evaluates it,

@@ -81,6 +81,9 @@ def lib():
         L.orc_backward_f64.restype = None
         L.orc_backward_f64.argtypes = [c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_void_p,
                                        c_void_p, c_int64, c_void_p, c_void_p]
+        L.orc_brute_f64_dv.restype = None
+        L.orc_brute_f64_dv.argtypes = [c_void_p, c_void_p, c_int64, c_void_p, c_int64, c_void_p, c_void_p,
+                                       c_void_p, c_int]
         L.orc_ray_brute_f32.restype = c_double
         L.orc_ray_brute_f32.argtypes = [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_int64,
                                         c_float, c_float, c_float, c_void_p, c_void_p, c_void_p, c_int]
@@ -264,3 +267,15 @@ def ray_brute(verts, tris, orig, dirs, tmin=0.0, tmax=float("inf"), det_eps=0.0,
     secs = fn(_p(v), _p(t), t.shape[0], _p(o), _p(d), _p(tm), n, tmin, tmax, det_eps, _p(out_t),
               _p(out_tri), _p(out_uv), threads or nthreads())
     return {"t": out_t, "tri": out_tri, "uv": out_uv, "seconds": secs}
+
+
+def brute_f64_dv(verts64, tris, q, threads: int | None = None):
+    """FP64 brute force over FP64 vertices (e.g. instances placed by an FP64 transform)."""
+    v = np.ascontiguousarray(verts64, dtype=np.float64)
+    t, qq = _i32(tris), _f32(q)
+    n = qq.shape[0]
+    d2 = np.empty(n)
+    tri = np.empty(n, np.int32)
+    p = np.empty((n, 3))
+    lib().orc_brute_f64_dv(_p(v), _p(t), t.shape[0], _p(qq), n, _p(d2), _p(tri), _p(p), threads or nthreads())
+    return {"dist": np.sqrt(d2), "tri": tri, "point": p}

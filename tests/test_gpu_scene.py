@@ -1,0 +1,215 @@
+"""GPU instanced scenes (cp_scene_*): instances of a batch's meshes placed by
+similarity transforms, the reference's TLAS over transformed BLAS instances
+(src/vk/vulkan.cpp:777-856, src/rt/rt.cpp:31-45).
+
+The truth is the FP64 brute force over the world-space vertices, each the
+FP32 matrix applied to the FP32 object vertex in FP64.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def dev(a, cuda):
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(a)).to(cuda)
+
+
+def random_similarities(n, seed, reflect=True):
+    """(n, 3, 4) float32: random rotation (some reflected), scale 0.5..2, translation in [-4, 4]^3."""
+    rng = np.random.default_rng(seed)
+    q = rng.normal(size=(n, 4))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    w, x, y, z = q.T
+    R = np.stack([np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)], -1),
+                  np.stack([2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)], -1),
+                  np.stack([2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)], -1)], 1)
+    if reflect:
+        R[::3, :, 0] *= -1.0
+    s = rng.uniform(0.5, 2.0, n)
+    T = np.zeros((n, 3, 4))
+    T[:, :, :3] = R * s[:, None, None]
+    T[:, :, 3] = rng.uniform(-4, 4, (n, 3))
+    return T.astype(np.float32)
+
+
+def world_soup(meshes, inst_mesh, T):
+    """All instances' triangles in world space, FP64 (the oracle's input)."""
+    vs, ts, off = [], [], 0
+    for m, t in zip(inst_mesh, T):
+        v, tri = meshes[m]
+        M = t.astype(np.float64)
+        vs.append(v.astype(np.float64) @ M[:, :3].T + M[:, 3])
+        ts.append(tri + off)
+        off += v.shape[0]
+    ntri = np.array([meshes[m][1].shape[0] for m in inst_mesh])
+    return np.concatenate(vs), np.concatenate(ts).astype(np.int32), np.concatenate([[0], np.cumsum(ntri)])
+
+
+def make_batch(cpq, cuda, meshes, K=4):
+    from gpurt_cpq import workloads as W
+
+    V, voff, T, toff, _, _ = W.concat_batch([(v, t, None) for v, t in meshes],
+                                            [np.zeros((0, 3), np.float32)] * len(meshes))
+    return cpq.Batch(dev(V, cuda), voff, dev(T, cuda), toff, branching=K)
+
+
+def check_scene(orc, meshes, inst_mesh, T, q, r, rel=1e-6):
+    wv, wt, toff = world_soup(meshes, inst_mesh, T)
+    ref = orc.brute_f64_dv(wv, wt, q)
+    d = r.dist.cpu().numpy().astype(np.float64)
+    inst = r.instance.cpu().numpy()
+    tri = r.tri.cpu().numpy()
+    assert np.all(inst >= 0) and np.all(tri >= 0)
+    scale = np.abs(wv).max()
+    # the answer is the distance to the reported triangle, never below the truth
+    # by more than the float-float finish, and above it by at most the FP32
+    # selection among near-equal triangles (~1e-7 of the coordinates)
+    err = d - ref["dist"]
+    assert np.all(err >= -1e-6 * ref["dist"] - 1e-12 * scale), err.min()
+    far = ref["dist"] >= 1e-2 * scale
+    assert np.all(err[far] <= rel * ref["dist"][far]), (err[far] / ref["dist"][far]).max()
+    assert np.all(err <= rel * ref["dist"] + 4e-7 * scale), (err - rel * ref["dist"]).max()
+    # the reported (instance, triangle) gives that distance and the point lies on it
+    g = toff[inst] + tri
+    pts = r.point.cpu().numpy().astype(np.float64)
+    np.testing.assert_allclose(np.linalg.norm(pts - q, axis=1), d, rtol=2e-6, atol=1e-6 * scale)
+    mm = np.nonzero(g != ref["tri"])[0]
+    for i in mm[:200]:
+        a, b, c = wv[wt[g[i]]]
+        d2, _, _ = orc.point_tri_f64(q[i].astype(np.float64), a, b, c)
+        assert abs(np.sqrt(d2) - d[i]) <= 1e-6 * d[i] + 1e-6 * scale
+    for i in range(0, len(q), max(1, len(q) // 300)):
+        a, b, c = wv[wt[g[i]]]
+        d2, _, _ = orc.point_tri_f64(pts[i], a, b, c)
+        assert np.sqrt(d2) <= 1e-6 * scale
+    return ref
+
+
+@pytest.mark.parametrize("K", [2, 4, 8])
+def test_scene_vs_fp64(orc, cpq, cuda, K):
+    from gpurt_cpq import workloads as W
+
+    meshes = [W.icosphere(3), W.torus(60, 24), W.heightfield(48, seed=3)[:2]]
+    rng = np.random.default_rng(11)
+    n = 37
+    inst_mesh = rng.integers(0, len(meshes), n).astype(np.int32)
+    T = random_similarities(n, seed=12)
+    b = make_batch(cpq, cuda, meshes, K)
+    sc = cpq.Scene(b, inst_mesh, T)
+    wv, wt, _ = world_soup(meshes, inst_mesh, T)
+    lo, hi = wv.min(0), wv.max(0)
+    pad = 0.2 * (hi - lo)
+    far = rng.uniform(lo - pad, hi + pad, (20000, 3))
+    near = W.surface_points(wv.astype(np.float32), wt, 10000, rng).astype(np.float64)
+    near += rng.normal(size=near.shape) * np.linalg.norm(hi - lo) * 10.0 ** rng.uniform(-6, -2, (len(near), 1))
+    q = np.concatenate([far, near]).astype(np.float32)
+    r = sc.query(dev(q, cuda), want_bary=True)
+    check_scene(orc, meshes, inst_mesh, T, q, r)
+    bary = r.bary.cpu().numpy()
+    assert np.all(bary >= -1e-6) and np.all(bary.sum(1) <= 1 + 1e-6)
+
+
+def test_scene_identity_matches_mesh(orc, cpq, cuda):
+    """One instance at the identity gives the plain query's answers."""
+    from gpurt_cpq import workloads as W
+
+    v, t = W.torus(80, 30)
+    b = make_batch(cpq, cuda, [(v, t)], 4)
+    T = np.zeros((1, 3, 4), np.float32)
+    T[0, :, :3] = np.eye(3)
+    sc = cpq.Scene(b, [0], T)
+    q = W.uniform_queries(30000, [-1.6, -1.6, -0.6], [1.6, 1.6, 0.6], seed=5)
+    r = sc.query(dev(q, cuda))
+    m = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=4)
+    rm = m.query(dev(q, cuda))
+    np.testing.assert_allclose(r.dist.cpu().numpy(), rm.dist.cpu().numpy(), rtol=1e-6, atol=0)
+    assert np.all(r.instance.cpu().numpy() == 0)
+    same = (r.tri.cpu().numpy() == rm.tri.cpu().numpy()).mean()
+    assert same > 0.99
+    check_scene(orc, [(v, t)], [0], T, q, r)
+
+
+def test_scene_many_instances_and_update(orc, cpq, cuda):
+    """A few thousand small instances (deep top level), then new transforms."""
+    from gpurt_cpq import workloads as W
+
+    meshes = [W.icosphere(1, 0.1), W.torus(12, 6, 0.1, 0.03)]
+    rng = np.random.default_rng(21)
+    n = 3000
+    inst_mesh = rng.integers(0, 2, n).astype(np.int32)
+    T = random_similarities(n, seed=22)
+    T[:, :, 3] *= 5.0
+    b = make_batch(cpq, cuda, meshes, 4)
+    sc = cpq.Scene(b, inst_mesh, T)
+    q = rng.uniform(-22, 22, (20000, 3)).astype(np.float32)
+    check_scene(orc, meshes, inst_mesh, T, q, sc.query(dev(q, cuda)))
+    T2 = random_similarities(n, seed=23)
+    T2[:, :, 3] *= 5.0
+    sc.update(T2)
+    r = sc.query(dev(q, cuda))
+    check_scene(orc, meshes, inst_mesh, T2, q, r)
+    fresh = cpq.Scene(b, inst_mesh, T2).query(dev(q, cuda))
+    assert np.array_equal(r.dist.cpu().numpy(), fresh.dist.cpu().numpy())
+
+
+def test_scene_workspace_and_unsorted(cpq, cuda):
+    import torch
+
+    from gpurt_cpq import workloads as W
+
+    meshes = [W.icosphere(2)]
+    T = random_similarities(8, seed=2)
+    sc = cpq.Scene(make_batch(cpq, cuda, meshes, 2), np.zeros(8, np.int32), T)
+    q = dev(np.random.default_rng(1).uniform(-6, 6, (5000, 3)).astype(np.float32), cuda)
+    r0 = sc.query(q)
+    ws = torch.empty(sc.workspace_size(5000), dtype=torch.uint8, device=cuda)
+    r1 = sc.query(q, workspace=ws)
+    o = cpq.query_opts(sort_queries=False)
+    r2 = sc.query(q, opts=o)
+    assert torch.equal(r0.dist, r1.dist)
+    torch.testing.assert_close(r0.dist, r2.dist, rtol=1e-6, atol=0)
+
+
+def test_scene_rejects_bad_input(cpq, cuda):
+    from gpurt_cpq import workloads as W
+    from gpurt_cpq._lib import CP_ERROR_INVALID_VALUE, CpError
+
+    b = make_batch(cpq, cuda, [W.icosphere(1)], 4)
+    T = random_similarities(2, seed=1)
+    shear = T.copy()
+    shear[0, 0, 1] += 0.1
+    with pytest.raises(CpError, match="not a similarity") as e:
+        cpq.Scene(b, [0, 0], shear)
+    assert e.value.status == CP_ERROR_INVALID_VALUE
+    with pytest.raises(CpError, match="mesh id out of range"):
+        cpq.Scene(b, [0, 1], T)
+    bad = T.copy()
+    bad[1, 2, 3] = np.nan
+    with pytest.raises(CpError, match="non-finite"):
+        cpq.Scene(b, [0, 0], bad)
+    zero = np.zeros((1, 3, 4), np.float32)
+    with pytest.raises(CpError, match="singular"):
+        cpq.Scene(b, [0], zero)
+    sc = cpq.Scene(b, [0, 0], T)
+    with pytest.raises(CpError, match="not a similarity"):
+        sc.update(shear)
+
+
+def test_gltf_instances_as_scene(orc, cpq, cuda, tmp_path):
+    """A glTF file's primitives as a batch and its node instances as a scene:
+    the same answers as the flattened world mesh."""
+    from test_gltf import _scene, _write
+
+    doc, data = _scene()
+    s = cpq.load_gltf(str(_write(tmp_path, doc, data, "glb")))
+    b = cpq.Batch(dev(s.verts, cuda), s.vert_offsets, dev(s.tris, cuda), s.tri_offsets, branching=4)
+    sc = cpq.Scene(b, s.instance_primitive, s.instance_world)
+    q = np.random.default_rng(3).uniform(-2, 12, (5000, 3)).astype(np.float32)
+    r = sc.query(dev(q, cuda))
+    meshes = [(s.verts[s.vert_offsets[i]:s.vert_offsets[i + 1]],
+               s.tris[s.tri_offsets[i]:s.tri_offsets[i + 1]]) for i in range(len(s.tri_offsets) - 1)]
+    check_scene(orc, meshes, s.instance_primitive, s.instance_world[:, :3, :].astype(np.float32), q, r)
