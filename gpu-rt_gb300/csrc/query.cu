@@ -1250,7 +1250,7 @@ struct InstArgs {
     const TriRec* brecs;
     const int32_t* broot;      // per mesh
     const int32_t* inst_mesh;  // per instance
-    const float* inst_inv;     // 12 per instance: object <- world, row-major 3 x 4
+    const float* inst_inv;     // 12 per instance: object <- world, row-major 3 x 4 (3 x 3 part used)
     const float* inst_fwd;     // 12 per instance: world <- object
     const float* inst_s2;      // 2 per instance: squared scale (ranking), its lower bound (pruning)
     const float* queries;
@@ -1270,6 +1270,17 @@ __device__ __forceinline__ void affine(const float* m, float x, float y, float z
     ox = fmaf(m[0], x, fmaf(m[1], y, fmaf(m[2], z, m[3])));
     oy = fmaf(m[4], x, fmaf(m[5], y, fmaf(m[6], z, m[7])));
     oz = fmaf(m[8], x, fmaf(m[9], y, fmaf(m[10], z, m[11])));
+}
+
+// World to object coordinates: the translation off first, then the inverse's
+// 3 x 3 part, so the rounding is relative to the point's distance from the
+// instance's origin and not to its world coordinates.
+__device__ __forceinline__ void to_object(const float* inv, const float* fwd, float x, float y, float z,
+                                          float& ox, float& oy, float& oz) {
+    const float dx = x - fwd[3], dy = y - fwd[7], dz = z - fwd[11];
+    ox = fmaf(inv[0], dx, fmaf(inv[1], dy, inv[2] * dz));
+    oy = fmaf(inv[4], dx, fmaf(inv[5], dy, inv[6] * dz));
+    oz = fmaf(inv[8], dx, fmaf(inv[9], dy, inv[10] * dz));
 }
 
 // Closest-first walk of one mesh's BVH from `root` for one point: nodes whose
@@ -1378,9 +1389,8 @@ __device__ void instance_point(const InstArgs& a, const WideNode<K>* __restrict_
         const int first = leaf_first(cur), cnt = leaf_count(cur);
         for (int k = 0; k < cnt; ++k) {
             const int inst = __float_as_int(__ldg(&a.trecs[first + k].p2.y));
-            const float* inv = a.inst_inv + 12 * inst;
             float ox, oy, oz;
-            affine(inv, qx, qy, qz, ox, oy, oz);
+            to_object(a.inst_inv + 12 * inst, a.inst_fwd + 12 * inst, qx, qy, qz, ox, oy, oz);
             const float s2 = a.inst_s2[2 * inst], s2lo = a.inst_s2[2 * inst + 1];
             // object-space bound: below it lies every triangle whose world
             // distance can beat `best` (s2lo bounds the transform's

@@ -244,3 +244,54 @@ def soup(seed: int = 5, clusters: int = 4096, per: int = 2048, sigma: float = 0.
     v += centres[:, None, :]
     tris = np.arange(clusters * per * 3, dtype=np.int32).reshape(-1, 3)
     return v.reshape(-1, 3), tris
+
+
+def random_rotations(n: int, rng) -> np.ndarray:
+    """(n, 3, 3) rotations from uniform random unit quaternions, FP64."""
+    qr = rng.normal(size=(n, 4))
+    qr /= np.linalg.norm(qr, axis=1, keepdims=True)
+    w, x, y, z = qr.T
+    return np.stack([np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)], -1),
+                     np.stack([2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)], -1),
+                     np.stack([2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)], -1)], 1)
+
+
+def flatten_instances(meshes, inst_mesh, T):
+    """All instances' triangles in one world-space FP32 mesh."""
+    wv, wt, off = [], [], 0
+    for m, t in zip(inst_mesh, T):
+        v, tri = meshes[m]
+        t64 = t.astype(np.float64)
+        wv.append((v.astype(np.float64) @ t64[:, :3].T + t64[:, 3]).astype(np.float32))
+        wt.append(tri + off)
+        off += v.shape[0]
+    return np.concatenate(wv), np.concatenate(wt).astype(np.int32)
+
+
+def instanced_scene(seed: int = 31, nq: int = 16 * M, grid: int = 16):
+    """grid^3 similarity instances (random rotation, scale 0.6..1.2) of three
+    meshes at pitch 3; queries half uniform over the grid, half N(0, 0.02) off
+    the instances' surfaces.  Returns (meshes, inst_mesh, T (n, 3, 4) f32, q)."""
+    meshes = [icosphere(4), torus(100, 40), heightfield(64, seed=3)]
+    n_inst = grid ** 3
+    rng = np.random.default_rng(seed)
+    inst_mesh = rng.integers(0, len(meshes), n_inst).astype(np.int32)
+    R = random_rotations(n_inst, rng)
+    g = np.stack(np.meshgrid(*[np.arange(grid)] * 3, indexing="ij"), -1).reshape(-1, 3)
+    T = np.zeros((n_inst, 3, 4))
+    T[:, :, :3] = R * rng.uniform(0.6, 1.2, n_inst)[:, None, None]
+    T[:, :, 3] = 3.0 * g + rng.uniform(-0.3, 0.3, (n_inst, 3))
+    T = T.astype(np.float32)
+    half = nq // 2
+    lo, hi = np.full(3, -2.0), np.full(3, 3.0 * (grid - 1) + 2.0)
+    far = rng.uniform(lo, hi, (half, 3))
+    k = rng.integers(0, n_inst, nq - half)
+    near = np.empty((nq - half, 3))
+    for m, (v, tri) in enumerate(meshes):
+        sel = np.nonzero(inst_mesh[k] == m)[0]
+        p = surface_points(v, tri, len(sel), rng)
+        t = T[k[sel]].astype(np.float64)
+        near[sel] = np.einsum("nij,nj->ni", t[:, :, :3], p) + t[:, :, 3]
+    near += rng.normal(0.0, 0.02, near.shape)
+    q = np.concatenate([far, near]).astype(np.float32)
+    return meshes, inst_mesh, T, q[rng.permutation(nq)]

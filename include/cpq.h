@@ -425,9 +425,8 @@ CP_API cp_status cp_scene_create(const cp_batch* batch, const int32_t* instance_
                                  cp_stream_t stream, cp_scene** out);
 
 /*
- * New transforms for every instance (same meshes), or the same ones after the
- * batch's vertices changed: re-derives the instance frames and rebuilds the
- * top level.  Synchronises `stream`.
+ * New transforms for every instance (same meshes): re-derives the instance
+ * frames and rebuilds the top level.  Synchronises `stream`.
  */
 CP_API cp_status cp_scene_update(cp_scene* scene, const float* instance_transform, cp_stream_t stream);
 
