@@ -331,7 +331,7 @@ def our_arm(args):
     trav_ms = tms.value / max(tl.value, 1)
     # packet kernel: per-warp node visits / triangle tests, from one more
     # (untimed) query through the counting build of the kernel
-    counts = (c_uint64 * 4)()
+    counts = (c_uint64 * 6)()
     lib.cp_timing_enable(CP_TIMING_COUNTERS)
     lib.cp_traversal_stats(counts, 1)
     mesh.query(qd, workspace=ws, opts=qopts, out=out)
@@ -342,7 +342,10 @@ def our_arm(args):
                      "warp_node_visits_per_32_queries": counts[0] * 32 / per_q,
                      "warp_tri_tests_per_32_queries": counts[1] * 32 / per_q,
                      "warp_pops_per_32_queries": counts[2] * 32 / per_q,
-                     "warp_skipped_pops_per_32_queries": counts[3] * 32 / per_q} if counts[0] else None
+                     "warp_skipped_pops_per_32_queries": counts[3] * 32 / per_q,
+                     "lane_tri_tests_per_query": counts[4] / per_q,
+                     "warp_tri_rounds_per_32_queries": counts[5] * 32 / per_q,
+                     "tri_round_lane_use": counts[4] / max(counts[5] * 32, 1)} if counts[0] else None
     ms = max_over_ranks(ms, world, dev)
     value = whole_job_rate(nq * args.steps, world, ms * 1e-3)
     assert mesh.device_status() == 0
@@ -387,8 +390,8 @@ def our_arm(args):
                 "hbm_gbs": hbm, "l2_gbs_measured": l2_gbs,
                 "hbm_only_frac": B_IO / t_kernel / 1e9 / hbm,
                 "packet_counters": packet_visits}
-    # read by the traversal: K-wide nodes (32K B), 48-B exact and 64-B test records
-    traversal_mb = (info.num_wide_nodes * 32 * 4 + info.num_triangles * (48 + 64)) / 1e6
+    # read by the traversal: K-wide nodes (32K B), 48-B exact and 80-B test records
+    traversal_mb = (info.num_wide_nodes * 32 * 4 + info.num_triangles * (48 + 80)) / 1e6
     if rank == 0:
         res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,

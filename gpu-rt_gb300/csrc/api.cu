@@ -300,11 +300,11 @@ CP_API cp_status cp_timing_read(double* traverse_ms, int64_t* launches, int32_t 
     return CP_SUCCESS;
 }
 
-CP_API cp_status cp_traversal_stats(uint64_t* counts4, int32_t reset) {
-    if (!counts4) return fail(CP_ERROR_INVALID_VALUE, "counts4 is NULL");
-    unsigned long long c[4];
+CP_API cp_status cp_traversal_stats(uint64_t* counts6, int32_t reset) {
+    if (!counts6) return fail(CP_ERROR_INVALID_VALUE, "counts6 is NULL");
+    unsigned long long c[kStatCount];
     CP_CUDA(traversal_stats(c, reset != 0), "traversal stats");
-    for (int k = 0; k < 4; ++k) counts4[k] = c[k];
+    for (int k = 0; k < kStatCount; ++k) counts6[k] = c[k];
     return CP_SUCCESS;
 }
 
@@ -439,7 +439,12 @@ CP_API cp_status cp_query_host(const cp_mesh* m, const float* queries, int64_t n
     if (s != CP_SUCCESS) return s;
     const Bvh& b = m->bvh;
     cudaStream_t user = reinterpret_cast<cudaStream_t>(stream);
-    const int64_t chunk = nq < (int64_t(1) << 22) ? nq : (int64_t(1) << 22);
+    // One ordering over as many queries as possible: a 32-query packet's
+    // extent shrinks with the density of the ordered set, so splitting a batch
+    // into chunks costs more traversal time (16M queries in 4M chunks: +4 ms)
+    // than overlapping their copies with it saves (H2D + D2H: 2.7 ms).  Only
+    // batches beyond 64M queries (about 4 GB of scratch) are pipelined.
+    const int64_t chunk = nq < (int64_t(1) << 26) ? nq : (int64_t(1) << 26);
     const int64_t nchunks = (nq + chunk - 1) / chunk;
     const int nslots = nchunks > 1 ? 2 : 1;
     cudaStream_t st[2] = {nullptr, nullptr};

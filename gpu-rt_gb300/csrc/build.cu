@@ -280,26 +280,48 @@ __device__ __forceinline__ uint32_t degenerate_flag(float3 a, float3 b, float3 c
 
 __device__ __forceinline__ FastTri make_fast_tri(float3 a, float3 b, float3 c, int32_t local,
                                                  bool degenerate) {
-    const float abx = b.x - a.x, aby = b.y - a.y, abz = b.z - a.z;
-    const float acx = c.x - a.x, acy = c.y - a.y, acz = c.z - a.z;
-    const float bcx = c.x - b.x, bcy = c.y - b.y, bcz = c.z - b.z;
-    const float aa = abx * abx + aby * aby + abz * abz;
-    const float cc = acx * acx + acy * acy + acz * acz;
-    const float bb = abx * acx + aby * acy + abz * acz;
-    const float ee = bcx * bcx + bcy * bcy + bcz * bcz;
-    float g0 = __int_as_float(0x7fc00000), g1 = g0, g2 = g0;  // NaN: never inside
-    if (!degenerate) {
-        const float inv_det = 1.0f / (aa * cc - bb * bb);
-        g0 = cc * inv_det;
-        g1 = bb * inv_det;
-        g2 = aa * inv_det;
+    const float3 ab = make_float3(b.x - a.x, b.y - a.y, b.z - a.z);
+    const float3 ac = make_float3(c.x - a.x, c.y - a.y, c.z - a.z);
+    const float aa = ab.x * ab.x + ab.y * ab.y + ab.z * ab.z;
+    const float cc = ac.x * ac.x + ac.y * ac.y + ac.z * ac.z;
+    // e1: along ab, else along ac, else any axis (a point)
+    float3 e1 = make_float3(1.0f, 0.0f, 0.0f);
+    if (aa > 0.0f) {
+        const float r = 1.0f / sqrtf(aa);
+        e1 = make_float3(ab.x * r, ab.y * r, ab.z * r);
+    } else if (cc > 0.0f) {
+        const float r = 1.0f / sqrtf(cc);
+        e1 = make_float3(ac.x * r, ac.y * r, ac.z * r);
     }
+    // e2: ac's part across e1; for a zero-area triangle any unit vector
+    // across e1 (from the axis e1 leans on least)
+    const float ce = ac.x * e1.x + ac.y * e1.y + ac.z * e1.z;
+    float3 w = make_float3(ac.x - ce * e1.x, ac.y - ce * e1.y, ac.z - ce * e1.z);
+    float ww = w.x * w.x + w.y * w.y + w.z * w.z;
+    if (degenerate || !(ww > 0.0f)) {
+        const float ax = fabsf(e1.x), ay = fabsf(e1.y), az = fabsf(e1.z);
+        const float3 t = ax <= ay && ax <= az ? make_float3(1.0f, 0.0f, 0.0f)
+                         : ay <= az           ? make_float3(0.0f, 1.0f, 0.0f)
+                                              : make_float3(0.0f, 0.0f, 1.0f);
+        const float te = t.x * e1.x + t.y * e1.y + t.z * e1.z;
+        w = make_float3(t.x - te * e1.x, t.y - te * e1.y, t.z - te * e1.z);
+        ww = w.x * w.x + w.y * w.y + w.z * w.z;
+    }
+    const float rw = 1.0f / sqrtf(ww);
+    const float3 e2 = make_float3(w.x * rw, w.y * rw, w.z * rw);
+    const float3 n = make_float3(e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x);
+    const float L1 = ab.x * e1.x + ab.y * e1.y + ab.z * e1.z;
+    const float x2 = ce;
+    const float y2 = fmaxf(ac.x * e2.x + ac.y * e2.y + ac.z * e2.z, 0.0f);
+    const float bx = x2 - L1;
+    const float l2 = x2 * x2 + y2 * y2, l3 = bx * bx + y2 * y2;
     FastTri f;
-    f.p0 = make_float4(a.x, a.y, a.z, abx);
-    f.p1 = make_float4(aby, abz, acx, acy);
-    f.p2 = make_float4(acz, g0, g1, g2);
-    f.p3 = make_float4(aa > 0.0f ? 1.0f / aa : 0.0f, cc > 0.0f ? 1.0f / cc : 0.0f,
-                       ee > 0.0f ? 1.0f / ee : 0.0f, __int_as_float(local));
+    f.p0 = make_float4(a.x, a.y, a.z, L1);
+    f.p1 = make_float4(e1.x, e1.y, e1.z, x2);
+    f.p2 = make_float4(e2.x, e2.y, e2.z, y2);
+    f.p3 = make_float4(n.x, n.y, n.z, bx);
+    f.p4 = make_float4(l2 > 0.0f ? 1.0f / l2 : 0.0f, l3 > 0.0f ? 1.0f / l3 : 0.0f,
+                       degenerate ? INFINITY : 0.0f, __int_as_float(local));
     return f;
 }
 

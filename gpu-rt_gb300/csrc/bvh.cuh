@@ -106,7 +106,11 @@ cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int6
 // CUDA-event timing of traversal launches (diagnostic; see cp_timing_enable).
 void timing_enable(bool events, bool counters);
 cudaError_t timing_read(double* ms, int64_t* launches, bool reset);
-cudaError_t traversal_stats(unsigned long long* out4, bool reset);
+// Counters of the counting packet kernel: warp node visits, leaf triangles
+// (per warp leaf visit), stack pops, skipped pops, lane-triangle tests
+// (active lanes x leaf triangles) and triangle rounds executed.
+constexpr int kStatCount = 6;
+cudaError_t traversal_stats(unsigned long long* out, bool reset);
 
 // Proxy triangles for the top level of an instanced scene: per instance the
 // world box of its mesh in `bottom` as (lo, hi, hi); verts 2n x 3, tris n x 3.

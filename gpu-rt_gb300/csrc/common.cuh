@@ -51,15 +51,31 @@ struct alignas(16) TriRec {
     float4 p0, p1, p2;
 };
 
-// 64-byte record for the traversal's distance test, in the same (leaf) order
-// as TriRec: {a.xyz ab.x} {ab.yz ac.xy} {ac.z G0 G1 G2} {1/|ab|^2 1/|ac|^2
-// 1/|bc|^2 idx}.  (G0, G1, G2) is the inverse Gram matrix of (ab, ac) up to
-// the shared determinant, so the plane projection's barycentrics are
-// v = G0 (ab.ap) - G1 (ac.ap), w = G2 (ac.ap) - G1 (ab.ap); zero-area
-// triangles store NaN there (never "inside").  Zero-length edges store 0.
+// 80-byte record for the traversal's distance test, in the same (leaf) order
+// as TriRec.  The triangle in its own orthonormal frame (e1 along ab, e2 in
+// the plane towards c, n = e1 x e2): a at the origin, b at (L1, 0), c at
+// (x2, y2) with y2 >= 0, so a query's offset from a gives in-plane (u, v) and
+// height h by three dot products, and the rest is a 2D point-triangle test:
+//   {a.xyz L1} {e1.xyz x2} {e2.xyz y2} {n.xyz x2 - L1}
+//   {1/|ac|^2 1/|bc|^2 vmin idx}
+// vmin is 0, or +inf for a zero-area triangle (never "inside"); zero-length
+// edges store 0 for their inverse.
 struct alignas(16) FastTri {
-    float4 p0, p1, p2, p3;
+    float4 p0, p1, p2, p3, p4;
 };
+static_assert(sizeof(FastTri) == 80, "FastTri is five 16-byte loads");
+
+__device__ __forceinline__ FastTri load_fast(const FastTri* p) {
+    const float4* fp = reinterpret_cast<const float4*>(p);
+    FastTri f;
+    f.p0 = __ldg(fp);
+    f.p1 = __ldg(fp + 1);
+    f.p2 = __ldg(fp + 2);
+    f.p3 = __ldg(fp + 3);
+    f.p4 = __ldg(fp + 4);
+    return f;
+}
+__device__ __forceinline__ int fast_index(const FastTri& f) { return __float_as_int(f.p4.w); }
 
 __host__ __device__ inline int32_t pack_leaf(int32_t first, int32_t count) {
     return ~((first << kLeafShift) | (count - 1));

@@ -171,50 +171,36 @@ __device__ __forceinline__ void load_row2(const float* __restrict__ p, f32x2 (&r
     }
 }
 
-// Branch-free squared distance for the traversal, on a FastTri record.  If
-// the plane projection's barycentrics lie inside the triangle the answer is
-// the plane residual; otherwise the closest point is on the boundary, so it
-// is the nearest of the three edge segments (each clamped with a saturating
-// multiply).  Nearly all work is FMA-pipe arithmetic, and lanes that test the
-// same triangle from different Voronoi regions do not diverge.
+// Branch-free squared distance for the traversal, on a FastTri record: the
+// query's offset from a in the triangle's frame, (u, v) in the plane and h
+// off it, then h^2 plus the squared 2D distance to the triangle (a, b, c) =
+// ((0, 0), (L1, 0), (x2, y2)) — zero inside, else the nearest of the three
+// edge segments, each clamped with a saturating multiply.  Nearly all work is
+// FMA-pipe arithmetic, and lanes that test the same triangle from different
+// Voronoi regions do not diverge.  The frame is FP32, so the value is the
+// distance to the triangle to a few ulps of |q - a|; the winner is
+// re-evaluated exactly.
 __device__ __forceinline__ float tri_d2_fast(float qx, float qy, float qz, const FastTri& f) {
     const float apx = qx - f.p0.x, apy = qy - f.p0.y, apz = qz - f.p0.z;
-    const float abx = f.p0.w, aby = f.p1.x, abz = f.p1.y;
-    const float acx = f.p1.z, acy = f.p1.w, acz = f.p2.x;
-    const float dab = abx * apx + aby * apy + abz * apz;
-    const float dac = acx * apx + acy * apy + acz * apz;
-    // edge ab
-    const float tab = __saturatef(dab * f.p3.x);
-    float rx = apx - tab * abx, ry = apy - tab * aby, rz = apz - tab * abz;
-    float d2 = rx * rx + ry * ry + rz * rz;
-    // edge ac
-    const float tac = __saturatef(dac * f.p3.y);
-    rx = apx - tac * acx;
-    ry = apy - tac * acy;
-    rz = apz - tac * acz;
-    d2 = fminf(d2, rx * rx + ry * ry + rz * rz);
-    // edge bc, from b
-    const float bpx = apx - abx, bpy = apy - aby, bpz = apz - abz;
-    const float bcx = acx - abx, bcy = acy - aby, bcz = acz - abz;
-    const float tbc = __saturatef((bcx * bpx + bcy * bpy + bcz * bpz) * f.p3.z);
-    rx = bpx - tbc * bcx;
-    ry = bpy - tbc * bcy;
-    rz = bpz - tbc * bcz;
-    d2 = fminf(d2, rx * rx + ry * ry + rz * rz);
-    // face: barycentrics of the plane projection
-    const float v = f.p2.y * dab - f.p2.z * dac;
-    const float w = f.p2.w * dac - f.p2.z * dab;
-    rx = apx - (v * abx + w * acx);
-    ry = apy - (v * aby + w * acy);
-    rz = apz - (v * abz + w * acz);
-    const float d2f = rx * rx + ry * ry + rz * rz;
-    const bool inside = v >= 0.0f && w >= 0.0f && v + w <= 1.0f;  // false for NaN
-    // Every candidate is the distance to a point of the triangle, so each is
-    // an upper bound; the face one is taken only when it is the smallest.
-    // For a sliver the FP32 barycentrics carry errors of eps / sin^2 of its
-    // angle and may place an "inside" point far from the foot: the edges then
-    // bound the answer by half the sliver's width above the true distance.
-    return inside ? fminf(d2f, d2) : d2;
+    const float u = fmaf(f.p1.x, apx, fmaf(f.p1.y, apy, f.p1.z * apz));
+    const float v = fmaf(f.p2.x, apx, fmaf(f.p2.y, apy, f.p2.z * apz));
+    const float h = fmaf(f.p3.x, apx, fmaf(f.p3.y, apy, f.p3.z * apz));
+    const float L1 = f.p0.w, x2 = f.p1.w, y2 = f.p2.w, bx = f.p3.w;
+    // edge ab: the u axis from 0 to L1
+    const float du = u - fminf(fmaxf(u, 0.0f), L1);
+    const float d_ab = fmaf(du, du, v * v);
+    // edge ac: from the origin to (x2, y2)
+    const float s2 = __saturatef(fmaf(u, x2, v * y2) * f.p4.x);
+    const float cx = fmaf(-s2, x2, u), cy = fmaf(-s2, y2, v);
+    const float d_ac = fmaf(cx, cx, cy * cy);
+    // edge bc: from (L1, 0) to (x2, y2)
+    const float bu = u - L1;
+    const float s3 = __saturatef(fmaf(bu, bx, v * y2) * f.p4.y);
+    const float ex = fmaf(-s3, bx, bu), ey = fmaf(-s3, y2, v);
+    const float d_bc = fmaf(ex, ex, ey * ey);
+    // inside: left of ab, ca and bc (counter-clockwise, y2 >= 0)
+    const bool inside = v >= f.p4.z && fmaf(u, y2, -v * x2) >= 0.0f && fmaf(bu, y2, -v * bx) <= 0.0f;
+    return fmaf(h, h, inside ? 0.0f : fminf(d_ab, fminf(d_ac, d_bc)));
 }
 
 // Degenerate triangle in FP32 with barycentrics (weights of b and c).
@@ -458,14 +444,9 @@ __global__ void __launch_bounds__(256) k_traverse(TraverseArgs a) {
             } else {
                 const int first = leaf_first(cur), cnt = leaf_count(cur);
                 for (int k = 0; k < cnt; ++k) {
-                    const float4* fp = reinterpret_cast<const float4*>(a.fast + first + k);
-                    FastTri f;
-                    f.p0 = __ldg(fp);
-                    f.p1 = __ldg(fp + 1);
-                    f.p2 = __ldg(fp + 2);
-                    f.p3 = __ldg(fp + 3);
+                    const FastTri f = load_fast(a.fast + first + k);
                     const float d2 = tri_d2_fast(qx, qy, qz, f);
-                    const int idx = __float_as_int(f.p3.w);
+                    const int idx = fast_index(f);
                     if (d2 < best || (d2 == best && idx < best_idx)) {
                         best = d2;
                         best_rec = first + k;
@@ -649,7 +630,7 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
     float4* st_q = reinterpret_cast<float4*>(wbase + packet_stack_bytes(K, cap));
     const uint32_t lt_mask = lanemask_lt();
     const WideNode<K>* __restrict__ nodes = static_cast<const WideNode<K>*>(a.nodes);
-    unsigned long long n_nodes = 0, n_tris = 0, n_pops = 0, n_skips = 0;
+    unsigned long long n_nodes = 0, n_tris = 0, n_pops = 0, n_skips = 0, n_lane_tris = 0, n_rounds = 0;
 
     for (;;) {
         unsigned long long base = 0;
@@ -752,6 +733,7 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                     if (kStats) n_tris += cnt;
                     const uint32_t act = __ballot_sync(kFull, leaf_active);
                     const int na = __popc(act);
+                    if (kStats) n_lane_tris += (unsigned long long)na * cnt;
                     if (kCompact && cnt >= 2 && na >= 1 && na <= 16) {
                         // Few lanes need this leaf: spread its (query, triangle)
                         // pairs over the warp.  A round covers kpr = 32 / na
@@ -768,16 +750,12 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                         const bool worker = lane < sp2.kpr * na;
                         const float4 qq = st_q[worker ? lane - kk * na : 0];
                         for (int k0 = 0; k0 < cnt; k0 += sp2.kpr) {
+                            if (kStats) ++n_rounds;
                             unsigned long long key = kNoKey;
                             const int k = k0 + kk;
                             if (worker && k < cnt) {
-                                const float4* fp = reinterpret_cast<const float4*>(a.fast + first + k);
-                                FastTri f;
-                                f.p0 = __ldg(fp);
-                                f.p1 = __ldg(fp + 1);
-                                f.p2 = __ldg(fp + 2);
-                                f.p3 = __ldg(fp + 3);
-                                key = best_key(tri_d2_fast(qq.x, qq.y, qq.z, f), __float_as_int(f.p3.w));
+                                const FastTri f = load_fast(a.fast + first + k);
+                                key = best_key(tri_d2_fast(qq.x, qq.y, qq.z, f), fast_index(f));
                             }
                             const int nk = min(sp2.kpr, cnt - k0);
                             for (int j = 0; j < nk; ++j) {
@@ -786,15 +764,11 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                             }
                         }
                     } else {
+                        if (kStats) n_rounds += cnt;
                         for (int k = 0; k < cnt; ++k) {
-                            const float4* fp = reinterpret_cast<const float4*>(a.fast + first + k);
-                            FastTri f;
-                            f.p0 = __ldg(fp);
-                            f.p1 = __ldg(fp + 1);
-                            f.p2 = __ldg(fp + 2);
-                            f.p3 = __ldg(fp + 3);
+                            const FastTri f = load_fast(a.fast + first + k);
                             if (leaf_active)
-                                best = min(best, best_key(tri_d2_fast(qx, qy, qz, f), __float_as_int(f.p3.w)));
+                                best = min(best, best_key(tri_d2_fast(qx, qy, qz, f), fast_index(f)));
                         }
                     }
                     if (mine) lim = key_d2(best);
@@ -840,6 +814,8 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
         atomicAdd(&a.stats[1], n_tris);
         atomicAdd(&a.stats[2], n_pops);
         atomicAdd(&a.stats[3], n_skips);
+        atomicAdd(&a.stats[4], n_lane_tris);
+        atomicAdd(&a.stats[5], n_rounds);
     }
 }
 
@@ -1325,14 +1301,9 @@ __device__ void walk_mesh(const WideNode<K>* __restrict__ nodes, const FastTri* 
         } else {
             const int first = leaf_first(cur), cnt = leaf_count(cur);
             for (int k = 0; k < cnt; ++k) {
-                const float4* fp = reinterpret_cast<const float4*>(fast + first + k);
-                FastTri f;
-                f.p0 = __ldg(fp);
-                f.p1 = __ldg(fp + 1);
-                f.p2 = __ldg(fp + 2);
-                f.p3 = __ldg(fp + 3);
+                const FastTri f = load_fast(fast + first + k);
                 const float d2 = tri_d2_fast(qx, qy, qz, f);
-                const int i = __float_as_int(f.p3.w);
+                const int i = fast_index(f);
                 if (d2 < lim || (d2 == lim && rec >= 0 && i < idx)) {
                     lim = d2;
                     rec = first + k;
@@ -1549,21 +1520,21 @@ void timing_enable(bool events, bool counters) {
     g_timing.on = events;
     g_timing.counters = counters;
     if (counters && !g_timing.stats) {
-        if (cudaMalloc(&g_timing.stats, 4 * sizeof(unsigned long long)) == cudaSuccess)
-            cudaMemset(g_timing.stats, 0, 4 * sizeof(unsigned long long));
+        if (cudaMalloc(&g_timing.stats, kStatCount * sizeof(unsigned long long)) == cudaSuccess)
+            cudaMemset(g_timing.stats, 0, kStatCount * sizeof(unsigned long long));
         else
             g_timing.stats = nullptr;
     }
 }
 
-cudaError_t traversal_stats(unsigned long long* out4, bool reset) {
+cudaError_t traversal_stats(unsigned long long* out, bool reset) {
     std::lock_guard<std::mutex> lock(g_timing.mu);
-    for (int k = 0; k < 4; ++k) out4[k] = 0;
+    for (int k = 0; k < kStatCount; ++k) out[k] = 0;
     if (!g_timing.stats) return cudaSuccess;
     cudaError_t e = cudaDeviceSynchronize();
     if (e != cudaSuccess) return e;
-    e = cudaMemcpy(out4, g_timing.stats, 4 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
-    if (e == cudaSuccess && reset) e = cudaMemset(g_timing.stats, 0, 4 * sizeof(unsigned long long));
+    e = cudaMemcpy(out, g_timing.stats, kStatCount * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && reset) e = cudaMemset(g_timing.stats, 0, kStatCount * sizeof(unsigned long long));
     return e;
 }
 

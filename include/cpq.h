@@ -142,16 +142,18 @@ CP_API uint64_t cp_kernel_launches(void);
  * is bracketed by CUDA events on its own stream; cp_timing_read waits for
  * them and returns the summed device time (ms) and the number of launches
  * since the last reset.  CP_TIMING_COUNTERS: packet traversals run a
- * counting build of the kernel (a few percent slower) whose per-warp node
- * visits, leaf triangle tests, stack pops and skipped pops (counts4[0..3],
- * summed over warps) cp_traversal_stats returns; it synchronises the device.
+ * counting build of the kernel (a few percent slower) whose counts, summed
+ * over warps, cp_traversal_stats returns in counts6: [0] warp node visits,
+ * [1] leaf triangles per warp leaf visit, [2] stack pops, [3] skipped pops,
+ * [4] lane-triangle tests (active lanes x leaf triangles), [5] triangle
+ * rounds executed by warps; it synchronises the device.
  * No counterpart in the reference (its only timing is an FPS readout,
  * src/gpurt.cpp:275). */
 #define CP_TIMING_EVENTS 1
 #define CP_TIMING_COUNTERS 2
 CP_API cp_status cp_timing_enable(int32_t flags);
 CP_API cp_status cp_timing_read(double* traverse_ms, int64_t* launches, int32_t reset);
-CP_API cp_status cp_traversal_stats(uint64_t* counts4, int32_t reset);
+CP_API cp_status cp_traversal_stats(uint64_t* counts6, int32_t reset);
 
 /* Diagnostic: read bandwidth (GB/s) of 128-bit L2 loads over a `bytes`-sized
  * buffer, best of 5 timed launches of `reps` sweeps each.  A buffer smaller
@@ -225,9 +227,11 @@ CP_API cp_status cp_query(const cp_mesh* mesh, const float* queries, int64_t nq,
                           size_t workspace_bytes, cp_stream_t stream);
 
 /*
- * cp_query with HOST arrays: copies the queries to the device in chunks,
- * queries each chunk and copies the results back, overlapping the copies of
- * one chunk with the traversal of the previous one.  Host arrays should be
+ * cp_query with HOST arrays: copies the queries to the device, queries them
+ * and copies the results back.  Up to 64M queries are ordered and traversed
+ * as one set (denser sets traverse faster than chunks of them); larger calls
+ * go in 64M-query chunks whose copies overlap the previous chunk's traversal
+ * on a second stream.  Host arrays should be
  * pinned (cudaHostAlloc / cudaHostRegister) for full copy speed.  Synchronous:
  * the outputs are ready when it returns.
  */

@@ -453,6 +453,26 @@ def test_host_buffers_match_device(cpq, cuda):
     assert torch.equal(h["bary"], d.bary.cpu())
 
 
+def test_host_buffers_two_chunks(cpq, cuda):
+    """Past 64M queries the host path pipelines chunks on two streams; the
+    answers are those of one device call (each query's answer does not depend
+    on the ordering, only ties between equal distances may pick another
+    triangle)."""
+    import torch
+
+    from gpurt_cpq import workloads as W
+
+    v, t = W.torus(100, 40)
+    nq = (1 << 26) + 4097
+    q = torch.from_numpy(W.uniform_queries(nq, -1.5, 1.5, 9)).pin_memory()
+    m = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=4)
+    h = m.query_host(q)
+    d = m.query(q.to(cuda))
+    torch.testing.assert_close(h["dist"], d.dist.cpu(), rtol=1e-6, atol=0)
+    assert (h["tri"] == d.tri.cpu()).float().mean() > 0.9999
+    del d, h
+
+
 def test_refit_moves_vertices(orc, cpq, cuda):
     from gpurt_cpq import workloads as W
 
