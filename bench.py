@@ -331,7 +331,7 @@ def our_arm(args):
     trav_ms = tms.value / max(tl.value, 1)
     # packet kernel: per-warp node visits / triangle tests, from one more
     # (untimed) query through the counting build of the kernel
-    counts = (c_uint64 * 6)()
+    counts = (c_uint64 * 7)()
     lib.cp_timing_enable(CP_TIMING_COUNTERS)
     lib.cp_traversal_stats(counts, 1)
     mesh.query(qd, workspace=ws, opts=qopts, out=out)
@@ -345,7 +345,8 @@ def our_arm(args):
                      "warp_skipped_pops_per_32_queries": counts[3] * 32 / per_q,
                      "lane_tri_tests_per_query": counts[4] / per_q,
                      "warp_tri_rounds_per_32_queries": counts[5] * 32 / per_q,
-                     "tri_round_lane_use": counts[4] / max(counts[5] * 32, 1)} if counts[0] else None
+                     "tri_round_lane_use": counts[4] / max(counts[5] * 32, 1),
+                     "node_visit_lane_use": counts[6] / max(counts[0] * 32, 1)} if counts[0] else None
     ms = max_over_ranks(ms, world, dev)
     value = whole_job_rate(nq * args.steps, world, ms * 1e-3)
     assert mesh.device_status() == 0

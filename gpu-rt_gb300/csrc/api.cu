@@ -300,11 +300,11 @@ CP_API cp_status cp_timing_read(double* traverse_ms, int64_t* launches, int32_t 
     return CP_SUCCESS;
 }
 
-CP_API cp_status cp_traversal_stats(uint64_t* counts6, int32_t reset) {
-    if (!counts6) return fail(CP_ERROR_INVALID_VALUE, "counts6 is NULL");
+CP_API cp_status cp_traversal_stats(uint64_t* counts7, int32_t reset) {
+    if (!counts7) return fail(CP_ERROR_INVALID_VALUE, "counts7 is NULL");
     unsigned long long c[kStatCount];
     CP_CUDA(traversal_stats(c, reset != 0), "traversal stats");
-    for (int k = 0; k < kStatCount; ++k) counts6[k] = c[k];
+    for (int k = 0; k < kStatCount; ++k) counts7[k] = c[k];
     return CP_SUCCESS;
 }
 

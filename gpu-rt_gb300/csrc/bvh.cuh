@@ -108,8 +108,9 @@ void timing_enable(bool events, bool counters);
 cudaError_t timing_read(double* ms, int64_t* launches, bool reset);
 // Counters of the counting packet kernel: warp node visits, leaf triangles
 // (per warp leaf visit), stack pops, skipped pops, lane-triangle tests
-// (active lanes x leaf triangles) and triangle rounds executed.
-constexpr int kStatCount = 6;
+// (active lanes x leaf triangles), triangle rounds executed and lane-node
+// visits (lanes whose bound admitted the node, summed over warp visits).
+constexpr int kStatCount = 7;
 cudaError_t traversal_stats(unsigned long long* out, bool reset);
 
 // Proxy triangles for the top level of an instanced scene: per instance the

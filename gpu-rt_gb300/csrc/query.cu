@@ -630,7 +630,8 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
     float4* st_q = reinterpret_cast<float4*>(wbase + packet_stack_bytes(K, cap));
     const uint32_t lt_mask = lanemask_lt();
     const WideNode<K>* __restrict__ nodes = static_cast<const WideNode<K>*>(a.nodes);
-    unsigned long long n_nodes = 0, n_tris = 0, n_pops = 0, n_skips = 0, n_lane_tris = 0, n_rounds = 0;
+    unsigned long long n_nodes = 0, n_tris = 0, n_pops = 0, n_skips = 0, n_lane_tris = 0, n_rounds = 0,
+                       n_lane_nodes = 0;
 
     for (;;) {
         unsigned long long base = 0;
@@ -663,10 +664,15 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
             uint32_t t_order = 0;  // the top entry's slots still to visit, next in the low nibble
             int t_cnt = 0;         // and their number
             int cur = a.wide_root[mesh];
-            bool leaf_active = false;  // for leaves: this lane's bound beat its best
+            // this lane's bound admitted the node being visited (the root, a
+            // wide node, admits the round's lanes); used at leaves
+            bool leaf_active = mine;
             for (;;) {
                 if (cur >= 0) {
-                    if (kStats) ++n_nodes;
+                    if (kStats) {
+                        ++n_nodes;
+                        n_lane_nodes += __popc(__ballot_sync(kFull, leaf_active));
+                    }
                     const WideNode<K>* nd = nodes + cur;
                     f32x2 lox[K / 2], hix[K / 2], loy[K / 2], hiy[K / 2], loz[K / 2], hiz[K / 2];
                     int32_t ch[K];
@@ -749,19 +755,21 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                         const int kk = (int)(((float)lane + 0.5f) * sp2.inv);
                         const bool worker = lane < sp2.kpr * na;
                         const float4 qq = st_q[worker ? lane - kk * na : 0];
+                        // a worker serves the same query in every round: keep
+                        // its minimum and gather once
+                        unsigned long long key = kNoKey;
                         for (int k0 = 0; k0 < cnt; k0 += sp2.kpr) {
                             if (kStats) ++n_rounds;
-                            unsigned long long key = kNoKey;
                             const int k = k0 + kk;
                             if (worker && k < cnt) {
                                 const FastTri f = load_fast(a.fast + first + k);
-                                key = best_key(tri_d2_fast(qq.x, qq.y, qq.z, f), fast_index(f));
+                                key = min(key, best_key(tri_d2_fast(qq.x, qq.y, qq.z, f), fast_index(f)));
                             }
-                            const int nk = min(sp2.kpr, cnt - k0);
-                            for (int j = 0; j < nk; ++j) {
-                                const unsigned long long got = __shfl_sync(kFull, key, (r + j * na) & 31);
-                                if (leaf_active) best = min(best, got);
-                            }
+                        }
+                        const int nk = min(sp2.kpr, cnt);
+                        for (int j = 0; j < nk; ++j) {
+                            const unsigned long long got = __shfl_sync(kFull, key, (r + j * na) & 31);
+                            if (leaf_active) best = min(best, got);
                         }
                     } else {
                         if (kStats) n_rounds += cnt;
@@ -816,6 +824,7 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
         atomicAdd(&a.stats[3], n_skips);
         atomicAdd(&a.stats[4], n_lane_tris);
         atomicAdd(&a.stats[5], n_rounds);
+        atomicAdd(&a.stats[6], n_lane_nodes);
     }
 }
 

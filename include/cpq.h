@@ -143,17 +143,18 @@ CP_API uint64_t cp_kernel_launches(void);
  * them and returns the summed device time (ms) and the number of launches
  * since the last reset.  CP_TIMING_COUNTERS: packet traversals run a
  * counting build of the kernel (a few percent slower) whose counts, summed
- * over warps, cp_traversal_stats returns in counts6: [0] warp node visits,
+ * over warps, cp_traversal_stats returns in counts7: [0] warp node visits,
  * [1] leaf triangles per warp leaf visit, [2] stack pops, [3] skipped pops,
  * [4] lane-triangle tests (active lanes x leaf triangles), [5] triangle
- * rounds executed by warps; it synchronises the device.
+ * rounds executed by warps, [6] lane-node visits (lanes whose bound
+ * admitted the visited node); it synchronises the device.
  * No counterpart in the reference (its only timing is an FPS readout,
  * src/gpurt.cpp:275). */
 #define CP_TIMING_EVENTS 1
 #define CP_TIMING_COUNTERS 2
 CP_API cp_status cp_timing_enable(int32_t flags);
 CP_API cp_status cp_timing_read(double* traverse_ms, int64_t* launches, int32_t reset);
-CP_API cp_status cp_traversal_stats(uint64_t* counts6, int32_t reset);
+CP_API cp_status cp_traversal_stats(uint64_t* counts7, int32_t reset);
 
 /* Diagnostic: read bandwidth (GB/s) of 128-bit L2 loads over a `bytes`-sized
  * buffer, best of 5 timed launches of `reps` sweeps each.  A buffer smaller
