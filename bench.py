@@ -57,8 +57,8 @@ CANON_V_NODE = 84.273
 CANON_V_TRI = 44.413
 # DRAM bytes (read + write) per query of one traversal launch, from the ncu
 # capture summarised in profiles/k_traverse_packet_large_heightfield.md
-# (4.154 + 1.714 GB for 16,777,216 queries, leaf 4)
-NCU_TRAFFIC_PER_QUERY = 349.7
+# (4.220 + 1.714 GB for 16,777,216 queries, leaf 8)
+NCU_TRAFFIC_PER_QUERY = 353.7
 
 
 def parse():

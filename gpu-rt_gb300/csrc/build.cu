@@ -278,49 +278,52 @@ __device__ __forceinline__ uint32_t degenerate_flag(float3 a, float3 b, float3 c
     return (nn > __fmul_rn(1e-10f, __fmul_rn(lab, lac))) ? 0u : kTriDegenerate;
 }
 
+// The frame is computed in FP64 from the FP32 vertices and each stored value
+// rounded once, so its directions are within half an ulp of the exact ones:
+// the test's error is then the FP32 arithmetic of the query alone.
 __device__ __forceinline__ FastTri make_fast_tri(float3 a, float3 b, float3 c, int32_t local,
                                                  bool degenerate) {
-    const float3 ab = make_float3(b.x - a.x, b.y - a.y, b.z - a.z);
-    const float3 ac = make_float3(c.x - a.x, c.y - a.y, c.z - a.z);
-    const float aa = ab.x * ab.x + ab.y * ab.y + ab.z * ab.z;
-    const float cc = ac.x * ac.x + ac.y * ac.y + ac.z * ac.z;
+    const double abx = (double)b.x - a.x, aby = (double)b.y - a.y, abz = (double)b.z - a.z;
+    const double acx = (double)c.x - a.x, acy = (double)c.y - a.y, acz = (double)c.z - a.z;
+    const double aa = abx * abx + aby * aby + abz * abz;
+    const double cc = acx * acx + acy * acy + acz * acz;
     // e1: along ab, else along ac, else any axis (a point)
-    float3 e1 = make_float3(1.0f, 0.0f, 0.0f);
-    if (aa > 0.0f) {
-        const float r = 1.0f / sqrtf(aa);
-        e1 = make_float3(ab.x * r, ab.y * r, ab.z * r);
-    } else if (cc > 0.0f) {
-        const float r = 1.0f / sqrtf(cc);
-        e1 = make_float3(ac.x * r, ac.y * r, ac.z * r);
+    double e1x = 1.0, e1y = 0.0, e1z = 0.0;
+    if (aa > 0.0) {
+        const double r = 1.0 / sqrt(aa);
+        e1x = abx * r; e1y = aby * r; e1z = abz * r;
+    } else if (cc > 0.0) {
+        const double r = 1.0 / sqrt(cc);
+        e1x = acx * r; e1y = acy * r; e1z = acz * r;
     }
     // e2: ac's part across e1; for a zero-area triangle any unit vector
     // across e1 (from the axis e1 leans on least)
-    const float ce = ac.x * e1.x + ac.y * e1.y + ac.z * e1.z;
-    float3 w = make_float3(ac.x - ce * e1.x, ac.y - ce * e1.y, ac.z - ce * e1.z);
-    float ww = w.x * w.x + w.y * w.y + w.z * w.z;
-    if (degenerate || !(ww > 0.0f)) {
-        const float ax = fabsf(e1.x), ay = fabsf(e1.y), az = fabsf(e1.z);
-        const float3 t = ax <= ay && ax <= az ? make_float3(1.0f, 0.0f, 0.0f)
-                         : ay <= az           ? make_float3(0.0f, 1.0f, 0.0f)
-                                              : make_float3(0.0f, 0.0f, 1.0f);
-        const float te = t.x * e1.x + t.y * e1.y + t.z * e1.z;
-        w = make_float3(t.x - te * e1.x, t.y - te * e1.y, t.z - te * e1.z);
-        ww = w.x * w.x + w.y * w.y + w.z * w.z;
+    const double ce = acx * e1x + acy * e1y + acz * e1z;
+    double wx = acx - ce * e1x, wy = acy - ce * e1y, wz = acz - ce * e1z;
+    double ww = wx * wx + wy * wy + wz * wz;
+    if (degenerate || !(ww > 0.0)) {
+        const double ax = fabs(e1x), ay = fabs(e1y), az = fabs(e1z);
+        const double tx = (ax <= ay && ax <= az) ? 1.0 : 0.0;
+        const double ty = (tx == 0.0 && ay <= az) ? 1.0 : 0.0;
+        const double tz = (tx == 0.0 && ty == 0.0) ? 1.0 : 0.0;
+        const double te = tx * e1x + ty * e1y + tz * e1z;
+        wx = tx - te * e1x; wy = ty - te * e1y; wz = tz - te * e1z;
+        ww = wx * wx + wy * wy + wz * wz;
     }
-    const float rw = 1.0f / sqrtf(ww);
-    const float3 e2 = make_float3(w.x * rw, w.y * rw, w.z * rw);
-    const float3 n = make_float3(e1.y * e2.z - e1.z * e2.y, e1.z * e2.x - e1.x * e2.z, e1.x * e2.y - e1.y * e2.x);
-    const float L1 = ab.x * e1.x + ab.y * e1.y + ab.z * e1.z;
-    const float x2 = ce;
-    const float y2 = fmaxf(ac.x * e2.x + ac.y * e2.y + ac.z * e2.z, 0.0f);
-    const float bx = x2 - L1;
-    const float l2 = x2 * x2 + y2 * y2, l3 = bx * bx + y2 * y2;
+    const double rw = 1.0 / sqrt(ww);
+    const double e2x = wx * rw, e2y = wy * rw, e2z = wz * rw;
+    const double nx = e1y * e2z - e1z * e2y, ny = e1z * e2x - e1x * e2z, nz = e1x * e2y - e1y * e2x;
+    const double L1 = abx * e1x + aby * e1y + abz * e1z;
+    const double x2 = ce;
+    const double y2 = fmax(acx * e2x + acy * e2y + acz * e2z, 0.0);
+    const double bx = x2 - L1;
+    const double l2 = x2 * x2 + y2 * y2, l3 = bx * bx + y2 * y2;
     FastTri f;
-    f.p0 = make_float4(a.x, a.y, a.z, L1);
-    f.p1 = make_float4(e1.x, e1.y, e1.z, x2);
-    f.p2 = make_float4(e2.x, e2.y, e2.z, y2);
-    f.p3 = make_float4(n.x, n.y, n.z, bx);
-    f.p4 = make_float4(l2 > 0.0f ? 1.0f / l2 : 0.0f, l3 > 0.0f ? 1.0f / l3 : 0.0f,
+    f.p0 = make_float4(a.x, a.y, a.z, (float)L1);
+    f.p1 = make_float4((float)e1x, (float)e1y, (float)e1z, (float)x2);
+    f.p2 = make_float4((float)e2x, (float)e2y, (float)e2z, (float)y2);
+    f.p3 = make_float4((float)nx, (float)ny, (float)nz, (float)bx);
+    f.p4 = make_float4(l2 > 0.0 ? (float)(1.0 / l2) : 0.0f, l3 > 0.0 ? (float)(1.0 / l3) : 0.0f,
                        degenerate ? INFINITY : 0.0f, __int_as_float(local));
     return f;
 }
