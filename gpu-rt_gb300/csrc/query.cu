@@ -109,6 +109,13 @@ __device__ __forceinline__ float max3f(float a, float b, float c) {
     return d;
 }
 
+// min(a, b, c) in one instruction (three-input min.f32, sm_100 and later).
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+
 __device__ __forceinline__ float box_lb2(float qx, float qy, float qz, float lox, float hix,
                                          float loy, float hiy, float loz, float hiz) {
     const float dx = max3f(lox - qx, qx - hix, 0.0f);
@@ -175,32 +182,36 @@ __device__ __forceinline__ void load_row2(const float* __restrict__ p, f32x2 (&r
 // query's offset from a in the triangle's frame, (u, v) in the plane and h
 // off it, then h^2 plus the squared 2D distance to the triangle (a, b, c) =
 // ((0, 0), (L1, 0), (x2, y2)) — zero inside, else the nearest of the three
-// edge segments, each clamped with a saturating multiply.  Nearly all work is
-// FMA-pipe arithmetic, and lanes that test the same triangle from different
-// Voronoi regions do not diverge.  The frame is FP32, so the value is the
-// distance to the triangle to a few ulps of |q - a|; the winner is
-// re-evaluated exactly.
+// edge segments, each clamped with a saturating multiply.  The ALU pipe is
+// the kernel's busiest, so clamps and the inside test are written for the
+// FMA pipe: the distance along ab beyond [0, L1] is (|u| + |u - L1| - L1) / 2
+// (abs is an operand modifier), and "inside" becomes a factor
+// sat(max of the three edge functions * 2^126), 0 when none is positive.
+// Lanes that test the same triangle from different Voronoi regions do not
+// diverge.  The frame is rounded from FP64, so the value is the distance to
+// the triangle to a few ulps of |q - a|; the winner is re-evaluated exactly.
 __device__ __forceinline__ float tri_d2_fast(float qx, float qy, float qz, const FastTri& f) {
     const float apx = qx - f.p0.x, apy = qy - f.p0.y, apz = qz - f.p0.z;
     const float u = fmaf(f.p1.x, apx, fmaf(f.p1.y, apy, f.p1.z * apz));
     const float v = fmaf(f.p2.x, apx, fmaf(f.p2.y, apy, f.p2.z * apz));
     const float h = fmaf(f.p3.x, apx, fmaf(f.p3.y, apy, f.p3.z * apz));
     const float L1 = f.p0.w, x2 = f.p1.w, y2 = f.p2.w, bx = f.p3.w;
-    // edge ab: the u axis from 0 to L1
-    const float du = u - fminf(fmaxf(u, 0.0f), L1);
-    const float d_ab = fmaf(du, du, v * v);
+    const float bu = u - L1;
+    // edge ab: twice the distance along the u axis outside [0, L1]
+    const float xa = (fabsf(u) + fabsf(bu)) - L1;
+    const float d_ab = fmaf(0.25f * xa, xa, v * v);
     // edge ac: from the origin to (x2, y2)
     const float s2 = __saturatef(fmaf(u, x2, v * y2) * f.p4.x);
     const float cx = fmaf(-s2, x2, u), cy = fmaf(-s2, y2, v);
     const float d_ac = fmaf(cx, cx, cy * cy);
     // edge bc: from (L1, 0) to (x2, y2)
-    const float bu = u - L1;
     const float s3 = __saturatef(fmaf(bu, bx, v * y2) * f.p4.y);
     const float ex = fmaf(-s3, bx, bu), ey = fmaf(-s3, y2, v);
     const float d_bc = fmaf(ex, ex, ey * ey);
-    // inside: left of ab, ca and bc (counter-clockwise, y2 >= 0)
-    const bool inside = v >= f.p4.z && fmaf(u, y2, -v * x2) >= 0.0f && fmaf(bu, y2, -v * bx) <= 0.0f;
-    return fmaf(h, h, inside ? 0.0f : fminf(d_ab, fminf(d_ac, d_bc)));
+    // outside ab, ca or bc (counter-clockwise, y2 >= 0); vmin = +inf marks a
+    // zero-area triangle, never inside
+    const float out = max3f(f.p4.z - v, fmaf(v, x2, -u * y2), fmaf(bu, y2, -v * bx));
+    return fmaf(h, h, min3f(d_ab, d_ac, d_bc) * __saturatef(out * 0x1p126f));
 }
 
 // Degenerate triangle in FP32 with barycentrics (weights of b and c).
