@@ -739,9 +739,13 @@ CP_API cp_status cp_batch_query(cp_batch* bt, const float* queries, const int64_
 
 struct cp_scene {
     Bvh top;                    // over the instances' proxies, one per instance
+    Bvh baked;                  // world-space copies of the general-affine instances
+    bool has_baked = false;
     const cp_batch* batch = nullptr;
     int32_t n = 0;
+    int32_t n_baked = 0;
     int32_t* d_inst_mesh = nullptr;
+    int32_t* d_baked = nullptr; // n: baked copy of each instance, or -1
     float* d_fwd = nullptr;     // n x 12 world <- object
     float* d_inv = nullptr;     // n x 12 object <- world
     float* d_s2 = nullptr;      // n x 2: squared scale, lower bound of the squared stretch
@@ -749,14 +753,19 @@ struct cp_scene {
 
 namespace {
 
-// Per instance: the matrix as given, its inverse (in double, rounded once),
-// the squared scale s^2 = tr(M^T M) / 3 and a lower bound of M^T M's smallest
-// eigenvalue (Gershgorin).  Refuses non-finite and non-similarity matrices.
+// Per instance: the matrix as given and whether it is a similarity (M^T M =
+// s^2 I within 1e-5 s^2, invertible) — such instances are walked in object
+// space with the inverse (FP64, rounded once), s^2 for ranking and a
+// Gershgorin lower bound of M^T M's eigenvalues for pruning; every other
+// affine matrix (non-uniform scale, shear, singular) is baked.  Refuses
+// non-finite matrices.
 cp_status instance_frames(const float* T, int32_t n, std::vector<float>& fwd, std::vector<float>& inv,
-                          std::vector<float>& s2) {
+                          std::vector<float>& s2, std::vector<int32_t>& baked) {
     fwd.assign(T, T + (size_t)12 * n);
-    inv.resize((size_t)12 * n);
-    s2.resize((size_t)2 * n);
+    inv.assign((size_t)12 * n, 0.0f);
+    s2.assign((size_t)2 * n, 1.0f);
+    baked.assign((size_t)n, -1);
+    int32_t nb = 0;
     for (int32_t i = 0; i < n; ++i) {
         const float* t = T + (size_t)12 * i;
         for (int k = 0; k < 12; ++k)
@@ -771,8 +780,6 @@ cp_status instance_frames(const float* T, int32_t n, std::vector<float>& fwd, st
         for (int j = 0; j < 3; ++j)
             for (int k = 0; k < 3; ++k) G[j][k] = M[0][j] * M[0][k] + M[1][j] * M[1][k] + M[2][j] * M[2][k];
         const double s = (G[0][0] + G[1][1] + G[2][2]) / 3.0;
-        if (!(s > 1e-30) || !std::isfinite(s))
-            return fail(CP_ERROR_INVALID_VALUE, "instance " + std::to_string(i) + ": singular transform");
         double dev = 0.0, lo = INFINITY;
         for (int j = 0; j < 3; ++j) {
             double off = 0.0;
@@ -782,13 +789,14 @@ cp_status instance_frames(const float* T, int32_t n, std::vector<float>& fwd, st
             }
             lo = std::min(lo, G[j][j] - off);
         }
-        if (dev > 1e-5 * s)
-            return fail(CP_ERROR_INVALID_VALUE,
-                        "instance " + std::to_string(i) +
-                            ": transform is not a similarity (rotation or reflection, uniform scale, translation)");
         const double det = M[0][0] * (M[1][1] * M[2][2] - M[1][2] * M[2][1]) -
                            M[0][1] * (M[1][0] * M[2][2] - M[1][2] * M[2][0]) +
                            M[0][2] * (M[1][0] * M[2][1] - M[1][1] * M[2][0]);
+        const bool similarity = s > 1e-30 && std::isfinite(s) && dev <= 1e-5 * s && det != 0.0 && lo > 0.0;
+        if (!similarity) {
+            baked[i] = nb++;
+            continue;
+        }
         double A[3][3];  // inverse by the adjugate
         for (int r = 0; r < 3; ++r)
             for (int c = 0; c < 3; ++c) {
@@ -806,16 +814,77 @@ cp_status instance_frames(const float* T, int32_t n, std::vector<float>& fwd, st
     return CP_SUCCESS;
 }
 
-// Frames to the device, proxies, top-level build.  The top level has the
-// batch's branching factor and one instance per leaf.
+// Frames to the device, world-space copies of the general-affine instances,
+// proxies, top-level build.  Every level has the batch's branching factor;
+// the top level holds one instance per leaf, the baked copies the batch's
+// leaf size.
 cp_status scene_build(cp_scene* sc, const float* T, cudaStream_t st) {
     std::vector<float> fwd, inv, s2;
-    cp_status s = instance_frames(T, sc->n, fwd, inv, s2);
+    std::vector<int32_t> baked;
+    cp_status s = instance_frames(T, sc->n, fwd, inv, s2, baked);
     if (s != CP_SUCCESS) return s;
     const size_t n = (size_t)sc->n;
+    const Bvh& bottom = sc->batch->bvh;
     CP_CUDA(cudaMemcpyAsync(sc->d_fwd, fwd.data(), sizeof(float) * 12 * n, cudaMemcpyHostToDevice, st), "scene upload");
     CP_CUDA(cudaMemcpyAsync(sc->d_inv, inv.data(), sizeof(float) * 12 * n, cudaMemcpyHostToDevice, st), "scene upload");
     CP_CUDA(cudaMemcpyAsync(sc->d_s2, s2.data(), sizeof(float) * 2 * n, cudaMemcpyHostToDevice, st), "scene upload");
+    CP_CUDA(cudaMemcpyAsync(sc->d_baked, baked.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice, st),
+            "scene upload");
+    // world-space copies, one mesh each, in the mesh's local triangle order
+    std::vector<int32_t> list;
+    std::vector<int64_t> out_off(1, 0), voff(1, 0);
+    std::vector<int32_t> h_mesh(n);
+    CP_CUDA(cudaMemcpyAsync(h_mesh.data(), sc->d_inst_mesh, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st),
+            "scene upload");
+    CP_CUDA(cudaStreamSynchronize(st), "scene upload");
+    for (size_t i = 0; i < n; ++i) {
+        if (baked[i] < 0) continue;
+        const int m = h_mesh[i];
+        const int64_t nt = bottom.h_toff[m + 1] - bottom.h_toff[m];
+        list.push_back((int32_t)i);
+        out_off.push_back(out_off.back() + nt);
+        voff.push_back(3 * out_off.back());
+    }
+    const int64_t total = out_off.back();
+    if (total > kMaxTriangles) return fail(CP_ERROR_NOT_SUPPORTED, "more than 2^27 - 1 baked triangles");
+    bvh_free(sc->baked);
+    sc->baked = Bvh();
+    sc->has_baked = false;
+    sc->n_baked = (int32_t)list.size();
+    if (total > 0) {
+        float* verts = nullptr;
+        int32_t *tris = nullptr, *d_list = nullptr;
+        int64_t* d_off = nullptr;
+        cudaError_t e = cudaMalloc(&verts, sizeof(float) * 9 * total);
+        if (e == cudaSuccess) e = cudaMalloc(&tris, sizeof(int32_t) * 3 * total);
+        if (e == cudaSuccess) e = cudaMalloc(&d_list, sizeof(int32_t) * list.size());
+        if (e == cudaSuccess) e = cudaMalloc(&d_off, sizeof(int64_t) * out_off.size());
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_list, list.data(), sizeof(int32_t) * list.size(), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_off, out_off.data(), sizeof(int64_t) * out_off.size(), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = instance_bake(bottom, d_list, sc->d_inst_mesh, sc->d_fwd, d_off, (int32_t)list.size(), total, verts,
+                              tris, st);
+        cp_status bs = CP_SUCCESS;
+        if (e == cudaSuccess) {
+            cp_build_opts bo;
+            cp_build_opts_default(&bo);
+            bo.branching = bottom.p.K;
+            bo.leaf_size = bottom.p.leaf_size;
+            std::vector<int64_t> toff(out_off.begin(), out_off.end());
+            bs = build_common(sc->baked, verts, 12, tris, voff, toff, &bo, st);
+        }
+        cudaError_t e2 = cudaStreamSynchronize(st);
+        cudaFree(verts);
+        cudaFree(tris);
+        cudaFree(d_list);
+        cudaFree(d_off);
+        if (e != cudaSuccess) return cuda_fail(e, "scene bake");
+        if (bs != CP_SUCCESS) return bs;
+        if (e2 != cudaSuccess) return cuda_fail(e2, "scene bake");
+        sc->has_baked = true;
+    }
     float* verts = nullptr;
     int32_t* tris = nullptr;
     if (cudaMalloc(&verts, sizeof(float) * 6 * n) != cudaSuccess ||
@@ -823,13 +892,13 @@ cp_status scene_build(cp_scene* sc, const float* T, cudaStream_t st) {
         cudaFree(verts);
         return fail(CP_ERROR_OUT_OF_MEMORY, "scene proxies");
     }
-    cudaError_t e = instance_proxies(sc->batch->bvh, sc->d_inst_mesh, sc->d_fwd, sc->n, verts, tris, st);
+    cudaError_t e = instance_proxies(bottom, sc->d_inst_mesh, sc->d_fwd, sc->n, verts, tris, st);
     if (e == cudaSuccess) {
         bvh_free(sc->top);
         sc->top = Bvh();
         cp_build_opts bo;
         cp_build_opts_default(&bo);
-        bo.branching = sc->batch->bvh.p.K;
+        bo.branching = bottom.p.K;
         bo.leaf_size = 1;
         s = build_common(sc->top, verts, 12, tris, {0, (int64_t)(2 * n)}, {0, (int64_t)n}, &bo, st);
     }
@@ -844,10 +913,12 @@ cp_status scene_build(cp_scene* sc, const float* T, cudaStream_t st) {
 
 void scene_free(cp_scene* sc) {
     cudaFree(sc->d_inst_mesh);
+    cudaFree(sc->d_baked);
     cudaFree(sc->d_fwd);
     cudaFree(sc->d_inv);
     cudaFree(sc->d_s2);
     bvh_free(sc->top);
+    bvh_free(sc->baked);
     delete sc;
 }
 
@@ -874,6 +945,7 @@ CP_API cp_status cp_scene_create(const cp_batch* batch, const int32_t* instance_
     sc->n = n_instances;
     const size_t n = (size_t)n_instances;
     if (cudaMalloc(&sc->d_inst_mesh, sizeof(int32_t) * n) != cudaSuccess ||
+        cudaMalloc(&sc->d_baked, sizeof(int32_t) * n) != cudaSuccess ||
         cudaMalloc(&sc->d_fwd, sizeof(float) * 12 * n) != cudaSuccess ||
         cudaMalloc(&sc->d_inv, sizeof(float) * 12 * n) != cudaSuccess ||
         cudaMalloc(&sc->d_s2, sizeof(float) * 2 * n) != cudaSuccess) {
@@ -938,8 +1010,14 @@ CP_API cp_status cp_scene_query(const cp_scene* scene, const float* queries, int
     } else if (ws_bytes < need) {
         return fail(CP_ERROR_SCRATCH_TOO_SMALL, "workspace smaller than cp_scene_query_workspace_size()");
     }
-    cudaError_t e = bvh_instance_query(scene->top, scene->batch->bvh, scene->d_inst_mesh, scene->d_inv,
-                                       scene->d_fwd, scene->d_s2, queries, nq, qp.sort != 0, out_point,
+    InstanceSet is;
+    is.mesh = scene->d_inst_mesh;
+    is.baked = scene->d_baked;
+    is.inv = scene->d_inv;
+    is.fwd = scene->d_fwd;
+    is.s2 = scene->d_s2;
+    is.baked_bvh = scene->has_baked ? &scene->baked : nullptr;
+    cudaError_t e = bvh_instance_query(scene->top, scene->batch->bvh, is, queries, nq, qp.sort != 0, out_point,
                                        out_dist, out_instance, out_tri, out_bary, workspace, ws_bytes, st);
     if (own) cudaFreeAsync(own, st);
     if (e != cudaSuccess) return cuda_fail(e, "scene query");

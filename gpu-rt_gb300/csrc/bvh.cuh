@@ -93,10 +93,12 @@ size_t query_workspace_bytes(const Bvh& b, int64_t nq, const QueryParams& qp);
 // The visiting order of nq points (queries or ray origins): their Hilbert
 // order when `sort` (else nullptr), in a workspace of
 // query_workspace_bytes(b, nq, {sort}) bytes, plus the zeroed work counter of
-// a persistent traversal.  Stream-ordered; no host synchronisation.
+// a persistent traversal.  `coarse` sorts only the Hilbert index's top bits
+// (about 16 points per curve segment): a radix pass less, for per-thread
+// walks.  Stream-ordered; no host synchronisation.
 cudaError_t order_points(const Bvh& b, const float* points, int64_t nq, const int64_t* d_qoff,
                          bool sort, void* ws, size_t ws_bytes, cudaStream_t st, const int32_t** perm,
-                         unsigned long long** counter);
+                         unsigned long long** counter, bool coarse = false);
 
 // q_off: device array of nmeshes + 1 query offsets (nullptr for one mesh).
 cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int64_t* d_qoff,
@@ -118,17 +120,33 @@ cudaError_t traversal_stats(unsigned long long* out, bool reset);
 cudaError_t instance_proxies(const Bvh& bottom, const int32_t* inst_mesh, const float* inst_fwd,
                              int32_t n, float* verts, int32_t* tris, cudaStream_t st);
 
-// Closest points over instances (similarity transforms) of a batch's meshes:
-// `top` is a BVH over the instances' proxies (local index = instance),
-// `bottom` the batch.  inst_inv / inst_fwd: 12 floats per instance (object <-
-// world, world <- object, row-major 3 x 4); inst_s2: 2 per instance, the
-// squared scale and a lower bound of the smallest squared stretch.
+// The instances of a scene on the device.  Similarity instances are walked
+// through the batch's own BVHs in object space; general affine ones through
+// world-space copies (`baked_bvh`, one mesh per such instance, built from
+// instance_bake's output).
+struct InstanceSet {
+    const int32_t* mesh = nullptr;   // per instance: the batch mesh it places
+    const int32_t* baked = nullptr;  // per instance: its baked copy, or -1
+    const float* inv = nullptr;      // 12 per instance: object <- world, row-major 3 x 4
+    const float* fwd = nullptr;      // 12 per instance: world <- object
+    const float* s2 = nullptr;       // 2 per instance: squared scale, lower bound of the squared stretch
+    const Bvh* baked_bvh = nullptr;  // null when every instance is a similarity
+};
+
+// World-space triangles of the baked instances: for each j < nb, instance
+// baked_inst[j]'s mesh in its local triangle order at out_off[j] (host
+// prefix sums copied to the device, total = out_off[nb]); verts 9 floats and
+// tris 3 local indices (3i, 3i+1, 3i+2) per triangle.
+cudaError_t instance_bake(const Bvh& bottom, const int32_t* baked_inst, const int32_t* inst_mesh,
+                          const float* inst_fwd, const int64_t* out_off, int32_t nb, int64_t total, float* verts,
+                          int32_t* tris, cudaStream_t st);
+
+// Closest points over the instances of a batch's meshes: `top` is a BVH
+// over the instances' proxies (local index = instance), `bottom` the batch.
 // Workspace: query_workspace_bytes(top, nq, ...) with the same sort flag.
-cudaError_t bvh_instance_query(const Bvh& top, const Bvh& bottom, const int32_t* inst_mesh,
-                               const float* inst_inv, const float* inst_fwd, const float* inst_s2,
-                               const float* queries, int64_t nq, bool sort, float* out_point,
-                               float* out_dist, int32_t* out_inst, int32_t* out_tri, float* out_bary,
-                               void* ws, size_t ws_bytes, cudaStream_t st);
+cudaError_t bvh_instance_query(const Bvh& top, const Bvh& bottom, const InstanceSet& is, const float* queries,
+                               int64_t nq, bool sort, float* out_point, float* out_dist, int32_t* out_inst,
+                               int32_t* out_tri, float* out_bary, void* ws, size_t ws_bytes, cudaStream_t st);
 
 cudaError_t bvh_backward(const Bvh& b, const float* queries, const int32_t* tri, const float* bary,
                          const float* grad_dist, int64_t nq, float* grad_q, float* grad_verts,

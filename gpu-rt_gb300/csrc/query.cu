@@ -1245,7 +1245,13 @@ struct InstArgs {
     const FastTri* bfast;
     const TriRec* brecs;
     const int32_t* broot;      // per mesh
+    const int32_t* binv_order; // the batch's global triangle -> record position
+    const int64_t* btoff;      // the batch's per-mesh triangle offsets
+    const void* knodes;        // baked level: world-space copies of the general-affine instances
+    const FastTri* kfast;
+    const int32_t* kroot;      // per baked instance
     const int32_t* inst_mesh;  // per instance
+    const int32_t* inst_baked; // per instance: its baked copy, or -1 (a similarity)
     const float* inst_inv;     // 12 per instance: object <- world, row-major 3 x 4 (3 x 3 part used)
     const float* inst_fwd;     // 12 per instance: world <- object
     const float* inst_s2;      // 2 per instance: squared scale (ranking), its lower bound (pruning)
@@ -1342,7 +1348,7 @@ __device__ void instance_point(const InstArgs& a, const WideNode<K>* __restrict_
     const int64_t qi = a.perm ? (int64_t)a.perm[i] : i;
     const float qx = a.queries[3 * qi], qy = a.queries[3 * qi + 1], qz = a.queries[3 * qi + 2];
     float best = INFINITY;
-    int binst = -1, brec = -1, bidx = INT_MAX;
+    int binst = -1, bidx = INT_MAX;
     // top level: closest first over instance boxes, instances walked as found
     int tsp = 0;
     tstack[tsp++] = make_float2(0.0f, __int_as_float(troot));
@@ -1380,27 +1386,38 @@ __device__ void instance_point(const InstArgs& a, const WideNode<K>* __restrict_
         const int first = leaf_first(cur), cnt = leaf_count(cur);
         for (int k = 0; k < cnt; ++k) {
             const int inst = __float_as_int(__ldg(&a.trecs[first + k].p2.y));
-            float ox, oy, oz;
-            to_object(a.inst_inv + 12 * inst, a.inst_fwd + 12 * inst, qx, qy, qz, ox, oy, oz);
-            const float s2 = a.inst_s2[2 * inst], s2lo = a.inst_s2[2 * inst + 1];
-            // object-space bound: below it lies every triangle whose world
-            // distance can beat `best` (s2lo bounds the transform's
-            // smallest squared stretch), widened for the FP32 rounding
-            float lim = best < INFINITY ? best / s2lo * (1.0f + 1e-5f) : INFINITY;
+            const int baked = a.inst_baked[inst];
             int rec = -1, idx = INT_MAX;
-            walk_mesh<K>(bnodes, a.bfast, a.brecs, a.broot[a.inst_mesh[inst]], ox, oy, oz, lim, rec,
-                           idx, bstack, a.status);
+            float d2w;
+            if (baked >= 0) {
+                // a general affine instance: its world-space copy, no transform
+                float lim = best;
+                walk_mesh<K>(static_cast<const WideNode<K>*>(a.knodes), a.kfast, nullptr, a.kroot[baked], qx, qy,
+                             qz, lim, rec, idx, bstack, a.status);
+                d2w = lim;
+            } else {
+                float ox, oy, oz;
+                to_object(a.inst_inv + 12 * inst, a.inst_fwd + 12 * inst, qx, qy, qz, ox, oy, oz);
+                const float s2 = a.inst_s2[2 * inst], s2lo = a.inst_s2[2 * inst + 1];
+                // object-space bound: below it lies every triangle whose world
+                // distance can beat `best` (s2lo bounds the transform's
+                // smallest squared stretch), widened for the FP32 rounding
+                float lim = best < INFINITY ? best / s2lo * (1.0f + 1e-5f) : INFINITY;
+                walk_mesh<K>(bnodes, a.bfast, a.brecs, a.broot[a.inst_mesh[inst]], ox, oy, oz, lim, rec, idx,
+                             bstack, a.status);
+                d2w = lim * s2;
+            }
             if (rec < 0) continue;
-            const float d2w = lim * s2;
             if (d2w < best || (d2w == best && (inst < binst || (inst == binst && idx < bidx)))) {
                 best = d2w;
                 binst = inst;
-                brec = rec;
                 bidx = idx;
             }
         }
     }
     float dist = __int_as_float(0x7fc00000), px = dist, py = dist, pz = dist, bv = dist, bw = dist;
+    // the winner's exact object-space record, whichever level found it
+    const int brec = binst >= 0 ? a.binv_order[a.btoff[a.inst_mesh[binst]] + bidx] : -1;
     if (brec >= 0) {
         const float4* rp = reinterpret_cast<const float4*>(a.brecs + brec);
         TriRec r;
@@ -1427,7 +1444,15 @@ __device__ void instance_point(const InstArgs& a, const WideNode<K>* __restrict_
         t.ac = ff3_sub(wv[2], wv[0]);
         t.ap = ff3_sub(q3, wv[0]);
         ff v, w;
-        if (__float_as_uint(r.p2.z) & kTriDegenerate) {
+        // degenerate in world space: the object triangle's flag, or the same
+        // area test on the rounded world edges (a singular matrix flattens
+        // triangles)
+        const float e1x = ff_to_float(t.ab.x), e1y = ff_to_float(t.ab.y), e1z = ff_to_float(t.ab.z);
+        const float e2x = ff_to_float(t.ac.x), e2y = ff_to_float(t.ac.y), e2z = ff_to_float(t.ac.z);
+        const float cx = e1y * e2z - e1z * e2y, cy = e1z * e2x - e1x * e2z, cz = e1x * e2y - e1y * e2x;
+        const float l1 = e1x * e1x + e1y * e1y + e1z * e1z, l2 = e2x * e2x + e2y * e2y + e2z * e2z;
+        const bool flat = !(cx * cx + cy * cy + cz * cz > 1e-10f * (l1 * l2));
+        if ((__float_as_uint(r.p2.z) & kTriDegenerate) || flat) {
             TriRec rw = r;  // degenerate: the FP32 edge search on the rounded world vertices
             rw.p0 = make_float4(ff_to_float(wv[0].x), ff_to_float(wv[0].y), ff_to_float(wv[0].z),
                                 ff_to_float(wv[1].x));
@@ -1517,6 +1542,38 @@ __global__ void k_instance_proxies(const float* __restrict__ box, const int32_t*
     tris[3 * (int64_t)i + 2] = 2 * i + 1;
 }
 
+// World-space copies of general-affine instances, one triangle per thread:
+// triangle g of the output is local triangle i of baked instance j (g =
+// out_off[j] + i), its exact record through the batch's inverse order, its
+// vertices through the instance matrix in FP64 and rounded once; the copy
+// keeps the mesh's local triangle order, so its indices are the mesh's.
+__global__ void k_bake_instances(const TriRec* __restrict__ recs, const int32_t* __restrict__ inv_order,
+                                 const int64_t* __restrict__ toff, const int32_t* __restrict__ baked_inst,
+                                 const int32_t* __restrict__ inst_mesh, const float* __restrict__ fwd,
+                                 const int64_t* __restrict__ out_off, int32_t nb, int64_t total,
+                                 float* __restrict__ verts, int32_t* __restrict__ tris) {
+    const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= total) return;
+    int lo = 0, hi = nb - 1;  // the last j with out_off[j] <= g
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (out_off[mid] <= g) lo = mid;
+        else hi = mid - 1;
+    }
+    const int64_t i = g - out_off[lo];
+    const int inst = baked_inst[lo];
+    const TriRec r = recs[inv_order[toff[inst_mesh[inst]] + i]];
+    const float* m = fwd + 12 * (int64_t)inst;
+    const float v[3][3] = {{r.p0.x, r.p0.y, r.p0.z}, {r.p0.w, r.p1.x, r.p1.y}, {r.p1.z, r.p1.w, r.p2.x}};
+    for (int k = 0; k < 3; ++k)
+        for (int c = 0; c < 3; ++c)
+            verts[9 * g + 3 * k + c] = (float)((double)m[4 * c] * v[k][0] + (double)m[4 * c + 1] * v[k][1] +
+                                               (double)m[4 * c + 2] * v[k][2] + (double)m[4 * c + 3]);
+    tris[3 * g] = (int32_t)(3 * i);
+    tris[3 * g + 1] = (int32_t)(3 * i + 1);
+    tris[3 * g + 2] = (int32_t)(3 * i + 2);
+}
+
 template <int K>
 cudaError_t launch_instances(const InstArgs& args, cudaStream_t st) {
     auto kern = k_instances<K>;
@@ -1587,7 +1644,7 @@ size_t query_workspace_bytes(const Bvh& b, int64_t nq, const QueryParams& qp) {
 
 cudaError_t order_points(const Bvh& b, const float* queries, int64_t nq, const int64_t* d_qoff,
                          bool sort, void* ws, size_t ws_bytes, cudaStream_t st, const int32_t** perm_out,
-                         unsigned long long** counter_out) {
+                         unsigned long long** counter_out, bool coarse) {
     const QueryLayout L = layout(nq, b.nmeshes, sort);
     if (ws_bytes < L.total) return cudaErrorInvalidValue;
     unsigned char* w = static_cast<unsigned char*>(ws);
@@ -1612,6 +1669,18 @@ cudaError_t order_points(const Bvh& b, const float* queries, int64_t nq, const i
         k_query_frame<<<(unsigned)((b.nmeshes + 255) / 256), 256, 0, st>>>(frame, b.nmeshes,
                                                                            (float)(1u << qbits)); note_launch();
         const int key_bits = 3 * qbits + b.mesh_bits;
+        // Coarse: only the Hilbert index's top bits are sorted, about 16
+        // points per curve segment on average, a radix pass less per 10 bits
+        // dropped.  Per-thread ray walks gain (4% on 16M rays); packets of
+        // closest-point queries lose far more (near-surface queries crowd
+        // into few segments, 35% more node visits), so they sort every bit.
+        int begin_bit = 0;
+        if (coarse) {
+            int floor_log2 = 0;
+            while ((int64_t(1) << (floor_log2 + 1)) <= nq) ++floor_log2;
+            const int keep = std::min(3 * qbits, std::max(floor_log2 - 4, std::min(3 * qbits, 12)));
+            begin_bit = 3 * qbits - keep;
+        }
         const unsigned kgrid = (unsigned)((nq + 255) / 256);
         bool in_alt = false;
         if (key_bits <= 32) {
@@ -1622,14 +1691,14 @@ cudaError_t order_points(const Bvh& b, const float* queries, int64_t nq, const i
                                                           k32, vals); note_launch();
             e = cudaGetLastError();
             if (e != cudaSuccess) return e;
-            e = radix_sort_pairs<uint32_t>(k32, vals, k32_alt, vals_alt, nq, 0, key_bits,
+            e = radix_sort_pairs<uint32_t>(k32, vals, k32_alt, vals_alt, nq, begin_bit, key_bits,
                                            w + L.sort_ws, L.sort_ws_bytes, st, &in_alt);
         } else {
             k_query_keys<uint64_t><<<kgrid, 256, 0, st>>>(queries, nq, d_qoff, b.nmeshes, frame, qbits,
                                                           keys, vals); note_launch();
             e = cudaGetLastError();
             if (e != cudaSuccess) return e;
-            e = radix_sort_pairs<uint64_t>(keys, vals, keys_alt, vals_alt, nq, 0, key_bits,
+            e = radix_sort_pairs<uint64_t>(keys, vals, keys_alt, vals_alt, nq, begin_bit, key_bits,
                                            w + L.sort_ws, L.sort_ws_bytes, st, &in_alt);
         }
         if (e != cudaSuccess) return e;
@@ -1703,13 +1772,22 @@ cudaError_t instance_proxies(const Bvh& bottom, const int32_t* inst_mesh, const 
     return cudaGetLastError();
 }
 
-cudaError_t bvh_instance_query(const Bvh& top, const Bvh& bottom, const int32_t* inst_mesh,
-                               const float* inst_inv, const float* inst_fwd, const float* inst_s2,
-                               const float* queries, int64_t nq, bool sort, float* out_point,
-                               float* out_dist, int32_t* out_inst, int32_t* out_tri, float* out_bary,
-                               void* ws, size_t ws_bytes, cudaStream_t st) {
+cudaError_t instance_bake(const Bvh& bottom, const int32_t* baked_inst, const int32_t* inst_mesh,
+                          const float* inst_fwd, const int64_t* out_off, int32_t nb, int64_t total, float* verts,
+                          int32_t* tris, cudaStream_t st) {
+    if (total <= 0) return cudaSuccess;
+    k_bake_instances<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(bottom.recs, bottom.inv_order, bottom.d_toff,
+                                                                      baked_inst, inst_mesh, inst_fwd, out_off, nb,
+                                                                      total, verts, tris);
+    note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t bvh_instance_query(const Bvh& top, const Bvh& bottom, const InstanceSet& is, const float* queries,
+                               int64_t nq, bool sort, float* out_point, float* out_dist, int32_t* out_inst,
+                               int32_t* out_tri, float* out_bary, void* ws, size_t ws_bytes, cudaStream_t st) {
     if (nq <= 0) return cudaSuccess;
-    if (top.p.K != bottom.p.K) return cudaErrorInvalidValue;
+    if (top.p.K != bottom.p.K || (is.baked_bvh && is.baked_bvh->p.K != bottom.p.K)) return cudaErrorInvalidValue;
     InstArgs a;
     cudaError_t e = order_points(top, queries, nq, nullptr, sort, ws, ws_bytes, st, &a.perm, &a.counter);
     if (e != cudaSuccess) return e;
@@ -1720,10 +1798,16 @@ cudaError_t bvh_instance_query(const Bvh& top, const Bvh& bottom, const int32_t*
     a.bfast = bottom.fast;
     a.brecs = bottom.recs;
     a.broot = bottom.wide_root;
-    a.inst_mesh = inst_mesh;
-    a.inst_inv = inst_inv;
-    a.inst_fwd = inst_fwd;
-    a.inst_s2 = inst_s2;
+    a.binv_order = bottom.inv_order;
+    a.btoff = bottom.d_toff;
+    a.knodes = is.baked_bvh ? is.baked_bvh->nodes : nullptr;
+    a.kfast = is.baked_bvh ? is.baked_bvh->fast : nullptr;
+    a.kroot = is.baked_bvh ? is.baked_bvh->wide_root : nullptr;
+    a.inst_mesh = is.mesh;
+    a.inst_baked = is.baked;
+    a.inst_inv = is.inv;
+    a.inst_fwd = is.fwd;
+    a.inst_s2 = is.s2;
     a.queries = queries;
     a.nq = nq;
     a.out_point = out_point;

@@ -254,7 +254,8 @@ cudaError_t bvh_ray_query(const Bvh& b, const float* orig, const float* dir, con
                           int32_t* out_tri, float* out_uv, void* ws, size_t ws_bytes, cudaStream_t st) {
     if (n <= 0) return cudaSuccess;
     RayArgs args;
-    cudaError_t e = order_points(b, orig, n, d_off, rp.sort != 0, ws, ws_bytes, st, &args.perm, &args.counter);
+    cudaError_t e = order_points(b, orig, n, d_off, rp.sort != 0, ws, ws_bytes, st, &args.perm, &args.counter,
+                                 /*coarse=*/true);
     if (e != cudaSuccess) return e;
     args.nodes = b.nodes;
     args.recs = b.recs;

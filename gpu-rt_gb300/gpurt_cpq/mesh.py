@@ -353,7 +353,7 @@ def _transforms(transforms) -> np.ndarray:
 
 
 class Scene:
-    """Instances of a batch's meshes placed by similarity transforms
+    """Instances of a batch's meshes placed by affine transforms
     (cp_scene_create); queries are in world space.  Keeps the batch alive."""
 
     def __init__(self, batch: Batch, instance_mesh, transforms, *, stream=None):

@@ -412,17 +412,18 @@ CP_API cp_status cp_batch_query(cp_batch* batch, const float* queries, const int
  * (Accel::recreate(blas, T), src/vk/vulkan.cpp:777-856; one model matrix per
  * object, src/rt/rt.cpp:31-45).  A top-level BVH over the instances' world
  * boxes is built on the device; a query walks it closest first and each
- * instance's mesh BVH in object space, and the winner is re-evaluated in
- * float-float in world space.
+ * instance's mesh BVH, and the winner is re-evaluated in float-float in world
+ * space from the exact object-space triangle and the instance matrix.
  *   batch               the meshes; it must outlive the scene
  *   instance_mesh       HOST array, n_instances mesh ids in [0, nmeshes)
  *   instance_transform  HOST array, n_instances x 12 floats, row-major 3 x 4
- *                       [R | t] taking object to world coordinates
- * Transforms must be similarities (rotation or reflection, uniform scale,
- * translation): M^T M = s^2 I within 1e-5 s^2 per entry, else
- * CP_ERROR_INVALID_VALUE.  Distances and points are in world units; the
- * accuracy bound of cp_query holds for transforms that are similarities to
- * FP32 rounding; a deviation d from one adds up to about d/2 of the distance.
+ *                       [M | t] taking object to world coordinates
+ * Any finite affine matrix is accepted (non-finite: CP_ERROR_INVALID_VALUE).
+ * Similarities (rotation or reflection, uniform scale, translation: M^T M =
+ * s^2 I within 1e-5 s^2) share the batch mesh's BVH, walked in object space;
+ * any other matrix (non-uniform scale, shear, singular) gets a world-space
+ * copy of its mesh with its own BVH, built here, whose triangles keep the
+ * mesh's local indices.  Distances and points are in world units.
  * Synchronises `stream`.
  */
 CP_API cp_status cp_scene_create(const cp_batch* batch, const int32_t* instance_mesh,
@@ -431,7 +432,8 @@ CP_API cp_status cp_scene_create(const cp_batch* batch, const int32_t* instance_
 
 /*
  * New transforms for every instance (same meshes): re-derives the instance
- * frames and rebuilds the top level.  Synchronises `stream`.
+ * frames, rebuilds the world-space copies and the top level.  Synchronises
+ * `stream`.
  */
 CP_API cp_status cp_scene_update(cp_scene* scene, const float* instance_transform, cp_stream_t stream);
 

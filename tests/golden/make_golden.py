@@ -16,6 +16,12 @@ Run from the repository root:  python tests/golden/make_golden.py
 3. small_sample.npz — FP64 brute-force answers for the first 4,096 queries of
    the small workload (icosphere level 4, queries U[-2,2]^3, seed 0), and the
    exact bytes of its vertex array, as a cross-platform regression anchor.
+4. cbox_scene.npz — the reference's media/cbox/cbox.gltf as instances: its 9
+   triangle primitives (16,720 triangles, mesh space), one instance per
+   (node, primitive) with the node's world matrix (glTF matrix or TRS,
+   composed down the node tree, rounded to FP32 3 x 4), seeded queries and
+   their FP64 brute-force answers over the world-space vertices (the FP32
+   matrix applied to the FP32 vertex in FP64).  Needs the reference checkout.
 """
 from __future__ import annotations
 
@@ -113,6 +119,89 @@ def _gltf_meshes(path: Path):
     return meshes
 
 
+def _gltf_instances(path: Path):
+    """One (primitive index, 4 x 4 world matrix) per node primitive, depth-first
+    from the default scene's roots; primitives numbered as _gltf_meshes
+    returns them (triangle lists in file order)."""
+    g = json.loads(path.read_text())
+    first, k = [], 0
+    for m in g["meshes"]:
+        first.append(k)
+        k += sum(1 for p in m["primitives"] if p.get("mode", 4) == 4)
+
+    def local(n):
+        if "matrix" in n:
+            return np.array(n["matrix"], np.float64).reshape(4, 4).T  # column-major
+        t = np.array(n.get("translation", [0, 0, 0]), np.float64)
+        x, y, z, w = n.get("rotation", [0, 0, 0, 1])
+        s = np.array(n.get("scale", [1, 1, 1]), np.float64)
+        R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                      [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                      [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+        M = np.eye(4)
+        M[:3, :3] = R * s[None, :]
+        M[:3, 3] = t
+        return M
+
+    out = []
+
+    def visit(i, parent):
+        n = g["nodes"][i]
+        W = parent @ local(n)
+        if "mesh" in n:
+            j = first[n["mesh"]]
+            for p in g["meshes"][n["mesh"]]["primitives"]:
+                if p.get("mode", 4) == 4:
+                    out.append((j, W))
+                    j += 1
+        for c in n.get("children", []):
+            visit(c, W)
+
+    for r in g["scenes"][g.get("scene", 0)]["nodes"]:
+        visit(r, np.eye(4))
+    return out
+
+
+def write_cbox_scene(ref_root: Path):
+    from oracle import oracle as O
+
+    path = ref_root / "media" / "cbox" / "cbox.gltf"
+    meshes = _gltf_meshes(path)
+    inst = _gltf_instances(path)
+    prim = np.array([j for j, _ in inst], np.int32)
+    T = np.stack([W[:3, :4] for _, W in inst]).astype(np.float32)
+    wv, wt, off = [], [], 0
+    for j, t in zip(prim, T):
+        v, tri = meshes[j]
+        t64 = t.astype(np.float64)
+        wv.append(v.astype(np.float64) @ t64[:, :3].T + t64[:, 3])
+        wt.append(tri + off)
+        off += len(v)
+    wv, wt = np.concatenate(wv), np.concatenate(wt).astype(np.int32)
+    rng = np.random.default_rng(11)
+    lo, hi = wv.min(0), wv.max(0)
+    c, h = 0.5 * (lo + hi), 0.6 * (hi - lo)
+    far = c - h + 2 * h * rng.random((4096, 3))
+    k = rng.integers(0, len(wt), 2048)
+    r1, r2 = np.sqrt(rng.random(2048)), rng.random(2048)
+    a, b, cc = (wv[wt[k, j]] for j in range(3))
+    near = (1 - r1)[:, None] * a + (r1 * (1 - r2))[:, None] * b + (r1 * r2)[:, None] * cc
+    near += rng.normal(0.0, 0.01, near.shape)
+    q = np.concatenate([far, near]).astype(np.float32)
+    bf = O.brute_f64_dv(wv, wt, q)
+    ntri = np.array([len(meshes[j][1]) for j in prim])
+    toff_i = np.concatenate([[0], np.cumsum(ntri)])
+    inst_of = np.searchsorted(toff_i, bf["tri"], side="right") - 1
+    V = np.concatenate([m[0] for m in meshes])
+    TT = np.concatenate([m[1] for m in meshes])
+    voff = np.concatenate([[0], np.cumsum([len(m[0]) for m in meshes])]).astype(np.int64)
+    toff = np.concatenate([[0], np.cumsum([len(m[1]) for m in meshes])]).astype(np.int64)
+    np.savez_compressed(HERE / "cbox_scene.npz", verts=V, tris=TT, vert_offsets=voff, tri_offsets=toff,
+                        instance_primitive=prim, instance_transform=T, queries=q, dist=bf["dist"],
+                        instance=inst_of.astype(np.int32), tri=(bf["tri"] - toff_i[inst_of]).astype(np.int32),
+                        source=np.array(str(path.relative_to(ref_root))))
+
+
 def write_ref_meshes(ref_root: Path):
     from oracle import oracle as O
 
@@ -153,6 +242,7 @@ if __name__ == "__main__":
     ref = Path(os.environ.get("REFERENCE_ROOT", "/root/reference"))
     if (ref / "media" / "cube.gltf").exists():
         write_ref_meshes(ref)
+        write_cbox_scene(ref)
     else:
         print("reference checkout not found; ref_meshes.npz left as committed")
     write_small_sample()

@@ -31,6 +31,23 @@ def test_reference_scenes_match_fixture(cpq):
     assert len(scenes[0].instance_primitive) == 1  # the cube node; light and camera have no mesh
 
 
+def test_cbox_reader_matches_fixture(cpq):
+    """The reference's Cornell box: primitives and node instances as the
+    fixture's independent Python reader (tests/golden/make_golden.py) made
+    them."""
+    path = REF_MEDIA / "cbox" / "cbox.gltf"
+    if not path.exists():
+        pytest.skip("reference media not present")
+    g = np.load(GOLDEN / "cbox_scene.npz")
+    s = cpq.load_gltf(str(path))
+    np.testing.assert_array_equal(s.verts, g["verts"])
+    np.testing.assert_array_equal(s.tris, g["tris"])
+    np.testing.assert_array_equal(s.vert_offsets, g["vert_offsets"])
+    np.testing.assert_array_equal(s.tri_offsets, g["tri_offsets"])
+    np.testing.assert_array_equal(s.instance_primitive, g["instance_primitive"])
+    np.testing.assert_array_equal(s.instance_world[:, :3, :].astype(np.float32), g["instance_transform"])
+
+
 def _write(tmp: Path, doc: dict, bin_data: bytes, mode: str) -> Path:
     """mode: "data" (base64 URI), "file" (external .bin) or "glb"."""
     doc = json.loads(json.dumps(doc))
