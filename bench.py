@@ -59,6 +59,17 @@ CANON_V_TRI = 44.413
 # capture summarised in profiles/k_traverse_packet_large_heightfield.md
 # (4.220 + 1.714 GB for 16,777,216 queries, leaf 8)
 NCU_TRAFFIC_PER_QUERY = 353.7
+# Adjoint per query: reads q 12 + triangle 4 + barycentrics 8 + upstream
+# gradient 4 + 3 vertex indices 12 + 3 vertices 36; writes d/dq 12 and three
+# atomic read-modify-writes of 12 B to d/dvertices (72)
+BWD_BYTES_PER_QUERY = 160
+# Build per triangle (algorithmic): validation 48 (indices + vertex gather),
+# centroid bounds 48, Morton keys 60 (gather + key and index out), 7 radix
+# passes of 64-bit keys with an index 224 (histogram read 8, scatter 12 in and
+# 12 out), Karras nodes 28 (key reads, three child/parent words out), refit
+# 252 (gather 48, exact and test records out 48 + 80, box 24, inverse order 4,
+# child boxes in and box out per inner node 48)
+BUILD_BYTES_PER_TRI = 660
 
 
 def parse():
@@ -404,6 +415,12 @@ def our_arm(args):
                           "block_size": qopts.block_size, "short_stack": qopts.short_stack,
                           "sort_queries": bool(qopts.sort_queries),
                           "wide_nodes": info.num_wide_nodes, "build_ms": info.build_ms,
+                          "build_roofline": {
+                              "bytes_per_triangle": BUILD_BYTES_PER_TRI,
+                              "achieved_gbs": BUILD_BYTES_PER_TRI * info.num_triangles / (info.build_ms * 1e-3) / 1e9
+                              if info.build_ms > 0 else None,
+                              "frac_of_hbm": BUILD_BYTES_PER_TRI * info.num_triangles / (info.build_ms * 1e-3) / 1e9
+                              / measured_peaks()["hbm_gbs"] if info.build_ms > 0 else None},
                           "l2": f"inputs larger than L2 ({nq * 12 / 1e6:.0f} MB queries + "
                                 f"{nq * 20 / 1e6:.0f} MB outputs + {traversal_mb:.0f} MB of nodes and "
                                 "triangle records per step); no flush",
@@ -470,12 +487,23 @@ def torus_arm(args):
 
     ms_f = _timed(torch, fwd, args.steps, args.warmup)
     ms_fb = _timed(torch, fwd_bwd, args.steps, args.warmup)
+
+    def bwd():
+        gv.zero_()
+        mesh.backward(qd, out.tri, out.bary, gd, grad_verts=gv)
+
+    ms_b = _timed(torch, bwd, args.steps, args.warmup)
+    bwd_gbs = BWD_BYTES_PER_QUERY * nq / (ms_b * 1e-3) / 1e9
     _line("closest-point fwd+bwd queries/s (torus 200k tris, 4M queries)", nq / (ms_fb * 1e-3),
           "queries/s", ms_fb, args,
           {"workload": "torus R=1 r=0.3 500x200 (200,000 tris), 4,194,304 queries U[-1.5,1.5]^3, "
                        "upstream gradient N(0,1); forward caches (tri, bary), adjoint recomputes",
            "branching": 4, "leaf_size": 2},
           {"forward_only": {"value": nq / (ms_f * 1e-3), "ms_per_step": ms_f},
+           "backward_only": {"value": nq / (ms_b * 1e-3), "ms_per_step": ms_b,
+                             "roofline": {"bound": "hbm", "achieved": bwd_gbs, "peak": measured_peaks()["hbm_gbs"],
+                                          "unit": "GB/s", "frac": bwd_gbs / measured_peaks()["hbm_gbs"],
+                                          "of": "measured", "bytes_per_query": BWD_BYTES_PER_QUERY}},
            "fwd_bwd_over_fwd": ms_fb / ms_f, "target_fwd_bwd_over_fwd": 2.5})
 
 

@@ -6,7 +6,10 @@
 //   exclusive scan of that array: the global start of (digit d, tile t);
 //   k_scatter      ranks the tile's keys, stages them in shared memory in
 //                  digit order and writes digit runs out contiguously.
-// A tile is 256 threads x IT keys (IT = 16 for 32-bit keys, 8 for 64-bit).
+// A tile is 256 threads x IT keys (IT = 32 for 32-bit keys, 8 for 64-bit):
+// with 1024 digits, an 8192-key tile writes runs of 8 keys (a full 32-byte
+// sector) where a 4096-key tile wrote half sectors — the ordering of 16M
+// queries took 1.24 ms instead of 1.50 (48 keys per thread: 1.34).
 // Ranking needs no block-wide barrier per round: warp w owns the tile's keys
 // [w*32*IT, (w+1)*32*IT) and ranks them round by round (32 consecutive keys,
 // lanes in order) against its own digit counters — match_any groups equal
@@ -32,7 +35,7 @@ constexpr int kScanChunk = kScanThreads * kScanItems;
 
 template <typename KeyT>
 constexpr int items_per_thread() {
-    return sizeof(KeyT) == 4 ? 16 : 8;
+    return sizeof(KeyT) == 4 ? 32 : 8;
 }
 template <typename KeyT>
 constexpr int tile_keys() {
