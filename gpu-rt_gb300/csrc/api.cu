@@ -741,6 +741,7 @@ struct cp_scene {
     Bvh top;                    // over the instances' proxies, one per instance
     Bvh baked;                  // world-space copies of the general-affine instances
     bool has_baked = false;
+    bool valid = false;         // false while a build is under way or after one failed
     const cp_batch* batch = nullptr;
     int32_t n = 0;
     int32_t n_baked = 0;
@@ -822,7 +823,8 @@ cp_status scene_build(cp_scene* sc, const float* T, cudaStream_t st) {
     std::vector<float> fwd, inv, s2;
     std::vector<int32_t> baked;
     cp_status s = instance_frames(T, sc->n, fwd, inv, s2, baked);
-    if (s != CP_SUCCESS) return s;
+    if (s != CP_SUCCESS) return s;  // nothing changed: the scene stays as it was
+    sc->valid = false;              // from here on a failure leaves it unusable
     const size_t n = (size_t)sc->n;
     const Bvh& bottom = sc->batch->bvh;
     CP_CUDA(cudaMemcpyAsync(sc->d_fwd, fwd.data(), sizeof(float) * 12 * n, cudaMemcpyHostToDevice, st), "scene upload");
@@ -908,6 +910,7 @@ cp_status scene_build(cp_scene* sc, const float* T, cudaStream_t st) {
     if (e != cudaSuccess) return cuda_fail(e, "scene proxies");
     if (s != CP_SUCCESS) return s;
     if (e2 != cudaSuccess) return cuda_fail(e2, "scene build");
+    sc->valid = true;
     return CP_SUCCESS;
 }
 
@@ -993,6 +996,7 @@ CP_API cp_status cp_scene_query(const cp_scene* scene, const float* queries, int
                                 int32_t* out_instance, int32_t* out_tri, float* out_bary,
                                 void* workspace, size_t ws_bytes, cp_stream_t stream) {
     if (!scene) return fail(CP_ERROR_INVALID_VALUE, "scene is NULL");
+    if (!scene->valid) return fail(CP_ERROR_INVALID_VALUE, "scene unusable: its last update failed");
     if (nq < 0) return fail(CP_ERROR_INVALID_VALUE, "negative query count");
     if (nq > INT32_MAX) return fail(CP_ERROR_NOT_SUPPORTED, "more than 2^31 - 1 queries in one call");
     if (nq == 0) return CP_SUCCESS;

@@ -61,7 +61,7 @@ typedef enum cp_status {
     CP_ERROR_OUT_OF_MEMORY = 2,   /* a device or host allocation failed */
     CP_ERROR_CUDA = 3,            /* a CUDA runtime call failed */
     CP_ERROR_DEVICE_FAULT = 4,    /* a kernel reported an error through its status word */
-    CP_ERROR_NOT_SUPPORTED = 5,   /* no GPU, or an option this build does not support */
+    CP_ERROR_NOT_SUPPORTED = 5,   /* no GPU, or an option the library does not support */
     CP_ERROR_SCRATCH_TOO_SMALL = 6 /* a workspace or fixed scratch area is too small */
 } cp_status;
 
@@ -433,7 +433,9 @@ CP_API cp_status cp_scene_create(const cp_batch* batch, const int32_t* instance_
 /*
  * New transforms for every instance (same meshes): re-derives the instance
  * frames, rebuilds the world-space copies and the top level.  Synchronises
- * `stream`.
+ * `stream`.  A non-finite matrix is refused with the scene unchanged; a
+ * failure after that (out of memory) leaves the scene unusable until an
+ * update succeeds (cp_scene_query then returns CP_ERROR_INVALID_VALUE).
  */
 CP_API cp_status cp_scene_update(cp_scene* scene, const float* instance_transform, cp_stream_t stream);
 
