@@ -1340,81 +1340,10 @@ __device__ void walk_mesh(const WideNode<K>* __restrict__ nodes, const FastTri* 
     }
 }
 
-// One query of the two-level walk (index i in the work order).
-template <int K>
-__device__ void instance_point(const InstArgs& a, const WideNode<K>* __restrict__ tnodes,
-                               const WideNode<K>* __restrict__ bnodes, int32_t troot, int64_t i,
-                               float2* tstack, float2* bstack) {
-    const int64_t qi = a.perm ? (int64_t)a.perm[i] : i;
-    const float qx = a.queries[3 * qi], qy = a.queries[3 * qi + 1], qz = a.queries[3 * qi + 2];
-    float best = INFINITY;
-    int binst = -1, bidx = INT_MAX;
-    // top level: closest first over instance boxes, instances walked as found
-    int tsp = 0;
-    tstack[tsp++] = make_float2(0.0f, __int_as_float(troot));
-    while (tsp > 0) {
-        const float2 e = tstack[--tsp];
-        if (!(e.x < best)) continue;
-        const int cur = __float_as_int(e.y);
-        if (cur >= 0) {
-            const WideNode<K>* nd = tnodes + cur;
-            float lox[K], hix[K], loy[K], hiy[K], loz[K], hiz[K];
-            int32_t ch[K];
-            load_row<K>(nd->lox, lox);
-            load_row<K>(nd->hix, hix);
-            load_row<K>(nd->loy, loy);
-            load_row<K>(nd->hiy, hiy);
-            load_row<K>(nd->loz, loz);
-            load_row<K>(nd->hiz, hiz);
-            load_row_i<K>(nd->child, ch);
-            float lb[K];
-#pragma unroll
-            for (int s = 0; s < K; ++s) {
-                const float d = box_lb2(qx, qy, qz, lox[s], hix[s], loy[s], hiy[s], loz[s], hiz[s]);
-                lb[s] = d < best ? d : INFINITY;
-            }
-            sort_children<K>(lb, ch);
-#pragma unroll
-            for (int s = K - 1; s >= 0; --s) {
-                if (lb[s] < INFINITY) {
-                    if (tsp < kStackTotal) tstack[tsp++] = make_float2(lb[s], __int_as_float(ch[s]));
-                    else atomicOr(a.status, 1u);
-                }
-            }
-            continue;
-        }
-        const int first = leaf_first(cur), cnt = leaf_count(cur);
-        for (int k = 0; k < cnt; ++k) {
-            const int inst = __float_as_int(__ldg(&a.trecs[first + k].p2.y));
-            const int baked = a.inst_baked[inst];
-            int rec = -1, idx = INT_MAX;
-            float d2w;
-            if (baked >= 0) {
-                // a general affine instance: its world-space copy, no transform
-                float lim = best;
-                walk_mesh<K>(static_cast<const WideNode<K>*>(a.knodes), a.kfast, nullptr, a.kroot[baked], qx, qy,
-                             qz, lim, rec, idx, bstack, a.status);
-                d2w = lim;
-            } else {
-                float ox, oy, oz;
-                to_object(a.inst_inv + 12 * inst, a.inst_fwd + 12 * inst, qx, qy, qz, ox, oy, oz);
-                const float s2 = a.inst_s2[2 * inst], s2lo = a.inst_s2[2 * inst + 1];
-                // object-space bound: below it lies every triangle whose world
-                // distance can beat `best` (s2lo bounds the transform's
-                // smallest squared stretch), widened for the FP32 rounding
-                float lim = best < INFINITY ? best / s2lo * (1.0f + 1e-5f) : INFINITY;
-                walk_mesh<K>(bnodes, a.bfast, a.brecs, a.broot[a.inst_mesh[inst]], ox, oy, oz, lim, rec, idx,
-                             bstack, a.status);
-                d2w = lim * s2;
-            }
-            if (rec < 0) continue;
-            if (d2w < best || (d2w == best && (inst < binst || (inst == binst && idx < bidx)))) {
-                best = d2w;
-                binst = inst;
-                bidx = idx;
-            }
-        }
-    }
+// The winner of an instanced query, finished in world space from its exact
+// object-space record (any walk: per thread or packet), and the outputs.
+__device__ void instance_finish(const InstArgs& a, int64_t qi, float qx, float qy, float qz, int binst,
+                                int bidx) {
     float dist = __int_as_float(0x7fc00000), px = dist, py = dist, pz = dist, bv = dist, bw = dist;
     // the winner's exact object-space record, whichever level found it
     const int brec = binst >= 0 ? a.binv_order[a.btoff[a.inst_mesh[binst]] + bidx] : -1;
@@ -1491,6 +1420,84 @@ __device__ void instance_point(const InstArgs& a, const WideNode<K>* __restrict_
     }
 }
 
+// One query of the two-level walk (index i in the work order).
+template <int K>
+__device__ void instance_point(const InstArgs& a, const WideNode<K>* __restrict__ tnodes,
+                               const WideNode<K>* __restrict__ bnodes, int32_t troot, int64_t i,
+                               float2* tstack, float2* bstack) {
+    const int64_t qi = a.perm ? (int64_t)a.perm[i] : i;
+    const float qx = a.queries[3 * qi], qy = a.queries[3 * qi + 1], qz = a.queries[3 * qi + 2];
+    float best = INFINITY;
+    int binst = -1, bidx = INT_MAX;
+    // top level: closest first over instance boxes, instances walked as found
+    int tsp = 0;
+    tstack[tsp++] = make_float2(0.0f, __int_as_float(troot));
+    while (tsp > 0) {
+        const float2 e = tstack[--tsp];
+        if (!(e.x < best)) continue;
+        const int cur = __float_as_int(e.y);
+        if (cur >= 0) {
+            const WideNode<K>* nd = tnodes + cur;
+            float lox[K], hix[K], loy[K], hiy[K], loz[K], hiz[K];
+            int32_t ch[K];
+            load_row<K>(nd->lox, lox);
+            load_row<K>(nd->hix, hix);
+            load_row<K>(nd->loy, loy);
+            load_row<K>(nd->hiy, hiy);
+            load_row<K>(nd->loz, loz);
+            load_row<K>(nd->hiz, hiz);
+            load_row_i<K>(nd->child, ch);
+            float lb[K];
+#pragma unroll
+            for (int s = 0; s < K; ++s) {
+                const float d = box_lb2(qx, qy, qz, lox[s], hix[s], loy[s], hiy[s], loz[s], hiz[s]);
+                lb[s] = d < best ? d : INFINITY;
+            }
+            sort_children<K>(lb, ch);
+#pragma unroll
+            for (int s = K - 1; s >= 0; --s) {
+                if (lb[s] < INFINITY) {
+                    if (tsp < kStackTotal) tstack[tsp++] = make_float2(lb[s], __int_as_float(ch[s]));
+                    else atomicOr(a.status, 1u);
+                }
+            }
+            continue;
+        }
+        const int first = leaf_first(cur), cnt = leaf_count(cur);
+        for (int k = 0; k < cnt; ++k) {
+            const int inst = __float_as_int(__ldg(&a.trecs[first + k].p2.y));
+            const int baked = a.inst_baked[inst];
+            int rec = -1, idx = INT_MAX;
+            float d2w;
+            if (baked >= 0) {
+                // a general affine instance: its world-space copy, no transform
+                float lim = best;
+                walk_mesh<K>(static_cast<const WideNode<K>*>(a.knodes), a.kfast, nullptr, a.kroot[baked], qx, qy,
+                             qz, lim, rec, idx, bstack, a.status);
+                d2w = lim;
+            } else {
+                float ox, oy, oz;
+                to_object(a.inst_inv + 12 * inst, a.inst_fwd + 12 * inst, qx, qy, qz, ox, oy, oz);
+                const float s2 = a.inst_s2[2 * inst], s2lo = a.inst_s2[2 * inst + 1];
+                // object-space bound: below it lies every triangle whose world
+                // distance can beat `best` (s2lo bounds the transform's
+                // smallest squared stretch), widened for the FP32 rounding
+                float lim = best < INFINITY ? best / s2lo * (1.0f + 1e-5f) : INFINITY;
+                walk_mesh<K>(bnodes, a.bfast, a.brecs, a.broot[a.inst_mesh[inst]], ox, oy, oz, lim, rec, idx,
+                             bstack, a.status);
+                d2w = lim * s2;
+            }
+            if (rec < 0) continue;
+            if (d2w < best || (d2w == best && (inst < binst || (inst == binst && idx < bidx)))) {
+                best = d2w;
+                binst = inst;
+                bidx = idx;
+            }
+        }
+    }
+    instance_finish(a, qi, qx, qy, qz, binst, bidx);
+}
+
 template <int K>
 __global__ void __launch_bounds__(128) k_instances(InstArgs a) {
     const int lane = threadIdx.x & 31;
@@ -1507,6 +1514,254 @@ __global__ void __launch_bounds__(128) k_instances(InstArgs a) {
         const int64_t i = (int64_t)base + lane;
         if (i < a.nq) instance_point<K>(a, tnodes, bnodes, troot, i, tstack, bstack);
     }
+}
+
+// ---- instances: packet walk ---------------------------------------------------
+//
+// The warp-packet traversal of k_traverse_packet as a device function over
+// any wide BVH: per-lane query and bound, one shared stack entry per level in
+// `stk` (packet_stack_bytes(K, cap)), the packet descending first into the
+// child nearest to any lane.  Leaves go to `leaf(first, count, admitted,
+// lim)`, which tests them for the lanes its bound admitted and lowers `lim`.
+// Lanes that take no part enter with lim = -inf.  The scene kernel nests it:
+// at the top level a leaf is an instance, whose handler runs the same walk
+// over that instance's mesh with the lanes' object-space queries.
+template <int K, class Leaf>
+__device__ __forceinline__ void packet_walk(const WideNode<K>* __restrict__ nodes, int32_t root, float qx, float qy,
+                                            float qz, bool active, float& lim, unsigned char* stk, int cap,
+                                            uint32_t* status, Leaf& leaf) {
+    const int lane = threadIdx.x & 31;
+    const bool lane0 = lane == 0;
+    float* st_bnd = reinterpret_cast<float*>(stk) + lane * K;  // entry e, slot s at [e * 32 * K + s]
+    int32_t* st_ch = reinterpret_cast<int32_t*>(stk + (size_t)cap * 128 * K);
+    uint2* st_state = reinterpret_cast<uint2*>(stk + (size_t)cap * 132 * K);
+    const f32x2 qx2 = f2_pack(qx, qx), qy2 = f2_pack(qy, qy), qz2 = f2_pack(qz, qz);
+    int sp = 0;
+    uint32_t t_order = 0;
+    int t_cnt = 0;
+    int cur = root;
+    bool leaf_active = active;
+    for (;;) {
+        if (cur >= 0) {
+            const WideNode<K>* nd = nodes + cur;
+            f32x2 lox[K / 2], hix[K / 2], loy[K / 2], hiy[K / 2], loz[K / 2], hiz[K / 2];
+            int32_t ch[K];
+            load_row2<K>(nd->lox, lox);
+            load_row2<K>(nd->hix, hix);
+            load_row2<K>(nd->loy, loy);
+            load_row2<K>(nd->hiy, hiy);
+            load_row2<K>(nd->loz, loz);
+            load_row2<K>(nd->hiz, hiz);
+            load_row_i<K>(nd->child, ch);
+            float lb[K];
+#pragma unroll
+            for (int j = 0; j < K / 2; ++j) {
+                const f32x2 dx = box_axis2(qx2, lox[j], hix[j]);
+                const f32x2 dy = box_axis2(qy2, loy[j], hiy[j]);
+                const f32x2 dz = box_axis2(qz2, loz[j], hiz[j]);
+                f2_unpack(f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx))), lb[2 * j], lb[2 * j + 1]);
+            }
+            uint32_t mine_need = 0, kmine = 0xFFFFFFFFu;
+#pragma unroll
+            for (int s = 0; s < K; ++s) {
+                const bool want = lb[s] < lim;
+                mine_need |= (want ? 1u : 0u) << s;
+                kmine = min(kmine, want ? ((__float_as_uint(lb[s]) & 0x7FFFFFF8u) | (uint32_t)s) : 0xFFFFFFFFu);
+            }
+            const uint32_t need = __reduce_or_sync(kFull, mine_need);
+            if (need != 0) {
+                const int f = (int)(__reduce_min_sync(kFull, kmine) & 7u);
+                const uint32_t rest = need & ~(1u << f);
+                if (rest != 0) {
+                    if (sp > 0) {
+                        if (t_cnt == 0) --sp;
+                        else if (lane0) st_state[sp - 1] = make_uint2(t_order, (uint32_t)t_cnt);
+                    }
+                    if (sp >= cap) {  // cannot happen: cap bounds the depth
+                        atomicOr(status, 1u);
+                        sp = cap - 1;
+                    }
+                    store_row<K>(st_bnd + sp * 32 * K, lb);
+                    if (lane0) store_row<K>(st_ch + sp * K, ch);
+                    t_order = c_slot_lists.v[rest];
+                    t_cnt = __popc(rest);
+                    ++sp;
+                    __syncwarp();
+                }
+                int32_t cf = ch[0];
+#pragma unroll
+                for (int s = 1; s < K; ++s) cf = f == s ? ch[s] : cf;
+                cur = cf;
+                leaf_active = (mine_need >> f) & 1u;
+                continue;
+            }
+        } else {
+            leaf(leaf_first(cur), leaf_count(cur), leaf_active, lim);
+        }
+        bool found = false;
+        for (;;) {
+            if (t_cnt == 0) {
+                if (sp <= 1) break;
+                --sp;
+                const uint2 s2 = st_state[sp - 1];
+                t_order = s2.x;
+                t_cnt = (int)s2.y;
+                continue;
+            }
+            const int s = (int)(t_order & 15u);
+            t_order >>= 4;
+            --t_cnt;
+            const int e = sp - 1;
+            const bool want = st_bnd[e * 32 * K + s] < lim;
+            if (__any_sync(kFull, want)) {
+                cur = st_ch[e * K + s];
+                leaf_active = want;
+                found = true;
+                break;
+            }
+        }
+        __syncwarp();
+        if (!found) break;
+    }
+}
+
+__host__ __device__ constexpr size_t scene_warp_bytes(int K, int cap_t, int cap_b) {
+    return packet_stack_bytes(K, cap_t) + packet_stack_bytes(K, cap_b) + 32 * sizeof(float4);
+}
+
+template <int K>
+__global__ void __launch_bounds__(128) k_instances_packet(InstArgs a, int cap_t, int cap_b) {
+    extern __shared__ __align__(16) unsigned char s_sc[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned char* stk_t = s_sc + (size_t)warp * scene_warp_bytes(K, cap_t, cap_b);
+    unsigned char* stk_b = stk_t + packet_stack_bytes(K, cap_t);
+    float4* st_q = reinterpret_cast<float4*>(stk_b + packet_stack_bytes(K, cap_b));
+    const uint32_t lt_mask = lanemask_lt();
+    const WideNode<K>* __restrict__ tnodes = static_cast<const WideNode<K>*>(a.tnodes);
+    const int32_t troot = __ldg(a.troot);
+    for (;;) {
+        unsigned long long base = 0;
+        if (lane == 0) base = atomicAdd(a.counter, 32ull);
+        base = __shfl_sync(kFull, base, 0);
+        if (base >= (unsigned long long)a.nq) break;
+        const int64_t i = (int64_t)base + lane;
+        const bool valid = i < a.nq;
+        int64_t qi = 0;
+        float qx = 0.f, qy = 0.f, qz = 0.f;
+        if (valid) {
+            qi = a.perm ? (int64_t)a.perm[i] : i;
+            qx = a.queries[3 * qi];
+            qy = a.queries[3 * qi + 1];
+            qz = a.queries[3 * qi + 2];
+        }
+        // world best: squared distance, then (instance, triangle) for ties
+        float best = INFINITY;
+        int binst = -1, bidx = INT_MAX;
+        // the instance being walked: this lane's object-space query and key
+        float ox = 0.f, oy = 0.f, oz = 0.f;
+        unsigned long long okey = kNoKey;
+        const FastTri* mfast = nullptr;
+        auto mesh_leaf = [&](int first, int cnt, bool admitted, float& lim) {
+            const uint32_t act = __ballot_sync(kFull, admitted);
+            const int na = __popc(act);
+            if (cnt >= 2 && na >= 1 && na <= 16) {
+                // (query, triangle) pairs spread over the warp, as in k_traverse_packet
+                const LeafSplit sp2 = c_leaf_splits.v[na];
+                const int r = __popc(act & lt_mask);
+                if (admitted) st_q[r] = make_float4(ox, oy, oz, 0.0f);
+                __syncwarp();
+                const int kk = (int)(((float)lane + 0.5f) * sp2.inv);
+                const bool worker = lane < sp2.kpr * na;
+                const float4 qq = st_q[worker ? lane - kk * na : 0];
+                unsigned long long key = kNoKey;
+                for (int k0 = 0; k0 < cnt; k0 += sp2.kpr) {
+                    const int k = k0 + kk;
+                    if (worker && k < cnt) {
+                        const FastTri f = load_fast(mfast + first + k);
+                        key = min(key, best_key(tri_d2_fast(qq.x, qq.y, qq.z, f), fast_index(f)));
+                    }
+                }
+                const int nk = min(sp2.kpr, cnt);
+                for (int j = 0; j < nk; ++j) {
+                    const unsigned long long got = __shfl_sync(kFull, key, (r + j * na) & 31);
+                    if (admitted) okey = min(okey, got);
+                }
+                __syncwarp();  // st_q is read before the next leaf writes it
+            } else {
+                for (int k = 0; k < cnt; ++k) {
+                    const FastTri f = load_fast(mfast + first + k);
+                    if (admitted) okey = min(okey, best_key(tri_d2_fast(ox, oy, oz, f), fast_index(f)));
+                }
+            }
+            lim = fminf(lim, key_d2(okey));
+        };
+        auto instance_leaf = [&](int first, int cnt, bool admitted, float& lim) {
+            for (int k = 0; k < cnt; ++k) {
+                const int inst = __float_as_int(__ldg(&a.trecs[first + k].p2.y));
+                const int baked = a.inst_baked[inst];
+                const bool act = admitted;
+                float lim0, s2 = 1.0f;
+                const WideNode<K>* bn;
+                int32_t root;
+                if (baked >= 0) {
+                    ox = qx;
+                    oy = qy;
+                    oz = qz;
+                    lim0 = best;
+                    bn = static_cast<const WideNode<K>*>(a.knodes);
+                    mfast = a.kfast;
+                    root = a.kroot[baked];
+                } else {
+                    to_object(a.inst_inv + 12 * inst, a.inst_fwd + 12 * inst, qx, qy, qz, ox, oy, oz);
+                    s2 = a.inst_s2[2 * inst];
+                    const float s2lo = a.inst_s2[2 * inst + 1];
+                    lim0 = best < INFINITY ? best / s2lo * (1.0f + 1e-5f) : INFINITY;
+                    bn = static_cast<const WideNode<K>*>(a.bnodes);
+                    mfast = a.bfast;
+                    root = a.broot[a.inst_mesh[inst]];
+                }
+                okey = kNoKey;
+                float limb = act ? lim0 : -INFINITY;
+                if (__any_sync(kFull, act)) packet_walk<K>(bn, root, ox, oy, oz, act, limb, stk_b, cap_b, a.status, mesh_leaf);
+                const float d2o = key_d2(okey);
+                if (act && d2o < lim0) {
+                    const float d2w = d2o * s2;
+                    const int idx = (int)(uint32_t)okey;
+                    if (d2w < best || (d2w == best && (inst < binst || (inst == binst && idx < bidx)))) {
+                        best = d2w;
+                        binst = inst;
+                        bidx = idx;
+                    }
+                }
+            }
+            if (admitted) lim = best;
+        };
+        float limw = valid ? INFINITY : -INFINITY;
+        packet_walk<K>(tnodes, troot, qx, qy, qz, valid, limw, stk_t, cap_t, a.status, instance_leaf);
+        if (valid) instance_finish(a, qi, qx, qy, qz, binst, bidx);
+    }
+}
+
+template <int K>
+cudaError_t launch_instances_packet(const InstArgs& args, int cap_t, int cap_b, cudaStream_t st) {
+    auto kern = k_instances_packet<K>;
+    const int block = 128;
+    const size_t smem = (size_t)(block / 32) * scene_warp_bytes(K, cap_t, cap_b);
+    cudaError_t e = ensure_smem_limit(reinterpret_cast<const void*>(kern), smem);
+    if (e != cudaSuccess) return e;
+    int sms = 0;
+    e = sm_count(&sms);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0;
+    e = cpq::blocks_per_sm(reinterpret_cast<const void*>(kern), block, smem, &per_sm);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    int64_t grid = (int64_t)sms * per_sm;
+    const int64_t need = ((args.nq + 31) / 32 * 32 + block - 1) / block;
+    if (grid > need) grid = need;
+    kern<<<(unsigned)grid, block, smem, st>>>(args, cap_t, cap_b);
+    note_launch();
+    return cudaGetLastError();
 }
 
 // One proxy triangle (lo, hi, hi) per instance: the world box of its mesh's
@@ -1816,6 +2071,16 @@ cudaError_t bvh_instance_query(const Bvh& top, const Bvh& bottom, const Instance
     a.out_tri = out_tri;
     a.out_bary = out_bary;
     a.status = bottom.status;
+    if (sort) {
+        // Hilbert-ordered queries: warp packets at both levels
+        const int cap_t = top.max_wide_depth + 1;
+        const int cap_b = std::max(bottom.max_wide_depth, is.baked_bvh ? is.baked_bvh->max_wide_depth : 0) + 1;
+        switch (top.p.K) {
+            case 2: return launch_instances_packet<2>(a, cap_t, cap_b, st);
+            case 4: return launch_instances_packet<4>(a, cap_t, cap_b, st);
+            default: return launch_instances_packet<8>(a, cap_t, cap_b, st);
+        }
+    }
     switch (top.p.K) {
         case 2: return launch_instances<2>(a, st);
         case 4: return launch_instances<4>(a, st);
