@@ -724,6 +724,19 @@ def scene_arm(args):
     out = flat.query(qd, workspace=wsf, opts=o)
     ms_f = _timed(torch, lambda: flat.query(qd, workspace=wsf, opts=o, out=out), args.steps, args.warmup)
     diff = float((r.dist - out.dist).abs().max())
+    # rays from the query points in seeded random directions, through the
+    # instances (cp_scene_ray_query) and through the flattened mesh
+    rd = np.random.default_rng(17).normal(size=q.shape).astype(np.float32)
+    rd /= np.linalg.norm(rd, axis=1, keepdims=True)
+    rdd = torch.from_numpy(rd).to(dev)
+    rs = scene.ray_query(qd, rdd)
+    ms_rs = _timed(torch, lambda: scene.ray_query(qd, rdd), args.steps, args.warmup)
+    rf = flat.ray_query(qd, rdd)
+    ms_rf = _timed(torch, lambda: flat.ray_query(qd, rdd), args.steps, args.warmup)
+    both = torch.isfinite(rf.t) & torch.isfinite(rs.t)
+    # rays grazing an edge may hit in one geometry and pass on in the other
+    # (the flattened mesh's vertices are rounded copies): count them
+    ray_t_off = float((((rs.t - rf.t).abs() / rf.t.abs().clamp_min(1.0))[both] > 1e-4).float().mean())
     _line("instanced-scene closest-point queries/s (4,096 instances, 16M queries)", nq / (ms_s * 1e-3),
           "queries/s", ms_s, args,
           {"workload": "4,096 similarity instances (random rotation, scale 0.6-1.2) of icosphere L4 / "
@@ -734,7 +747,12 @@ def scene_arm(args):
           {"flattened_mesh": {"value": nq / (ms_f * 1e-3), "ms_per_step": ms_f, "tris": int(wt.shape[0]),
                               "note": "world vertices rounded to FP32 (up to 2^-24 of coordinates <= 47); "
                                       "the scene places the exact FP32 object vertices"},
-           "max_abs_diff_vs_flattened": diff})
+           "max_abs_diff_vs_flattened": diff,
+           "rays": {"value": nq / (ms_rs * 1e-3), "unit": "rays/s", "ms_per_step": ms_rs,
+                    "flattened_mesh": {"value": nq / (ms_rf * 1e-3), "ms_per_step": ms_rf},
+                    "hit_fraction": float(torch.isfinite(rs.t).float().mean()),
+                    "hit_fraction_flattened": float(torch.isfinite(rf.t).float().mean()),
+                    "frac_hits_t_off_by_1e-4_vs_flattened": ray_t_off}})
 
 
 def main():

@@ -1028,6 +1028,58 @@ CP_API cp_status cp_scene_query(const cp_scene* scene, const float* queries, int
     return CP_SUCCESS;
 }
 
+CP_API cp_status cp_scene_ray_workspace_size(const cp_scene* scene, int64_t n, const cp_ray_opts* opts,
+                                             size_t* bytes) {
+    if (!scene || !bytes) return fail(CP_ERROR_INVALID_VALUE, "scene or bytes is NULL");
+    if (n < 0) return fail(CP_ERROR_INVALID_VALUE, "negative ray count");
+    RayParams rp;
+    cp_status s = to_ray_params(opts, &rp);
+    if (s != CP_SUCCESS) return s;
+    QueryParams qp;
+    qp.sort = rp.sort;
+    *bytes = query_workspace_bytes(scene->top, n, qp);
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_scene_ray_query(const cp_scene* scene, const float* origins, const float* directions,
+                                    const float* tmax_per_ray, int64_t n, const cp_ray_opts* opts,
+                                    float* out_t, int32_t* out_instance, int32_t* out_tri, float* out_uv,
+                                    void* workspace, size_t ws_bytes, cp_stream_t stream) {
+    if (!scene) return fail(CP_ERROR_INVALID_VALUE, "scene is NULL");
+    if (!scene->valid) return fail(CP_ERROR_INVALID_VALUE, "scene unusable: its last update failed");
+    if (n < 0) return fail(CP_ERROR_INVALID_VALUE, "negative ray count");
+    if (n > INT32_MAX) return fail(CP_ERROR_NOT_SUPPORTED, "more than 2^31 - 1 rays in one call");
+    if (n == 0) return CP_SUCCESS;
+    if (!origins || !directions) return fail(CP_ERROR_INVALID_VALUE, "origins or directions is NULL");
+    RayParams rp;
+    cp_status s = to_ray_params(opts, &rp);
+    if (s != CP_SUCCESS) return s;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    QueryParams qp;
+    qp.sort = rp.sort;
+    const size_t need = query_workspace_bytes(scene->top, n, qp);
+    void* own = nullptr;
+    if (!workspace) {
+        CP_CUDA(ws_alloc(&own, need, st), "workspace allocation");
+        workspace = own;
+        ws_bytes = need;
+    } else if (ws_bytes < need) {
+        return fail(CP_ERROR_SCRATCH_TOO_SMALL, "workspace smaller than cp_scene_ray_workspace_size()");
+    }
+    InstanceSet is;
+    is.mesh = scene->d_inst_mesh;
+    is.baked = scene->d_baked;
+    is.inv = scene->d_inv;
+    is.fwd = scene->d_fwd;
+    is.s2 = scene->d_s2;
+    is.baked_bvh = scene->has_baked ? &scene->baked : nullptr;
+    cudaError_t e = scene_ray_query(scene->top, scene->batch->bvh, is, origins, directions, tmax_per_ray, n, rp,
+                                    out_t, out_instance, out_tri, out_uv, workspace, ws_bytes, st);
+    if (own) cudaFreeAsync(own, st);
+    if (e != cudaSuccess) return cuda_fail(e, "scene ray query");
+    return CP_SUCCESS;
+}
+
 // ---- inspection ------------------------------------------------------------
 
 CP_API cp_status cp_mesh_export_build(const cp_mesh* m, uint64_t* keys, int32_t* order, int32_t* left,

@@ -25,4 +25,13 @@ cudaError_t bvh_ray_query(const Bvh& b, const float* orig, const float* dir, con
                           int64_t n, const int64_t* d_off, const RayParams& rp, float* out_t,
                           int32_t* out_tri, float* out_uv, void* ws, size_t ws_bytes, cudaStream_t st);
 
+// Closest (or any) hit of n world-space rays over an instanced scene (top:
+// BVH over the instances, bottom: the batch, is: the instances).  Outputs
+// (each optional): t, instance, triangle local to the instance's mesh, (u, v).
+// Workspace: query_workspace_bytes(top, n, {sort}).
+cudaError_t scene_ray_query(const Bvh& top, const Bvh& bottom, const InstanceSet& is, const float* orig,
+                            const float* dir, const float* tmax_per_ray, int64_t n, const RayParams& rp,
+                            float* out_t, int32_t* out_inst, int32_t* out_tri, float* out_uv, void* ws,
+                            size_t ws_bytes, cudaStream_t st);
+
 }  // namespace cpq

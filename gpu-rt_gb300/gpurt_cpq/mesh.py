@@ -344,6 +344,14 @@ class SceneResult:
     bary: torch.Tensor | None    # (N, 2) float32
 
 
+@dataclass
+class SceneRayResult:
+    t: torch.Tensor          # (N,) float32, +inf on a miss
+    instance: torch.Tensor   # (N,) int32, -1 on a miss
+    tri: torch.Tensor        # (N,) int32, local to the instance's mesh
+    uv: torch.Tensor | None  # (N, 2) float32
+
+
 def _transforms(transforms) -> np.ndarray:
     """(n, 3, 4) or (n, 4, 4) object-to-world matrices -> (n, 12) float32 row-major 3 x 4."""
     t = np.asarray(transforms.cpu() if isinstance(transforms, torch.Tensor) else transforms)
@@ -390,6 +398,26 @@ class Scene:
         o = opts or query_opts()
         check(lib.cp_scene_query_workspace_size(self._h, nq, byref(o), byref(b)), "workspace")
         return b.value
+
+    def ray_query(self, origins: torch.Tensor, directions: torch.Tensor, *,
+                  tmax_per_ray: torch.Tensor | None = None, opts: RayOpts | None = None,
+                  want_uv: bool = True, stream=None) -> SceneRayResult:
+        """Closest (or any) hit of each world-space ray (cp_scene_ray_query)."""
+        _check_dev(origins, "origins", torch.float32, 3)
+        _check_dev(directions, "directions", torch.float32, 3)
+        n = int(origins.shape[0])
+        if directions.shape[0] != n:
+            raise ValueError("origins and directions must have the same length")
+        dev = origins.device
+        out = SceneRayResult(t=torch.empty((n,), dtype=torch.float32, device=dev),
+                             instance=torch.empty((n,), dtype=torch.int32, device=dev),
+                             tri=torch.empty((n,), dtype=torch.int32, device=dev),
+                             uv=torch.empty((n, 2), dtype=torch.float32, device=dev) if want_uv else None)
+        o = opts or ray_opts()
+        check(lib.cp_scene_ray_query(self._h, _ptr(origins), _ptr(directions), _ptr(tmax_per_ray), n, byref(o),
+                                     _ptr(out.t), _ptr(out.instance), _ptr(out.tri), _ptr(out.uv),
+                                     c_void_p(None), 0, _stream(stream)), "cp_scene_ray_query")
+        return out
 
     def query(self, points: torch.Tensor, *, want_point: bool = True, want_bary: bool = False,
               opts: QueryOpts | None = None, workspace: torch.Tensor | None = None,

@@ -457,6 +457,25 @@ CP_API cp_status cp_scene_query(const cp_scene* scene, const float* queries, int
                                 int32_t* out_instance, int32_t* out_tri, float* out_bary,
                                 void* workspace, size_t workspace_bytes, cp_stream_t stream);
 
+CP_API cp_status cp_scene_ray_workspace_size(const cp_scene* scene, int64_t n, const cp_ray_opts* opts,
+                                             size_t* bytes);
+
+/*
+ * Closest (or, with opts->any_hit, some) hit of each world-space ray over the
+ * scene: the reference's trace_ray / visibility against its TLAS
+ * (src/shaders/rt/rt.rgen:257-291; src/vk/vulkan.cpp:777-856).  Options and
+ * tmax_per_ray as in cp_ray_query.  A similarity instance is hit in object
+ * space (o' = A (o - t), d' = A d: the hit parameter t is the world one), a
+ * general one on its world-space copy.  Outputs (each may be NULL): t (+inf on
+ * a miss), instance (-1), triangle local to the instance's mesh (-1), weights
+ * (u, v) of its b and c vertices.  The closest hit is the least (t, instance,
+ * triangle).
+ */
+CP_API cp_status cp_scene_ray_query(const cp_scene* scene, const float* origins, const float* directions,
+                                    const float* tmax_per_ray, int64_t n, const cp_ray_opts* opts,
+                                    float* out_t, int32_t* out_instance, int32_t* out_tri, float* out_uv,
+                                    void* workspace, size_t workspace_bytes, cp_stream_t stream);
+
 /* ---- autotuner ------------------------------------------------------------ */
 
 /*

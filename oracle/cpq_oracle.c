@@ -1335,3 +1335,49 @@ void orc_brute_f64_dv(const double* verts, const int32_t* tris, int64_t nt, cons
     brute_dv_ctx c = {verts, tris, nt, q, out_d2, out_p, out_tri};
     parallel_for(nq, 16, nthreads, brute_dv_range, &c);
 }
+
+/* FP64 closest hit over FP64 vertices (instanced scenes placed in FP64). */
+typedef struct {
+    const double* verts;
+    const int32_t* tris;
+    int64_t nt;
+    const float *orig, *dir;
+    double tmin, tmax;
+    double *t, *uv;
+    int32_t* tri;
+} ray_dv_ctx;
+
+static void ray_dv_range(void* vctx, int64_t b, int64_t e) {
+    ray_dv_ctx* c = (ray_dv_ctx*)vctx;
+    for (int64_t i = b; i < e; ++i) {
+        const double o[3] = {c->orig[3 * i], c->orig[3 * i + 1], c->orig[3 * i + 2]};
+        const double d[3] = {c->dir[3 * i], c->dir[3 * i + 1], c->dir[3 * i + 2]};
+        double bt = INFINITY, bu = 0.0, bv = 0.0;
+        int32_t bi = -1;
+        for (int64_t k = 0; k < c->nt; ++k) {
+            const int32_t* ix = c->tris + 3 * k;
+            double t, u, v;
+            if (!mt_f64(o, d, c->verts + 3 * (int64_t)ix[0], c->verts + 3 * (int64_t)ix[1],
+                        c->verts + 3 * (int64_t)ix[2], 0.0, &t, &u, &v))
+                continue;
+            if (!(t >= c->tmin && t <= c->tmax)) continue;
+            if (t < bt) {
+                bt = t;
+                bu = u;
+                bv = v;
+                bi = (int32_t)k;
+            }
+        }
+        c->t[i] = bt;
+        c->tri[i] = bi;
+        c->uv[2 * i] = bu;
+        c->uv[2 * i + 1] = bv;
+    }
+}
+
+void orc_ray_brute_f64_dv(const double* verts, const int32_t* tris, int64_t nt, const float* orig,
+                          const float* dir, int64_t n, double tmin, double tmax, double* out_t,
+                          int32_t* out_tri, double* out_uv, int nthreads) {
+    ray_dv_ctx c = {verts, tris, nt, orig, dir, tmin, tmax, out_t, out_uv, out_tri};
+    parallel_for(n, 16, nthreads, ray_dv_range, &c);
+}

@@ -138,6 +138,13 @@ double orc_ray_brute_f64(const float* verts, const int32_t* tris, int64_t nt, co
                          double tmax, double det_eps, double* out_t, int32_t* out_tri,
                          double* out_uv, int nthreads);
 
+/* FP64 closest hit of every ray over FP64 vertices (no det epsilon): the
+ * truth for rays through instanced scenes, whose world vertices are the FP32
+ * object vertices through FP32 matrices evaluated in FP64. */
+void orc_ray_brute_f64_dv(const double* verts, const int32_t* tris, int64_t nt, const float* orig,
+                          const float* dir, int64_t n, double tmin, double tmax, double* out_t,
+                          int32_t* out_tri, double* out_uv, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

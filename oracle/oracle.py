@@ -90,6 +90,9 @@ def lib():
         L.orc_ray_brute_f64.restype = c_double
         L.orc_ray_brute_f64.argtypes = [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p, c_int64,
                                         c_double, c_double, c_double, c_void_p, c_void_p, c_void_p, c_int]
+        L.orc_ray_brute_f64_dv.restype = None
+        L.orc_ray_brute_f64_dv.argtypes = [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_int64, c_double,
+                                           c_double, c_void_p, c_void_p, c_void_p, c_int]
         _lib = L
     return _lib
 
@@ -279,3 +282,16 @@ def brute_f64_dv(verts64, tris, q, threads: int | None = None):
     p = np.empty((n, 3))
     lib().orc_brute_f64_dv(_p(v), _p(t), t.shape[0], _p(qq), n, _p(d2), _p(tri), _p(p), threads or nthreads())
     return {"dist": np.sqrt(d2), "tri": tri, "point": p}
+
+
+def ray_brute_f64_dv(verts64, tris, orig, dirs, tmin=0.0, tmax=float("inf"), threads: int | None = None):
+    """FP64 closest hit of every ray over FP64 vertices (instanced scenes)."""
+    v = np.ascontiguousarray(verts64, dtype=np.float64)
+    t, o, d = _i32(tris), _f32(orig), _f32(dirs)
+    n = o.shape[0]
+    out_t = np.empty(n)
+    out_tri = np.empty(n, np.int32)
+    out_uv = np.empty((n, 2))
+    lib().orc_ray_brute_f64_dv(_p(v), _p(t), t.shape[0], _p(o), _p(d), n, tmin, tmax, _p(out_t), _p(out_tri),
+                               _p(out_uv), threads or nthreads())
+    return {"t": out_t, "tri": out_tri, "uv": out_uv}

@@ -254,6 +254,123 @@ def test_scene_rejects_bad_input(cpq, cuda):
         sc.update(T[:1])
 
 
+def _mt64(o, d, a, b, c):
+    """FP64 Möller–Trumbore hit parameter of one ray and triangle (nan on a miss)."""
+    e1, e2 = b - a, c - a
+    p = np.cross(d, e2)
+    det = e1 @ p
+    if det == 0.0:
+        return np.nan
+    s = o - a
+    u = (s @ p) / det
+    q = np.cross(s, e1)
+    v = (d @ q) / det
+    if u < 0 or v < 0 or u + v > 1:
+        return np.nan
+    return (e2 @ q) / det
+
+
+def _scene_rays(rng, wv, n):
+    lo, hi = wv.min(0), wv.max(0)
+    o = rng.uniform(lo - 1, hi + 1, (n, 3)).astype(np.float32)
+    target = rng.uniform(lo, hi, (n, 3))
+    d = (target - o).astype(np.float32)
+    return o, d
+
+
+def test_scene_rays_identity_matches_mesh(cpq, cuda):
+    """One instance at the identity: the same hits, bit for bit, as the plain
+    ray query on the mesh (identical object-space arithmetic)."""
+    from gpurt_cpq import workloads as W
+
+    v, t = W.torus(80, 30)
+    T = np.zeros((1, 3, 4), np.float32)
+    T[0, :, :3] = np.eye(3)
+    sc = cpq.Scene(make_batch(cpq, cuda, [(v, t)], 4), [0], T)
+    rng = np.random.default_rng(7)
+    o, d = _scene_rays(rng, v.astype(np.float64), 30000)
+    r = sc.ray_query(dev(o, cuda), dev(d, cuda))
+    m = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=4).ray_query(dev(o, cuda), dev(d, cuda))
+    assert torch_equal(r.t, m.t) and torch_equal(r.tri, m.tri) and torch_equal(r.uv, m.uv)
+    assert np.all(r.instance.cpu().numpy()[m.tri.cpu().numpy() >= 0] == 0)
+
+
+def torch_equal(a, b):
+    import torch
+    return bool(torch.equal(a, b))
+
+
+@pytest.mark.parametrize("K", [2, 4, 8])
+def test_scene_rays_vs_fp64(orc, cpq, cuda, K):
+    """Similarity and general affine instances, rays aimed into the scene:
+    hits against the FP64 brute force over world-space vertices."""
+    from gpurt_cpq import workloads as W
+
+    meshes = [W.icosphere(2), W.torus(40, 16)]
+    T = random_similarities(12, seed=8)
+    T[1, :, :3] = T[1, :, :3] @ np.diag([3.0, 1.0, 0.5]).astype(np.float32)
+    T[2, 0, 1] += 0.7
+    T[5, :, :3] = T[5, :, :3] @ np.diag([1.0, 1.0, 0.0]).astype(np.float32)
+    inst_mesh = (np.arange(12) % 2).astype(np.int32)
+    sc = cpq.Scene(make_batch(cpq, cuda, meshes, K), inst_mesh, T)
+    wv, wt, toff = world_soup(meshes, inst_mesh, T)
+    rng = np.random.default_rng(9)
+    o, d = _scene_rays(rng, wv, 20000)
+    r = sc.ray_query(dev(o, cuda), dev(d, cuda))
+    ref = orc.ray_brute_f64_dv(wv, wt, o, d)
+    t = r.t.cpu().numpy().astype(np.float64)
+    inst, tri = r.instance.cpu().numpy(), r.tri.cpu().numpy()
+    hit, hit64 = np.isfinite(t), np.isfinite(ref["t"])
+    scale = 1.0 + np.abs(wv).max()
+    # a hit or miss may differ only where the FP64 ray grazes a triangle's
+    # boundary (barycentrics within 1e-4 of an edge) or the plane it hits
+    for i in np.nonzero(hit != hit64)[0]:
+        if hit64[i]:
+            u, v = ref["uv"][i]
+            assert min(u, v, 1 - u - v) < 1e-4, (i, u, v)
+        else:
+            g = toff[inst[i]] + tri[i]
+            a, b, c = wv[wt[g]]
+            t64 = _mt64(o[i].astype(np.float64), d[i].astype(np.float64), a, b, c)
+            assert np.isnan(t64) or abs(t64 - t[i]) <= 1e-4 * scale, (i, t64, t[i])
+    both = hit & hit64
+    assert both.mean() > 0.3
+    # the hit parameter: FP32 object-space arithmetic against FP64
+    err = np.abs(t[both] - ref["t"][both])
+    assert np.all(err <= 2e-5 * scale * (1.0 + ref["t"][both])), err.max()
+    # another triangle than the FP64 one only where both are hit at the same t
+    g = toff[inst] + tri
+    for i in np.nonzero(both & (g != ref["tri"]))[0][:300]:
+        a, b, c = wv[wt[g[i]]]
+        t64 = _mt64(o[i].astype(np.float64), d[i].astype(np.float64), a, b, c)
+        assert not np.isnan(t64) and abs(t64 - ref["t"][i]) <= 2e-5 * scale * (1 + ref["t"][i]), (i, t64)
+
+
+def test_scene_rays_any_hit_and_segments(cpq, cuda):
+    from gpurt_cpq import workloads as W
+
+    import torch
+
+    meshes = [W.icosphere(2)]
+    T = random_similarities(6, seed=10)
+    T[3, :, :3] = T[3, :, :3] @ np.diag([2.0, 1.0, 1.0]).astype(np.float32)
+    sc = cpq.Scene(make_batch(cpq, cuda, meshes, 4), np.zeros(6, np.int32), T)
+    wv, _, _ = world_soup(meshes, np.zeros(6, np.int32), T)
+    o, d = _scene_rays(np.random.default_rng(11), wv, 20000)
+    od, dd = dev(o, cuda), dev(d, cuda)
+    closest = sc.ray_query(od, dd)
+    anyh = sc.ray_query(od, dd, opts=cpq.ray_opts(any_hit=True))
+    assert torch.equal(torch.isfinite(anyh.t), torch.isfinite(closest.t))
+    hit = torch.isfinite(closest.t)
+    assert bool((anyh.t[hit] >= closest.t[hit]).all())
+    # segment ends just before / after the closest hit
+    tm = torch.where(hit, closest.t, torch.ones_like(closest.t))
+    before = sc.ray_query(od, dd, tmax_per_ray=tm * 0.999, opts=cpq.ray_opts(any_hit=True))
+    after = sc.ray_query(od, dd, tmax_per_ray=tm * 1.001)
+    assert bool((~torch.isfinite(before.t[hit]) | (before.t[hit] < closest.t[hit])).all())
+    assert torch.equal(after.t[hit], closest.t[hit])
+
+
 def test_cbox_scene_vs_fp64(orc, cpq, cuda):
     """The reference's Cornell box (media/cbox, 16,720 triangles in 9
     primitives placed by 10 node instances), from the committed fixture:
