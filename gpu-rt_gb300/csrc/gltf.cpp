@@ -327,7 +327,14 @@ struct Model {
         if (a.get("sparse")) throw std::runtime_error("sparse accessors are not supported");
         Accessor r;
         r.ctype = (int)a.integer("componentType", 0);
-        r.count = (size_t)a.integer("count", 0);
+        // sizes and offsets: non-negative, and every bound below is checked
+        // without a sum or product that could wrap
+        auto size_of = [](const Json& j, const char* k) {
+            const int64_t v = j.integer(k, 0);
+            if (v < 0) throw std::runtime_error(std::string("negative \"") + k + "\"");
+            return (size_t)v;
+        };
+        r.count = size_of(a, "count");
         const std::string& type = a.at("type").str;
         r.ncomp = type == "SCALAR" ? 1 : type == "VEC2" ? 2 : type == "VEC3" ? 3 : type == "VEC4" ? 4 : 0;
         if (!r.ncomp) throw std::runtime_error("unsupported accessor type " + type);
@@ -345,15 +352,16 @@ struct Model {
         const int64_t bi = bv.integer("buffer", -1);
         if (bi < 0 || bi >= (int64_t)buffers.size()) throw std::runtime_error("bufferView buffer out of range");
         const std::vector<uint8_t>& buf = buffers[(size_t)bi];
-        const size_t view_off = (size_t)bv.integer("byteOffset", 0);
-        const size_t view_len = (size_t)bv.integer("byteLength", 0);
-        const size_t off = (size_t)a.integer("byteOffset", 0);
+        const size_t view_off = size_of(bv, "byteOffset");
+        const size_t view_len = size_of(bv, "byteLength");
+        const size_t off = size_of(a, "byteOffset");
         const size_t elem = csize * (size_t)r.ncomp;
-        r.stride = (size_t)bv.integer("byteStride", 0);
+        r.stride = size_of(bv, "byteStride");
         if (r.stride == 0) r.stride = elem;
         if (r.stride < elem) throw std::runtime_error("byteStride smaller than the element");
-        if (view_off + view_len > buf.size()) throw std::runtime_error("bufferView past the end of its buffer");
-        if (r.count && off + (r.count - 1) * r.stride + elem > view_len)
+        if (view_off > buf.size() || view_len > buf.size() - view_off)
+            throw std::runtime_error("bufferView past the end of its buffer");
+        if (r.count && (off > view_len || elem > view_len - off || (r.count - 1) > (view_len - off - elem) / r.stride))
             throw std::runtime_error("accessor past the end of its bufferView");
         r.data = buf.data() + view_off + off;
         return r;

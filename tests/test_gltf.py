@@ -194,3 +194,57 @@ def test_gltf_scene_queries(orc, cpq, cuda, tmp_path):
     ref = orc.brute_f64(v, t, q)
     d = r.dist.cpu().numpy().astype(np.float64)
     assert np.max(np.abs(d - ref["dist"]) / np.maximum(ref["dist"], 1e-30)) <= 1e-6
+
+
+def test_malformed_files_never_crash(cpq, tmp_path):
+    """Seeded mutations of valid .gltf and .glb files — truncation, byte
+    flips, numbers in the JSON replaced by huge, negative or fractional
+    values — load cleanly or raise CpError; the process never crashes and no
+    index reaches past its vertices."""
+    import re
+
+    from gpurt_cpq._lib import CpError
+
+    rng = np.random.default_rng(2024)
+    doc, data = _scene()
+    gl = _write(tmp_path, doc, data, "data").read_bytes()
+    glb = _write(tmp_path, doc, data, "glb").read_bytes()
+    numbers = [m.start() for m in re.finditer(rb"\d+", gl)]
+    outcomes = {"ok": 0, "error": 0}
+    for k in range(400):
+        src, ext = (gl, ".gltf") if k % 2 == 0 else (glb, ".glb")
+        b = bytearray(src)
+        kind = k % 5
+        if kind == 0:
+            b = b[: int(rng.integers(1, len(b)))]
+        elif kind == 1:
+            for _ in range(int(rng.integers(1, 8))):
+                b[int(rng.integers(0, len(b)))] ^= 1 << int(rng.integers(0, 8))
+        elif kind == 2 and ext == ".gltf":
+            at = numbers[int(rng.integers(0, len(numbers)))]
+            end = at
+            while end < len(b) and chr(b[end]).isdigit():
+                end += 1
+            b[at:end] = [b"4294967295", b"-1", b"99999999999999999999", b"0.5", b"1e300"][int(rng.integers(0, 5))]
+        elif kind == 3 and ext == ".glb":
+            # damage the chunk headers (lengths and types)
+            for off in (12, 16, 20 + int.from_bytes(src[12:16], "little")):
+                if off + 4 <= len(b):
+                    b[off:off + 4] = int(rng.integers(0, 2**32)).to_bytes(4, "little")
+        else:
+            cut = int(rng.integers(0, len(b)))
+            b = b[:cut] + b[cut + int(rng.integers(1, 64)):]
+        f = tmp_path / f"m{k}{ext}"
+        f.write_bytes(bytes(b))
+        try:
+            s = cpq.load_gltf(str(f))
+        except CpError:
+            outcomes["error"] += 1
+            continue
+        outcomes["ok"] += 1
+        nv = np.diff(s.vert_offsets)
+        for p in range(len(nv)):
+            t = s.tris[s.tri_offsets[p]:s.tri_offsets[p + 1]]
+            assert t.size == 0 or (t.min() >= 0 and t.max() < nv[p])
+        assert np.all(s.instance_primitive >= 0) and np.all(s.instance_primitive < len(nv))
+    assert outcomes["error"] > 0 and outcomes["ok"] > 0
