@@ -1742,12 +1742,23 @@ __global__ void __launch_bounds__(128) k_instances_packet(InstArgs a, int cap_t,
     }
 }
 
+// Returns cudaErrorNotSupported (nothing launched) when even one warp's two
+// stacks exceed a block's shared memory: the caller takes the per-thread walk.
 template <int K>
 cudaError_t launch_instances_packet(const InstArgs& args, int cap_t, int cap_b, cudaStream_t st) {
     auto kern = k_instances_packet<K>;
-    const int block = 128;
-    const size_t smem = (size_t)(block / 32) * scene_warp_bytes(K, cap_t, cap_b);
-    cudaError_t e = ensure_smem_limit(reinterpret_cast<const void*>(kern), smem);
+    int block = 128;
+    size_t smem = (size_t)(block / 32) * scene_warp_bytes(K, cap_t, cap_b);
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return e;
+    while (block > 32 && smem > (size_t)optin) {  // very deep trees: fewer warps per block
+        block /= 2;
+        smem = (size_t)(block / 32) * scene_warp_bytes(K, cap_t, cap_b);
+    }
+    if (smem > (size_t)optin) return cudaErrorNotSupported;
+    e = ensure_smem_limit(reinterpret_cast<const void*>(kern), smem);
     if (e != cudaSuccess) return e;
     int sms = 0;
     e = sm_count(&sms);
@@ -1755,7 +1766,7 @@ cudaError_t launch_instances_packet(const InstArgs& args, int cap_t, int cap_b, 
     int per_sm = 0;
     e = cpq::blocks_per_sm(reinterpret_cast<const void*>(kern), block, smem, &per_sm);
     if (e != cudaSuccess) return e;
-    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    if (per_sm < 1) return cudaErrorNotSupported;
     int64_t grid = (int64_t)sms * per_sm;
     const int64_t need = ((args.nq + 31) / 32 * 32 + block - 1) / block;
     if (grid > need) grid = need;
@@ -2076,10 +2087,12 @@ cudaError_t bvh_instance_query(const Bvh& top, const Bvh& bottom, const Instance
         const int cap_t = top.max_wide_depth + 1;
         const int cap_b = std::max(bottom.max_wide_depth, is.baked_bvh ? is.baked_bvh->max_wide_depth : 0) + 1;
         switch (top.p.K) {
-            case 2: return launch_instances_packet<2>(a, cap_t, cap_b, st);
-            case 4: return launch_instances_packet<4>(a, cap_t, cap_b, st);
-            default: return launch_instances_packet<8>(a, cap_t, cap_b, st);
+            case 2: e = launch_instances_packet<2>(a, cap_t, cap_b, st); break;
+            case 4: e = launch_instances_packet<4>(a, cap_t, cap_b, st); break;
+            default: e = launch_instances_packet<8>(a, cap_t, cap_b, st); break;
         }
+        if (e != cudaErrorNotSupported) return e;
+        // the stacks do not fit in shared memory: the per-thread walk below
     }
     switch (top.p.K) {
         case 2: return launch_instances<2>(a, st);
