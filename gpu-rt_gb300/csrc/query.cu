@@ -1629,8 +1629,11 @@ __host__ __device__ constexpr size_t scene_warp_bytes(int K, int cap_t, int cap_
     return packet_stack_bytes(K, cap_t) + packet_stack_bytes(K, cap_b) + 32 * sizeof(float4);
 }
 
+// 7 blocks of 128 per SM: what two 4-wide stacks per warp leave of shared
+// memory on the scenes measured; the register cap it implies (73) spills 32
+// bytes, and 28 warps instead of 24 gave 1% more queries per second.
 template <int K>
-__global__ void __launch_bounds__(128) k_instances_packet(InstArgs a, int cap_t, int cap_b) {
+__global__ void __launch_bounds__(128, 7) k_instances_packet(InstArgs a, int cap_t, int cap_b) {
     extern __shared__ __align__(16) unsigned char s_sc[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned char* stk_t = s_sc + (size_t)warp * scene_warp_bytes(K, cap_t, cap_b);
