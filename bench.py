@@ -367,7 +367,7 @@ def our_arm(args):
     hout = {"dist": torch.empty(nq, dtype=torch.float32).pin_memory(),
             "tri": torch.empty(nq, dtype=torch.int32).pin_memory(),
             "point": torch.empty((nq, 3), dtype=torch.float32).pin_memory()}
-    e2e_steps = max(1, min(args.steps, 5))
+    e2e_steps = max(1, min(args.steps, 10))
     mesh.query_host(qh, opts=qopts, out=hout)
     if world > 1:
         torch.distributed.barrier()
