@@ -95,3 +95,51 @@ def test_workload_shapes():
     assert (a == q).all()
     meshes, queries = W.batched(nmeshes=6, tri_range=(1000, 20000), q_range=(100, 1000))
     assert len(meshes) == 6 and all(1 <= len(x) for x in queries)
+
+
+def test_argument_checks_of_every_handle_kind(cpq):
+    """NULL handles, NULL arrays, empty or inconsistent sizes and unknown flags
+    are refused with CP_ERROR_INVALID_VALUE and a message, before any device
+    work — for meshes, batches, scenes, rays, glTF files and diagnostics."""
+    import numpy as np
+    from ctypes import byref, c_size_t, c_uint64, c_void_p
+
+    from gpurt_cpq._lib import CP_ERROR_INVALID_VALUE, lib
+
+    def refused(st, text):
+        assert st == CP_ERROR_INVALID_VALUE, st
+        assert text.encode() in lib.cp_last_error_string(), lib.cp_last_error_string()
+
+    out = c_void_p()
+    size = c_size_t()
+    some = np.zeros(64, np.float32)
+    p = c_void_p(some.ctypes.data)
+    # scenes: the batch and both host arrays are required, and instances
+    refused(lib.cp_scene_create(None, p, p, 1, None, byref(out)), "NULL")
+    refused(lib.cp_scene_create(p, p, p, 0, None, byref(out)), "at least one instance")
+    refused(lib.cp_scene_query(None, p, 1, None, None, None, None, None, None, None, 0, None), "scene is NULL")
+    refused(lib.cp_scene_ray_query(None, p, p, None, 1, None, None, None, None, None, None, 0, None),
+            "scene is NULL")
+    refused(lib.cp_scene_update(None, p, None), "NULL")
+    refused(lib.cp_scene_query_workspace_size(None, 1, None, byref(size)), "NULL")
+    refused(lib.cp_scene_ray_workspace_size(None, 1, None, byref(size)), "NULL")
+    assert lib.cp_scene_destroy(None) == 0
+    # rays and the no-allocation query on a NULL mesh
+    refused(lib.cp_ray_query(None, p, p, None, 1, None, None, None, None, None, 0, None), "mesh")
+    refused(lib.cp_query_noalloc(None, p, 1, None, None, None, None, None, None), "mesh is NULL")
+    # batches: arrays, mesh count, offsets starting at zero, no empty mesh
+    off = np.array([0, 3], np.int64)
+    bad_off = np.array([1, 3], np.int64)
+    empty = np.array([0, 0], np.int64)
+    po, pb, pe = (c_void_p(a.ctypes.data) for a in (off, bad_off, empty))
+    refused(lib.cp_batch_create(None, po, p, po, 1, None, None, byref(out)), "NULL")
+    refused(lib.cp_batch_create(p, po, p, po, 0, None, None, byref(out)), "nmeshes")
+    refused(lib.cp_batch_create(p, pb, p, po, 1, None, None, byref(out)), "start at 0")
+    refused(lib.cp_batch_create(p, po, p, pe, 1, None, None, byref(out)), "at least one triangle")
+    # glTF and diagnostics
+    refused(lib.cp_gltf_load(None, byref(out)), "NULL")
+    lib.cp_gltf_free(None)
+    refused(lib.cp_timing_enable(4), "unknown flag")
+    refused(lib.cp_traversal_stats(None, 0), "NULL")
+    counts = (c_uint64 * 7)()
+    assert lib.cp_traversal_stats(counts, 0) == 0
