@@ -84,7 +84,7 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--leaf", type=int, default=0)
     ap.add_argument("--workload", default="large",
-                    choices=["large", "torus", "batched", "dynamic", "small", "rays", "scene"],
+                    choices=["large", "torus", "batched", "dynamic", "small", "rays", "scene", "camera"],
                     help="large is the headline; the others measure the other forms")
     return ap.parse_args()
 
@@ -755,6 +755,58 @@ def scene_arm(args):
                     "frac_hits_t_off_by_1e-4_vs_flattened": ray_t_off}})
 
 
+def camera_arm(args):
+    """The reference's own render loop on its own scene: one primary ray per
+    pixel through the Cornell box's instances (trace_ray against the TLAS,
+    rt.rgen:551-565 make_camera_ray, 257-270), then one shadow ray per hit to
+    a point on the ceiling light (visibility, rt.rgen:272-291, as
+    integrate_direct uses it).  The scene comes from the committed fixture of
+    media/cbox/cbox.gltf; 1920 x 1440 pixels."""
+    import torch
+
+    import gpurt_cpq as cpq
+    from gpurt_cpq import workloads as W
+
+    dev = torch.device("cuda", 0)
+    g = np.load(ROOT / "tests" / "golden" / "cbox_scene.npz")
+    batch = cpq.Batch(torch.from_numpy(g["verts"]).to(dev), g["vert_offsets"], torch.from_numpy(g["tris"]).to(dev),
+                      g["tri_offsets"], branching=4, leaf_size=4)
+    scene = cpq.Scene(batch, g["instance_primitive"], g["instance_transform"])
+    w, h = 1920, 1440
+    o, d = W.camera_rays(w, h, W.CBOX_EYE, W.CBOX_YFOV, W.CBOX_ASPECT)
+    od, dd = torch.from_numpy(o).to(dev), torch.from_numpy(d).to(dev)
+    n = od.shape[0]
+    prim = scene.ray_query(od, dd)
+    ms_p = _timed(torch, lambda: scene.ray_query(od, dd), args.steps, args.warmup)
+    # shadow rays: from each hit to a seeded point on the light's lower face
+    li = W.CBOX_LIGHT_INSTANCE
+    m = int(g["instance_primitive"][li])
+    lv = g["verts"][g["vert_offsets"][m]:g["vert_offsets"][m + 1]].astype(np.float64)
+    t34 = g["instance_transform"][li].astype(np.float64)
+    wl = lv @ t34[:, :3].T + t34[:, 3]
+    lo, hi = wl.min(0), wl.max(0)
+    rng = np.random.default_rng(21)
+    tgt = np.stack([rng.uniform(lo[0], hi[0], n), np.full(n, lo[1]), rng.uniform(lo[2], hi[2], n)], -1)
+    hit = torch.isfinite(prim.t)
+    so = (od + dd * prim.t.clamp_max(1e30)[:, None])[hit].contiguous()
+    sd = (torch.from_numpy(tgt.astype(np.float32)).to(dev)[hit] - so).contiguous()
+    ns = so.shape[0]
+    seg = torch.full((ns,), 1.0 - 1e-4, device=dev)
+    sopts = cpq.ray_opts(any_hit=True, tmin=1e-4)
+    shadow = scene.ray_query(so, sd, tmax_per_ray=seg, opts=sopts)
+    ms_s = _timed(torch, lambda: scene.ray_query(so, sd, tmax_per_ray=seg, opts=sopts), args.steps, args.warmup)
+    frame_ms = ms_p + ms_s
+    _line("Cornell box frame: primary + shadow rays/s through its instances", (n + ns) / (frame_ms * 1e-3),
+          "rays/s", frame_ms, args,
+          {"workload": f"media/cbox/cbox.gltf (fixture: 9 primitives, 10 instances, {len(g['tris']):,} tris), "
+                       f"{w}x{h} primary rays from its camera, one shadow ray per hit to its ceiling light",
+           "branching": 4, "leaf_size": 4},
+          {"primary": {"value": n / (ms_p * 1e-3), "ms_per_step": ms_p, "rays": n,
+                       "hit_fraction": float(hit.float().mean())},
+           "shadow": {"value": ns / (ms_s * 1e-3), "ms_per_step": ms_s, "rays": ns,
+                      "occluded_fraction": float(torch.isfinite(shadow.t).float().mean())}})
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -763,7 +815,8 @@ def main():
         our_arm(args)
     else:
         {"torus": torus_arm, "batched": batched_arm, "dynamic": dynamic_arm,
-         "small": small_arm, "rays": rays_arm, "scene": scene_arm}[args.workload](args)
+         "small": small_arm, "rays": rays_arm, "scene": scene_arm,
+         "camera": camera_arm}[args.workload](args)
 
 
 if __name__ == "__main__":

@@ -295,3 +295,25 @@ def instanced_scene(seed: int = 31, nq: int = 16 * M, grid: int = 16):
     near += rng.normal(0.0, 0.02, near.shape)
     q = np.concatenate([far, near]).astype(np.float32)
     return meshes, inst_mesh, T, q[rng.permutation(nq)]
+
+
+def camera_rays(width: int, height: int, eye, yfov: float, aspect: float) -> tuple[np.ndarray, np.ndarray]:
+    """Pinhole primary rays through pixel centres, looking down -z from `eye`
+    (row 0 at the top): origins (n, 3) and unit directions (n, 3), float32."""
+    th = np.tan(0.5 * yfov)
+    i = (np.arange(width) + 0.5) / width * 2.0 - 1.0
+    j = 1.0 - (np.arange(height) + 0.5) / height * 2.0
+    X, Y = np.meshgrid(i * th * aspect, j * th)
+    d = np.stack([X, Y, -np.ones_like(X)], -1).reshape(-1, 3)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    o = np.broadcast_to(np.asarray(eye, np.float64), d.shape)
+    return np.ascontiguousarray(o, np.float32), d.astype(np.float32)
+
+
+# The Cornell box's camera (media/cbox/cbox.gltf: node CamInst, camera
+# "default"): eye on the +z axis, looking down -z, vertical field of view
+# 0.7175 rad at 4:3; its ceiling light is instance 5.
+CBOX_EYE = (0.0, 0.0, 19.992091970966317)
+CBOX_YFOV = 0.7175414562225342
+CBOX_ASPECT = 4.0 / 3.0
+CBOX_LIGHT_INSTANCE = 5

@@ -346,6 +346,34 @@ def test_scene_rays_vs_fp64(orc, cpq, cuda, K):
         assert not np.isnan(t64) and abs(t64 - ref["t"][i]) <= 2e-5 * scale * (1 + ref["t"][i]), (i, t64)
 
 
+def test_cbox_camera_rays_vs_fp64(orc, cpq, cuda):
+    """The reference's Cornell box seen from its own camera (96 x 72 primary
+    rays through the scene's instances) against the FP64 brute force."""
+    from pathlib import Path
+
+    from gpurt_cpq import workloads as W
+
+    g = np.load(Path(__file__).resolve().parent / "golden" / "cbox_scene.npz")
+    b = cpq.Batch(dev(g["verts"], cuda), g["vert_offsets"], dev(g["tris"], cuda), g["tri_offsets"], branching=4)
+    sc = cpq.Scene(b, g["instance_primitive"], g["instance_transform"])
+    o, d = W.camera_rays(96, 72, W.CBOX_EYE, W.CBOX_YFOV, W.CBOX_ASPECT)
+    r = sc.ray_query(dev(o, cuda), dev(d, cuda))
+    nv = np.diff(g["vert_offsets"])
+    meshes = [(g["verts"][g["vert_offsets"][i]:g["vert_offsets"][i + 1]],
+               g["tris"][g["tri_offsets"][i]:g["tri_offsets"][i + 1]]) for i in range(len(nv))]
+    wv, wt, toff = world_soup(meshes, g["instance_primitive"], g["instance_transform"])
+    ref = orc.ray_brute_f64_dv(wv, wt, o, d)
+    t = r.t.cpu().numpy().astype(np.float64)
+    hit, hit64 = np.isfinite(t), np.isfinite(ref["t"])
+    assert 0.5 < hit64.mean() < 0.7  # the box, open toward the camera, fills 59% of the view
+    for i in np.nonzero(hit != hit64)[0]:
+        u, v = ref["uv"][i]
+        assert hit64[i] and min(u, v, 1 - u - v) < 1e-4, (i, u, v)
+    both = hit & hit64
+    assert np.all(np.abs(t[both] - ref["t"][both]) <= 2e-5 * (1 + ref["t"][both])), \
+        np.abs(t[both] - ref["t"][both]).max()
+
+
 def test_scene_rays_any_hit_and_segments(cpq, cuda):
     from gpurt_cpq import workloads as W
 
