@@ -11,7 +11,6 @@ CUDA stream.
 """
 from __future__ import annotations
 
-import ctypes
 from ctypes import byref, c_int32, c_int64, c_size_t, c_uint32, c_void_p
 from dataclasses import dataclass
 
