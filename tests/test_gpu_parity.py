@@ -499,3 +499,36 @@ def test_refit_moves_vertices(orc, cpq, cuda):
                 pts = v2[t[order[f:f + c]]].reshape(-1, 3)
                 lo, hi = boxes[node, 0::2, s], boxes[node, 1::2, s]
                 assert np.all(pts >= lo) and np.all(pts <= hi)
+
+
+def test_autotuner_picks_valid_options_and_caches(orc, cpq, cuda, tmp_path):
+    """cp_autotune times candidates on the given mesh and queries, returns
+    options the library accepts, writes one line per size class and
+    branching to its cache, and answers a second call from the cache with the
+    same choice; the tuned mesh answers within the FP64 bound."""
+    import time
+
+    from gpurt_cpq import workloads as W
+
+    v, t = W.torus(120, 48)
+    q = W.uniform_queries(200000, -1.5, 1.5, 31)
+    vd, td, qd = dev(v, cuda), dev(t, cuda), dev(q, cuda)
+    cache = tmp_path / "tune.txt"
+    t0 = time.perf_counter()
+    bo, qo = cpq.autotune(vd, td, qd, cache_path=str(cache), branching=4)
+    first = time.perf_counter() - t0
+    assert bo.branching == 4 and 1 <= bo.leaf_size <= 15
+    assert 32 <= qo.block_size <= 256 and qo.block_size % 32 == 0
+    assert qo.traversal in (1, 2)
+    lines = [ln.split() for ln in cache.read_text().splitlines() if ln.strip() and not ln.startswith("#")]
+    assert len(lines) == 1 and int(lines[0][2]) == 4
+    assert (int(lines[0][0]), int(lines[0][1])) == (cpq.lib.cp_size_class(len(t)), cpq.lib.cp_size_class(len(q)))
+    t0 = time.perf_counter()
+    bo2, qo2 = cpq.autotune(vd, td, qd, cache_path=str(cache), branching=4)
+    assert time.perf_counter() - t0 < first
+    assert (bo2.leaf_size, qo2.block_size, qo2.traversal, qo2.short_stack) == \
+        (bo.leaf_size, qo.block_size, qo.traversal, qo.short_stack)
+    m = cpq.Mesh(vd, td, branching=bo.branching, leaf_size=bo.leaf_size)
+    d = m.query(qd[:8192], opts=qo).dist.cpu().numpy()
+    ref = orc.exact_f64(v, t, q[:8192])["dist"]
+    assert (np.abs(d - ref) / ref).max() <= 1e-6
