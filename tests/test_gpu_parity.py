@@ -532,3 +532,44 @@ def test_autotuner_picks_valid_options_and_caches(orc, cpq, cuda, tmp_path):
     d = m.query(qd[:8192], opts=qo).dist.cpu().numpy()
     ref = orc.exact_f64(v, t, q[:8192])["dist"]
     assert (np.abs(d - ref) / ref).max() <= 1e-6
+
+
+def test_timing_and_counters(cpq, cuda):
+    """cp_timing_enable(EVENTS) brackets each traversal launch with events
+    (cp_timing_read: device ms and launch count, reset on read);
+    cp_timing_enable(COUNTERS) runs the counting build, whose per-warp counts
+    are consistent with the query; both off leave nothing recorded."""
+    from ctypes import byref, c_double, c_int64, c_uint64
+
+    from gpurt_cpq import workloads as W
+    from gpurt_cpq._lib import CP_TIMING_COUNTERS, CP_TIMING_EVENTS, lib
+
+    v, t = W.torus(100, 40)
+    q = dev(W.uniform_queries(65536, -1.5, 1.5, 41), cuda)
+    m = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=4, leaf_size=8)
+    o = cpq.query_opts(traversal="packet")
+    ms, n = c_double(), c_int64()
+    counts = (c_uint64 * 7)()
+    try:
+        assert lib.cp_timing_enable(CP_TIMING_EVENTS) == 0
+        lib.cp_timing_read(byref(ms), byref(n), 1)
+        for _ in range(3):
+            m.query(q, opts=o)
+        assert lib.cp_timing_read(byref(ms), byref(n), 1) == 0
+        assert n.value == 3 and ms.value > 0.0
+        assert lib.cp_timing_enable(CP_TIMING_COUNTERS) == 0
+        lib.cp_traversal_stats(counts, 1)
+        r = m.query(q, opts=o)
+        assert lib.cp_traversal_stats(counts, 1) == 0
+        nodes, leaf_tris, pops, skips, lane_tris, rounds, lane_nodes = list(counts)
+        packets = 65536 // 32
+        assert nodes >= packets and pops >= skips and leaf_tris >= rounds > 0
+        assert lane_tris <= 32 * rounds and lane_nodes <= 32 * nodes
+        assert r.dist.isfinite().all()
+        lib.cp_timing_enable(0)
+        lib.cp_timing_read(byref(ms), byref(n), 1)
+        m.query(q, opts=o)
+        lib.cp_timing_read(byref(ms), byref(n), 1)
+        assert n.value == 0
+    finally:
+        lib.cp_timing_enable(0)
