@@ -1,18 +1,29 @@
-// query.cu — closest-point traversal, query ordering and the adjoint kernel.
+// query.cu — closest-point traversal, query ordering, instanced scenes and the
+// adjoint kernel.
 //
 // Replaces the reference's per-pixel traceRayEXT over its TLAS
 // (src/shaders/rt/rt.rgen:257-270) and the slab test hit_bbox
 // (src/shaders/rt/rtcommon.glsl:242-251) with a closest-first descent: a
 // child box is visited only while its squared distance lower bound is below
-// the best squared distance found so far.  Point-triangle distance follows
-// the Voronoi-region method (Ericson 2005, section 5.1.5).
+// the best squared distance found so far.  Candidates are ranked with an FP32
+// point-triangle distance in each triangle's own frame; the winner is
+// re-evaluated in float-float by the Voronoi-region method (Ericson 2005,
+// section 5.1.5).
 //
-// Kernel shape (GB300, 152 SMs): a persistent grid of SMs x resident blocks;
-// each warp takes 32 consecutive (Hilbert-ordered) queries from a global
-// counter, one query per lane, and leaves when the counter runs past the end
-// (warp-uniform exit).  Each thread keeps the top `S` entries of its stack in
-// shared memory (a ring in a per-warp slice, [slot][thread] so a warp's
-// accesses hit 32 distinct banks) and spills older entries to local memory.
+// Kernels (GB300, 152 SMs; each a persistent grid of SMs x resident blocks
+// taking 32 consecutive Hilbert-ordered queries per warp from a global
+// counter, with a warp-uniform exit):
+//   k_traverse_packet  the default: the 32 lanes walk one shared stack in
+//                      shared memory, one entry per wide level;
+//   k_traverse         one query per thread, the top `S` stack entries in
+//                      shared memory ([slot][thread], 32 distinct banks),
+//                      older ones spilled to local memory;
+//   k_instances_packet, k_instances
+//                      the same two shapes over an instanced scene: a top
+//                      level of instance boxes, each instance's mesh walked
+//                      with the query in its object space (or on a world-space
+//                      copy), the winner finished in world space;
+//   k_backward         the adjoint of the distance.
 // Node rows and triangle records are read with 128-bit read-only loads.
 #include <cfloat>
 #include <climits>
