@@ -259,3 +259,26 @@ def test_ray_f32_agrees_with_f64(orc):
     assert same.mean() > 0.99
     both = same & (a["tri"] >= 0)
     np.testing.assert_allclose(a["t"][both], b["t"][both], rtol=1e-5, atol=1e-6)
+
+
+def test_fp64_vertex_brute_forces_match_fp32_vertex_ones(orc):
+    """The FP64-vertex brute forces (for instanced scenes) give the same
+    answers as the FP32-vertex ones when the vertices are FP32 values."""
+    import numpy as np
+
+    from gpurt_cpq import workloads as W
+
+    v, t = W.icosphere(2)
+    rng = np.random.default_rng(3)
+    q = rng.uniform(-2, 2, (2000, 3)).astype(np.float32)
+    a = orc.brute_f64(v, t, q)
+    b = orc.brute_f64_dv(v.astype(np.float64), t, q)
+    np.testing.assert_array_equal(a["tri"], b["tri"])
+    np.testing.assert_array_equal(a["dist"], b["dist"])
+    d = rng.normal(size=(2000, 3)).astype(np.float32)
+    ra = orc.ray_brute(v, t, q, d, fp64=True)
+    rb = orc.ray_brute_f64_dv(v.astype(np.float64), t, q, d)
+    np.testing.assert_array_equal(ra["tri"], rb["tri"])
+    hit = np.isfinite(ra["t"])
+    np.testing.assert_array_equal(ra["t"][hit], rb["t"][hit])
+    assert np.all(~np.isfinite(rb["t"][~hit]))
