@@ -407,6 +407,9 @@ class Scene:
         n = int(origins.shape[0])
         if directions.shape[0] != n:
             raise ValueError("origins and directions must have the same length")
+        if tmax_per_ray is not None and (not tmax_per_ray.is_cuda or tmax_per_ray.dtype != torch.float32
+                                         or tmax_per_ray.numel() != n or not tmax_per_ray.is_contiguous()):
+            raise ValueError("tmax_per_ray must be a contiguous CUDA float32 tensor of one value per ray")
         dev = origins.device
         out = SceneRayResult(t=torch.empty((n,), dtype=torch.float32, device=dev),
                              instance=torch.empty((n,), dtype=torch.int32, device=dev),
