@@ -30,6 +30,16 @@ namespace cpq {
 static std::atomic<uint64_t> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+// Allocations still to succeed before one fails; -1: off.  Firing disarms it.
+static std::atomic<int64_t> g_fail_after{-1};
+bool alloc_fault() {
+    int64_t v = g_fail_after.load(std::memory_order_relaxed);
+    while (v >= 0) {
+        if (g_fail_after.compare_exchange_weak(v, v - 1, std::memory_order_relaxed)) return v == 0;
+    }
+    return false;
+}
+
 namespace {
 struct KernelCache {
     std::mutex mu;
@@ -163,6 +173,7 @@ cudaError_t get_pool(cudaMemPool_t* out) {
 }
 
 cudaError_t ws_alloc(void** p, size_t bytes, cudaStream_t st) {
+    if (alloc_fault()) return cudaErrorMemoryAllocation;
     cudaMemPool_t pool;
     cudaError_t e = get_pool(&pool);
     if (e != cudaSuccess) return e;
@@ -287,6 +298,10 @@ CP_API const char* cp_status_string(cp_status s) {
 CP_API int32_t cp_version(void) { return 100; }
 
 CP_API uint64_t cp_kernel_launches(void) { return g_launches.load(std::memory_order_relaxed); }
+
+CP_API void cp_debug_fail_allocation(int64_t after) {
+    g_fail_after.store(after < 0 ? -1 : after, std::memory_order_relaxed);
+}
 
 CP_API cp_status cp_timing_enable(int32_t flags) {
     if (flags & ~(CP_TIMING_EVENTS | CP_TIMING_COUNTERS))

@@ -572,6 +572,7 @@ cudaError_t dalloc(Bvh& b, T** p, size_t count) {
     *p = nullptr;
     if (count == 0) count = 1;
     size_t bytes = count * sizeof(T);
+    if (alloc_fault()) return cudaErrorMemoryAllocation;
     cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), bytes);
     if (e != cudaSuccess) return e;
     b.allocations.push_back(*p);
@@ -586,6 +587,7 @@ struct TmpAlloc {
     template <typename T>
     cudaError_t get(T** p, size_t count) {
         if (count == 0) count = 1;
+        if (alloc_fault()) return cudaErrorMemoryAllocation;
         cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(p), count * sizeof(T), st);
         if (e == cudaSuccess) ptrs.push_back(*p);
         return e;
@@ -621,9 +623,17 @@ cudaError_t bvh_build(Bvh& b, const float* verts, int64_t vstride, const int32_t
                       const std::vector<int64_t>& h_voff, const std::vector<int64_t>& h_toff,
                       const BuildParams& p, cudaStream_t st, bool* bad_input, std::string* why) {
     *bad_input = false;
-    cudaEvent_t ev0, ev1;
-    CK(cudaEventCreate(&ev0));
-    CK(cudaEventCreate(&ev1));
+    // the two timing events are destroyed on every return path
+    struct Events {
+        cudaEvent_t a = nullptr, b = nullptr;
+        ~Events() {
+            if (a) cudaEventDestroy(a);
+            if (b) cudaEventDestroy(b);
+        }
+    } ev;
+    CK(cudaEventCreate(&ev.a));
+    CK(cudaEventCreate(&ev.b));
+    cudaEvent_t ev0 = ev.a, ev1 = ev.b;
     CK(cudaEventRecord(ev0, st));
     CK(cudaGetDevice(&b.device));
     b.p = p;
@@ -809,8 +819,6 @@ cudaError_t bvh_build(Bvh& b, const float* verts, int64_t vstride, const int32_t
     CK(cudaEventRecord(ev1, st));
     CK(cudaEventSynchronize(ev1));
     cudaEventElapsedTime(&b.build_ms, ev0, ev1);
-    cudaEventDestroy(ev0);
-    cudaEventDestroy(ev1);
     b.num_leaves = h_scr[3];
     return cudaSuccess;
 }

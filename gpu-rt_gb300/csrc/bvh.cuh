@@ -108,6 +108,10 @@ cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int6
 // CUDA-event timing of traversal launches (diagnostic; see cp_timing_enable).
 void timing_enable(bool events, bool counters);
 cudaError_t timing_read(double* ms, int64_t* launches, bool reset);
+// Allocation-failure injection for tests (cp_debug_fail_allocation): true
+// when the library's next device allocation is to fail.
+bool alloc_fault();
+
 // Counters of the counting packet kernel: warp node visits, leaf triangles
 // (per warp leaf visit), stack pops, skipped pops, lane-triangle tests
 // (active lanes x leaf triangles), triangle rounds executed and lane-node

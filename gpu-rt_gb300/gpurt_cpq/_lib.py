@@ -108,6 +108,7 @@ SIGNATURES = {
     "cp_batch_query": (c_int32, [c_void_p, c_void_p, c_void_p, POINTER(QueryOpts), c_void_p,
                                  c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_int32,
                                  c_void_p]),
+    "cp_debug_fail_allocation": (None, [c_int64]),
     "cp_scene_create": (c_int32, [c_void_p, c_void_p, c_void_p, c_int32, c_void_p, POINTER(c_void_p)]),
     "cp_scene_update": (c_int32, [c_void_p, c_void_p, c_void_p]),
     "cp_scene_destroy": (c_int32, [c_void_p]),

@@ -153,6 +153,14 @@ CP_API uint64_t cp_kernel_launches(void);
 #define CP_TIMING_EVENTS 1
 #define CP_TIMING_COUNTERS 2
 CP_API cp_status cp_timing_enable(int32_t flags);
+
+/* Test hook (fault injection on the host): the library's next `after` device
+ * allocations succeed and the one after fails as if the device were out of
+ * memory — the call that made it returns CP_ERROR_OUT_OF_MEMORY, having
+ * released what it held — after which the hook disarms itself; a negative
+ * value disarms it at once.  Covers BVH builds, their temporaries and query
+ * workspaces. */
+CP_API void cp_debug_fail_allocation(int64_t after);
 CP_API cp_status cp_timing_read(double* traverse_ms, int64_t* launches, int32_t reset);
 CP_API cp_status cp_traversal_stats(uint64_t* counts7, int32_t reset);
 

@@ -573,3 +573,52 @@ def test_timing_and_counters(cpq, cuda):
         assert n.value == 0
     finally:
         lib.cp_timing_enable(0)
+
+
+def test_allocation_failures_are_reported_and_release_memory(cpq, cuda):
+    """Host-side fault injection (cp_debug_fail_allocation): a device
+    allocation failing at any point of a build, or in a query's workspace,
+    returns CP_ERROR_OUT_OF_MEMORY through the C ABI and releases what the
+    call held; the hook disarms itself after firing.  The whole sweep runs
+    twice: one-time growth (modules loaded on first use, memory pools) lands
+    in the first pass, a leak would show again in the second."""
+    import torch
+
+    from gpurt_cpq import workloads as W
+    from gpurt_cpq._lib import CP_ERROR_OUT_OF_MEMORY, CpError, lib
+
+    v, t = W.icosphere(3)
+    vd, td = dev(v, cuda), dev(t, cuda)
+    q = dev(W.uniform_queries(4096, -2, 2, 51), cuda)
+    ref = cpq.Mesh(vd, td, branching=4).query(q).dist
+
+    def sweep():
+        failed_at = []
+        for k in range(500):
+            lib.cp_debug_fail_allocation(k)
+            try:
+                m = cpq.Mesh(vd, td, branching=4)
+            except CpError as e:
+                assert e.status == CP_ERROR_OUT_OF_MEMORY, e
+                failed_at.append(k)
+                # the hook fired and disarmed: the next build succeeds untouched
+                cpq.Mesh(vd, td, branching=4).close()
+                continue
+            lib.cp_debug_fail_allocation(-1)
+            break
+        assert len(failed_at) >= 10 and failed_at == list(range(len(failed_at)))
+        lib.cp_debug_fail_allocation(0)
+        with pytest.raises(CpError) as e:
+            m.query(q)  # its workspace comes from the pool: that allocation fails
+        assert e.value.status == CP_ERROR_OUT_OF_MEMORY
+        assert torch.equal(m.query(q).dist, ref)
+        m.close()
+        torch.cuda.synchronize()
+        return torch.cuda.mem_get_info()[0]
+
+    try:
+        first = sweep()
+        second = sweep()
+    finally:
+        lib.cp_debug_fail_allocation(-1)
+    assert abs(second - first) < (16 << 20), (first, second)
