@@ -1,7 +1,9 @@
 """ORACLE — test infrastructure only.
 
 ctypes wrapper of oracle/liboracle.so (cpq_oracle.c): the FP64 closest-point
-checker and the FP32 CPU restatement of the LBVH build and traversal.  Only
+checker and the FP32 CPU restatement of the LBVH build and traversal.  The
+same library holds the shading restatement (shade_oracle.c), whose
+signatures are registered here and wrapped in oracle/shade.py.  Only
 tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may import
 this module; the product never does.
 
@@ -26,7 +28,7 @@ LIB = HERE / "liboracle.so"
 
 def build() -> Path:
     """Compile liboracle.so with the committed Makefile (gcc, no fast-math)."""
-    src = [HERE / "cpq_oracle.c", HERE / "cpq_oracle.h"]
+    src = [HERE / n for n in ("cpq_oracle.c", "cpq_oracle.h", "shade_oracle.c", "shade_oracle.h", "Makefile")]
     if LIB.exists() and all(LIB.stat().st_mtime >= s.stat().st_mtime for s in src):
         return LIB
     subprocess.run(["make", "-s", "-C", str(HERE), "liboracle.so"], check=True)
@@ -93,8 +95,30 @@ def lib():
         L.orc_ray_brute_f64_dv.restype = None
         L.orc_ray_brute_f64_dv.argtypes = [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_int64, c_double,
                                            c_double, c_void_p, c_void_p, c_void_p, c_int]
+        _shade_signatures(L)
         _lib = L
     return _lib
+
+
+def _shade_signatures(L) -> None:
+    """Argument types of the shading restatement (shade_oracle.h)."""
+    P = c_void_p
+    for name, args, res in [
+        ("orc_sh_tea", [c_int64, P, P, P], None),
+        ("orc_sh_lcg_stream", [ctypes.c_uint32, c_int64, P, P], None),
+        ("orc_sh_radical_inverse", [c_int64, P, P], None),
+        ("orc_sh_math", [c_int32, c_int64, P, P, P], None),
+        ("orc_sh_sample", [c_int32, c_int64, ctypes.c_uint32, P, c_float, P, P, P], None),
+        ("orc_sh_material", [c_int32, c_int64, P, c_float, P, P, P, P, P], None),
+        ("orc_sh_triangle_pdf", [c_int64, P, P, P, P], None),
+        ("orc_sh_hit_bbox", [c_int64, P, P, P, P, P], None),
+        ("orc_sh_make_tanspace", [c_int64, P, P, P], None),
+        ("orc_sh_light_pdf", [P, c_int64, P, P, P], None),
+        ("orc_sh_render", [P, P, P, P, P], c_int),
+    ]:
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
 
 
 def nthreads() -> int:

@@ -1,0 +1,197 @@
+"""ORACLE — test infrastructure only.
+
+ctypes wrapper of the FP32 restatement of the reference's path-tracer
+shading math (oracle/shade_oracle.c: rtcommon.glsl, rt.rgen, restir.glsl).
+Only tests/ may import this module; the product never does.
+
+Parity with the reference is unpinned: its shaders run only under Vulkan,
+which this machine cannot bring up, and seed their random numbers from the
+clock (rt.rgen:569).  The tests pin the restatement by hand-checked values
+(random numbers, radical inverse) and by the mathematics the shader
+implements (pdf normalisation, sampler/pdf agreement, unbiased integrators
+agreeing in expectation).
+"""
+from __future__ import annotations
+
+from ctypes import Structure, byref, c_float, c_int32, c_int64, c_uint32, c_void_p
+
+import numpy as np
+
+from . import oracle as _o
+
+# orc_sh_sample kinds
+UNIFORM_HEMISPHERE, COSINE_HEMISPHERE, COSPOW_HEMISPHERE, GGX_SAMPLE, BP_SAMPLE, TRIANGLE_SAMPLE = range(6)
+BLINN_PHONG, GGX = 0, 1
+DIRECT, MATERIAL, MIS, RESTIR_DIRECT, RESTIR = range(5)
+
+
+class ShadeScene(Structure):
+    _fields_ = [("nt", c_int64), ("verts", c_void_p), ("normals", c_void_p), ("obj", c_void_p),
+                ("nobj", c_int32), ("albedo", c_void_p), ("emissive", c_void_p), ("metal_rough", c_void_p)]
+
+
+class ShadeCamera(Structure):
+    _fields_ = [("eye", c_float * 3), ("right", c_float * 3), ("up", c_float * 3), ("fwd", c_float * 3),
+                ("tan_half_y", c_float), ("aspect", c_float), ("width", c_int32), ("height", c_int32)]
+
+
+class ShadeParams(Structure):
+    _fields_ = [("clear", c_float * 3), ("env", c_float * 3), ("samples", c_int32), ("max_depth", c_int32),
+                ("qmc", c_int32), ("integrator", c_int32), ("brdf", c_int32), ("use_rr", c_int32),
+                ("use_metalness", c_int32), ("frame", c_int32), ("max_frame", c_int32),
+                ("new_samples", c_int32), ("temporal_multiplier", c_int32), ("seed", c_uint32)]
+
+
+def _L():
+    return _o.lib()
+
+
+def _p(a):
+    return _o._p(a)
+
+
+def _v3(a):
+    return np.ascontiguousarray(np.asarray(a, np.float32).reshape(-1, 3))
+
+
+def tea(v0, v1) -> np.ndarray:
+    a = np.ascontiguousarray(v0, np.uint32)
+    b = np.ascontiguousarray(v1, np.uint32)
+    out = np.empty(a.shape[0], np.uint32)
+    _L().orc_sh_tea(a.shape[0], _p(a), _p(b), _p(out))
+    return out
+
+
+def lcg_stream(seed: int, n: int):
+    u = np.empty(n, np.uint32)
+    f = np.empty(n, np.float32)
+    _L().orc_sh_lcg_stream(seed, n, _p(u), _p(f))
+    return u, f
+
+
+def radical_inverse(bits) -> np.ndarray:
+    b = np.ascontiguousarray(bits, np.uint32)
+    out = np.empty(b.shape[0], np.float32)
+    _L().orc_sh_radical_inverse(b.shape[0], _p(b), _p(out))
+    return out
+
+
+def _math(kind, x, y=None):
+    xx = np.ascontiguousarray(x, np.float32)
+    yy = np.ascontiguousarray(y if y is not None else np.zeros_like(xx), np.float32)
+    out = np.empty(xx.shape[0], np.float32)
+    _L().orc_sh_math(kind, xx.shape[0], _p(xx), _p(yy), _p(out))
+    return out
+
+
+def sin(x):
+    return _math(0, x)
+
+
+def cos(x):
+    return _math(1, x)
+
+
+def pow(x, y):  # noqa: A001 - the restatement's own pow
+    return _math(2, x, y)
+
+
+def sample(kind: int, n: int, seed: int, frame, param: float = 0.0, wo=None):
+    """n draws of one sampler from one lcg stream: (directions or barycentrics, ok)."""
+    f = np.ascontiguousarray(np.asarray(frame, np.float32).reshape(9))
+    w = None if wo is None else np.ascontiguousarray(np.asarray(wo, np.float32).reshape(3))
+    dirs = np.empty((n, 3), np.float32)
+    ok = np.empty(n, np.uint8)
+    _L().orc_sh_sample(kind, n, seed, _p(f), param, _p(w), _p(dirs), _p(ok))
+    return dirs, ok.astype(bool)
+
+
+def material(brdf: int, albedo, roughness: float, wo, frame, wi):
+    """(pdf, eval) of MAT_pdf / MAT_eval for directions wi at one shading point."""
+    a = np.ascontiguousarray(np.asarray(albedo, np.float32).reshape(3))
+    w = np.ascontiguousarray(np.asarray(wo, np.float32).reshape(3))
+    f = np.ascontiguousarray(np.asarray(frame, np.float32).reshape(9))
+    d = _v3(wi)
+    pdf = np.empty(d.shape[0], np.float32)
+    ev = np.empty((d.shape[0], 3), np.float32)
+    _L().orc_sh_material(brdf, d.shape[0], _p(a), roughness, _p(w), _p(f), _p(d), _p(pdf), _p(ev))
+    return pdf, ev
+
+
+def triangle_pdf(o, d, tri) -> np.ndarray:
+    oo, dd = _v3(o), _v3(d)
+    t = np.ascontiguousarray(np.asarray(tri, np.float32).reshape(9))
+    out = np.empty(oo.shape[0], np.float32)
+    _L().orc_sh_triangle_pdf(oo.shape[0], _p(oo), _p(dd), _p(t), _p(out))
+    return out
+
+
+def hit_bbox(o, d, bmin, bmax) -> np.ndarray:
+    oo, dd = _v3(o), _v3(d)
+    lo = np.ascontiguousarray(np.asarray(bmin, np.float32).reshape(3))
+    hi = np.ascontiguousarray(np.asarray(bmax, np.float32).reshape(3))
+    out = np.empty(oo.shape[0], np.uint8)
+    _L().orc_sh_hit_bbox(oo.shape[0], _p(oo), _p(dd), _p(lo), _p(hi), _p(out))
+    return out.astype(bool)
+
+
+def make_tanspace(n):
+    nn = _v3(n)
+    t = np.empty_like(nn)
+    b = np.empty_like(nn)
+    _L().orc_sh_make_tanspace(nn.shape[0], _p(nn), _p(t), _p(b))
+    return t, b
+
+
+class Scene:
+    """World-space triangles with per-vertex normals and one constant material
+    per object (albedo, emission, metalness, roughness); an object whose
+    emission has a component above zero is a light.  Objects' triangles are
+    contiguous."""
+
+    def __init__(self, verts, normals, obj, albedo, emissive, metal_rough):
+        self.verts = np.ascontiguousarray(np.asarray(verts, np.float32).reshape(-1, 9))
+        self.normals = np.ascontiguousarray(np.asarray(normals, np.float32).reshape(-1, 9))
+        self.obj = np.ascontiguousarray(obj, np.int32)
+        self.albedo = np.ascontiguousarray(np.asarray(albedo, np.float32).reshape(-1, 3))
+        self.emissive = np.ascontiguousarray(np.asarray(emissive, np.float32).reshape(-1, 3))
+        self.metal_rough = np.ascontiguousarray(np.asarray(metal_rough, np.float32).reshape(-1, 2))
+        self._s = ShadeScene(self.verts.shape[0], self.verts.ctypes.data, self.normals.ctypes.data,
+                             self.obj.ctypes.data, self.albedo.shape[0], self.albedo.ctypes.data,
+                             self.emissive.ctypes.data, self.metal_rough.ctypes.data)
+
+    def light_pdf(self, p, d) -> np.ndarray:
+        pp, dd = _v3(p), _v3(d)
+        out = np.empty(pp.shape[0], np.float32)
+        _L().orc_sh_light_pdf(byref(self._s), pp.shape[0], _p(pp), _p(dd), _p(out))
+        return out
+
+    def render(self, camera: ShadeCamera, *, integrator=DIRECT, brdf=BLINN_PHONG, samples=8, max_depth=8,
+               use_rr=True, qmc=False, use_metalness=False, frame=0, max_frame=256, new_samples=4,
+               temporal_multiplier=16, clear=(0.3, 0.3, 0.3), env=(0.0, 0.0, 0.0), seed=1, image=None,
+               gbuffer=False):
+        """One frame, the reference's defaults unless given (rt.h:38-53;
+        env_scale 0).  Returns the image (height, width, 3) and, if asked,
+        the first-hit buffer (height, width, 9)."""
+        p = ShadeParams((c_float * 3)(*clear), (c_float * 3)(*env), samples, max_depth, int(qmc), integrator,
+                        brdf, int(use_rr), int(use_metalness), frame, max_frame, new_samples,
+                        temporal_multiplier, seed)
+        img = np.zeros((camera.height, camera.width, 3), np.float32) if image is None else image
+        assert img.dtype == np.float32 and img.flags.c_contiguous and img.shape == (camera.height, camera.width, 3)
+        g = np.zeros((camera.height, camera.width, 9), np.float32) if gbuffer else None
+        rc = _L().orc_sh_render(byref(self._s), byref(camera), byref(p), _p(img), _p(g))
+        if rc != 0:
+            raise ValueError("orc_sh_render refused its arguments")
+        return (img, g) if gbuffer else img
+
+
+def camera(eye, target, up, yfov: float, width: int, height: int) -> ShadeCamera:
+    """Pinhole camera at eye looking at target (row 0 at the top)."""
+    e = np.asarray(eye, np.float64)
+    f = np.asarray(target, np.float64) - e
+    f /= np.linalg.norm(f)
+    r = np.cross(f, np.asarray(up, np.float64))
+    r /= np.linalg.norm(r)
+    u = np.cross(r, f)
+    c3 = lambda v: (c_float * 3)(*[float(x) for x in v])  # noqa: E731
+    return ShadeCamera(c3(e), c3(r), c3(u), c3(f), float(np.tan(0.5 * yfov)), width / height, width, height)

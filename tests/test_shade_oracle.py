@@ -1,0 +1,348 @@
+"""The shading restatement (oracle/shade_oracle.c) against known answers and
+the mathematics the reference's shaders implement (rtcommon.glsl, rt.rgen,
+restir.glsl).
+
+The shaders cannot run here (Vulkan), so parity with the reference itself is
+unpinned; these tests pin the restatement instead:
+  - random numbers: TEA and the lcg against an independent Python
+    restatement, the radical inverse against hand values;
+  - the restatement's own sin / cos / pow within 2 ulp of FP64;
+  - samplers: unit directions in the right hemisphere with the analytic
+    moments of their densities;
+  - materials: each pdf integrates over the upper hemisphere to its
+    sampler's acceptance rate, and the sampler's directions reproduce the
+    pdf (E[g(wi)] against quadrature of g * pdf), for Blinn-Phong and GGX;
+  - triangle and light pdfs integrate to 1 over the sphere;
+  - integrators: direct lighting, material sampling and MIS (and ReSTIR's
+    direct-only mode) estimate the same image of a floor under an area light,
+    with and without Russian roulette; a mirror floor reflects the light
+    exactly.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from oracle import shade as S
+
+FRAME = np.array([[1, 0, 0], [0, 1, 0], [0, 0, 1]], np.float32)  # T, B, N = x, y, z
+
+
+# ---------------------------------------------------------------- random numbers
+
+def _tea_py(v0: int, v1: int) -> int:
+    m = 0xFFFFFFFF
+    s0 = 0
+    for _ in range(16):
+        s0 = (s0 + 0x9E3779B9) & m
+        v0 = (v0 + ((((v1 << 4) & m) + 0xA341316C) ^ ((v1 + s0) & m) ^ ((v1 >> 5) + 0xC8013EA4))) & m
+        v1 = (v1 + ((((v0 << 4) & m) + 0xAD90777D) ^ ((v0 + s0) & m) ^ ((v0 >> 5) + 0x7E95761E))) & m
+    return v0
+
+
+def test_tea_matches_python_restatement():
+    rng = np.random.default_rng(5)
+    a = rng.integers(0, 2**32, 200, dtype=np.uint64).astype(np.uint32)
+    b = rng.integers(0, 2**32, 200, dtype=np.uint64).astype(np.uint32)
+    a[:3] = [0, 1, 0xFFFFFFFF]
+    b[:3] = [0, 0, 0xFFFFFFFF]
+    got = S.tea(a, b)
+    assert [int(x) for x in got] == [_tea_py(int(x), int(y)) for x, y in zip(a, b)]
+
+
+def test_lcg_stream():
+    u, f = S.lcg_stream(0, 4)
+    s, want = 0, []
+    for _ in range(4):
+        s = (1664525 * s + 1013904223) % 2**32
+        want.append(s & 0xFFFFFF)
+    assert u.tolist() == want
+    assert want[0] == 1013904223 & 0xFFFFFF
+    np.testing.assert_array_equal(f, np.asarray(want, np.float32) / np.float32(2**24))
+    # randf lies in [0, 1) for every state of a long stream
+    _, f = S.lcg_stream(12345, 1 << 16)
+    assert f.min() >= 0.0 and f.max() < 1.0
+
+
+def test_radical_inverse_known_values():
+    got = S.radical_inverse([0, 1, 2, 3, 4, 5, 0x80000000, 0xFFFFFFFF])
+    np.testing.assert_array_equal(got, np.float32([0.0, 0.5, 0.25, 0.75, 0.125, 0.625, 2.0**-32, 1.0]))
+
+
+# ------------------------------------------------------------------ own math
+
+def test_sin_cos_within_two_ulp():
+    x = np.linspace(0.0, 6.3, 200001, dtype=np.float32)
+    x = np.concatenate([x, np.float32(2.0 * 3.141592) * np.random.default_rng(2).random(50000, np.float32)])
+    for got, ref in ((S.sin(x), np.sin(x.astype(np.float64))), (S.cos(x), np.cos(x.astype(np.float64)))):
+        ulp = np.spacing(np.maximum(np.abs(ref), 2.0**-24).astype(np.float32)).astype(np.float64)
+        assert (np.abs(got - ref) / ulp).max() <= 2.0
+
+
+def test_pow_within_two_ulp():
+    rng = np.random.default_rng(3)
+    x = rng.random(200000, np.float32)
+    y = np.concatenate([rng.random(100000, np.float32) * 200.0, np.float32(1.0) / (rng.random(100000, np.float32)
+                                                                                    * 100.0 + 1.0)])
+    ref = np.power(x.astype(np.float64), y.astype(np.float64))
+    got = S.pow(x, y)
+    keep = ref > 1e-30
+    ulp = np.spacing(ref[keep].astype(np.float32)).astype(np.float64)
+    assert (np.abs(got[keep] - ref[keep]) / ulp).max() <= 2.0
+    assert S.pow(np.float32([0.0, 0.0, 1.0, 0.5]), np.float32([5.0, 0.25, 7.0, 1.0])).tolist() == [0.0, 0.0, 1.0,
+                                                                                                   0.5]
+
+
+# ------------------------------------------------------------------ samplers
+
+N_SAMP = 200000
+
+
+def _se(x):
+    return x.std() / np.sqrt(len(x))
+
+
+@pytest.mark.parametrize("kind,param,axis,mean", [
+    (S.UNIFORM_HEMISPHERE, 0.0, 1, 0.5),        # cos theta uniform, about the frame's y axis
+    (S.COSINE_HEMISPHERE, 0.0, 2, 2.0 / 3.0),
+    (S.COSPOW_HEMISPHERE, 3.0, 2, 4.0 / 5.0),   # E[cos] = (e + 1) / (e + 2)
+    (S.COSPOW_HEMISPHERE, 20.0, 2, 21.0 / 22.0),
+])
+def test_hemisphere_samplers(kind, param, axis, mean):
+    d, ok = S.sample(kind, N_SAMP, 77, FRAME, param)
+    assert ok.all()
+    np.testing.assert_allclose(np.linalg.norm(d, axis=1), 1.0, atol=2e-6)
+    c = d[:, axis].astype(np.float64)
+    assert c.min() >= 0.0
+    assert abs(c.mean() - mean) < 5 * _se(c)
+    # azimuth uniform: the two other components average to zero
+    for k in {0, 1, 2} - {axis}:
+        assert abs(d[:, k].mean()) < 5 * _se(d[:, k].astype(np.float64))
+
+
+def test_triangle_sample_uniform():
+    b, ok = S.sample(S.TRIANGLE_SAMPLE, N_SAMP, 9, FRAME)
+    assert ok.all() and b.min() >= -1e-7
+    np.testing.assert_allclose(b.sum(1), 1.0, atol=1e-6)
+    for k in range(3):
+        assert abs(b[:, k].mean() - 1.0 / 3.0) < 5 * _se(b[:, k].astype(np.float64))
+        # second moment of a barycentric under the uniform density: 1/6
+        assert abs((b[:, k].astype(np.float64) ** 2).mean() - 1.0 / 6.0) < 5 * _se(b[:, k].astype(np.float64) ** 2)
+
+
+def _hemisphere_grid(n_cos=1024, n_phi=1024):
+    c = (np.arange(n_cos) + 0.5) / n_cos
+    p = (np.arange(n_phi) + 0.5) / n_phi * 2 * np.pi
+    C, P = np.meshgrid(c, p, indexing="ij")
+    s = np.sqrt(1 - C * C)
+    w = np.stack([s * np.cos(P), s * np.sin(P), C], -1).reshape(-1, 3)
+    return w.astype(np.float32), (1.0 / n_cos) * (2 * np.pi / n_phi)
+
+
+WO = np.float32([0.45, -0.2, -0.87])  # incoming direction (towards the surface)
+WO = WO / np.linalg.norm(WO)
+
+
+@pytest.mark.parametrize("brdf,rough", [(S.BLINN_PHONG, 0.5), (S.BLINN_PHONG, 0.15), (S.GGX, 0.6), (S.GGX, 0.35)])
+def test_material_pdf_matches_its_sampler(brdf, rough):
+    kind = S.BP_SAMPLE if brdf == S.BLINN_PHONG else S.GGX_SAMPLE
+    d, ok = S.sample(kind, N_SAMP, 1234, FRAME, rough, wo=WO)
+    grid, dw = _hemisphere_grid()
+    pdf, ev = S.material(brdf, [1, 1, 1], rough, WO, FRAME, grid)
+    pdf = pdf.astype(np.float64)
+    # the pdf over the upper hemisphere integrates to the sampler's acceptance rate
+    acc = ok.mean()
+    se_acc = np.sqrt(acc * (1 - acc) / N_SAMP) + 1e-4
+    assert abs(pdf.sum() * dw - acc) < 5 * se_acc + 2e-3
+    # and the accepted directions follow it: E[g(wi) 1{ok}] = integral of g pdf
+    for g in (lambda w: w[:, 2], lambda w: w[:, 0] ** 2, lambda w: w[:, 0] * w[:, 1] + w[:, 2] ** 3):
+        est = np.where(ok, g(d.astype(np.float64)), 0.0)
+        quad = (g(grid.astype(np.float64)) * pdf).sum() * dw
+        assert abs(est.mean() - quad) < 5 * _se(est) + 2e-3
+    # the throughput of a sampled bounce, eval / pdf, averages to the hemisphere integral of eval
+    p_s, e_s = S.material(brdf, [1, 1, 1], rough, WO, FRAME, d[ok])
+    keep = p_s > 0
+    tp = np.zeros(N_SAMP)
+    tp[np.flatnonzero(ok)[keep]] = e_s[keep, 0] / p_s[keep]
+    assert abs(tp.mean() - ev[:, 0].astype(np.float64).sum() * dw) < 5 * _se(tp) + 2e-3
+    # energy: no material returns more than arrives
+    assert ev[:, 0].astype(np.float64).sum() * dw <= 1.0 + 1e-2
+
+
+def test_materials_vanish_below_the_surface():
+    w = np.float32([[0.3, 0.1, -0.5], [0.0, 0.0, -1.0]])
+    for brdf in (S.BLINN_PHONG, S.GGX):
+        pdf, ev = S.material(brdf, [0.5, 0.6, 0.7], 0.4, WO, FRAME, w)
+        assert (pdf == 0).all() and (ev == 0).all()
+        # and above it when the view comes from below
+        pdf, ev = S.material(brdf, [0.5, 0.6, 0.7], 0.4, -WO, FRAME, np.float32([[0, 0, 1]]))
+        assert (pdf == 0).all() and (ev == 0).all()
+
+
+def test_blinn_phong_eval_is_albedo_times_pdf():
+    grid, _ = _hemisphere_grid(64, 64)
+    pdf, ev = S.material(S.BLINN_PHONG, [0.25, 0.5, 0.75], 0.3, WO, FRAME, grid)
+    np.testing.assert_array_equal(ev, np.float32([0.25, 0.5, 0.75]) * pdf[:, None])
+
+
+# ---------------------------------------------------------- triangles, boxes, frames
+
+def _sphere_dirs(n, seed):
+    v = np.random.default_rng(seed).normal(size=(n, 3))
+    return (v / np.linalg.norm(v, axis=1, keepdims=True)).astype(np.float32)
+
+
+def test_triangle_pdf_integrates_to_one():
+    tri = np.float32([[-0.4, 0.5, -0.3], [0.6, 0.6, -0.2], [0.1, 0.4, 0.7]])
+    n = 400000
+    d = _sphere_dirs(n, 11)
+    pdf = S.triangle_pdf(np.zeros((n, 3), np.float32), d, tri).astype(np.float64)
+    est = pdf * 4 * np.pi
+    assert abs(est.mean() - 1.0) < 5 * _se(est)
+
+
+def test_hit_bbox_against_fp64_slabs():
+    rng = np.random.default_rng(21)
+    n = 20000
+    o = (rng.random((n, 3)) * 4 - 2).astype(np.float32)
+    d = _sphere_dirs(n, 22)
+    lo, hi = np.float32([-0.5, -0.3, -0.4]), np.float32([0.6, 0.2, 0.5])
+    got = S.hit_bbox(o, d, lo, hi)
+    o64, d64 = o.astype(np.float64), d.astype(np.float64)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        t0, t1 = (lo - o64) / d64, (hi - o64) / d64
+    tn = np.maximum(np.fmin(t0, t1).max(1), 0.0)
+    tf = np.fmax(t0, t1).min(1)
+    clear = np.abs(tn - tf) > 1e-4  # away from grazing cases
+    assert clear.mean() > 0.95
+    np.testing.assert_array_equal(got[clear], (tn <= tf)[clear])
+    assert got.any() and not got.all()
+
+
+def test_make_tanspace_orthonormal():
+    n = _sphere_dirs(5000, 31)
+    n[:4] = [[1, 0, 0], [0, 1, 0], [0, 0, -1], [0.6, 0.8, 0]]
+    t, b = S.make_tanspace(n)
+    for a in (t, b):
+        np.testing.assert_allclose(np.linalg.norm(a, axis=1), 1.0, atol=1e-6)
+    for x, y in ((t, n), (b, n), (t, b)):
+        assert np.abs((x * y).sum(1)).max() < 1e-6
+    np.testing.assert_allclose(b, np.cross(n, t), atol=1e-6)
+
+
+# ------------------------------------------------------------------- scenes
+
+def _quad(y, half, up, x0=0.0, z0=0.0):
+    """Two triangles of the square |x - x0|, |z - z0| <= half at height y,
+    wound so their geometric normal is +y (up) or -y."""
+    a, b = [x0 - half, y, z0 - half], [x0 + half, y, z0 - half]
+    c, d = [x0 + half, y, z0 + half], [x0 - half, y, z0 + half]
+    tris = [[a, d, c], [a, c, b]] if up else [[a, b, c], [a, c, d]]
+    n = [0, 1, 0] if up else [0, -1, 0]
+    return np.float32(tris), np.float32([[n] * 3] * 2)
+
+
+def floor_and_light(rough=0.5, albedo=(0.8, 0.7, 0.6), light_e=(6.0, 6.0, 6.0)):
+    fv, fn = _quad(0.0, 1.0, True)
+    lv, ln = _quad(1.0, 0.25, False, x0=0.2)
+    return S.Scene(np.concatenate([fv, lv]), np.concatenate([fn, ln]), [0, 0, 1, 1],
+                   albedo=[albedo, (0, 0, 0)], emissive=[(0, 0, 0), light_e], metal_rough=[(0, rough), (0, 0.5)])
+
+
+CAM = S.camera(eye=(0.0, 0.9, 1.6), target=(0.0, 0.0, 0.0), up=(0, 1, 0), yfov=0.9, width=12, height=9)
+
+
+def test_light_pdf_integrates_to_one():
+    sc = floor_and_light()
+    n = 400000
+    d = _sphere_dirs(n, 41)
+    p = np.tile(np.float32([0.1, 0.0, 0.2]), (n, 1))
+    est = sc.light_pdf(p, d).astype(np.float64) * 4 * np.pi
+    assert abs(est.mean() - 1.0) < 5 * _se(est)
+
+
+def _rows(sc, seeds, **kw):
+    """Per-seed renders reduced to the mean of each image row (channel 0)."""
+    return np.stack([sc.render(CAM, seed=s, **kw)[..., 0].mean(1) for s in seeds]).astype(np.float64)
+
+
+@pytest.mark.parametrize("brdf", [S.BLINN_PHONG, S.GGX])
+def test_integrators_agree_on_direct_lighting(brdf):
+    """Floor under an area light, nothing to bounce off twice: direct
+    lighting, material sampling to depth 2, MIS to depth 2 (and to depth 8
+    with Russian roulette) and ReSTIR's direct-only mode all estimate the
+    same image.  Compared per image row and over the whole image, each
+    against the standard error of the per-seed means."""
+    sc = floor_and_light()
+    seeds = range(1, 9)
+    ref = _rows(sc, seeds, integrator=S.DIRECT, brdf=brdf, samples=96, use_rr=False)
+    assert ref.mean(0).max() > 0.05  # the floor is lit
+    for integ, depth, rr in ((S.MATERIAL, 2, False), (S.MIS, 2, False), (S.MIS, 8, True),
+                             (S.RESTIR_DIRECT, 8, False)):
+        got = _rows(sc, seeds, integrator=integ, brdf=brdf, samples=96, max_depth=depth, use_rr=rr)
+        n = len(seeds)
+        se = np.sqrt(ref.var(0, ddof=1) / n + got.var(0, ddof=1) / n)
+        lit = se > 0  # rows of the floor; the rows of clear colour are exact in both
+        np.testing.assert_array_equal(got.mean(0)[~lit], ref.mean(0)[~lit])
+        z = np.abs(got.mean(0) - ref.mean(0))[lit] / se[lit]
+        assert z.max() < 5.0, (integ, depth, rr, z)
+        whole_se = np.sqrt(ref.mean(1).var(ddof=1) / n + got.mean(1).var(ddof=1) / n)
+        assert abs(got.mean() - ref.mean()) < 5 * whole_se, (integ, depth, rr)
+
+
+def test_primary_misses_and_emitters():
+    sc = floor_and_light()
+    cam = S.camera(eye=(0.2, 0.5, 0.0), target=(0.2, 2.0, 0.0), up=(0, 0, 1), yfov=0.3, width=4, height=4)
+    img = sc.render(cam, integrator=S.DIRECT, samples=2, clear=(0.1, 0.2, 0.3))
+    # looking straight up at the light: every pixel sees its emission
+    np.testing.assert_array_equal(img, np.full((4, 4, 3), 6.0, np.float32))
+    cam = S.camera(eye=(0.0, 0.5, 0.0), target=(0.0, 0.5, 5.0), up=(0, 1, 0), yfov=0.2, width=4, height=4)
+    for integ in (S.DIRECT, S.MATERIAL, S.MIS, S.RESTIR):
+        img = sc.render(cam, integrator=integ, samples=2, clear=(0.1, 0.2, 0.3))
+        np.testing.assert_array_equal(img, np.broadcast_to(np.float32([0.1, 0.2, 0.3]), (4, 4, 3)))
+
+
+def test_mirror_floor_reflects_the_light_exactly():
+    sc = floor_and_light(rough=0.0, albedo=(0.5, 0.25, 1.0))
+    # the mirror image of the light (centre (0.2, 1, 0)) is at (0.2, -1, 0)
+    cam = S.camera(eye=(0.2, 0.4, 0.0), target=(0.2, -1.0, 0.0), up=(0, 0, 1), yfov=0.1, width=3, height=3)
+    img = sc.render(cam, integrator=S.MATERIAL, samples=1, max_depth=3, use_rr=False)
+    np.testing.assert_allclose(img, np.broadcast_to(np.float32([3.0, 1.5, 6.0]), (3, 3, 3)), rtol=1e-6)
+
+
+def test_render_is_deterministic_and_blends_frames():
+    sc = floor_and_light()
+    a = sc.render(CAM, integrator=S.MIS, samples=4, seed=7)
+    b = sc.render(CAM, integrator=S.MIS, samples=4, seed=7)
+    np.testing.assert_array_equal(a, b)
+    c = sc.render(CAM, integrator=S.MIS, samples=4, seed=8)
+    assert not np.array_equal(a, c)
+    # frame 1 blends half and half into the previous image: rendered onto
+    # zeros it leaves half its own average, onto `a` that plus half of `a`
+    img = a.copy()
+    half_new = sc.render(CAM, integrator=S.MIS, samples=4, seed=9, frame=1)
+    sc.render(CAM, integrator=S.MIS, samples=4, seed=9, frame=1, image=img)
+    np.testing.assert_array_equal(img, a * np.float32(0.5) + half_new)
+
+
+def test_gbuffer_holds_first_hit():
+    sc = floor_and_light()
+    img, g = sc.render(CAM, integrator=S.DIRECT, samples=1, gbuffer=True)
+    hit = np.abs(g[..., 3:6]).sum(-1) > 0
+    assert hit.any()
+    np.testing.assert_allclose(np.linalg.norm(g[hit][:, 3:6], axis=1), 1.0, atol=1e-6)
+    on_floor = hit & (np.abs(g[..., 1]) < 1e-6)
+    np.testing.assert_allclose(g[on_floor][:, 6:9], np.broadcast_to(np.float32([0.8, 0.7, 0.6]),
+                                                                     (on_floor.sum(), 3)))
+
+
+def test_render_refuses_bad_arguments():
+    sc = floor_and_light()
+    for kw in ({"integrator": 5}, {"brdf": 2}, {"samples": 0}, {"qmc": True, "max_frame": 0}):
+        with pytest.raises(ValueError):
+            sc.render(CAM, **kw)
+    dark = S.Scene(*[a for a in (_quad(0.0, 1.0, True))], [0, 0], albedo=[(1, 1, 1)], emissive=[(0, 0, 0)],
+                   metal_rough=[(0, 0.5)])
+    with pytest.raises(ValueError):  # light sampling with no light
+        dark.render(CAM, integrator=S.DIRECT)
+    dark.render(CAM, integrator=S.MATERIAL, samples=1)  # material sampling needs none
