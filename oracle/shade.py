@@ -96,6 +96,22 @@ def pow(x, y):  # noqa: A001 - the restatement's own pow
     return _math(2, x, y)
 
 
+def exp(x):
+    return _math(3, x)
+
+
+FILMIC, EXPONENTIAL, NO_TONEMAP = range(3)
+
+
+def tonemap(img, kind: int = EXPONENTIAL, exposure: float = 1.0, gamma: float = 2.2) -> np.ndarray:
+    """tonemap.frag per colour component; defaults as effect.h:25-27."""
+    a = np.ascontiguousarray(img, np.float32)
+    out = np.empty_like(a)
+    if _L().orc_sh_tonemap(kind, exposure, gamma, a.size, _p(a), _p(out)) != 0:
+        raise ValueError("unknown tone mapping")
+    return out
+
+
 def sample(kind: int, n: int, seed: int, frame, param: float = 0.0, wo=None):
     """n draws of one sampler from one lcg stream: (directions or barycentrics, ok)."""
     f = np.ascontiguousarray(np.asarray(frame, np.float32).reshape(9))

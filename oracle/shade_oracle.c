@@ -88,8 +88,35 @@ static inline float sh_cos(float x) {
  * ln m = 2 atanh(s), s = (m - 1) / (m + 1), |s| < 0.172, summed to s^15;
  * 2^t = 2^k e^(f ln 2), k = nearest integer to t, |f| <= 1/2, Taylor to
  * degree 13.  Both series truncate below 1e-15 relative. */
+static const double kLn2 = 0.69314718055994530942;
+
+/* 2^t in FP64: 2^k e^((t - k) ln 2), k the nearest integer to t, the
+ * exponential's Taylor series to degree 13 (|(t - k) ln 2| <= 0.35) */
+static double sh_exp2_d(double t) {
+    static const double kInvFact[14] = {1.0,
+                                        1.0,
+                                        1.0 / 2.0,
+                                        1.0 / 6.0,
+                                        1.0 / 24.0,
+                                        1.0 / 120.0,
+                                        1.0 / 720.0,
+                                        1.0 / 5040.0,
+                                        1.0 / 40320.0,
+                                        1.0 / 362880.0,
+                                        1.0 / 3628800.0,
+                                        1.0 / 39916800.0,
+                                        1.0 / 479001600.0,
+                                        1.0 / 6227020800.0};
+    if (t > 200.0) return INFINITY;
+    if (t < -200.0) return 0.0;
+    const double k = nearbyint(t);
+    const double g = (t - k) * kLn2;
+    double p = kInvFact[13];
+    for (int j = 12; j >= 0; --j) p = kInvFact[j] + g * p;
+    return ldexp(p, (int)k);
+}
+
 static float sh_pow(float xf, float yf) {
-    const double kLn2 = 0.69314718055994530942;
     if (xf != xf || yf != yf) return NAN;
     if (xf < 0.0f) return NAN;
     if (xf == 0.0f) return yf > 0.0f ? 0.0f : (yf == 0.0f ? 1.0f : INFINITY);
@@ -107,26 +134,13 @@ static float sh_pow(float xf, float yf) {
     for (int j = 13; j >= 1; j -= 2) series = 1.0 / (double)j + s2 * series;
     const double lnm = 2.0 * s * series;
     const double t = (double)yf * ((double)e + lnm / kLn2);
-    if (t > 200.0) return INFINITY;
-    if (t < -200.0) return 0.0f;
-    const double k = nearbyint(t);
-    const double g = (t - k) * kLn2;
-    double p = 1.0 / 6227020800.0; /* 1/13! */
-    static const double kInvFact[13] = {1.0,
-                                        1.0,
-                                        1.0 / 2.0,
-                                        1.0 / 6.0,
-                                        1.0 / 24.0,
-                                        1.0 / 120.0,
-                                        1.0 / 720.0,
-                                        1.0 / 5040.0,
-                                        1.0 / 40320.0,
-                                        1.0 / 362880.0,
-                                        1.0 / 3628800.0,
-                                        1.0 / 39916800.0,
-                                        1.0 / 479001600.0};
-    for (int j = 12; j >= 0; --j) p = kInvFact[j] + g * p;
-    return (float)ldexp(p, (int)k);
+    return (float)sh_exp2_d(t);
+}
+
+/* e^x = 2^(x / ln 2) in FP64, rounded once */
+static float sh_exp(float x) {
+    if (x != x) return NAN;
+    return (float)sh_exp2_d((double)x / kLn2);
 }
 
 /* ===================================================================== */
@@ -889,6 +903,26 @@ static void render_pixel(const ctx_t* c, const orc_shade_camera* cam, int x, int
 }
 
 /* ===================================================================== */
+/* tone mapping (tonemap.frag)                                            */
+/* ===================================================================== */
+
+/* Hable's filmic curve with the shader's constants (tonemap.frag:16-25) */
+static float filmic(float c) {
+    const float A = 0.15f, B = 0.50f, C = 0.10f, D = 0.20f, E = 0.02f, F = 0.30f;
+    return ((c * (A * c + C * B) + D * E) / (c * (A * c + B) + D * F)) - E / F;
+}
+
+/* type 0 filmic (tonemap.frag:27-31), 1 exponential (:33-37), 2 none */
+static float tonemap1(int type, float c, float exposure, float gamma) {
+    if (type == 0) {
+        const float w = 1.0f / filmic(11.2f);
+        return sh_pow(filmic(c * exposure) * w, 1.0f / gamma);
+    }
+    if (type == 1) return sh_pow(1.0f - sh_exp(-c * exposure), 1.0f / gamma);
+    return c;
+}
+
+/* ===================================================================== */
 /* exported batch entry points                                            */
 /* ===================================================================== */
 
@@ -910,7 +944,13 @@ void orc_sh_radical_inverse(int64_t n, const uint32_t* bits, float* out) {
 
 void orc_sh_math(int32_t kind, int64_t n, const float* x, const float* y, float* out) {
     for (int64_t i = 0; i < n; ++i)
-        out[i] = kind == 0 ? sh_sin(x[i]) : kind == 1 ? sh_cos(x[i]) : sh_pow(x[i], y[i]);
+        out[i] = kind == 0 ? sh_sin(x[i]) : kind == 1 ? sh_cos(x[i]) : kind == 2 ? sh_pow(x[i], y[i]) : sh_exp(x[i]);
+}
+
+int orc_sh_tonemap(int32_t type, float exposure, float gamma, int64_t n, const float* in, float* out) {
+    if (type < 0 || type > 2 || n < 0) return -1;
+    for (int64_t i = 0; i < n; ++i) out[i] = tonemap1(type, in[i], exposure, gamma);
+    return 0;
 }
 
 void orc_sh_sample(int32_t kind, int64_t n, uint32_t seed, const float* frame9, float param, const float* wo,

@@ -6,11 +6,11 @@
  * hemisphere / lobe / triangle samplers, the Blinn-Phong and GGX materials,
  * the light sampling and brute-force light pdf, the five integrators
  * (direct, material sampling, MIS, ReSTIR direct-only, ReSTIR) with Russian
- * roulette, and the per-pixel camera ray.  It is the checker for shading
- * kernels; nothing in the product links it.
+ * roulette, the per-pixel camera ray, and the tone mapping of tonemap.frag.
+ * It is the checker for shading kernels; nothing in the product links it.
  *
  * Where the shader leaves a value to the driver, this restatement fixes it:
- *  - sin, cos and pow are computed by this file's own routines (Cody-Waite
+ *  - sin, cos, pow and exp are computed by this file's own routines (Cody-Waite
  *    reduction with Taylor polynomials; exp2 / log2 through the atanh
  *    series), so a device implementation spelling out the same operations
  *    can match it bit for bit; every other operation is one IEEE FP32
@@ -79,8 +79,13 @@ void orc_sh_tea(int64_t n, const uint32_t* v0, const uint32_t* v1, uint32_t* out
 void orc_sh_lcg_stream(uint32_t seed, int64_t n, uint32_t* lcg_out, float* randf_out);
 void orc_sh_radical_inverse(int64_t n, const uint32_t* bits, float* out);
 
-/* this file's own sin / cos / pow: kind 0 sin(x), 1 cos(x), 2 pow(x, y) */
+/* this file's own sin / cos / pow / exp: kind 0 sin(x), 1 cos(x), 2 pow(x, y), 3 exp(x) */
 void orc_sh_math(int32_t kind, int64_t n, const float* x, const float* y, float* out);
+
+/* tonemap.frag per colour component: type 0 Hable's filmic curve scaled to
+ * white at 11.2, 1 exponential 1 - exp(-c exposure), both followed by
+ * pow(., 1 / gamma); 2 unchanged.  Returns 0, or -1 for an unknown type. */
+int orc_sh_tonemap(int32_t type, float exposure, float gamma, int64_t n, const float* in, float* out);
 
 /* n samples drawn one after another from one lcg stream started at `seed`.
  * kind 0 uniform_hemisphere, 1 cosine_hemisphere, 2 cospow_hemisphere(param),

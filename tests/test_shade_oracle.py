@@ -6,17 +6,19 @@ The shaders cannot run here (Vulkan), so parity with the reference itself is
 unpinned; these tests pin the restatement instead:
   - random numbers: TEA and the lcg against an independent Python
     restatement, the radical inverse against hand values;
-  - the restatement's own sin / cos / pow within 2 ulp of FP64;
+  - the restatement's own sin / cos / pow / exp within 2 ulp of FP64, and
+    its tone mapping against the FP64 formulas of tonemap.frag;
   - samplers: unit directions in the right hemisphere with the analytic
     moments of their densities;
   - materials: each pdf integrates over the upper hemisphere to its
     sampler's acceptance rate, and the sampler's directions reproduce the
     pdf (E[g(wi)] against quadrature of g * pdf), for Blinn-Phong and GGX;
   - triangle and light pdfs integrate to 1 over the sphere;
-  - integrators: direct lighting, material sampling and MIS (and ReSTIR's
-    direct-only mode) estimate the same image of a floor under an area light,
-    with and without Russian roulette; a mirror floor reflects the light
-    exactly.
+  - integrators: direct lighting, material sampling, MIS and both ReSTIR
+    modes estimate the same image of a floor under an area light, with and
+    without Russian roulette; in a corner that inter-reflects, material
+    sampling, ReSTIR and MIS to depth 8 agree; a mirror floor reflects the
+    light exactly.
 """
 from __future__ import annotations
 
@@ -91,6 +93,47 @@ def test_pow_within_two_ulp():
     assert (np.abs(got[keep] - ref[keep]) / ulp).max() <= 2.0
     assert S.pow(np.float32([0.0, 0.0, 1.0, 0.5]), np.float32([5.0, 0.25, 7.0, 1.0])).tolist() == [0.0, 0.0, 1.0,
                                                                                                    0.5]
+
+
+def test_exp_within_two_ulp():
+    x = np.concatenate([-np.linspace(0.0, 80.0, 200001, dtype=np.float32),
+                        np.linspace(0.0, 80.0, 1001, dtype=np.float32)])
+    ref = np.exp(x.astype(np.float64))
+    got = S.exp(x)
+    ulp = np.spacing(ref.astype(np.float32)).astype(np.float64)
+    assert (np.abs(got - ref) / ulp).max() <= 2.0
+    assert S.exp(np.float32([0.0]))[0] == 1.0
+
+
+# -------------------------------------------------------------- tone mapping
+
+def _filmic64(c):
+    A, B, C, D, E, F = 0.15, 0.50, 0.10, 0.20, 0.02, 0.30
+    return (c * (A * c + C * B) + D * E) / (c * (A * c + B) + D * F) - E / F
+
+
+def test_tonemap_against_fp64_formulas():
+    c = np.concatenate([np.linspace(0.0, 4.0, 4001), np.geomspace(4.0, 1e4, 500)]).astype(np.float32)
+    c64 = c.astype(np.float64)
+    for exposure, gamma in ((1.0, 2.2), (0.37, 1.0), (3.0, 2.4)):
+        e = np.float32(exposure)
+        want = (1.0 - np.exp(-c64 * np.float64(e))) ** (1.0 / np.float64(np.float32(gamma)))
+        got = S.tonemap(c, S.EXPONENTIAL, exposure, gamma).astype(np.float64)
+        np.testing.assert_allclose(got, want, rtol=2e-6, atol=1e-6)
+        want = np.maximum(_filmic64(c64 * e) / _filmic64(11.2), 0.0) ** (1.0 / np.float64(np.float32(gamma)))
+        got = S.tonemap(c, S.FILMIC, exposure, gamma).astype(np.float64)
+        # at black the curve's constant terms cancel in FP32 to ~7e-9 instead
+        # of 0 (the shader's formula in FP32), which the gamma power lifts
+        away = c64 * e >= 1e-3
+        np.testing.assert_allclose(got[away], want[away], rtol=1e-5, atol=1e-5)
+        assert 0.0 <= got[0] < 1e-3
+        assert np.all(np.diff(got[:4001]) >= 0)  # monotone
+    img = np.random.default_rng(4).random((3, 5, 3), np.float32) * 3
+    np.testing.assert_array_equal(S.tonemap(img, S.NO_TONEMAP), img)
+    # the filmic curve reaches white at 11.2 / exposure
+    assert abs(S.tonemap(np.float32([11.2]), S.FILMIC, 1.0, 2.2)[0] - 1.0) < 1e-6
+    with pytest.raises(ValueError):
+        S.tonemap(img, 3)
 
 
 # ------------------------------------------------------------------ samplers
@@ -278,16 +321,55 @@ def test_integrators_agree_on_direct_lighting(brdf):
     ref = _rows(sc, seeds, integrator=S.DIRECT, brdf=brdf, samples=96, use_rr=False)
     assert ref.mean(0).max() > 0.05  # the floor is lit
     for integ, depth, rr in ((S.MATERIAL, 2, False), (S.MIS, 2, False), (S.MIS, 8, True),
-                             (S.RESTIR_DIRECT, 8, False)):
+                             (S.RESTIR_DIRECT, 8, False), (S.RESTIR, 8, True)):
         got = _rows(sc, seeds, integrator=integ, brdf=brdf, samples=96, max_depth=depth, use_rr=rr)
-        n = len(seeds)
-        se = np.sqrt(ref.var(0, ddof=1) / n + got.var(0, ddof=1) / n)
-        lit = se > 0  # rows of the floor; the rows of clear colour are exact in both
-        np.testing.assert_array_equal(got.mean(0)[~lit], ref.mean(0)[~lit])
-        z = np.abs(got.mean(0) - ref.mean(0))[lit] / se[lit]
-        assert z.max() < 5.0, (integ, depth, rr, z)
-        whole_se = np.sqrt(ref.mean(1).var(ddof=1) / n + got.mean(1).var(ddof=1) / n)
-        assert abs(got.mean() - ref.mean()) < 5 * whole_se, (integ, depth, rr)
+        _agree(got, ref, (integ, depth, rr))
+
+
+def _agree(got, ref, what):
+    n = got.shape[0]
+    se = np.sqrt(ref.var(0, ddof=1) / n + got.var(0, ddof=1) / n)
+    lit = se > 0  # rows the light reaches; rows of clear colour are exact in both
+    np.testing.assert_array_equal(got.mean(0)[~lit], ref.mean(0)[~lit])
+    z = np.abs(got.mean(0) - ref.mean(0))[lit] / se[lit]
+    assert z.max() < 5.0, (what, z)
+    whole_se = np.sqrt(ref.mean(1).var(ddof=1) / n + got.mean(1).var(ddof=1) / n)
+    assert abs(got.mean() - ref.mean()) < 5 * whole_se, what
+
+
+def corner_and_light(brdf_rough=0.6, albedo=0.35):
+    """A floor and two walls meeting in a corner under an area light: light
+    reaches the camera after several bounces."""
+    fv, fn = _quad(0.0, 1.0, True)
+    # the wall x = -1 (normal +x) and the wall z = -1 (normal +z), as rotated floors
+    wx = fv[..., [1, 0, 2]].copy()
+    wx[..., 0] -= 1.0
+    wx[..., 1] += 1.0
+    wz = fv[..., [0, 2, 1]].copy()
+    wz[..., 2] -= 1.0
+    wz[..., 1] += 1.0
+    nx = np.broadcast_to(np.float32([1, 0, 0]), (2, 3, 3))
+    nz = np.broadcast_to(np.float32([0, 0, 1]), (2, 3, 3))
+    lv, ln = _quad(1.2, 0.2, False, x0=0.1, z0=0.1)
+    a = (albedo,) * 3
+    return S.Scene(np.concatenate([fv, wx, wz, lv]), np.concatenate([fn, nx, nz, ln]), [0, 0, 1, 1, 2, 2, 3, 3],
+                   albedo=[a, a, a, (0, 0, 0)], emissive=[(0, 0, 0)] * 3 + [(8.0, 8.0, 8.0)],
+                   metal_rough=[(0, brdf_rough)] * 3 + [(0, 0.5)])
+
+
+@pytest.mark.parametrize("brdf", [S.BLINN_PHONG, S.GGX])
+def test_integrators_agree_with_interreflection(brdf):
+    """ReSTIR and material sampling to the same depth count the same paths;
+    MIS to that depth differs from them only by part of the paths of the
+    last bounce, negligible at albedo 0.35 and depth 8."""
+    sc = corner_and_light()
+    seeds = range(11, 19)
+    ref = _rows(sc, seeds, integrator=S.MATERIAL, brdf=brdf, samples=64, max_depth=8, use_rr=False)
+    one = _rows(sc, seeds, integrator=S.MATERIAL, brdf=brdf, samples=64, max_depth=2, use_rr=False)
+    assert ref.mean() > one.mean() * 1.02  # inter-reflection adds light
+    for integ, rr in ((S.RESTIR, False), (S.MIS, False), (S.MIS, True)):
+        got = _rows(sc, seeds, integrator=integ, brdf=brdf, samples=64, max_depth=8, use_rr=rr)
+        _agree(got, ref, (integ, rr))
 
 
 def test_primary_misses_and_emitters():
