@@ -9,7 +9,8 @@
  * roulette, the per-pixel camera ray, and the tone mapping of tonemap.frag.
  * It is the checker for shading kernels; nothing in the product links it.
  *
- * Where the shader leaves a value to the driver, this restatement fixes it:
+ * Where the shader leaves a value to the GLSL implementation or the clock,
+ * this restatement fixes it:
  *  - sin, cos, pow and exp are computed by this file's own routines (Cody-Waite
  *    reduction with Taylor polynomials; exp2 / log2 through the atanh
  *    series), so a device implementation spelling out the same operations
