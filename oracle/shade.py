@@ -39,7 +39,40 @@ class ShadeParams(Structure):
     _fields_ = [("clear", c_float * 3), ("env", c_float * 3), ("samples", c_int32), ("max_depth", c_int32),
                 ("qmc", c_int32), ("integrator", c_int32), ("brdf", c_int32), ("use_rr", c_int32),
                 ("use_metalness", c_int32), ("frame", c_int32), ("max_frame", c_int32),
-                ("new_samples", c_int32), ("temporal_multiplier", c_int32), ("seed", c_uint32)]
+                ("new_samples", c_int32), ("temporal_multiplier", c_int32), ("use_temporal", c_int32),
+                ("seed", c_uint32)]
+
+
+class ShadeTemporal(Structure):
+    _fields_ = [("prev_pv", c_void_p), ("prev_gbuf", c_void_p), ("prev_res", c_void_p), ("out_res", c_void_p)]
+
+
+# orc_shade_reservoir
+RESERVOIR = np.dtype([("pos", "<f4", 3), ("normal", "<f4", 3), ("emissive", "<f4", 3), ("w_sum", "<f4"),
+                      ("w", "<f4"), ("n_seen", "<u4")])
+assert RESERVOIR.itemsize == 48
+
+
+class TemporalState:
+    """ReSTIR's state between frames: the previous frame's view-projection,
+    first-hit buffer and reservoirs.  `advance` makes this frame's outputs
+    the next frame's inputs."""
+
+    def __init__(self, camera: "ShadeCamera"):
+        self.h, self.w = camera.height, camera.width
+        self.prev_pv = view_projection(camera)
+        self.prev_gbuf = None
+        self.prev_res = None
+        self.out_res = np.zeros((self.h, self.w), RESERVOIR)
+
+    def advance(self, gbuf, camera: "ShadeCamera"):
+        self.prev_gbuf = np.ascontiguousarray(gbuf, np.float32)
+        self.prev_res = self.out_res
+        self.out_res = np.zeros((self.h, self.w), RESERVOIR)
+        self.prev_pv = view_projection(camera)
+
+    def _struct(self) -> ShadeTemporal:
+        return ShadeTemporal(_p(self.prev_pv), _p(self.prev_gbuf), _p(self.prev_res), _p(self.out_res))
 
 
 def _L():
@@ -184,18 +217,21 @@ class Scene:
 
     def render(self, camera: ShadeCamera, *, integrator=DIRECT, brdf=BLINN_PHONG, samples=8, max_depth=8,
                use_rr=True, qmc=False, use_metalness=False, frame=0, max_frame=256, new_samples=4,
-               temporal_multiplier=16, clear=(0.3, 0.3, 0.3), env=(0.0, 0.0, 0.0), seed=1, image=None,
-               gbuffer=False):
+               temporal_multiplier=16, use_temporal=True, clear=(0.3, 0.3, 0.3), env=(0.0, 0.0, 0.0), seed=1,
+               image=None, gbuffer=False, temporal: TemporalState | None = None):
         """One frame, the reference's defaults unless given (rt.h:38-53;
         env_scale 0).  Returns the image (height, width, 3) and, if asked,
-        the first-hit buffer (height, width, 9)."""
+        the first-hit buffer (height, width, 9).  `temporal` carries ReSTIR's
+        reservoirs between frames (its out_res is written)."""
         p = ShadeParams((c_float * 3)(*clear), (c_float * 3)(*env), samples, max_depth, int(qmc), integrator,
                         brdf, int(use_rr), int(use_metalness), frame, max_frame, new_samples,
-                        temporal_multiplier, seed)
+                        temporal_multiplier, int(use_temporal), seed)
         img = np.zeros((camera.height, camera.width, 3), np.float32) if image is None else image
         assert img.dtype == np.float32 and img.flags.c_contiguous and img.shape == (camera.height, camera.width, 3)
         g = np.zeros((camera.height, camera.width, 9), np.float32) if gbuffer else None
-        rc = _L().orc_sh_render(byref(self._s), byref(camera), byref(p), _p(img), _p(g))
+        ts = None if temporal is None else temporal._struct()
+        rc = _L().orc_sh_render(byref(self._s), byref(camera), byref(p), _p(img), _p(g),
+                                None if ts is None else byref(ts))
         if rc != 0:
             raise ValueError("orc_sh_render refused its arguments")
         return (img, g) if gbuffer else img
@@ -211,3 +247,16 @@ def camera(eye, target, up, yfov: float, width: int, height: int) -> ShadeCamera
     u = np.cross(r, f)
     c3 = lambda v: (c_float * 3)(*[float(x) for x in v])  # noqa: E731
     return ShadeCamera(c3(e), c3(r), c3(u), c3(f), float(np.tan(0.5 * yfov)), width / height, width, height)
+
+
+def view_projection(cam: ShadeCamera) -> np.ndarray:
+    """4 x 4 row-major matrix taking a world point to the clip coordinates
+    whose (x/w + 1)/2, (y/w + 1)/2 are the camera's image coordinates (row 0
+    at the top), the inverse of the renderer's camera ray; w is the depth."""
+    e, r, u, f = (np.asarray(v, np.float64) for v in (cam.eye, cam.right, cam.up, cam.fwd))
+    sx, sy = cam.tan_half_y * cam.aspect, cam.tan_half_y
+    m = np.zeros((4, 4))
+    m[0, :3], m[0, 3] = r / sx, -np.dot(e, r) / sx
+    m[1, :3], m[1, 3] = -u / sy, np.dot(e, u) / sy
+    m[3, :3], m[3, 3] = f, -np.dot(e, f)
+    return np.ascontiguousarray(m, np.float32)

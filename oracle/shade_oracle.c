@@ -395,6 +395,8 @@ typedef struct {
 typedef struct {
     const orc_shade_scene* s;
     const orc_shade_params* p;
+    const orc_shade_temporal* tmp;
+    int32_t width, height;
     light_rec* lights;
     uint32_t n_lights;
 } ctx_t;
@@ -713,6 +715,66 @@ static reservoir res_new(void) {
     return r;
 }
 
+static reservoir res_load(const orc_shade_reservoir* o) {
+    reservoir r;
+    r.pos = ld(o->pos);
+    r.normal = ld(o->normal);
+    r.emissive = ld(o->emissive);
+    r.w_sum = o->w_sum;
+    r.w = o->w;
+    r.n_seen = o->n_seen;
+    return r;
+}
+
+static void res_store(const reservoir* r, orc_shade_reservoir* o) {
+    const float f[9] = {r->pos.x, r->pos.y, r->pos.z, r->normal.x, r->normal.y, r->normal.z,
+                        r->emissive.x, r->emissive.y, r->emissive.z};
+    memcpy(o->pos, f, 3 * sizeof(float));
+    memcpy(o->normal, f + 3, 3 * sizeof(float));
+    memcpy(o->emissive, f + 6, 3 * sizeof(float));
+    o->w_sum = r->w_sum;
+    o->w = r->w;
+    o->n_seen = r->n_seen;
+}
+
+/* The previous frame's reservoir for a hit, when the reprojected first hit
+ * agrees in position, albedo and normal (rt.rgen:457-479): returns 0 where
+ * the shader leaves the reuse loop.  Buffers are read with the nearest texel
+ * and repeat addressing of the G-buffer sampler (rt.cpp:449-450,
+ * vulkan.cpp:522-531); a reservoir index at the image edge is clamped. */
+static int temporal_reservoir(const ctx_t* c, const hit_info* hit, const mat_info* m, const shade_info* sh,
+                              reservoir* prev) {
+    const orc_shade_temporal* T = c->tmp;
+    float pp[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (T && T->prev_pv) {
+        const float* M = T->prev_pv;
+        for (int i = 0; i < 4; ++i)
+            pp[i] = M[4 * i] * hit->pos.x + M[4 * i + 1] * hit->pos.y + M[4 * i + 2] * hit->pos.z + M[4 * i + 3];
+    }
+    pp[0] = pp[0] / pp[3];
+    pp[1] = pp[1] / pp[3];
+    pp[0] = (pp[0] + 1.0f) * 0.5f;
+    pp[1] = (pp[1] + 1.0f) * 0.5f;
+    if (!(pp[0] > 0.0f && pp[1] > 0.0f && pp[0] < 1.0f && pp[1] < 1.0f)) return 0;
+    const int W = c->width, H = c->height;
+    int tx = (int)floorf(pp[0] * (float)W) % W, ty = (int)floorf(pp[1] * (float)H) % H;
+    float g[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (T && T->prev_gbuf) memcpy(g, T->prev_gbuf + 9 * ((int64_t)ty * W + tx), sizeof g);
+    const v3 pd = sub(ld(g), hit->pos);
+    if (dot(pd, pd) > 0.01f) return 0;
+    const v3 ad = sub(ld(g + 6), m->albedo);
+    if (dot(ad, ad) > 0.01f) return 0;
+    if (dot(ld(g + 3), sh->n) < 0.5f) return 0;
+    int fx = (int)(pp[0] * (float)W), fy = (int)(pp[1] * (float)H);
+    fx = fx < W ? fx : W - 1;
+    fy = fy < H ? fy : H - 1;
+    if (T && T->prev_res)
+        *prev = res_load(&T->prev_res[(int64_t)fy * W + fx]);
+    else
+        *prev = res_new();
+    return 1;
+}
+
 static void res_update(uint32_t* seed, reservoir* r, float weight, v3 pos, v3 normal, v3 emissive) {
     r->n_seen++;
     r->w_sum += weight;
@@ -740,10 +802,10 @@ static float update_weight(const ctx_t* c, reservoir* r, const hit_info* hit, co
     return p_hat;
 }
 
-/* the temporal branch that reads the previous frame's buffers
- * (rt.rgen:457-479) is not restated: reuse is across the samples of a pixel */
+/* rt.rgen:425-507: candidates, then reuse of the previous frame's reservoir
+ * (first sample, temporal reuse on) or of this pixel's previous sample */
 static void reservoir_sample(const ctx_t* c, uint32_t* seed, trace_info* tr, const hit_info* hit,
-                             const mat_info* m, const shade_info* sh, reservoir* prev) {
+                             const mat_info* m, const shade_info* sh, reservoir* prev, int first) {
     reservoir nr = res_new();
     for (int i = 0; i < c->p->new_samples; ++i) {
         const light_sample_t L = light_sample(c, seed, hit->pos);
@@ -755,6 +817,7 @@ static void reservoir_sample(const ctx_t* c, uint32_t* seed, trace_info* tr, con
     const float new_p = update_weight(c, &nr, hit, m, sh);
     if (new_p != 0.0f && occluded(c->s, hit->pos, nr.pos)) nr.w = 0.0f;
 
+    if (first && c->p->use_temporal && !temporal_reservoir(c, hit, m, sh, prev)) goto done;
     reservoir tres = res_new();
     res_update(seed, &tres, new_p * nr.w * (float)nr.n_seen, nr.pos, nr.normal, nr.emissive);
     const float old_p = update_weight(c, prev, hit, m, sh);
@@ -765,6 +828,7 @@ static void reservoir_sample(const ctx_t* c, uint32_t* seed, trace_info* tr, con
     (void)update_weight(c, &tres, hit, m, sh);
     nr = tres;
 
+done:
     if (nr.w != 0.0f) {
         const v3 dir = sub(nr.pos, hit->pos);
         const v3 wi = normalize3(dir);
@@ -778,7 +842,7 @@ static void reservoir_sample(const ctx_t* c, uint32_t* seed, trace_info* tr, con
 
 /* rt.rgen:509-548 */
 static void integrate_restir(const ctx_t* c, uint32_t* seed, trace_info* tr, const hit_info* hit,
-                             const mat_info* m, const shade_info* sh, int d_only, reservoir* prev) {
+                             const mat_info* m, const shade_info* sh, int d_only, reservoir* prev, int first) {
     const int brdf = c->p->brdf;
     if (any_pos(m->emissive)) {
         tr->acc = add(tr->acc, scl(mulv(m->emissive, tr->throughput), tr->mis));
@@ -791,7 +855,7 @@ static void integrate_restir(const ctx_t* c, uint32_t* seed, trace_info* tr, con
         tr->throughput = mulv(tr->throughput, m->albedo);
         tr->mis = 1.0f;
     } else {
-        if (tr->depth == 0) reservoir_sample(c, seed, tr, hit, m, sh, prev);
+        if (tr->depth == 0) reservoir_sample(c, seed, tr, hit, m, sh, prev, first);
         v3 wi;
         if (!mat_sample(brdf, seed, m, sh, &wi)) {
             tr->depth = c->p->max_depth;
@@ -874,8 +938,8 @@ static void render_pixel(const ctx_t* c, const orc_shade_camera* cam, int x, int
                 case 0: integrate_direct(c, &seed, &tr, &hit, &m, &sh); break;
                 case 1: integrate_mats(c, &seed, &tr, &hit, &m, &sh); break;
                 case 2: integrate_mis(c, &seed, &tr, &hit, &m, &sh); break;
-                case 3: integrate_restir(c, &seed, &tr, &hit, &m, &sh, 1, &prev); break;
-                default: integrate_restir(c, &seed, &tr, &hit, &m, &sh, 0, &prev); break;
+                case 3: integrate_restir(c, &seed, &tr, &hit, &m, &sh, 1, &prev, smp == 0); break;
+                default: integrate_restir(c, &seed, &tr, &hit, &m, &sh, 0, &prev, smp == 0); break;
             }
             if (p->use_rr) {
                 const float pc = fminf(fmaxf(tr.throughput.x, fmaxf(tr.throughput.y, tr.throughput.z)) + 0.001f, 0.95f);
@@ -885,6 +949,8 @@ static void render_pixel(const ctx_t* c, const orc_shade_camera* cam, int x, int
         }
         acc = add(acc, tr.acc);
     }
+    if (p->integrator >= 3 && c->tmp && c->tmp->out_res)
+        res_store(&prev, &c->tmp->out_res[(int64_t)y * cam->width + x]);
     const v3 avg = divs(acc, (float)p->samples);
     if (p->frame > 0) { /* mix(old, avg, 1 / (frame + 1)) */
         const float a = 1.0f / (float)(p->frame + 1);
@@ -1048,7 +1114,7 @@ void orc_sh_light_pdf(const orc_shade_scene* s, int64_t n, const float* p, const
 }
 
 int orc_sh_render(const orc_shade_scene* s, const orc_shade_camera* cam, const orc_shade_params* p, float* image,
-                  float* gbuf) {
+                  float* gbuf, const orc_shade_temporal* temporal) {
     if (!valid_scene(s) || !cam || !p || !image) return -1;
     if (cam->width <= 0 || cam->height <= 0 || p->samples <= 0 || p->max_depth < 0) return -1;
     if (p->integrator < 0 || p->integrator > 4 || p->brdf < 0 || p->brdf > 1) return -1;
@@ -1057,6 +1123,9 @@ int orc_sh_render(const orc_shade_scene* s, const orc_shade_camera* cam, const o
     memset(&c, 0, sizeof c);
     c.s = s;
     c.p = p;
+    c.tmp = temporal;
+    c.width = cam->width;
+    c.height = cam->height;
     if (collect_lights(s, &c.lights, &c.n_lights) != 0) return -1;
     /* every integrator but material sampling samples lights */
     if (c.n_lights == 0 && p->integrator != 1) {

@@ -72,8 +72,25 @@ typedef struct {
     int32_t max_frame;
     int32_t new_samples;   /* ReSTIR candidates per pixel */
     int32_t temporal_multiplier;
+    int32_t use_temporal;  /* ReSTIR: reuse the previous frame's reservoirs (rt.rgen:456-479) */
     uint32_t seed;
 } orc_shade_params;
+
+/* A ReSTIR reservoir (restir.glsl:1-8). */
+typedef struct {
+    float pos[3], normal[3], emissive[3];
+    float w_sum, w;
+    uint32_t n_seen;
+} orc_shade_reservoir;
+
+/* State carried between frames for ReSTIR's temporal reuse.  Any pointer may
+ * be NULL: a missing previous buffer reads as zeros, as an unwritten image. */
+typedef struct {
+    const float* prev_pv;                 /* 4 x 4 row-major: world to the previous frame's clip space */
+    const float* prev_gbuf;               /* height x width x 9: the previous frame's first-hit buffer */
+    const orc_shade_reservoir* prev_res;  /* height x width: the previous frame's final reservoirs */
+    orc_shade_reservoir* out_res;         /* height x width: this frame's final reservoirs (written) */
+} orc_shade_temporal;
 
 /* random numbers (rtcommon.glsl:99-135) */
 void orc_sh_tea(int64_t n, const uint32_t* v0, const uint32_t* v1, uint32_t* out);
@@ -113,10 +130,11 @@ void orc_sh_light_pdf(const orc_shade_scene* s, int64_t n, const float* p, const
 
 /* One frame: image is height x width x 3 (read when frame > 0, written);
  * gbuf, when not NULL, receives per pixel the first hit's position, shading
- * normal and albedo of sample 0 (9 floats; zeros on a miss).
+ * normal and albedo of sample 0 (9 floats; zeros on a miss); temporal, when
+ * not NULL, carries ReSTIR's state between frames.
  * Returns 0, or -1 on invalid arguments. */
 int orc_sh_render(const orc_shade_scene* s, const orc_shade_camera* c, const orc_shade_params* p, float* image,
-                  float* gbuf);
+                  float* gbuf, const orc_shade_temporal* temporal);
 
 #ifdef __cplusplus
 }
