@@ -443,6 +443,32 @@ def test_mirror_floor_reflects_the_light_exactly():
     np.testing.assert_allclose(img, np.broadcast_to(np.float32([3.0, 1.5, 6.0]), (3, 3, 3)), rtol=1e-6)
 
 
+def test_qmc_jitter_is_seed_independent():
+    """With Hammersley jitter (rt.rgen:553-555) a mirror render draws no
+    random numbers, so two seeds give the same frame; with random jitter on a
+    later frame they do not."""
+    sc = floor_and_light(rough=0.0)
+    kw = dict(integrator=S.MATERIAL, samples=4, max_depth=3, use_rr=False, frame=2, max_frame=8)
+    a = sc.render(CAM, qmc=True, seed=1, **kw)
+    b = sc.render(CAM, qmc=True, seed=2, **kw)
+    np.testing.assert_array_equal(a, b)
+    c = sc.render(CAM, qmc=False, seed=1, **kw)
+    d = sc.render(CAM, qmc=False, seed=2, **kw)
+    assert not np.array_equal(c, d)
+
+
+def test_metalness_mixes_albedo():
+    fv, fn = _quad(0.0, 1.0, True)
+    lv, ln = _quad(1.0, 0.25, False)
+    sc = S.Scene(np.concatenate([fv, lv]), np.concatenate([fn, ln]), [0, 0, 1, 1],
+                 albedo=[(0.8, 0.4, 0.2), (0, 0, 0)], emissive=[(0, 0, 0), (5, 5, 5)],
+                 metal_rough=[(0.25, 0.5), (0, 0.5)])
+    _, g = sc.render(CAM, integrator=S.DIRECT, samples=1, use_metalness=True, gbuffer=True)
+    on_floor = (np.abs(g[..., 3:6]).sum(-1) > 0) & (np.abs(g[..., 1]) < 1e-6)
+    want = np.float32(0.04) * np.float32(0.75) + np.float32([0.8, 0.4, 0.2]) * np.float32(0.25)
+    np.testing.assert_allclose(g[on_floor][:, 6:9], np.broadcast_to(want, (on_floor.sum(), 3)), rtol=1e-6)
+
+
 def test_render_is_deterministic_and_blends_frames():
     sc = floor_and_light()
     a = sc.render(CAM, integrator=S.MIS, samples=4, seed=7)
