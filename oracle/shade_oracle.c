@@ -8,9 +8,13 @@
  */
 #include "shade_oracle.h"
 
+#define _POSIX_C_SOURCE 200809L
 #include <math.h>
+#include <pthread.h>
+#include <stdatomic.h>
 #include <stdlib.h>
 #include <string.h>
+#include <unistd.h>
 
 #define SH_PI 3.141592f        /* rtcommon.glsl:6 (the shader's truncated constant) */
 #define SH_LARGE_DIST 10000000.0f /* rtcommon.glsl:7 */
@@ -1113,6 +1117,28 @@ void orc_sh_light_pdf(const orc_shade_scene* s, int64_t n, const float* p, const
     free(c.lights);
 }
 
+typedef struct {
+    const ctx_t* c;
+    const orc_shade_camera* cam;
+    float *image, *gbuf;
+    atomic_int next_row;
+} render_job;
+
+/* rows handed out one at a time; every pixel seeds its own stream, so the
+ * image does not depend on the number of threads */
+static void* render_rows(void* arg) {
+    render_job* j = (render_job*)arg;
+    for (;;) {
+        const int y = atomic_fetch_add(&j->next_row, 1);
+        if (y >= j->cam->height) break;
+        for (int x = 0; x < j->cam->width; ++x) {
+            const int64_t px = (int64_t)y * j->cam->width + x;
+            render_pixel(j->c, j->cam, x, y, j->image + 3 * px, j->gbuf ? j->gbuf + 9 * px : NULL);
+        }
+    }
+    return NULL;
+}
+
 int orc_sh_render(const orc_shade_scene* s, const orc_shade_camera* cam, const orc_shade_params* p, float* image,
                   float* gbuf, const orc_shade_temporal* temporal) {
     if (!valid_scene(s) || !cam || !p || !image) return -1;
@@ -1132,11 +1158,21 @@ int orc_sh_render(const orc_shade_scene* s, const orc_shade_camera* cam, const o
         free(c.lights);
         return -1;
     }
-    for (int y = 0; y < cam->height; ++y)
-        for (int x = 0; x < cam->width; ++x) {
-            const int64_t px = (int64_t)y * cam->width + x;
-            render_pixel(&c, cam, x, y, image + 3 * px, gbuf ? gbuf + 9 * px : NULL);
-        }
+    render_job job;
+    job.c = &c;
+    job.cam = cam;
+    job.image = image;
+    job.gbuf = gbuf;
+    atomic_init(&job.next_row, 0);
+    long hw = sysconf(_SC_NPROCESSORS_ONLN);
+    int nth = hw > 1 ? (int)(hw < 64 ? hw : 64) : 1;
+    if (nth > cam->height) nth = cam->height;
+    pthread_t th[64];
+    int started = 0;
+    for (int i = 1; i < nth; ++i)
+        if (pthread_create(&th[started], NULL, render_rows, &job) == 0) ++started;
+    render_rows(&job);
+    for (int i = 0; i < started; ++i) pthread_join(th[i], NULL);
     free(c.lights);
     return 0;
 }

@@ -21,7 +21,10 @@ Run from the repository root:  python tests/golden/make_golden.py
    (node, primitive) with the node's world matrix (glTF matrix or TRS,
    composed down the node tree, rounded to FP32 3 x 4), seeded queries and
    their FP64 brute-force answers over the world-space vertices (the FP32
-   matrix applied to the FP32 vertex in FP64).  Needs the reference checkout.
+   matrix applied to the FP32 vertex in FP64); for shading, each vertex's
+   normal and each primitive's material factors (base colour, emission,
+   metalness, roughness, glTF defaults where absent).  Needs the reference
+   checkout.
 """
 from __future__ import annotations
 
@@ -84,7 +87,11 @@ def write_kats():
         json.dump({"cases": cases, "tie_mesh": TIE_MESH}, f, indent=1)
 
 
-def _gltf_meshes(path: Path):
+def _gltf_meshes(path: Path, shading: bool = False):
+    """Triangle primitives in file order: (positions, triangles), and with
+    `shading` also the vertex normals and the material factors the
+    reference reads (scene.cpp:286-299) with glTF's defaults: base colour
+    1, emission 0, metalness 1, roughness 1."""
     g = json.loads(path.read_text())
     bufs = []
     for b in g["buffers"]:
@@ -115,7 +122,16 @@ def _gltf_meshes(path: Path):
                 continue
             pos = accessor(prim["attributes"]["POSITION"]).astype(np.float32)
             idx = accessor(prim["indices"]).reshape(-1, 3).astype(np.int32)
-            meshes.append((pos, idx))
+            if not shading:
+                meshes.append((pos, idx))
+                continue
+            nrm = accessor(prim["attributes"]["NORMAL"]).astype(np.float32)
+            mat = g["materials"][prim["material"]]
+            pbr = mat.get("pbrMetallicRoughness", {})
+            albedo = np.float32(pbr.get("baseColorFactor", [1, 1, 1, 1])[:3])
+            emissive = np.float32(mat.get("emissiveFactor", [0, 0, 0]))
+            mr = np.float32([pbr.get("metallicFactor", 1.0), pbr.get("roughnessFactor", 1.0)])
+            meshes.append((pos, idx, nrm, albedo, emissive, mr))
     return meshes
 
 
@@ -196,9 +212,14 @@ def write_cbox_scene(ref_root: Path):
     TT = np.concatenate([m[1] for m in meshes])
     voff = np.concatenate([[0], np.cumsum([len(m[0]) for m in meshes])]).astype(np.int64)
     toff = np.concatenate([[0], np.cumsum([len(m[1]) for m in meshes])]).astype(np.int64)
+    shade = _gltf_meshes(path, shading=True)
     np.savez_compressed(HERE / "cbox_scene.npz", verts=V, tris=TT, vert_offsets=voff, tri_offsets=toff,
                         instance_primitive=prim, instance_transform=T, queries=q, dist=bf["dist"],
                         instance=inst_of.astype(np.int32), tri=(bf["tri"] - toff_i[inst_of]).astype(np.int32),
+                        normals=np.concatenate([m[2] for m in shade]),
+                        prim_albedo=np.stack([m[3] for m in shade]),
+                        prim_emissive=np.stack([m[4] for m in shade]),
+                        prim_metal_rough=np.stack([m[5] for m in shade]),
                         source=np.array(str(path.relative_to(ref_root))))
 
 

@@ -505,3 +505,54 @@ def test_render_refuses_bad_arguments():
     with pytest.raises(ValueError):  # light sampling with no light
         dark.render(CAM, integrator=S.DIRECT)
     dark.render(CAM, integrator=S.MATERIAL, samples=1)  # material sampling needs none
+
+
+# ------------------------------------------------------- the reference's scene
+
+def cbox_shade_scene():
+    """The reference's Cornell box (media/cbox/cbox.gltf, from the committed
+    fixture): one object per instance, world-space vertices and normals (the
+    inverse-transpose of the instance matrix), the primitive's material."""
+    from pathlib import Path
+
+    z = np.load(Path(__file__).resolve().parent / "golden" / "cbox_scene.npz")
+    voff, toff = z["vert_offsets"], z["tri_offsets"]
+    V, N, Tr = [], [], []
+    albedo, emissive, mr, obj = [], [], [], []
+    for i, (j, T) in enumerate(zip(z["instance_primitive"], z["instance_transform"])):
+        v = z["verts"][voff[j]:voff[j + 1]].astype(np.float64)
+        n = z["normals"][voff[j]:voff[j + 1]].astype(np.float64)
+        tri = z["tris"][toff[j]:toff[j + 1]]
+        M = T.astype(np.float64)
+        V.append((v @ M[:, :3].T + M[:, 3])[tri])
+        N.append((n @ np.linalg.inv(M[:, :3]))[tri])
+        obj.append(np.full(len(tri), i, np.int32))
+        albedo.append(z["prim_albedo"][j])
+        emissive.append(z["prim_emissive"][j])
+        mr.append(z["prim_metal_rough"][j])
+    return S.Scene(np.concatenate(V), np.concatenate(N), np.concatenate(obj), albedo, emissive, mr)
+
+
+# the glTF's camera (node CamInst): on the +z axis looking down -z, vertical
+# field of view 0.7175 rad at 4:3
+CBOX_CAM = S.camera(eye=(0.0, 0.0, 19.992091970966317), target=(0.0, 0.0, 0.0), up=(0, 1, 0),
+                    yfov=0.7175414562225342, width=32, height=24)
+
+
+def test_cbox_renders():
+    sc = cbox_shade_scene()
+    img, g = sc.render(CBOX_CAM, integrator=S.DIRECT, samples=4, gbuffer=True, seed=3)
+    assert np.isfinite(img).all() and img.min() >= 0.0
+    # the ceiling light in view, at its emission exactly
+    assert (img == 10.0).all(-1).sum() >= 1
+    # the red and the green wall
+    alb = g[..., 6:9]
+    red = np.abs(alb - np.float32([1.0, 0.0, 1.0718736e-4])).max(-1) < 1e-6
+    green = np.abs(alb - np.float32([0.054592282, 1.0, 0.0])).max(-1) < 1e-6
+    assert red.sum() >= 4 and green.sum() >= 4
+    assert (img[red][:, 0] >= img[red][:, 1]).all() and img[red][:, 0].mean() > 2 * img[red][:, 1].mean() + 1e-6
+    assert img[green][:, 1].mean() > 2 * img[green][:, 0].mean()
+    # indirect light and the mirror sphere's reflections add to direct light
+    mis = sc.render(CBOX_CAM, integrator=S.MIS, samples=4, seed=3)
+    assert np.isfinite(mis).all() and mis.min() >= 0.0
+    assert mis.mean() > img.mean()
