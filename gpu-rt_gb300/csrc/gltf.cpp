@@ -1,12 +1,14 @@
 // gltf.cpp — glTF 2.0 ingest on the host (cp_gltf_*, include/cpq.h).
 //
 // Reads what the reference's Scene::load / Scene::parse_mesh take from
-// tinygltf (src/scene/scene.cpp:48-315, 317-391) for the closest-point path:
-// triangle geometry (POSITION + indices; strips and fans converted as
-// parse_mesh converts them) and node placement.  Self-contained: a small JSON
+// tinygltf (src/scene/scene.cpp:48-315, 317-391): triangle geometry
+// (POSITION + indices; strips and fans converted as parse_mesh converts
+// them), node placement, and for shading the vertex normals and material
+// factors (no textures).  Self-contained: a small JSON
 // reader, base64 "data:" URIs, external .bin buffers and .glb containers.
 // Everything is bounds-checked against the buffers it indexes; a malformed
 // file is an error, never an out-of-range read.
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -370,6 +372,8 @@ struct Model {
 
 struct Scene {
     std::vector<float> verts;
+    std::vector<float> normals;    // per vertex, zeros where the primitive has no NORMAL
+    std::vector<float> materials;  // per primitive: base colour rgb, emission rgb, metalness, roughness
     std::vector<int32_t> tris;
     std::vector<int64_t> voff{0}, toff{0};
     std::vector<int32_t> mesh_first_prim, mesh_num_prim;  // per glTF mesh: its triangle primitives
@@ -386,6 +390,45 @@ uint32_t index_at(const Accessor& a, size_t i) {
         case 5123: { uint16_t v; std::memcpy(&v, p, 2); return v; }
         default: { uint32_t v; std::memcpy(&v, p, 4); return v; }
     }
+}
+
+// n numbers of a JSON array member, or the defaults when the member is absent
+void numbers(const Json& j, const char* key, size_t n, const float* dflt, float* out) {
+    const Json* a = j.get(key);
+    if (!a) {
+        std::copy(dflt, dflt + n, out);
+        return;
+    }
+    if (a->kind != Json::Array || a->arr.size() < n)
+        throw std::runtime_error(std::string("\"") + key + "\" is not an array of " + std::to_string(n) + " numbers");
+    for (size_t k = 0; k < n; ++k) {
+        if (a->arr[k].kind != Json::Number) throw std::runtime_error(std::string("\"") + key + "\" holds a non-number");
+        out[k] = (float)a->arr[k].num;
+    }
+}
+
+// The factors Scene::parse_mesh copies into its Material (scene.cpp:286-299),
+// with glTF's defaults; a primitive without a material gets the default
+// material (the reference would index materials[-1]).  Textures are not read.
+void material_factors(const Model& m, const Json& prim, float* out) {
+    static const float kOne[4] = {1.0f, 1.0f, 1.0f, 1.0f}, kZero[3] = {0.0f, 0.0f, 0.0f};
+    std::copy(kOne, kOne + 3, out);
+    std::copy(kZero, kZero + 3, out + 3);
+    out[6] = 1.0f;
+    out[7] = 1.0f;
+    const int64_t mi = prim.integer("material", -1);
+    if (mi < 0) return;
+    const auto& mats = m.doc.array("materials");
+    if (mi >= (int64_t)mats.size()) throw std::runtime_error("material index out of range");
+    const Json& mat = mats[(size_t)mi];
+    if (const Json* pbr = mat.get("pbrMetallicRoughness")) {
+        float rgba[4];
+        numbers(*pbr, "baseColorFactor", 4, kOne, rgba);
+        std::copy(rgba, rgba + 3, out);
+        out[6] = (float)pbr->number("metallicFactor", 1.0);
+        out[7] = (float)pbr->number("roughnessFactor", 1.0);
+    }
+    numbers(mat, "emissiveFactor", 3, kZero, out + 3);
 }
 
 void add_primitives(const Model& m, Scene& s) {
@@ -429,6 +472,23 @@ void add_primitives(const Model& m, Scene& s) {
                 std::memcpy(p, pos.data + k * pos.stride, 12);
                 s.verts.insert(s.verts.end(), p, p + 3);
             }
+            // normals as parse_mesh pairs them with positions: the k-th for
+            // vertex k, zero past the accessor's count (scene.cpp:304-307)
+            size_t nn = 0;
+            Accessor na;
+            if (const Json* n_j = attrs.get("NORMAL")) {
+                na = m.accessor((int64_t)n_j->num);
+                if (na.ctype != 5126 || na.ncomp != 3) throw std::runtime_error("NORMAL must be FLOAT VEC3");
+                nn = std::min(na.count, nv);
+            }
+            for (size_t k = 0; k < nv; ++k) {
+                float n[3] = {0.0f, 0.0f, 0.0f};
+                if (k < nn) std::memcpy(n, na.data + k * na.stride, 12);
+                s.normals.insert(s.normals.end(), n, n + 3);
+            }
+            float mat[8];
+            material_factors(m, prim, mat);
+            s.materials.insert(s.materials.end(), mat, mat + 8);
             for (uint32_t v : t) s.tris.push_back((int32_t)v);
             s.voff.push_back(s.voff.back() + (int64_t)nv);
             s.toff.push_back(s.toff.back() + (int64_t)(t.size() / 3));
@@ -583,6 +643,14 @@ CP_API cp_status cp_gltf_primitives(const cp_gltf* g, int32_t* n, const float** 
     if (tris) *tris = g->s.tris.data();
     if (vert_offsets) *vert_offsets = g->s.voff.data();
     if (tri_offsets) *tri_offsets = g->s.toff.data();
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_gltf_shading(const cp_gltf* g, int32_t* n, const float** normals, const float** materials) {
+    if (!g || !n) return cpq::set_error(CP_ERROR_INVALID_VALUE, "scene or count is NULL");
+    *n = (int32_t)(g->s.voff.size() - 1);
+    if (normals) *normals = g->s.normals.data();
+    if (materials) *materials = g->s.materials.data();
     return CP_SUCCESS;
 }
 

@@ -1,4 +1,5 @@
-"""glTF 2.0 ingest (cp_gltf_*): triangle primitives and their placement.
+"""glTF 2.0 ingest (cp_gltf_*): triangle primitives, their placement, and
+their vertex normals and material factors for shading.
 
 ``load_gltf`` copies what the library read into numpy arrays; ``world_mesh``
 flattens the instances into one world-space triangle soup for
@@ -24,6 +25,8 @@ class GltfScene:
     tri_offsets: np.ndarray    # (P + 1,) int64
     instance_primitive: np.ndarray  # (I,) int32
     instance_world: np.ndarray      # (I, 4, 4) float32, row-major
+    normals: np.ndarray        # (V, 3) float32, object space; zero where a primitive has none
+    materials: np.ndarray      # (P, 8) float32: base colour rgb, emission rgb, metalness, roughness
 
     def world_mesh(self) -> tuple[np.ndarray, np.ndarray]:
         """All instances in world space as one mesh (vertices, triangles)."""
@@ -63,6 +66,11 @@ def load_gltf(path: str) -> GltfScene:
         check(lib.cp_gltf_instances(h, byref(ni), byref(ip), byref(iw)), "cp_gltf_instances")
         prim = _array(ip, ni.value, np.int32)
         world = _array(iw, ni.value * 16, np.float32).reshape(-1, 4, 4)
-        return GltfScene(verts, tris, voff, toff, prim, world)
+        ns = c_int32()
+        pn, pm = c_void_p(), c_void_p()
+        check(lib.cp_gltf_shading(h, byref(ns), byref(pn), byref(pm)), "cp_gltf_shading")
+        normals = _array(pn, int(voff[-1]) * 3, np.float32).reshape(-1, 3)
+        materials = _array(pm, ns.value * 8, np.float32).reshape(-1, 8)
+        return GltfScene(verts, tris, voff, toff, prim, world, normals, materials)
     finally:
         lib.cp_gltf_free(h)

@@ -270,6 +270,14 @@ CP_API cp_status cp_query_host(const cp_mesh* mesh, const float* queries, int64_
  * reference reads only "matrix", so it places TRS-only nodes at identity.)
  * Matrices are 4 x 4 row-major floats.
  *
+ * Shading inputs (cp_gltf_shading): per vertex the NORMAL attribute,
+ * aligned with the vertices and zero where a primitive has none or fewer
+ * normals than positions (as parse_mesh pairs them, scene.cpp:304-307); per
+ * primitive 8 floats, the material factors parse_mesh copies
+ * (scene.cpp:286-299): baseColorFactor rgb, emissiveFactor rgb,
+ * metallicFactor, roughnessFactor, with glTF's defaults (1, 0, 1, 1) and the
+ * default material for a primitive without one.  Textures are not read.
+ *
  * Arrays returned by cp_gltf_* are owned by the handle and live until
  * cp_gltf_free.  Errors (unreadable file, malformed JSON, an accessor out of
  * its buffer, an index past its vertices) return CP_ERROR_INVALID_VALUE with
@@ -284,6 +292,8 @@ CP_API cp_status cp_gltf_primitives(const cp_gltf* scene, int32_t* num_primitive
                                     const int64_t** vert_offsets, const int64_t** tri_offsets);
 CP_API cp_status cp_gltf_instances(const cp_gltf* scene, int32_t* num_instances,
                                    const int32_t** primitive, const float** world);
+CP_API cp_status cp_gltf_shading(const cp_gltf* scene, int32_t* num_primitives, const float** normals,
+                                 const float** materials);
 
 /* ---- ray queries ----------------------------------------------------------- */
 

@@ -46,6 +46,11 @@ def test_cbox_reader_matches_fixture(cpq):
     np.testing.assert_array_equal(s.tri_offsets, g["tri_offsets"])
     np.testing.assert_array_equal(s.instance_primitive, g["instance_primitive"])
     np.testing.assert_array_equal(s.instance_world[:, :3, :].astype(np.float32), g["instance_transform"])
+    # shading inputs: normals, and the material factors with glTF's defaults
+    np.testing.assert_array_equal(s.normals, g["normals"])
+    np.testing.assert_array_equal(s.materials[:, 0:3], g["prim_albedo"])
+    np.testing.assert_array_equal(s.materials[:, 3:6], g["prim_emissive"])
+    np.testing.assert_array_equal(s.materials[:, 6:8], g["prim_metal_rough"])
 
 
 def _write(tmp: Path, doc: dict, bin_data: bytes, mode: str) -> Path:
@@ -158,6 +163,69 @@ def test_synthetic_scene(cpq, tmp_path, mode):
     assert v.shape == (4 + 4 + 5 + 4 + 3, 3) and t.shape == (2 + 2 + 3 + 2 + 1, 3)
     np.testing.assert_allclose(v[1], [10, 2, 0], atol=1e-5)       # (1,0,0) rotated, scaled, moved
     np.testing.assert_allclose(v[4 + 1], [10, 2, 6], atol=1e-5)   # child: z + 3 before the parent's scale
+
+
+def _append(doc, data, arr, ctype, typ):
+    """Append an accessor over `arr` to a document from _scene()."""
+    b = arr.tobytes()
+    doc["bufferViews"].append({"buffer": 0, "byteOffset": len(data), "byteLength": len(b)})
+    doc["accessors"].append({"bufferView": len(doc["bufferViews"]) - 1, "componentType": ctype,
+                             "count": len(arr), "type": typ})
+    return len(doc["accessors"]) - 1, data + b + b"\0" * (-len(b) % 4)
+
+
+def _shading_scene():
+    doc, data = _scene()
+    qn = np.float32([[0, 0, 1], [0, 0.6, 0.8], [0, 0, -1], [1, 0, 0]])
+    a_qn, data = _append(doc, data, qn, 5126, "VEC3")
+    a_fn, data = _append(doc, data, qn[:2], 5126, "VEC3")  # fewer normals than the fan's 4 vertices
+    doc["meshes"][0]["primitives"][0]["attributes"]["NORMAL"] = a_qn
+    doc["meshes"][0]["primitives"][0]["material"] = 0
+    doc["meshes"][1]["primitives"][0]["material"] = 1
+    doc["meshes"][1]["primitives"][1]["attributes"]["NORMAL"] = a_fn
+    doc["meshes"][1]["primitives"][3]["material"] = 0
+    doc["materials"] = [{"pbrMetallicRoughness": {"baseColorFactor": [0.5, 0.25, 0.125, 1.0], "metallicFactor": 0.0,
+                                                  "roughnessFactor": 0.3},
+                         "emissiveFactor": [1.0, 2.0, 3.0]},
+                        {"pbrMetallicRoughness": {"roughnessFactor": 0.7}}]
+    return doc, data, qn
+
+
+@pytest.mark.parametrize("mode", ["data", "file", "glb"])
+def test_shading_inputs(cpq, tmp_path, mode):
+    """Vertex normals (zero past the NORMAL accessor's count, or without one)
+    and material factors with glTF's defaults, as parse_mesh reads them."""
+    doc, data, qn = _shading_scene()
+    s = cpq.load_gltf(str(_write(tmp_path, doc, data, mode)))
+    assert s.normals.shape == s.verts.shape
+    np.testing.assert_array_equal(s.normals[0:4], qn)                    # quad
+    np.testing.assert_array_equal(s.normals[4:9], np.zeros((5, 3)))      # strip: no NORMAL
+    np.testing.assert_array_equal(s.normals[9:11], qn[:2])               # fan: two normals,
+    np.testing.assert_array_equal(s.normals[11:13], np.zeros((2, 3)))    # then zeros
+    np.testing.assert_array_equal(s.normals[13:16], np.zeros((3, 3)))
+    mat0 = [0.5, 0.25, 0.125, 1.0, 2.0, 3.0, 0.0, 0.3]
+    np.testing.assert_array_equal(s.materials, np.float32([
+        mat0,
+        [1, 1, 1, 0, 0, 0, 1, 0.7],   # strip: material 1, defaults but its roughness
+        [1, 1, 1, 0, 0, 0, 1, 1],     # fan: no material
+        mat0,                         # unindexed triangle: material 0
+    ]))
+
+
+def test_shading_input_errors(cpq, tmp_path):
+    from gpurt_cpq._lib import CpError
+
+    for change, msg in (
+        (lambda d: d["meshes"][0]["primitives"][0].__setitem__("material", 5), "material index out of range"),
+        (lambda d: d["materials"][0]["pbrMetallicRoughness"].__setitem__("baseColorFactor", "red"), "not an array"),
+        (lambda d: d["materials"][0].__setitem__("emissiveFactor", [1, "x", 3]), "non-number"),
+        (lambda d: d["accessors"][d["meshes"][0]["primitives"][0]["attributes"]["NORMAL"]].__setitem__(
+            "type", "VEC2"), "NORMAL must be FLOAT VEC3"),
+    ):
+        doc, data, _ = _shading_scene()
+        change(doc)
+        with pytest.raises(CpError, match=msg):
+            cpq.load_gltf(str(_write(tmp_path, doc, data, "data")))
 
 
 def test_errors_are_reported(cpq, tmp_path):
