@@ -6,9 +6,9 @@
  * expression rounds as written, in the shader's left-to-right order.  Each
  * function names the shader lines it restates.
  */
+#define _POSIX_C_SOURCE 200809L
 #include "shade_oracle.h"
 
-#define _POSIX_C_SOURCE 200809L
 #include <math.h>
 #include <pthread.h>
 #include <stdatomic.h>
