@@ -14,6 +14,8 @@ unpinned; these tests pin the restatement instead:
     sampler's acceptance rate, and the sampler's directions reproduce the
     pdf (E[g(wi)] against quadrature of g * pdf), for Blinn-Phong and GGX;
   - triangle and light pdfs integrate to 1 over the sphere;
+  - direct lighting per pixel against an FP64 quadrature over the light's
+    area with the material formulas written independently here;
   - integrators: direct lighting, material sampling, MIS and both ReSTIR
     modes estimate the same image of a floor under an area light, with and
     without Russian roulette; in a corner that inter-reflects, material
@@ -556,3 +558,68 @@ def test_cbox_renders():
     mis = sc.render(CBOX_CAM, integrator=S.MIS, samples=4, seed=3)
     assert np.isfinite(mis).all() and mis.min() >= 0.0
     assert mis.mean() > img.mean()
+
+
+def _bp_eval64(albedo, rough, wo, n, wi):
+    """Blinn-Phong eval of rtcommon.glsl:255-270 in FP64, independently of
+    the restatement (wi: (k, 3))."""
+    o_dn = -wo @ n
+    i_dn = wi @ n
+    h = wi - wo
+    h /= np.linalg.norm(h, axis=-1, keepdims=True)
+    e = 1.0 / rough
+    pdf = (e + 1) / (2 * 3.141592) * np.maximum(h @ n, 0) ** e / (4 * (h @ -wo))
+    return np.where((o_dn > 0) & (i_dn > 0), pdf, 0.0)[:, None] * albedo
+
+
+def _ggx_eval64(albedo, rough, wo, n, wi):
+    """GGX eval of rtcommon.glsl:281-324 in FP64."""
+    o_dn = -wo @ n
+    i_dn = wi @ n
+    h = wi - wo
+    h /= np.linalg.norm(h, axis=-1, keepdims=True)
+    a2 = rough * rough
+    n_dh = np.maximum(h @ n, 0)
+    b = n_dh * n_dh * (a2 - 1) + 1
+    d = a2 / (3.141592 * b * b)
+    g = 2 * o_dn * i_dn / (o_dn * np.sqrt(a2 + (1 - a2) * i_dn * i_dn) + i_dn * np.sqrt(a2 + (1 - a2) * o_dn * o_dn))
+    f = albedo + (1 - albedo) * ((1 - i_dn) ** 5)[:, None]
+    ev = f * (d * g / (4 * o_dn))[:, None]
+    return np.where(((o_dn > 0) & (i_dn > 0))[:, None], ev, 0.0)
+
+
+@pytest.mark.parametrize("brdf", [S.BLINN_PHONG, S.GGX])
+def test_direct_lighting_matches_quadrature(brdf):
+    """Each floor pixel's direct-lighting estimate (rt.rgen:392-412) against
+    an FP64 midpoint quadrature of the same integral over the light's area,
+    sum of eval(wi) L |n_light . wi| / r^2 dA, written independently here."""
+    albedo, rough, emit = np.float64([0.8, 0.7, 0.6]), 0.5, 6.0
+    sc = floor_and_light(rough=rough, albedo=tuple(albedo), light_e=(emit,) * 3)
+    _, g = sc.render(CAM, integrator=S.DIRECT, samples=1, gbuffer=True)
+    seeds = range(31, 39)
+    imgs = np.stack([sc.render(CAM, integrator=S.DIRECT, brdf=brdf, samples=128, seed=s)
+                     for s in seeds]).astype(np.float64)
+    mean, se = imgs.mean(0), imgs.std(0, ddof=1) / np.sqrt(len(seeds))
+    # the light: y = 1, x in [-0.05, 0.45], z in [-0.25, 0.25], facing down
+    k = 96
+    u = (np.arange(k) + 0.5) / k
+    X, Z = np.meshgrid(-0.05 + 0.5 * u, -0.25 + 0.5 * u, indexing="ij")
+    lp = np.stack([X.ravel(), np.ones(k * k), Z.ravel()], -1)
+    dA = (0.5 / k) ** 2
+    eye = np.float64(list(CAM.eye))
+    ev = _bp_eval64 if brdf == S.BLINN_PHONG else _ggx_eval64
+    checked = 0
+    for y in range(CAM.height):
+        for x in range(CAM.width):
+            p = g[y, x, :3].astype(np.float64)
+            if abs(p[1]) > 1e-6 or not np.any(g[y, x, 3:6]):
+                continue  # not the floor
+            wo = (p - eye) / np.linalg.norm(p - eye)
+            d = lp - p
+            r2 = (d * d).sum(1)
+            wi = d / np.sqrt(r2)[:, None]
+            want = (ev(albedo, rough, wo, np.float64([0, 1, 0]), wi) * (emit * np.abs(wi[:, 1]) / r2 * dA)[:, None]).sum(0)
+            z = np.abs(mean[y, x] - want) / (se[y, x] + 1e-4 * want + 1e-9)
+            assert z.max() < 5.0, (brdf, y, x, mean[y, x], want, se[y, x])
+            checked += 1
+    assert checked >= 40
