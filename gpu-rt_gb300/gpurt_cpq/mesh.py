@@ -48,7 +48,10 @@ def build_opts(branching: int = 2, leaf_size: int = 4, collapse: str = "count",
     lib.cp_build_opts_default(byref(o))
     o.branching = branching
     o.leaf_size = leaf_size
-    o.collapse = {"count": CP_COLLAPSE_COUNT, "sah": CP_COLLAPSE_SAH}[collapse]
+    modes = {"count": CP_COLLAPSE_COUNT, "sah": CP_COLLAPSE_SAH}
+    if collapse not in modes:
+        raise ValueError(f"collapse must be one of {sorted(modes)}, not {collapse!r}")
+    o.collapse = modes[collapse]
     o.sah_node_cost = sah_node_cost
     o.sah_tri_cost = sah_tri_cost
     return o
@@ -64,7 +67,10 @@ def query_opts(block_size: int = 0, sort_queries: bool = True, blocks_per_sm: in
     o.blocks_per_sm = blocks_per_sm
     if short_stack:
         o.short_stack = short_stack
-    o.traversal = {"auto": 0, "thread": 1, "packet": 2}[traversal]
+    kinds = {"auto": 0, "thread": 1, "packet": 2}
+    if traversal not in kinds:
+        raise ValueError(f"traversal must be one of {sorted(kinds)}, not {traversal!r}")
+    o.traversal = kinds[traversal]
     return o
 
 

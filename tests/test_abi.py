@@ -6,6 +6,7 @@ import ctypes
 import re
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 HEADER = Path(__file__).resolve().parents[1] / "include" / "cpq.h"
@@ -143,3 +144,40 @@ def test_argument_checks_of_every_handle_kind(cpq):
     refused(lib.cp_traversal_stats(None, 0), "NULL")
     counts = (c_uint64 * 7)()
     assert lib.cp_traversal_stats(counts, 0) == 0
+
+
+def test_python_option_helpers(cpq):
+    """The binding's option structs carry what they are given and the
+    library's defaults otherwise; unknown names are refused."""
+    from gpurt_cpq import mesh as M
+
+    b = cpq.build_opts(branching=8, leaf_size=2, collapse="sah", sah_node_cost=1.5, sah_tri_cost=0.25)
+    assert (b.branching, b.leaf_size, b.collapse) == (8, 2, M.CP_COLLAPSE_SAH)
+    assert (b.sah_node_cost, b.sah_tri_cost) == (1.5, 0.25)
+    assert cpq.build_opts().collapse == M.CP_COLLAPSE_COUNT
+    d = cpq.query_opts()
+    q = cpq.query_opts(block_size=128, sort_queries=False, short_stack=24, traversal="packet")
+    assert (q.block_size, q.sort_queries, q.short_stack, q.traversal) == (128, 0, 24, 2)
+    assert (cpq.query_opts(traversal="thread").traversal, d.traversal, d.sort_queries) == (1, 0, 1)
+    r = cpq.ray_opts(tmin=1e-5, tmax=1e7, det_epsilon=1e-5, any_hit=True, sort_rays=False)
+    assert abs(r.tmin - 1e-5) < 1e-12 and r.tmax == 1e7 and r.any_hit == 1 and r.sort_rays == 0
+    with pytest.raises(ValueError, match="collapse"):
+        cpq.build_opts(collapse="median")
+    with pytest.raises(ValueError, match="traversal"):
+        cpq.query_opts(traversal="warp")
+
+
+def test_scene_transform_shapes():
+    """Scene transforms: (n, 3, 4) and (n, 4, 4) give row-major 3 x 4 rows;
+    other shapes are refused."""
+    import torch
+    from gpurt_cpq.mesh import _transforms
+
+    m = np.arange(2 * 16, dtype=np.float64).reshape(2, 4, 4)
+    want = m[:, :3, :].reshape(2, 12).astype(np.float32)
+    np.testing.assert_array_equal(_transforms(m), want)
+    np.testing.assert_array_equal(_transforms(m[:, :3, :]), want)
+    np.testing.assert_array_equal(_transforms(torch.from_numpy(m)), want)
+    for bad in (m.reshape(2, 16), m[:, :2, :], m[0]):
+        with pytest.raises(ValueError):
+            _transforms(bad)
