@@ -40,7 +40,7 @@ class ShadeParams(Structure):
                 ("qmc", c_int32), ("integrator", c_int32), ("brdf", c_int32), ("use_rr", c_int32),
                 ("use_metalness", c_int32), ("frame", c_int32), ("max_frame", c_int32),
                 ("new_samples", c_int32), ("temporal_multiplier", c_int32), ("use_temporal", c_int32),
-                ("seed", c_uint32)]
+                ("debug_view", c_int32), ("seed", c_uint32)]
 
 
 class ShadeTemporal(Structure):
@@ -217,15 +217,15 @@ class Scene:
 
     def render(self, camera: ShadeCamera, *, integrator=DIRECT, brdf=BLINN_PHONG, samples=8, max_depth=8,
                use_rr=True, qmc=False, use_metalness=False, frame=0, max_frame=256, new_samples=4,
-               temporal_multiplier=16, use_temporal=True, clear=(0.3, 0.3, 0.3), env=(0.0, 0.0, 0.0), seed=1,
-               image=None, gbuffer=False, temporal: TemporalState | None = None):
+               temporal_multiplier=16, use_temporal=True, debug_view=0, clear=(0.3, 0.3, 0.3),
+               env=(0.0, 0.0, 0.0), seed=1, image=None, gbuffer=False, temporal: TemporalState | None = None):
         """One frame, the reference's defaults unless given (rt.h:38-53;
         env_scale 0).  Returns the image (height, width, 3) and, if asked,
         the first-hit buffer (height, width, 9).  `temporal` carries ReSTIR's
         reservoirs between frames (its out_res is written)."""
         p = ShadeParams((c_float * 3)(*clear), (c_float * 3)(*env), samples, max_depth, int(qmc), integrator,
                         brdf, int(use_rr), int(use_metalness), frame, max_frame, new_samples,
-                        temporal_multiplier, int(use_temporal), seed)
+                        temporal_multiplier, int(use_temporal), debug_view, seed)
         img = np.zeros((camera.height, camera.width, 3), np.float32) if image is None else image
         assert img.dtype == np.float32 and img.flags.c_contiguous and img.shape == (camera.height, camera.width, 3)
         g = np.zeros((camera.height, camera.width, 9), np.float32) if gbuffer else None

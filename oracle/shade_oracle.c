@@ -746,14 +746,16 @@ static void res_store(const reservoir* r, orc_shade_reservoir* o) {
  * the shader leaves the reuse loop.  Buffers are read with the nearest texel
  * and repeat addressing of the G-buffer sampler (rt.cpp:449-450,
  * vulkan.cpp:522-531); a reservoir index at the image edge is clamped. */
-static int temporal_reservoir(const ctx_t* c, const hit_info* hit, const mat_info* m, const shade_info* sh,
-                              reservoir* prev) {
+/* A point projected into the previous frame (rt.rgen:459-461, 648-650):
+ * returns 0 unless it lands inside the image; then uv holds its image
+ * coordinates and g the previous first-hit buffer's nearest texel (zeros
+ * where there is no buffer). */
+static int prev_texel(const ctx_t* c, v3 pos, float uv[2], float g[9]) {
     const orc_shade_temporal* T = c->tmp;
     float pp[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     if (T && T->prev_pv) {
         const float* M = T->prev_pv;
-        for (int i = 0; i < 4; ++i)
-            pp[i] = M[4 * i] * hit->pos.x + M[4 * i + 1] * hit->pos.y + M[4 * i + 2] * hit->pos.z + M[4 * i + 3];
+        for (int i = 0; i < 4; ++i) pp[i] = M[4 * i] * pos.x + M[4 * i + 1] * pos.y + M[4 * i + 2] * pos.z + M[4 * i + 3];
     }
     pp[0] = pp[0] / pp[3];
     pp[1] = pp[1] / pp[3];
@@ -761,9 +763,20 @@ static int temporal_reservoir(const ctx_t* c, const hit_info* hit, const mat_inf
     pp[1] = (pp[1] + 1.0f) * 0.5f;
     if (!(pp[0] > 0.0f && pp[1] > 0.0f && pp[0] < 1.0f && pp[1] < 1.0f)) return 0;
     const int W = c->width, H = c->height;
-    int tx = (int)floorf(pp[0] * (float)W) % W, ty = (int)floorf(pp[1] * (float)H) % H;
-    float g[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    if (T && T->prev_gbuf) memcpy(g, T->prev_gbuf + 9 * ((int64_t)ty * W + tx), sizeof g);
+    const int tx = (int)floorf(pp[0] * (float)W) % W, ty = (int)floorf(pp[1] * (float)H) % H;
+    memset(g, 0, 9 * sizeof(float));
+    if (T && T->prev_gbuf) memcpy(g, T->prev_gbuf + 9 * ((int64_t)ty * W + tx), 9 * sizeof(float));
+    uv[0] = pp[0];
+    uv[1] = pp[1];
+    return 1;
+}
+
+static int temporal_reservoir(const ctx_t* c, const hit_info* hit, const mat_info* m, const shade_info* sh,
+                              reservoir* prev) {
+    const orc_shade_temporal* T = c->tmp;
+    float pp[2], g[9];
+    if (!prev_texel(c, hit->pos, pp, g)) return 0;
+    const int W = c->width, H = c->height;
     const v3 pd = sub(ld(g), hit->pos);
     if (dot(pd, pd) > 0.01f) return 0;
     const v3 ad = sub(ld(g + 6), m->albedo);
@@ -965,6 +978,14 @@ static void render_pixel(const ctx_t* c, const orc_shade_camera* cam, int x, int
         out[0] = avg.x;
         out[1] = avg.y;
         out[2] = avg.z;
+    }
+    if (p->debug_view > 0) { /* the previous frame's buffers, reprojected (rt.rgen:647-671) */
+        float uv[2], g[9];
+        if (dot(g_norm, g_norm) > 0.5f && prev_texel(c, g_pos, uv, g)) {
+            if (p->debug_view <= 3) memcpy(out, g + 3 * (p->debug_view - 1), 3 * sizeof(float));
+        } else {
+            out[0] = out[1] = out[2] = 0.0f;
+        }
     }
     if (gbuf) {
         const float g[9] = {g_pos.x, g_pos.y, g_pos.z, g_norm.x, g_norm.y, g_norm.z, g_alb.x, g_alb.y, g_alb.z};

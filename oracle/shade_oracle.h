@@ -73,6 +73,7 @@ typedef struct {
     int32_t new_samples;   /* ReSTIR candidates per pixel */
     int32_t temporal_multiplier;
     int32_t use_temporal;  /* ReSTIR: reuse the previous frame's reservoirs (rt.rgen:456-479) */
+    int32_t debug_view;    /* 1, 2, 3: write the previous frame's position, normal, albedo, reprojected */
     uint32_t seed;
 } orc_shade_params;
 

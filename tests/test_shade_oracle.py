@@ -425,6 +425,22 @@ def test_restir_temporal_reuse_is_unbiased():
     assert n3.max() == 16 and (n3 == 16).mean() > 0.8, np.bincount(n3)
 
 
+def test_debug_view_shows_the_previous_buffers():
+    """debug_view 1-3 (rt.rgen:647-671): each pixel shows the previous
+    frame's position, normal or albedo at its first hit reprojected; with a
+    still camera that is the pixel's own previous value; misses are 0."""
+    sc = floor_and_light()
+    st = S.TemporalState(CAM)
+    _, g0 = sc.render(CAM, integrator=S.DIRECT, samples=1, gbuffer=True)
+    st.advance(g0, CAM)
+    hit = np.abs(g0[..., 3:6]).sum(-1) > 0
+    for view in (1, 2, 3):
+        img = sc.render(CAM, integrator=S.DIRECT, samples=1, frame=1, seed=5, debug_view=view, temporal=st)
+        same = (img == g0[..., 3 * (view - 1):3 * view]).all(-1)
+        assert same[hit].mean() > 0.9, view
+        np.testing.assert_array_equal(img[~hit], 0.0)
+
+
 def test_primary_misses_and_emitters():
     sc = floor_and_light()
     cam = S.camera(eye=(0.2, 0.5, 0.0), target=(0.2, 2.0, 0.0), up=(0, 0, 1), yfov=0.3, width=4, height=4)
