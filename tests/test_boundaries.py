@@ -32,7 +32,8 @@ def test_nothing_committed_uses_scratch_paths():
         files = subprocess.run(["git", "ls-files"], cwd=ROOT, capture_output=True, text=True,
                                check=True).stdout.split()
     except (OSError, subprocess.CalledProcessError):
-        files = [str(p.relative_to(ROOT)) for p in ROOT.rglob("*") if p.is_file() and ".git" not in p.parts]
+        skip = {".git", "_work", "gpurun_out", "baseline", "__pycache__"}
+        files = [str(p.relative_to(ROOT)) for p in ROOT.rglob("*") if p.is_file() and not skip & set(p.parts)]
     pat = re.compile(r"(?<![A-Za-z0-9])_work/")
     hits = []
     for f in files:
