@@ -42,6 +42,31 @@ class GltfScene:
         return np.concatenate(vs), np.concatenate(ts).astype(np.int32)
 
 
+    def world_shading(self) -> dict[str, np.ndarray]:
+        """All instances in world space for shading, one object per instance
+        (as Scene::load adds objects): per triangle its three vertices
+        ``verts`` (T, 3, 3) and normals ``normals`` (T, 3, 3; the instance's
+        inverse-transpose applied, not renormalised) and its object ``obj``
+        (T,); per object its primitive's ``materials`` (I, 8)."""
+        vs, ns, obj, mats = [], [], [], []
+        for i, (p, w) in enumerate(zip(self.instance_primitive, self.instance_world)):
+            lo, hi = self.vert_offsets[p], self.vert_offsets[p + 1]
+            t = self.tris[self.tri_offsets[p]:self.tri_offsets[p + 1]]
+            m = w[:3, :4].astype(np.float64)
+            v = self.verts[lo:hi].astype(np.float64) @ m[:, :3].T + m[:, 3]
+            n = self.normals[lo:hi].astype(np.float64) @ np.linalg.inv(m[:, :3])
+            vs.append(v[t])
+            ns.append(n[t])
+            obj.append(np.full(len(t), i, np.int32))
+            mats.append(self.materials[p])
+        if not vs:
+            z = np.zeros((0, 3, 3), np.float32)
+            return {"verts": z, "normals": z.copy(), "obj": np.zeros(0, np.int32),
+                    "materials": np.zeros((0, 8), np.float32)}
+        return {"verts": np.concatenate(vs).astype(np.float32), "normals": np.concatenate(ns).astype(np.float32),
+                "obj": np.concatenate(obj), "materials": np.stack(mats).astype(np.float32)}
+
+
 def _array(ptr, count, dtype):
     if count == 0:
         return np.zeros(0, dtype)

@@ -551,6 +551,24 @@ def cbox_shade_scene():
     return S.Scene(np.concatenate(V), np.concatenate(N), np.concatenate(obj), albedo, emissive, mr)
 
 
+def test_gltf_world_shading_matches_the_fixture_scene(cpq):
+    """The library's reader, flattened by GltfScene.world_shading, gives the
+    shading scene built here from the fixture (the reference's Cornell box)."""
+    from pathlib import Path
+
+    path = Path("/root/reference/media/cbox/cbox.gltf")
+    if not path.exists():
+        pytest.skip("reference media not present")
+    w = cpq.load_gltf(str(path)).world_shading()
+    sc = cbox_shade_scene()
+    np.testing.assert_allclose(w["verts"].reshape(-1, 9), sc.verts, rtol=0, atol=1e-5)
+    np.testing.assert_allclose(w["normals"].reshape(-1, 9), sc.normals, rtol=0, atol=1e-5)
+    np.testing.assert_array_equal(w["obj"], sc.obj)
+    np.testing.assert_array_equal(w["materials"][:, 0:3], sc.albedo)
+    np.testing.assert_array_equal(w["materials"][:, 3:6], sc.emissive)
+    np.testing.assert_array_equal(w["materials"][:, 6:8], sc.metal_rough)
+
+
 # the glTF's camera (node CamInst): on the +z axis looking down -z, vertical
 # field of view 0.7175 rad at 4:3
 CBOX_CAM = S.camera(eye=(0.0, 0.0, 19.992091970966317), target=(0.0, 0.0, 0.0), up=(0, 1, 0),
