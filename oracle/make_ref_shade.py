@@ -1,0 +1,67 @@
+"""ORACLE recipe: compile the reference's own shading functions as C++.
+
+Reads src/shaders/rt/rtcommon.glsl and restir.glsl from a checkout of the
+reference (REFERENCE_ROOT, default /root/reference), applies the textual
+rewrites below so they compile as C++ against oracle/glsl_shim.h, writes the
+result to oracle/_ref/rtcommon_ref.h and builds oracle/_ref/libref_shade.so
+from oracle/ref_shade_wrap.cpp.  Everything it writes stays in oracle/_ref/
+(git-ignored); without a checkout it builds nothing.
+
+Rewrites (syntax only; no function body is changed):
+  - #version / #extension / #include lines are dropped;
+  - the push-constant block `layout(push_constant) uniform Constants {...} consts;`
+    becomes a C++ struct with one global instance;
+  - `inout T x` and `out T x` parameters become `T& x`;
+  - floating literals get an `f` suffix (GLSL float literals are FP32);
+  - `vec2(randf(seed), randf(seed))` becomes brace initialisation, which
+    evaluates its arguments left to right as GLSL does (C++ leaves the
+    order of function arguments unspecified).
+"""
+from __future__ import annotations
+
+import os
+import re
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+OUT = HERE / "_ref"
+LIB = OUT / "libref_shade.so"
+
+
+def rewrite(src: str) -> str:
+    lines = [ln for ln in src.splitlines() if not re.match(r"\s*#\s*(version|extension|include)\b", ln)]
+    s = "\n".join(lines)
+    s = re.sub(r"layout\s*\(\s*push_constant\s*\)\s*uniform\s+(\w+)", r"struct \1", s)
+    s = re.sub(r"\b(inout|out)\s+(\w+)\s+(\w+)", r"\2& \3", s)
+    s = re.sub(r"(?<![\w.])(\d+\.\d*(?:[eE][-+]?\d+)?|\d+[eE][-+]?\d+)(?![\w.])", r"\1f", s)
+    s = s.replace("vec2(randf(seed), randf(seed))", "vec2{randf(seed), randf(seed)}")
+    return s
+
+
+def build(ref_root: Path | None = None) -> Path | None:
+    """Generate and compile; returns the library, or None without a checkout."""
+    root = Path(ref_root or os.environ.get("REFERENCE_ROOT", "/root/reference"))
+    rt = root / "src" / "shaders" / "rt"
+    if not (rt / "rtcommon.glsl").exists():
+        return None
+    OUT.mkdir(exist_ok=True)
+    body = rewrite((rt / "rtcommon.glsl").read_text()) + "\n" + rewrite((rt / "restir.glsl").read_text())
+    hdr = OUT / "rtcommon_ref.h"
+    text = ("// generated by oracle/make_ref_shade.py from the reference's shaders; not committed\n#pragma once\n"
+            "#undef M_PI\n" + body)  # the shader's own 3.141592, not the C library's
+    if not hdr.exists() or hdr.read_text() != text:
+        hdr.write_text(text)
+    wrap = HERE / "ref_shade_wrap.cpp"
+    deps = [hdr, wrap, HERE / "glsl_shim.h"]
+    if LIB.exists() and all(LIB.stat().st_mtime >= d.stat().st_mtime for d in deps):
+        return LIB
+    subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+                    "-Wno-return-type", "-I", str(HERE), "-I", str(OUT), "-o", str(LIB), str(wrap)], check=True)
+    return LIB
+
+
+if __name__ == "__main__":
+    lib = build(Path(sys.argv[1]) if len(sys.argv) > 1 else None)
+    print(lib if lib else "no reference checkout: nothing built")

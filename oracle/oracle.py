@@ -116,6 +116,7 @@ def _shade_signatures(L) -> None:
         ("orc_sh_light_pdf", [P, c_int64, P, P, P], None),
         ("orc_sh_render", [P, P, P, P, P, P], c_int),
         ("orc_sh_tonemap", [c_int32, c_float, c_float, c_int64, P, P], c_int),
+        ("orc_sh_reservoir_stream", [ctypes.c_uint32, c_int64, P, P, P], None),
     ]:
         fn = getattr(L, name)
         fn.argtypes = args

@@ -4,15 +4,17 @@ ctypes wrapper of the FP32 restatement of the reference's path-tracer
 shading math (oracle/shade_oracle.c: rtcommon.glsl, rt.rgen, restir.glsl).
 Only tests/ may import this module; the product never does.
 
-Parity with the reference is unpinned: its shaders run only under Vulkan,
-which this machine cannot bring up, and seed their random numbers from the
-clock (rt.rgen:569).  The tests pin the restatement by hand-checked values
-(random numbers, radical inverse) and by the mathematics the shader
-implements (pdf normalisation, sampler/pdf agreement, unbiased integrators
-agreeing in expectation).
+The functions of rtcommon.glsl and restir.glsl are checked against the
+reference's own code compiled as C++ (make_ref_shade.py, ``ref=True`` below);
+the integrators of rt.rgen need the ray-tracing pipeline, which cannot run
+here, and seed their random numbers from the clock (rt.rgen:569), so the
+tests pin them by the mathematics they implement (pdf normalisation,
+sampler/pdf agreement, unbiased integrators agreeing in expectation, a
+quadrature of direct lighting).
 """
 from __future__ import annotations
 
+import ctypes
 from ctypes import Structure, byref, c_float, c_int32, c_int64, c_uint32, c_void_p
 
 import numpy as np
@@ -79,6 +81,46 @@ def _L():
     return _o.lib()
 
 
+_ref = None
+
+
+def ref_lib():
+    """The reference's own shading functions (rtcommon.glsl, restir.glsl)
+    compiled as C++ into oracle/_ref by make_ref_shade.py, or None where no
+    checkout of the reference exists."""
+    global _ref
+    if _ref is None:
+        from . import make_ref_shade
+
+        path = make_ref_shade.build()
+        if path is None:
+            _ref = False
+        else:
+            L = ctypes.CDLL(str(path))
+            P = c_void_p
+            for name, args in [("ref_tea", [c_int64, P, P, P]), ("ref_lcg_stream", [c_uint32, c_int64, P, P]),
+                               ("ref_radical_inverse", [c_int64, P, P]),
+                               ("ref_sample", [c_int32, c_int64, c_uint32, P, c_float, P, P, P]),
+                               ("ref_material", [c_int32, c_int64, P, c_float, P, P, P, P, P]),
+                               ("ref_triangle_pdf", [c_int64, P, P, P, P]), ("ref_hit_bbox", [c_int64, P, P, P, P, P]),
+                               ("ref_make_tanspace", [c_int64, P, P, P]),
+                               ("ref_reservoir_stream", [c_uint32, c_int64, P, P, P])]:
+                getattr(L, name).argtypes = args
+                getattr(L, name).restype = None
+            _ref = L
+    return _ref or None
+
+
+def _fn(name: str, ref: bool):
+    """orc_sh_<name> of the restatement, or ref_<name> of the reference's code."""
+    if ref:
+        L = ref_lib()
+        if L is None:
+            raise RuntimeError("the reference's shaders are not available here")
+        return getattr(L, "ref_" + name)
+    return getattr(_L(), "orc_sh_" + name)
+
+
 def _p(a):
     return _o._p(a)
 
@@ -87,26 +129,36 @@ def _v3(a):
     return np.ascontiguousarray(np.asarray(a, np.float32).reshape(-1, 3))
 
 
-def tea(v0, v1) -> np.ndarray:
+def tea(v0, v1, ref: bool = False) -> np.ndarray:
     a = np.ascontiguousarray(v0, np.uint32)
     b = np.ascontiguousarray(v1, np.uint32)
     out = np.empty(a.shape[0], np.uint32)
-    _L().orc_sh_tea(a.shape[0], _p(a), _p(b), _p(out))
+    _fn("tea", ref)(a.shape[0], _p(a), _p(b), _p(out))
     return out
 
 
-def lcg_stream(seed: int, n: int):
+def lcg_stream(seed: int, n: int, ref: bool = False):
     u = np.empty(n, np.uint32)
     f = np.empty(n, np.float32)
-    _L().orc_sh_lcg_stream(seed, n, _p(u), _p(f))
+    _fn("lcg_stream", ref)(seed, n, _p(u), _p(f))
     return u, f
 
 
-def radical_inverse(bits) -> np.ndarray:
+def radical_inverse(bits, ref: bool = False) -> np.ndarray:
     b = np.ascontiguousarray(bits, np.uint32)
     out = np.empty(b.shape[0], np.float32)
-    _L().orc_sh_radical_inverse(b.shape[0], _p(b), _p(out))
+    _fn("radical_inverse", ref)(b.shape[0], _p(b), _p(out))
     return out
+
+
+def reservoir_stream(seed: int, weights, ref: bool = False):
+    """res_update over `weights` from one lcg stream: the selected index and
+    w_sum after each update."""
+    w = np.ascontiguousarray(weights, np.float32)
+    chosen = np.empty(w.shape[0], np.int32)
+    ws = np.empty(w.shape[0], np.float32)
+    _fn("reservoir_stream", ref)(seed, w.shape[0], _p(w), _p(chosen), _p(ws))
+    return chosen, ws
 
 
 def _math(kind, x, y=None):
@@ -145,17 +197,17 @@ def tonemap(img, kind: int = EXPONENTIAL, exposure: float = 1.0, gamma: float = 
     return out
 
 
-def sample(kind: int, n: int, seed: int, frame, param: float = 0.0, wo=None):
+def sample(kind: int, n: int, seed: int, frame, param: float = 0.0, wo=None, ref: bool = False):
     """n draws of one sampler from one lcg stream: (directions or barycentrics, ok)."""
     f = np.ascontiguousarray(np.asarray(frame, np.float32).reshape(9))
     w = None if wo is None else np.ascontiguousarray(np.asarray(wo, np.float32).reshape(3))
     dirs = np.empty((n, 3), np.float32)
     ok = np.empty(n, np.uint8)
-    _L().orc_sh_sample(kind, n, seed, _p(f), param, _p(w), _p(dirs), _p(ok))
+    _fn("sample", ref)(kind, n, seed, _p(f), param, _p(w), _p(dirs), _p(ok))
     return dirs, ok.astype(bool)
 
 
-def material(brdf: int, albedo, roughness: float, wo, frame, wi):
+def material(brdf: int, albedo, roughness: float, wo, frame, wi, ref: bool = False):
     """(pdf, eval) of MAT_pdf / MAT_eval for directions wi at one shading point."""
     a = np.ascontiguousarray(np.asarray(albedo, np.float32).reshape(3))
     w = np.ascontiguousarray(np.asarray(wo, np.float32).reshape(3))
@@ -163,32 +215,32 @@ def material(brdf: int, albedo, roughness: float, wo, frame, wi):
     d = _v3(wi)
     pdf = np.empty(d.shape[0], np.float32)
     ev = np.empty((d.shape[0], 3), np.float32)
-    _L().orc_sh_material(brdf, d.shape[0], _p(a), roughness, _p(w), _p(f), _p(d), _p(pdf), _p(ev))
+    _fn("material", ref)(brdf, d.shape[0], _p(a), roughness, _p(w), _p(f), _p(d), _p(pdf), _p(ev))
     return pdf, ev
 
 
-def triangle_pdf(o, d, tri) -> np.ndarray:
+def triangle_pdf(o, d, tri, ref: bool = False) -> np.ndarray:
     oo, dd = _v3(o), _v3(d)
     t = np.ascontiguousarray(np.asarray(tri, np.float32).reshape(9))
     out = np.empty(oo.shape[0], np.float32)
-    _L().orc_sh_triangle_pdf(oo.shape[0], _p(oo), _p(dd), _p(t), _p(out))
+    _fn("triangle_pdf", ref)(oo.shape[0], _p(oo), _p(dd), _p(t), _p(out))
     return out
 
 
-def hit_bbox(o, d, bmin, bmax) -> np.ndarray:
+def hit_bbox(o, d, bmin, bmax, ref: bool = False) -> np.ndarray:
     oo, dd = _v3(o), _v3(d)
     lo = np.ascontiguousarray(np.asarray(bmin, np.float32).reshape(3))
     hi = np.ascontiguousarray(np.asarray(bmax, np.float32).reshape(3))
     out = np.empty(oo.shape[0], np.uint8)
-    _L().orc_sh_hit_bbox(oo.shape[0], _p(oo), _p(dd), _p(lo), _p(hi), _p(out))
+    _fn("hit_bbox", ref)(oo.shape[0], _p(oo), _p(dd), _p(lo), _p(hi), _p(out))
     return out.astype(bool)
 
 
-def make_tanspace(n):
+def make_tanspace(n, ref: bool = False):
     nn = _v3(n)
     t = np.empty_like(nn)
     b = np.empty_like(nn)
-    _L().orc_sh_make_tanspace(nn.shape[0], _p(nn), _p(t), _p(b))
+    _fn("make_tanspace", ref)(nn.shape[0], _p(nn), _p(t), _p(b))
     return t, b
 
 

@@ -1095,6 +1095,15 @@ void orc_sh_material(int32_t brdf, int64_t n, const float* albedo3, float roughn
     }
 }
 
+void orc_sh_reservoir_stream(uint32_t seed, int64_t n, const float* weights, int32_t* chosen, float* w_sum) {
+    reservoir r = res_new();
+    for (int64_t i = 0; i < n; ++i) {
+        res_update(&seed, &r, weights[i], mk((float)i, 0.0f, 0.0f), mk(0, 0, 0), mk(0, 0, 0));
+        chosen[i] = (int32_t)r.pos.x;
+        w_sum[i] = r.w_sum;
+    }
+}
+
 void orc_sh_triangle_pdf(int64_t n, const float* o, const float* d, const float* tri9, float* out) {
     const v3 a = ld(tri9), b = ld(tri9 + 3), c = ld(tri9 + 6);
     for (int64_t i = 0; i < n; ++i) out[i] = triangle_pdf(ld(o + 3 * i), ld(d + 3 * i), a, b, c);

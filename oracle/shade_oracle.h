@@ -29,8 +29,10 @@
  *    a zero determinant counting as a miss; barycentrics (1-u-v, u, v) as
  *    rt.rchit:12.
  *
- * Parity with the reference is statistical at most: its seeds come from the
- * clock and its Vulkan path cannot run here.
+ * The functions of rtcommon.glsl and restir.glsl are checked against the
+ * reference's own code compiled as C++ (make_ref_shade.py); the integrators
+ * of rt.rgen, whose seeds come from the clock and whose ray tracing needs
+ * Vulkan, only statistically and against the mathematics.
  */
 #ifndef SHADE_ORACLE_H
 #define SHADE_ORACLE_H
@@ -119,6 +121,10 @@ void orc_sh_sample(int32_t kind, int64_t n, uint32_t seed, const float* frame9, 
  * one shading point: frame9 = T, B, N; wo incoming. */
 void orc_sh_material(int32_t brdf, int64_t n, const float* albedo3, float roughness, const float* wo,
                      const float* frame9, const float* wi, float* pdf, float* eval3);
+
+/* res_update (restir.glsl:17-27) over a stream of weights from one lcg
+ * stream: after each update, the index of the selected candidate and w_sum */
+void orc_sh_reservoir_stream(uint32_t seed, int64_t n, const float* weights, int32_t* chosen, float* w_sum);
 
 /* triangle_pdf(o, d, v0, v1, v2) and hit_bbox(o, d, bmin, bmax) per ray */
 void orc_sh_triangle_pdf(int64_t n, const float* o, const float* d, const float* tri9, float* out);
