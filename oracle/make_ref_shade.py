@@ -1,16 +1,25 @@
 """ORACLE recipe: compile the reference's own shading functions as C++.
 
-Reads src/shaders/rt/rtcommon.glsl and restir.glsl from a checkout of the
-reference (REFERENCE_ROOT, default /root/reference), applies the textual
-rewrites below so they compile as C++ against oracle/glsl_shim.h, writes the
-result to oracle/_ref/rtcommon_ref.h and builds oracle/_ref/libref_shade.so
-from oracle/ref_shade_wrap.cpp.  Everything it writes stays in oracle/_ref/
+Reads src/shaders/rt/rtcommon.glsl, restir.glsl and rt.rgen (the
+ray-generation shader: camera, integrators, ReSTIR, accumulation) from a
+checkout of the reference (REFERENCE_ROOT, default /root/reference), applies
+the textual rewrites below so they compile as C++ against
+oracle/glsl_shim.h, writes the result to oracle/_ref/rtcommon_ref.h and
+builds oracle/_ref/libref_shade.so from oracle/ref_shade_wrap.cpp, linked
+against the oracle's liboracle.so (its sin / cos / pow / exp and scene
+tracer stand behind the shim).  Everything it writes stays in oracle/_ref/
 (git-ignored); without a checkout it builds nothing.
 
 Rewrites (syntax only; no function body is changed):
-  - #version / #extension / #include lines are dropped;
-  - the push-constant block `layout(push_constant) uniform Constants {...} consts;`
-    becomes a C++ struct with one global instance;
+  - #version / #extension / #include lines are dropped (the three files are
+    concatenated in include order);
+  - uniform blocks (`layout(...) uniform Name {...} inst;`, the push
+    constants and the uniform buffer) become C++ structs with one global
+    instance; storage-buffer blocks over one unsized array become a global
+    pointer (an array of such blocks, a global array of structs holding
+    one); other `layout(...) uniform T name;` declarations (images,
+    samplers, the acceleration structure) and the ray payload become plain
+    globals; `void main()` becomes `void rt_main()`;
   - `inout T x` and `out T x` parameters become `T& x`;
   - floating literals get an `f` suffix (GLSL float literals are FP32);
   - `vec2(randf(seed), randf(seed))` becomes brace initialisation, which
@@ -33,7 +42,16 @@ LIB = OUT / "libref_shade.so"
 def rewrite(src: str) -> str:
     lines = [ln for ln in src.splitlines() if not re.match(r"\s*#\s*(version|extension|include)\b", ln)]
     s = "\n".join(lines)
-    s = re.sub(r"layout\s*\(\s*push_constant\s*\)\s*uniform\s+(\w+)", r"struct \1", s)
+    lay = r"layout\s*\([^)]*\)\s*"
+    s = re.sub(lay + r"uniform\s+(\w+)\s*\{", r"struct \1 {", s)
+    s = re.sub(lay + r"(?:readonly\s+|writeonly\s+)?buffer\s+(\w+)\s*\{\s*(\w+)\s+(\w+)\s*\[\s*\]\s*;\s*\}\s*(\w+)\s*"
+               r"\[\s*\]\s*;", r"struct \1 { \2* \3; }; \1* \4;", s)
+    s = re.sub(lay + r"(?:readonly\s+|writeonly\s+)?buffer\s+(\w+)\s*\{\s*(\w+)\s+(\w+)\s*\[\s*\]\s*;\s*\}\s*;",
+               r"\2* \3;", s)
+    s = re.sub(lay + r"uniform\s+(\w+)\s+(\w+)\s*\[\s*\]\s*;", r"\1* \2;", s)
+    s = re.sub(lay + r"uniform\s+(\w+)\s+(\w+)\s*;", r"\1 \2;", s)
+    s = re.sub(lay + r"rayPayloadEXT\s+", "", s)
+    s = re.sub(r"\bvoid\s+main\s*\(\s*\)", "void rt_main()", s)
     s = re.sub(r"\b(inout|out)\s+(\w+)\s+(\w+)", r"\2& \3", s)
     s = re.sub(r"(?<![\w.])(\d+\.\d*(?:[eE][-+]?\d+)?|\d+[eE][-+]?\d+)(?![\w.])", r"\1f", s)
     s = s.replace("vec2(randf(seed), randf(seed))", "vec2{randf(seed), randf(seed)}")
@@ -47,18 +65,25 @@ def build(ref_root: Path | None = None) -> Path | None:
     if not (rt / "rtcommon.glsl").exists():
         return None
     OUT.mkdir(exist_ok=True)
-    body = rewrite((rt / "rtcommon.glsl").read_text()) + "\n" + rewrite((rt / "restir.glsl").read_text())
+    body = "\n".join(rewrite((rt / f).read_text()) for f in ("rtcommon.glsl", "restir.glsl", "rt.rgen"))
     hdr = OUT / "rtcommon_ref.h"
     text = ("// generated by oracle/make_ref_shade.py from the reference's shaders; not committed\n#pragma once\n"
             "#undef M_PI\n" + body)  # the shader's own 3.141592, not the C library's
     if not hdr.exists() or hdr.read_text() != text:
         hdr.write_text(text)
+    try:
+        from . import oracle as O  # imported as oracle.make_ref_shade
+    except ImportError:
+        import oracle as O  # run as a script from oracle/
+
+    orc = O.build()
     wrap = HERE / "ref_shade_wrap.cpp"
-    deps = [hdr, wrap, HERE / "glsl_shim.h"]
+    deps = [hdr, wrap, HERE / "glsl_shim.h", HERE / "shade_oracle.h", orc]
     if LIB.exists() and all(LIB.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return LIB
     subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
-                    "-Wno-return-type", "-I", str(HERE), "-I", str(OUT), "-o", str(LIB), str(wrap)], check=True)
+                    "-Wno-return-type", "-I", str(HERE), "-I", str(OUT), "-o", str(LIB), str(wrap),
+                    "-L", str(HERE), "-loracle", "-Wl,-rpath,$ORIGIN/.."], check=True)
     return LIB
 
 

@@ -4,13 +4,13 @@ ctypes wrapper of the FP32 restatement of the reference's path-tracer
 shading math (oracle/shade_oracle.c: rtcommon.glsl, rt.rgen, restir.glsl).
 Only tests/ may import this module; the product never does.
 
-The functions of rtcommon.glsl and restir.glsl are checked against the
-reference's own code compiled as C++ (make_ref_shade.py, ``ref=True`` below);
-the integrators of rt.rgen need the ray-tracing pipeline, which cannot run
-here, and seed their random numbers from the clock (rt.rgen:569), so the
-tests pin them by the mathematics they implement (pdf normalisation,
-sampler/pdf agreement, unbiased integrators agreeing in expectation, a
-quadrature of direct lighting).
+Everything here runs either on the restatement or (``ref=True``) on the
+reference's own rtcommon.glsl, restir.glsl and rt.rgen compiled as C++
+(make_ref_shade.py), which share only what GLSL leaves to the
+implementation (sin / cos / pow / exp and the ray tracer); the tests
+require the two to agree bit for bit, and pin the mathematics besides (pdf
+normalisation, sampler/pdf agreement, unbiased integrators agreeing in
+expectation, a quadrature of direct lighting).
 """
 from __future__ import annotations
 
@@ -107,6 +107,8 @@ def ref_lib():
                                ("ref_reservoir_stream", [c_uint32, c_int64, P, P, P])]:
                 getattr(L, name).argtypes = args
                 getattr(L, name).restype = None
+            L.ref_render.argtypes = [P] * 6
+            L.ref_render.restype = c_int32
             _ref = L
     return _ref or None
 
@@ -270,11 +272,14 @@ class Scene:
     def render(self, camera: ShadeCamera, *, integrator=DIRECT, brdf=BLINN_PHONG, samples=8, max_depth=8,
                use_rr=True, qmc=False, use_metalness=False, frame=0, max_frame=256, new_samples=4,
                temporal_multiplier=16, use_temporal=True, debug_view=0, clear=(0.3, 0.3, 0.3),
-               env=(0.0, 0.0, 0.0), seed=1, image=None, gbuffer=False, temporal: TemporalState | None = None):
+               env=(0.0, 0.0, 0.0), seed=1, image=None, gbuffer=False, temporal: TemporalState | None = None,
+               ref: bool = False):
         """One frame, the reference's defaults unless given (rt.h:38-53;
         env_scale 0).  Returns the image (height, width, 3) and, if asked,
         the first-hit buffer (height, width, 9).  `temporal` carries ReSTIR's
-        reservoirs between frames (its out_res is written)."""
+        reservoirs between frames (its out_res is written).  With `ref` the
+        frame comes from the reference's own rt.rgen compiled as C++
+        (make_ref_shade.py) instead of the restatement."""
         p = ShadeParams((c_float * 3)(*clear), (c_float * 3)(*env), samples, max_depth, int(qmc), integrator,
                         brdf, int(use_rr), int(use_metalness), frame, max_frame, new_samples,
                         temporal_multiplier, int(use_temporal), debug_view, seed)
@@ -282,7 +287,7 @@ class Scene:
         assert img.dtype == np.float32 and img.flags.c_contiguous and img.shape == (camera.height, camera.width, 3)
         g = np.zeros((camera.height, camera.width, 9), np.float32) if gbuffer else None
         ts = None if temporal is None else temporal._struct()
-        rc = _L().orc_sh_render(byref(self._s), byref(camera), byref(p), _p(img), _p(g),
+        rc = _fn("render", ref)(byref(self._s), byref(camera), byref(p), _p(img), _p(g),
                                 None if ts is None else byref(ts))
         if rc != 0:
             raise ValueError("orc_sh_render refused its arguments")

@@ -913,7 +913,8 @@ static v3 camera_ray(const orc_shade_camera* cam, const orc_shade_params* p, uin
     const float uy = ((float)y + jy) / (float)cam->height;
     const float nx = ux * 2.0f - 1.0f, ny = uy * 2.0f - 1.0f;
     const v3 r = ld(cam->right), u = ld(cam->up), f = ld(cam->fwd);
-    const float sx = nx * cam->tan_half_y * cam->aspect, sy = -(ny * cam->tan_half_y);
+    /* as the inverse projection's product would: scale x by tan * aspect */
+    const float sx = nx * (cam->tan_half_y * cam->aspect), sy = -(ny * cam->tan_half_y);
     return normalize3(comb(r, sx, u, sy, f, 1.0f));
 }
 
@@ -1093,6 +1094,19 @@ void orc_sh_material(int32_t brdf, int64_t n, const float* albedo3, float roughn
         eval3[3 * i + 1] = e.y;
         eval3[3 * i + 2] = e.z;
     }
+}
+
+float orc_sh_sin(float x) { return sh_sin(x); }
+float orc_sh_cos(float x) { return sh_cos(x); }
+float orc_sh_pow(float x, float y) { return sh_pow(x, y); }
+float orc_sh_exp(float x) { return sh_exp(x); }
+
+int32_t orc_sh_trace(const orc_shade_scene* s, const float* o, const float* d, float tmin, float tmax, int32_t any,
+                     float* u, float* v) {
+    const hit_rec h = trace(s, ld(o), ld(d), tmin, tmax, any);
+    *u = h.u;
+    *v = h.v;
+    return h.hit ? (int32_t)h.tri : -1;
 }
 
 void orc_sh_reservoir_stream(uint32_t seed, int64_t n, const float* weights, int32_t* chosen, float* w_sum) {

@@ -29,10 +29,10 @@
  *    a zero determinant counting as a miss; barycentrics (1-u-v, u, v) as
  *    rt.rchit:12.
  *
- * The functions of rtcommon.glsl and restir.glsl are checked against the
- * reference's own code compiled as C++ (make_ref_shade.py); the integrators
- * of rt.rgen, whose seeds come from the clock and whose ray tracing needs
- * Vulkan, only statistically and against the mathematics.
+ * Checked bit for bit against the reference's own rtcommon.glsl, restir.glsl
+ * and rt.rgen compiled as C++ (make_ref_shade.py), which take from this file
+ * only what GLSL leaves to the implementation: sin / cos / pow / exp and the
+ * scene tracer.
  */
 #ifndef SHADE_ORACLE_H
 #define SHADE_ORACLE_H
@@ -102,6 +102,16 @@ void orc_sh_radical_inverse(int64_t n, const uint32_t* bits, float* out);
 
 /* this file's own sin / cos / pow / exp: kind 0 sin(x), 1 cos(x), 2 pow(x, y), 3 exp(x) */
 void orc_sh_math(int32_t kind, int64_t n, const float* x, const float* y, float* out);
+
+/* the same routines one value at a time, and the renderer's scene tracer:
+ * the nearest hit (or, with `any`, the first found) with t in [tmin, tmax],
+ * its triangle (-1 on a miss) and the (u, v) of vertices 1 and 2 */
+float orc_sh_sin(float x);
+float orc_sh_cos(float x);
+float orc_sh_pow(float x, float y);
+float orc_sh_exp(float x);
+int32_t orc_sh_trace(const orc_shade_scene* s, const float* o, const float* d, float tmin, float tmax, int32_t any,
+                     float* u, float* v);
 
 /* tonemap.frag per colour component: type 0 Hable's filmic curve scaled to
  * white at 11.2, 1 exponential 1 - exp(-c exposure), both followed by

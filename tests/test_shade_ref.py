@@ -1,14 +1,17 @@
-"""The shading restatement against the reference's own shader code.
+"""The shading restatement against the reference's own shader code, bit for bit.
 
-oracle/make_ref_shade.py compiles the reference's rtcommon.glsl and
-restir.glsl as C++ (syntax rewrites only, against oracle/glsl_shim.h) from a
-checkout of the reference; these tests run both on the same inputs.  Where
-the shader uses only IEEE operations and sqrt (random numbers, reservoir
-updates, the triangle pdf, the slab test, the tangent frame, triangle
-sampling) the two agree bit for bit; where it calls pow, sin or cos (the
-materials and hemisphere samplers) the restatement's own routines stand
-against the C library's, so results agree to a few ulp and sampled
-directions to 1e-5.  Skipped where no checkout of the reference exists.
+oracle/make_ref_shade.py compiles the reference's rtcommon.glsl, restir.glsl
+and rt.rgen as C++ (syntax rewrites only, against the GLSL environment of
+oracle/glsl_shim.h) from a checkout of the reference.  GLSL leaves sin, cos,
+pow and exp to the implementation, and the ray-tracing pipeline's traversal
+to the driver: the shim takes both from the restatement, so everything else
+is the reference's code.  These tests run both on the same inputs and
+require identical results: the shader functions one by one, and whole
+frames of rt.rgen's main (every integrator and material, Russian roulette,
+Hammersley jitter, metalness, jittered later frames, ReSTIR with and without
+the previous frame's reservoirs, the debug views) on a floor under a light, a
+corner that inter-reflects, and the reference's Cornell box.  Skipped where
+no checkout of the reference exists.
 """
 from __future__ import annotations
 
@@ -27,68 +30,138 @@ def _dirs(n, seed):
     return (v / np.linalg.norm(v, axis=1, keepdims=True)).astype(np.float32)
 
 
-def test_random_numbers_bit_exact():
+def _same(a, b):
+    for x, y in zip(a, b) if isinstance(a, tuple) else ((a, b),):
+        np.testing.assert_array_equal(x, y)
+
+
+# ------------------------------------------------------------ shader functions
+
+def test_random_numbers():
     rng = np.random.default_rng(1)
     a = rng.integers(0, 2**32, 5000, dtype=np.uint64).astype(np.uint32)
     b = rng.integers(0, 2**32, 5000, dtype=np.uint64).astype(np.uint32)
-    np.testing.assert_array_equal(S.tea(a, b), S.tea(a, b, ref=True))
+    _same(S.tea(a, b), S.tea(a, b, ref=True))
     for seed in (0, 1, 0xDEADBEEF):
-        for x, y in zip(S.lcg_stream(seed, 10000), S.lcg_stream(seed, 10000, ref=True)):
-            np.testing.assert_array_equal(x, y)
-    np.testing.assert_array_equal(S.radical_inverse(a), S.radical_inverse(a, ref=True))
+        _same(S.lcg_stream(seed, 10000), S.lcg_stream(seed, 10000, ref=True))
+    _same(S.radical_inverse(a), S.radical_inverse(a, ref=True))
 
 
-def test_reservoir_updates_bit_exact():
+def test_reservoir_updates():
     w = np.random.default_rng(2).random(20000).astype(np.float32)
     w[::7] = 0.0
     for seed in (3, 99):
-        for x, y in zip(S.reservoir_stream(seed, w), S.reservoir_stream(seed, w, ref=True)):
-            np.testing.assert_array_equal(x, y)
+        _same(S.reservoir_stream(seed, w), S.reservoir_stream(seed, w, ref=True))
 
 
-def test_geometry_bit_exact():
+def test_geometry():
     n = 20000
-    rng = np.random.default_rng(4)
-    o = (rng.random((n, 3)) * 2 - 1).astype(np.float32)
+    o = (np.random.default_rng(4).random((n, 3)) * 2 - 1).astype(np.float32)
     d = _dirs(n, 5)
     tri = np.float32([[-0.4, 0.5, -0.3], [0.6, 0.6, -0.2], [0.1, 0.4, 0.7]])
-    got, want = S.triangle_pdf(o, d, tri), S.triangle_pdf(o, d, tri, ref=True)
+    want = S.triangle_pdf(o, d, tri, ref=True)
     assert (want > 0).sum() > 500
-    np.testing.assert_array_equal(got, want)
+    _same(S.triangle_pdf(o, d, tri), want)
     lo, hi = np.float32([-0.5, -0.3, -0.4]), np.float32([0.6, 0.2, 0.5])
-    np.testing.assert_array_equal(S.hit_bbox(o * 3, d, lo, hi), S.hit_bbox(o * 3, d, lo, hi, ref=True))
-    for x, y in zip(S.make_tanspace(d), S.make_tanspace(d, ref=True)):
-        np.testing.assert_array_equal(x, y)
-
-
-def test_triangle_sampling_bit_exact():
-    for x, y in zip(S.sample(S.TRIANGLE_SAMPLE, 50000, 6, FRAME), S.sample(S.TRIANGLE_SAMPLE, 50000, 6, FRAME,
-                                                                                ref=True)):
-        np.testing.assert_array_equal(x, y)
+    _same(S.hit_bbox(o * 3, d, lo, hi), S.hit_bbox(o * 3, d, lo, hi, ref=True))
+    _same(S.make_tanspace(d), S.make_tanspace(d, ref=True))
 
 
 @pytest.mark.parametrize("brdf", [S.BLINN_PHONG, S.GGX])
 @pytest.mark.parametrize("rough", [0.05, 0.3, 0.8])
-def test_materials_agree(brdf, rough):
+def test_materials(brdf, rough):
     wo = np.float32([0.45, -0.2, -0.87])
     wo /= np.linalg.norm(wo)
     wi = _dirs(50000, 7)
-    p0, e0 = S.material(brdf, [0.9, 0.5, 0.2], rough, wo, FRAME, wi)
-    p1, e1 = S.material(brdf, [0.9, 0.5, 0.2], rough, wo, FRAME, wi, ref=True)
-    np.testing.assert_array_equal(p0 == 0, p1 == 0)
-    np.testing.assert_allclose(p0, p1, rtol=2e-6, atol=1e-30)
-    np.testing.assert_allclose(e0, e1, rtol=2e-6, atol=1e-30)
+    got = S.material(brdf, [0.9, 0.5, 0.2], rough, wo, FRAME, wi)
+    assert (got[0] > 0).mean() > 0.3
+    _same(got, S.material(brdf, [0.9, 0.5, 0.2], rough, wo, FRAME, wi, ref=True))
 
 
 @pytest.mark.parametrize("kind,param", [(S.UNIFORM_HEMISPHERE, 0.0), (S.COSINE_HEMISPHERE, 0.0),
-                                        (S.COSPOW_HEMISPHERE, 7.0), (S.GGX_SAMPLE, 0.3), (S.BP_SAMPLE, 0.2)])
-def test_samplers_agree(kind, param):
+                                        (S.COSPOW_HEMISPHERE, 7.0), (S.GGX_SAMPLE, 0.3), (S.BP_SAMPLE, 0.2),
+                                        (S.TRIANGLE_SAMPLE, 0.0)])
+def test_samplers(kind, param):
     wo = np.float32([0.3, 0.1, -0.95])
     wo /= np.linalg.norm(wo)
-    d0, ok0 = S.sample(kind, 50000, 8, FRAME, param, wo=wo)
-    d1, ok1 = S.sample(kind, 50000, 8, FRAME, param, wo=wo, ref=True)
-    # the same random numbers drive both: directions agree to the ulps of sin/cos/pow
-    np.testing.assert_allclose(d0, d1, rtol=0, atol=1e-5)
-    # acceptance can differ only for directions grazing the surface
-    diff = ok0 != ok1
-    assert diff.mean() < 1e-4 and np.all(np.abs(d1[diff] @ FRAME[2]) < 1e-5)
+    _same(S.sample(kind, 50000, 8, FRAME, param, wo=wo), S.sample(kind, 50000, 8, FRAME, param, wo=wo, ref=True))
+
+
+# ------------------------------------------------------------------ frames
+
+def _scenes():
+    import test_shade_oracle as T
+
+    return {"floor": (T.floor_and_light(), T.CAM), "corner": (T.corner_and_light(), T.CAM),
+            "cbox": (T.cbox_shade_scene(), S.camera(eye=(0.0, 0.0, 19.992091970966317), target=(0.0, 0.0, 0.0),
+                                                    up=(0, 1, 0), yfov=0.7175414562225342, width=16, height=12))}
+
+
+@pytest.fixture(scope="module")
+def scenes():
+    return _scenes()
+
+
+def _frame_pair(sc, cam, **kw):
+    a = sc.render(cam, gbuffer=True, **kw)
+    b = sc.render(cam, gbuffer=True, ref=True, **kw)
+    return a, b
+
+
+@pytest.mark.parametrize("name", ["floor", "corner", "cbox"])
+@pytest.mark.parametrize("integrator", [S.DIRECT, S.MATERIAL, S.MIS, S.RESTIR_DIRECT, S.RESTIR])
+@pytest.mark.parametrize("brdf", [S.BLINN_PHONG, S.GGX])
+def test_frames_bit_exact(scenes, name, integrator, brdf):
+    sc, cam = scenes[name]
+    a, b = _frame_pair(sc, cam, integrator=integrator, brdf=brdf, samples=4, seed=11)
+    _same(a, b)
+    assert a[0].max() > 0.0
+
+
+@pytest.mark.parametrize("opts", [dict(use_rr=False, max_depth=5), dict(qmc=True, frame=3, max_frame=16),
+                                  dict(use_metalness=True, integrator=S.MIS), dict(frame=2, env=(0.2, 0.3, 0.4)),
+                                  dict(integrator=S.RESTIR, new_samples=7, temporal_multiplier=3)])
+def test_frame_options_bit_exact(scenes, opts):
+    sc, cam = scenes["corner"]
+    kw = dict(integrator=S.MIS, samples=4, seed=12)
+    kw.update(opts)
+    if kw.get("frame", 0) > 0:  # a later frame blends into the previous image
+        base = np.random.default_rng(13).random((cam.height, cam.width, 3)).astype(np.float32)
+        a = sc.render(cam, image=base.copy(), **kw)
+        b = sc.render(cam, image=base.copy(), ref=True, **kw)
+        _same(a, b)
+    else:
+        _same(*_frame_pair(sc, cam, **kw))
+
+
+@pytest.mark.parametrize("integrator", [S.RESTIR_DIRECT, S.RESTIR])
+def test_restir_across_frames_bit_exact(scenes, integrator):
+    """Four frames of temporal reuse: images, first-hit buffers and the
+    reservoirs handed to the next frame all identical."""
+    sc, cam = scenes["floor"]
+    states = [S.TemporalState(cam), S.TemporalState(cam)]
+    imgs = [np.zeros((cam.height, cam.width, 3), np.float32) for _ in range(2)]
+    for frame in range(4):
+        outs = []
+        for k, ref in enumerate((False, True)):
+            _, g = sc.render(cam, integrator=integrator, samples=2, frame=frame, seed=40 + frame, image=imgs[k],
+                             gbuffer=True, temporal=states[k], ref=ref)
+            outs.append(g)
+        _same(imgs[0], imgs[1])
+        _same(outs[0], outs[1])
+        assert states[0].out_res.tobytes() == states[1].out_res.tobytes()
+        for k in range(2):
+            states[k].advance(outs[k], cam)
+    assert states[0].prev_res["n_seen"].max() > states[0].prev_res["n_seen"].min()
+
+
+@pytest.mark.parametrize("view", [1, 2, 3])
+def test_debug_views_bit_exact(scenes, view):
+    sc, cam = scenes["floor"]
+    st = [S.TemporalState(cam), S.TemporalState(cam)]
+    for k, ref in enumerate((False, True)):
+        _, g = sc.render(cam, integrator=S.DIRECT, samples=1, gbuffer=True, ref=ref)
+        st[k].advance(g, cam)
+    a = sc.render(cam, integrator=S.DIRECT, samples=1, frame=1, seed=5, debug_view=view, temporal=st[0])
+    b = sc.render(cam, integrator=S.DIRECT, samples=1, frame=1, seed=5, debug_view=view, temporal=st[1], ref=True)
+    _same(a, b)
