@@ -1,7 +1,7 @@
 // glsl_shim.h — ORACLE: test infrastructure only.
 //
 // The GLSL types, built-ins and ray-tracing environment that the reference's
-// rtcommon.glsl, restir.glsl and rt.rgen use, in C++, so that those shader
+// rtcommon.glsl, restir.glsl, rt.rgen and tonemap.frag use, in C++, so that those shader
 // files compile as C++ (after the textual rewrites of make_ref_shade.py) and
 // serve as the reference's own code for the shading oracle.  Every
 // operation is one FP32 operation as GLSL defines it (dot and matrix
@@ -82,6 +82,9 @@ struct vec4 {
         struct {
             float x, y, z, w;
         };
+        struct {
+            float r, g, b, a;
+        };
         float c[4];
         sw2<0, 1> xy;
         sw3<0, 1, 2> xyz;
@@ -149,6 +152,7 @@ inline vec3 operator/(float s, vec3 a) { return vec3(s / a.x, s / a.y, s / a.z);
 inline vec3 operator+(float s, vec3 a) { return vec3(s + a.x, s + a.y, s + a.z); }
 inline vec3 operator-(float s, vec3 a) { return vec3(s - a.x, s - a.y, s - a.z); }
 inline vec3 operator-(vec3 a, float s) { return vec3(a.x - s, a.y - s, a.z - s); }
+inline vec3 operator+(vec3 a, float s) { return vec3(a.x + s, a.y + s, a.z + s); }
 inline vec3& operator+=(vec3& a, vec3 b) { return a = a + b; }
 inline vec3& operator*=(vec3& a, vec3 b) { return a = a * b; }
 inline vec3& operator/=(vec3& a, float s) { return a = a / s; }
@@ -174,6 +178,8 @@ inline float sin(float a) { return orc_sh_sin(a); }
 inline float cos(float a) { return orc_sh_cos(a); }
 inline float pow(float a, float b) { return orc_sh_pow(a, b); }
 inline float exp(float a) { return orc_sh_exp(a); }
+inline vec3 pow(vec3 a, vec3 b) { return vec3(pow(a.x, b.x), pow(a.y, b.y), pow(a.z, b.z)); }
+inline vec3 exp(vec3 a) { return vec3(exp(a.x), exp(a.y), exp(a.z)); }
 inline float min(float a, float b) { return std::fmin(a, b); }
 inline float max(float a, float b) { return std::fmax(a, b); }
 inline uint min(uint a, uint b) { return a < b ? a : b; }

@@ -1,7 +1,8 @@
 """ORACLE recipe: compile the reference's own shading functions as C++.
 
 Reads src/shaders/rt/rtcommon.glsl, restir.glsl and rt.rgen (the
-ray-generation shader: camera, integrators, ReSTIR, accumulation) from a
+ray-generation shader: camera, integrators, ReSTIR, accumulation), and
+src/shaders/tonemap.frag (into oracle/_ref/tonemap_ref.h), from a
 checkout of the reference (REFERENCE_ROOT, default /root/reference), applies
 the textual rewrites below so they compile as C++ against
 oracle/glsl_shim.h, writes the result to oracle/_ref/rtcommon_ref.h and
@@ -19,7 +20,8 @@ Rewrites (syntax only; no function body is changed):
     pointer (an array of such blocks, a global array of structs holding
     one); other `layout(...) uniform T name;` declarations (images,
     samplers, the acceleration structure) and the ray payload become plain
-    globals; `void main()` becomes `void rt_main()`;
+    globals, as do a stage's `layout(...) in/out` variables; `void main()`
+    becomes `void rt_main()`;
   - `inout T x` and `out T x` parameters become `T& x`;
   - floating literals get an `f` suffix (GLSL float literals are FP32);
   - `vec2(randf(seed), randf(seed))` becomes brace initialisation, which
@@ -51,6 +53,7 @@ def rewrite(src: str) -> str:
     s = re.sub(lay + r"uniform\s+(\w+)\s+(\w+)\s*\[\s*\]\s*;", r"\1* \2;", s)
     s = re.sub(lay + r"uniform\s+(\w+)\s+(\w+)\s*;", r"\1 \2;", s)
     s = re.sub(lay + r"rayPayloadEXT\s+", "", s)
+    s = re.sub(lay + r"(?:in|out)\s+(\w+)\s+(\w+)\s*;", r"\1 \2;", s)  # stage inputs and outputs
     s = re.sub(r"\bvoid\s+main\s*\(\s*\)", "void rt_main()", s)
     s = re.sub(r"\b(inout|out)\s+(\w+)\s+(\w+)", r"\2& \3", s)
     s = re.sub(r"(?<![\w.])(\d+\.\d*(?:[eE][-+]?\d+)?|\d+[eE][-+]?\d+)(?![\w.])", r"\1f", s)
@@ -77,8 +80,13 @@ def build(ref_root: Path | None = None) -> Path | None:
         import oracle as O  # run as a script from oracle/
 
     orc = O.build()
+    tm = OUT / "tonemap_ref.h"
+    tm_text = ("// generated by oracle/make_ref_shade.py from the reference's tonemap.frag; not committed\n"
+               "#pragma once\n" + rewrite((root / "src" / "shaders" / "tonemap.frag").read_text()))
+    if not tm.exists() or tm.read_text() != tm_text:
+        tm.write_text(tm_text)
     wrap = HERE / "ref_shade_wrap.cpp"
-    deps = [hdr, wrap, HERE / "glsl_shim.h", HERE / "shade_oracle.h", orc]
+    deps = [hdr, tm, wrap, HERE / "glsl_shim.h", HERE / "shade_oracle.h", orc]
     if LIB.exists() and all(LIB.stat().st_mtime >= d.stat().st_mtime for d in deps):
         return LIB
     subprocess.run(["g++", "-O2", "-std=c++17", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",

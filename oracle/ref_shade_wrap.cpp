@@ -12,6 +12,10 @@
 #include "glsl_shim.h"
 #include "rtcommon_ref.h"
 
+namespace tm {  // tonemap.frag has push constants of its own, also named Constants
+#include "tonemap_ref.h"
+}  // namespace tm
+
 static_assert(sizeof(Reservoir) == sizeof(orc_shade_reservoir), "reservoir layouts differ");
 
 namespace {
@@ -283,6 +287,20 @@ int ref_render(const orc_shade_scene* s, const orc_shade_camera* cam, const orc_
             }
         }
     if (tmp && tmp->out_res && p->integrator >= 3) std::memcpy(tmp->out_res, out.data(), np * sizeof(Reservoir));
+    return 0;
+}
+
+// tonemap.frag's curves per colour value: type 0 tonemapUT, 1 tonemapExp,
+// 2 unchanged (its main)
+int ref_tonemap(int32_t type, float exposure, float gamma, int64_t n, const float* in, float* out) {
+    if (type < 0 || type > 2) return -1;
+    tm::consts.exposure = exposure;
+    tm::consts.gamma = gamma;
+    tm::consts.type = type;
+    for (int64_t i = 0; i < n; ++i) {
+        const vec4 c(in[i], in[i], in[i], 1.0f);
+        out[i] = type == 0 ? tm::tonemapUT(c).x : type == 1 ? tm::tonemapExp(c).x : c.x;
+    }
     return 0;
 }
 

@@ -109,6 +109,8 @@ def ref_lib():
                 getattr(L, name).restype = None
             L.ref_render.argtypes = [P] * 6
             L.ref_render.restype = c_int32
+            L.ref_tonemap.argtypes = [c_int32, c_float, c_float, c_int64, P, P]
+            L.ref_tonemap.restype = c_int32
             _ref = L
     return _ref or None
 
@@ -190,11 +192,11 @@ def exp(x):
 FILMIC, EXPONENTIAL, NO_TONEMAP = range(3)
 
 
-def tonemap(img, kind: int = EXPONENTIAL, exposure: float = 1.0, gamma: float = 2.2) -> np.ndarray:
+def tonemap(img, kind: int = EXPONENTIAL, exposure: float = 1.0, gamma: float = 2.2, ref: bool = False) -> np.ndarray:
     """tonemap.frag per colour component; defaults as effect.h:25-27."""
     a = np.ascontiguousarray(img, np.float32)
     out = np.empty_like(a)
-    if _L().orc_sh_tonemap(kind, exposure, gamma, a.size, _p(a), _p(out)) != 0:
+    if _fn("tonemap", ref)(kind, exposure, gamma, a.size, _p(a), _p(out)) != 0:
         raise ValueError("unknown tone mapping")
     return out
 

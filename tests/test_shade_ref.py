@@ -1,12 +1,13 @@
 """The shading restatement against the reference's own shader code, bit for bit.
 
-oracle/make_ref_shade.py compiles the reference's rtcommon.glsl, restir.glsl
-and rt.rgen as C++ (syntax rewrites only, against the GLSL environment of
+oracle/make_ref_shade.py compiles the reference's rtcommon.glsl, restir.glsl,
+rt.rgen and tonemap.frag as C++ (syntax rewrites only, against the GLSL environment of
 oracle/glsl_shim.h) from a checkout of the reference.  GLSL leaves sin, cos,
 pow and exp to the implementation, and the ray-tracing pipeline's traversal
 to the driver: the shim takes both from the restatement, so everything else
 is the reference's code.  These tests run both on the same inputs and
-require identical results: the shader functions one by one, and whole
+require identical results: the shader functions one by one, the tone
+mapping curves, and whole
 frames of rt.rgen's main (every integrator and material, Russian roulette,
 Hammersley jitter, metalness, jittered later frames, ReSTIR with and without
 the previous frame's reservoirs, the debug views) on a floor under a light, a
@@ -85,6 +86,13 @@ def test_samplers(kind, param):
     wo = np.float32([0.3, 0.1, -0.95])
     wo /= np.linalg.norm(wo)
     _same(S.sample(kind, 50000, 8, FRAME, param, wo=wo), S.sample(kind, 50000, 8, FRAME, param, wo=wo, ref=True))
+
+
+def test_tonemapping():
+    c = np.concatenate([np.linspace(0.0, 4.0, 4001), np.geomspace(4.0, 1e4, 500)]).astype(np.float32)
+    for kind in (S.FILMIC, S.EXPONENTIAL, S.NO_TONEMAP):
+        for exposure, gamma in ((1.0, 2.2), (0.37, 1.0), (3.0, 2.4)):
+            _same(S.tonemap(c, kind, exposure, gamma), S.tonemap(c, kind, exposure, gamma, ref=True))
 
 
 # ------------------------------------------------------------------ frames
