@@ -124,6 +124,15 @@ void ref_triangle_pdf(int64_t n, const float* o, const float* d, const float* tr
         out[i] = triangle_pdf(ld3(o + 3 * i), ld3(d + 3 * i), ld3(tri9), ld3(tri9 + 3), ld3(tri9 + 6));
 }
 
+// the shader's triangle_hit (rtcommon.glsl:181-202) per ray: hit flag and point
+void ref_triangle_hit(int64_t n, const float* o, const float* d, const float* tri9, uint8_t* hit, float* hitp) {
+    for (int64_t i = 0; i < n; ++i) {
+        vec3 p;
+        hit[i] = triangle_hit(ld3(o + 3 * i), ld3(d + 3 * i), ld3(tri9), ld3(tri9 + 3), ld3(tri9 + 6), p) ? 1 : 0;
+        st3(hitp + 3 * i, p);
+    }
+}
+
 void ref_hit_bbox(int64_t n, const float* o, const float* d, const float* bmin, const float* bmax, uint8_t* out) {
     for (int64_t i = 0; i < n; ++i) out[i] = hit_bbox(ld3(o + 3 * i), ld3(d + 3 * i), ld3(bmin), ld3(bmax)) ? 1 : 0;
 }

@@ -104,6 +104,7 @@ def ref_lib():
                                ("ref_material", [c_int32, c_int64, P, c_float, P, P, P, P, P]),
                                ("ref_triangle_pdf", [c_int64, P, P, P, P]), ("ref_hit_bbox", [c_int64, P, P, P, P, P]),
                                ("ref_make_tanspace", [c_int64, P, P, P]),
+                               ("ref_triangle_hit", [c_int64, P, P, P, P, P]),
                                ("ref_reservoir_stream", [c_uint32, c_int64, P, P, P])]:
                 getattr(L, name).argtypes = args
                 getattr(L, name).restype = None
@@ -229,6 +230,17 @@ def triangle_pdf(o, d, tri, ref: bool = False) -> np.ndarray:
     out = np.empty(oo.shape[0], np.float32)
     _fn("triangle_pdf", ref)(oo.shape[0], _p(oo), _p(dd), _p(t), _p(out))
     return out
+
+
+def triangle_hit_ref(o, d, tri):
+    """The reference's own triangle_hit (rtcommon.glsl:181-202) per ray:
+    (hit, hit point)."""
+    oo, dd = _v3(o), _v3(d)
+    t = np.ascontiguousarray(np.asarray(tri, np.float32).reshape(9))
+    hit = np.empty(oo.shape[0], np.uint8)
+    p = np.zeros_like(oo)
+    _fn("triangle_hit", True)(oo.shape[0], _p(oo), _p(dd), _p(t), _p(hit), _p(p))
+    return hit.astype(bool), p
 
 
 def hit_bbox(o, d, bmin, bmax, ref: bool = False) -> np.ndarray:

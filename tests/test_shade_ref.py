@@ -173,3 +173,30 @@ def test_debug_views_bit_exact(scenes, view):
     a = sc.render(cam, integrator=S.DIRECT, samples=1, frame=1, seed=5, debug_view=view, temporal=st[0])
     b = sc.render(cam, integrator=S.DIRECT, samples=1, frame=1, seed=5, debug_view=view, temporal=st[1], ref=True)
     _same(a, b)
+
+
+# ------------------------------------------------- the ray query's arithmetic
+
+def test_ray_restatement_matches_triangle_hit():
+    """The FP32 ray restatement that the GPU ray kernels match bit for bit
+    (cpq_oracle.c, det epsilon 1e-5, t >= 0) against the reference's own
+    triangle_hit: the same hits, and o + t d is the shader's hit point."""
+    from oracle import oracle as O
+
+    rng = np.random.default_rng(21)
+    tri = np.float32([[-0.4, 0.5, -0.3], [0.6, 0.6, -0.2], [0.1, 0.4, 0.7]])
+    n = 50000
+    o = (rng.random((n, 3)) * 4 - 2).astype(np.float32)
+    # half the rays aimed at points of the triangle, half at random
+    b = rng.random((n, 2))
+    b = np.where(b.sum(1, keepdims=True) > 1, 1 - b, b)
+    target = tri[0] + b[:, :1] * (tri[1] - tri[0]) + b[:, 1:] * (tri[2] - tri[0])
+    d = np.where(np.arange(n)[:, None] % 2 == 0, target - o, rng.normal(size=(n, 3)))
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    hit, p = S.triangle_hit_ref(o, d, tri)
+    r = O.ray_brute(tri, np.int32([[0, 1, 2]]), o, d, tmin=0.0, tmax=float("inf"), det_eps=1e-5)
+    mine = r["tri"] >= 0
+    assert hit.sum() > 20000
+    np.testing.assert_array_equal(mine, hit)
+    t = r["t"][hit].astype(np.float32)[:, None]
+    np.testing.assert_array_equal(o[hit] + t * d[hit], p[hit])
