@@ -32,7 +32,10 @@ def test_nothing_committed_uses_scratch_paths():
         files = subprocess.run(["git", "ls-files"], cwd=ROOT, capture_output=True, text=True,
                                check=True).stdout.split()
     except (OSError, subprocess.CalledProcessError):
-        skip = {".git", "_work", "gpurun_out", "baseline", "__pycache__"}
+        # folders the repository ignores (entries of .gitignore naming one) are not committed
+        ignored = {ln.strip().strip("/").split("/")[0] for ln in (ROOT / ".gitignore").read_text().splitlines()
+                   if ln.strip().endswith("/") and not ln.startswith("#")}
+        skip = {".git"} | ignored
         files = [str(p.relative_to(ROOT)) for p in ROOT.rglob("*") if p.is_file() and not skip & set(p.parts)]
     pat = re.compile(r"(?<![A-Za-z0-9])_work/")
     hits = []
