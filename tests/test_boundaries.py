@@ -32,11 +32,24 @@ def test_nothing_committed_uses_scratch_paths():
         files = subprocess.run(["git", "ls-files"], cwd=ROOT, capture_output=True, text=True,
                                check=True).stdout.split()
     except (OSError, subprocess.CalledProcessError):
-        # folders the repository ignores (entries of .gitignore naming one) are not committed
-        ignored = {ln.strip().strip("/").split("/")[0] for ln in (ROOT / ".gitignore").read_text().splitlines()
-                   if ln.strip().endswith("/") and not ln.startswith("#")}
-        skip = {".git"} | ignored
-        files = [str(p.relative_to(ROOT)) for p in ROOT.rglob("*") if p.is_file() and not skip & set(p.parts)]
+        # folders the repository ignores (.gitignore entries ending in "/") are not committed:
+        # an entry with an inner "/" is a path from the root, others match any folder name
+        import fnmatch
+
+        dirs = [ln.strip().strip("/") for ln in (ROOT / ".gitignore").read_text().splitlines()
+                if ln.strip().endswith("/") and not ln.startswith("#")]
+
+        def ignored(rel: Path) -> bool:
+            parts = rel.parts[:-1]
+            for d in dirs:
+                if "/" in d:
+                    if "/".join(parts).startswith(d):
+                        return True
+                elif any(fnmatch.fnmatch(q, d) for q in parts):
+                    return True
+            return ".git" in parts
+
+        files = [str(p.relative_to(ROOT)) for p in ROOT.rglob("*") if p.is_file() and not ignored(p.relative_to(ROOT))]
     pat = re.compile(r"(?<![A-Za-z0-9])_work/")
     hits = []
     for f in files:
