@@ -24,9 +24,17 @@ from MEASURED_PEAKS.json and BW_L2 measured here; frac = t_roof / t_kernel.
 Multi-GPU: the path needs no exchange; each rank runs the same workload on its
 own GPU (replicas, weak scaling), barrier + max-over-ranks timing.
 
+The headline line also carries `forms`: the three other targets, each measured
+in the same run on the same GPU with its own clock record (forward + backward
+over forward on the torus workload, the batched workload against per-mesh
+launches, and the dynamic soup loop's time per iteration).
+
 --impl reference: the reference's closest-point code is not in its mounted
 tree (its FCPW-GPU branch is absent), so the reference arm times the CPU
-restatement of the same algorithm (the oracle port) on all host cores.
+restatement of the same algorithm (the oracle port) on all host cores, on the
+same workload and config: every step is all 16,777,216 queries.  It loads the
+workload generator by file path, so no CUDA library of this package is mapped
+into that process.
 """
 from __future__ import annotations
 
@@ -50,15 +58,26 @@ import numpy as np  # noqa: E402
 METRIC = "closest-point queries/s (large heightfield, 2.09M tris, 16M queries)"
 UNIT = "queries/s"
 N_QUERIES = 16 * (1 << 20)
+DATA = "synthetic (seeded heightfield + queries, generated on the host)"
+
+
+def bench_config(world: int) -> dict:
+    """The workload both arms run, identical in each arm's JSON line."""
+    return {"workload": "large heightfield: 1024x1024 vertices (2,093,058 tris), 16,777,216 queries "
+                        "(50% near-surface sigma 0.01, 50% box)",
+            "l2": "inputs larger than L2 (201 MB queries + 336 MB outputs per step, and the BVH's "
+                  "nodes and triangle records); no flush",
+            "parallelism": f"replicas x{world}"}
 B_IO = 32.0
 # canonical visit counts (binary LBVH, leaf 4) of this seeded workload, from the
 # CPU restatement on the first 65,536 queries; re-measured in the CPU leg
 CANON_V_NODE = 84.273
 CANON_V_TRI = 44.413
-# DRAM bytes (read + write) per query of one traversal launch, from the ncu
-# capture summarised in profiles/k_traverse_packet_large_heightfield.md
-# (4.220 + 1.714 GB for 16,777,216 queries, leaf 8)
-NCU_TRAFFIC_PER_QUERY = 353.7
+# DRAM bytes (read + write) per query of one traversal launch at the leaf size
+# the autotuner picks for this workload, from one ncu capture of
+# dram__bytes_read.sum + dram__bytes_write.sum on the same command; keyed by
+# leaf size so a run that picks another leaf reports null, not a stale figure
+NCU_TRAFFIC_PER_QUERY = {8: 353.7}
 # Adjoint per query: reads q 12 + triangle 4 + barycentrics 8 + upstream
 # gradient 4 + 3 vertex indices 12 + 3 vertices 36; writes d/dq 12 and three
 # atomic read-modify-writes of 12 B to d/dvertices (72)
@@ -81,6 +100,8 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=1 << 21,
                     help="queries timed on the host cores for the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the torus, batched and dynamic forms in the headline run")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--leaf", type=int, default=0)
     ap.add_argument("--workload", default="large",
@@ -202,10 +223,24 @@ def measure_l2_gbs(torch) -> float:
     return best
 
 
-def workload():
-    from gpurt_cpq import workloads as W
+def workloads_module():
+    """gpurt_cpq/workloads.py loaded by file path: the generators are numpy
+    only, and importing them through the package would map its CUDA library
+    into a process that must not use it (the reference arm)."""
+    import importlib.util
 
-    return W.large()
+    name = "gpurt_cpq_workloads_standalone"
+    if name in sys.modules:
+        return sys.modules[name]
+    spec = importlib.util.spec_from_file_location(name, PKG / "gpurt_cpq" / "workloads.py")
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def workload():
+    return workloads_module().large()
 
 
 def cpu_leg(v, t, q, sample: int) -> dict:
@@ -232,6 +267,8 @@ def emit(obj):
 
 
 def reference_arm(args):
+    """The CPU restatement (oracle port) on all host cores over the same
+    workload: every warm-up and timed step queries all 16,777,216 points."""
     rank, world, _ = dist_env()
     if world > 1:
         import torch.distributed as td
@@ -249,25 +286,20 @@ def reference_arm(args):
     t0 = time.perf_counter()
     tree = O.Tree(v, t, 2, 4, 0)
     build_s = time.perf_counter() - t0
-    per_step = min(args.cpu_sample, q.shape[0])
-    for w in range(args.warmup):
-        tree.query(q[w * per_step % q.shape[0]:][:per_step], threads=threads)
+    for _ in range(args.warmup):
+        tree.query(q, threads=threads)
     secs = 0.0
-    done = 0
-    for k in range(args.steps):
-        off = (k * per_step) % (q.shape[0] - per_step + 1)
-        r = tree.query(q[off:off + per_step], threads=threads)
-        secs += r["seconds"]
-        done += per_step
-    value = done / secs
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        tree.query(q, threads=threads)
+        secs += time.perf_counter() - t0
+    value = q.shape[0] * args.steps / secs
     emit({"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-          "data": "synthetic (seeded heightfield + queries)",
-          "config": {"workload": "large heightfield: 1024x1024 vertices (2,093,058 tris), 16,777,216 "
-                                 "queries; each step a bounded sample", "sample_per_step": per_step},
+          "data": DATA, "config": bench_config(world),
           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                           "sample": f"{per_step} queries per step, canonical binary LBVH leaf 4 "
+                           "sample": f"all {q.shape[0]} queries per step, canonical binary LBVH leaf 4 "
                                      f"(built in {build_s:.2f} s), {cpu_model()}; the reference's "
                                      "own closest-point code is absent from its tree"},
           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
@@ -393,7 +425,7 @@ def our_arm(args):
     peak_eff = (B_IO + b_trav) / t_roof / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak_eff, "unit": "GB/s",
                 "frac": achieved / peak_eff, "of": "measured",
-                "traffic": None if NCU_TRAFFIC_PER_QUERY is None else NCU_TRAFFIC_PER_QUERY * nq,
+                "traffic": NCU_TRAFFIC_PER_QUERY[leaf] * nq if leaf in NCU_TRAFFIC_PER_QUERY else None,
                 "kernel": "k_traverse_packet" if packet_visits else "k_traverse",
                 "kernel_ms_per_launch": trav_ms,
                 "model": "t_roof = B_io/BW_HBM + B_trav/BW_L2 (algorithmic bytes of the canonical "
@@ -402,31 +434,27 @@ def our_arm(args):
                 "hbm_gbs": hbm, "l2_gbs_measured": l2_gbs,
                 "hbm_only_frac": B_IO / t_kernel / 1e9 / hbm,
                 "packet_counters": packet_visits}
-    # read by the traversal: K-wide nodes (32K B), 48-B exact and 80-B test records
-    traversal_mb = (info.num_wide_nodes * 32 * 4 + info.num_triangles * (48 + 80)) / 1e6
+    forms = None
+    if world == 1 and not args.no_forms:
+        forms = run_forms(args)
     if rank == 0:
+        build_gbs = (BUILD_BYTES_PER_TRI * info.num_triangles / (info.build_ms * 1e-3) / 1e9
+                     if info.build_ms > 0 else None)
         res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-               "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-               "data": "synthetic (seeded heightfield + queries, generated on the host)",
-               "config": {"workload": "large heightfield: 1024x1024 vertices (2,093,058 tris), "
-                                      "16,777,216 queries (50% near-surface sigma 0.01, 50% box)",
-                          "branching": 4, "leaf_size": leaf, "autotuned": tuned,
-                          "block_size": qopts.block_size, "short_stack": qopts.short_stack,
-                          "sort_queries": bool(qopts.sort_queries),
-                          "wide_nodes": info.num_wide_nodes, "build_ms": info.build_ms,
-                          "build_roofline": {
-                              "bytes_per_triangle": BUILD_BYTES_PER_TRI,
-                              "achieved_gbs": BUILD_BYTES_PER_TRI * info.num_triangles / (info.build_ms * 1e-3) / 1e9
-                              if info.build_ms > 0 else None,
-                              "frac_of_hbm": BUILD_BYTES_PER_TRI * info.num_triangles / (info.build_ms * 1e-3) / 1e9
-                              / measured_peaks()["hbm_gbs"] if info.build_ms > 0 else None},
-                          "l2": f"inputs larger than L2 ({nq * 12 / 1e6:.0f} MB queries + "
-                                f"{nq * 20 / 1e6:.0f} MB outputs + {traversal_mb:.0f} MB of nodes and "
-                                "triangle records per step); no flush",
-                          "parallelism": f"replicas x{world}"},
+               "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": DATA,
+               "config": bench_config(world),
+               "build": {"branching": 4, "leaf_size": leaf, "autotuned": tuned,
+                         "block_size": qopts.block_size, "short_stack": qopts.short_stack,
+                         "sort_queries": bool(qopts.sort_queries),
+                         "wide_nodes": info.num_wide_nodes, "build_ms": info.build_ms,
+                         "build_roofline": {"bytes_per_triangle": BUILD_BYTES_PER_TRI,
+                                            "achieved_gbs": build_gbs,
+                                            "frac_of_hbm": build_gbs / hbm if build_gbs else None}},
                "e2e": e2e, "roofline": roofline, "gpu_launches": int(launches),
                "clocks": clk}
+        if forms is not None:
+            res["forms"] = forms
         if cpu is not None:
             res["cpu_baseline"] = {k: cpu[k] for k in ("value", "unit", "cores", "kind", "sample")}
         emit(res)
@@ -460,7 +488,21 @@ def _line(metric, value, unit, ms, args, config, extra):
     emit(res)
 
 
-def torus_arm(args):
+def _form(metric, value, unit, ms, steps, warmup, config, extra) -> dict:
+    """One form's result: what its own JSON line carries."""
+    res = {"metric": metric, "value": value, "unit": unit, "ms_per_step": ms, "steps": steps,
+           "warmup": warmup, "config": config}
+    res.update(extra)
+    return res
+
+
+def _emit_form(args, f: dict):
+    extra = {k: v for k, v in f.items()
+             if k not in ("metric", "value", "unit", "ms_per_step", "steps", "warmup", "config")}
+    _line(f["metric"], f["value"], f["unit"], f["ms_per_step"], args, f["config"], extra)
+
+
+def torus_form(steps: int, warmup: int) -> dict:
     """Forward + adjoint on the differentiable workload vs forward alone."""
     import torch
 
@@ -485,26 +527,30 @@ def torus_arm(args):
         gv.zero_()
         mesh.backward(qd, out.tri, out.bary, gd, grad_verts=gv)
 
-    ms_f = _timed(torch, fwd, args.steps, args.warmup)
-    ms_fb = _timed(torch, fwd_bwd, args.steps, args.warmup)
+    ms_f = _timed(torch, fwd, steps, warmup)
+    ms_fb = _timed(torch, fwd_bwd, steps, warmup)
 
     def bwd():
         gv.zero_()
         mesh.backward(qd, out.tri, out.bary, gd, grad_verts=gv)
 
-    ms_b = _timed(torch, bwd, args.steps, args.warmup)
+    ms_b = _timed(torch, bwd, steps, warmup)
     bwd_gbs = BWD_BYTES_PER_QUERY * nq / (ms_b * 1e-3) / 1e9
-    _line("closest-point fwd+bwd queries/s (torus 200k tris, 4M queries)", nq / (ms_fb * 1e-3),
-          "queries/s", ms_fb, args,
-          {"workload": "torus R=1 r=0.3 500x200 (200,000 tris), 4,194,304 queries U[-1.5,1.5]^3, "
-                       "upstream gradient N(0,1); forward caches (tri, bary), adjoint recomputes",
-           "branching": 4, "leaf_size": 2},
-          {"forward_only": {"value": nq / (ms_f * 1e-3), "ms_per_step": ms_f},
-           "backward_only": {"value": nq / (ms_b * 1e-3), "ms_per_step": ms_b,
-                             "roofline": {"bound": "hbm", "achieved": bwd_gbs, "peak": measured_peaks()["hbm_gbs"],
-                                          "unit": "GB/s", "frac": bwd_gbs / measured_peaks()["hbm_gbs"],
-                                          "of": "measured", "bytes_per_query": BWD_BYTES_PER_QUERY}},
-           "fwd_bwd_over_fwd": ms_fb / ms_f, "target_fwd_bwd_over_fwd": 2.5})
+    return _form("closest-point fwd+bwd queries/s (torus 200k tris, 4M queries)", nq / (ms_fb * 1e-3),
+                 "queries/s", ms_fb, steps, warmup,
+                 {"workload": "torus R=1 r=0.3 500x200 (200,000 tris), 4,194,304 queries U[-1.5,1.5]^3, "
+                              "upstream gradient N(0,1); forward caches (tri, bary), adjoint recomputes",
+                  "branching": 4, "leaf_size": 2},
+                 {"forward_only": {"value": nq / (ms_f * 1e-3), "ms_per_step": ms_f},
+                  "backward_only": {"value": nq / (ms_b * 1e-3), "ms_per_step": ms_b,
+                                    "roofline": {"bound": "hbm", "achieved": bwd_gbs, "peak": measured_peaks()["hbm_gbs"],
+                                                 "unit": "GB/s", "frac": bwd_gbs / measured_peaks()["hbm_gbs"],
+                                                 "of": "measured", "bytes_per_query": BWD_BYTES_PER_QUERY}},
+                  "fwd_bwd_over_fwd": ms_fb / ms_f, "target_fwd_bwd_over_fwd": 2.5})
+
+
+def torus_arm(args):
+    _emit_form(args, torus_form(args.steps, args.warmup))
 
 
 def rays_arm(args):
@@ -536,7 +582,7 @@ def rays_arm(args):
            "hit_fraction": float((r.tri >= 0).float().mean())})
 
 
-def batched_arm(args):
+def batched_form(steps: int, warmup: int) -> dict:
     """256 uneven meshes: one batched build + one persistent graph-captured
     launch, against plain per-mesh builds and launches on the same GPU."""
     import torch
@@ -562,7 +608,7 @@ def batched_arm(args):
     def batched_step():
         batch.query(Qd, qoff, workspace=ws, opts=o, use_graph=True, out=out)
 
-    ms_b = _timed(torch, batched_step, args.steps, args.warmup)
+    ms_b = _timed(torch, batched_step, steps, warmup)
     d_batched = out.dist.clone()
     # plain per-mesh: one build and one launch sequence per mesh
     vparts = [Vd[voff[i]:voff[i + 1]] for i in range(len(meshes))]
@@ -583,22 +629,26 @@ def batched_arm(args):
         for i in range(len(meshes)):
             plain[i].query(qparts[i], workspace=wss[i], opts=o, out=outs[i])
 
-    ms_p = _timed(torch, plain_step, args.steps, args.warmup)
+    ms_p = _timed(torch, plain_step, steps, warmup)
     rel = float(((out.dist - d_batched).abs() / d_batched.clamp_min(1e-30)).max())
     tri_counts = [int(toff[i + 1] - toff[i]) for i in range(len(meshes))]
-    _line("closest-point queries/s (batched: 256 uneven meshes, one launch)", nq / (ms_b * 1e-3),
-          "queries/s", ms_b, args,
-          {"workload": f"256 deformed icospheres/tori, {int(toff[-1])} tris "
-                       f"({min(tri_counts)}..{max(tri_counts)} per mesh), {nq} queries "
-                       f"({int(np.diff(qoff).min())}..{int(np.diff(qoff).max())} per mesh)",
-           "branching": 4, "leaf_size": 2, "graph": True},
-          {"per_mesh_launches": {"value": nq / (ms_p * 1e-3), "ms_per_step": ms_p},
-           "speedup_vs_per_mesh": ms_p / ms_b, "target_speedup": 3.0,
-           "max_rel_diff_batched_vs_per_mesh": rel,
-           "build_ms": {"batched": build_batch_ms, "per_mesh_total": build_plain_ms}})
+    return _form("closest-point queries/s (batched: 256 uneven meshes, one launch)", nq / (ms_b * 1e-3),
+                 "queries/s", ms_b, steps, warmup,
+                 {"workload": f"256 deformed icospheres/tori, {int(toff[-1])} tris "
+                              f"({min(tri_counts)}..{max(tri_counts)} per mesh), {nq} queries "
+                              f"({int(np.diff(qoff).min())}..{int(np.diff(qoff).max())} per mesh)",
+                  "branching": 4, "leaf_size": 2, "graph": True},
+                 {"per_mesh_launches": {"value": nq / (ms_p * 1e-3), "ms_per_step": ms_p},
+                  "speedup_vs_per_mesh": ms_p / ms_b, "target_speedup": 3.0,
+                  "max_rel_diff_batched_vs_per_mesh": rel,
+                  "build_ms": {"batched": build_batch_ms, "per_mesh_total": build_plain_ms}})
 
 
-def dynamic_arm(args):
+def batched_arm(args):
+    _emit_form(args, batched_form(args.steps, args.warmup))
+
+
+def dynamic_form(steps: int, warmup: int) -> dict:
     """8M-triangle soup: per iteration perturb the vertices, refit, query 64M
     fixed points and 1M moving points, adjoint on the moving points, and a
     gradient step on their squared distance."""
@@ -645,7 +695,7 @@ def dynamic_arm(args):
     side = torch.cuda.Stream()
     side.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(side):
-        for _ in range(max(1, args.warmup)):
+        for _ in range(max(1, warmup)):
             iteration()
     torch.cuda.current_stream().wait_stream(side)
     graph = torch.cuda.CUDAGraph()
@@ -665,14 +715,47 @@ def dynamic_arm(args):
     rebuild_ms = (time.perf_counter() - t0) * 1e3
     del rebuilt
     nq = qfix.shape[0] + pts.shape[0]
-    _line("closest-point queries/s (dynamic soup loop: refit + fwd + bwd per iteration)",
-          nq / (ms * 1e-3), "queries/s", ms, args,
-          {"workload": "4,096 Gaussian clusters x 2,048 tris (8,388,608-tri soup), vertices "
-                       "perturbed N(0,1e-4) per iteration, 67,108,864 fixed + 1,048,576 moving "
-                       "queries, 50 iterations of refit + forward + adjoint + step",
-           "branching": 4, "leaf_size": 2, "iterations": iters, "graph": True},
-          {"build_ms": build_ms, "rebuild_ms": rebuild_ms, "final_mean_dist":
-           float(outp.dist.mean())})
+    return _form("closest-point queries/s (dynamic soup loop: refit + fwd + bwd per iteration)",
+                 nq / (ms * 1e-3), "queries/s", ms, iters, max(1, warmup),
+                 {"workload": "4,096 Gaussian clusters x 2,048 tris (8,388,608-tri soup), vertices "
+                              "perturbed N(0,1e-4) per iteration, 67,108,864 fixed + 1,048,576 moving "
+                              "queries, 50 iterations of refit + forward + adjoint + step",
+                  "branching": 4, "leaf_size": 2, "iterations": iters, "graph": True},
+                 {"build_ms": build_ms, "rebuild_ms": rebuild_ms, "final_mean_dist":
+                  float(outp.dist.mean())})
+
+
+def dynamic_arm(args):
+    _emit_form(args, dynamic_form(args.steps, args.warmup))
+
+
+def run_forms(args) -> dict:
+    """The torus, batched and dynamic forms in the headline run, each timed
+    like its own `--workload` line (at most 10 timed steps, at least 3 warm-up
+    steps) with the SM clocks sampled while it runs."""
+    import torch
+
+    steps, warmup = max(1, min(args.steps, 10)), max(3, min(args.warmup, 5))
+    out = {}
+    for key, fn, keep in (
+            ("torus_fwd_bwd", torus_form, ("fwd_bwd_over_fwd", "target_fwd_bwd_over_fwd", "forward_only",
+                                           "backward_only")),
+            ("batched", batched_form, ("speedup_vs_per_mesh", "target_speedup", "per_mesh_launches",
+                                       "max_rel_diff_batched_vs_per_mesh", "autotuned")),
+            ("dynamic", dynamic_form, ("build_ms", "rebuild_ms"))):
+        torch.cuda.synchronize()
+        clocks = ClockSampler(torch.cuda.current_device())
+        f = fn(steps, warmup)
+        torch.cuda.synchronize()
+        clk = clocks.stop()
+        entry = {k: f[k] for k in ("metric", "value", "unit", "ms_per_step", "steps", "warmup") if k in f}
+        entry["workload"] = f["config"]["workload"]
+        entry.update({k: f[k] for k in keep if k in f})
+        entry["clocks"] = clk
+        out[key] = entry
+        torch.cuda.empty_cache()
+    out["dynamic"]["ms_per_iteration"] = out["dynamic"]["ms_per_step"]
+    return out
 
 
 def small_arm(args):

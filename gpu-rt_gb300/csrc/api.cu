@@ -1097,11 +1097,12 @@ CP_API cp_status cp_scene_ray_query(const cp_scene* scene, const float* origins,
 
 // ---- inspection ------------------------------------------------------------
 
-CP_API cp_status cp_mesh_export_build(const cp_mesh* m, uint64_t* keys, int32_t* order, int32_t* left,
-                                      int32_t* right, int32_t* parent, uint8_t* cluster,
-                                      int32_t* wide_src) {
-    if (!m) return fail(CP_ERROR_INVALID_VALUE, "mesh is NULL");
-    const Bvh& b = m->bvh;
+}  // extern "C"
+
+namespace {
+
+cp_status export_build(const Bvh& b, uint64_t* keys, int32_t* order, int32_t* left, int32_t* right,
+                       int32_t* parent, uint8_t* cluster, int32_t* wide_src) {
     const int64_t n = b.nt, nn = 2 * n - 1;
     CP_CUDA(cudaDeviceSynchronize(), "export");
     if (keys) CP_CUDA(cudaMemcpy(keys, b.keys, 8 * n, cudaMemcpyDeviceToHost), "export");
@@ -1114,9 +1115,7 @@ CP_API cp_status cp_mesh_export_build(const cp_mesh* m, uint64_t* keys, int32_t*
     return CP_SUCCESS;
 }
 
-CP_API cp_status cp_mesh_export_wide(const cp_mesh* m, float* boxes, int32_t* refs, int32_t* counts) {
-    if (!m) return fail(CP_ERROR_INVALID_VALUE, "mesh is NULL");
-    const Bvh& b = m->bvh;
+cp_status export_wide(const Bvh& b, float* boxes, int32_t* refs, int32_t* counts) {
     const int K = b.p.K;
     const size_t node_bytes = (size_t)32 * K;
     std::vector<unsigned char> h(node_bytes * (size_t)b.num_wide);
@@ -1145,6 +1144,34 @@ CP_API cp_status cp_mesh_export_wide(const cp_mesh* m, float* boxes, int32_t* re
         }
     }
     return CP_SUCCESS;
+}
+
+}  // namespace
+
+extern "C" {
+
+CP_API cp_status cp_mesh_export_build(const cp_mesh* m, uint64_t* keys, int32_t* order, int32_t* left,
+                                      int32_t* right, int32_t* parent, uint8_t* cluster,
+                                      int32_t* wide_src) {
+    if (!m) return fail(CP_ERROR_INVALID_VALUE, "mesh is NULL");
+    return export_build(m->bvh, keys, order, left, right, parent, cluster, wide_src);
+}
+
+CP_API cp_status cp_mesh_export_wide(const cp_mesh* m, float* boxes, int32_t* refs, int32_t* counts) {
+    if (!m) return fail(CP_ERROR_INVALID_VALUE, "mesh is NULL");
+    return export_wide(m->bvh, boxes, refs, counts);
+}
+
+CP_API cp_status cp_batch_export_build(const cp_batch* bt, uint64_t* keys, int32_t* order, int32_t* left,
+                                       int32_t* right, int32_t* parent, uint8_t* cluster,
+                                       int32_t* wide_src) {
+    if (!bt) return fail(CP_ERROR_INVALID_VALUE, "batch is NULL");
+    return export_build(bt->bvh, keys, order, left, right, parent, cluster, wide_src);
+}
+
+CP_API cp_status cp_batch_export_wide(const cp_batch* bt, float* boxes, int32_t* refs, int32_t* counts) {
+    if (!bt) return fail(CP_ERROR_INVALID_VALUE, "batch is NULL");
+    return export_wide(bt->bvh, boxes, refs, counts);
 }
 
 }  // extern "C"

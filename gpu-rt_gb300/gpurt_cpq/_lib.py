@@ -125,6 +125,9 @@ SIGNATURES = {
     "cp_mesh_export_build": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                        c_void_p, c_void_p]),
     "cp_mesh_export_wide": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "cp_batch_export_build": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
+                                        c_void_p, c_void_p]),
+    "cp_batch_export_wide": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p]),
 }
 
 

@@ -248,29 +248,35 @@ class Mesh:
 
     # -- inspection ----------------------------------------------------------
     def export_build(self) -> dict:
-        n = self.num_triangles
-        info = self.info()
-        out = {"keys": np.empty(n, np.uint64), "order": np.empty(n, np.int32),
-               "left": np.empty(max(n - 1, 1), np.int32), "right": np.empty(max(n - 1, 1), np.int32),
-               "parent": np.empty(2 * n - 1, np.int32), "cluster": np.empty(2 * n - 1, np.uint8),
-               "wide_src": np.empty(info.num_wide_nodes, np.int32)}
-        check(lib.cp_mesh_export_build(self._h, *(c_void_p(out[k].ctypes.data) for k in
-                                                  ("keys", "order", "left", "right", "parent",
-                                                   "cluster", "wide_src"))), "export")
-        if n == 1:
-            out["left"] = out["left"][:0]
-            out["right"] = out["right"][:0]
-        return out
+        return _export_build(lib.cp_mesh_export_build, self._h, self.num_triangles,
+                             self.info().num_wide_nodes)
 
     def export_wide(self) -> dict:
         info = self.info()
-        K, w = info.branching, info.num_wide_nodes
-        out = {"boxes": np.empty(w * 6 * K, np.float32), "refs": np.empty(w * K, np.int32),
-               "counts": np.empty(w * K, np.int32)}
-        check(lib.cp_mesh_export_wide(self._h, c_void_p(out["boxes"].ctypes.data),
-                                      c_void_p(out["refs"].ctypes.data),
-                                      c_void_p(out["counts"].ctypes.data)), "export")
-        return out
+        return _export_wide(lib.cp_mesh_export_wide, self._h, info.branching, info.num_wide_nodes)
+
+
+def _export_build(fn, handle, n: int, num_wide: int) -> dict:
+    """The build's intermediate arrays (cp_mesh_export_build / cp_batch_export_build)."""
+    out = {"keys": np.empty(n, np.uint64), "order": np.empty(n, np.int32),
+           "left": np.empty(max(n - 1, 1), np.int32), "right": np.empty(max(n - 1, 1), np.int32),
+           "parent": np.empty(2 * n - 1, np.int32), "cluster": np.empty(2 * n - 1, np.uint8),
+           "wide_src": np.empty(num_wide, np.int32)}
+    check(fn(handle, *(c_void_p(out[k].ctypes.data) for k in
+                       ("keys", "order", "left", "right", "parent", "cluster", "wide_src"))), "export")
+    if n == 1:
+        out["left"] = out["left"][:0]
+        out["right"] = out["right"][:0]
+    return out
+
+
+def _export_wide(fn, handle, K: int, w: int) -> dict:
+    """Wide-node boxes, child refs and counts (cp_mesh_export_wide / cp_batch_export_wide)."""
+    out = {"boxes": np.empty(w * 6 * K, np.float32), "refs": np.empty(w * K, np.int32),
+           "counts": np.empty(w * K, np.int32)}
+    check(fn(handle, c_void_p(out["boxes"].ctypes.data), c_void_p(out["refs"].ctypes.data),
+             c_void_p(out["counts"].ctypes.data)), "export")
+    return out
 
 
 class Batch:
@@ -312,6 +318,15 @@ class Batch:
         o = opts or query_opts()
         check(lib.cp_batch_query_workspace_size(self._h, nq, byref(o), byref(b)), "workspace")
         return b.value
+
+    def export_build(self) -> dict:
+        info = self.info()
+        return _export_build(lib.cp_batch_export_build, self._h, info["num_triangles"],
+                             info["num_wide_nodes"])
+
+    def export_wide(self) -> dict:
+        return _export_wide(lib.cp_batch_export_wide, self._h, self.opts.branching,
+                            self.info()["num_wide_nodes"])
 
     def query(self, points: torch.Tensor, q_offsets, *, want_point: bool = True,
               want_bary: bool = False, opts: QueryOpts | None = None,

@@ -344,16 +344,22 @@ CP_API cp_status cp_ray_query(const cp_mesh* mesh, const float* origins, const f
  * host owns all device memory, or code running while its own allocator holds
  * a lock.  Same arguments and results as cp_query, minus the workspace: the
  * scratch comes from a fixed 32 MiB device array inside the library
- * (cp_query_noalloc_scratch_bytes), which each GPU that loads the library
- * holds until the process exits.  That is enough for 1,048,576 queries per
- * call with sort_queries on (any count with it off); larger calls return
- * CP_ERROR_SCRATCH_TOO_SMALL with a message and launch nothing.  The call
- * makes no cudaMalloc / cudaFree and no other allocation.  The first call on
- * a device looks up the array's device address (cudaGetSymbolAddress with
- * that device current), so make that first call before any stream capture.
- * All calls share the one array: calls that overlap on the GPU (other
- * streams, other threads) race and give wrong results — keep them ordered on
- * one stream.  This entry point has no counterpart in the reference.
+ * (cp_query_noalloc_scratch_bytes).  At most 1,048,576 queries per call with
+ * sort_queries on (any count up to 2^31 - 1 with it off); a larger call
+ * returns CP_ERROR_SCRATCH_TOO_SMALL with a message and launches nothing.
+ * The runtime loads the array on a device lazily, at the first call made with
+ * that device current, and the device holds it until the process exits: that
+ * first call is the one that allocates (32 MiB) and can fail with
+ * CP_ERROR_OUT_OF_MEMORY.  Make it at start-up — a call with nq == 0 (NULL
+ * pointers allowed) loads the array and does nothing else — before the host
+ * claims the rest of the device memory and before any stream capture.  After
+ * that the call makes no cudaMalloc / cudaFree and no other allocation.  It
+ * looks the array's address up on every call (cudaGetSymbolAddress), so it
+ * stays valid across cudaDeviceReset.  All calls share the one array and find
+ * the last call's contents in it (each call clears what must start at zero):
+ * calls that overlap on the GPU (other streams, other threads) race and give
+ * wrong results — keep them ordered on one stream.  This entry point has no
+ * counterpart in the reference.
  */
 CP_API cp_status cp_query_noalloc(const cp_mesh* mesh, const float* queries, int64_t nq,
                                   const cp_query_opts* opts, float* out_point, float* out_dist,
@@ -538,6 +544,16 @@ CP_API cp_status cp_mesh_export_build(const cp_mesh* mesh, uint64_t* keys, int32
  */
 CP_API cp_status cp_mesh_export_wide(const cp_mesh* mesh, float* boxes, int32_t* refs,
                                      int32_t* counts);
+
+/* The same two exports for a batch: one build over every mesh's triangles
+ * (keys carry the mesh id in their high bits, so each mesh's triangles are
+ * one sorted run and one subtree).  No counterpart in the reference (its
+ * acceleration structures are opaque driver objects, src/vk/vulkan.cpp:777-936). */
+CP_API cp_status cp_batch_export_build(const cp_batch* batch, uint64_t* keys, int32_t* order,
+                                       int32_t* left, int32_t* right, int32_t* parent,
+                                       uint8_t* cluster, int32_t* wide_src);
+CP_API cp_status cp_batch_export_wide(const cp_batch* batch, float* boxes, int32_t* refs,
+                                      int32_t* counts);
 
 #ifdef __cplusplus
 }

@@ -61,9 +61,15 @@ def rewrite(src: str) -> str:
     return s
 
 
+def reference_root() -> Path:
+    """The reference checkout the oracle's recipes and reference-reading
+    tests use: REFERENCE_ROOT, default /root/reference (may be absent)."""
+    return Path(os.environ.get("REFERENCE_ROOT", "/root/reference"))
+
+
 def build(ref_root: Path | None = None) -> Path | None:
     """Generate and compile; returns the library, or None without a checkout."""
-    root = Path(ref_root or os.environ.get("REFERENCE_ROOT", "/root/reference"))
+    root = Path(ref_root) if ref_root else reference_root()
     rt = root / "src" / "shaders" / "rt"
     if not (rt / "rtcommon.glsl").exists():
         return None

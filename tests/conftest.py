@@ -36,3 +36,15 @@ def cuda():
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     return torch.device("cuda:0")
+
+
+@pytest.fixture(scope="session")
+def reference_root():
+    """The reference checkout (one lookup, in the oracle's recipe); tests that
+    read its files skip where it is absent, as on a GPU machine."""
+    from oracle.make_ref_shade import reference_root as lookup
+
+    root = lookup()
+    if not (root / "src").is_dir():
+        pytest.skip("no checkout of the reference")
+    return root

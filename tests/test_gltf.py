@@ -15,10 +15,10 @@ import numpy as np
 import pytest
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
-REF_MEDIA = Path("/root/reference/media")
 
 
-def test_reference_scenes_match_fixture(cpq):
+def test_reference_scenes_match_fixture(cpq, reference_root):
+    REF_MEDIA = reference_root / "media"
     if not (REF_MEDIA / "cube.gltf").exists():
         pytest.skip("reference media not present")
     g = np.load(GOLDEN / "ref_meshes.npz")
@@ -31,11 +31,11 @@ def test_reference_scenes_match_fixture(cpq):
     assert len(scenes[0].instance_primitive) == 1  # the cube node; light and camera have no mesh
 
 
-def test_cbox_reader_matches_fixture(cpq):
+def test_cbox_reader_matches_fixture(cpq, reference_root):
     """The reference's Cornell box: primitives and node instances as the
     fixture's independent Python reader (tests/golden/make_golden.py) made
     them."""
-    path = REF_MEDIA / "cbox" / "cbox.gltf"
+    path = reference_root / "media" / "cbox" / "cbox.gltf"
     if not path.exists():
         pytest.skip("reference media not present")
     g = np.load(GOLDEN / "cbox_scene.npz")

@@ -23,18 +23,22 @@ def bary3(b2):
 
 
 def test_backward_torus(orc, cpq, cuda):
-    """The differentiable workload's mesh (200k triangles) with 1M queries."""
+    """The differentiable workload at its full size: torus of 200,000
+    triangles, 4,194,304 queries uniform in [-1.5, 1.5]^3, upstream gradient
+    N(0, 1)."""
     from gpurt_cpq import workloads as W
 
-    v, t, q, g = W.torus_workload(nq=1 << 20)
-    m = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=4)
+    v, t, q, g = W.torus_workload()
+    assert q.shape[0] == 4 * (1 << 20) and t.shape[0] == 200_000
+    m = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=4, leaf_size=2)
     qd, gd = dev(q, cuda), dev(g, cuda)
     r = m.query(qd, want_point=True, want_bary=True)
     gq, gv = m.backward(qd, r.tri, r.bary, gd)
     gq, gv = gq.cpu().numpy(), gv.cpu().numpy()
     tri, b2 = r.tri.cpu().numpy(), r.bary.cpu().numpy()
+    g64 = g.astype(np.float64)
     # 1. the FP64 analytic gradient at the GPU's own (tri, bary)
-    rq, rv = orc.backward_f64(v, t, q, tri, bary3(b2), g.astype(np.float64))
+    rq, rv = orc.backward_f64(v, t, q, tri, bary3(b2), g64)
     assert np.abs(gq - rq).max() <= GRAD_ATOL
     scale = np.maximum(1.0, np.abs(rv))
     assert (np.abs(gv - rv) / scale).max() <= 1e-4
@@ -48,40 +52,67 @@ def test_backward_torus(orc, cpq, cuda):
     gq_x = gq_x.cpu().numpy()
     idx = np.random.default_rng(1).choice(q.shape[0], 10000, replace=False)
     d_sel, b_sel = orc.dist_to_tri_f64(v, t, q[idx], tri[idx], want_bary=True)
-    rq2, _ = orc.backward_f64(v, t, q[idx], tri[idx], b_sel, g[idx].astype(np.float64))
+    rq2, _ = orc.backward_f64(v, t, q[idx], tri[idx], b_sel, g64[idx])
     err2 = np.abs(gq_x[idx] - rq2).max(axis=1)
     assert err2.max() <= GRAD_ATOL, np.sort(err2)[-10:]
-    e = orc.exact_f64(v, t, q[idx])
+    e_all = orc.exact_f64(v, t, q)  # the FP64 optimum of every query
+    e = {k: e_all[k][idx] for k in ("dist", "tri", "point")}
     assert np.all((d_sel - e["dist"]) / e["dist"] <= 1e-6)
-    # 3. central finite differences in FP64 on the same 10k queries
+    # 3. central finite differences in FP64 on the same 10k queries, at the
+    #    configured step h = 1e-4 and at h / 2.  A central difference measures
+    #    the gradient only where the distance is smooth across the stencil:
+    #    the FP64 closest triangle is the same at q and at every q +- h and
+    #    q +- h/2 (a stencil across a medial sheet of the polyhedral surface
+    #    straddles a jump in the gradient).  Its truncation error is |g| h^2 / 6
+    #    times the distance's third derivative: zero in a face's region, up to
+    #    about |g| h^2 / d^2 near an edge or vertex.  The Richardson
+    #    combination (4 D(h/2) - D(h)) / 3 cancels it, leaving the FP32 error
+    #    of the adjoint itself.
     q64 = q[idx].astype(np.float64)
-    fd = np.zeros((len(idx), 3))
+    fd = {FD_H: np.zeros((len(idx), 3)), FD_H / 2: np.zeros((len(idx), 3))}
     smooth = np.ones(len(idx), bool)
-    for k in range(3):
-        qp, qm = q64.copy(), q64.copy()
-        qp[:, k] += FD_H
-        qm[:, k] -= FD_H
-        dp, tp = orc.exact_f64_dq(v, t, qp)
-        dm, tm = orc.exact_f64_dq(v, t, qm)
-        fd[:, k] = g[idx] * (dp - dm) / (2 * FD_H)
-        smooth &= (tp == e["tri"]) & (tm == e["tri"])
-    # A central difference measures the gradient only where the distance is
-    # smooth across the stencil: the FP64 closest triangle is the same at q and
-    # at q +- h on every axis (a stencil across a medial sheet of the
-    # polyhedral surface straddles a jump in the gradient), and the
-    # truncation error ~h^2/(6 d^2) near an edge or vertex feature is small
-    # (d >= 0.01).  Compare there, at queries whose forward closest point is
-    # the FP64 optimum's (tied closest points elsewhere, see 2.).
+    for h in fd:
+        for k in range(3):
+            qp, qm = q64.copy(), q64.copy()
+            qp[:, k] += h
+            qm[:, k] -= h
+            dp, tp = orc.exact_f64_dq(v, t, qp)
+            dm, tm = orc.exact_f64_dq(v, t, qm)
+            fd[h][:, k] = g64[idx] * (dp - dm) / (2 * h)
+            smooth &= (tp == e["tri"]) & (tm == e["tri"])
+    # compare at queries whose forward closest point is the FP64 optimum's
+    # (tied closest points elsewhere, see 2.) and at least 0.01 from the surface
     same = np.linalg.norm(r.point.cpu().numpy()[idx] - e["point"], axis=1) <= 1e-6
     assert same.mean() >= 0.95
     use = same & smooth & (e["dist"] >= 0.01)
     assert use.mean() >= 0.8
-    err = np.abs(gq[idx] - fd).max(axis=1)[use]
-    print(f"FD check on {use.sum()} smooth queries: median {np.median(err):.2e}, "
-          f"p99 {np.percentile(err, 99):.2e}, max {err.max():.2e}")
+    err_h = np.abs(gq[idx] - fd[FD_H]).max(axis=1)
+    allow = 1e-5 + np.abs(g64[idx]) * FD_H ** 2 / e["dist"] ** 2
+    assert np.all(err_h[use] <= allow[use]), np.sort((err_h / allow)[use])[-5:]
+    rich = (4.0 * fd[FD_H / 2] - fd[FD_H]) / 3.0
+    err = np.abs(gq[idx] - rich).max(axis=1)[use]
+    print(f"FD check on {use.sum()} smooth queries (Richardson h = 1e-4, 5e-5): median {np.median(err):.2e}, "
+          f"p99 {np.percentile(err, 99):.2e}, max {err.max():.2e}; plain h = 1e-4: "
+          f"p99 {np.percentile(err_h[use], 99):.2e}, max {err_h[use].max():.2e}")
     assert np.median(err) <= 1e-6
-    assert np.percentile(err, 99) <= 1e-4
-    assert err.max() <= 1e-3
+    assert np.percentile(err, 99) <= 1e-5
+    assert err.max() <= 1e-4
+    # 4. d/dvertices independent of the forward's choice: the FP64 analytic
+    #    gradient at each query's FP64 optimum (its own triangle and weights)
+    #    over every query whose GPU closest point is that optimum's point,
+    #    against the GPU adjoint of the forward's (tri, bary) with the upstream
+    #    gradient of the other queries zeroed.  Equal closest points at a
+    #    shared edge or vertex put equal weights on the same vertices,
+    #    whichever triangle holds them.
+    agree = np.linalg.norm(r.point.cpu().numpy() - e_all["point"], axis=1) <= 1e-6
+    assert agree.mean() >= 0.95
+    g_m = np.where(agree, g, 0.0).astype(np.float32)
+    _, gv_m = m.backward(qd, r.tri, r.bary, dev(g_m, cuda))
+    _, rv_opt = orc.backward_f64(v, t, q, e_all["tri"], e_all["bary"], g_m.astype(np.float64))
+    dv_err = np.abs(gv_m.cpu().numpy() - rv_opt) / np.maximum(1.0, np.abs(rv_opt))
+    print(f"d/dvertices vs the FP64 optimum's gradient over {agree.sum()} queries: "
+          f"max {dv_err.max():.2e}, p99 {np.percentile(dv_err, 99):.2e}")
+    assert dv_err.max() <= 1e-4
 
 
 def test_backward_zero_distance_and_invalid(cpq, cuda):

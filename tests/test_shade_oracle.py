@@ -551,12 +551,10 @@ def cbox_shade_scene():
     return S.Scene(np.concatenate(V), np.concatenate(N), np.concatenate(obj), albedo, emissive, mr)
 
 
-def test_gltf_world_shading_matches_the_fixture_scene(cpq):
+def test_gltf_world_shading_matches_the_fixture_scene(cpq, reference_root):
     """The library's reader, flattened by GltfScene.world_shading, gives the
     shading scene built here from the fixture (the reference's Cornell box)."""
-    from pathlib import Path
-
-    path = Path("/root/reference/media/cbox/cbox.gltf")
+    path = reference_root / "media" / "cbox" / "cbox.gltf"
     if not path.exists():
         pytest.skip("reference media not present")
     w = cpq.load_gltf(str(path)).world_shading()
