@@ -40,6 +40,22 @@ namespace cpq {
 namespace {
 
 constexpr int kStackTotal = 256;   // >= (K-1)(depth+1) for any 64+32-bit-key LBVH
+
+// Packet traversal work claims: kSeedChunk consecutive packets per claim (each
+// packet after a chunk's first seeds its limits from the packet before it,
+// from kSeedPoints of its closest points), then kTailPackets single packets
+// per warp at the end.
+#ifndef CPQ_SEED_CHUNK
+#define CPQ_SEED_CHUNK 16
+#endif
+#ifndef CPQ_SEED_POINTS
+#define CPQ_SEED_POINTS 8
+#endif
+constexpr unsigned long long kSeedChunk = CPQ_SEED_CHUNK;
+constexpr int kSeedPoints = CPQ_SEED_POINTS;
+constexpr unsigned long long kTailPackets = 4;
+static_assert(kSeedPoints == 1 || kSeedPoints == 2 || kSeedPoints == 4 || kSeedPoints == 8 ||
+                  kSeedPoints == 16 || kSeedPoints == 32, "seed points: a power of two up to 32");
 constexpr unsigned kFull = 0xffffffffu;
 
 __device__ __forceinline__ int mesh_of(const int64_t* __restrict__ off, int nmeshes, int64_t i) {
@@ -395,9 +411,11 @@ struct TraverseArgs {
     float* out_dist;
     int32_t* out_tri;
     float* out_bary;
-    unsigned long long* counter;
+    unsigned long long* counter;  // [0] chunk claims, [1] single-packet claims (packet kernel)
     uint32_t* status;
     unsigned long long* stats;  // optional: node visits, leaf triangle tests, pops, skipped pops
+    const float* box;           // binary node boxes (lo xyz, hi xyz); a mesh's box at its root
+    const int32_t* mesh_root;   // per mesh: its binary root
 };
 
 template <int K, int S>
@@ -516,9 +534,15 @@ __global__ void __launch_bounds__(256) k_traverse(TraverseArgs a) {
     }
 }
 
+// The winner's float-float re-evaluation and the outputs; the closest point
+// (NaN when nothing was found) is also returned in (px, py, pz).
 __device__ __forceinline__ void write_result(const TraverseArgs& a, int64_t qi, float qx, float qy,
-                                             float qz, int best_rec, int best_idx) {
-    float dist = __int_as_float(0x7fc00000), px = dist, py = dist, pz = dist, bv = dist, bw = dist;
+                                             float qz, int best_rec, int best_idx, float& px, float& py,
+                                             float& pz) {
+    float dist = __int_as_float(0x7fc00000), bv = dist, bw = dist;
+    px = dist;
+    py = dist;
+    pz = dist;
     if (best_rec >= 0) {
         const float4* rp = reinterpret_cast<const float4*>(a.recs + best_rec);
         TriRec r;
@@ -634,7 +658,11 @@ __constant__ LeafSplits c_leaf_splits = make_leaf_splits();
 // skipped when no lane still needs it.  Only the top entry can be used up,
 // and a push reuses it, so the stack holds one entry per wide level at most;
 // `cap` (max wide depth + 1) is that bound, so it cannot overflow.  Lanes of
-// different meshes in one chunk (batches) are served one mesh at a time.
+// different meshes in one packet (batches) are served one mesh at a time.
+// A warp claims kSeedChunk consecutive packets at once; each packet after the
+// first starts every lane's limit at a padded upper bound from the previous
+// packet's closest points (its neighbours along the curve), so the first
+// leaves a packet reaches are not tested against an infinite limit.
 // kCompact (trees whose leaves hold 3 or more triangles) spreads a leaf's
 // (query, triangle) pairs over the warp when few lanes need the leaf; it
 // costs 512 bytes of shared memory per warp, which with 2-triangle leaves
@@ -655,188 +683,249 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
     unsigned long long n_nodes = 0, n_tris = 0, n_pops = 0, n_skips = 0, n_lane_tris = 0, n_rounds = 0,
                        n_lane_nodes = 0;
 
+    // Work: packets of 32 consecutive ordered queries.  Up to `split` they are
+    // claimed kSeedChunk at a time from counter[0]; the last kTailPackets per
+    // warp one at a time from counter[1], so that the warps finish together.
+    const unsigned long long nq = (unsigned long long)a.nq;
+    const unsigned long long npk = (nq + 31) / 32;
+    const unsigned long long tail = (unsigned long long)gridDim.x * (blockDim.x >> 5) * kTailPackets;
+    const unsigned long long split = (npk > tail ? (npk - tail) / kSeedChunk * kSeedChunk : 0ull) * 32;
     for (;;) {
-        unsigned long long base = 0;
-        if (lane == 0) base = atomicAdd(a.counter, 32ull);
-        base = __shfl_sync(kFull, base, 0);
-        if (base >= (unsigned long long)a.nq) break;  // warp-uniform exit
-        const int64_t i = (int64_t)base + lane;
-        const bool valid = i < a.nq;
-        int64_t qi = 0;
-        float qx = 0.f, qy = 0.f, qz = 0.f;
-        int m = 0;
-        if (valid) {
-            qi = a.perm ? (int64_t)a.perm[i] : i;
-            qx = a.queries[3 * qi];
-            qy = a.queries[3 * qi + 1];
-            qz = a.queries[3 * qi + 2];
-            m = a.nmeshes > 1 ? mesh_of(a.qoff, a.nmeshes, qi) : 0;
-        }
-        const f32x2 qx2 = f2_pack(qx, qx), qy2 = f2_pack(qy, qy), qz2 = f2_pack(qz, qz);
-        unsigned long long best = kNoKey;
-        unsigned pending = __ballot_sync(kFull, valid);
-        while (pending) {
-            const int leader = __ffs(pending) - 1;
-            const int mesh = __shfl_sync(kFull, m, leader);
-            const bool mine = ((pending >> lane) & 1u) && m == mesh;
-            pending &= ~__ballot_sync(kFull, mine);
-            // lanes outside this round never need anything: bound -inf
-            float lim = mine ? key_d2(best) : -INFINITY;
-            int sp = 0;            // stack entries; only the top one can be used up
-            uint32_t t_order = 0;  // the top entry's slots still to visit, next in the low nibble
-            int t_cnt = 0;         // and their number
-            int cur = a.wide_root[mesh];
-            // this lane's bound admitted the node being visited (the root, a
-            // wide node, admits the round's lanes); used at leaves
-            bool leaf_active = mine;
-            for (;;) {
-                if (cur >= 0) {
-                    if (kStats) {
-                        ++n_nodes;
-                        n_lane_nodes += __popc(__ballot_sync(kFull, leaf_active));
-                    }
-                    const WideNode<K>* nd = nodes + cur;
-                    f32x2 lox[K / 2], hix[K / 2], loy[K / 2], hiy[K / 2], loz[K / 2], hiz[K / 2];
-                    int32_t ch[K];
-                    load_row2<K>(nd->lox, lox);
-                    load_row2<K>(nd->hix, hix);
-                    load_row2<K>(nd->loy, loy);
-                    load_row2<K>(nd->hiy, hiy);
-                    load_row2<K>(nd->loz, loz);
-                    load_row2<K>(nd->hiz, hiz);
-                    load_row_i<K>(nd->child, ch);
-                    // box lower bounds, two children per packed operation
-                    float lb[K];
-#pragma unroll
-                    for (int j = 0; j < K / 2; ++j) {
-                        const f32x2 dx = box_axis2(qx2, lox[j], hix[j]);
-                        const f32x2 dy = box_axis2(qy2, loy[j], hiy[j]);
-                        const f32x2 dz = box_axis2(qz2, loz[j], hiz[j]);
-                        f2_unpack(f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx))), lb[2 * j], lb[2 * j + 1]);
-                    }
-                    // each lane's needed children, and its nearest as the least
-                    // (bound bits | slot) unsigned key: non-negative floats
-                    // order as their bit patterns, and the cleared sign bit
-                    // keeps every needed key below the sentinel
-                    uint32_t mine_need = 0, kmine = 0xFFFFFFFFu;
-#pragma unroll
-                    for (int s = 0; s < K; ++s) {
-                        const bool want = lb[s] < lim;
-                        mine_need |= (want ? 1u : 0u) << s;
-                        kmine = min(kmine, want ? ((__float_as_uint(lb[s]) & 0x7FFFFFF8u) | (uint32_t)s)
-                                                : 0xFFFFFFFFu);
-                    }
-                    const uint32_t need = __reduce_or_sync(kFull, mine_need);
-                    if (need != 0) {
-                        // go first to the child nearest to any lane
-                        const int f = (int)(__reduce_min_sync(kFull, kmine) & 7u);
-                        const uint32_t rest = need & ~(1u << f);
-                        if (rest != 0) {
-                            // the node becomes the top entry; a used-up top
-                            // entry is overwritten, a live one keeps its list
-                            if (sp > 0) {
-                                if (t_cnt == 0) --sp;
-                                else if (lane0) st_state[sp - 1] = make_uint2(t_order, (uint32_t)t_cnt);
-                            }
-                            if (sp >= cap) {  // cannot happen: cap bounds the depth
-                                atomicOr(a.status, 1u);
-                                sp = cap - 1;
-                            }
-                            store_row<K>(st_bnd + sp * 32 * K, lb);
-                            if (lane0) store_row<K>(st_ch + sp * K, ch);
-                            t_order = c_slot_lists.v[rest];
-                            t_cnt = __popc(rest);
-                            ++sp;
-                            __syncwarp();
-                        }
-                        int32_t cf = ch[0];
-#pragma unroll
-                        for (int s = 1; s < K; ++s) cf = f == s ? ch[s] : cf;
-                        cur = cf;
-                        leaf_active = (mine_need >> f) & 1u;
-                        continue;
-                    }
-                } else {
-                    const int first = leaf_first(cur), cnt = leaf_count(cur);
-                    if (kStats) n_tris += cnt;
-                    const uint32_t act = __ballot_sync(kFull, leaf_active);
-                    const int na = __popc(act);
-                    if (kStats) n_lane_tris += (unsigned long long)na * cnt;
-                    if (kCompact && cnt >= 2 && na >= 1 && na <= 16) {
-                        // Few lanes need this leaf: spread its (query, triangle)
-                        // pairs over the warp.  A round covers kpr = 32 / na
-                        // triangles: lane w tests triangle k0 + w / na against
-                        // the (w % na)-th active lane's query, and each active
-                        // lane takes the minimum of its keys (order-free, so
-                        // the result is the same).
-                        const LeafSplit sp2 = c_leaf_splits.v[na];
-                        const int r = __popc(act & lt_mask);
-                        if (leaf_active) st_q[r] = make_float4(qx, qy, qz, 0.0f);
-                        __syncwarp();
-                        // w / na, exact: (w + 1/2) / na is at least 1/32 from an integer
-                        const int kk = (int)(((float)lane + 0.5f) * sp2.inv);
-                        const bool worker = lane < sp2.kpr * na;
-                        const float4 qq = st_q[worker ? lane - kk * na : 0];
-                        // a worker serves the same query in every round: keep
-                        // its minimum and gather once
-                        unsigned long long key = kNoKey;
-                        for (int k0 = 0; k0 < cnt; k0 += sp2.kpr) {
-                            if (kStats) ++n_rounds;
-                            const int k = k0 + kk;
-                            if (worker && k < cnt) {
-                                const FastTri f = load_fast(a.fast + first + k);
-                                key = min(key, best_key(tri_d2_fast(qq.x, qq.y, qq.z, f), fast_index(f)));
-                            }
-                        }
-                        const int nk = min(sp2.kpr, cnt);
-                        for (int j = 0; j < nk; ++j) {
-                            const unsigned long long got = __shfl_sync(kFull, key, (r + j * na) & 31);
-                            if (leaf_active) best = min(best, got);
-                        }
-                    } else {
-                        if (kStats) n_rounds += cnt;
-                        for (int k = 0; k < cnt; ++k) {
-                            const FastTri f = load_fast(a.fast + first + k);
-                            if (leaf_active)
-                                best = min(best, best_key(tri_d2_fast(qx, qy, qz, f), fast_index(f)));
-                        }
-                    }
-                    if (mine) lim = key_d2(best);
-                }
-                // pop: the top entry's next slot that some lane still needs
-                bool found = false;
-                for (;;) {
-                    if (t_cnt == 0) {
-                        if (sp <= 1) break;
-                        --sp;
-                        const uint2 s2 = st_state[sp - 1];
-                        t_order = s2.x;
-                        t_cnt = (int)s2.y;
-                        continue;
-                    }
-                    const int s = (int)(t_order & 15u);
-                    t_order >>= 4;
-                    --t_cnt;
-                    const int e = sp - 1;
-                    const bool want = st_bnd[e * 32 * K + s] < lim;
-                    if (kStats) ++n_pops;
-                    if (__any_sync(kFull, want)) {
-                        cur = st_ch[e * K + s];
-                        leaf_active = want;
-                        found = true;
-                        break;
-                    }
-                    if (kStats) ++n_skips;
-                }
-                __syncwarp();  // the reads above come before a push's writes
-                if (!found) break;
+        unsigned long long start = 0, stop = 0;
+        if (lane == 0) {
+            start = atomicAdd(a.counter, 32ull * kSeedChunk);
+            if (start < split) {
+                stop = min(start + 32ull * kSeedChunk, split);
+            } else {
+                start = split + atomicAdd(a.counter + 1, 32ull);
+                stop = start + 32;
             }
         }
-        if (valid) {
-            // the winner's record: its triangle through the build's inverse order
-            const int idx = (int)(uint32_t)best;
-            const int rec = best == kNoKey ? -1 : a.inv_order[a.toff[m] + idx];
-            write_result(a, qi, qx, qy, qz, rec, idx);
+        start = __shfl_sync(kFull, start, 0);
+        stop = __shfl_sync(kFull, min(stop, nq), 0);
+        if (start >= nq) break;  // warp-uniform exit
+        // this lane's closest point in the chunk's previous packet (NaN: none) and its mesh
+        float spx = __int_as_float(0x7fc00000), spy = spx, spz = spx;
+        int smesh = -1;
+        for (unsigned long long base = start; base < stop; base += 32) {
+            const int64_t i = (int64_t)base + lane;
+            const bool valid = i < a.nq;
+            int64_t qi = 0;
+            float qx = 0.f, qy = 0.f, qz = 0.f;
+            int m = 0;
+            if (valid) {
+                qi = a.perm ? (int64_t)a.perm[i] : i;
+                qx = a.queries[3 * qi];
+                qy = a.queries[3 * qi + 1];
+                qz = a.queries[3 * qi + 2];
+                m = a.nmeshes > 1 ? mesh_of(a.qoff, a.nmeshes, qi) : 0;
+            }
+            // Seed: each lane's limit starts at its least distance to the closest
+            // points of lanes 0, 4, ..., 28 of the previous packet (same mesh),
+            // padded.  Those points lie on the mesh up to FP32 rounding, so the
+            // padded distance (1 + 1e-4 relative, plus 4e-6 of the mesh's extent,
+            // the query's magnitude and the distance) exceeds the query's true
+            // distance by far more than the box and triangle tests err: no box or
+            // triangle that can hold the nearest triangle is pruned, and the
+            // answer is the unseeded one.
+            float seed = INFINITY;
+            if (base != start) {
+                float m2 = INFINITY;
+#pragma unroll
+                for (int j = 0; j < 32; j += 32 / kSeedPoints) {
+                    const float px = __shfl_sync(kFull, spx, j), py = __shfl_sync(kFull, spy, j),
+                                pz = __shfl_sync(kFull, spz, j);
+                    const int pm = __shfl_sync(kFull, smesh, j);
+                    const float dx = qx - px, dy = qy - py, dz = qz - pz;
+                    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                    if (pm == m && d2 < m2) m2 = d2;  // a NaN point fails the compare
+                }
+                if (valid && m2 < INFINITY) {
+                    const float* bx = a.box + 6 * (int64_t)__ldg(a.mesh_root + m);
+                    const float ext = max3f(__ldg(bx + 3) - __ldg(bx), __ldg(bx + 4) - __ldg(bx + 1),
+                                            __ldg(bx + 5) - __ldg(bx + 2));
+                    const float qa = max3f(fabsf(qx), fabsf(qy), fabsf(qz));
+                    const float d = sqrtf(m2);
+                    const float sd = fmaf(d, 1.0001f, 4e-6f * (ext + qa + d));
+                    seed = sd * sd;
+                }
+            }
+            const f32x2 qx2 = f2_pack(qx, qx), qy2 = f2_pack(qy, qy), qz2 = f2_pack(qz, qz);
+            unsigned long long best = kNoKey;
+            unsigned pending = __ballot_sync(kFull, valid);
+            for (;;) {
+                while (pending) {
+                    const int leader = __ffs(pending) - 1;
+                    const int mesh = __shfl_sync(kFull, m, leader);
+                    const bool mine = ((pending >> lane) & 1u) && m == mesh;
+                    pending &= ~__ballot_sync(kFull, mine);
+                    // lanes outside this round never need anything: bound -inf
+                    float lim = mine ? fminf(seed, key_d2(best)) : -INFINITY;
+                    int sp = 0;            // stack entries; only the top one can be used up
+                    uint32_t t_order = 0;  // the top entry's slots still to visit, next in the low nibble
+                    int t_cnt = 0;         // and their number
+                    int cur = a.wide_root[mesh];
+                    // this lane's bound admitted the node being visited (the root, a
+                    // wide node, admits the round's lanes); used at leaves
+                    bool leaf_active = mine;
+                    for (;;) {
+                        if (cur >= 0) {
+                            if (kStats) {
+                                ++n_nodes;
+                                n_lane_nodes += __popc(__ballot_sync(kFull, leaf_active));
+                            }
+                            const WideNode<K>* nd = nodes + cur;
+                            f32x2 lox[K / 2], hix[K / 2], loy[K / 2], hiy[K / 2], loz[K / 2], hiz[K / 2];
+                            int32_t ch[K];
+                            load_row2<K>(nd->lox, lox);
+                            load_row2<K>(nd->hix, hix);
+                            load_row2<K>(nd->loy, loy);
+                            load_row2<K>(nd->hiy, hiy);
+                            load_row2<K>(nd->loz, loz);
+                            load_row2<K>(nd->hiz, hiz);
+                            load_row_i<K>(nd->child, ch);
+                            // box lower bounds, two children per packed operation
+                            float lb[K];
+#pragma unroll
+                            for (int j = 0; j < K / 2; ++j) {
+                                const f32x2 dx = box_axis2(qx2, lox[j], hix[j]);
+                                const f32x2 dy = box_axis2(qy2, loy[j], hiy[j]);
+                                const f32x2 dz = box_axis2(qz2, loz[j], hiz[j]);
+                                f2_unpack(f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx))), lb[2 * j], lb[2 * j + 1]);
+                            }
+                            // each lane's needed children, and its nearest as the least
+                            // (bound bits | slot) unsigned key: non-negative floats
+                            // order as their bit patterns, and the cleared sign bit
+                            // keeps every needed key below the sentinel
+                            uint32_t mine_need = 0, kmine = 0xFFFFFFFFu;
+#pragma unroll
+                            for (int s = 0; s < K; ++s) {
+                                const bool want = lb[s] < lim;
+                                mine_need |= (want ? 1u : 0u) << s;
+                                kmine = min(kmine, want ? ((__float_as_uint(lb[s]) & 0x7FFFFFF8u) | (uint32_t)s)
+                                                        : 0xFFFFFFFFu);
+                            }
+                            const uint32_t need = __reduce_or_sync(kFull, mine_need);
+                            if (need != 0) {
+                                // go first to the child nearest to any lane
+                                const int f = (int)(__reduce_min_sync(kFull, kmine) & 7u);
+                                const uint32_t rest = need & ~(1u << f);
+                                if (rest != 0) {
+                                    // the node becomes the top entry; a used-up top
+                                    // entry is overwritten, a live one keeps its list
+                                    if (sp > 0) {
+                                        if (t_cnt == 0) --sp;
+                                        else if (lane0) st_state[sp - 1] = make_uint2(t_order, (uint32_t)t_cnt);
+                                    }
+                                    if (sp >= cap) {  // cannot happen: cap bounds the depth
+                                        atomicOr(a.status, 1u);
+                                        sp = cap - 1;
+                                    }
+                                    store_row<K>(st_bnd + sp * 32 * K, lb);
+                                    if (lane0) store_row<K>(st_ch + sp * K, ch);
+                                    t_order = c_slot_lists.v[rest];
+                                    t_cnt = __popc(rest);
+                                    ++sp;
+                                    __syncwarp();
+                                }
+                                int32_t cf = ch[0];
+#pragma unroll
+                                for (int s = 1; s < K; ++s) cf = f == s ? ch[s] : cf;
+                                cur = cf;
+                                leaf_active = (mine_need >> f) & 1u;
+                                continue;
+                            }
+                        } else {
+                            const int first = leaf_first(cur), cnt = leaf_count(cur);
+                            if (kStats) n_tris += cnt;
+                            const uint32_t act = __ballot_sync(kFull, leaf_active);
+                            const int na = __popc(act);
+                            if (kStats) n_lane_tris += (unsigned long long)na * cnt;
+                            if (kCompact && cnt >= 2 && na >= 1 && na <= 16) {
+                                // Few lanes need this leaf: spread its (query, triangle)
+                                // pairs over the warp.  A round covers kpr = 32 / na
+                                // triangles: lane w tests triangle k0 + w / na against
+                                // the (w % na)-th active lane's query, and each active
+                                // lane takes the minimum of its keys (order-free, so
+                                // the result is the same).
+                                const LeafSplit sp2 = c_leaf_splits.v[na];
+                                const int r = __popc(act & lt_mask);
+                                if (leaf_active) st_q[r] = make_float4(qx, qy, qz, 0.0f);
+                                __syncwarp();
+                                // w / na, exact: (w + 1/2) / na is at least 1/32 from an integer
+                                const int kk = (int)(((float)lane + 0.5f) * sp2.inv);
+                                const bool worker = lane < sp2.kpr * na;
+                                const float4 qq = st_q[worker ? lane - kk * na : 0];
+                                // a worker serves the same query in every round: keep
+                                // its minimum and gather once
+                                unsigned long long key = kNoKey;
+                                for (int k0 = 0; k0 < cnt; k0 += sp2.kpr) {
+                                    if (kStats) ++n_rounds;
+                                    const int k = k0 + kk;
+                                    if (worker && k < cnt) {
+                                        const FastTri f = load_fast(a.fast + first + k);
+                                        key = min(key, best_key(tri_d2_fast(qq.x, qq.y, qq.z, f), fast_index(f)));
+                                    }
+                                }
+                                const int nk = min(sp2.kpr, cnt);
+                                for (int j = 0; j < nk; ++j) {
+                                    const unsigned long long got = __shfl_sync(kFull, key, (r + j * na) & 31);
+                                    if (leaf_active) best = min(best, got);
+                                }
+                            } else {
+                                if (kStats) n_rounds += cnt;
+                                for (int k = 0; k < cnt; ++k) {
+                                    const FastTri f = load_fast(a.fast + first + k);
+                                    if (leaf_active)
+                                        best = min(best, best_key(tri_d2_fast(qx, qy, qz, f), fast_index(f)));
+                                }
+                            }
+                            if (mine) lim = fminf(seed, key_d2(best));
+                        }
+                        // pop: the top entry's next slot that some lane still needs
+                        bool found = false;
+                        for (;;) {
+                            if (t_cnt == 0) {
+                                if (sp <= 1) break;
+                                --sp;
+                                const uint2 s2 = st_state[sp - 1];
+                                t_order = s2.x;
+                                t_cnt = (int)s2.y;
+                                continue;
+                            }
+                            const int s = (int)(t_order & 15u);
+                            t_order >>= 4;
+                            --t_cnt;
+                            const int e = sp - 1;
+                            const bool want = st_bnd[e * 32 * K + s] < lim;
+                            if (kStats) ++n_pops;
+                            if (__any_sync(kFull, want)) {
+                                cur = st_ch[e * K + s];
+                                leaf_active = want;
+                                found = true;
+                                break;
+                            }
+                            if (kStats) ++n_skips;
+                        }
+                        __syncwarp();  // the reads above come before a push's writes
+                        if (!found) break;
+                    }
+                }
+                // a lane whose seed left it no triangle (not expected: the seed is an
+                // upper bound with a margin) runs again unseeded
+                pending = __ballot_sync(kFull, valid && best == kNoKey && seed < INFINITY);
+                if (!pending) break;
+                seed = INFINITY;
+            }
+            if (valid) {
+                // the winner's record: its triangle through the build's inverse order
+                const int idx = (int)(uint32_t)best;
+                const int rec = best == kNoKey ? -1 : a.inv_order[a.toff[m] + idx];
+                write_result(a, qi, qx, qy, qz, rec, idx, spx, spy, spz);
+                smesh = m;
+            } else {
+                smesh = -1;
+        }
         }
     }
     if (kStats && a.stats && lane == 0) {
@@ -1931,7 +2020,7 @@ cudaError_t order_points(const Bvh& b, const float* queries, int64_t nq, const i
     unsigned long long* counter = reinterpret_cast<unsigned long long*>(w + L.counter);
     *counter_out = counter;
     *perm_out = nullptr;
-    cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st);
+    cudaError_t e = cudaMemsetAsync(counter, 0, 2 * sizeof(unsigned long long), st);
     if (e != cudaSuccess) return e;
     const int32_t* perm = nullptr;
     if (sort && nq > 1) {
@@ -2015,6 +2104,8 @@ cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int6
     args.counter = counter;
     args.status = b.status;
     args.stats = nullptr;
+    args.box = b.box;
+    args.mesh_root = b.mesh_root;
     {
         cudaStreamCaptureStatus capst = cudaStreamCaptureStatusNone;
         cudaStreamIsCapturing(st, &capst);

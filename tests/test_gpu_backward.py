@@ -63,11 +63,14 @@ def test_backward_torus(orc, cpq, cuda):
     #    the gradient only where the distance is smooth across the stencil:
     #    the FP64 closest triangle is the same at q and at every q +- h and
     #    q +- h/2 (a stencil across a medial sheet of the polyhedral surface
-    #    straddles a jump in the gradient).  Its truncation error is |g| h^2 / 6
-    #    times the distance's third derivative: zero in a face's region, up to
-    #    about |g| h^2 / d^2 near an edge or vertex.  The Richardson
-    #    combination (4 D(h/2) - D(h)) / 3 cancels it, leaving the FP32 error
-    #    of the adjoint itself.
+    #    straddles a jump in the gradient).  Where the stencil stays in one
+    #    triangle's face region the distance is linear across it and the
+    #    difference is exact up to FP64 rounding, so there the configured step
+    #    measures the FP32 error of the adjoint itself.  Near an edge or vertex
+    #    its truncation error grows like |g| h^2 / d^2, and a stencil that
+    #    crosses from a face's region into an edge's (the same triangle) meets a
+    #    jump in the second derivative; the Richardson combination
+    #    (4 D(h/2) - D(h)) / 3 cancels the h^2 term.
     q64 = q[idx].astype(np.float64)
     fd = {FD_H: np.zeros((len(idx), 3)), FD_H / 2: np.zeros((len(idx), 3))}
     smooth = np.ones(len(idx), bool)
@@ -86,17 +89,29 @@ def test_backward_torus(orc, cpq, cuda):
     assert same.mean() >= 0.95
     use = same & smooth & (e["dist"] >= 0.01)
     assert use.mean() >= 0.8
+    # face-region queries: the FP64 closest point lies more than 2h inside
+    # every edge of its triangle (the projection moves it by at most h)
+    tv = v[t[e["tri"]]].astype(np.float64)
+    area2 = np.linalg.norm(np.cross(tv[:, 1] - tv[:, 0], tv[:, 2] - tv[:, 0]), axis=1)
+    b3 = e_all["bary"][idx]
+    inside = np.ones(len(idx), bool)
+    for k in range(3):
+        opp = np.linalg.norm(tv[:, (k + 2) % 3] - tv[:, (k + 1) % 3], axis=1)
+        inside &= b3[:, k] * area2 / opp > 2 * FD_H
+    face = use & inside
+    assert face.sum() >= 0.5 * use.sum()
     err_h = np.abs(gq[idx] - fd[FD_H]).max(axis=1)
-    allow = 1e-5 + np.abs(g64[idx]) * FD_H ** 2 / e["dist"] ** 2
-    assert np.all(err_h[use] <= allow[use]), np.sort((err_h / allow)[use])[-5:]
     rich = (4.0 * fd[FD_H / 2] - fd[FD_H]) / 3.0
-    err = np.abs(gq[idx] - rich).max(axis=1)[use]
-    print(f"FD check on {use.sum()} smooth queries (Richardson h = 1e-4, 5e-5): median {np.median(err):.2e}, "
-          f"p99 {np.percentile(err, 99):.2e}, max {err.max():.2e}; plain h = 1e-4: "
-          f"p99 {np.percentile(err_h[use], 99):.2e}, max {err_h[use].max():.2e}")
-    assert np.median(err) <= 1e-6
-    assert np.percentile(err, 99) <= 1e-5
-    assert err.max() <= 1e-4
+    err_r = np.abs(gq[idx] - rich).max(axis=1)
+    print(f"FD check, h = 1e-4: {face.sum()} face-region queries max {err_h[face].max():.2e}, "
+          f"p99 {np.percentile(err_h[face], 99):.2e}; all {use.sum()} smooth queries p99 "
+          f"{np.percentile(err_h[use], 99):.2e}, max {err_h[use].max():.2e}; Richardson (h, h/2) p99 "
+          f"{np.percentile(err_r[use], 99):.2e}, max {err_r[use].max():.2e}")
+    assert err_h[face].max() <= 1e-5
+    assert np.median(err_r[use]) <= 1e-6
+    assert np.percentile(err_r[use], 99) <= 1e-5
+    assert np.percentile(err_h[use], 99) <= 1e-4
+    assert err_h[use].max() <= 1e-3
     # 4. d/dvertices independent of the forward's choice: the FP64 analytic
     #    gradient at each query's FP64 optimum (its own triangle and weights)
     #    over every query whose GPU closest point is that optimum's point,
