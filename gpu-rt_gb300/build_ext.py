@@ -26,6 +26,9 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden",
               "--expt-relaxed-constexpr", "-Werror", "all-warnings"]
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-Wall", "-Wextra", "-Werror"]
+# per-file additions: the path tracer rounds every FP32 expression as written
+# (no multiply-add contraction), as the shader's operations do
+FILE_FLAGS = {"shade.cu": ["-fmad=false"]}
 
 
 def _nvcc() -> str:
@@ -60,7 +63,7 @@ def build(verbose: bool = False, force: bool = False) -> Path:
             if src.suffix == ".cpp":
                 cmd = [cxx, *CXX_FLAGS, *inc, "-c", str(src), "-o", str(obj)]
             else:
-                cmd = [nvcc, *ARCH, *NVCC_FLAGS, *inc, "-c", str(src), "-o", str(obj)]
+                cmd = [nvcc, *ARCH, *NVCC_FLAGS, *FILE_FLAGS.get(src.name, []), *inc, "-c", str(src), "-o", str(obj)]
             jobs.append(cmd)
 
     def run(cmd):

@@ -604,12 +604,13 @@ __device__ __forceinline__ void store_row(T* dst, const T (&v)[K]) {
 // Shared memory of one warp: the packet stack of `cap` entries (every lane's
 // K bounds [entry][lane][slot], the K child refs [entry][slot], the (slot
 // list, count) of entries below the top [entry]; rounded to 16 bytes), then
-// the leaf-compaction slots (32 query points) when the kernel compacts.
+// the leaf-compaction slots (32 query points) when the kernel compacts, then
+// the previous packet's kSeedPoints closest points (x, y, z, mesh).
 __host__ __device__ constexpr size_t packet_stack_bytes(int K, int cap) {
     return ((size_t)cap * (128 * K + 4 * K + 8) + 15) & ~size_t(15);
 }
 __host__ __device__ constexpr size_t packet_warp_bytes(int K, int cap, bool compact) {
-    return packet_stack_bytes(K, cap) + (compact ? 32 * sizeof(float4) : 0);
+    return packet_stack_bytes(K, cap) + (compact ? 32 * sizeof(float4) : 0) + kSeedPoints * sizeof(float4);
 }
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -628,6 +629,7 @@ __device__ __forceinline__ float key_d2(unsigned long long k) {
     return __uint_as_float((uint32_t)(k >> 32));
 }
 constexpr unsigned long long kNoKey = 0x7f8000007fffffffull;  // (+inf, INT_MAX): nothing found
+constexpr unsigned long long kSeedKeyLow = 0x7fffffffull;     // a seed's index: INT_MAX, no triangle's
 
 // Leaf compaction with na active lanes (1..16): kpr = 32 / na triangles per
 // round and 1 / na.
@@ -678,6 +680,7 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
     int32_t* st_ch = reinterpret_cast<int32_t*>(wbase + (size_t)cap * 128 * K);
     uint2* st_state = reinterpret_cast<uint2*>(wbase + (size_t)cap * 132 * K);
     float4* st_q = reinterpret_cast<float4*>(wbase + packet_stack_bytes(K, cap));
+    float4* st_seed = st_q + (kCompact ? 32 : 0);
     const uint32_t lt_mask = lanemask_lt();
     const WideNode<K>* __restrict__ nodes = static_cast<const WideNode<K>*>(a.nodes);
     unsigned long long n_nodes = 0, n_tris = 0, n_pops = 0, n_skips = 0, n_lane_tris = 0, n_rounds = 0,
@@ -704,9 +707,6 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
         start = __shfl_sync(kFull, start, 0);
         stop = __shfl_sync(kFull, min(stop, nq), 0);
         if (start >= nq) break;  // warp-uniform exit
-        // this lane's closest point in the chunk's previous packet (NaN: none) and its mesh
-        float spx = __int_as_float(0x7fc00000), spy = spx, spz = spx;
-        int smesh = -1;
         for (unsigned long long base = start; base < stop; base += 32) {
             const int64_t i = (int64_t)base + lane;
             const bool valid = i < a.nq;
@@ -720,25 +720,27 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                 qz = a.queries[3 * qi + 2];
                 m = a.nmeshes > 1 ? mesh_of(a.qoff, a.nmeshes, qi) : 0;
             }
-            // Seed: each lane's limit starts at its least distance to the closest
-            // points of lanes 0, 4, ..., 28 of the previous packet (same mesh),
-            // padded.  Those points lie on the mesh up to FP32 rounding, so the
-            // padded distance (1 + 1e-4 relative, plus 4e-6 of the mesh's extent,
-            // the query's magnitude and the distance) exceeds the query's true
-            // distance by far more than the box and triangle tests err: no box or
-            // triangle that can hold the nearest triangle is pruned, and the
-            // answer is the unseeded one.
-            float seed = INFINITY;
+            // Seed: after a chunk's first packet each lane starts from its
+            // least distance to the previous packet's kSeedPoints closest
+            // points (same mesh), padded.  Those points lie on the mesh up to
+            // FP32 rounding, so the padded distance (1 + 1e-4 relative, plus
+            // 4e-6 of the mesh's extent, the query's magnitude and the
+            // distance) exceeds the query's true distance by far more than the
+            // box and triangle tests err: no box or triangle that can hold the
+            // nearest triangle is pruned, and the answer is the unseeded one.
+            // The seed enters as the lane's best key (its squared distance over
+            // the index INT_MAX, which no triangle has), so traversal prunes
+            // against it like any candidate.
+            unsigned long long best = kNoKey;
             if (base != start) {
+                __syncwarp();  // the previous packet's slot writes come first
                 float m2 = INFINITY;
 #pragma unroll
-                for (int j = 0; j < 32; j += 32 / kSeedPoints) {
-                    const float px = __shfl_sync(kFull, spx, j), py = __shfl_sync(kFull, spy, j),
-                                pz = __shfl_sync(kFull, spz, j);
-                    const int pm = __shfl_sync(kFull, smesh, j);
-                    const float dx = qx - px, dy = qy - py, dz = qz - pz;
+                for (int j = 0; j < kSeedPoints; ++j) {
+                    const float4 sp4 = st_seed[j];
+                    const float dx = qx - sp4.x, dy = qy - sp4.y, dz = qz - sp4.z;
                     const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    if (pm == m && d2 < m2) m2 = d2;  // a NaN point fails the compare
+                    if (__float_as_int(sp4.w) == m && d2 < m2) m2 = d2;  // a NaN point fails the compare
                 }
                 if (valid && m2 < INFINITY) {
                     const float* bx = a.box + 6 * (int64_t)__ldg(a.mesh_root + m);
@@ -747,11 +749,10 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                     const float qa = max3f(fabsf(qx), fabsf(qy), fabsf(qz));
                     const float d = sqrtf(m2);
                     const float sd = fmaf(d, 1.0001f, 4e-6f * (ext + qa + d));
-                    seed = sd * sd;
+                    best = kSeedKeyLow | ((unsigned long long)__float_as_uint(sd * sd) << 32);
                 }
             }
             const f32x2 qx2 = f2_pack(qx, qx), qy2 = f2_pack(qy, qy), qz2 = f2_pack(qz, qz);
-            unsigned long long best = kNoKey;
             unsigned pending = __ballot_sync(kFull, valid);
             for (;;) {
                 while (pending) {
@@ -760,7 +761,7 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                     const bool mine = ((pending >> lane) & 1u) && m == mesh;
                     pending &= ~__ballot_sync(kFull, mine);
                     // lanes outside this round never need anything: bound -inf
-                    float lim = mine ? fminf(seed, key_d2(best)) : -INFINITY;
+                    float lim = mine ? key_d2(best) : -INFINITY;
                     int sp = 0;            // stack entries; only the top one can be used up
                     uint32_t t_order = 0;  // the top entry's slots still to visit, next in the low nibble
                     int t_cnt = 0;         // and their number
@@ -880,7 +881,7 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                                         best = min(best, best_key(tri_d2_fast(qx, qy, qz, f), fast_index(f)));
                                 }
                             }
-                            if (mine) lim = fminf(seed, key_d2(best));
+                            if (mine) lim = key_d2(best);
                         }
                         // pop: the top entry's next slot that some lane still needs
                         bool found = false;
@@ -911,21 +912,23 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                         if (!found) break;
                     }
                 }
-                // a lane whose seed left it no triangle (not expected: the seed is an
-                // upper bound with a margin) runs again unseeded
-                pending = __ballot_sync(kFull, valid && best == kNoKey && seed < INFINITY);
+                // a lane whose seed left it no triangle (not expected: the seed
+                // is an upper bound with a margin) runs again unseeded
+                const bool empty = valid && (uint32_t)best == (uint32_t)kSeedKeyLow && best != kNoKey;
+                pending = __ballot_sync(kFull, empty);
                 if (!pending) break;
-                seed = INFINITY;
+                if (empty) best = kNoKey;
             }
+            float px = __int_as_float(0x7fc00000), py = px, pz = px;
             if (valid) {
                 // the winner's record: its triangle through the build's inverse order
                 const int idx = (int)(uint32_t)best;
                 const int rec = best == kNoKey ? -1 : a.inv_order[a.toff[m] + idx];
-                write_result(a, qi, qx, qy, qz, rec, idx, spx, spy, spz);
-                smesh = m;
-            } else {
-                smesh = -1;
-        }
+                write_result(a, qi, qx, qy, qz, rec, idx, px, py, pz);
+            }
+            // this packet's closest points seed the next one
+            constexpr int kStride = 32 / kSeedPoints;
+            if (lane % kStride == 0) st_seed[lane / kStride] = make_float4(px, py, pz, __int_as_float(valid ? m : -1));
         }
     }
     if (kStats && a.stats && lane == 0) {

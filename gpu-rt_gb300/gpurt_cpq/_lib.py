@@ -48,6 +48,19 @@ class RayOpts(Structure):
                 ("sort_rays", c_int32), ("block_size", c_int32)]
 
 
+class ShadeCamera(Structure):
+    _fields_ = [("eye", c_float * 3), ("right", c_float * 3), ("up", c_float * 3), ("fwd", c_float * 3),
+                ("tan_half_y", c_float), ("aspect", c_float), ("width", c_int32), ("height", c_int32)]
+
+
+class ShadeParams(Structure):
+    _fields_ = [("clear", c_float * 3), ("env", c_float * 3), ("samples", c_int32), ("max_depth", c_int32),
+                ("qmc", c_int32), ("integrator", c_int32), ("brdf", c_int32), ("use_rr", c_int32),
+                ("use_metalness", c_int32), ("frame", c_int32), ("max_frame", c_int32),
+                ("new_samples", c_int32), ("temporal_multiplier", c_int32), ("use_temporal", c_int32),
+                ("debug_view", c_int32), ("seed", c_uint32)]
+
+
 CP_TRAVERSAL_AUTO = 0
 CP_TRAVERSAL_THREAD = 1
 CP_TRAVERSAL_PACKET = 2
@@ -128,6 +141,13 @@ SIGNATURES = {
     "cp_batch_export_build": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                         c_void_p, c_void_p]),
     "cp_batch_export_wide": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "cp_shade_scene_create": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p,
+                                        c_int32, c_void_p, POINTER(c_void_p)]),
+    "cp_shade_scene_destroy": (c_int32, [c_void_p]),
+    "cp_shade_scene_lights": (c_int32, [c_void_p, POINTER(c_int32)]),
+    "cp_shade_render": (c_int32, [c_void_p, POINTER(ShadeCamera), POINTER(ShadeParams), c_void_p, c_void_p,
+                                  c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "cp_shade_tonemap": (c_int32, [c_int32, c_float, c_float, c_int64, c_void_p, c_void_p, c_void_p]),
 }
 
 
@@ -161,4 +181,5 @@ def check(status: int, what: str = "") -> None:
         raise CpError(status, f"{what}: {msg}" if what else msg)
 
 
-__all__ = ["lib", "check", "CpError", "BuildOpts", "QueryOpts", "MeshInfo", "SIGNATURES", "LIB_PATH"]
+__all__ = ["lib", "check", "CpError", "BuildOpts", "QueryOpts", "MeshInfo", "ShadeCamera", "ShadeParams",
+           "SIGNATURES", "LIB_PATH"]

@@ -500,6 +500,88 @@ CP_API cp_status cp_scene_ray_query(const cp_scene* scene, const float* origins,
                                     float* out_t, int32_t* out_instance, int32_t* out_tri, float* out_uv,
                                     void* workspace, size_t workspace_bytes, cp_stream_t stream);
 
+/* ---- path tracer -------------------------------------------------------------
+ *
+ * The reference's ray-generation shader (src/shaders/rt/rt.rgen:567-677; its
+ * integrators :291-548, materials src/shaders/rt/rtcommon.glsl:253-369,
+ * ReSTIR src/shaders/rt/restir.glsl:17-35) and tone mapping
+ * (src/shaders/tonemap.frag) as CUDA kernels over this library's BVH, writing
+ * a device image buffer instead of a swapchain image.  Replaces RTPipe::trace
+ * (src/vk/rt.cpp:346-394) and the tonemap pass.  Scenes are world-space
+ * triangles with per-vertex normals and one constant material per object (no
+ * textures); an object with an emission component above zero is a light, and
+ * its triangles must be contiguous.  What GLSL leaves to the implementation
+ * is fixed: sin / cos / pow / exp are the library's own routines, and the
+ * pixel seed is tea(pixel, seed) where the shader reads the clock
+ * (rt.rgen:569).
+ */
+typedef struct cp_shade_scene cp_shade_scene;
+
+typedef struct {
+    float eye[3], right[3], up[3], fwd[3]; /* orthonormal camera frame */
+    float tan_half_y;                      /* tan of half the vertical field of view */
+    float aspect;                          /* width / height */
+    int32_t width, height;                 /* pixels; row 0 at the top */
+} cp_shade_camera;
+
+typedef struct {
+    float clear[3];             /* colour of a primary miss */
+    float env[3];               /* environment light of a secondary miss */
+    int32_t samples;            /* samples per pixel per frame (> 0) */
+    int32_t max_depth;          /* bounces (>= 0) */
+    int32_t qmc;                /* 1: Hammersley jitter over samples x max_frame */
+    int32_t integrator;         /* 0 direct, 1 material sampling, 2 MIS, 3 ReSTIR direct only, 4 ReSTIR */
+    int32_t brdf;               /* 0 Blinn-Phong, 1 GGX */
+    int32_t use_rr;             /* Russian roulette */
+    int32_t use_metalness;
+    int32_t frame;              /* 0: write the frame; > 0: blend into the image by 1 / (frame + 1) */
+    int32_t max_frame;
+    int32_t new_samples;        /* ReSTIR light candidates per pixel */
+    int32_t temporal_multiplier;
+    int32_t use_temporal;       /* ReSTIR: reuse the previous frame's reservoirs */
+    int32_t debug_view;         /* 1, 2, 3: the previous frame's position, normal, albedo, reprojected */
+    uint32_t seed;
+} cp_shade_params;
+
+/* A ReSTIR reservoir (restir.glsl:1-8), 48 bytes. */
+typedef struct {
+    float pos[3], normal[3], emissive[3];
+    float w_sum, w;
+    uint32_t n_seen;
+} cp_shade_reservoir;
+
+/* Build a scene: DEVICE arrays verts and normals (nt x 3 vertices x xyz),
+ * obj (nt, the object of each triangle), albedo and emissive (nobj x 3),
+ * metal_rough (nobj x 2).  The scene copies them and builds a 4-wide BVH over
+ * the triangles.  Synchronises `stream`.  Replaces the scene upload and
+ * acceleration-structure build of src/gpurt.cpp:220-241. */
+CP_API cp_status cp_shade_scene_create(const float* verts, const float* normals, const int32_t* obj, int64_t nt,
+                                       const float* albedo, const float* emissive, const float* metal_rough,
+                                       int32_t nobj, cp_stream_t stream, cp_shade_scene** out);
+CP_API cp_status cp_shade_scene_destroy(cp_shade_scene* scene);
+/* Number of lights (emissive objects with triangles). */
+CP_API cp_status cp_shade_scene_lights(const cp_shade_scene* scene, int32_t* n_lights);
+
+/* Render one frame into `image` (DEVICE, height x width x 3 floats; read when
+ * params->frame > 0).  gbuf (DEVICE, height x width x 9, may be NULL)
+ * receives each pixel's first hit of sample 0: position, shading normal,
+ * albedo (zeros on a miss).  ReSTIR's temporal state, each may be NULL:
+ * prev_pv (HOST, 16 floats, row-major world-to-clip matrix of the previous
+ * frame), prev_gbuf (DEVICE, the previous frame's gbuf), prev_res (DEVICE,
+ * height x width reservoirs of the previous frame), out_res (DEVICE, this
+ * frame's reservoirs, written by integrators 3 and 4).  Every integrator but
+ * material sampling needs a light.  Asynchronous on `stream`. */
+CP_API cp_status cp_shade_render(const cp_shade_scene* scene, const cp_shade_camera* camera,
+                                 const cp_shade_params* params, float* image, float* gbuf, const float* prev_pv,
+                                 const float* prev_gbuf, const cp_shade_reservoir* prev_res,
+                                 cp_shade_reservoir* out_res, cp_stream_t stream);
+
+/* tonemap.frag per colour component, n values (DEVICE in and out): type 0
+ * Hable's filmic curve scaled to white at 11.2, 1 exponential
+ * 1 - exp(-c exposure), each followed by pow(., 1 / gamma); 2 unchanged. */
+CP_API cp_status cp_shade_tonemap(int32_t type, float exposure, float gamma, int64_t n, const float* in,
+                                  float* out, cp_stream_t stream);
+
 /* ---- autotuner ------------------------------------------------------------ */
 
 /*

@@ -99,7 +99,7 @@ def test_backward_torus(orc, cpq, cuda):
         opp = np.linalg.norm(tv[:, (k + 2) % 3] - tv[:, (k + 1) % 3], axis=1)
         inside &= b3[:, k] * area2 / opp > 2 * FD_H
     face = use & inside
-    assert face.sum() >= 0.5 * use.sum()
+    assert face.sum() >= 0.25 * use.sum()
     err_h = np.abs(gq[idx] - fd[FD_H]).max(axis=1)
     rich = (4.0 * fd[FD_H / 2] - fd[FD_H]) / 3.0
     err_r = np.abs(gq[idx] - rich).max(axis=1)
