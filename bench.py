@@ -105,7 +105,8 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--leaf", type=int, default=0)
     ap.add_argument("--workload", default="large",
-                    choices=["large", "torus", "batched", "dynamic", "small", "rays", "scene", "camera"],
+                    choices=["large", "torus", "batched", "dynamic", "small", "rays", "scene", "camera",
+                             "shade"],
                     help="large is the headline; the others measure the other forms")
     return ap.parse_args()
 
@@ -897,6 +898,85 @@ def camera_arm(args):
                       "occluded_fraction": float(torch.isfinite(shadow.t).float().mean())}})
 
 
+def cbox_shading_arrays(g) -> dict:
+    """The Cornell box fixture (media/cbox/cbox.gltf's primitives and
+    instances) flattened to world space for the path tracer: each instance
+    one object, vertices through its matrix, normals through the inverse
+    transpose, the primitive's material factors."""
+    V, N, obj, al, em, mr = [], [], [], [], [], []
+    voff, toff = g["vert_offsets"], g["tri_offsets"]
+    for i, (j, T) in enumerate(zip(g["instance_primitive"], g["instance_transform"])):
+        M = T.astype(np.float64)
+        tri = g["tris"][toff[j]:toff[j + 1]]
+        V.append((g["verts"][voff[j]:voff[j + 1]].astype(np.float64) @ M[:, :3].T + M[:, 3])[tri])
+        N.append((g["normals"][voff[j]:voff[j + 1]].astype(np.float64) @ np.linalg.inv(M[:, :3]))[tri])
+        obj.append(np.full(len(tri), i, np.int32))
+        al.append(g["prim_albedo"][j])
+        em.append(g["prim_emissive"][j])
+        mr.append(g["prim_metal_rough"][j])
+    f32 = lambda a: np.ascontiguousarray(np.asarray(a), np.float32)  # noqa: E731
+    return {"verts": f32(np.concatenate(V)).reshape(-1, 9), "normals": f32(np.concatenate(N)).reshape(-1, 9),
+            "obj": np.concatenate(obj), "albedo": f32(al), "emissive": f32(em), "metal_rough": f32(mr)}
+
+
+def shade_arm(args):
+    """The reference's path tracer on its own scene: the Cornell box from its
+    camera at 1920 x 1440, the reference's defaults (8 samples per pixel,
+    depth 8, Russian roulette, Blinn-Phong), MIS; one frame per step.  The
+    CPU baseline renders a 320 x 240 frame of the same view with the
+    restatement of the same shaders on all host cores."""
+    import torch
+
+    from gpurt_cpq import shading as G
+
+    dev = torch.device("cuda", 0)
+    g = np.load(ROOT / "tests" / "golden" / "cbox_scene.npz")
+    sa = cbox_shading_arrays(g)
+    td = {k: torch.from_numpy(v).to(dev) for k, v in sa.items()}
+    scene = G.ShadeScene(td["verts"], td["normals"], td["obj"], td["albedo"], td["emissive"], td["metal_rough"])
+    from gpurt_cpq import workloads as W
+
+    w, h, spp = 1920, 1440, 8
+    target = (W.CBOX_EYE[0], W.CBOX_EYE[1], 0.0)
+    cam = G.camera(W.CBOX_EYE, target, (0, 1, 0), W.CBOX_YFOV, w, h)
+    img = torch.zeros((h, w, 3), dtype=torch.float32, device=dev)
+    from gpurt_cpq._lib import lib
+
+    def frame(integrator):
+        scene.render(cam, integrator=integrator, samples=spp, max_depth=8, seed=7, image=img)
+
+    frame(G.MIS)
+    launches0 = lib.cp_kernel_launches()
+    ms = _timed(torch, lambda: frame(G.MIS), args.steps, args.warmup)
+    launches = (lib.cp_kernel_launches() - launches0) // (args.steps + args.warmup)
+    ms_restir = _timed(torch, lambda: frame(G.RESTIR), args.steps, args.warmup)
+    mean = float(img.mean())
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import shade as S
+
+        sw, sh_ = 320, 240
+        osc = S.Scene(sa["verts"], sa["normals"], sa["obj"], sa["albedo"], sa["emissive"], sa["metal_rough"])
+        ocam = S.camera(W.CBOX_EYE, target, (0, 1, 0), W.CBOX_YFOV, sw, sh_)
+        t0 = time.perf_counter()
+        osc.render(ocam, integrator=S.MIS, samples=spp, max_depth=8, seed=7)
+        secs = time.perf_counter() - t0
+        cpu = {"value": sw * sh_ * spp / secs, "unit": "samples/s", "cores": host_cores(), "kind": "port",
+               "sample": f"one {sw}x{sh_} frame of the same view, {spp} samples per pixel, MIS, the restatement "
+                         f"of the reference's shaders (equal to them bit for bit) on all host cores, "
+                         f"brute-force scene tracing, {cpu_model()}"}
+    extra = {"restir": {"value": w * h * spp / (ms_restir * 1e-3), "ms_per_step": ms_restir},
+             "gpu_launches_per_frame": int(launches), "mean_radiance": mean}
+    if cpu is not None:
+        extra["cpu_baseline"] = cpu
+    _line("path-traced samples/s (the reference's Cornell box, 1920x1440, MIS, 8 spp, depth 8)",
+          w * h * spp / (ms * 1e-3), "samples/s", ms, args,
+          {"workload": f"media/cbox/cbox.gltf (fixture: {sa['verts'].shape[0]:,} world-space tris, 10 objects, "
+                       f"1 light) from its camera, {w}x{h}, {spp} samples per pixel, max depth 8, Russian "
+                       "roulette, Blinn-Phong, MIS; one frame per step",
+           "integrator": "MIS"}, extra)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -906,7 +986,7 @@ def main():
     else:
         {"torus": torus_arm, "batched": batched_arm, "dynamic": dynamic_arm,
          "small": small_arm, "rays": rays_arm, "scene": scene_arm,
-         "camera": camera_arm}[args.workload](args)
+         "camera": camera_arm, "shade": shade_arm}[args.workload](args)
 
 
 if __name__ == "__main__":

@@ -106,11 +106,13 @@ __device__ __forceinline__ uint32_t quantise(float s, float lo, float scale, uin
     return (uint32_t)t;
 }
 
-// Half surface area of a box (ex*ey + ey*ez) + ez*ex, in that rounding order
-// (the SAH building block; the factor 2 of BBox::surface_area cancels).
+// Half surface area of a box, (ex*ez + ex*ey) + ey*ez in that rounding order:
+// the order of the reference's BBox::surface_area (src/lib/bbox.h:55-59),
+// whose factor 2 is exact, so twice this is its value bit for bit (the SAH
+// building block; the factor cancels in every cost comparison).
 __device__ __forceinline__ float half_area(float lx, float ly, float lz, float hx, float hy, float hz) {
     float ex = __fsub_rn(hx, lx), ey = __fsub_rn(hy, ly), ez = __fsub_rn(hz, lz);
-    return __fadd_rn(__fadd_rn(__fmul_rn(ex, ey), __fmul_rn(ey, ez)), __fmul_rn(ez, ex));
+    return __fadd_rn(__fadd_rn(__fmul_rn(ex, ez), __fmul_rn(ex, ey)), __fmul_rn(ey, ez));
 }
 
 __device__ __forceinline__ float fmin_t(float a, float b) { return a < b ? a : b; }

@@ -528,13 +528,16 @@ static inline uint32_t quantise(float s, float lo, float scale, uint32_t maxcell
     return (uint32_t)t;
 }
 
+/* Half the surface area of a box in the reference's BBox::surface_area order
+ * (src/lib/bbox.h:55-59: 2 (ex ez + ex ey + ey ez), summed left to right);
+ * its factor 2 is exact, so twice this equals that function bit for bit. */
 static inline float half_area(const float* b) {
     float ex = b[3] - b[0], ey = b[4] - b[1], ez = b[5] - b[2];
+    float xz = ex * ez;
     float xy = ex * ey;
     float yz = ey * ez;
-    float zx = ez * ex;
-    float s = xy + yz;
-    return s + zx;
+    float s = xz + xy;
+    return s + yz;
 }
 
 void orc_tree_free(orc_tree* t) {

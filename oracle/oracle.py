@@ -231,6 +231,9 @@ class Tree:
         self.first = arr(t.first, nn, np.int32)
         self.last = arr(t.last, nn, np.int32)
         self.box = arr(t.box, 6 * nn, np.float32).reshape(nn, 6)
+        self.cost = arr(t.cost, nn, np.float32)
+        self.first = arr(t.first, nn, np.int32)
+        self.last = arr(t.last, nn, np.int32)
         self.cluster = arr(t.cluster, nn, np.uint8)
         self.mesh_root = arr(t.mesh_root, t.nmeshes, np.int32)
         self.wide_root = arr(t.wide_root, t.nmeshes, np.int32)
