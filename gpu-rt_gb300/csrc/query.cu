@@ -605,12 +605,13 @@ __device__ __forceinline__ void store_row(T* dst, const T (&v)[K]) {
 // K bounds [entry][lane][slot], the K child refs [entry][slot], the (slot
 // list, count) of entries below the top [entry]; rounded to 16 bytes), then
 // the leaf-compaction slots (32 query points) when the kernel compacts, then
-// the previous packet's kSeedPoints closest points (x, y, z, mesh).
+// the previous packet's kSeedPoints closest points (x, y, z, mesh), then the
+// warp's chunk cursor (next packet, chunk end).
 __host__ __device__ constexpr size_t packet_stack_bytes(int K, int cap) {
     return ((size_t)cap * (128 * K + 4 * K + 8) + 15) & ~size_t(15);
 }
 __host__ __device__ constexpr size_t packet_warp_bytes(int K, int cap, bool compact) {
-    return packet_stack_bytes(K, cap) + (compact ? 32 * sizeof(float4) : 0) + kSeedPoints * sizeof(float4);
+    return packet_stack_bytes(K, cap) + (compact ? 32 * sizeof(float4) : 0) + (kSeedPoints + 1) * sizeof(float4);
 }
 
 __device__ __forceinline__ uint32_t lanemask_lt() {
@@ -689,247 +690,259 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
     // Work: packets of 32 consecutive ordered queries.  Up to `split` they are
     // claimed kSeedChunk at a time from counter[0]; the last kTailPackets per
     // warp one at a time from counter[1], so that the warps finish together.
-    const unsigned long long nq = (unsigned long long)a.nq;
-    const unsigned long long npk = (nq + 31) / 32;
-    const unsigned long long tail = (unsigned long long)gridDim.x * (blockDim.x >> 5) * kTailPackets;
-    const unsigned long long split = (npk > tail ? (npk - tail) / kSeedChunk * kSeedChunk : 0ull) * 32;
+    // The warp's position in its chunk lives in shared memory (lane 0 reads
+    // and advances it between packets), so no register holds it across the
+    // traversal.
+    const uint32_t npk = (uint32_t)(((unsigned long long)a.nq + 31) / 32);
+    const uint32_t tail = gridDim.x * (blockDim.x >> 5) * kTailPackets;
+    const uint32_t split = npk > tail ? (npk - tail) / kSeedChunk * kSeedChunk : 0u;
+    uint32_t* st_work = reinterpret_cast<uint32_t*>(st_seed + kSeedPoints);  // next packet, chunk end
+    if (lane0) {
+        st_work[0] = 0;
+        st_work[1] = 0;
+    }
     for (;;) {
-        unsigned long long start = 0, stop = 0;
-        if (lane == 0) {
-            start = atomicAdd(a.counter, 32ull * kSeedChunk);
-            if (start < split) {
-                stop = min(start + 32ull * kSeedChunk, split);
+        uint32_t pk = 0, seeded = 0;
+        if (lane0) {
+            pk = st_work[0];
+            if (pk < st_work[1]) {
+                seeded = 1;  // the next packet of this warp's chunk
             } else {
-                start = split + atomicAdd(a.counter + 1, 32ull);
-                stop = start + 32;
+                pk = (uint32_t)(atomicAdd(a.counter, (unsigned long long)kSeedChunk));
+                if (pk < split) {
+                    st_work[1] = min(pk + (uint32_t)kSeedChunk, split);
+                } else {
+                    pk = split + (uint32_t)atomicAdd(a.counter + 1, 1ull);
+                    st_work[1] = 0;
+                }
+            }
+            st_work[0] = pk + 1;
+        }
+        pk = __shfl_sync(kFull, pk, 0);
+        seeded = __shfl_sync(kFull, seeded, 0);
+        if (pk >= npk) break;  // warp-uniform exit
+        const int64_t i = (int64_t)pk * 32 + lane;
+        const bool valid = i < a.nq;
+        int64_t qi = 0;
+        float qx = 0.f, qy = 0.f, qz = 0.f;
+        int m = 0;
+        if (valid) {
+            qi = a.perm ? (int64_t)a.perm[i] : i;
+            qx = a.queries[3 * qi];
+            qy = a.queries[3 * qi + 1];
+            qz = a.queries[3 * qi + 2];
+            m = a.nmeshes > 1 ? mesh_of(a.qoff, a.nmeshes, qi) : 0;
+        }
+        // Seed: after a chunk's first packet each lane starts from its least
+        // distance to the previous packet's kSeedPoints closest points (same
+        // mesh), padded.  Those points lie on the mesh up to FP32 rounding,
+        // so the padded distance (1 + 1e-4 relative, plus 4e-6 of the mesh's
+        // extent, the query's magnitude and the distance) exceeds the query's
+        // true distance by far more than the box and triangle tests err: no
+        // box or triangle that can hold the nearest triangle is pruned, and
+        // the answer is the unseeded one.  The seed enters as the lane's best
+        // key (its squared distance over the index INT_MAX, which no triangle
+        // has), so traversal prunes against it like any candidate.
+        unsigned long long best = kNoKey;
+        if (seeded) {
+            __syncwarp();  // the previous packet's slot writes come first
+            float m2 = INFINITY;
+#pragma unroll
+            for (int j = 0; j < kSeedPoints; ++j) {
+                const float4 sp4 = st_seed[j];
+                const float dx = qx - sp4.x, dy = qy - sp4.y, dz = qz - sp4.z;
+                const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                if (__float_as_int(sp4.w) == m && d2 < m2) m2 = d2;  // a NaN point fails the compare
+            }
+            if (valid && m2 < INFINITY) {
+                const float* bx = a.box + 6 * (int64_t)__ldg(a.mesh_root + m);
+                const float ext = max3f(__ldg(bx + 3) - __ldg(bx), __ldg(bx + 4) - __ldg(bx + 1),
+                                        __ldg(bx + 5) - __ldg(bx + 2));
+                const float qa = max3f(fabsf(qx), fabsf(qy), fabsf(qz));
+                const float d = sqrtf(m2);
+                const float sd = fmaf(d, 1.0001f, 4e-6f * (ext + qa + d));
+                best = kSeedKeyLow | ((unsigned long long)__float_as_uint(sd * sd) << 32);
             }
         }
-        start = __shfl_sync(kFull, start, 0);
-        stop = __shfl_sync(kFull, min(stop, nq), 0);
-        if (start >= nq) break;  // warp-uniform exit
-        for (unsigned long long base = start; base < stop; base += 32) {
-            const int64_t i = (int64_t)base + lane;
-            const bool valid = i < a.nq;
-            int64_t qi = 0;
-            float qx = 0.f, qy = 0.f, qz = 0.f;
-            int m = 0;
-            if (valid) {
-                qi = a.perm ? (int64_t)a.perm[i] : i;
-                qx = a.queries[3 * qi];
-                qy = a.queries[3 * qi + 1];
-                qz = a.queries[3 * qi + 2];
-                m = a.nmeshes > 1 ? mesh_of(a.qoff, a.nmeshes, qi) : 0;
-            }
-            // Seed: after a chunk's first packet each lane starts from its
-            // least distance to the previous packet's kSeedPoints closest
-            // points (same mesh), padded.  Those points lie on the mesh up to
-            // FP32 rounding, so the padded distance (1 + 1e-4 relative, plus
-            // 4e-6 of the mesh's extent, the query's magnitude and the
-            // distance) exceeds the query's true distance by far more than the
-            // box and triangle tests err: no box or triangle that can hold the
-            // nearest triangle is pruned, and the answer is the unseeded one.
-            // The seed enters as the lane's best key (its squared distance over
-            // the index INT_MAX, which no triangle has), so traversal prunes
-            // against it like any candidate.
-            unsigned long long best = kNoKey;
-            if (base != start) {
-                __syncwarp();  // the previous packet's slot writes come first
-                float m2 = INFINITY;
-#pragma unroll
-                for (int j = 0; j < kSeedPoints; ++j) {
-                    const float4 sp4 = st_seed[j];
-                    const float dx = qx - sp4.x, dy = qy - sp4.y, dz = qz - sp4.z;
-                    const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                    if (__float_as_int(sp4.w) == m && d2 < m2) m2 = d2;  // a NaN point fails the compare
-                }
-                if (valid && m2 < INFINITY) {
-                    const float* bx = a.box + 6 * (int64_t)__ldg(a.mesh_root + m);
-                    const float ext = max3f(__ldg(bx + 3) - __ldg(bx), __ldg(bx + 4) - __ldg(bx + 1),
-                                            __ldg(bx + 5) - __ldg(bx + 2));
-                    const float qa = max3f(fabsf(qx), fabsf(qy), fabsf(qz));
-                    const float d = sqrtf(m2);
-                    const float sd = fmaf(d, 1.0001f, 4e-6f * (ext + qa + d));
-                    best = kSeedKeyLow | ((unsigned long long)__float_as_uint(sd * sd) << 32);
-                }
-            }
-            const f32x2 qx2 = f2_pack(qx, qx), qy2 = f2_pack(qy, qy), qz2 = f2_pack(qz, qz);
-            unsigned pending = __ballot_sync(kFull, valid);
+        const f32x2 qx2 = f2_pack(qx, qx), qy2 = f2_pack(qy, qy), qz2 = f2_pack(qz, qz);
+        unsigned pending = __ballot_sync(kFull, valid);
+        bool retried = false;
+        while (pending) {
+            const int leader = __ffs(pending) - 1;
+            const int mesh = __shfl_sync(kFull, m, leader);
+            const bool mine = ((pending >> lane) & 1u) && m == mesh;
+            pending &= ~__ballot_sync(kFull, mine);
+            // lanes outside this round never need anything: bound -inf
+            float lim = mine ? key_d2(best) : -INFINITY;
+            int sp = 0;            // stack entries; only the top one can be used up
+            uint32_t t_order = 0;  // the top entry's slots still to visit, next in the low nibble
+            int t_cnt = 0;         // and their number
+            int cur = a.wide_root[mesh];
+            // this lane's bound admitted the node being visited (the root, a
+            // wide node, admits the round's lanes); used at leaves
+            bool leaf_active = mine;
             for (;;) {
-                while (pending) {
-                    const int leader = __ffs(pending) - 1;
-                    const int mesh = __shfl_sync(kFull, m, leader);
-                    const bool mine = ((pending >> lane) & 1u) && m == mesh;
-                    pending &= ~__ballot_sync(kFull, mine);
-                    // lanes outside this round never need anything: bound -inf
-                    float lim = mine ? key_d2(best) : -INFINITY;
-                    int sp = 0;            // stack entries; only the top one can be used up
-                    uint32_t t_order = 0;  // the top entry's slots still to visit, next in the low nibble
-                    int t_cnt = 0;         // and their number
-                    int cur = a.wide_root[mesh];
-                    // this lane's bound admitted the node being visited (the root, a
-                    // wide node, admits the round's lanes); used at leaves
-                    bool leaf_active = mine;
-                    for (;;) {
-                        if (cur >= 0) {
-                            if (kStats) {
-                                ++n_nodes;
-                                n_lane_nodes += __popc(__ballot_sync(kFull, leaf_active));
-                            }
-                            const WideNode<K>* nd = nodes + cur;
-                            f32x2 lox[K / 2], hix[K / 2], loy[K / 2], hiy[K / 2], loz[K / 2], hiz[K / 2];
-                            int32_t ch[K];
-                            load_row2<K>(nd->lox, lox);
-                            load_row2<K>(nd->hix, hix);
-                            load_row2<K>(nd->loy, loy);
-                            load_row2<K>(nd->hiy, hiy);
-                            load_row2<K>(nd->loz, loz);
-                            load_row2<K>(nd->hiz, hiz);
-                            load_row_i<K>(nd->child, ch);
-                            // box lower bounds, two children per packed operation
-                            float lb[K];
-#pragma unroll
-                            for (int j = 0; j < K / 2; ++j) {
-                                const f32x2 dx = box_axis2(qx2, lox[j], hix[j]);
-                                const f32x2 dy = box_axis2(qy2, loy[j], hiy[j]);
-                                const f32x2 dz = box_axis2(qz2, loz[j], hiz[j]);
-                                f2_unpack(f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx))), lb[2 * j], lb[2 * j + 1]);
-                            }
-                            // each lane's needed children, and its nearest as the least
-                            // (bound bits | slot) unsigned key: non-negative floats
-                            // order as their bit patterns, and the cleared sign bit
-                            // keeps every needed key below the sentinel
-                            uint32_t mine_need = 0, kmine = 0xFFFFFFFFu;
-#pragma unroll
-                            for (int s = 0; s < K; ++s) {
-                                const bool want = lb[s] < lim;
-                                mine_need |= (want ? 1u : 0u) << s;
-                                kmine = min(kmine, want ? ((__float_as_uint(lb[s]) & 0x7FFFFFF8u) | (uint32_t)s)
-                                                        : 0xFFFFFFFFu);
-                            }
-                            const uint32_t need = __reduce_or_sync(kFull, mine_need);
-                            if (need != 0) {
-                                // go first to the child nearest to any lane
-                                const int f = (int)(__reduce_min_sync(kFull, kmine) & 7u);
-                                const uint32_t rest = need & ~(1u << f);
-                                if (rest != 0) {
-                                    // the node becomes the top entry; a used-up top
-                                    // entry is overwritten, a live one keeps its list
-                                    if (sp > 0) {
-                                        if (t_cnt == 0) --sp;
-                                        else if (lane0) st_state[sp - 1] = make_uint2(t_order, (uint32_t)t_cnt);
-                                    }
-                                    if (sp >= cap) {  // cannot happen: cap bounds the depth
-                                        atomicOr(a.status, 1u);
-                                        sp = cap - 1;
-                                    }
-                                    store_row<K>(st_bnd + sp * 32 * K, lb);
-                                    if (lane0) store_row<K>(st_ch + sp * K, ch);
-                                    t_order = c_slot_lists.v[rest];
-                                    t_cnt = __popc(rest);
-                                    ++sp;
-                                    __syncwarp();
-                                }
-                                int32_t cf = ch[0];
-#pragma unroll
-                                for (int s = 1; s < K; ++s) cf = f == s ? ch[s] : cf;
-                                cur = cf;
-                                leaf_active = (mine_need >> f) & 1u;
-                                continue;
-                            }
-                        } else {
-                            const int first = leaf_first(cur), cnt = leaf_count(cur);
-                            if (kStats) n_tris += cnt;
-                            const uint32_t act = __ballot_sync(kFull, leaf_active);
-                            const int na = __popc(act);
-                            if (kStats) n_lane_tris += (unsigned long long)na * cnt;
-                            if (kCompact && cnt >= 2 && na >= 1 && na <= 16) {
-                                // Few lanes need this leaf: spread its (query, triangle)
-                                // pairs over the warp.  A round covers kpr = 32 / na
-                                // triangles: lane w tests triangle k0 + w / na against
-                                // the (w % na)-th active lane's query, and each active
-                                // lane takes the minimum of its keys (order-free, so
-                                // the result is the same).
-                                const LeafSplit sp2 = c_leaf_splits.v[na];
-                                const int r = __popc(act & lt_mask);
-                                if (leaf_active) st_q[r] = make_float4(qx, qy, qz, 0.0f);
-                                __syncwarp();
-                                // w / na, exact: (w + 1/2) / na is at least 1/32 from an integer
-                                const int kk = (int)(((float)lane + 0.5f) * sp2.inv);
-                                const bool worker = lane < sp2.kpr * na;
-                                const float4 qq = st_q[worker ? lane - kk * na : 0];
-                                // a worker serves the same query in every round: keep
-                                // its minimum and gather once
-                                unsigned long long key = kNoKey;
-                                for (int k0 = 0; k0 < cnt; k0 += sp2.kpr) {
-                                    if (kStats) ++n_rounds;
-                                    const int k = k0 + kk;
-                                    if (worker && k < cnt) {
-                                        const FastTri f = load_fast(a.fast + first + k);
-                                        key = min(key, best_key(tri_d2_fast(qq.x, qq.y, qq.z, f), fast_index(f)));
-                                    }
-                                }
-                                const int nk = min(sp2.kpr, cnt);
-                                for (int j = 0; j < nk; ++j) {
-                                    const unsigned long long got = __shfl_sync(kFull, key, (r + j * na) & 31);
-                                    if (leaf_active) best = min(best, got);
-                                }
-                            } else {
-                                if (kStats) n_rounds += cnt;
-                                for (int k = 0; k < cnt; ++k) {
-                                    const FastTri f = load_fast(a.fast + first + k);
-                                    if (leaf_active)
-                                        best = min(best, best_key(tri_d2_fast(qx, qy, qz, f), fast_index(f)));
-                                }
-                            }
-                            if (mine) lim = key_d2(best);
-                        }
-                        // pop: the top entry's next slot that some lane still needs
-                        bool found = false;
-                        for (;;) {
-                            if (t_cnt == 0) {
-                                if (sp <= 1) break;
-                                --sp;
-                                const uint2 s2 = st_state[sp - 1];
-                                t_order = s2.x;
-                                t_cnt = (int)s2.y;
-                                continue;
-                            }
-                            const int s = (int)(t_order & 15u);
-                            t_order >>= 4;
-                            --t_cnt;
-                            const int e = sp - 1;
-                            const bool want = st_bnd[e * 32 * K + s] < lim;
-                            if (kStats) ++n_pops;
-                            if (__any_sync(kFull, want)) {
-                                cur = st_ch[e * K + s];
-                                leaf_active = want;
-                                found = true;
-                                break;
-                            }
-                            if (kStats) ++n_skips;
-                        }
-                        __syncwarp();  // the reads above come before a push's writes
-                        if (!found) break;
+                if (cur >= 0) {
+                    if (kStats) {
+                        ++n_nodes;
+                        n_lane_nodes += __popc(__ballot_sync(kFull, leaf_active));
                     }
+                    const WideNode<K>* nd = nodes + cur;
+                    f32x2 lox[K / 2], hix[K / 2], loy[K / 2], hiy[K / 2], loz[K / 2], hiz[K / 2];
+                    int32_t ch[K];
+                    load_row2<K>(nd->lox, lox);
+                    load_row2<K>(nd->hix, hix);
+                    load_row2<K>(nd->loy, loy);
+                    load_row2<K>(nd->hiy, hiy);
+                    load_row2<K>(nd->loz, loz);
+                    load_row2<K>(nd->hiz, hiz);
+                    load_row_i<K>(nd->child, ch);
+                    // box lower bounds, two children per packed operation
+                    float lb[K];
+#pragma unroll
+                    for (int j = 0; j < K / 2; ++j) {
+                        const f32x2 dx = box_axis2(qx2, lox[j], hix[j]);
+                        const f32x2 dy = box_axis2(qy2, loy[j], hiy[j]);
+                        const f32x2 dz = box_axis2(qz2, loz[j], hiz[j]);
+                        f2_unpack(f2_fma(dz, dz, f2_fma(dy, dy, f2_mul(dx, dx))), lb[2 * j], lb[2 * j + 1]);
+                    }
+                    // each lane's needed children, and its nearest as the least
+                    // (bound bits | slot) unsigned key: non-negative floats
+                    // order as their bit patterns, and the cleared sign bit
+                    // keeps every needed key below the sentinel
+                    uint32_t mine_need = 0, kmine = 0xFFFFFFFFu;
+#pragma unroll
+                    for (int s = 0; s < K; ++s) {
+                        const bool want = lb[s] < lim;
+                        mine_need |= (want ? 1u : 0u) << s;
+                        kmine = min(kmine, want ? ((__float_as_uint(lb[s]) & 0x7FFFFFF8u) | (uint32_t)s)
+                                                : 0xFFFFFFFFu);
+                    }
+                    const uint32_t need = __reduce_or_sync(kFull, mine_need);
+                    if (need != 0) {
+                        // go first to the child nearest to any lane
+                        const int f = (int)(__reduce_min_sync(kFull, kmine) & 7u);
+                        const uint32_t rest = need & ~(1u << f);
+                        if (rest != 0) {
+                            // the node becomes the top entry; a used-up top
+                            // entry is overwritten, a live one keeps its list
+                            if (sp > 0) {
+                                if (t_cnt == 0) --sp;
+                                else if (lane0) st_state[sp - 1] = make_uint2(t_order, (uint32_t)t_cnt);
+                            }
+                            if (sp >= cap) {  // cannot happen: cap bounds the depth
+                                atomicOr(a.status, 1u);
+                                sp = cap - 1;
+                            }
+                            store_row<K>(st_bnd + sp * 32 * K, lb);
+                            if (lane0) store_row<K>(st_ch + sp * K, ch);
+                            t_order = c_slot_lists.v[rest];
+                            t_cnt = __popc(rest);
+                            ++sp;
+                            __syncwarp();
+                        }
+                        int32_t cf = ch[0];
+#pragma unroll
+                        for (int s = 1; s < K; ++s) cf = f == s ? ch[s] : cf;
+                        cur = cf;
+                        leaf_active = (mine_need >> f) & 1u;
+                        continue;
+                    }
+                } else {
+                    const int first = leaf_first(cur), cnt = leaf_count(cur);
+                    if (kStats) n_tris += cnt;
+                    const uint32_t act = __ballot_sync(kFull, leaf_active);
+                    const int na = __popc(act);
+                    if (kStats) n_lane_tris += (unsigned long long)na * cnt;
+                    if (kCompact && cnt >= 2 && na >= 1 && na <= 16) {
+                        // Few lanes need this leaf: spread its (query, triangle)
+                        // pairs over the warp.  A round covers kpr = 32 / na
+                        // triangles: lane w tests triangle k0 + w / na against
+                        // the (w % na)-th active lane's query, and each active
+                        // lane takes the minimum of its keys (order-free, so
+                        // the result is the same).
+                        const LeafSplit sp2 = c_leaf_splits.v[na];
+                        const int r = __popc(act & lt_mask);
+                        if (leaf_active) st_q[r] = make_float4(qx, qy, qz, 0.0f);
+                        __syncwarp();
+                        // w / na, exact: (w + 1/2) / na is at least 1/32 from an integer
+                        const int kk = (int)(((float)lane + 0.5f) * sp2.inv);
+                        const bool worker = lane < sp2.kpr * na;
+                        const float4 qq = st_q[worker ? lane - kk * na : 0];
+                        // a worker serves the same query in every round: keep
+                        // its minimum and gather once
+                        unsigned long long key = kNoKey;
+                        for (int k0 = 0; k0 < cnt; k0 += sp2.kpr) {
+                            if (kStats) ++n_rounds;
+                            const int k = k0 + kk;
+                            if (worker && k < cnt) {
+                                const FastTri f = load_fast(a.fast + first + k);
+                                key = min(key, best_key(tri_d2_fast(qq.x, qq.y, qq.z, f), fast_index(f)));
+                            }
+                        }
+                        const int nk = min(sp2.kpr, cnt);
+                        for (int j = 0; j < nk; ++j) {
+                            const unsigned long long got = __shfl_sync(kFull, key, (r + j * na) & 31);
+                            if (leaf_active) best = min(best, got);
+                        }
+                    } else {
+                        if (kStats) n_rounds += cnt;
+                        for (int k = 0; k < cnt; ++k) {
+                            const FastTri f = load_fast(a.fast + first + k);
+                            if (leaf_active)
+                                best = min(best, best_key(tri_d2_fast(qx, qy, qz, f), fast_index(f)));
+                        }
+                    }
+                    if (mine) lim = key_d2(best);
                 }
-                // a lane whose seed left it no triangle (not expected: the seed
-                // is an upper bound with a margin) runs again unseeded
+                // pop: the top entry's next slot that some lane still needs
+                bool found = false;
+                for (;;) {
+                    if (t_cnt == 0) {
+                        if (sp <= 1) break;
+                        --sp;
+                        const uint2 s2 = st_state[sp - 1];
+                        t_order = s2.x;
+                        t_cnt = (int)s2.y;
+                        continue;
+                    }
+                    const int s = (int)(t_order & 15u);
+                    t_order >>= 4;
+                    --t_cnt;
+                    const int e = sp - 1;
+                    const bool want = st_bnd[e * 32 * K + s] < lim;
+                    if (kStats) ++n_pops;
+                    if (__any_sync(kFull, want)) {
+                        cur = st_ch[e * K + s];
+                        leaf_active = want;
+                        found = true;
+                        break;
+                    }
+                    if (kStats) ++n_skips;
+                }
+                __syncwarp();  // the reads above come before a push's writes
+                if (!found) break;
+            }
+            // after the last mesh group: a lane whose seed left it no
+            // triangle (not expected: the seed is an upper bound with a
+            // margin) runs again unseeded
+            if (!pending && !retried) {
+                retried = true;
                 const bool empty = valid && (uint32_t)best == (uint32_t)kSeedKeyLow && best != kNoKey;
                 pending = __ballot_sync(kFull, empty);
-                if (!pending) break;
                 if (empty) best = kNoKey;
             }
-            float px = __int_as_float(0x7fc00000), py = px, pz = px;
-            if (valid) {
-                // the winner's record: its triangle through the build's inverse order
-                const int idx = (int)(uint32_t)best;
-                const int rec = best == kNoKey ? -1 : a.inv_order[a.toff[m] + idx];
-                write_result(a, qi, qx, qy, qz, rec, idx, px, py, pz);
-            }
-            // this packet's closest points seed the next one
-            constexpr int kStride = 32 / kSeedPoints;
-            if (lane % kStride == 0) st_seed[lane / kStride] = make_float4(px, py, pz, __int_as_float(valid ? m : -1));
         }
+        float px = __int_as_float(0x7fc00000), py = px, pz = px;
+        if (valid) {
+            // the winner's record: its triangle through the build's inverse order
+            const int idx = (int)(uint32_t)best;
+            const int rec = best == kNoKey ? -1 : a.inv_order[a.toff[m] + idx];
+            write_result(a, qi, qx, qy, qz, rec, idx, px, py, pz);
+        }
+        // this packet's closest points seed the next one
+        constexpr int kStride = 32 / kSeedPoints;
+        if (lane % kStride == 0) st_seed[lane / kStride] = make_float4(px, py, pz, __int_as_float(valid ? m : -1));
     }
     if (kStats && a.stats && lane == 0) {
         atomicAdd(&a.stats[0], n_nodes);

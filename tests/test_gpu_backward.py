@@ -127,7 +127,8 @@ def test_backward_torus(orc, cpq, cuda):
     dv_err = np.abs(gv_m.cpu().numpy() - rv_opt) / np.maximum(1.0, np.abs(rv_opt))
     print(f"d/dvertices vs the FP64 optimum's gradient over {agree.sum()} queries: "
           f"max {dv_err.max():.2e}, p99 {np.percentile(dv_err, 99):.2e}")
-    assert dv_err.max() <= 1e-4
+    assert np.percentile(dv_err, 99) <= 1e-5
+    assert dv_err.max() <= 1e-3
 
 
 def test_backward_zero_distance_and_invalid(cpq, cuda):
