@@ -591,8 +591,10 @@ def rays_arm(args):
 
 
 def batched_form(steps: int, warmup: int) -> dict:
-    """256 uneven meshes: one batched build + one persistent graph-captured
-    launch, against plain per-mesh builds and launches on the same GPU."""
+    """256 uneven meshes: a leaf size per size class (cp_batch_autotune), one
+    batched build + one persistent graph-captured launch, against plain
+    per-mesh builds (each with its mesh's leaf size) and launches on the same
+    GPU."""
     import torch
 
     import gpurt_cpq as cpq
@@ -603,12 +605,16 @@ def batched_form(steps: int, warmup: int) -> dict:
     V, voff, T, toff, Q, qoff = W.concat_batch(meshes, queries)
     Vd, Td, Qd = (torch.from_numpy(x).to(dev) for x in (V, T, Q))
     nq = Qd.shape[0]
+    t0 = time.perf_counter()
+    leaves, o = cpq.autotune_batch(Vd, voff, Td, toff, Qd, qoff, branching=4)
+    tune_s = time.perf_counter() - t0
+    cls = np.floor(np.log2(np.diff(toff))).astype(int)
+    per_class = {int(c): int(leaves[cls == c][0]) for c in np.unique(cls)}
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    batch = cpq.Batch(Vd, voff, Td, toff, branching=4, leaf_size=2)
+    batch = cpq.Batch(Vd, voff, Td, toff, branching=4, leaf_sizes=leaves)
     torch.cuda.synchronize()
     build_batch_ms = (time.perf_counter() - t0) * 1e3
-    o = cpq.query_opts()
     ws = torch.empty(batch.workspace_size(nq, o), dtype=torch.uint8, device=dev)
     out = cpq.QueryResult(point=torch.empty((nq, 3), device=dev), dist=torch.empty(nq, device=dev),
                           tri=torch.empty(nq, dtype=torch.int32, device=dev), bary=None)
@@ -624,7 +630,7 @@ def batched_form(steps: int, warmup: int) -> dict:
     qparts = [Qd[qoff[i]:qoff[i + 1]] for i in range(len(meshes))]
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    plain = [cpq.Mesh(vparts[i], tparts[i].contiguous(), branching=4, leaf_size=2)
+    plain = [cpq.Mesh(vparts[i], tparts[i].contiguous(), branching=4, leaf_size=int(leaves[i]))
              for i in range(len(meshes))]
     torch.cuda.synchronize()
     build_plain_ms = (time.perf_counter() - t0) * 1e3
@@ -645,8 +651,9 @@ def batched_form(steps: int, warmup: int) -> dict:
                  {"workload": f"256 deformed icospheres/tori, {int(toff[-1])} tris "
                               f"({min(tri_counts)}..{max(tri_counts)} per mesh), {nq} queries "
                               f"({int(np.diff(qoff).min())}..{int(np.diff(qoff).max())} per mesh)",
-                  "branching": 4, "leaf_size": 2, "graph": True},
-                 {"per_mesh_launches": {"value": nq / (ms_p * 1e-3), "ms_per_step": ms_p},
+                  "branching": 4, "leaf_size": "per size class (autotuned)", "graph": True},
+                 {"autotuned": {"leaf_size_by_tri_class": per_class, "tune_s": tune_s},
+                  "per_mesh_launches": {"value": nq / (ms_p * 1e-3), "ms_per_step": ms_p},
                   "speedup_vs_per_mesh": ms_p / ms_b, "target_speedup": 3.0,
                   "max_rel_diff_batched_vs_per_mesh": rel,
                   "build_ms": {"batched": build_batch_ms, "per_mesh_total": build_plain_ms}})

@@ -8,6 +8,7 @@
 // nothing synchronously and stays on its stream.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <atomic>
 #include <cmath>
 #include <cstdio>
@@ -226,10 +227,21 @@ cp_status to_query_params(const cp_query_opts* o, QueryParams* q) {
 
 cp_status build_common(Bvh& b, const float* verts, int64_t vstride_bytes, const int32_t* tris,
                        const std::vector<int64_t>& voff, const std::vector<int64_t>& toff,
-                       const cp_build_opts* opts, cp_stream_t stream) {
+                       const cp_build_opts* opts, cp_stream_t stream, const int32_t* mesh_leaf = nullptr) {
     BuildParams p;
     cp_status s = to_build_params(opts, &p);
     if (s != CP_SUCCESS) return s;
+    if (mesh_leaf) {
+        const int32_t nm = (int32_t)toff.size() - 1;
+        p.mesh_leaf.assign(mesh_leaf, mesh_leaf + nm);
+        int32_t mx = 1;
+        for (int32_t i = 0; i < nm; ++i) {
+            if (p.mesh_leaf[i] < 1 || p.mesh_leaf[i] > kMaxLeafSize)
+                return fail(CP_ERROR_INVALID_VALUE, "leaf size of mesh " + std::to_string(i) + " must be in 1..15");
+            mx = std::max(mx, p.mesh_leaf[i]);
+        }
+        p.leaf_size = mx;
+    }
     if (vstride_bytes < 12 || vstride_bytes % 4)
         return fail(CP_ERROR_INVALID_VALUE, "vertex stride must be a multiple of 4 bytes and >= 12");
     bool bad = false;
@@ -616,6 +628,12 @@ CP_API cp_status cp_ray_query(const cp_mesh* m, const float* origins, const floa
 CP_API cp_status cp_batch_create(const float* verts, const int64_t* vert_offsets, const int32_t* tris,
                                  const int64_t* tri_offsets, int32_t nmeshes,
                                  const cp_build_opts* opts, cp_stream_t stream, cp_batch** out) {
+    return cp_batch_create_leaves(verts, vert_offsets, tris, tri_offsets, nmeshes, nullptr, opts, stream, out);
+}
+
+CP_API cp_status cp_batch_create_leaves(const float* verts, const int64_t* vert_offsets, const int32_t* tris,
+                                        const int64_t* tri_offsets, int32_t nmeshes, const int32_t* leaf_sizes,
+                                        const cp_build_opts* opts, cp_stream_t stream, cp_batch** out) {
     if (!out) return fail(CP_ERROR_INVALID_VALUE, "out is NULL");
     *out = nullptr;
     if (!verts || !tris || !vert_offsets || !tri_offsets)
@@ -634,7 +652,7 @@ CP_API cp_status cp_batch_create(const float* verts, const int64_t* vert_offsets
     if (s != CP_SUCCESS) return s;
     cp_batch* bt = new (std::nothrow) cp_batch();
     if (!bt) return fail(CP_ERROR_OUT_OF_MEMORY, "host allocation of the handle failed");
-    s = build_common(bt->bvh, verts, 12, tris, voff, toff, opts, stream);
+    s = build_common(bt->bvh, verts, 12, tris, voff, toff, opts, stream, leaf_sizes);
     if (s != CP_SUCCESS) {
         delete bt;
         return s;

@@ -342,7 +342,8 @@ __global__ void k_refit(const float* __restrict__ verts, int64_t stride,
                         float* box, float* cost, uint8_t* __restrict__ leaf_flag,
                         uint32_t* __restrict__ arrive, TriRec* __restrict__ recs,
                         FastTri* __restrict__ fast, int32_t* __restrict__ inv_order,
-                        int leaf_size, int collapse, float c_node, float c_tri) {
+                        int leaf_size, const int32_t* __restrict__ mesh_leaf, int collapse, float c_node,
+                        float c_tri) {
     int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const int32_t t = order[k];
@@ -407,7 +408,8 @@ __global__ void k_refit(const float* __restrict__ verts, int64_t stride,
             const int32_t f = first[p], e = last[p];
             const int32_t size = e - f + 1;
             bool same_mesh = nmeshes <= 1 || ((keys[f] >> key_mesh_shift) == (keys[e] >> key_mesh_shift));
-            bool leafable = size <= leaf_size && same_mesh;
+            const int limit = mesh_leaf ? mesh_leaf[nmeshes > 1 ? (int)(keys[f] >> key_mesh_shift) : 0] : leaf_size;
+            bool leafable = size <= limit && same_mesh;
             if (collapse == 1) {
                 float Ap = half_area(pl[0], pl[1], pl[2], ph[0], ph[1], ph[2]);
                 float split = __fmul_rn(c_node, Ap);
@@ -617,6 +619,7 @@ void bvh_free(Bvh& b) {
     b.device_bytes = 0;
     b.nodes = nullptr;
     b.recs = nullptr;
+    b.mesh_leaf = nullptr;
 }
 
 cudaError_t bvh_build(Bvh& b, const float* verts, int64_t vstride, const int32_t* tris,
@@ -673,6 +676,11 @@ cudaError_t bvh_build(Bvh& b, const float* verts, int64_t vstride, const int32_t
     CK(dalloc(b, &b.recs, (size_t)n));
     CK(dalloc(b, &b.fast, (size_t)n));
     CK(dalloc(b, &b.status, (size_t)64));
+    if (!p.mesh_leaf.empty()) {
+        if ((int)p.mesh_leaf.size() != nm) return cudaErrorInvalidValue;
+        CK(dalloc(b, &b.mesh_leaf, (size_t)nm));
+        CK(cudaMemcpyAsync(b.mesh_leaf, b.p.mesh_leaf.data(), sizeof(int32_t) * nm, cudaMemcpyHostToDevice, st));
+    }
 
     CK(cudaMemcpyAsync(b.tris, tris, sizeof(int32_t) * 3 * n, cudaMemcpyDeviceToDevice, st));
     CK(cudaMemcpyAsync(b.d_voff, h_voff.data(), sizeof(int64_t) * (nm + 1), cudaMemcpyHostToDevice, st));
@@ -763,7 +771,7 @@ cudaError_t bvh_build(Bvh& b, const float* verts, int64_t vstride, const int32_t
     k_refit<true><<<grid_for(n), kThreads, 0, st>>>(
         verts, vstride, b.tris, b.order, b.keys, n, b.d_voff, b.d_toff, nm, key_shift, b.left,
         b.right, b.parent, b.first, b.last, b.box, b.cost, b.leaf_flag, b.arrive, b.recs,
-        b.fast, b.inv_order, p.leaf_size, p.collapse, p.c_node, p.c_tri); note_launch();
+        b.fast, b.inv_order, p.leaf_size, b.mesh_leaf, p.collapse, p.c_node, p.c_tri); note_launch();
     CK(cudaGetLastError());
     int32_t* max_depth = reinterpret_cast<int32_t*>(scratch + 1);
     k_wide_flags<<<grid_for(nn), kThreads, 0, st>>>(n, b.keys, nm, key_shift, b.parent, b.first,
@@ -830,7 +838,7 @@ cudaError_t bvh_refit(Bvh& b, const float* verts, int64_t vstride, cudaStream_t 
     k_refit<false><<<grid_for(n), kThreads, 0, st>>>(
         verts, vstride, b.tris, b.order, b.keys, n, b.d_voff, b.d_toff, b.nmeshes, key_shift,
         b.left, b.right, b.parent, b.first, b.last, b.box, b.cost, b.leaf_flag, b.arrive, b.recs,
-        b.fast, b.inv_order, b.p.leaf_size, b.p.collapse, b.p.c_node, b.p.c_tri); note_launch();
+        b.fast, b.inv_order, b.p.leaf_size, nullptr, b.p.collapse, b.p.c_node, b.p.c_tri); note_launch();
     CK(cudaGetLastError());
     const int64_t slots = b.num_wide * b.p.K;
     switch (b.p.K) {

@@ -17,6 +17,9 @@ struct BuildParams {
     int collapse = 0;       // 0 count, 1 SAH
     float c_node = 1.0f;    // SAH node-visit cost
     float c_tri = 1.0f;     // SAH triangle-test cost
+    // optional, per mesh of a batch: max triangles per leaf (then leaf_size is
+    // their maximum); empty: leaf_size for every mesh
+    std::vector<int32_t> mesh_leaf;
 };
 
 // Everything a build leaves on the device.  A single mesh is a batch of one.
@@ -57,6 +60,7 @@ struct Bvh {
     uint8_t* cluster = nullptr;     // 2nt - 1
     uint32_t* arrive = nullptr;     // 2nt - 1 refit counters
     int32_t* mesh_root = nullptr;   // nmeshes: binary root per mesh
+    int32_t* mesh_leaf = nullptr;   // nmeshes: per-mesh leaf limit, or nullptr (leaf_size)
     int32_t* wide_src = nullptr;    // num_wide
     int32_t* slot_src = nullptr;    // num_wide x K: binary node per child slot (-1 empty)
     uint32_t* status = nullptr;     // device status word (CP_DEVICE_* bits)

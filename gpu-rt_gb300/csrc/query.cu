@@ -46,10 +46,10 @@ constexpr int kStackTotal = 256;   // >= (K-1)(depth+1) for any 64+32-bit-key LB
 // from kSeedPoints of its closest points), then kTailPackets single packets
 // per warp at the end.
 #ifndef CPQ_SEED_CHUNK
-#define CPQ_SEED_CHUNK 16
+#define CPQ_SEED_CHUNK 4
 #endif
 #ifndef CPQ_SEED_POINTS
-#define CPQ_SEED_POINTS 8
+#define CPQ_SEED_POINTS 16
 #endif
 constexpr unsigned long long kSeedChunk = CPQ_SEED_CHUNK;
 constexpr int kSeedPoints = CPQ_SEED_POINTS;

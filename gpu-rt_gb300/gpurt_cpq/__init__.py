@@ -9,7 +9,8 @@ from ._lib import CpError, LIB_PATH, lib  # noqa: F401  (raises if the library i
 from . import shading  # noqa: F401
 from .gltf import GltfScene, load_gltf  # noqa: F401
 from .mesh import (Batch, Mesh, QueryResult, RayResult, Scene, SceneRayResult, SceneResult,  # noqa: F401
-                   autotune, build_opts, closest_distance, query_opts, ray_opts)
+                   autotune, autotune_batch, build_opts, closest_distance, query_opts, ray_opts)
 
-__all__ = ["Mesh", "Batch", "Scene", "SceneResult", "SceneRayResult", "QueryResult", "RayResult", "closest_distance", "autotune", "build_opts",
+__all__ = ["Mesh", "Batch", "Scene", "SceneResult", "SceneRayResult", "QueryResult", "RayResult", "closest_distance", "autotune", "autotune_batch",
+           "build_opts",
            "query_opts", "ray_opts", "load_gltf", "GltfScene", "CpError", "lib", "LIB_PATH", "shading"]

@@ -135,6 +135,10 @@ SIGNATURES = {
     "cp_autotune": (c_int32, [c_void_p, c_int64, c_void_p, c_int64, c_void_p, c_int64, c_char_p,
                               POINTER(BuildOpts), POINTER(QueryOpts)]),
     "cp_size_class": (c_int32, [c_int64]),
+    "cp_batch_autotune": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_void_p, c_void_p, c_int32,
+                                    c_char_p, c_void_p, POINTER(QueryOpts)]),
+    "cp_batch_create_leaves": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_void_p,
+                                         POINTER(BuildOpts), c_void_p, POINTER(c_void_p)]),
     "cp_mesh_export_build": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p,
                                        c_void_p, c_void_p]),
     "cp_mesh_export_wide": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p]),

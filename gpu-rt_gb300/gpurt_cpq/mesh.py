@@ -283,7 +283,10 @@ class Batch:
     """Many meshes with one batched build and one persistent query launch."""
 
     def __init__(self, verts: torch.Tensor, vert_offsets, tris: torch.Tensor, tri_offsets, *,
-                 branching: int = 2, leaf_size: int = 4, collapse: str = "count", stream=None):
+                 branching: int = 2, leaf_size: int = 4, collapse: str = "count", leaf_sizes=None,
+                 stream=None):
+        """leaf_sizes (one per mesh, e.g. from autotune_batch) replaces leaf_size
+        mesh by mesh (cp_batch_create_leaves)."""
         _check_dev(verts, "verts", torch.float32, 3)
         _check_dev(tris, "tris", torch.int32, 3)
         self.vert_offsets = np.ascontiguousarray(vert_offsets, dtype=np.int64)
@@ -291,9 +294,19 @@ class Batch:
         self.nmeshes = len(self.tri_offsets) - 1
         self.opts = build_opts(branching, leaf_size, collapse)
         h = c_void_p()
-        check(lib.cp_batch_create(_ptr(verts), c_void_p(self.vert_offsets.ctypes.data), _ptr(tris),
-                                  c_void_p(self.tri_offsets.ctypes.data), self.nmeshes,
-                                  byref(self.opts), _stream(stream), byref(h)), "cp_batch_create")
+        if leaf_sizes is None:
+            self.leaf_sizes = None
+            check(lib.cp_batch_create(_ptr(verts), c_void_p(self.vert_offsets.ctypes.data), _ptr(tris),
+                                      c_void_p(self.tri_offsets.ctypes.data), self.nmeshes,
+                                      byref(self.opts), _stream(stream), byref(h)), "cp_batch_create")
+        else:
+            self.leaf_sizes = np.ascontiguousarray(leaf_sizes, dtype=np.int32)
+            if self.leaf_sizes.shape != (self.nmeshes,):
+                raise ValueError("leaf_sizes needs one value per mesh")
+            check(lib.cp_batch_create_leaves(_ptr(verts), c_void_p(self.vert_offsets.ctypes.data), _ptr(tris),
+                                             c_void_p(self.tri_offsets.ctypes.data), self.nmeshes,
+                                             c_void_p(self.leaf_sizes.ctypes.data), byref(self.opts),
+                                             _stream(stream), byref(h)), "cp_batch_create_leaves")
         self._h = h
 
     def close(self) -> None:
@@ -462,6 +475,27 @@ class Scene:
                                  _ptr(out.instance), _ptr(out.tri), _ptr(out.bary), ws_ptr, ws_bytes,
                                  _stream(stream)), "cp_scene_query")
         return out
+
+
+def autotune_batch(verts: torch.Tensor, vert_offsets, tris: torch.Tensor, tri_offsets, queries: torch.Tensor,
+                   q_offsets, branching: int = 4, cache_path: str | None = None):
+    """Run cp_batch_autotune: a leaf size per mesh, chosen per size class
+    (floor(log2(triangles))) by timing each class's own meshes and queries.
+    Returns (leaf_sizes, QueryOpts)."""
+    _check_dev(verts, "verts", torch.float32, 3)
+    _check_dev(tris, "tris", torch.int32, 3)
+    _check_dev(queries, "queries", torch.float32, 3)
+    voff = np.ascontiguousarray(vert_offsets, dtype=np.int64)
+    toff = np.ascontiguousarray(tri_offsets, dtype=np.int64)
+    qoff = np.ascontiguousarray(q_offsets, dtype=np.int64)
+    leaves = np.zeros(len(toff) - 1, np.int32)
+    qo = QueryOpts()
+    torch.cuda.synchronize()
+    check(lib.cp_batch_autotune(_ptr(verts), c_void_p(voff.ctypes.data), _ptr(tris), c_void_p(toff.ctypes.data),
+                                len(toff) - 1, _ptr(queries), c_void_p(qoff.ctypes.data), branching,
+                                cache_path.encode() if cache_path else None, c_void_p(leaves.ctypes.data),
+                                byref(qo)), "cp_batch_autotune")
+    return leaves, qo
 
 
 def autotune(verts: torch.Tensor, tris: torch.Tensor, sample: torch.Tensor,

@@ -405,6 +405,17 @@ CP_API cp_status cp_batch_create(const float* verts, const int64_t* vert_offsets
                                  const int32_t* tris, const int64_t* tri_offsets, int32_t nmeshes,
                                  const cp_build_opts* opts, cp_stream_t stream, cp_batch** out);
 
+/* cp_batch_create with a leaf size per mesh: leaf_sizes (HOST, nmeshes values
+ * in 1..15) replaces opts->leaf_size mesh by mesh, in the same single build
+ * (each mesh's leaves hold at most its own count; the wide nodes and the one
+ * persistent query launch are shared).  cp_batch_autotune picks them per
+ * size class.  The reference's per-mesh BLAS builds take no such parameter
+ * (src/vk/vulkan.cpp:881-936). */
+CP_API cp_status cp_batch_create_leaves(const float* verts, const int64_t* vert_offsets,
+                                        const int32_t* tris, const int64_t* tri_offsets, int32_t nmeshes,
+                                        const int32_t* leaf_sizes, const cp_build_opts* opts,
+                                        cp_stream_t stream, cp_batch** out);
+
 CP_API cp_status cp_batch_destroy(cp_batch* batch);
 
 /* Per-mesh root info: number of meshes and wide-node count of the whole batch. */
@@ -599,6 +610,20 @@ CP_API cp_status cp_shade_tonemap(int32_t type, float exposure, float gamma, int
 CP_API cp_status cp_autotune(const float* verts, int64_t nv, const int32_t* tris, int64_t nt,
                              const float* queries, int64_t nq, const char* cache_path,
                              cp_build_opts* best_build, cp_query_opts* best_query);
+
+/* The batched form tuned per size class: meshes are grouped by
+ * cp_size_class(triangles); for each class the class's own meshes and queries
+ * (DEVICE arrays as for cp_batch_create and cp_batch_query; offsets HOST) are
+ * built as a batch and queried at leaf sizes 1, 2, 4 and 8, and the fastest
+ * is that class's leaf size.  Writes leaf_sizes (HOST, nmeshes) for
+ * cp_batch_create_leaves, and the query options (the packet traversal's
+ * defaults).  With cache_path, results are read from and written to the
+ * autotuner's cache file (lines marked B, keyed by triangle class, the class's
+ * mean queries per mesh and branching).  Synchronous. */
+CP_API cp_status cp_batch_autotune(const float* verts, const int64_t* vert_offsets, const int32_t* tris,
+                                   const int64_t* tri_offsets, int32_t nmeshes, const float* queries,
+                                   const int64_t* q_offsets, int32_t branching, const char* cache_path,
+                                   int32_t* leaf_sizes, cp_query_opts* best_query);
 
 /* Size class used by the autotuner cache: floor(log2(num_triangles)). */
 CP_API int32_t cp_size_class(int64_t num_triangles);

@@ -550,10 +550,37 @@ void orc_tree_free(orc_tree* t) {
     free(t);
 }
 
+static int build_tree(const float* verts, const int64_t* vert_offsets, const int32_t* tris,
+                      const int64_t* tri_offsets, int32_t nmeshes, int64_t nv_total, int64_t nt_total,
+                      int32_t K, int32_t leaf_size, const int32_t* mesh_leaf, int32_t collapse, float c_node,
+                      float c_tri, orc_tree** out);
+
 int orc_build(const float* verts, const int64_t* vert_offsets, const int32_t* tris,
               const int64_t* tri_offsets, int32_t nmeshes, int64_t nv_total, int64_t nt_total,
               int32_t K, int32_t leaf_size, int32_t collapse, float c_node, float c_tri,
               orc_tree** out) {
+    return build_tree(verts, vert_offsets, tris, tri_offsets, nmeshes, nv_total, nt_total, K, leaf_size, NULL,
+                      collapse, c_node, c_tri, out);
+}
+
+int orc_build_leaves(const float* verts, const int64_t* vert_offsets, const int32_t* tris,
+                     const int64_t* tri_offsets, int32_t nmeshes, int64_t nv_total, int64_t nt_total,
+                     int32_t K, const int32_t* mesh_leaf, int32_t collapse, float c_node, float c_tri,
+                     orc_tree** out) {
+    if (!mesh_leaf || nmeshes <= 0) return 1;
+    int32_t mx = 1;
+    for (int32_t m = 0; m < nmeshes; ++m) {
+        if (mesh_leaf[m] < 1 || mesh_leaf[m] > 15) return 1;
+        if (mesh_leaf[m] > mx) mx = mesh_leaf[m];
+    }
+    return build_tree(verts, vert_offsets, tris, tri_offsets, nmeshes, nv_total, nt_total, K, mx, mesh_leaf,
+                      collapse, c_node, c_tri, out);
+}
+
+static int build_tree(const float* verts, const int64_t* vert_offsets, const int32_t* tris,
+                      const int64_t* tri_offsets, int32_t nmeshes, int64_t nv_total, int64_t nt_total,
+                      int32_t K, int32_t leaf_size, const int32_t* mesh_leaf, int32_t collapse, float c_node,
+                      float c_tri, orc_tree** out) {
     (void)nv_total;
     *out = NULL;
     if (nt_total <= 0 || nmeshes <= 0) return 1;
@@ -733,7 +760,8 @@ int orc_build(const float* verts, const int64_t* vert_offsets, const int32_t* tr
             }
             int32_t size = T->last[p] - T->first[p] + 1;
             int same_mesh = T->mesh_of_tri[T->first[p]] == T->mesh_of_tri[T->last[p]];
-            int leafable = size <= leaf_size && same_mesh;
+            int limit = mesh_leaf ? mesh_leaf[T->mesh_of_tri[T->first[p]]] : leaf_size;
+            int leafable = size <= limit && same_mesh;
             if (collapse == 1) {
                 float Ap = half_area(pb);
                 float split = c_node * Ap;

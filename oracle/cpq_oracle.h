@@ -100,6 +100,12 @@ int orc_build(const float* verts, const int64_t* vert_offsets, const int32_t* tr
               const int64_t* tri_offsets, int32_t nmeshes, int64_t nv_total, int64_t nt_total,
               int32_t branching, int32_t leaf_size, int32_t collapse, float c_node, float c_tri,
               orc_tree** out);
+/* orc_build with a leaf size per mesh (mesh_leaf: nmeshes values in 1..15;
+ * leaf_size is then ignored), as cp_batch_create_leaves builds. */
+int orc_build_leaves(const float* verts, const int64_t* vert_offsets, const int32_t* tris,
+                     const int64_t* tri_offsets, int32_t nmeshes, int64_t nv_total, int64_t nt_total,
+                     int32_t branching, const int32_t* mesh_leaf, int32_t collapse, float c_node, float c_tri,
+                     orc_tree** out);
 void orc_tree_free(orc_tree* t);
 
 /* FP32 closest-first traversal of the wide tree (the CPU baseline).

@@ -75,6 +75,9 @@ def lib():
         L.orc_build.restype = c_int
         L.orc_build.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_int64, c_int64,
                                 c_int32, c_int32, c_int32, c_float, c_float, POINTER(POINTER(OrcTree))]
+        L.orc_build_leaves.restype = c_int
+        L.orc_build_leaves.argtypes = [c_void_p, c_void_p, c_void_p, c_void_p, c_int32, c_int64, c_int64,
+                                       c_int32, c_void_p, c_int32, c_float, c_float, POINTER(POINTER(OrcTree))]
         L.orc_tree_free.restype = None
         L.orc_tree_free.argtypes = [POINTER(OrcTree)]
         L.orc_query_f32.restype = c_double
@@ -202,15 +205,21 @@ class Tree:
     """FP32 CPU restatement of the GPU build (owns the C tree)."""
 
     def __init__(self, verts, tris, branching=2, leaf_size=4, collapse=0, c_node=1.0, c_tri=1.0,
-                 vert_offsets=None, tri_offsets=None):
+                 vert_offsets=None, tri_offsets=None, mesh_leaf=None):
         self.verts, self.tris = _f32(verts), _i32(tris)
         self.voff = None if vert_offsets is None else np.ascontiguousarray(vert_offsets, np.int64)
         self.toff = None if tri_offsets is None else np.ascontiguousarray(tri_offsets, np.int64)
         nm = 1 if self.toff is None else len(self.toff) - 1
         ptr = POINTER(OrcTree)()
-        rc = lib().orc_build(_p(self.verts), _p(self.voff), _p(self.tris), _p(self.toff), nm,
-                             self.verts.shape[0], self.tris.shape[0], branching, leaf_size,
-                             collapse, c_node, c_tri, ctypes.byref(ptr))
+        if mesh_leaf is None:
+            rc = lib().orc_build(_p(self.verts), _p(self.voff), _p(self.tris), _p(self.toff), nm,
+                                 self.verts.shape[0], self.tris.shape[0], branching, leaf_size,
+                                 collapse, c_node, c_tri, ctypes.byref(ptr))
+        else:
+            self.mesh_leaf = np.ascontiguousarray(mesh_leaf, np.int32)
+            rc = lib().orc_build_leaves(_p(self.verts), _p(self.voff), _p(self.tris), _p(self.toff), nm,
+                                        self.verts.shape[0], self.tris.shape[0], branching, _p(self.mesh_leaf),
+                                        collapse, c_node, c_tri, ctypes.byref(ptr))
         if rc != 0:
             raise RuntimeError(f"orc_build failed ({rc})")
         self._ptr = ptr

@@ -108,3 +108,59 @@ def test_batch_rejects_bad_offsets(cpq, cuda):
     b = cpq.Batch(dev(v, cuda), [0, 3], dev(t, cuda), [0, 1])
     with pytest.raises((CpError, ValueError)):
         b.query(dev(np.zeros((4, 3), np.float32), cuda), [0, 5])
+
+
+def test_batch_per_mesh_leaf_sizes_bit_exact(orc, cpq, cuda):
+    """A leaf size per mesh in one build (cp_batch_create_leaves): keys,
+    topology and wide nodes equal the restatement built with the same sizes,
+    and the answers are FP64's."""
+    from gpurt_cpq import workloads as W
+
+    meshes, queries = W.batched(seed=9, nmeshes=12, tri_range=(20, 3000), q_range=(10, 200))
+    V, voff, T, toff, Q, qoff = W.concat_batch(meshes, queries)
+    leaves = np.array([1, 2, 4, 8, 3, 15, 2, 1, 8, 4, 6, 2], np.int32)
+    ref = orc.Tree(V, T, 4, 0, 0, vert_offsets=voff, tri_offsets=toff, mesh_leaf=leaves)
+    b = cpq.Batch(dev(V, cuda), voff, dev(T, cuda), toff, branching=4, leaf_sizes=leaves)
+    bld, wide = b.export_build(), b.export_wide()
+    for k in ("keys", "order", "left", "right", "parent", "cluster", "wide_src"):
+        np.testing.assert_array_equal(bld[k], getattr(ref, k), err_msg=k)
+    np.testing.assert_array_equal(wide["boxes"].view(np.uint32), ref.wide_box.view(np.uint32))
+    np.testing.assert_array_equal(wide["refs"], ref.wide_ref)
+    np.testing.assert_array_equal(wide["counts"], ref.wide_count)
+    # every mesh's leaves hold at most its own count
+    counts, refs = wide["counts"], wide["refs"]
+    tri_mesh = np.searchsorted(toff, np.arange(toff[-1]), side="right") - 1
+    for c, r in zip(counts, refs):
+        if c > 0:
+            assert c <= leaves[tri_mesh[ref.order[r]]]
+    r = b.query(dev(Q, cuda), qoff)
+    d, tri = r.dist.cpu().numpy(), r.tri.cpu().numpy()
+    for m in range(len(toff) - 1):
+        s = slice(qoff[m], qoff[m + 1])
+        check_mesh(orc, V[voff[m]:voff[m + 1]], T[toff[m]:toff[m + 1]], Q[s], d[s], tri[s])
+
+
+def test_batch_autotune_per_size_class(orc, cpq, cuda, tmp_path):
+    """cp_batch_autotune: one leaf size per triangle-count class, written to
+    and read back from the cache file; the tuned batch answers as FP64."""
+    from gpurt_cpq import workloads as W
+
+    meshes, queries = W.batched(seed=5, nmeshes=24, tri_range=(1000, 40000), q_range=(500, 5000))
+    V, voff, T, toff, Q, qoff = W.concat_batch(meshes, queries)
+    Vd, Td, Qd = dev(V, cuda), dev(T, cuda), dev(Q, cuda)
+    cache = tmp_path / "tune.txt"
+    leaves, qo = cpq.autotune_batch(Vd, voff, Td, toff, Qd, qoff, branching=4, cache_path=str(cache))
+    cls = np.floor(np.log2(np.diff(toff))).astype(int)
+    assert set(np.unique(leaves)) <= {1, 2, 4, 8}
+    for c in np.unique(cls):
+        assert len(set(leaves[cls == c])) == 1  # one choice per class
+    lines = [ln.split() for ln in cache.read_text().splitlines() if ln.startswith("B ")]
+    assert sorted(int(x[1]) for x in lines) == sorted(np.unique(cls).tolist())
+    again, _ = cpq.autotune_batch(Vd, voff, Td, toff, Qd, qoff, branching=4, cache_path=str(cache))
+    np.testing.assert_array_equal(again, leaves)  # from the cache
+    b = cpq.Batch(Vd, voff, Td, toff, branching=4, leaf_sizes=leaves)
+    r = b.query(Qd, qoff, opts=qo)
+    d, tri = r.dist.cpu().numpy(), r.tri.cpu().numpy()
+    for m in range(len(toff) - 1):
+        s = slice(qoff[m], qoff[m + 1])
+        check_mesh(orc, V[voff[m]:voff[m + 1]], T[toff[m]:toff[m + 1]], Q[s], d[s], tri[s])
