@@ -53,7 +53,10 @@ constexpr int kStackTotal = 256;   // >= (K-1)(depth+1) for any 64+32-bit-key LB
 #endif
 constexpr unsigned long long kSeedChunk = CPQ_SEED_CHUNK;
 constexpr int kSeedPoints = CPQ_SEED_POINTS;
-constexpr unsigned long long kTailPackets = 4;
+#ifndef CPQ_TAIL_PACKETS
+#define CPQ_TAIL_PACKETS 4
+#endif
+constexpr unsigned long long kTailPackets = CPQ_TAIL_PACKETS;
 static_assert(kSeedPoints == 1 || kSeedPoints == 2 || kSeedPoints == 4 || kSeedPoints == 8 ||
                   kSeedPoints == 16 || kSeedPoints == 32, "seed points: a power of two up to 32");
 constexpr unsigned kFull = 0xffffffffu;
