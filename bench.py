@@ -822,6 +822,18 @@ def scene_arm(args):
     out = flat.query(qd, workspace=wsf, opts=o)
     ms_f = _timed(torch, lambda: flat.query(qd, workspace=wsf, opts=o, out=out), args.steps, args.warmup)
     diff = float((r.dist - out.dist).abs().max())
+    # moving every instance: rebuild (cp_scene_update) against refit (cp_scene_refit)
+    T2 = T.copy()
+    T2[:, :, 3] += np.float32(0.25)
+    upd_ms, refit_ms = [], []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        scene.update(T2 if len(upd_ms) % 2 == 0 else T)
+        upd_ms.append((time.perf_counter() - t0) * 1e3)
+        t0 = time.perf_counter()
+        scene.refit(T if len(refit_ms) % 2 == 0 else T2)
+        refit_ms.append((time.perf_counter() - t0) * 1e3)
+    scene.update(T)
     # rays from the query points in seeded random directions, through the
     # instances (cp_scene_ray_query) and through the flattened mesh
     rd = np.random.default_rng(17).normal(size=q.shape).astype(np.float32)
@@ -846,6 +858,7 @@ def scene_arm(args):
                               "note": "world vertices rounded to FP32 (up to 2^-24 of coordinates <= 47); "
                                       "the scene places the exact FP32 object vertices"},
            "max_abs_diff_vs_flattened": diff,
+           "instance_update_ms": {"rebuild": min(upd_ms), "refit": min(refit_ms)},
            "rays": {"value": nq / (ms_rs * 1e-3), "unit": "rays/s", "ms_per_step": ms_rs,
                     "flattened_mesh": {"value": nq / (ms_rf * 1e-3), "ms_per_step": ms_rf},
                     "hit_fraction": float(torch.isfinite(rs.t).float().mean()),

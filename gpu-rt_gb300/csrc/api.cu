@@ -783,6 +783,8 @@ struct cp_scene {
     float* d_fwd = nullptr;     // n x 12 world <- object
     float* d_inv = nullptr;     // n x 12 object <- world
     float* d_s2 = nullptr;      // n x 2: squared scale, lower bound of the squared stretch
+    std::vector<int32_t> h_baked;  // host copy of d_baked (which instances have world-space copies)
+    std::vector<int64_t> bake_off; // triangle offsets of the baked copies (n_baked + 1)
 };
 
 namespace {
@@ -882,6 +884,8 @@ cp_status scene_build(cp_scene* sc, const float* T, cudaStream_t st) {
     }
     const int64_t total = out_off.back();
     if (total > kMaxTriangles) return fail(CP_ERROR_NOT_SUPPORTED, "more than 2^27 - 1 baked triangles");
+    sc->h_baked = baked;
+    sc->bake_off = out_off;
     bvh_free(sc->baked);
     sc->baked = Bvh();
     sc->has_baked = false;
@@ -947,6 +951,70 @@ cp_status scene_build(cp_scene* sc, const float* T, cudaStream_t st) {
     return CP_SUCCESS;
 }
 
+// New transforms with the scene's instance kinds unchanged: the top level and
+// the world-space copies keep their topology; the copies are re-baked, the
+// proxies recomputed, and both trees refit bottom-up (boxes and triangle
+// records), as a TLAS update does instead of a rebuild.
+cp_status scene_refit(cp_scene* sc, const float* T, cudaStream_t st) {
+    std::vector<float> fwd, inv, s2;
+    std::vector<int32_t> baked;
+    cp_status s = instance_frames(T, sc->n, fwd, inv, s2, baked);
+    if (s != CP_SUCCESS) return s;  // nothing changed: the scene stays as it was
+    if (!sc->valid || baked != sc->h_baked) return scene_build(sc, T, st);  // kinds changed: rebuild
+    sc->valid = false;
+    const size_t n = (size_t)sc->n;
+    const Bvh& bottom = sc->batch->bvh;
+    CP_CUDA(cudaMemcpyAsync(sc->d_fwd, fwd.data(), sizeof(float) * 12 * n, cudaMemcpyHostToDevice, st), "scene upload");
+    CP_CUDA(cudaMemcpyAsync(sc->d_inv, inv.data(), sizeof(float) * 12 * n, cudaMemcpyHostToDevice, st), "scene upload");
+    CP_CUDA(cudaMemcpyAsync(sc->d_s2, s2.data(), sizeof(float) * 2 * n, cudaMemcpyHostToDevice, st), "scene upload");
+    cudaError_t e = cudaSuccess;
+    if (sc->has_baked) {
+        std::vector<int32_t> list;
+        for (size_t i = 0; i < n; ++i)
+            if (baked[i] >= 0) list.push_back((int32_t)i);
+        const int64_t total = sc->bake_off.back();
+        float* verts = nullptr;
+        int32_t *tris = nullptr, *d_list = nullptr;
+        int64_t* d_off = nullptr;
+        e = cudaMalloc(&verts, sizeof(float) * 9 * total);
+        if (e == cudaSuccess) e = cudaMalloc(&tris, sizeof(int32_t) * 3 * total);
+        if (e == cudaSuccess) e = cudaMalloc(&d_list, sizeof(int32_t) * list.size());
+        if (e == cudaSuccess) e = cudaMalloc(&d_off, sizeof(int64_t) * sc->bake_off.size());
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_list, list.data(), sizeof(int32_t) * list.size(), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(d_off, sc->bake_off.data(), sizeof(int64_t) * sc->bake_off.size(),
+                                cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess)
+            e = instance_bake(bottom, d_list, sc->d_inst_mesh, sc->d_fwd, d_off, (int32_t)list.size(), total, verts,
+                              tris, st);
+        if (e == cudaSuccess) e = bvh_refit(sc->baked, verts, 3, st);
+        cudaError_t e2 = cudaStreamSynchronize(st);
+        cudaFree(verts);
+        cudaFree(tris);
+        cudaFree(d_list);
+        cudaFree(d_off);
+        if (e == cudaSuccess) e = e2;
+        if (e != cudaSuccess) return cuda_fail(e, "scene refit (copies)");
+    }
+    float* verts = nullptr;
+    int32_t* tris = nullptr;
+    if (cudaMalloc(&verts, sizeof(float) * 6 * n) != cudaSuccess ||
+        cudaMalloc(&tris, sizeof(int32_t) * 3 * n) != cudaSuccess) {
+        cudaFree(verts);
+        return fail(CP_ERROR_OUT_OF_MEMORY, "scene proxies");
+    }
+    e = instance_proxies(bottom, sc->d_inst_mesh, sc->d_fwd, sc->n, verts, tris, st);
+    if (e == cudaSuccess) e = bvh_refit(sc->top, verts, 3, st);
+    cudaError_t e2 = cudaStreamSynchronize(st);
+    cudaFree(verts);
+    cudaFree(tris);
+    if (e == cudaSuccess) e = e2;
+    if (e != cudaSuccess) return cuda_fail(e, "scene refit");
+    sc->valid = true;
+    return CP_SUCCESS;
+}
+
 void scene_free(cp_scene* sc) {
     cudaFree(sc->d_inst_mesh);
     cudaFree(sc->d_baked);
@@ -1006,6 +1074,11 @@ CP_API cp_status cp_scene_create(const cp_batch* batch, const int32_t* instance_
 CP_API cp_status cp_scene_update(cp_scene* scene, const float* instance_transform, cp_stream_t stream) {
     if (!scene || !instance_transform) return fail(CP_ERROR_INVALID_VALUE, "scene or transforms is NULL");
     return scene_build(scene, instance_transform, reinterpret_cast<cudaStream_t>(stream));
+}
+
+CP_API cp_status cp_scene_refit(cp_scene* scene, const float* instance_transform, cp_stream_t stream) {
+    if (!scene || !instance_transform) return fail(CP_ERROR_INVALID_VALUE, "scene or transforms is NULL");
+    return scene_refit(scene, instance_transform, reinterpret_cast<cudaStream_t>(stream));
 }
 
 CP_API cp_status cp_scene_destroy(cp_scene* scene) {

@@ -125,6 +125,7 @@ SIGNATURES = {
     "cp_debug_fail_allocation": (None, [c_int64]),
     "cp_scene_create": (c_int32, [c_void_p, c_void_p, c_void_p, c_int32, c_void_p, POINTER(c_void_p)]),
     "cp_scene_update": (c_int32, [c_void_p, c_void_p, c_void_p]),
+    "cp_scene_refit": (c_int32, [c_void_p, c_void_p, c_void_p]),
     "cp_scene_destroy": (c_int32, [c_void_p]),
     "cp_scene_ray_workspace_size": (c_int32, [c_void_p, c_int64, POINTER(RayOpts), POINTER(c_size_t)]),
     "cp_scene_ray_query": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, POINTER(RayOpts),

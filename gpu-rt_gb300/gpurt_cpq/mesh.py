@@ -415,6 +415,14 @@ class Scene:
             raise ValueError("one transform per instance")
         check(lib.cp_scene_update(self._h, c_void_p(t.ctypes.data), _stream(stream)), "cp_scene_update")
 
+    def refit(self, transforms, *, stream=None) -> None:
+        """New transforms keeping the trees' topology (cp_scene_refit): the
+        TLAS update of the reference, where update() is its rebuild."""
+        t = _transforms(transforms)
+        if len(t) != self.n:
+            raise ValueError("one transform per instance")
+        check(lib.cp_scene_refit(self._h, c_void_p(t.ctypes.data), _stream(stream)), "cp_scene_refit")
+
     def close(self) -> None:
         if getattr(self, "_h", None) and self._h.value:
             lib.cp_scene_destroy(self._h)

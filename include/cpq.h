@@ -474,6 +474,19 @@ CP_API cp_status cp_scene_create(const cp_batch* batch, const int32_t* instance_
  */
 CP_API cp_status cp_scene_update(cp_scene* scene, const float* instance_transform, cp_stream_t stream);
 
+/*
+ * New transforms for every instance, keeping the trees' topology: the
+ * world-space copies are re-baked and the top level's instance boxes
+ * recomputed, and both BVHs are refit bottom-up (boxes and triangle records)
+ * instead of rebuilt — the reference's TLAS update as against its BLAS
+ * rebuild (src/gpurt.h:63-65, src/gpurt.cpp:220-241).  Answers are those of a
+ * rebuild; a tree refit after large motions is slower to walk.  An instance
+ * that changes kind (similarity <-> general affine) changes the copies, so
+ * then this rebuilds as cp_scene_update does.  Synchronises `stream`; errors
+ * as cp_scene_update.
+ */
+CP_API cp_status cp_scene_refit(cp_scene* scene, const float* instance_transform, cp_stream_t stream);
+
 CP_API cp_status cp_scene_destroy(cp_scene* scene);
 
 CP_API cp_status cp_scene_query_workspace_size(const cp_scene* scene, int64_t nq,

@@ -234,6 +234,44 @@ def test_scene_general_affine(orc, cpq, cuda):
     check_scene(orc, meshes, inst_mesh, T2, q, sc.query(dev(q, cuda)))
 
 
+def test_scene_refit_equals_rebuild(orc, cpq, cuda):
+    """cp_scene_refit keeps the trees' topology (the reference's TLAS update);
+    its answers are a freshly built scene's bit for bit, after every instance
+    moved with its kind kept (similarities and general affine maps), and after
+    two instances changed kind (the copies change: it rebuilds)."""
+    import torch
+
+    from gpurt_cpq import workloads as W
+
+    meshes = [W.icosphere(2), W.torus(40, 16)]
+    n = 40
+    inst_mesh = (np.arange(n) % 2).astype(np.int32)
+    T = random_similarities(n, seed=31)
+    T[5, :, :3] = T[5, :, :3] @ np.diag([3.0, 1.0, 0.5]).astype(np.float32)  # general affine
+    T[9, 0, 1] += 0.7                                                         # shear
+    b = make_batch(cpq, cuda, meshes, 4)
+    sc = cpq.Scene(b, inst_mesh, T)
+    q = np.random.default_rng(32).uniform(-7, 7, (30000, 3)).astype(np.float32)
+    qd = dev(q, cuda)
+    T2 = random_similarities(n, seed=33)
+    T2[5, :, :3] = T2[5, :, :3] @ np.diag([2.0, 1.0, 0.7]).astype(np.float32)
+    T2[9, 0, 1] += 0.4
+    sc.refit(T2)
+    r = sc.query(qd, want_bary=True)
+    f = cpq.Scene(b, inst_mesh, T2).query(qd, want_bary=True)
+    for k in ("dist", "point", "instance", "tri", "bary"):
+        assert torch.equal(getattr(r, k), getattr(f, k)), k
+    check_scene(orc, meshes, inst_mesh, T2, q, r)
+    T3 = T2.copy()
+    T3[5] = random_similarities(1, seed=34)[0]                                 # general -> similarity
+    T3[7, :, :3] = T3[7, :, :3] @ np.diag([1.0, 1.0, 2.0]).astype(np.float32)  # similarity -> general
+    sc.refit(T3)
+    r3 = sc.query(qd)
+    f3 = cpq.Scene(b, inst_mesh, T3).query(qd)
+    assert torch.equal(r3.dist, f3.dist) and torch.equal(r3.tri, f3.tri) and torch.equal(r3.instance, f3.instance)
+    check_scene(orc, meshes, inst_mesh, T3, q, r3)
+
+
 def test_scene_rejects_bad_input(cpq, cuda):
     from gpurt_cpq import workloads as W
     from gpurt_cpq._lib import CP_ERROR_INVALID_VALUE, CpError
