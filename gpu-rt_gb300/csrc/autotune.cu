@@ -11,6 +11,7 @@
 
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <fstream>
 #include <sstream>
 #include <string>
@@ -212,6 +213,48 @@ void write_batch_cache(const char* path, const std::vector<BatchEntry>& batch) {
 
 }  // namespace
 
+namespace {
+
+// Query time (ms, best of 3 after a warm-up) of the whole batch built with
+// the given per-mesh leaf sizes.
+cp_status time_batch(const float* verts, const int64_t* voff, const int32_t* tris, const int64_t* toff,
+                     int32_t nmeshes, const float* queries, const int64_t* qoff, int32_t branching,
+                     const std::vector<int32_t>& leaves, float* dist, cudaStream_t st, cudaEvent_t e0,
+                     cudaEvent_t e1, float* ms_out) {
+    cp_build_opts bo;
+    cp_build_opts_default(&bo);
+    bo.branching = branching;
+    cp_batch* b = nullptr;
+    cp_status s = cp_batch_create_leaves(verts, voff, tris, toff, nmeshes, leaves.data(), &bo, st, &b);
+    if (s != CP_SUCCESS) return s;
+    cp_query_opts qo;
+    cp_query_opts_default(&qo);
+    const int64_t nq = qoff[nmeshes];
+    size_t wsb = 0;
+    cp_batch_query_workspace_size(b, nq, &qo, &wsb);
+    void* ws = nullptr;
+    if (cudaMalloc(&ws, wsb) != cudaSuccess) {
+        cp_batch_destroy(b);
+        return CP_ERROR_OUT_OF_MEMORY;
+    }
+    float ms = 1e30f;
+    for (int rep = 0; rep < 4 && s == CP_SUCCESS; ++rep) {
+        cudaEventRecord(e0, st);
+        s = cp_batch_query(b, queries, qoff, &qo, nullptr, dist, nullptr, nullptr, ws, wsb, 0, st);
+        cudaEventRecord(e1, st);
+        cudaEventSynchronize(e1);
+        float t = 0.0f;
+        cudaEventElapsedTime(&t, e0, e1);
+        if (rep > 0 && t < ms) ms = t;  // the first run warms caches
+    }
+    cudaFree(ws);
+    cp_batch_destroy(b);
+    *ms_out = ms;
+    return s;
+}
+
+}  // namespace
+
 extern "C" CP_API cp_status cp_batch_autotune(const float* verts, const int64_t* vert_offsets, const int32_t* tris,
                                               const int64_t* tri_offsets, int32_t nmeshes, const float* queries,
                                               const int64_t* q_offsets, int32_t branching, const char* cache_path,
@@ -221,139 +264,99 @@ extern "C" CP_API cp_status cp_batch_autotune(const float* verts, const int64_t*
         return CP_ERROR_INVALID_VALUE;
     if (branching != 2 && branching != 4 && branching != 8) return CP_ERROR_INVALID_VALUE;
     cp_query_opts_default(best_query);
-    // size classes of the meshes
+    // size classes of the meshes, and each class's mean queries per mesh
     std::vector<int> cls(nmeshes);
-    std::vector<std::vector<int32_t>> members(64);
+    std::vector<int64_t> cls_meshes(64, 0), cls_queries(64, 0);
     for (int32_t m = 0; m < nmeshes; ++m) {
         const int64_t nt = tri_offsets[m + 1] - tri_offsets[m];
         if (nt <= 0 || vert_offsets[m + 1] <= vert_offsets[m] || q_offsets[m + 1] < q_offsets[m])
             return CP_ERROR_INVALID_VALUE;
         cls[m] = cp_size_class(nt);
-        members[cls[m]].push_back(m);
+        ++cls_meshes[cls[m]];
+        cls_queries[cls[m]] += q_offsets[m + 1] - q_offsets[m];
     }
+    std::vector<int> classes, qcls(64, 0);
+    for (int c = 0; c < 64; ++c)
+        if (cls_meshes[c]) {
+            classes.push_back(c);
+            const int64_t mean = cls_queries[c] / cls_meshes[c];
+            qcls[c] = cp_size_class(mean > 0 ? mean : 1);
+        }
+    // all classes in the cache: no timing
     std::vector<BatchEntry> cache = read_batch_cache(cache_path);
-    int best_leaf[64];
-    for (int c = 0; c < 64; ++c) best_leaf[c] = 0;
-    std::vector<BatchEntry> found;
-
-    cudaStream_t st;
-    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return CP_ERROR_CUDA;
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    cp_status result = CP_SUCCESS;
-    const int leaves[4] = {1, 2, 4, 8};
-    for (int c = 0; c < 64 && result == CP_SUCCESS; ++c) {
-        const std::vector<int32_t>& mem = members[c];
-        if (mem.empty()) continue;
-        // the class's meshes and queries, back to back
-        std::vector<int64_t> voff{0}, toff{0}, qoff{0};
-        for (int32_t m : mem) {
-            voff.push_back(voff.back() + vert_offsets[m + 1] - vert_offsets[m]);
-            toff.push_back(toff.back() + tri_offsets[m + 1] - tri_offsets[m]);
-            qoff.push_back(qoff.back() + q_offsets[m + 1] - q_offsets[m]);
-        }
-        const int64_t nq = qoff.back();
-        const int qcls = cp_size_class(nq / (int64_t)mem.size() > 0 ? nq / (int64_t)mem.size() : 1);
-        bool cached = false;
+    int leaf_of[64] = {0};
+    bool all_cached = true;
+    for (int c : classes) {
+        bool hit = false;
         for (const BatchEntry& e : cache)
-            if (e.cls == c && e.qcls == qcls && e.K == branching) {
-                best_leaf[c] = e.leaf;
-                found.push_back(e);
-                cached = true;
+            if (e.cls == c && e.qcls == qcls[c] && e.K == branching) {
+                leaf_of[c] = e.leaf;
+                hit = true;
                 break;
             }
-        if (cached) continue;
-        if (nq == 0) {  // nothing to time: the single-mesh default
-            best_leaf[c] = 4;
-            continue;
-        }
-        float* v = nullptr;
-        int32_t* t = nullptr;
-        float* q = nullptr;
+        all_cached = all_cached && hit;
+    }
+    if (!all_cached) {
+        // One build and one launch serve every class, so each choice is timed
+        // on the whole batch: first the best uniform leaf size, then one class
+        // at a time (most queries first) tries the other sizes, a change kept
+        // when the whole batch gets at least 2% faster.
+        cudaStream_t st;
+        if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) return CP_ERROR_CUDA;
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
         float* dist = nullptr;
-        void* ws = nullptr;
-        if (cudaMalloc(&v, sizeof(float) * 3 * voff.back()) != cudaSuccess ||
-            cudaMalloc(&t, sizeof(int32_t) * 3 * toff.back()) != cudaSuccess ||
-            cudaMalloc(&q, sizeof(float) * 3 * nq) != cudaSuccess ||
-            cudaMalloc(&dist, sizeof(float) * nq) != cudaSuccess) {
-            result = CP_ERROR_OUT_OF_MEMORY;
-        }
-        for (size_t k = 0; k < mem.size() && result == CP_SUCCESS; ++k) {
-            const int32_t m = mem[k];
-            if (cudaMemcpyAsync(v + 3 * voff[k], verts + 3 * vert_offsets[m],
-                                sizeof(float) * 3 * (voff[k + 1] - voff[k]), cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
-                cudaMemcpyAsync(t + 3 * toff[k], tris + 3 * tri_offsets[m],
-                                sizeof(int32_t) * 3 * (toff[k + 1] - toff[k]), cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
-                cudaMemcpyAsync(q + 3 * qoff[k], queries + 3 * q_offsets[m],
-                                sizeof(float) * 3 * (qoff[k + 1] - qoff[k]), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
-                result = CP_ERROR_CUDA;
-        }
-        BatchEntry best = {c, qcls, branching, 4, 1e30f};
+        cp_status result = cudaMalloc(&dist, sizeof(float) * (q_offsets[nmeshes] + 1)) == cudaSuccess
+                               ? CP_SUCCESS
+                               : CP_ERROR_OUT_OF_MEMORY;
+        const int sizes[4] = {1, 2, 4, 8};
+        std::vector<int32_t> leaves(nmeshes, 2);
+        float best_ms = 1e30f;
+        int uniform = 2;
         for (int li = 0; li < 4 && result == CP_SUCCESS; ++li) {
-            cp_build_opts bo;
-            cp_build_opts_default(&bo);
-            bo.branching = branching;
-            bo.leaf_size = leaves[li];
-            cp_batch* b = nullptr;
-            cp_status s = cp_batch_create(v, voff.data(), t, toff.data(), (int32_t)mem.size(), &bo, st, &b);
-            if (s != CP_SUCCESS) {
-                result = s;
-                break;
+            std::fill(leaves.begin(), leaves.end(), sizes[li]);
+            float ms = 0.0f;
+            result = time_batch(verts, vert_offsets, tris, tri_offsets, nmeshes, queries, q_offsets, branching, leaves,
+                                dist, st, e0, e1, &ms);
+            if (result == CP_SUCCESS && ms < best_ms) {
+                best_ms = ms;
+                uniform = sizes[li];
             }
-            cp_query_opts qo;
-            cp_query_opts_default(&qo);
-            size_t wsb = 0;
-            cp_batch_query_workspace_size(b, nq, &qo, &wsb);
-            if (ws) cudaFree(ws);
-            ws = nullptr;
-            if (cudaMalloc(&ws, wsb) != cudaSuccess) {
-                cp_batch_destroy(b);
-                result = CP_ERROR_OUT_OF_MEMORY;
-                break;
-            }
-            float ms = 1e30f;
-            for (int rep = 0; rep < 3 && s == CP_SUCCESS; ++rep) {
-                cudaEventRecord(e0, st);
-                s = cp_batch_query(b, q, qoff.data(), &qo, nullptr, dist, nullptr, nullptr, ws, wsb, 0, st);
-                cudaEventRecord(e1, st);
-                cudaEventSynchronize(e1);
-                float tms = 0.0f;
-                cudaEventElapsedTime(&tms, e0, e1);
-                if (rep > 0 && tms < ms) ms = tms;  // the first run warms caches
-            }
-            cp_batch_destroy(b);
-            if (s != CP_SUCCESS) {
-                result = s;
-                break;
-            }
-            if (ms < best.ms) best = {c, qcls, branching, leaves[li], ms};
         }
-        cudaFree(ws);
-        cudaFree(v);
-        cudaFree(t);
-        cudaFree(q);
+        for (int c : classes) leaf_of[c] = uniform;
+        std::vector<int> order = classes;
+        std::sort(order.begin(), order.end(), [&](int a, int b) { return cls_queries[a] > cls_queries[b]; });
+        for (int c : order) {
+            for (int li = 0; li < 4 && result == CP_SUCCESS; ++li) {
+                if (sizes[li] == leaf_of[c]) continue;
+                for (int32_t m = 0; m < nmeshes; ++m) leaves[m] = cls[m] == c ? sizes[li] : leaf_of[cls[m]];
+                float ms = 0.0f;
+                result = time_batch(verts, vert_offsets, tris, tri_offsets, nmeshes, queries, q_offsets, branching,
+                                    leaves, dist, st, e0, e1, &ms);
+                if (result == CP_SUCCESS && ms < 0.98f * best_ms) {
+                    best_ms = ms;
+                    leaf_of[c] = sizes[li];
+                }
+            }
+        }
         cudaFree(dist);
-        if (result == CP_SUCCESS) {
-            best_leaf[c] = best.leaf;
-            found.push_back(best);
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaStreamDestroy(st);
+        if (result != CP_SUCCESS) return result;
+        if (cache_path) {
+            std::vector<BatchEntry> out;
+            for (const BatchEntry& e : cache) {
+                bool replaced = false;
+                for (int c : classes)
+                    if (e.cls == c && e.qcls == qcls[c] && e.K == branching) replaced = true;
+                if (!replaced) out.push_back(e);
+            }
+            for (int c : classes) out.push_back({c, qcls[c], branching, leaf_of[c], best_ms});
+            write_batch_cache(cache_path, out);
         }
     }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    cudaStreamDestroy(st);
-    if (result != CP_SUCCESS) return result;
-    for (int32_t m = 0; m < nmeshes; ++m) leaf_sizes[m] = best_leaf[cls[m]];
-    if (cache_path) {
-        std::vector<BatchEntry> out;
-        for (const BatchEntry& e : cache) {
-            bool replaced = false;
-            for (const BatchEntry& f : found)
-                if (f.cls == e.cls && f.qcls == e.qcls && f.K == e.K) replaced = true;
-            if (!replaced) out.push_back(e);
-        }
-        for (const BatchEntry& f : found) out.push_back(f);
-        write_batch_cache(cache_path, out);
-    }
+    for (int32_t m = 0; m < nmeshes; ++m) leaf_sizes[m] = leaf_of[cls[m]];
     return CP_SUCCESS;
 }

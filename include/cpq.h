@@ -625,14 +625,16 @@ CP_API cp_status cp_autotune(const float* verts, int64_t nv, const int32_t* tris
                              cp_build_opts* best_build, cp_query_opts* best_query);
 
 /* The batched form tuned per size class: meshes are grouped by
- * cp_size_class(triangles); for each class the class's own meshes and queries
- * (DEVICE arrays as for cp_batch_create and cp_batch_query; offsets HOST) are
- * built as a batch and queried at leaf sizes 1, 2, 4 and 8, and the fastest
- * is that class's leaf size.  Writes leaf_sizes (HOST, nmeshes) for
- * cp_batch_create_leaves, and the query options (the packet traversal's
- * defaults).  With cache_path, results are read from and written to the
- * autotuner's cache file (lines marked B, keyed by triangle class, the class's
- * mean queries per mesh and branching).  Synchronous. */
+ * cp_size_class(triangles), and each class gets a leaf size in {1, 2, 4, 8}.
+ * One build and one launch serve every class, so each choice is timed on the
+ * whole batch (DEVICE arrays as for cp_batch_create and cp_batch_query;
+ * offsets HOST): first the best uniform size, then one class at a time, most
+ * queries first, tries the others, a change kept when the batch gets at least
+ * 2% faster.  Writes leaf_sizes (HOST, nmeshes) for cp_batch_create_leaves,
+ * and the query options (the packet traversal's defaults).  With cache_path,
+ * results are read from and written to the autotuner's cache file (lines
+ * marked B, keyed by triangle class, the class's mean queries per mesh and
+ * branching); a batch whose classes are all there is not timed.  Synchronous. */
 CP_API cp_status cp_batch_autotune(const float* verts, const int64_t* vert_offsets, const int32_t* tris,
                                    const int64_t* tri_offsets, int32_t nmeshes, const float* queries,
                                    const int64_t* q_offsets, int32_t branching, const char* cache_path,
