@@ -56,6 +56,14 @@ constexpr int kSeedPoints = CPQ_SEED_POINTS;
 #ifndef CPQ_TAIL_PACKETS
 #define CPQ_TAIL_PACKETS 4
 #endif
+// A warp claims a chunk only while its packets are cheap (at most this many
+// node visits): seeds pay on coherent packets, and a chunk spreads the
+// packets in flight over more of the curve, which costs expensive packets
+// (large working sets) more than their seeds save.
+#ifndef CPQ_CHUNK_VISITS
+#define CPQ_CHUNK_VISITS 128
+#endif
+constexpr uint32_t kChunkVisits = CPQ_CHUNK_VISITS;
 constexpr unsigned long long kTailPackets = CPQ_TAIL_PACKETS;
 static_assert(kSeedPoints == 1 || kSeedPoints == 2 || kSeedPoints == 4 || kSeedPoints == 8 ||
                   kSeedPoints == 16 || kSeedPoints == 32, "seed points: a power of two up to 32");
@@ -205,6 +213,47 @@ __device__ __forceinline__ void load_row2(const float* __restrict__ p, f32x2 (&r
             r[j] = v.x;
             r[j + 1] = v.y;
         }
+    }
+}
+
+// Node rows with an L2 evict-last policy: the wide nodes (128 B each, tens of
+// MB for millions of triangles) are re-read by every packet in their region,
+// while triangle records and query data stream through, so they are asked to
+// stay in L2 longer.
+#ifndef CPQ_NODE_KEEP
+#define CPQ_NODE_KEEP 0
+#endif
+__device__ __forceinline__ uint64_t l2_keep_policy() {
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+template <int K>
+__device__ __forceinline__ void load_row2_keep(const float* __restrict__ p, f32x2 (&r)[K / 2], uint64_t pol) {
+    if constexpr (K == 2) {
+        unsigned long long v;
+        asm("ld.global.nc.L2::cache_hint.u64 %0, [%1], %2;" : "=l"(v) : "l"(p), "l"(pol));
+        r[0] = v;
+    } else {
+#pragma unroll
+        for (int j = 0; j < K / 2; j += 2) {
+            unsigned long long x, y;
+            asm("ld.global.nc.L2::cache_hint.v2.u64 {%0, %1}, [%2], %3;"
+                : "=l"(x), "=l"(y) : "l"(p + 2 * j), "l"(pol));
+            r[j] = x;
+            r[j + 1] = y;
+        }
+    }
+}
+template <int K>
+__device__ __forceinline__ void load_row_i_keep(const int32_t* __restrict__ p, int32_t (&r)[K], uint64_t pol) {
+    if constexpr (K == 2) {
+        asm("ld.global.nc.L2::cache_hint.v2.s32 {%0, %1}, [%2], %3;" : "=r"(r[0]), "=r"(r[1]) : "l"(p), "l"(pol));
+    } else {
+#pragma unroll
+        for (int j = 0; j < K; j += 4)
+            asm("ld.global.nc.L2::cache_hint.v4.s32 {%0, %1, %2, %3}, [%4], %5;"
+                : "=r"(r[j]), "=r"(r[j + 1]), "=r"(r[j + 2]), "=r"(r[j + 3]) : "l"(p + j), "l"(pol));
     }
 }
 
@@ -537,6 +586,24 @@ __global__ void __launch_bounds__(256) k_traverse(TraverseArgs a) {
     }
 }
 
+// Streaming (evict-first) access for data a traversal touches once: the
+// queries gathered through the ordering and the results scattered back.  The
+// hint keeps them from displacing the tree's nodes and triangle records,
+// which neighbouring packets re-read, from L2.
+#ifndef CPQ_STREAM_IO
+#define CPQ_STREAM_IO 1
+#endif
+template <typename T>
+__device__ __forceinline__ T ld_stream(const T* p) {
+    if constexpr (CPQ_STREAM_IO) return __ldcs(p);
+    else return *p;
+}
+template <typename T>
+__device__ __forceinline__ void st_stream(T* p, T v) {
+    if constexpr (CPQ_STREAM_IO) __stcs(p, v);
+    else *p = v;
+}
+
 // The winner's float-float re-evaluation and the outputs; the closest point
 // (NaN when nothing was found) is also returned in (px, py, pz).
 __device__ __forceinline__ void write_result(const TraverseArgs& a, int64_t qi, float qx, float qy,
@@ -556,16 +623,18 @@ __device__ __forceinline__ void write_result(const TraverseArgs& a, int64_t qi, 
     } else {
         atomicOr(a.status, 4u);
     }
-    if (a.out_dist) a.out_dist[qi] = dist;
-    if (a.out_tri) a.out_tri[qi] = best_rec >= 0 ? best_idx : -1;
+    // results land in the caller's (random) query order and are written once:
+    // evict-first stores, so they do not push the tree out of L2
+    if (a.out_dist) st_stream(a.out_dist + qi, dist);
+    if (a.out_tri) st_stream(a.out_tri + qi, best_rec >= 0 ? best_idx : -1);
     if (a.out_point) {
-        a.out_point[3 * qi] = px;
-        a.out_point[3 * qi + 1] = py;
-        a.out_point[3 * qi + 2] = pz;
+        st_stream(a.out_point + 3 * qi, px);
+        st_stream(a.out_point + 3 * qi + 1, py);
+        st_stream(a.out_point + 3 * qi + 2, pz);
     }
     if (a.out_bary) {
-        a.out_bary[2 * qi] = bv;
-        a.out_bary[2 * qi + 1] = bw;
+        st_stream(a.out_bary + 2 * qi, bv);
+        st_stream(a.out_bary + 2 * qi + 1, bw);
     }
 }
 
@@ -609,7 +678,7 @@ __device__ __forceinline__ void store_row(T* dst, const T (&v)[K]) {
 // list, count) of entries below the top [entry]; rounded to 16 bytes), then
 // the leaf-compaction slots (32 query points) when the kernel compacts, then
 // the previous packet's kSeedPoints closest points (x, y, z, mesh), then the
-// warp's chunk cursor (next packet, chunk end).
+// warp's chunk cursor (next packet, chunk end, the last packet's node visits).
 __host__ __device__ constexpr size_t packet_stack_bytes(int K, int cap) {
     return ((size_t)cap * (128 * K + 4 * K + 8) + 15) & ~size_t(15);
 }
@@ -691,18 +760,22 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                        n_lane_nodes = 0;
 
     // Work: packets of 32 consecutive ordered queries.  Up to `split` they are
-    // claimed kSeedChunk at a time from counter[0]; the last kTailPackets per
-    // warp one at a time from counter[1], so that the warps finish together.
+    // claimed from counter[0], kSeedChunk at a time while the warp's last
+    // packet was cheap (at most kChunkVisits node visits), else one at a
+    // time; the last kTailPackets per warp one at a time from counter[1], so
+    // that the warps finish together.
     // The warp's position in its chunk lives in shared memory (lane 0 reads
     // and advances it between packets), so no register holds it across the
     // traversal.
     const uint32_t npk = (uint32_t)(((unsigned long long)a.nq + 31) / 32);
     const uint32_t tail = gridDim.x * (blockDim.x >> 5) * kTailPackets;
     const uint32_t split = npk > tail ? (npk - tail) / kSeedChunk * kSeedChunk : 0u;
-    uint32_t* st_work = reinterpret_cast<uint32_t*>(st_seed + kSeedPoints);  // next packet, chunk end
+    // next packet, chunk end, node visits of the last packet
+    uint32_t* st_work = reinterpret_cast<uint32_t*>(st_seed + kSeedPoints);
     if (lane0) {
         st_work[0] = 0;
         st_work[1] = 0;
+        st_work[2] = 0;
     }
     for (;;) {
         uint32_t pk = 0, seeded = 0;
@@ -711,9 +784,10 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
             if (pk < st_work[1]) {
                 seeded = 1;  // the next packet of this warp's chunk
             } else {
-                pk = (uint32_t)(atomicAdd(a.counter, (unsigned long long)kSeedChunk));
+                const uint32_t chunk = st_work[2] <= kChunkVisits ? (uint32_t)kSeedChunk : 1u;
+                pk = (uint32_t)(atomicAdd(a.counter, (unsigned long long)chunk));
                 if (pk < split) {
-                    st_work[1] = min(pk + (uint32_t)kSeedChunk, split);
+                    st_work[1] = min(pk + chunk, split);
                 } else {
                     pk = split + (uint32_t)atomicAdd(a.counter + 1, 1ull);
                     st_work[1] = 0;
@@ -730,10 +804,10 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
         float qx = 0.f, qy = 0.f, qz = 0.f;
         int m = 0;
         if (valid) {
-            qi = a.perm ? (int64_t)a.perm[i] : i;
-            qx = a.queries[3 * qi];
-            qy = a.queries[3 * qi + 1];
-            qz = a.queries[3 * qi + 2];
+            qi = a.perm ? (int64_t)ld_stream(a.perm + i) : i;
+            qx = ld_stream(a.queries + 3 * qi);
+            qy = ld_stream(a.queries + 3 * qi + 1);
+            qz = ld_stream(a.queries + 3 * qi + 2);
             m = a.nmeshes > 1 ? mesh_of(a.qoff, a.nmeshes, qi) : 0;
         }
         // Seed: after a chunk's first packet each lane starts from its least
@@ -770,6 +844,7 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
         const f32x2 qx2 = f2_pack(qx, qx), qy2 = f2_pack(qy, qy), qz2 = f2_pack(qz, qz);
         unsigned pending = __ballot_sync(kFull, valid);
         bool retried = false;
+        uint32_t visits = 0;  // warp-uniform: this packet's node visits
         while (pending) {
             const int leader = __ffs(pending) - 1;
             const int mesh = __shfl_sync(kFull, m, leader);
@@ -790,16 +865,28 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                         ++n_nodes;
                         n_lane_nodes += __popc(__ballot_sync(kFull, leaf_active));
                     }
+                    ++visits;
                     const WideNode<K>* nd = nodes + cur;
                     f32x2 lox[K / 2], hix[K / 2], loy[K / 2], hiy[K / 2], loz[K / 2], hiz[K / 2];
                     int32_t ch[K];
-                    load_row2<K>(nd->lox, lox);
-                    load_row2<K>(nd->hix, hix);
-                    load_row2<K>(nd->loy, loy);
-                    load_row2<K>(nd->hiy, hiy);
-                    load_row2<K>(nd->loz, loz);
-                    load_row2<K>(nd->hiz, hiz);
-                    load_row_i<K>(nd->child, ch);
+                    if constexpr (CPQ_NODE_KEEP) {
+                        const uint64_t pol = l2_keep_policy();
+                        load_row2_keep<K>(nd->lox, lox, pol);
+                        load_row2_keep<K>(nd->hix, hix, pol);
+                        load_row2_keep<K>(nd->loy, loy, pol);
+                        load_row2_keep<K>(nd->hiy, hiy, pol);
+                        load_row2_keep<K>(nd->loz, loz, pol);
+                        load_row2_keep<K>(nd->hiz, hiz, pol);
+                        load_row_i_keep<K>(nd->child, ch, pol);
+                    } else {
+                        load_row2<K>(nd->lox, lox);
+                        load_row2<K>(nd->hix, hix);
+                        load_row2<K>(nd->loy, loy);
+                        load_row2<K>(nd->hiy, hiy);
+                        load_row2<K>(nd->loz, loz);
+                        load_row2<K>(nd->hiz, hiz);
+                        load_row_i<K>(nd->child, ch);
+                    }
                     // box lower bounds, two children per packed operation
                     float lb[K];
 #pragma unroll
@@ -943,6 +1030,7 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
             const int rec = best == kNoKey ? -1 : a.inv_order[a.toff[m] + idx];
             write_result(a, qi, qx, qy, qz, rec, idx, px, py, pz);
         }
+        if (lane0) st_work[2] = visits;
         // this packet's closest points seed the next one
         constexpr int kStride = 32 / kSeedPoints;
         if (lane % kStride == 0) st_seed[lane / kStride] = make_float4(px, py, pz, __int_as_float(valid ? m : -1));
