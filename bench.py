@@ -100,10 +100,14 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=1 << 21,
                     help="queries timed on the host cores for the CPU baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--width", type=int, default=1920, help="shade workload: image width")
+    ap.add_argument("--height", type=int, default=1440, help="shade workload: image height")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the torus, batched and dynamic forms in the headline run")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--leaf", type=int, default=0)
+    ap.add_argument("--seed-chunk", type=int, default=1,
+                    help="packets per claim of the seeded packet traversal without the autotuner (1: unseeded)")
     ap.add_argument("--workload", default="large",
                     choices=["large", "torus", "batched", "dynamic", "small", "rays", "scene", "camera",
                              "shade"],
@@ -338,7 +342,7 @@ def our_arm(args):
 
     # 4-wide BVH; leaf size, block size and traversal kernel autotuned on the
     # workload's own query set (warp coherence depends on the query density)
-    leaf, qopts = 4, cpq.query_opts()
+    leaf, qopts = 4, cpq.query_opts(seed_chunk=args.seed_chunk)
     tuned = None
     if args.leaf:
         leaf = args.leaf
@@ -347,7 +351,7 @@ def our_arm(args):
         leaf, qopts = bo.leaf_size, qo
         tuned = {"leaf_size": bo.leaf_size, "block_size": qo.block_size,
                  "traversal": ["auto", "thread", "packet"][qo.traversal],
-                 "short_stack": qo.short_stack}
+                 "short_stack": qo.short_stack, "seed_chunk": qo.seed_chunk}
     mesh = cpq.Mesh(vd, td_, branching=4, leaf_size=leaf)
     info = mesh.info()
     ws = torch.empty(mesh.workspace_size(nq, qopts), dtype=torch.uint8, device=dev)
@@ -453,6 +457,7 @@ def our_arm(args):
                "config": bench_config(world),
                "build": {"branching": 4, "leaf_size": leaf, "autotuned": tuned,
                          "block_size": qopts.block_size, "short_stack": qopts.short_stack,
+                         "seed_chunk": qopts.seed_chunk,
                          "sort_queries": bool(qopts.sort_queries),
                          "wide_nodes": info.num_wide_nodes, "build_ms": info.build_ms,
                          "build_roofline": {"bytes_per_triangle": BUILD_BYTES_PER_TRI,
@@ -685,7 +690,8 @@ def dynamic_form(steps: int, warmup: int) -> dict:
     mesh = cpq.Mesh(vd, td, branching=4, leaf_size=2)
     torch.cuda.synchronize()
     build_ms = (time.perf_counter() - t0) * 1e3
-    o = cpq.query_opts()
+    # seeded packets (4 per claim): 212 against 247 ms per iteration unseeded
+    o = cpq.query_opts(seed_chunk=4)
     wsf = torch.empty(mesh.workspace_size(qfix.shape[0], o), dtype=torch.uint8, device=dev)
     wsp = torch.empty(mesh.workspace_size(pts.shape[0], o), dtype=torch.uint8, device=dev)
     outf = mesh.query(qfix, want_point=False, workspace=wsf, opts=o)
@@ -735,7 +741,7 @@ def dynamic_form(steps: int, warmup: int) -> dict:
                  {"workload": "4,096 Gaussian clusters x 2,048 tris (8,388,608-tri soup), vertices "
                               "perturbed N(0,1e-4) per iteration, 67,108,864 fixed + 1,048,576 moving "
                               "queries, 50 iterations of refit + forward + adjoint + step",
-                  "branching": 4, "leaf_size": 2, "iterations": iters, "graph": True},
+                  "branching": 4, "leaf_size": 2, "iterations": iters, "graph": True, "seed_chunk": 4},
                  {"build_ms": build_ms, "rebuild_ms": rebuild_ms, "final_mean_dist":
                   float(outp.dist.mean())})
 
@@ -956,7 +962,7 @@ def shade_arm(args):
     scene = G.ShadeScene(td["verts"], td["normals"], td["obj"], td["albedo"], td["emissive"], td["metal_rough"])
     from gpurt_cpq import workloads as W
 
-    w, h, spp = 1920, 1440, 8
+    w, h, spp = args.width, args.height, 8
     target = (W.CBOX_EYE[0], W.CBOX_EYE[1], 0.0)
     cam = G.camera(W.CBOX_EYE, target, (0, 1, 0), W.CBOX_YFOV, w, h)
     img = torch.zeros((h, w, 3), dtype=torch.float32, device=dev)
@@ -989,7 +995,7 @@ def shade_arm(args):
              "gpu_launches_per_frame": int(launches), "mean_radiance": mean}
     if cpu is not None:
         extra["cpu_baseline"] = cpu
-    _line("path-traced samples/s (the reference's Cornell box, 1920x1440, MIS, 8 spp, depth 8)",
+    _line(f"path-traced samples/s (the reference's Cornell box, {w}x{h}, MIS, 8 spp, depth 8)",
           w * h * spp / (ms * 1e-3), "samples/s", ms, args,
           {"workload": f"media/cbox/cbox.gltf (fixture: {sa['verts'].shape[0]:,} world-space tris, 10 objects, "
                        f"1 light) from its camera, {w}x{h}, {spp} samples per pixel, max depth 8, Russian "

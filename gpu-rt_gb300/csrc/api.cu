@@ -217,11 +217,14 @@ cp_status to_query_params(const cp_query_opts* o, QueryParams* q) {
         return fail(CP_ERROR_INVALID_VALUE, "blocks_per_sm must be in 0..64");
     if (o->traversal < CP_TRAVERSAL_AUTO || o->traversal > CP_TRAVERSAL_PACKET)
         return fail(CP_ERROR_INVALID_VALUE, "traversal must be CP_TRAVERSAL_AUTO, _THREAD or _PACKET");
+    if (o->seed_chunk < 0 || o->seed_chunk > 16)
+        return fail(CP_ERROR_INVALID_VALUE, "seed_chunk must be in 0..16");
     q->block = block;
     q->sort = o->sort_queries ? 1 : 0;
     q->blocks_per_sm = o->blocks_per_sm;
     q->short_stack = ss;
     q->traversal = o->traversal;
+    q->seed_chunk = o->seed_chunk ? o->seed_chunk : 1;
     return CP_SUCCESS;
 }
 
@@ -290,6 +293,7 @@ CP_API void cp_query_opts_default(cp_query_opts* o) {
     o->blocks_per_sm = 0;
     o->short_stack = 8;
     o->traversal = CP_TRAVERSAL_AUTO;
+    o->seed_chunk = 1;
 }
 
 CP_API const char* cp_last_error_string(void) { return g_last_error.c_str(); }

@@ -3,9 +3,10 @@
 // The reference has no tuner; its only knobs are UI sliders that feed push
 // constants (src/gpurt.cpp:283-322, src/vk/rt.h:85-102).  Results are cached
 // in a plain text file, one line per (triangle class, query class, branching):
-//   <tri_class> <query_class> <branching> <leaf_size> <block_size> <short_stack> <ms>
-// where a class is floor(log2(count)) and short_stack 0 stands for the
-// warp-packet traversal; batches (cp_batch_autotune) add lines of their own,
+//   <tri_class> <query_class> <branching> <leaf_size> <block_size> <short_stack> <ms> <seed_chunk>
+// where a class is floor(log2(count)), short_stack 0 stands for the
+// warp-packet traversal and seed_chunk is its packets per claim (1: unseeded;
+// a line without the column reads as 1); batches (cp_batch_autotune) add lines of their own,
 // marked B, with a leaf size per triangle class.
 #include <cuda_runtime.h>
 
@@ -24,6 +25,7 @@ namespace {
 struct Entry {
     int cls, qcls, K, leaf, block, stack;
     float ms;
+    int seed = 1;  // packet traversal's seed chunk (lines without the column: 1)
 };
 
 std::vector<Entry> read_cache(const char* path) {
@@ -34,7 +36,11 @@ std::vector<Entry> read_cache(const char* path) {
     while (std::getline(f, line)) {
         std::istringstream is(line);
         Entry e;
-        if (is >> e.cls >> e.qcls >> e.K >> e.leaf >> e.block >> e.stack >> e.ms) out.push_back(e);
+        if (is >> e.cls >> e.qcls >> e.K >> e.leaf >> e.block >> e.stack >> e.ms) {
+            int seed = 1;
+            if (is >> seed && seed >= 1 && seed <= 16) e.seed = seed;
+            out.push_back(e);
+        }
     }
     return out;
 }
@@ -52,7 +58,7 @@ void write_cache(const char* path, const std::vector<Entry>& es) {
     for (const std::string& l : batch_lines) f << l << '\n';
     for (const Entry& e : es)
         f << e.cls << ' ' << e.qcls << ' ' << e.K << ' ' << e.leaf << ' ' << e.block << ' ' << e.stack
-          << ' ' << e.ms << '\n';
+          << ' ' << e.ms << ' ' << e.seed << '\n';
 }
 
 }  // namespace
@@ -80,6 +86,7 @@ extern "C" CP_API cp_status cp_autotune(const float* verts, int64_t nv, const in
             best_query->block_size = e.block;
             best_query->short_stack = e.stack ? e.stack : 8;
             best_query->traversal = e.stack ? CP_TRAVERSAL_THREAD : CP_TRAVERSAL_PACKET;
+            best_query->seed_chunk = e.stack ? 1 : e.seed;
             return CP_SUCCESS;
         }
 
@@ -113,14 +120,16 @@ extern "C" CP_API cp_status cp_autotune(const float* verts, int64_t nv, const in
                 break;
             }
             for (int bi = 0; bi < 2; ++bi)
-                for (int si = 0; si < 4; ++si) {
+                for (int si = 0; si < 5; ++si) {
                     // stacks[0..2]: per-thread traversal with that short stack;
-                    // si == 3: warp-packet traversal
+                    // si == 3: warp-packet traversal; si == 4: packets seeded
+                    // from the packet before (chunks of 4)
                     cp_query_opts qo;
                     cp_query_opts_default(&qo);
                     qo.block_size = blocks[bi];
                     qo.short_stack = si < 3 ? stacks[si] : 8;
                     qo.traversal = si < 3 ? CP_TRAVERSAL_THREAD : CP_TRAVERSAL_PACKET;
+                    qo.seed_chunk = si == 4 ? 4 : 1;
                     size_t wsb = 0;
                     cp_query_workspace_size(mesh, nq, &qo, &wsb);
                     void* ws = nullptr;
@@ -144,7 +153,8 @@ extern "C" CP_API cp_status cp_autotune(const float* verts, int64_t nv, const in
                         break;
                     }
                     if (ms < best.ms)
-                        best = {cls, qcls, Ks[ki], leaves[li], blocks[bi], si < 3 ? stacks[si] : 0, ms};
+                        best = {cls, qcls, Ks[ki], leaves[li], blocks[bi], si < 3 ? stacks[si] : 0, ms,
+                                si == 4 ? 4 : 1};
                 }
             cp_mesh_destroy(mesh);
         }
@@ -159,6 +169,7 @@ extern "C" CP_API cp_status cp_autotune(const float* verts, int64_t nv, const in
     best_query->block_size = best.block;
     best_query->short_stack = best.stack ? best.stack : 8;
     best_query->traversal = best.stack ? CP_TRAVERSAL_THREAD : CP_TRAVERSAL_PACKET;
+    best_query->seed_chunk = best.stack ? 1 : best.seed;
     if (cache_path) {
         std::vector<Entry> out;
         for (const Entry& e : cache)

@@ -89,6 +89,7 @@ struct QueryParams {
     int blocks_per_sm = 0;
     int short_stack = 8;
     int traversal = 0;  // 0 auto (packet when sorted), 1 per-thread, 2 warp packet
+    int seed_chunk = 1; // packet traversal: packets per claim, seeded after the first (1: no seeding)
     bool no_timing = false;  // never create timing events, even when cp_timing_enable is on
 };
 

@@ -41,29 +41,17 @@ namespace {
 
 constexpr int kStackTotal = 256;   // >= (K-1)(depth+1) for any 64+32-bit-key LBVH
 
-// Packet traversal work claims: kSeedChunk consecutive packets per claim (each
-// packet after a chunk's first seeds its limits from the packet before it,
-// from kSeedPoints of its closest points), then kTailPackets single packets
-// per warp at the end.
-#ifndef CPQ_SEED_CHUNK
-#define CPQ_SEED_CHUNK 4
-#endif
+// Packet traversal work claims: `seed_chunk` (a query option) consecutive
+// packets per claim, each packet after a chunk's first seeding its limits from
+// kSeedPoints closest points of the packet before it, then kTailPackets single
+// packets per warp at the end.
 #ifndef CPQ_SEED_POINTS
 #define CPQ_SEED_POINTS 16
 #endif
-constexpr unsigned long long kSeedChunk = CPQ_SEED_CHUNK;
 constexpr int kSeedPoints = CPQ_SEED_POINTS;
 #ifndef CPQ_TAIL_PACKETS
 #define CPQ_TAIL_PACKETS 4
 #endif
-// A warp claims a chunk only while its packets are cheap (at most this many
-// node visits): seeds pay on coherent packets, and a chunk spreads the
-// packets in flight over more of the curve, which costs expensive packets
-// (large working sets) more than their seeds save.
-#ifndef CPQ_CHUNK_VISITS
-#define CPQ_CHUNK_VISITS 128
-#endif
-constexpr uint32_t kChunkVisits = CPQ_CHUNK_VISITS;
 constexpr unsigned long long kTailPackets = CPQ_TAIL_PACKETS;
 static_assert(kSeedPoints == 1 || kSeedPoints == 2 || kSeedPoints == 4 || kSeedPoints == 8 ||
                   kSeedPoints == 16 || kSeedPoints == 32, "seed points: a power of two up to 32");
@@ -213,47 +201,6 @@ __device__ __forceinline__ void load_row2(const float* __restrict__ p, f32x2 (&r
             r[j] = v.x;
             r[j + 1] = v.y;
         }
-    }
-}
-
-// Node rows with an L2 evict-last policy: the wide nodes (128 B each, tens of
-// MB for millions of triangles) are re-read by every packet in their region,
-// while triangle records and query data stream through, so they are asked to
-// stay in L2 longer.
-#ifndef CPQ_NODE_KEEP
-#define CPQ_NODE_KEEP 0
-#endif
-__device__ __forceinline__ uint64_t l2_keep_policy() {
-    uint64_t pol;
-    asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
-    return pol;
-}
-template <int K>
-__device__ __forceinline__ void load_row2_keep(const float* __restrict__ p, f32x2 (&r)[K / 2], uint64_t pol) {
-    if constexpr (K == 2) {
-        unsigned long long v;
-        asm("ld.global.nc.L2::cache_hint.u64 %0, [%1], %2;" : "=l"(v) : "l"(p), "l"(pol));
-        r[0] = v;
-    } else {
-#pragma unroll
-        for (int j = 0; j < K / 2; j += 2) {
-            unsigned long long x, y;
-            asm("ld.global.nc.L2::cache_hint.v2.u64 {%0, %1}, [%2], %3;"
-                : "=l"(x), "=l"(y) : "l"(p + 2 * j), "l"(pol));
-            r[j] = x;
-            r[j + 1] = y;
-        }
-    }
-}
-template <int K>
-__device__ __forceinline__ void load_row_i_keep(const int32_t* __restrict__ p, int32_t (&r)[K], uint64_t pol) {
-    if constexpr (K == 2) {
-        asm("ld.global.nc.L2::cache_hint.v2.s32 {%0, %1}, [%2], %3;" : "=r"(r[0]), "=r"(r[1]) : "l"(p), "l"(pol));
-    } else {
-#pragma unroll
-        for (int j = 0; j < K; j += 4)
-            asm("ld.global.nc.L2::cache_hint.v4.s32 {%0, %1, %2, %3}, [%4], %5;"
-                : "=r"(r[j]), "=r"(r[j + 1]), "=r"(r[j + 2]), "=r"(r[j + 3]) : "l"(p + j), "l"(pol));
     }
 }
 
@@ -468,6 +415,7 @@ struct TraverseArgs {
     unsigned long long* stats;  // optional: node visits, leaf triangle tests, pops, skipped pops
     const float* box;           // binary node boxes (lo xyz, hi xyz); a mesh's box at its root
     const int32_t* mesh_root;   // per mesh: its binary root
+    int seed_chunk;             // packet kernel: packets per claim (1: no seeding)
 };
 
 template <int K, int S>
@@ -678,7 +626,7 @@ __device__ __forceinline__ void store_row(T* dst, const T (&v)[K]) {
 // list, count) of entries below the top [entry]; rounded to 16 bytes), then
 // the leaf-compaction slots (32 query points) when the kernel compacts, then
 // the previous packet's kSeedPoints closest points (x, y, z, mesh), then the
-// warp's chunk cursor (next packet, chunk end, the last packet's node visits).
+// warp's chunk cursor (next packet, chunk end).
 __host__ __device__ constexpr size_t packet_stack_bytes(int K, int cap) {
     return ((size_t)cap * (128 * K + 4 * K + 8) + 15) & ~size_t(15);
 }
@@ -734,10 +682,13 @@ __constant__ LeafSplits c_leaf_splits = make_leaf_splits();
 // and a push reuses it, so the stack holds one entry per wide level at most;
 // `cap` (max wide depth + 1) is that bound, so it cannot overflow.  Lanes of
 // different meshes in one packet (batches) are served one mesh at a time.
-// A warp claims kSeedChunk consecutive packets at once; each packet after the
-// first starts every lane's limit at a padded upper bound from the previous
-// packet's closest points (its neighbours along the curve), so the first
-// leaves a packet reaches are not tested against an infinite limit.
+// With seed_chunk > 1 a warp claims that many consecutive packets at once;
+// each packet after the first starts every lane's limit at a padded upper
+// bound from the previous packet's closest points (its neighbours along the
+// curve), so the first leaves a packet reaches are not tested against an
+// infinite limit.  Chunks spread the packets in flight over more of the
+// curve, which costs cache locality; on coherent queries (points near a
+// surface) the seeds save more than that, on scattered ones less.
 // kCompact (trees whose leaves hold 3 or more triangles) spreads a leaf's
 // (query, triangle) pairs over the warp when few lanes need the leaf; it
 // costs 512 bytes of shared memory per warp, which with 2-triangle leaves
@@ -760,22 +711,19 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                        n_lane_nodes = 0;
 
     // Work: packets of 32 consecutive ordered queries.  Up to `split` they are
-    // claimed from counter[0], kSeedChunk at a time while the warp's last
-    // packet was cheap (at most kChunkVisits node visits), else one at a
-    // time; the last kTailPackets per warp one at a time from counter[1], so
-    // that the warps finish together.
+    // claimed `seed_chunk` at a time from counter[0]; the last kTailPackets per
+    // warp one at a time from counter[1], so that the warps finish together.
     // The warp's position in its chunk lives in shared memory (lane 0 reads
     // and advances it between packets), so no register holds it across the
     // traversal.
     const uint32_t npk = (uint32_t)(((unsigned long long)a.nq + 31) / 32);
     const uint32_t tail = gridDim.x * (blockDim.x >> 5) * kTailPackets;
-    const uint32_t split = npk > tail ? (npk - tail) / kSeedChunk * kSeedChunk : 0u;
-    // next packet, chunk end, node visits of the last packet
-    uint32_t* st_work = reinterpret_cast<uint32_t*>(st_seed + kSeedPoints);
+    const uint32_t chunk = (uint32_t)a.seed_chunk;
+    const uint32_t split = npk > tail ? (npk - tail) / chunk * chunk : 0u;
+    uint32_t* st_work = reinterpret_cast<uint32_t*>(st_seed + kSeedPoints);  // next packet, chunk end
     if (lane0) {
         st_work[0] = 0;
         st_work[1] = 0;
-        st_work[2] = 0;
     }
     for (;;) {
         uint32_t pk = 0, seeded = 0;
@@ -784,7 +732,6 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
             if (pk < st_work[1]) {
                 seeded = 1;  // the next packet of this warp's chunk
             } else {
-                const uint32_t chunk = st_work[2] <= kChunkVisits ? (uint32_t)kSeedChunk : 1u;
                 pk = (uint32_t)(atomicAdd(a.counter, (unsigned long long)chunk));
                 if (pk < split) {
                     st_work[1] = min(pk + chunk, split);
@@ -844,7 +791,6 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
         const f32x2 qx2 = f2_pack(qx, qx), qy2 = f2_pack(qy, qy), qz2 = f2_pack(qz, qz);
         unsigned pending = __ballot_sync(kFull, valid);
         bool retried = false;
-        uint32_t visits = 0;  // warp-uniform: this packet's node visits
         while (pending) {
             const int leader = __ffs(pending) - 1;
             const int mesh = __shfl_sync(kFull, m, leader);
@@ -865,28 +811,16 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                         ++n_nodes;
                         n_lane_nodes += __popc(__ballot_sync(kFull, leaf_active));
                     }
-                    ++visits;
                     const WideNode<K>* nd = nodes + cur;
                     f32x2 lox[K / 2], hix[K / 2], loy[K / 2], hiy[K / 2], loz[K / 2], hiz[K / 2];
                     int32_t ch[K];
-                    if constexpr (CPQ_NODE_KEEP) {
-                        const uint64_t pol = l2_keep_policy();
-                        load_row2_keep<K>(nd->lox, lox, pol);
-                        load_row2_keep<K>(nd->hix, hix, pol);
-                        load_row2_keep<K>(nd->loy, loy, pol);
-                        load_row2_keep<K>(nd->hiy, hiy, pol);
-                        load_row2_keep<K>(nd->loz, loz, pol);
-                        load_row2_keep<K>(nd->hiz, hiz, pol);
-                        load_row_i_keep<K>(nd->child, ch, pol);
-                    } else {
-                        load_row2<K>(nd->lox, lox);
-                        load_row2<K>(nd->hix, hix);
-                        load_row2<K>(nd->loy, loy);
-                        load_row2<K>(nd->hiy, hiy);
-                        load_row2<K>(nd->loz, loz);
-                        load_row2<K>(nd->hiz, hiz);
-                        load_row_i<K>(nd->child, ch);
-                    }
+                    load_row2<K>(nd->lox, lox);
+                    load_row2<K>(nd->hix, hix);
+                    load_row2<K>(nd->loy, loy);
+                    load_row2<K>(nd->hiy, hiy);
+                    load_row2<K>(nd->loz, loz);
+                    load_row2<K>(nd->hiz, hiz);
+                    load_row_i<K>(nd->child, ch);
                     // box lower bounds, two children per packed operation
                     float lb[K];
 #pragma unroll
@@ -1030,7 +964,6 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
             const int rec = best == kNoKey ? -1 : a.inv_order[a.toff[m] + idx];
             write_result(a, qi, qx, qy, qz, rec, idx, px, py, pz);
         }
-        if (lane0) st_work[2] = visits;
         // this packet's closest points seed the next one
         constexpr int kStride = 32 / kSeedPoints;
         if (lane % kStride == 0) st_seed[lane / kStride] = make_float4(px, py, pz, __int_as_float(valid ? m : -1));
@@ -2213,6 +2146,7 @@ cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int6
     args.stats = nullptr;
     args.box = b.box;
     args.mesh_root = b.mesh_root;
+    args.seed_chunk = qp.seed_chunk;
     {
         cudaStreamCaptureStatus capst = cudaStreamCaptureStatusNone;
         cudaStreamIsCapturing(st, &capst);

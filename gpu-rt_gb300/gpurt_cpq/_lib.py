@@ -40,7 +40,7 @@ class BuildOpts(Structure):
 
 class QueryOpts(Structure):
     _fields_ = [("block_size", c_int32), ("sort_queries", c_int32), ("blocks_per_sm", c_int32),
-                ("short_stack", c_int32), ("traversal", c_int32)]
+                ("short_stack", c_int32), ("traversal", c_int32), ("seed_chunk", c_int32)]
 
 
 class RayOpts(Structure):

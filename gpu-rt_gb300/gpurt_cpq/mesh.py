@@ -58,7 +58,9 @@ def build_opts(branching: int = 2, leaf_size: int = 4, collapse: str = "count",
 
 
 def query_opts(block_size: int = 0, sort_queries: bool = True, blocks_per_sm: int = 0,
-               short_stack: int = 0, traversal: str = "auto") -> QueryOpts:
+               short_stack: int = 0, traversal: str = "auto", seed_chunk: int = 0) -> QueryOpts:
+    """seed_chunk: packets a warp claims at once, each after the first seeded
+    from the previous packet's closest points (1 or 0: no seeding)."""
     o = QueryOpts()
     lib.cp_query_opts_default(byref(o))
     if block_size:
@@ -67,6 +69,8 @@ def query_opts(block_size: int = 0, sort_queries: bool = True, blocks_per_sm: in
     o.blocks_per_sm = blocks_per_sm
     if short_stack:
         o.short_stack = short_stack
+    if seed_chunk:
+        o.seed_chunk = seed_chunk
     kinds = {"auto": 0, "thread": 1, "packet": 2}
     if traversal not in kinds:
         raise ValueError(f"traversal must be one of {sorted(kinds)}, not {traversal!r}")

@@ -89,6 +89,9 @@ typedef struct cp_query_opts {
     int32_t blocks_per_sm;  /* persistent grid = SM count x this; 0 = from occupancy */
     int32_t short_stack;    /* per-thread stack entries kept in shared memory: 4, 8 or 16; 0 = default */
     int32_t traversal;      /* CP_TRAVERSAL_*: how lanes share work */
+    int32_t seed_chunk;     /* packet traversal: consecutive packets a warp claims at once, each after the
+                               first starting its lanes' limits at an upper bound from the previous packet's
+                               closest points: 1 (no seeding) .. 16; 0 = default (1) */
 } cp_query_opts;
 
 /* Traversal kernels.  PACKET: the 32 lanes of a warp take 32 consecutive
@@ -609,16 +612,17 @@ CP_API cp_status cp_shade_tonemap(int32_t type, float exposure, float gamma, int
 /* ---- autotuner ------------------------------------------------------------ */
 
 /*
- * Pick branching, leaf size, block size and traversal kernel (warp packet, or
- * per-thread with a short-stack depth) for a size class by timing candidate
- * builds and queries on the given mesh and queries (device arrays; pass the
- * real query set or one of the same density: packet coherence depends on
- * it).  The size class is (floor(log2(nt)), floor(log2(nq))).  The winner is
- * written to *best_build / *best_query and, when cache_path is not NULL,
- * stored in that text file (one "tri_class query_class branching leaf block
- * stack ms" line per class pair and branching, stack 0 = packet); a cached
- * class is returned without timing.  If best_build->branching is 2, 4 or 8 on
- * entry, only that branching is tried.  Synchronous.
+ * Pick branching, leaf size, block size and traversal kernel (warp packet,
+ * unseeded or seeded in chunks of 4 packets, or per-thread with a short-stack
+ * depth) for a size class by timing candidate builds and queries on the given
+ * mesh and queries (device arrays; pass the real query set or one of the same
+ * density: packet coherence depends on it).  The size class is
+ * (floor(log2(nt)), floor(log2(nq))).  The winner is written to *best_build /
+ * *best_query and, when cache_path is not NULL, stored in that text file (one
+ * "tri_class query_class branching leaf block stack ms seed_chunk" line per
+ * class pair and branching, stack 0 = packet); a cached class is returned
+ * without timing.  If best_build->branching is 2, 4 or 8 on entry, only that
+ * branching is tried.  Synchronous.
  */
 CP_API cp_status cp_autotune(const float* verts, int64_t nv, const int32_t* tris, int64_t nt,
                              const float* queries, int64_t nq, const char* cache_path,

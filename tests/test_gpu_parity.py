@@ -622,3 +622,33 @@ def test_allocation_failures_are_reported_and_release_memory(cpq, cuda):
     finally:
         lib.cp_debug_fail_allocation(-1)
     assert abs(second - first) < (16 << 20), (first, second)
+
+
+@pytest.mark.parametrize("K,leaf", [(2, 2), (4, 8), (8, 4)])
+def test_seeded_packets_change_no_answer(orc, cpq, cuda, K, leaf):
+    """Packets claimed in chunks and seeded from the packet before them give
+    the unseeded answers bit for bit (a seed is an upper bound with a margin
+    far above the tests' errors), on a mesh and on a batch whose packets
+    cross mesh boundaries; and they are FP64's."""
+    import torch
+
+    from gpurt_cpq import workloads as W
+
+    v, t = W.heightfield(256, seed=4)
+    q = np.concatenate([W.heightfield_queries(v, t, 60_000, seed=5), W.uniform_queries(40_000, -0.2, 1.2, 6)])
+    m = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=K, leaf_size=leaf)
+    qd = dev(q, cuda)
+    base = m.query(qd, want_bary=True, opts=cpq.query_opts(seed_chunk=1))
+    for chunk in (2, 4, 16):
+        r = m.query(qd, want_bary=True, opts=cpq.query_opts(seed_chunk=chunk))
+        for k in ("dist", "tri", "point", "bary"):
+            assert torch.equal(getattr(r, k), getattr(base, k)), (chunk, k)
+    check_against_fp64(orc, v, t, q[:20000], type(base)(point=base.point[:20000], dist=base.dist[:20000],
+                                                         tri=base.tri[:20000], bary=None))
+    meshes, queries = W.batched(seed=3, nmeshes=10, tri_range=(200, 20000), q_range=(100, 8000))
+    V, voff, T, toff, Q, qoff = W.concat_batch(meshes, queries)
+    b = cpq.Batch(dev(V, cuda), voff, dev(T, cuda), toff, branching=K, leaf_size=leaf)
+    b1 = b.query(dev(Q, cuda), qoff, opts=cpq.query_opts(seed_chunk=1))
+    b4 = b.query(dev(Q, cuda), qoff, opts=cpq.query_opts(seed_chunk=4))
+    assert torch.equal(b1.dist, b4.dist) and torch.equal(b1.tri, b4.tri)
+    assert m.device_status() == 0
