@@ -378,6 +378,37 @@ CP_API cp_status cp_mesh_refit(cp_mesh* m, const float* verts, int64_t vstride, 
     return CP_SUCCESS;
 }
 
+CP_API cp_status cp_mesh_save(const cp_mesh* m, const char* path) {
+    if (!m || !path) return fail(CP_ERROR_INVALID_VALUE, "mesh or path is NULL");
+    std::string why;
+    cudaError_t e = bvh_save(const_cast<cp_mesh*>(m)->bvh, path, &why);
+    if (!why.empty()) return fail(CP_ERROR_INVALID_VALUE, "cp_mesh_save: " + why);
+    if (e != cudaSuccess) return cuda_fail(e, "cp_mesh_save");
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_mesh_load(const char* path, cp_stream_t stream, cp_mesh** out) {
+    if (!out || !path) return fail(CP_ERROR_INVALID_VALUE, "path or out is NULL");
+    *out = nullptr;
+    cp_mesh* m = new (std::nothrow) cp_mesh();
+    if (!m) return fail(CP_ERROR_OUT_OF_MEMORY, "host allocation of the handle failed");
+    std::string why;
+    bool bad = false;
+    cudaError_t e = bvh_load(m->bvh, path, reinterpret_cast<cudaStream_t>(stream), &why, &bad);
+    if (e == cudaSuccess && m->bvh.nmeshes != 1) {
+        bad = true;
+        why = "the file holds a batch of " + std::to_string(m->bvh.nmeshes) + " meshes, not one mesh";
+    }
+    if (bad || e != cudaSuccess) {
+        bvh_free(m->bvh);
+        delete m;
+        if (bad) return fail(CP_ERROR_INVALID_VALUE, std::string("cp_mesh_load: ") + path + ": " + why);
+        return cuda_fail(e, "cp_mesh_load");
+    }
+    *out = m;
+    return CP_SUCCESS;
+}
+
 CP_API cp_status cp_mesh_destroy(cp_mesh* m) {
     if (!m) return CP_SUCCESS;
     bvh_free(m->bvh);

@@ -82,6 +82,12 @@ cudaError_t bvh_refit(Bvh& b, const float* verts, int64_t vert_stride, cudaStrea
 
 void bvh_free(Bvh& b);
 
+// A built BVH written to a file and read back (persist.cu).  bvh_save
+// synchronises the device; bvh_load validates the whole file on the host
+// before any device work (*bad_file and *why on refusal) and synchronises `st`.
+cudaError_t bvh_save(Bvh& b, const char* path, std::string* why);
+cudaError_t bvh_load(Bvh& b, const char* path, cudaStream_t st, std::string* why, bool* bad_file);
+
 // Query workspace and launch (query.cu).
 struct QueryParams {
     int block = 256;

@@ -90,6 +90,8 @@ SIGNATURES = {
                                  c_void_p, POINTER(c_void_p)]),
     "cp_mesh_refit": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p]),
     "cp_mesh_destroy": (c_int32, [c_void_p]),
+    "cp_mesh_save": (c_int32, [c_void_p, c_char_p]),
+    "cp_mesh_load": (c_int32, [c_char_p, c_void_p, POINTER(c_void_p)]),
     "cp_mesh_info": (c_int32, [c_void_p, POINTER(MeshInfo)]),
     "cp_mesh_device_status": (c_int32, [c_void_p, c_void_p, POINTER(c_uint32)]),
     "cp_query_workspace_size": (c_int32, [c_void_p, c_int64, POINTER(QueryOpts), POINTER(c_size_t)]),

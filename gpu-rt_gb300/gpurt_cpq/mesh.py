@@ -128,6 +128,25 @@ class Mesh:
         self._h = h
         self.device = verts.device
 
+    # -- saved BVHs -------------------------------------------------------------
+    def save(self, path) -> None:
+        """Write the built BVH to `path` (cp_mesh_save)."""
+        check(lib.cp_mesh_save(self._h, str(path).encode()), "cp_mesh_save")
+
+    @classmethod
+    def load(cls, path, *, device=None, stream=None) -> "Mesh":
+        """A mesh read from a file cp_mesh_save wrote, without a build (cp_mesh_load)."""
+        h = c_void_p()
+        check(lib.cp_mesh_load(str(path).encode(), _stream(stream), byref(h)), "cp_mesh_load")
+        m = cls.__new__(cls)
+        m._h = h
+        info = m.info()
+        m.num_vertices = int(info.num_vertices)
+        m.num_triangles = int(info.num_triangles)
+        m.opts = build_opts(info.branching, info.leaf_size)
+        m.device = device if device is not None else torch.device("cuda", torch.cuda.current_device())
+        return m
+
     # -- lifetime ------------------------------------------------------------
     def close(self) -> None:
         if getattr(self, "_h", None) and self._h.value:

@@ -644,6 +644,22 @@ CP_API cp_status cp_batch_autotune(const float* verts, const int64_t* vert_offse
                                    const int64_t* q_offsets, int32_t branching, const char* cache_path,
                                    int32_t* leaf_sizes, cp_query_opts* best_query);
 
+/* ---- saved BVHs ------------------------------------------------------------ */
+
+/* Write a built mesh (its BVH, triangle records and the arrays refit needs) to
+ * a file, and read one back as a new mesh that queries, refits and exports as
+ * the original does, without a build.  The file holds raw device arrays in
+ * this library's layout (host byte order), behind a header with the build's
+ * parameters and counts.  cp_mesh_load checks the whole file on the host
+ * before anything reaches the GPU — its size against the header, every index
+ * a kernel follows, that each wide tree is a tree within its depth bound — and
+ * refuses a damaged or foreign file with CP_ERROR_INVALID_VALUE and a message.
+ * Both are synchronous (cp_mesh_save waits for the device).  The reference
+ * keeps nothing between runs (its only file output is the image,
+ * src/gpurt.cpp:258-262). */
+CP_API cp_status cp_mesh_save(const cp_mesh* mesh, const char* path);
+CP_API cp_status cp_mesh_load(const char* path, cp_stream_t stream, cp_mesh** out);
+
 /* Size class used by the autotuner cache: floor(log2(num_triangles)). */
 CP_API int32_t cp_size_class(int64_t num_triangles);
 
