@@ -37,6 +37,19 @@
 namespace cpq {
 namespace {
 
+// The routines many call sites share — the scene tracer, sin / cos / pow /
+// exp, the materials and the light sampling — stay out of line: a pixel's
+// warp diverges across integrators, bounces and materials, and one copy of
+// each keeps the kernel's hot code in the instruction cache (inlined, the
+// kernel stalls mostly on instruction fetch).  Calls round nothing
+// differently: every operation is the same, and this file has no multiply-add
+// contraction.
+#ifndef CPQ_SHADE_INLINE
+#define SH_CALL __noinline__
+#else
+#define SH_CALL
+#endif
+
 constexpr float kPi = 3.141592f;          // rtcommon.glsl:6 (the shader's truncated constant)
 constexpr float kLargeDist = 10000000.0f;  // rtcommon.glsl:7
 constexpr float kEps = 0.00001f;           // rtcommon.glsl:8
@@ -72,7 +85,7 @@ __device__ __forceinline__ bool any_pos(v3 a) { return a.x > 0.0f || a.y > 0.0f 
 // round-to-nearest-integer, one multiply and one subtract), then the Taylor
 // polynomials of sin (to r^9) and cos (to r^10) on |r| <= pi/4 in FP32
 // Horner form: truncation below 2e-9 absolute, within about an ulp.
-__device__ void sh_sincos(float x, float* s, float* c) {
+__device__ SH_CALL void sh_sincos(float x, float* s, float* c) {
     const double kTwoOverPi = 0.63661977236758134308;
     const double kPiOver2 = 1.57079632679489661923;
     const double k = nearbyint((double)x * kTwoOverPi);
@@ -100,7 +113,7 @@ __constant__ double c_inv_fact[14] = {1.0,          1.0,           1.0 / 2.0,   
 
 // 2^t in FP64: 2^k e^((t - k) ln 2), k the nearest integer to t, the
 // exponential's Taylor series to degree 13 (|(t - k) ln 2| <= 0.35).
-__device__ double sh_exp2_d(double t) {
+__device__ SH_CALL double sh_exp2_d(double t) {
     if (t > 200.0) return INFINITY;
     if (t < -200.0) return 0.0;
     const double k = nearbyint(t);
@@ -113,7 +126,7 @@ __device__ double sh_exp2_d(double t) {
 // pow(x, y) for x >= 0: 2^(y log2 x) in FP64, rounded once.  log2 x = e +
 // ln(m) / ln 2 with x = m 2^e, m in [sqrt(1/2), sqrt(2)), and ln m =
 // 2 atanh(s), s = (m - 1) / (m + 1), summed to s^15.
-__device__ float sh_pow(float xf, float yf) {
+__device__ SH_CALL float sh_pow(float xf, float yf) {
     if (xf != xf || yf != yf) return NAN;
     if (xf < 0.0f) return NAN;
     if (xf == 0.0f) return yf > 0.0f ? 0.0f : (yf == 0.0f ? 1.0f : INFINITY);
@@ -212,7 +225,7 @@ __device__ bool triangle_hit(v3 o, v3 d, v3 pa, v3 pb, v3 pc, v3* hitp) {
     return t >= 0.0f;
 }
 // solid-angle pdf of d from o under uniform area sampling of the triangle
-__device__ float triangle_pdf(v3 o, v3 d, v3 v0, v3 v1, v3 v2) {
+__device__ SH_CALL float triangle_pdf(v3 o, v3 d, v3 v0, v3 v1, v3 v2) {
     v3 hitp;
     if (triangle_hit(o, d, v0, v1, v2, &hitp)) {
         const float a = 2.0f / length3(cross(sub(v1, v0), sub(v2, v0)));
@@ -322,13 +335,13 @@ __device__ bool ggx_sample(uint32_t* seed, const MatInfo& m, const ShadeInfo& sh
     *wi = reflect3(sh.wo, h);
     return dot(*wi, sh.n) > 0.0f;
 }
-__device__ float mat_pdf(int brdf, const MatInfo& m, const ShadeInfo& sh, v3 wi) {
+__device__ SH_CALL float mat_pdf(int brdf, const MatInfo& m, const ShadeInfo& sh, v3 wi) {
     return brdf == 0 ? bp_pdf(m, sh, wi) : ggx_pdf(m, sh, wi);
 }
-__device__ v3 mat_eval(int brdf, const MatInfo& m, const ShadeInfo& sh, v3 wi) {
+__device__ SH_CALL v3 mat_eval(int brdf, const MatInfo& m, const ShadeInfo& sh, v3 wi) {
     return brdf == 0 ? bp_eval(m, sh, wi) : ggx_eval(m, sh, wi);
 }
-__device__ bool mat_sample(int brdf, uint32_t* seed, const MatInfo& m, const ShadeInfo& sh, v3* wi) {
+__device__ SH_CALL bool mat_sample(int brdf, uint32_t* seed, const MatInfo& m, const ShadeInfo& sh, v3* wi) {
     return brdf == 0 ? bp_sample(seed, m, sh, wi) : ggx_sample(seed, m, sh, wi);
 }
 
@@ -376,7 +389,7 @@ struct HitRec {
 // The scene tracer: the nearest hit with t in [tmin, tmax] (ties to the
 // least triangle index), or with `any` whether there is one.
 template <int K>
-__device__ HitRec trace(const ShadeArgs& a, v3 o, v3 d, float tmin, float tmax, bool any, int32_t* stack) {
+__device__ SH_CALL HitRec trace(const ShadeArgs& a, v3 o, v3 d, float tmin, float tmax, bool any, int32_t* stack) {
     float bt = INFINITY, bu = 0.0f, bv = 0.0f;
     int bidx = INT_MAX;
     const bool found = raywalk::ray_walk<K>(static_cast<const WideNode<K>*>(a.nodes), a.recs, a.root, o.x, o.y, o.z,
@@ -438,7 +451,7 @@ struct LightSample {
     float pdf;
 };
 // a point on a uniformly chosen triangle of a uniformly chosen light (rt.rgen:150-194)
-__device__ LightSample light_sample(const ShadeArgs& a, uint32_t* seed, v3 p) {
+__device__ SH_CALL LightSample light_sample(const ShadeArgs& a, uint32_t* seed, v3 p) {
     const uint32_t li = sh_randu(seed, 0, a.n_lights);
     const LightRec& L = a.lights[li];
     const uint32_t n_tris = (uint32_t)L.count;
@@ -460,7 +473,7 @@ __device__ LightSample light_sample(const ShadeArgs& a, uint32_t* seed, v3 p) {
     return r;
 }
 // direction to a uniform point on a uniformly chosen light triangle (rt.rgen:196-220)
-__device__ v3 light_sample_dir(const ShadeArgs& a, uint32_t* seed, v3 p) {
+__device__ SH_CALL v3 light_sample_dir(const ShadeArgs& a, uint32_t* seed, v3 p) {
     const uint32_t li = sh_randu(seed, 0, a.n_lights);
     const LightRec& L = a.lights[li];
     const uint32_t ti = sh_randu(seed, 0, (uint32_t)L.count);
@@ -470,7 +483,7 @@ __device__ v3 light_sample_dir(const ShadeArgs& a, uint32_t* seed, v3 p) {
     return normalize3(sub(pt, p));
 }
 // brute-force solid-angle pdf of light sampling for direction d (rt.rgen:222-255)
-__device__ float light_pdf(const ShadeArgs& a, v3 p, v3 d) {
+__device__ SH_CALL float light_pdf(const ShadeArgs& a, v3 p, v3 d) {
     float oacc = 0.0f;
     for (uint32_t l = 0; l < a.n_lights; ++l) {
         const LightRec& L = a.lights[l];
