@@ -552,6 +552,12 @@ __device__ __forceinline__ void st_stream(T* p, T v) {
     else *p = v;
 }
 
+// The next node of a descent prefetched into L1 (a tuning option, off).
+#ifndef CPQ_PREFETCH_NEXT
+#define CPQ_PREFETCH_NEXT 0
+#endif
+__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
 // The winner's float-float re-evaluation and the outputs; the closest point
 // (NaN when nothing was found) is also returned in (px, py, pz).
 __device__ __forceinline__ void write_result(const TraverseArgs& a, int64_t qi, float qx, float qy,
@@ -847,6 +853,16 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                         // go first to the child nearest to any lane
                         const int f = (int)(__reduce_min_sync(kFull, kmine) & 7u);
                         const uint32_t rest = need & ~(1u << f);
+                        int32_t cf = ch[0];
+#pragma unroll
+                        for (int s = 1; s < K; ++s) cf = f == s ? ch[s] : cf;
+                        if constexpr (CPQ_PREFETCH_NEXT) {
+                            // its line (a node, or the leaf's first record) on its
+                            // way to L1 while the push below runs
+                            if (lane0)
+                                prefetch_l1(cf >= 0 ? static_cast<const void*>(nodes + cf)
+                                                    : static_cast<const void*>(a.fast + leaf_first(cf)));
+                        }
                         if (rest != 0) {
                             // the node becomes the top entry; a used-up top
                             // entry is overwritten, a live one keeps its list
@@ -865,9 +881,6 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                             ++sp;
                             __syncwarp();
                         }
-                        int32_t cf = ch[0];
-#pragma unroll
-                        for (int s = 1; s < K; ++s) cf = f == s ? ch[s] : cf;
                         cur = cf;
                         leaf_active = (mine_need >> f) & 1u;
                         continue;
