@@ -23,6 +23,7 @@
 #include "../../include/cpq.h"
 #include "bvh.cuh"
 #include "handles.cuh"
+#include "sort.cuh"
 #include "ray.cuh"
 
 using namespace cpq;
@@ -319,6 +320,14 @@ CP_API void cp_debug_fail_allocation(int64_t after) {
     g_fail_after.store(after < 0 ? -1 : after, std::memory_order_relaxed);
 }
 
+// Values 0..n-1: the identity permutation the sort starts from.
+__global__ void k_iota(int32_t* __restrict__ v, int64_t n) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) v[i] = (int32_t)i;
+}
+
+static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
 CP_API cp_status cp_timing_enable(int32_t flags) {
     if (flags & ~(CP_TIMING_EVENTS | CP_TIMING_COUNTERS))
         return fail(CP_ERROR_INVALID_VALUE, "cp_timing_enable: unknown flag bits");
@@ -487,6 +496,64 @@ CP_API cp_status cp_query(const cp_mesh* m, const float* queries, int64_t nq,
     if (s != CP_SUCCESS) return s;
     return query_impl(m->bvh, queries, nq, nullptr, qp, out_point, out_dist, out_tri, out_bary,
                       workspace, ws_bytes, reinterpret_cast<cudaStream_t>(stream));
+}
+
+CP_API cp_status cp_query_order(cp_mesh* m, const float* queries, int64_t nq, int32_t* perm, uint32_t* keys,
+                                cp_stream_t stream) {
+    if (!m) return fail(CP_ERROR_INVALID_VALUE, "mesh is NULL");
+    if (nq < 2 || nq > INT32_MAX) return fail(CP_ERROR_INVALID_VALUE, "cp_query_order: nq must be in 2..2^31 - 1");
+    if (!queries || !perm) return fail(CP_ERROR_INVALID_VALUE, "queries and perm are required");
+    if (m->bvh.nmeshes != 1) return fail(CP_ERROR_NOT_SUPPORTED, "cp_query_order: single meshes only");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    QueryParams qp;
+    cp_status s = to_query_params(nullptr, &qp);
+    if (s != CP_SUCCESS) return s;
+    qp.sort = 1;
+    const size_t need = query_workspace_bytes(m->bvh, nq, qp);
+    void* ws = nullptr;
+    CP_CUDA(ws_alloc(&ws, need, st), "workspace allocation");
+    const int32_t* order = nullptr;
+    unsigned long long* counter = nullptr;
+    cudaError_t e = order_points(m->bvh, queries, nq, nullptr, true, ws, need, st, &order, &counter, false, keys);
+    if (e == cudaSuccess && order)
+        e = cudaMemcpyAsync(perm, order, sizeof(int32_t) * nq, cudaMemcpyDeviceToDevice, st);
+    cudaFreeAsync(ws, st);
+    if (e != cudaSuccess) return cuda_fail(e, "cp_query_order");
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_debug_order_sort(const void* keys, int32_t key_bytes, int64_t n, int32_t begin_bit,
+                                     int32_t end_bit, int32_t* perm, cp_stream_t stream) {
+    if (!keys || !perm) return fail(CP_ERROR_INVALID_VALUE, "keys and perm are required");
+    if (key_bytes != 4 && key_bytes != 8) return fail(CP_ERROR_INVALID_VALUE, "key_bytes must be 4 or 8");
+    if (n < 2 || n > INT32_MAX) return fail(CP_ERROR_INVALID_VALUE, "n must be in 2..2^31 - 1");
+    if (begin_bit < 0 || end_bit <= begin_bit || end_bit > 8 * key_bytes)
+        return fail(CP_ERROR_INVALID_VALUE, "need 0 <= begin_bit < end_bit <= key width");
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const size_t kb = align256((size_t)key_bytes * n), vb = align256(sizeof(int32_t) * n);
+    const size_t sb = radix_sort_workspace_bytes(n);
+    unsigned char* ws = nullptr;
+    CP_CUDA(ws_alloc(reinterpret_cast<void**>(&ws), 2 * kb + 2 * vb + sb, st), "workspace allocation");
+    int32_t* vals = reinterpret_cast<int32_t*>(ws + 2 * kb);
+    int32_t* vals_alt = reinterpret_cast<int32_t*>(ws + 2 * kb + vb);
+    cudaError_t e = cudaMemcpyAsync(ws, keys, (size_t)key_bytes * n, cudaMemcpyDeviceToDevice, st);
+    if (e == cudaSuccess) {
+        k_iota<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(vals, n); note_launch();
+        e = cudaGetLastError();
+    }
+    bool in_alt = false;
+    if (e == cudaSuccess)
+        e = key_bytes == 4 ? radix_sort_pairs<uint32_t>(reinterpret_cast<uint32_t*>(ws), vals,
+                                                         reinterpret_cast<uint32_t*>(ws + kb), vals_alt, n,
+                                                         begin_bit, end_bit, ws + 2 * kb + 2 * vb, sb, st, &in_alt)
+                           : radix_sort_pairs<uint64_t>(reinterpret_cast<uint64_t*>(ws), vals,
+                                                         reinterpret_cast<uint64_t*>(ws + kb), vals_alt, n,
+                                                         begin_bit, end_bit, ws + 2 * kb + 2 * vb, sb, st, &in_alt);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(perm, in_alt ? vals_alt : vals, sizeof(int32_t) * n, cudaMemcpyDeviceToDevice, st);
+    cudaFreeAsync(ws, st);
+    if (e != cudaSuccess) return cuda_fail(e, "cp_debug_order_sort");
+    return CP_SUCCESS;
 }
 
 CP_API cp_status cp_query_host(const cp_mesh* m, const float* queries, int64_t nq,

@@ -106,10 +106,12 @@ size_t query_workspace_bytes(const Bvh& b, int64_t nq, const QueryParams& qp);
 // query_workspace_bytes(b, nq, {sort}) bytes, plus the zeroed work counter of
 // a persistent traversal.  `coarse` sorts only the Hilbert index's top bits
 // (about 16 points per curve segment): a radix pass less, for per-thread
-// walks.  Stream-ordered; no host synchronisation.
+// walks.  `keys_out` (optional; single meshes, whose keys have at most 32
+// bits) receives each point's key in input order.  Stream-ordered; no host
+// synchronisation.
 cudaError_t order_points(const Bvh& b, const float* points, int64_t nq, const int64_t* d_qoff,
                          bool sort, void* ws, size_t ws_bytes, cudaStream_t st, const int32_t** perm,
-                         unsigned long long** counter, bool coarse = false);
+                         unsigned long long** counter, bool coarse = false, uint32_t* keys_out = nullptr);
 
 // q_off: device array of nmeshes + 1 query offsets (nullptr for one mesh).
 cudaError_t bvh_query(const Bvh& b, const float* queries, int64_t nq, const int64_t* d_qoff,

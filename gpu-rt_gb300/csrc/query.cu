@@ -552,12 +552,6 @@ __device__ __forceinline__ void st_stream(T* p, T v) {
     else *p = v;
 }
 
-// The next node of a descent prefetched into L1 (a tuning option, off).
-#ifndef CPQ_PREFETCH_NEXT
-#define CPQ_PREFETCH_NEXT 0
-#endif
-__device__ __forceinline__ void prefetch_l1(const void* p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
-
 // The winner's float-float re-evaluation and the outputs; the closest point
 // (NaN when nothing was found) is also returned in (px, py, pz).
 __device__ __forceinline__ void write_result(const TraverseArgs& a, int64_t qi, float qx, float qy,
@@ -856,13 +850,6 @@ __global__ void __launch_bounds__(256, K == 8 ? 2 : 4) k_traverse_packet(Travers
                         int32_t cf = ch[0];
 #pragma unroll
                         for (int s = 1; s < K; ++s) cf = f == s ? ch[s] : cf;
-                        if constexpr (CPQ_PREFETCH_NEXT) {
-                            // its line (a node, or the leaf's first record) on its
-                            // way to L1 while the push below runs
-                            if (lane0)
-                                prefetch_l1(cf >= 0 ? static_cast<const void*>(nodes + cf)
-                                                    : static_cast<const void*>(a.fast + leaf_first(cf)));
-                        }
                         if (rest != 0) {
                             // the node becomes the top entry; a used-up top
                             // entry is overwritten, a live one keeps its list
@@ -2066,7 +2053,7 @@ size_t query_workspace_bytes(const Bvh& b, int64_t nq, const QueryParams& qp) {
 
 cudaError_t order_points(const Bvh& b, const float* queries, int64_t nq, const int64_t* d_qoff,
                          bool sort, void* ws, size_t ws_bytes, cudaStream_t st, const int32_t** perm_out,
-                         unsigned long long** counter_out, bool coarse) {
+                         unsigned long long** counter_out, bool coarse, uint32_t* keys_out) {
     const QueryLayout L = layout(nq, b.nmeshes, sort);
     if (ws_bytes < L.total) return cudaErrorInvalidValue;
     unsigned char* w = static_cast<unsigned char*>(ws);
@@ -2113,6 +2100,10 @@ cudaError_t order_points(const Bvh& b, const float* queries, int64_t nq, const i
                                                           k32, vals); note_launch();
             e = cudaGetLastError();
             if (e != cudaSuccess) return e;
+            if (keys_out) {
+                e = cudaMemcpyAsync(keys_out, k32, sizeof(uint32_t) * nq, cudaMemcpyDeviceToDevice, st);
+                if (e != cudaSuccess) return e;
+            }
             e = radix_sort_pairs<uint32_t>(k32, vals, k32_alt, vals_alt, nq, begin_bit, key_bits,
                                            w + L.sort_ws, L.sort_ws_bytes, st, &in_alt);
         } else {

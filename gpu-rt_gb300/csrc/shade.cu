@@ -104,28 +104,47 @@ __device__ SH_CALL void sh_sincos(float x, float* s, float* c) {
 }
 
 constexpr double kLn2 = 0.69314718055994530942;
+constexpr double kInvLn2 = 1.44269504088896340736;
 
-// 1 / j! for j = 0..13, each the correctly rounded quotient
-__constant__ double c_inv_fact[14] = {1.0,          1.0,           1.0 / 2.0,       1.0 / 6.0,
-                                      1.0 / 24.0,   1.0 / 120.0,   1.0 / 720.0,     1.0 / 5040.0,
-                                      1.0 / 40320.0, 1.0 / 362880.0, 1.0 / 3628800.0, 1.0 / 39916800.0,
-                                      1.0 / 479001600.0, 1.0 / 6227020800.0};
+// 1 / j! for j = 0..10, each the correctly rounded quotient
+__constant__ double c_inv_fact[11] = {1.0,        1.0,         1.0 / 2.0,      1.0 / 6.0,
+                                      1.0 / 24.0, 1.0 / 120.0, 1.0 / 720.0,    1.0 / 5040.0,
+                                      1.0 / 40320.0, 1.0 / 362880.0, 1.0 / 3628800.0};
+// 1 / j for odd j = 1..15
+__constant__ double c_inv_odd[8] = {1.0,        1.0 / 3.0,  1.0 / 5.0,  1.0 / 7.0,
+                                    1.0 / 9.0,  1.0 / 11.0, 1.0 / 13.0, 1.0 / 15.0};
+
+// 2^k for an integer |k| <= 1022, from its bits
+__device__ __forceinline__ double sh_pow2i(int k) { return __longlong_as_double((long long)(k + 1023) << 52); }
+
+// 1 / d in FP64 for d in [1.7, 2.5] without a division: the FP32 quotient
+// (relative error below 2^-23) refined by two Newton steps r += r (1 - d r),
+// each two fused multiply-adds that square the error (below 2^-52 after).
+__device__ __forceinline__ double sh_rcp_d(double d) {
+    double r = (double)(1.0f / (float)d);
+    double e = fma(-d, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-d, r, 1.0);
+    return fma(r, e, r);
+}
 
 // 2^t in FP64: 2^k e^((t - k) ln 2), k the nearest integer to t, the
-// exponential's Taylor series to degree 13 (|(t - k) ln 2| <= 0.35).
+// exponential's Taylor series to degree 10 (|(t - k) ln 2| <= 0.35:
+// truncation below 2.2e-13 relative) in fused multiply-adds, scaled exactly.
 __device__ SH_CALL double sh_exp2_d(double t) {
     if (t > 200.0) return INFINITY;
     if (t < -200.0) return 0.0;
     const double k = nearbyint(t);
     const double g = (t - k) * kLn2;
-    double p = c_inv_fact[13];
-    for (int j = 12; j >= 0; --j) p = c_inv_fact[j] + g * p;
-    return ldexp(p, (int)k);
+    double p = c_inv_fact[10];
+    for (int j = 9; j >= 0; --j) p = fma(g, p, c_inv_fact[j]);
+    return p * sh_pow2i((int)k);
 }
 
 // pow(x, y) for x >= 0: 2^(y log2 x) in FP64, rounded once.  log2 x = e +
 // ln(m) / ln 2 with x = m 2^e, m in [sqrt(1/2), sqrt(2)), and ln m =
-// 2 atanh(s), s = (m - 1) / (m + 1), summed to s^15.
+// 2 atanh(s), s = (m - 1) / (m + 1) (the quotient through sh_rcp_d), summed
+// to s^15 in fused multiply-adds.
 __device__ SH_CALL float sh_pow(float xf, float yf) {
     if (xf != xf || yf != yf) return NAN;
     if (xf < 0.0f) return NAN;
@@ -138,19 +157,19 @@ __device__ SH_CALL float sh_pow(float xf, float yf) {
         m = m * 2.0;
         e = e - 1;
     }
-    const double s = (m - 1.0) / (m + 1.0);
+    const double s = (m - 1.0) * sh_rcp_d(m + 1.0);
     const double s2 = s * s;
-    double series = 1.0 / 15.0;
-    for (int j = 13; j >= 1; j -= 2) series = 1.0 / (double)j + s2 * series;
+    double series = c_inv_odd[7];
+    for (int j = 6; j >= 0; --j) series = fma(s2, series, c_inv_odd[j]);
     const double lnm = 2.0 * s * series;
-    const double t = (double)yf * ((double)e + lnm / kLn2);
+    const double t = (double)yf * fma(lnm, kInvLn2, (double)e);
     return (float)sh_exp2_d(t);
 }
 
 // e^x = 2^(x / ln 2) in FP64, rounded once
 __device__ float sh_exp(float x) {
     if (x != x) return NAN;
-    return (float)sh_exp2_d((double)x / kLn2);
+    return (float)sh_exp2_d((double)x * kInvLn2);
 }
 
 // ---- random numbers (rtcommon.glsl:99-139) ----------------------------------

@@ -125,6 +125,8 @@ SIGNATURES = {
                                  c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_int32,
                                  c_void_p]),
     "cp_debug_fail_allocation": (None, [c_int64]),
+    "cp_debug_order_sort": (c_int32, [c_void_p, c_int32, c_int64, c_int32, c_int32, c_void_p, c_void_p]),
+    "cp_query_order": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     "cp_scene_create": (c_int32, [c_void_p, c_void_p, c_void_p, c_int32, c_void_p, POINTER(c_void_p)]),
     "cp_scene_update": (c_int32, [c_void_p, c_void_p, c_void_p]),
     "cp_scene_refit": (c_int32, [c_void_p, c_void_p, c_void_p]),

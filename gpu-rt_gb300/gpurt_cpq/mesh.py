@@ -173,6 +173,18 @@ class Mesh:
         check(lib.cp_mesh_device_status(self._h, _stream(stream), byref(bits)), "cp_mesh_device_status")
         return bits.value
 
+    def query_order(self, points: torch.Tensor, stream=None) -> tuple[torch.Tensor, torch.Tensor]:
+        """(perm, keys): the order cp_query with sort_queries walks these
+        queries in (perm[i] = the input index of the i-th) and each query's
+        Hilbert key in input order (int64, values below 2^30)."""
+        _check_dev(points, "points", torch.float32, 3)
+        n = points.shape[0]
+        perm = torch.empty(n, dtype=torch.int32, device=points.device)
+        keys = torch.empty(n, dtype=torch.int32, device=points.device)
+        check(lib.cp_query_order(self._h, _ptr(points), n, _ptr(perm), _ptr(keys), _stream(stream)),
+              "cp_query_order")
+        return perm, keys.to(torch.int64) & 0xFFFFFFFF
+
     # -- queries -------------------------------------------------------------
     def workspace_size(self, nq: int, opts: QueryOpts | None = None) -> int:
         b = c_size_t(0)

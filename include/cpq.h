@@ -217,6 +217,26 @@ CP_API cp_status cp_query_workspace_size(const cp_mesh* mesh, int64_t nq, const 
                                          size_t* bytes);
 
 /*
+ * Diagnostic: the order in which cp_query with sort_queries walks these
+ * queries — perm[i] is the input index of the i-th query along the Hilbert
+ * curve of the query box, keys (NULL: not written) each query's 30-bit curve
+ * index in input order — so that perm sorts keys stably.  nq >= 2; device
+ * arrays; asynchronous on `stream`.
+ */
+CP_API cp_status cp_query_order(cp_mesh* mesh, const float* queries, int64_t nq, int32_t* perm,
+                                uint32_t* keys, cp_stream_t stream);
+
+/*
+ * Diagnostic: the library's radix sort (the one that orders queries and rays
+ * and sorts the build's Morton keys) on caller keys — perm receives the
+ * permutation that sorts keys[0..n) (key_bytes 4 or 8, device) stably on
+ * bits [begin_bit, end_bit).  The keys are not modified.  Asynchronous on
+ * `stream`.
+ */
+CP_API cp_status cp_debug_order_sort(const void* keys, int32_t key_bytes, int64_t n, int32_t begin_bit,
+                                     int32_t end_bit, int32_t* perm, cp_stream_t stream);
+
+/*
  * Closest-point query.  Replaces the per-pixel traceRayEXT over the
  * acceleration structure (src/shaders/rt/rt.rgen:257-270) with a closest-first
  * BVH descent and an exact point-triangle distance at the leaves; the

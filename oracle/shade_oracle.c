@@ -91,36 +91,52 @@ static inline float sh_cos(float x) {
  * log2 x = e + ln(m) / ln 2 with x = m 2^e, m in [sqrt(1/2), sqrt(2)), and
  * ln m = 2 atanh(s), s = (m - 1) / (m + 1), |s| < 0.172, summed to s^15;
  * 2^t = 2^k e^(f ln 2), k = nearest integer to t, |f| <= 1/2, Taylor to
- * degree 13.  Both series truncate below 1e-15 relative. */
+ * degree 10.  The series truncate below 3e-13 relative.  The divisions are
+ * a multiply by 1/ln 2 and a Newton reciprocal, and the polynomials are
+ * fused multiply-adds (fma() rounds once, as the GPU's does), so the GPU
+ * kernels evaluate the same operations on their FP64 pipe, which on GB300
+ * has 1/64 of the FP32 rate. */
 static const double kLn2 = 0.69314718055994530942;
+static const double kInvLn2 = 1.44269504088896340736;
+
+/* 2^k for an integer |k| <= 1022, from its bits */
+static double sh_pow2i(int k) {
+    const uint64_t u = (uint64_t)(k + 1023) << 52;
+    double d;
+    memcpy(&d, &u, sizeof d);
+    return d;
+}
+
+/* 1 / d for d in [1.7, 2.5] without a division: the FP32 quotient (relative
+ * error below 2^-23) refined by two Newton steps r += r (1 - d r), each two
+ * fused multiply-adds that square the error (below 2^-52 after). */
+static double sh_rcp_d(double d) {
+    double r = (double)(1.0f / (float)d);
+    double e = fma(-d, r, 1.0);
+    r = fma(r, e, r);
+    e = fma(-d, r, 1.0);
+    return fma(r, e, r);
+}
 
 /* 2^t in FP64: 2^k e^((t - k) ln 2), k the nearest integer to t, the
- * exponential's Taylor series to degree 13 (|(t - k) ln 2| <= 0.35) */
+ * exponential's Taylor series to degree 10 (|(t - k) ln 2| <= 0.35),
+ * scaled exactly */
 static double sh_exp2_d(double t) {
-    static const double kInvFact[14] = {1.0,
-                                        1.0,
-                                        1.0 / 2.0,
-                                        1.0 / 6.0,
-                                        1.0 / 24.0,
-                                        1.0 / 120.0,
-                                        1.0 / 720.0,
-                                        1.0 / 5040.0,
-                                        1.0 / 40320.0,
-                                        1.0 / 362880.0,
-                                        1.0 / 3628800.0,
-                                        1.0 / 39916800.0,
-                                        1.0 / 479001600.0,
-                                        1.0 / 6227020800.0};
+    static const double kInvFact[11] = {1.0,         1.0,          1.0 / 2.0,      1.0 / 6.0,
+                                        1.0 / 24.0,  1.0 / 120.0,  1.0 / 720.0,    1.0 / 5040.0,
+                                        1.0 / 40320.0, 1.0 / 362880.0, 1.0 / 3628800.0};
     if (t > 200.0) return INFINITY;
     if (t < -200.0) return 0.0;
     const double k = nearbyint(t);
     const double g = (t - k) * kLn2;
-    double p = kInvFact[13];
-    for (int j = 12; j >= 0; --j) p = kInvFact[j] + g * p;
-    return ldexp(p, (int)k);
+    double p = kInvFact[10];
+    for (int j = 9; j >= 0; --j) p = fma(g, p, kInvFact[j]);
+    return p * sh_pow2i((int)k);
 }
 
 static float sh_pow(float xf, float yf) {
+    static const double kInvOdd[8] = {1.0,       1.0 / 3.0,  1.0 / 5.0,  1.0 / 7.0,
+                                      1.0 / 9.0, 1.0 / 11.0, 1.0 / 13.0, 1.0 / 15.0};
     if (xf != xf || yf != yf) return NAN;
     if (xf < 0.0f) return NAN;
     if (xf == 0.0f) return yf > 0.0f ? 0.0f : (yf == 0.0f ? 1.0f : INFINITY);
@@ -132,19 +148,19 @@ static float sh_pow(float xf, float yf) {
         m = m * 2.0;
         e = e - 1;
     }
-    const double s = (m - 1.0) / (m + 1.0);
+    const double s = (m - 1.0) * sh_rcp_d(m + 1.0);
     const double s2 = s * s;
-    double series = 1.0 / 15.0;
-    for (int j = 13; j >= 1; j -= 2) series = 1.0 / (double)j + s2 * series;
+    double series = kInvOdd[7];
+    for (int j = 6; j >= 0; --j) series = fma(s2, series, kInvOdd[j]);
     const double lnm = 2.0 * s * series;
-    const double t = (double)yf * ((double)e + lnm / kLn2);
+    const double t = (double)yf * fma(lnm, kInvLn2, (double)e);
     return (float)sh_exp2_d(t);
 }
 
 /* e^x = 2^(x / ln 2) in FP64, rounded once */
 static float sh_exp(float x) {
     if (x != x) return NAN;
-    return (float)sh_exp2_d((double)x / kLn2);
+    return (float)sh_exp2_d((double)x * kInvLn2);
 }
 
 /* ===================================================================== */
