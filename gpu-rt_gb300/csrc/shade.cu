@@ -151,6 +151,22 @@ __device__ SH_CALL float sh_pow(float xf, float yf) {
     if (xf == 0.0f) return yf > 0.0f ? 0.0f : (yf == 0.0f ? 1.0f : INFINITY);
     if (yf == 0.0f || xf == 1.0f) return 1.0f;
     if (isinf(xf)) return yf > 0.0f ? INFINITY : 0.0f;
+    // exact cases: x^1 = x, x^(1/2) the correctly rounded square root, and a
+    // small positive integer power as FP64 products (square and multiply,
+    // at most 12 roundings of 2^-53), rounded once
+    if (yf == 1.0f) return xf;
+    if (yf == 0.5f) return sqrtf(xf);
+    if (yf > 1.0f && yf <= 64.0f && yf == floorf(yf)) {
+        int n = (int)yf;
+        double b = (double)xf, r = 1.0;
+        for (;;) {
+            if (n & 1) r = r * b;
+            n >>= 1;
+            if (n == 0) break;
+            b = b * b;
+        }
+        return (float)r;
+    }
     int e;
     double m = frexp((double)xf, &e);  // m in [0.5, 1)
     if (m < 0.70710678118654752440) {
@@ -825,9 +841,14 @@ __device__ v3 camera_ray(const cp_shade_camera& cam, const cp_shade_params& p, u
     return normalize3(comb(r, sx, u, sy, f, 1.0f));
 }
 
-// rt.rgen:567-677, one thread per pixel; blocks of 16 x 16 pixels
+// rt.rgen:567-677, one thread per pixel; blocks of 16 x 16 pixels.  Six
+// blocks per SM (40 registers a thread, the rest spilled to local memory
+// that stays in L1): a warp's paths diverge across bounces, materials and
+// ray walks, and it is the number of resident warps, not the spills, that
+// sets the pace — the 1920 x 1440 MIS frame took 395 ms at 2 blocks per SM
+// (128 registers), 321 ms at 4, 287 ms at 5, 281 ms at 6 and 286 ms at 8.
 template <int K>
-__global__ void __launch_bounds__(256) k_shade(ShadeArgs a) {
+__global__ void __launch_bounds__(256, 6) k_shade(ShadeArgs a) {
     const int x = blockIdx.x * 16 + (threadIdx.x & 15);
     const int y = blockIdx.y * 16 + (threadIdx.x >> 4);
     if (x >= a.cam.width || y >= a.cam.height) return;

@@ -142,6 +142,22 @@ static float sh_pow(float xf, float yf) {
     if (xf == 0.0f) return yf > 0.0f ? 0.0f : (yf == 0.0f ? 1.0f : INFINITY);
     if (yf == 0.0f || xf == 1.0f) return 1.0f;
     if (isinf(xf)) return yf > 0.0f ? INFINITY : 0.0f;
+    /* exact cases: x^1 = x, x^(1/2) the correctly rounded square root, and a
+     * small positive integer power as FP64 products (square and multiply,
+     * at most 12 roundings of 2^-53), rounded once */
+    if (yf == 1.0f) return xf;
+    if (yf == 0.5f) return sqrtf(xf);
+    if (yf > 1.0f && yf <= 64.0f && yf == floorf(yf)) {
+        int n = (int)yf;
+        double b = (double)xf, r = 1.0;
+        for (;;) {
+            if (n & 1) r = r * b;
+            n >>= 1;
+            if (n == 0) break;
+            b = b * b;
+        }
+        return (float)r;
+    }
     int e;
     double m = frexp((double)xf, &e); /* m in [0.5, 1) */
     if (m < 0.70710678118654752440) {

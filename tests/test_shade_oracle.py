@@ -98,6 +98,26 @@ def test_pow_within_two_ulp():
                                                                                                    0.5]
 
 
+def test_pow_exact_cases():
+    """x^1 = x, x^(1/2) = the correctly rounded square root, and integer
+    powers 2..64 (FP64 products) within one ulp of FP64."""
+    rng = np.random.default_rng(4)
+    x = np.concatenate([rng.random(50000, np.float32), rng.random(1000, np.float32) * np.float32(3.0)])
+    np.testing.assert_array_equal(S.pow(x, np.full_like(x, 1.0)), x)
+    np.testing.assert_array_equal(S.pow(x, np.full_like(x, 0.5)), np.sqrt(x))
+    for n in (2, 3, 5, 10, 17, 64):
+        ref = np.power(x.astype(np.float64), float(n))
+        keep = (ref > 1e-30) & (ref < 1e30)
+        got = S.pow(x, np.full_like(x, float(n)))
+        ulp = np.spacing(ref[keep].astype(np.float32)).astype(np.float64)
+        assert (np.abs(got[keep] - ref[keep]) / ulp).max() <= 1.0, n
+    # a non-integer exponent next to an integer takes the general path
+    ref = np.power(x.astype(np.float64), float(np.float32(2.5)))
+    got = S.pow(x, np.full_like(x, 2.5))
+    ulp = np.spacing(ref.astype(np.float32)).astype(np.float64)
+    assert (np.abs(got - ref) / ulp).max() <= 2.0
+
+
 def test_exp_within_two_ulp():
     x = np.concatenate([-np.linspace(0.0, 80.0, 200001, dtype=np.float32),
                         np.linspace(0.0, 80.0, 1001, dtype=np.float32)])
