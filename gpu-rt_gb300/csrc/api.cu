@@ -833,7 +833,8 @@ CP_API cp_status cp_batch_query(cp_batch* bt, const float* queries, const int64_
     std::vector<uintptr_t> key = {(uintptr_t)queries, (uintptr_t)out_point, (uintptr_t)out_dist,
                                   (uintptr_t)out_tri, (uintptr_t)out_bary, (uintptr_t)workspace,
                                   (uintptr_t)qp.block, (uintptr_t)qp.sort, (uintptr_t)qp.blocks_per_sm,
-                                  (uintptr_t)qp.short_stack, (uintptr_t)qp.traversal, (uintptr_t)nq};
+                                  (uintptr_t)qp.short_stack, (uintptr_t)qp.traversal, (uintptr_t)qp.seed_chunk,
+                                  (uintptr_t)nq};
     for (int i = 0; i <= nm; ++i) key.push_back((uintptr_t)q_offsets[i]);
     if (!bt->exec || key != bt->graph_key) {
         if (bt->exec) {

@@ -96,6 +96,16 @@ def test_batch_synthetic_vs_fp64_and_per_mesh(orc, cpq, cuda):
         torch.cuda.synchronize()
         assert torch.equal(out.dist, r.dist)
         assert torch.equal(out.tri, r.tri)
+    # a replay launches nothing through the library; a changed option
+    # (here the seed chunk) captures a new graph, whose kernels it counts
+    from gpurt_cpq._lib import lib
+    n0 = lib.cp_kernel_launches()
+    b.query(qd, qoff, workspace=ws, use_graph=True, out=out)
+    assert lib.cp_kernel_launches() == n0
+    b.query(qd, qoff, workspace=ws, use_graph=True, out=out, opts=cpq.query_opts(seed_chunk=4))
+    torch.cuda.synchronize()
+    assert lib.cp_kernel_launches() > n0
+    assert torch.equal(out.dist, r.dist)
 
 
 def test_batch_rejects_bad_offsets(cpq, cuda):
