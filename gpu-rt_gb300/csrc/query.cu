@@ -44,13 +44,16 @@ constexpr int kStackTotal = 256;   // >= (K-1)(depth+1) for any 64+32-bit-key LB
 // Packet traversal work claims: `seed_chunk` (a query option) consecutive
 // packets per claim, each packet after a chunk's first seeding its limits from
 // kSeedPoints closest points of the packet before it, then kTailPackets single
-// packets per warp at the end.
+// packets per warp at the end.  The tail trades seeds for balance: on the
+// large heightfield (16M queries, chunks of 4) 16 tail packets per warp
+// took 10.05 ms against 10.25 with 4 and 10.40 with 32; claiming the tail two
+// at a time (half of it seeded) took 10.11.
 #ifndef CPQ_SEED_POINTS
 #define CPQ_SEED_POINTS 16
 #endif
 constexpr int kSeedPoints = CPQ_SEED_POINTS;
 #ifndef CPQ_TAIL_PACKETS
-#define CPQ_TAIL_PACKETS 4
+#define CPQ_TAIL_PACKETS 16
 #endif
 constexpr unsigned long long kTailPackets = CPQ_TAIL_PACKETS;
 static_assert(kSeedPoints == 1 || kSeedPoints == 2 || kSeedPoints == 4 || kSeedPoints == 8 ||
