@@ -1016,6 +1016,44 @@ __device__ __forceinline__ uint64_t hilbert3(uint32_t x, uint32_t y, uint32_t z,
     return (spread3(X[0]) << 2) | (spread3(X[1]) << 1) | spread3(X[2]);
 }
 
+// bit k of a 10-bit x to bit 3k, in 32-bit arithmetic
+__device__ __forceinline__ uint32_t spread3_10(uint32_t x) {
+    x &= 0x3ffu;
+    x = (x | (x << 16)) & 0x030000ffu;
+    x = (x | (x << 8)) & 0x0300f00fu;
+    x = (x | (x << 4)) & 0x030c30c3u;
+    x = (x | (x << 2)) & 0x09249249u;
+    return x;
+}
+
+// hilbert3 for 10 bits per axis (every single-mesh ordering), unrolled, with
+// selects in place of branches and 32-bit bit spreading: the same index.
+__device__ __forceinline__ uint32_t hilbert3_10(uint32_t x, uint32_t y, uint32_t z) {
+    uint32_t X0 = x, X1 = y, X2 = z;
+#pragma unroll
+    for (int b = 9; b >= 1; --b) {
+        const uint32_t Q = 1u << b, P = Q - 1;
+        X0 ^= (X0 & Q) ? P : 0u;
+        const uint32_t t1 = (X0 ^ X1) & P;
+        const bool h1 = (X1 & Q) != 0u;
+        X0 ^= h1 ? P : t1;
+        X1 ^= h1 ? 0u : t1;
+        const uint32_t t2 = (X0 ^ X2) & P;
+        const bool h2 = (X2 & Q) != 0u;
+        X0 ^= h2 ? P : t2;
+        X2 ^= h2 ? 0u : t2;
+    }
+    X1 ^= X0;
+    X2 ^= X1;
+    uint32_t t = 0;
+#pragma unroll
+    for (int b = 9; b >= 1; --b) t ^= (X2 & (1u << b)) ? ((1u << b) - 1u) : 0u;
+    X0 ^= t;
+    X1 ^= t;
+    X2 ^= t;
+    return (spread3_10(X0) << 2) | (spread3_10(X1) << 1) | spread3_10(X2);
+}
+
 // Ordering key of each query: its mesh in the high bits, then the Hilbert
 // index of its cell in the mesh's isotropic query frame.
 template <typename KeyT>
@@ -1034,7 +1072,8 @@ __global__ void k_query_keys(const float* __restrict__ q, int64_t nq, const int6
         t = fminf(fmaxf(t, 0.0f), maxcell);  // NaN -> 0
         c[k] = (uint32_t)t;
     }
-    keys[i] = (KeyT)(((uint64_t)m << (3 * qbits)) | hilbert3(c[0], c[1], c[2], qbits));
+    const uint64_t h = qbits == 10 ? hilbert3_10(c[0], c[1], c[2]) : hilbert3(c[0], c[1], c[2], qbits);
+    keys[i] = (KeyT)(((uint64_t)m << (3 * qbits)) | h);
     vals[i] = (int32_t)i;
 }
 

@@ -10,8 +10,9 @@ tests require:
   one to seven passes, tile-edge sizes, and key sets with degenerate digit
   distributions (all keys equal, already sorted, reversed, a handful of
   values, a narrow band whose high digits are constant);
-* cp_query_order's permutation to sort its Hilbert keys stably, the keys to
-  fit 30 bits, and consecutive queries along it to be close.
+* cp_query_order's keys to equal a restatement of Skilling's Hilbert index
+  over the FP32 query frame, its permutation to sort them stably, and
+  consecutive queries along it to be close.
 """
 from __future__ import annotations
 
@@ -86,6 +87,47 @@ def test_order_sort_large(cuda):
     assert np.array_equal(_sort(k64, 0, 40, cuda), _want(k64, 0, 40))
 
 
+def _hilbert3(x, y, z, bits):
+    """Skilling's 3D Hilbert index (2004, "Programming the Hilbert curve"),
+    vectorised: undo the excess rotations and reflections level by level,
+    Gray-decode, interleave the transposed coordinates (x's bit highest)."""
+    X = [x.astype(np.uint64), y.astype(np.uint64), z.astype(np.uint64)]
+    Q = 1 << (bits - 1)
+    while Q > 1:
+        P = np.uint64(Q - 1)
+        for i in range(3):
+            hi = (X[i] & np.uint64(Q)) != 0
+            t = (X[0] ^ X[i]) & P
+            X[0] = np.where(hi, X[0] ^ P, X[0] ^ t)
+            if i:
+                X[i] = np.where(hi, X[i], X[i] ^ t)
+        Q >>= 1
+    X[1] ^= X[0]
+    X[2] ^= X[1]
+    t = np.zeros_like(X[0])
+    Q = 1 << (bits - 1)
+    while Q > 1:
+        t = np.where((X[2] & np.uint64(Q)) != 0, t ^ np.uint64(Q - 1), t)
+        Q >>= 1
+    X = [v ^ t for v in X]
+    out = np.zeros_like(X[0])
+    for b in range(bits):
+        for j in range(3):
+            out |= ((X[j] >> np.uint64(b)) & np.uint64(1)) << np.uint64(3 * b + 2 - j)
+    return out
+
+
+def _query_cells(q):
+    """Each query's cell in the isotropic 1024^3 frame over the query box, in
+    FP32 as the ordering computes it."""
+    q = q.astype(np.float32)
+    lo, hi = q.min(0), q.max(0)
+    ext = np.float32((hi - lo).max())
+    scale = np.float32(1024.0) / ext
+    t = (q - lo) * scale
+    return np.minimum(np.maximum(t, np.float32(0)), np.float32(1023)).astype(np.uint32)
+
+
 def test_query_order_sorts_its_keys(cpq, cuda):
     import torch
 
@@ -97,6 +139,8 @@ def test_query_order_sorts_its_keys(cpq, cuda):
     perm, keys = m.query_order(torch.from_numpy(q).to(cuda))
     perm, keys = perm.cpu().numpy(), keys.cpu().numpy()
     assert keys.max() < 1 << 30
+    c = _query_cells(q)
+    assert np.array_equal(keys, _hilbert3(c[:, 0], c[:, 1], c[:, 2], 10).astype(np.int64))
     assert np.array_equal(np.sort(perm), np.arange(len(q)))
     assert np.array_equal(perm, np.argsort(keys, kind="stable"))
     # neighbours along the curve are close: far closer than random pairs
