@@ -405,22 +405,48 @@ def our_arm(args):
     value = whole_job_rate(nq * args.steps, world, ms * 1e-3)
     assert mesh.device_status() == 0
 
-    # end to end through the host entry point: pinned buffers, copies inside
+    # end to end through the host entry points: pinned buffers, every step's
+    # upload and download inside the timed region.  Headline: a stream of
+    # batches through cp_query_host_async on two streams taking alternate
+    # steps (double buffering: one step's copies under the other's kernels);
+    # beside it the blocking cp_query_host, one step at a time.
     qh = torch.from_numpy(q).pin_memory()
-    hout = {"dist": torch.empty(nq, dtype=torch.float32).pin_memory(),
-            "tri": torch.empty(nq, dtype=torch.int32).pin_memory(),
-            "point": torch.empty((nq, 3), dtype=torch.float32).pin_memory()}
+
+    def host_outs():
+        return {"dist": torch.empty(nq, dtype=torch.float32).pin_memory(),
+                "tri": torch.empty(nq, dtype=torch.int32).pin_memory(),
+                "point": torch.empty((nq, 3), dtype=torch.float32).pin_memory()}
+
+    hout = [host_outs(), host_outs()]
     e2e_steps = max(1, min(args.steps, 10))
-    mesh.query_host(qh, opts=qopts, out=hout)
+    mesh.query_host(qh, opts=qopts, out=hout[0])
     if world > 1:
         torch.distributed.barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        mesh.query_host(qh, opts=qopts, out=hout)
+        mesh.query_host(qh, opts=qopts, out=hout[0])
+    sync_s = max_over_ranks(time.perf_counter() - t0, world, dev)
+    streams = [torch.cuda.Stream(dev), torch.cuda.Stream(dev)]
+    for k in range(2):
+        mesh.query_host_async(qh, hout[k], opts=qopts, stream=streams[k])
+    for st in streams:
+        st.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        mesh.query_host_async(qh, hout[k % 2], opts=qopts, stream=streams[k % 2])
+    for st in streams:
+        st.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0, world, dev)
+    # the downloaded answers are the device call's
+    assert torch.equal(hout[(e2e_steps - 1) % 2]["dist"], out.dist.cpu())
     e2e = {"value": whole_job_rate(nq * e2e_steps, world, e2e_s), "unit": UNIT,
            "h2d_bytes_per_step": nq * 12, "d2h_bytes_per_step": nq * (12 + 4 + 4),
-           "steps": e2e_steps, "path": "cp_query_host, pinned host buffers"}
+           "steps": e2e_steps,
+           "path": "cp_query_host_async, pinned host buffers, two streams taking alternate steps",
+           "blocking": {"value": whole_job_rate(nq * e2e_steps, world, sync_s), "unit": UNIT,
+                        "path": "cp_query_host, one step at a time (copy in, query, copy out)"}}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

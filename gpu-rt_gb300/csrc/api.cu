@@ -635,6 +635,56 @@ CP_API cp_status cp_query_host(const cp_mesh* m, const float* queries, int64_t n
     return result;
 }
 
+// Pinned (page-locked) host memory, or memory the device maps directly.
+static bool is_pinned_host(const void* p) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeHost;
+}
+
+CP_API cp_status cp_query_host_async(const cp_mesh* m, const float* queries, int64_t nq,
+                                     const cp_query_opts* opts, float* out_point, float* out_dist,
+                                     int32_t* out_tri, float* out_bary, cp_stream_t stream) {
+    if (!m) return fail(CP_ERROR_INVALID_VALUE, "mesh is NULL");
+    if (nq < 0) return fail(CP_ERROR_INVALID_VALUE, "negative query count");
+    if (nq > INT32_MAX) return fail(CP_ERROR_NOT_SUPPORTED, "more than 2^31 - 1 queries in one call");
+    if (nq == 0) return CP_SUCCESS;
+    if (!queries) return fail(CP_ERROR_INVALID_VALUE, "queries is NULL");
+    const void* host[5] = {queries, out_point, out_dist, out_tri, out_bary};
+    for (const void* p : host)
+        if (p && !is_pinned_host(p))
+            return fail(CP_ERROR_INVALID_VALUE,
+                        "cp_query_host_async: every host array must be pinned (cudaHostAlloc / cudaHostRegister)");
+    QueryParams qp;
+    cp_status s = to_query_params(opts, &qp);
+    if (s != CP_SUCCESS) return s;
+    const Bvh& b = m->bvh;
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    const size_t wsb = query_workspace_bytes(b, nq, qp);
+    void* buf[6] = {};  // queries, point, dist, tri, bary, workspace
+    const size_t bytes[6] = {sizeof(float) * 3 * nq, out_point ? sizeof(float) * 3 * nq : 0,
+                             out_dist ? sizeof(float) * nq : 0, out_tri ? sizeof(int32_t) * nq : 0,
+                             out_bary ? sizeof(float) * 2 * nq : 0, wsb};
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 6 && e == cudaSuccess; ++k)
+        if (bytes[k]) e = ws_alloc(&buf[k], bytes[k], st);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(buf[0], queries, bytes[0], cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = bvh_query(b, static_cast<float*>(buf[0]), nq, nullptr, qp, static_cast<float*>(buf[1]),
+                      static_cast<float*>(buf[2]), static_cast<int32_t*>(buf[3]), static_cast<float*>(buf[4]), buf[5],
+                      wsb, st);
+    void* outs[4] = {out_point, out_dist, out_tri, out_bary};
+    for (int k = 0; k < 4 && e == cudaSuccess; ++k)
+        if (outs[k]) e = cudaMemcpyAsync(outs[k], buf[k + 1], bytes[k + 1], cudaMemcpyDeviceToHost, st);
+    for (void* p : buf)
+        if (p) cudaFreeAsync(p, st);
+    if (e != cudaSuccess) return cuda_fail(e, "cp_query_host_async");
+    return CP_SUCCESS;
+}
+
 CP_API cp_status cp_backward(const cp_mesh* m, const float* queries, const int32_t* tri,
                              const float* bary, const float* grad_dist, int64_t nq,
                              float* grad_queries, float* grad_verts, cp_stream_t stream) {

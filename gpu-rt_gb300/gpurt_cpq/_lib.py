@@ -97,6 +97,8 @@ SIGNATURES = {
     "cp_query_workspace_size": (c_int32, [c_void_p, c_int64, POINTER(QueryOpts), POINTER(c_size_t)]),
     "cp_query": (c_int32, [c_void_p, c_void_p, c_int64, POINTER(QueryOpts), c_void_p, c_void_p,
                            c_void_p, c_void_p, c_void_p, c_size_t, c_void_p]),
+    "cp_query_host_async": (c_int32, [c_void_p, c_void_p, c_int64, POINTER(QueryOpts), c_void_p, c_void_p,
+                                      c_void_p, c_void_p, c_void_p]),
     "cp_query_host": (c_int32, [c_void_p, c_void_p, c_int64, POINTER(QueryOpts), c_void_p, c_void_p,
                                 c_void_p, c_void_p, c_void_p]),
     "cp_query_noalloc": (c_int32, [c_void_p, c_void_p, c_int64, POINTER(QueryOpts), c_void_p,

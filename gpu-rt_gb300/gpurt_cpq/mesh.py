@@ -259,6 +259,20 @@ class Mesh:
                                 _stream()), "cp_query_host")
         return out
 
+    def query_host_async(self, points: torch.Tensor, out: dict, *, opts: QueryOpts | None = None,
+                         stream=None) -> dict:
+        """cp_query_host_async: pinned host tensors in and out, enqueued on
+        `stream` (default: the current stream); the outputs are ready when the
+        stream has reached this call.  `out` holds "dist", "tri" and
+        optionally "point" and "bary"."""
+        if points.is_cuda or points.dtype != torch.float32 or not points.is_contiguous():
+            raise ValueError("points must be a contiguous float32 CPU tensor")
+        o = opts or query_opts()
+        check(lib.cp_query_host_async(self._h, _ptr(points), int(points.shape[0]), byref(o),
+                                      _ptr(out.get("point")), _ptr(out["dist"]), _ptr(out["tri"]),
+                                      _ptr(out.get("bary")), _stream(stream)), "cp_query_host_async")
+        return out
+
     def refit(self, verts: torch.Tensor, stream=None) -> None:
         if not verts.is_cuda or verts.dtype != torch.float32 or verts.shape[0] != self.num_vertices:
             raise ValueError("verts must be a CUDA float32 tensor with the mesh's vertex count")

@@ -271,6 +271,25 @@ CP_API cp_status cp_query_host(const cp_mesh* mesh, const float* queries, int64_
                                const cp_query_opts* opts, float* out_point, float* out_dist,
                                int32_t* out_tri, float* out_bary, cp_stream_t stream);
 
+/*
+ * cp_query_host without the wait: enqueues on `stream` the copy of the
+ * queries to the device, the query (all nq as one ordered set) and the copies
+ * of the results back, and returns.  The outputs are ready once the stream
+ * reaches this point (synchronise it, or an event recorded after the call);
+ * until then the caller must neither change the queries nor read or reuse
+ * the outputs.  The host arrays must be pinned (cudaHostAlloc /
+ * cudaHostRegister; anything else is refused with CP_ERROR_INVALID_VALUE, as
+ * a copy from pageable memory would not be asynchronous).  Device buffers
+ * come from the library's stream-ordered pool and go back to it in stream
+ * order.  Calls on different streams overlap: with two streams taking
+ * alternate batches, one batch's copies run while the other's kernels do, so
+ * a stream of batches costs about the device time per batch.  nq up to
+ * 2^31 - 1.
+ */
+CP_API cp_status cp_query_host_async(const cp_mesh* mesh, const float* queries, int64_t nq,
+                                     const cp_query_opts* opts, float* out_point, float* out_dist,
+                                     int32_t* out_tri, float* out_bary, cp_stream_t stream);
+
 /* ---- glTF ingest (host) ---------------------------------------------------- */
 
 /*

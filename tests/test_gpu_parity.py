@@ -473,6 +473,48 @@ def test_host_buffers_two_chunks(cpq, cuda):
     del d, h
 
 
+def test_host_buffers_async_two_streams(cpq, cuda):
+    """cp_query_host_async: batches alternating over two streams (one batch's
+    copies under the other's kernels) give the device call's answers bit for
+    bit; every output set is written by its own batch; unpinned host arrays
+    are refused before anything is enqueued."""
+    import torch
+
+    from gpurt_cpq import CpError
+    from gpurt_cpq import workloads as W
+    from gpurt_cpq._lib import CP_ERROR_INVALID_VALUE
+
+    v, t = W.torus(100, 40)
+    m = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=4)
+    batches = [torch.from_numpy(W.uniform_queries(150_000 + 1000 * k, -1.5, 1.5, 20 + k)).pin_memory()
+               for k in range(5)]
+    want = [m.query(b.to(cuda), want_bary=True) for b in batches]
+    streams = [torch.cuda.Stream(), torch.cuda.Stream()]
+
+    def outs(n):
+        return {"dist": torch.full((n,), -1.0).pin_memory(), "tri": torch.full((n,), -7, dtype=torch.int32).pin_memory(),
+                "point": torch.empty((n, 3)).pin_memory(), "bary": torch.empty((n, 2)).pin_memory()}
+
+    got = [outs(b.shape[0]) for b in batches]
+    for k, b in enumerate(batches):
+        m.query_host_async(b, got[k], stream=streams[k % 2])
+    for s in streams:
+        s.synchronize()
+    for g, w in zip(got, want):
+        assert torch.equal(g["dist"], w.dist.cpu())
+        assert torch.equal(g["tri"], w.tri.cpu())
+        assert torch.equal(g["point"], w.point.cpu())
+        assert torch.equal(g["bary"], w.bary.cpu())
+    # pageable input or output: refused
+    with pytest.raises(CpError) as e:
+        m.query_host_async(batches[0].clone(), outs(batches[0].shape[0]))
+    assert e.value.status == CP_ERROR_INVALID_VALUE
+    page = {"dist": torch.empty(batches[0].shape[0]), "tri": torch.empty(batches[0].shape[0], dtype=torch.int32)}
+    with pytest.raises(CpError):
+        m.query_host_async(batches[0], page)
+    assert m.device_status() == 0
+
+
 def test_refit_moves_vertices(orc, cpq, cuda):
     from gpurt_cpq import workloads as W
 
