@@ -512,6 +512,21 @@ def test_host_buffers_async_two_streams(cpq, cuda):
     page = {"dist": torch.empty(batches[0].shape[0]), "tri": torch.empty(batches[0].shape[0], dtype=torch.int32)}
     with pytest.raises(CpError):
         m.query_host_async(batches[0], page)
+    # each of the call's device allocations failing in turn: out of memory,
+    # what it held released, and the next call answers
+    from gpurt_cpq._lib import CP_ERROR_OUT_OF_MEMORY, lib
+    for k in range(6):
+        lib.cp_debug_fail_allocation(k)
+        try:
+            with pytest.raises(CpError) as e:
+                m.query_host_async(batches[0], got[0])
+            assert e.value.status == CP_ERROR_OUT_OF_MEMORY, k
+        finally:
+            lib.cp_debug_fail_allocation(-1)
+    torch.cuda.synchronize()
+    m.query_host_async(batches[1], got[1])
+    torch.cuda.synchronize()
+    assert torch.equal(got[1]["dist"], want[1].dist.cpu())
     assert m.device_status() == 0
 
 
