@@ -8,8 +8,9 @@
 // products summed left to right; normalize(v) = v / length(v);
 // reflect(i, n) = i - 2 dot(n, i) n; mix(x, y, a) = x (1 - a) + y a).  sin,
 // cos, pow and exp, which GLSL leaves to the implementation, are the
-// restatement's own (shade_oracle.c), as is the scene tracer behind
-// traceRayEXT.  Compile with -ffp-contract=off.
+// restatement's own (shade_oracle.c), as are the scene tracer behind
+// traceRayEXT and the filtering of the material textures.  Compile with
+// -ffp-contract=off.
 #pragma once
 
 #include <cmath>
@@ -193,17 +194,25 @@ inline bool all(bvec2 v) { return v.x && v.y; }
 inline bool any(bvec3 v) { return v.x || v.y || v.z; }
 
 // ---- resources --------------------------------------------------------------
-// RGBA float images; a sampler reads its nearest texel with repeat
-// addressing (the G-buffer sampler of rt.cpp:449-450, vulkan.cpp:522-531)
+// RGBA float images read at their nearest texel with repeat addressing (the
+// G-buffer sampler of rt.cpp:449-450, vulkan.cpp:522-531), or RGBA8 sRGB
+// material textures (`texels`: rt.cpp:439-447's images and linear sampler)
+// through the restatement's texture()
 struct sampler2D {
     const float* data;
     int w, h;
+    const unsigned char* texels = nullptr;
 };
 struct image2D {
     float* data;
     int w, h;
 };
 inline vec4 texture(const sampler2D& s, vec2 uv) {
+    if (s.texels) {
+        float o[4];
+        orc_sh_texture(s.w, s.h, s.texels, uv.x, uv.y, o);
+        return vec4(o[0], o[1], o[2], o[3]);
+    }
     if (!s.data) return vec4();
     const int i = ((int)std::floor(uv.x * (float)s.w) % s.w + s.w) % s.w;
     const int j = ((int)std::floor(uv.y * (float)s.h) % s.h + s.h) % s.h;

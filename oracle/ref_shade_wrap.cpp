@@ -181,15 +181,27 @@ int ref_render(const orc_shade_scene* s, const orc_shade_camera* cam, const orc_
         so.emissive = vec4(ld3(s->emissive + 3 * o), 0.0f);
         so.metal_rough = vec4(s->metal_rough[2 * o], s->metal_rough[2 * o + 1], 0.0f, 0.0f);
         so.albedo_tex = so.emissive_tex = so.metal_rough_tex = so.normal_tex = -1;
+        if (s->obj_tex) {
+            so.albedo_tex = s->obj_tex[4 * o];
+            so.emissive_tex = s->obj_tex[4 * o + 1];
+            so.metal_rough_tex = s->obj_tex[4 * o + 2];
+            so.normal_tex = s->obj_tex[4 * o + 3];
+        }
         so.index = (uint)o;
         float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
         for (int64_t k = 0; k < count[o]; ++k)
             for (int j = 0; j < 3; ++j) {
                 const float* pv = s->verts + 9 * (g_first[o] + k) + 3 * j;
+                const int64_t t = g_first[o] + k;
+                const float* tc = s->texcoords ? s->texcoords + 6 * t + 2 * j : nullptr;
                 Vertex vx;
-                vx.pos_tx = vec4(ld3(pv), 0.0f);
-                vx.norm_ty = vec4(ld3(s->normals + 9 * (g_first[o] + k) + 3 * j), 0.0f);
+                vx.pos_tx = vec4(ld3(pv), tc ? tc[0] : 0.0f);
+                vx.norm_ty = vec4(ld3(s->normals + 9 * t + 3 * j), tc ? tc[1] : 0.0f);
                 vx.tangent = vec4();
+                if (s->tangents) {
+                    const float* tg = s->tangents + 12 * t + 4 * j;
+                    vx.tangent = vec4(tg[0], tg[1], tg[2], tg[3]);
+                }
                 vtx[o].push_back(vx);
                 idx[o].push_back((uint)(3 * k + j));
                 for (int a = 0; a < 3; ++a) {
@@ -213,7 +225,10 @@ int ref_render(const orc_shade_scene* s, const orc_shade_camera* cam, const orc_
     lights = lts.data();
     vertices = vb.data();
     indices = ib.data();
-    Textures = nullptr;
+    std::vector<sampler2D> texs((size_t)(s->ntex > 0 ? s->ntex : 0));
+    for (int32_t k = 0; k < s->ntex; ++k)
+        texs[k] = sampler2D{nullptr, s->tex_size[2 * k], s->tex_size[2 * k + 1], s->texels + 4 * s->tex_off[k]};
+    Textures = texs.empty() ? nullptr : texs.data();
 
     consts.clear_col = vec4(ld3(p->clear), 1.0f);
     consts.env_light = vec4(ld3(p->env), 1.0f);
@@ -222,7 +237,7 @@ int ref_render(const orc_shade_scene* s, const orc_shade_camera* cam, const orc_
     consts.max_frame = p->max_frame;
     consts.qmc = p->qmc;
     consts.max_depth = p->max_depth;
-    consts.use_normal_map = 0;
+    consts.use_normal_map = p->use_normal_map;
     consts.use_metalness = p->use_metalness;
     consts.use_temporal = p->use_temporal;
     consts.integrator = p->integrator;

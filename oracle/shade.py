@@ -29,7 +29,9 @@ DIRECT, MATERIAL, MIS, RESTIR_DIRECT, RESTIR = range(5)
 
 class ShadeScene(Structure):
     _fields_ = [("nt", c_int64), ("verts", c_void_p), ("normals", c_void_p), ("obj", c_void_p),
-                ("nobj", c_int32), ("albedo", c_void_p), ("emissive", c_void_p), ("metal_rough", c_void_p)]
+                ("nobj", c_int32), ("albedo", c_void_p), ("emissive", c_void_p), ("metal_rough", c_void_p),
+                ("texcoords", c_void_p), ("tangents", c_void_p), ("obj_tex", c_void_p), ("ntex", c_int32),
+                ("tex_size", c_void_p), ("tex_off", c_void_p), ("texels", c_void_p)]
 
 
 class ShadeCamera(Structure):
@@ -42,7 +44,7 @@ class ShadeParams(Structure):
                 ("qmc", c_int32), ("integrator", c_int32), ("brdf", c_int32), ("use_rr", c_int32),
                 ("use_metalness", c_int32), ("frame", c_int32), ("max_frame", c_int32),
                 ("new_samples", c_int32), ("temporal_multiplier", c_int32), ("use_temporal", c_int32),
-                ("debug_view", c_int32), ("seed", c_uint32)]
+                ("debug_view", c_int32), ("seed", c_uint32), ("use_normal_map", c_int32)]
 
 
 class ShadeTemporal(Structure):
@@ -260,22 +262,56 @@ def make_tanspace(n, ref: bool = False):
     return t, b
 
 
-class Scene:
-    """World-space triangles with per-vertex normals and one constant material
-    per object (albedo, emission, metalness, roughness); an object whose
-    emission has a component above zero is a light.  Objects' triangles are
-    contiguous."""
+def texture_pack(images):
+    """RGBA8 images (h, w, 4) uint8 -> (tex_size (n, 2) [w, h], tex_off (n + 1), texels)."""
+    images = [np.ascontiguousarray(im, np.uint8) for im in images]
+    for im in images:
+        assert im.ndim == 3 and im.shape[2] == 4 and im.shape[0] > 0 and im.shape[1] > 0
+    size = np.asarray([[im.shape[1], im.shape[0]] for im in images], np.int32).reshape(-1, 2)
+    off = np.zeros(len(images) + 1, np.int64)
+    off[1:] = np.cumsum([im.shape[0] * im.shape[1] for im in images])
+    texels = np.concatenate([im.reshape(-1) for im in images]) if images else np.zeros(4, np.uint8)
+    return size, off, np.ascontiguousarray(texels)
 
-    def __init__(self, verts, normals, obj, albedo, emissive, metal_rough):
+
+class Scene:
+    """World-space triangles with per-vertex normals and a material per object
+    (albedo, emission, metalness, roughness factors); an object whose
+    emission factor has a component above zero is a light.  Objects'
+    triangles are contiguous.  Optional: per-vertex texture coordinates
+    (nt, 3, 2) and tangents (nt, 3, 4: xyz, w), RGBA8 sRGB textures (a list of
+    (h, w, 4) uint8 images) and per object the texture replacing each factor
+    (obj_tex (nobj, 4): albedo, emissive, metal_rough, normal; -1 none)."""
+
+    def __init__(self, verts, normals, obj, albedo, emissive, metal_rough, *, texcoords=None, tangents=None,
+                 textures=None, obj_tex=None):
         self.verts = np.ascontiguousarray(np.asarray(verts, np.float32).reshape(-1, 9))
         self.normals = np.ascontiguousarray(np.asarray(normals, np.float32).reshape(-1, 9))
         self.obj = np.ascontiguousarray(obj, np.int32)
         self.albedo = np.ascontiguousarray(np.asarray(albedo, np.float32).reshape(-1, 3))
         self.emissive = np.ascontiguousarray(np.asarray(emissive, np.float32).reshape(-1, 3))
         self.metal_rough = np.ascontiguousarray(np.asarray(metal_rough, np.float32).reshape(-1, 2))
-        self._s = ShadeScene(self.verts.shape[0], self.verts.ctypes.data, self.normals.ctypes.data,
+        nt = self.verts.shape[0]
+        self.texcoords = None if texcoords is None else np.ascontiguousarray(
+            np.asarray(texcoords, np.float32).reshape(nt, 6))
+        self.tangents = None if tangents is None else np.ascontiguousarray(
+            np.asarray(tangents, np.float32).reshape(nt, 12))
+        self.textures = list(textures or [])
+        self.obj_tex = None if obj_tex is None else np.ascontiguousarray(
+            np.asarray(obj_tex, np.int32).reshape(-1, 4))
+        if self.obj_tex is not None:
+            assert self.obj_tex.shape[0] == self.albedo.shape[0]
+            assert self.obj_tex.max() < len(self.textures) and self.obj_tex.min() >= -1
+        self.tex_size, self.tex_off, self.texels = texture_pack(self.textures)
+
+        def ptr(a):
+            return None if a is None else a.ctypes.data
+
+        self._s = ShadeScene(nt, self.verts.ctypes.data, self.normals.ctypes.data,
                              self.obj.ctypes.data, self.albedo.shape[0], self.albedo.ctypes.data,
-                             self.emissive.ctypes.data, self.metal_rough.ctypes.data)
+                             self.emissive.ctypes.data, self.metal_rough.ctypes.data, ptr(self.texcoords),
+                             ptr(self.tangents), ptr(self.obj_tex), len(self.textures), self.tex_size.ctypes.data,
+                             self.tex_off.ctypes.data, self.texels.ctypes.data)
 
     def light_pdf(self, p, d) -> np.ndarray:
         pp, dd = _v3(p), _v3(d)
@@ -287,7 +323,7 @@ class Scene:
                use_rr=True, qmc=False, use_metalness=False, frame=0, max_frame=256, new_samples=4,
                temporal_multiplier=16, use_temporal=True, debug_view=0, clear=(0.3, 0.3, 0.3),
                env=(0.0, 0.0, 0.0), seed=1, image=None, gbuffer=False, temporal: TemporalState | None = None,
-               ref: bool = False):
+               use_normal_map=False, ref: bool = False):
         """One frame, the reference's defaults unless given (rt.h:38-53;
         env_scale 0).  Returns the image (height, width, 3) and, if asked,
         the first-hit buffer (height, width, 9).  `temporal` carries ReSTIR's
@@ -296,7 +332,7 @@ class Scene:
         (make_ref_shade.py) instead of the restatement."""
         p = ShadeParams((c_float * 3)(*clear), (c_float * 3)(*env), samples, max_depth, int(qmc), integrator,
                         brdf, int(use_rr), int(use_metalness), frame, max_frame, new_samples,
-                        temporal_multiplier, int(use_temporal), debug_view, seed)
+                        temporal_multiplier, int(use_temporal), debug_view, seed, int(use_normal_map))
         img = np.zeros((camera.height, camera.width, 3), np.float32) if image is None else image
         assert img.dtype == np.float32 and img.flags.c_contiguous and img.shape == (camera.height, camera.width, 3)
         g = np.zeros((camera.height, camera.width, 9), np.float32) if gbuffer else None
@@ -306,6 +342,26 @@ class Scene:
         if rc != 0:
             raise ValueError("orc_sh_render refused its arguments")
         return (img, g) if gbuffer else img
+
+
+def texture(image, u, v) -> np.ndarray:
+    """The restatement's texture() on one RGBA8 sRGB image at arrays of
+    (u, v): (n, 4) float32."""
+    im = np.ascontiguousarray(image, np.uint8)
+    u = np.ascontiguousarray(u, np.float32).reshape(-1)
+    v = np.ascontiguousarray(v, np.float32).reshape(-1)
+    out = np.empty((u.shape[0], 4), np.float32)
+    fn = _L().orc_sh_texture
+    for i in range(u.shape[0]):
+        fn(im.shape[1], im.shape[0], _p(im), c_float(u[i]), c_float(v[i]), _p(out[i]))
+    return out
+
+
+def srgb_decode() -> np.ndarray:
+    """The restatement's sRGB decode of each 8-bit value (256 floats)."""
+    fn = _L().orc_sh_srgb_decode
+    fn.restype = c_float
+    return np.asarray([fn(i) for i in range(256)], np.float32)
 
 
 def camera(eye, target, up, yfov: float, width: int, height: int) -> ShadeCamera:

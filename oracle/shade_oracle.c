@@ -330,6 +330,8 @@ static int hit_bbox(v3 o, v3 d, v3 bmin, v3 bmax) {
 typedef struct {
     v3 albedo, emissive;
     float roughness;
+    int use_tanspace; /* the object has a normal texture */
+    v3 tn;            /* its tangent-space normal at the hit */
 } mat_info;
 
 typedef struct {
@@ -421,6 +423,66 @@ static int mat_sample(int brdf, uint32_t* seed, const mat_info* m, const shade_i
 /* ===================================================================== */
 /* scene access                                                           */
 /* ===================================================================== */
+
+/* ===================================================================== */
+/* textures (rt.rgen:100-129; images RGBA8 sRGB, linear filter, repeat)    */
+/* ===================================================================== */
+
+/* sRGB to linear of one 8-bit value, with this file's pow */
+float orc_sh_srgb_decode(uint32_t byte) {
+    const float c = (float)(byte & 255u) / 255.0f;
+    return c <= 0.04045f ? c / 12.92f : sh_pow((c + 0.055f) / 1.055f, 2.4f);
+}
+
+static float g_srgb[256];
+static pthread_once_t g_srgb_once = PTHREAD_ONCE_INIT;
+static void srgb_init(void) {
+    for (uint32_t i = 0; i < 256; ++i) g_srgb[i] = orc_sh_srgb_decode(i);
+}
+
+/* x mod 1 in [0, 1); NaN, the infinities and a difference that rounds up to
+ * 1 give 0 */
+static float wrap01(float x) {
+    float f = x - floorf(x);
+    if (!(f >= 0.0f && f < 1.0f)) f = 0.0f;
+    return f;
+}
+
+static void texel(const uint8_t* texels, int64_t i, float t[4]) {
+    for (int k = 0; k < 3; ++k) t[k] = g_srgb[texels[4 * i + k]];
+    t[3] = (float)texels[4 * i + 3] / 255.0f;
+}
+
+/* bilinear blend at level 0 of the four texels around (u mod 1) w - 1/2,
+ * (v mod 1) h - 1/2, neighbours wrapping around the edges */
+void orc_sh_texture(int32_t w, int32_t h, const uint8_t* texels, float u, float v, float out[4]) {
+    pthread_once(&g_srgb_once, srgb_init);
+    const float fx = wrap01(u) * (float)w - 0.5f, fy = wrap01(v) * (float)h - 0.5f;
+    const float x0 = floorf(fx), y0 = floorf(fy);
+    const float ax = fx - x0, ay = fy - y0;
+    int i0 = (int)x0, j0 = (int)y0; /* in [-1, w - 1] and [-1, h - 1] */
+    if (i0 < 0) i0 = w - 1;
+    if (j0 < 0) j0 = h - 1;
+    const int i1 = i0 + 1 == w ? 0 : i0 + 1, j1 = j0 + 1 == h ? 0 : j0 + 1;
+    float t00[4], t10[4], t01[4], t11[4];
+    texel(texels, (int64_t)j0 * w + i0, t00);
+    texel(texels, (int64_t)j0 * w + i1, t10);
+    texel(texels, (int64_t)j1 * w + i0, t01);
+    texel(texels, (int64_t)j1 * w + i1, t11);
+    for (int k = 0; k < 4; ++k)
+        out[k] = (t00[k] * (1.0f - ax) + t10[k] * ax) * (1.0f - ay) + (t01[k] * (1.0f - ax) + t11[k] * ax) * ay;
+}
+
+/* texture `tex` of the scene at (u, v) */
+static void scene_tex(const orc_shade_scene* s, int32_t tex, float u, float v, float out[4]) {
+    orc_sh_texture(s->tex_size[2 * tex], s->tex_size[2 * tex + 1], s->texels + 4 * s->tex_off[tex], u, v, out);
+}
+
+/* the object's texture of kind k (0 albedo, 1 emissive, 2 metal_rough,
+ * 3 normal), or -1 */
+static inline int32_t obj_tex(const orc_shade_scene* s, int32_t o, int k) {
+    return s->obj_tex ? s->obj_tex[4 * o + k] : -1;
+}
 
 typedef struct {
     int32_t obj;
@@ -536,39 +598,82 @@ static int occluded(const orc_shade_scene* s, v3 a, v3 b) {
 }
 
 typedef struct {
-    v3 pos, normal;
+    v3 pos, normal, tangent;
+    float tc[2];
 } hit_info;
 
-/* interpolated world position and unit normal at a hit (rt.rgen:64-98) */
+static inline v3 tng(const orc_shade_scene* s, int64_t t, int j) {
+    if (!s->tangents) return mk(0.0f, 0.0f, 0.0f);
+    const float* q = s->tangents + 12 * t + 4 * j;
+    return scl(ld(q), q[3]);
+}
+static inline float tcd(const orc_shade_scene* s, int64_t t, int j, int k) {
+    return s->texcoords ? s->texcoords[6 * t + 2 * j + k] : 0.0f;
+}
+
+/* interpolated world position, unit normal, unit tangent and texture
+ * coordinates at a hit (rt.rgen:62-95; the model matrices are the identity
+ * for world-space triangles) */
 static hit_info make_hit_info(const orc_shade_scene* s, const hit_rec* h) {
     const float bx = 1.0f - h->u - h->v, by = h->u, bz = h->v;
     hit_info r;
     r.normal = normalize3(comb(nrm(s, h->tri, 0), bx, nrm(s, h->tri, 1), by, nrm(s, h->tri, 2), bz));
+    r.tangent = normalize3(comb(tng(s, h->tri, 0), bx, tng(s, h->tri, 1), by, tng(s, h->tri, 2), bz));
     r.pos = comb(vert(s, h->tri, 0), bx, vert(s, h->tri, 1), by, vert(s, h->tri, 2), bz);
+    for (int k = 0; k < 2; ++k)
+        r.tc[k] = tcd(s, h->tri, 0, k) * bx + tcd(s, h->tri, 1, k) * by + tcd(s, h->tri, 2, k) * bz;
     return r;
 }
 
-/* constant material of the hit object (rt.rgen:100-129, without textures) */
-static mat_info make_mat_info(const ctx_t* c, int32_t o) {
+/* material of the hit object at texture coordinates tc: each factor, or its
+ * texture where the object has one (rt.rgen:97-129) */
+static mat_info make_mat_info(const ctx_t* c, int32_t o, const float tc[2]) {
     const orc_shade_scene* s = c->s;
     mat_info m;
+    float t[4];
     m.albedo = ld(s->albedo + 3 * o);
+    if (obj_tex(s, o, 0) >= 0) {
+        scene_tex(s, obj_tex(s, o, 0), tc[0], tc[1], t);
+        m.albedo = mk(t[0], t[1], t[2]);
+    }
     m.emissive = ld(s->emissive + 3 * o);
-    const float metal = s->metal_rough[2 * o], rough = s->metal_rough[2 * o + 1];
+    if (obj_tex(s, o, 1) >= 0) {
+        scene_tex(s, obj_tex(s, o, 1), tc[0], tc[1], t);
+        m.emissive = mk(t[0], t[1], t[2]);
+    }
+    float metal = s->metal_rough[2 * o], rough = s->metal_rough[2 * o + 1];
+    if (obj_tex(s, o, 2) >= 0) {
+        scene_tex(s, obj_tex(s, o, 2), tc[0], tc[1], t);
+        metal = t[0];
+        rough = t[1];
+    }
     m.roughness = rough;
     if (c->p->use_metalness) { /* mix(vec3(0.04), albedo, metal) */
         m.albedo = mk(0.04f * (1.0f - metal) + m.albedo.x * metal, 0.04f * (1.0f - metal) + m.albedo.y * metal,
                       0.04f * (1.0f - metal) + m.albedo.z * metal);
     }
+    m.use_tanspace = obj_tex(s, o, 3) >= 0;
+    m.tn = mk(0.0f, 0.0f, 0.0f);
+    if (m.use_tanspace) { /* texture(...).xyz * 2.0 - 1.0 */
+        scene_tex(s, obj_tex(s, o, 3), tc[0], tc[1], t);
+        m.tn = mk(t[0] * 2.0f - 1.0f, t[1] * 2.0f - 1.0f, t[2] * 2.0f - 1.0f);
+    }
     return m;
 }
 
-/* shading frame facing the incoming ray (rt.rgen:131-148) */
-static shade_info make_shade_info(v3 wo, v3 normal) {
+/* shading frame facing the incoming ray, the normal bent by the normal
+ * map when it is on (rt.rgen:131-148) */
+static shade_info make_shade_info(const ctx_t* c, v3 wo, const hit_info* hit, const mat_info* m) {
     shade_info sh;
     sh.wo = wo;
+    v3 normal = hit->normal;
     if (dot(sh.wo, normal) > 0.0f) normal = neg(normal);
+    sh.t = hit->tangent;
     sh.n = normal;
+    if (m->use_tanspace && c->p->use_normal_map == 1) { /* N = normalize(mat3(T, B, N) * tn) */
+        sh.b = cross(sh.n, sh.t);
+        sh.n = normalize3(add(add(scl(sh.t, m->tn.x), scl(sh.b, m->tn.y)), scl(sh.n, m->tn.z)));
+    }
     make_tanspace(sh.n, &sh.t, &sh.b);
     return sh;
 }
@@ -592,6 +697,15 @@ static light_sample_t light_sample(const ctx_t* c, uint32_t* seed, v3 p) {
     light_sample_t r;
     r.pos = comb(v0, bary.x, v1, bary.y, v2, bary.z);
     r.emissive = ld(s->emissive + 3 * L->obj);
+    if (obj_tex(s, L->obj, 1) >= 0) {
+        /* the shader's coordinates: u interpolated, v vertex 1's at every
+         * corner (rt.rgen:175) */
+        const float tu = tcd(s, t, 0, 0) * bary.x + tcd(s, t, 1, 0) * bary.y + tcd(s, t, 2, 0) * bary.z;
+        const float tv = tcd(s, t, 1, 1) * bary.x + tcd(s, t, 1, 1) * bary.y + tcd(s, t, 1, 1) * bary.z;
+        float e[4];
+        scene_tex(s, obj_tex(s, L->obj, 1), tu, tv, e);
+        r.emissive = mk(e[0], e[1], e[2]);
+    }
     const v3 narea = cross(sub(v1, v0), sub(v2, v0));
     const float a = 2.0f / length3(narea);
     const v3 dist = sub(r.pos, p);
@@ -642,7 +756,8 @@ typedef struct {
 static v3 direct_light(const ctx_t* c, v3 o, v3 d) {
     const hit_rec h = trace(c->s, o, d, SH_EPS, SH_LARGE_DIST, 0);
     if (!h.hit) return ld(c->p->env);
-    return ld(c->s->emissive + 3 * c->s->obj[h.tri]);
+    const hit_info hit = make_hit_info(c->s, &h);
+    return make_mat_info(c, c->s->obj[h.tri], hit.tc).emissive;
 }
 
 /* rt.rgen:301-355 */
@@ -977,8 +1092,8 @@ static void render_pixel(const ctx_t* c, const orc_shade_camera* cam, int x, int
                 break;
             }
             const hit_info hit = make_hit_info(s, &h);
-            const mat_info m = make_mat_info(c, s->obj[h.tri]);
-            const shade_info sh = make_shade_info(tr.d, hit.normal);
+            const mat_info m = make_mat_info(c, s->obj[h.tri], hit.tc);
+            const shade_info sh = make_shade_info(c, tr.d, &hit, &m);
             if (smp == 0 && tr.depth == 0) {
                 g_pos = hit.pos;
                 g_norm = sh.n;

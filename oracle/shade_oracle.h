@@ -20,10 +20,15 @@
  *    clock (rt.rgen:569);
  *  - a new reservoir's sample (position, normal, emission) starts at zero
  *    (restir.glsl:29-35 leaves it undefined);
- *  - scenes are world-space triangles with per-vertex world normals and a
- *    constant material per object (no textures, no normal maps: the
- *    shader's tangent is replaced by make_tanspace before any use,
- *    rt.rgen:145, so it is not an input);
+ *  - scenes are world-space triangles with per-vertex world normals,
+ *    texture coordinates and tangents, and a material per object whose
+ *    factors (albedo, emission, metalness / roughness) may be replaced by
+ *    textures, with an optional normal map (rt.rgen:100-129, 131-148);
+ *  - texture() on the reference's material textures (RGBA8 sRGB images, one
+ *    level, linear filter, repeat addressing: rt.cpp:439-447) is this file's
+ *    own: each texel's colour decoded from sRGB with this file's pow
+ *    (alpha as stored / 255), then a bilinear blend at level 0 of the four
+ *    texels around (u mod 1) w - 1/2, (v mod 1) h - 1/2, in a fixed order;
  *  - the closest hit is the nearest Möller-Trumbore hit over all triangles
  *    with t in [1e-5, 1e7] (the shader's EPS and LARGE_DIST, rt.rgen:257-269),
  *    a zero determinant counting as a miss; barycentrics (1-u-v, u, v) as
@@ -52,6 +57,14 @@ typedef struct {
     const float* albedo;    /* nobj x 3 */
     const float* emissive;  /* nobj x 3; an object with any component > 0 is a light */
     const float* metal_rough; /* nobj x 2: metalness, roughness */
+    /* optional (NULL / 0: none) */
+    const float* texcoords;   /* nt x 3 vertices x (u, v) */
+    const float* tangents;    /* nt x 3 vertices x (xyz, w): the tangent is xyz * w */
+    const int32_t* obj_tex;   /* nobj x 4: albedo, emissive, metal_rough, normal texture, or -1 */
+    int32_t ntex;
+    const int32_t* tex_size;  /* ntex x (width, height) */
+    const int64_t* tex_off;   /* ntex + 1 texel offsets into texels */
+    const uint8_t* texels;    /* RGBA8 texels, sRGB colour, row 0 first */
 } orc_shade_scene;
 
 typedef struct {
@@ -77,6 +90,7 @@ typedef struct {
     int32_t use_temporal;  /* ReSTIR: reuse the previous frame's reservoirs (rt.rgen:456-479) */
     int32_t debug_view;    /* 1, 2, 3: write the previous frame's position, normal, albedo, reprojected */
     uint32_t seed;
+    int32_t use_normal_map; /* 1: bend the shading normal by the object's normal texture (rt.rgen:141-144) */
 } orc_shade_params;
 
 /* A ReSTIR reservoir (restir.glsl:1-8). */
@@ -112,6 +126,11 @@ float orc_sh_pow(float x, float y);
 float orc_sh_exp(float x);
 int32_t orc_sh_trace(const orc_shade_scene* s, const float* o, const float* d, float tmin, float tmax, int32_t any,
                      float* u, float* v);
+
+/* this file's texture(): the sample of a w x h RGBA8 sRGB image at (u, v),
+ * and the sRGB decode of one 8-bit value */
+void orc_sh_texture(int32_t w, int32_t h, const uint8_t* texels, float u, float v, float out[4]);
+float orc_sh_srgb_decode(uint32_t byte);
 
 /* tonemap.frag per colour component: type 0 Hable's filmic curve scaled to
  * white at 11.2, 1 exponential 1 - exp(-c exposure), both followed by

@@ -318,6 +318,114 @@ def floor_and_light(rough=0.5, albedo=(0.8, 0.7, 0.6), light_e=(6.0, 6.0, 6.0)):
 CAM = S.camera(eye=(0.0, 0.9, 1.6), target=(0.0, 0.0, 0.0), up=(0, 1, 0), yfov=0.9, width=12, height=9)
 
 
+def textured_scene(seed=5):
+    """A floor and a back wall under an emissive quad, every material
+    textured: checker albedo and random metal / roughness on the floor, an
+    albedo texture on the wall, a normal map on both, an emission texture on
+    the light.  Texture coordinates repeat past [0, 1] and go negative;
+    tangents flip sign between the floor's two triangles."""
+    rng = np.random.default_rng(seed)
+    fv, fn = _quad(0.0, 1.0, True)
+    wv = np.float32([[[-1, 0, -1], [1, 0, -1], [1, 1.2, -1]], [[-1, 0, -1], [1, 1.2, -1], [-1, 1.2, -1]]])
+    wn = np.float32([[[0, 0, 1]] * 3] * 2)
+    lv, ln = _quad(1.0, 0.25, False, x0=0.2)
+    verts = np.concatenate([fv, wv, lv])
+    normals = np.concatenate([fn, wn, ln])
+    obj = [0, 0, 1, 1, 2, 2]
+    tc = np.concatenate([(fv[..., [0, 2]] + 1.0) * 1.3, wv[..., [0, 1]] * 0.8 - 0.3, (lv[..., [0, 2]] - 0.2) * 2.0 + 0.5])
+    tg = np.zeros((6, 3, 4), np.float32)
+    tg[0, :, :] = [1, 0, 0, 1]
+    tg[1, :, :] = [1, 0, 0, -1]
+    tg[2:4, :, :] = [1, 0, 0, 1]
+    tg[4:, :, :] = [0, 0, 1, 1]
+    checker = np.where((np.add.outer(np.arange(8), np.arange(8)) % 2)[..., None] == 0,
+                       rng.integers(150, 256, (8, 8, 4)), rng.integers(20, 90, (8, 8, 4))).astype(np.uint8)
+    wall = rng.integers(0, 256, (5, 7, 4), dtype=np.uint8)
+    metal_rough = np.stack([rng.integers(0, 256, (4, 4)), rng.integers(40, 256, (4, 4)),
+                            np.zeros((4, 4)), np.full((4, 4), 255)], -1).astype(np.uint8)
+    normal = np.stack([rng.integers(100, 156, (4, 4)), rng.integers(100, 156, (4, 4)),
+                       rng.integers(220, 256, (4, 4)), np.full((4, 4), 255)], -1).astype(np.uint8)
+    emit = rng.integers(180, 256, (2, 2, 4), dtype=np.uint8)
+    textures = [checker, wall, metal_rough, normal, emit]
+    obj_tex = [[0, -1, 2, 3], [1, -1, -1, 3], [-1, 4, -1, -1]]
+    return S.Scene(verts, normals, obj, albedo=[(0.8, 0.7, 0.6), (0.5, 0.5, 0.5), (0, 0, 0)],
+                   emissive=[(0, 0, 0), (0, 0, 0), (6.0, 6.0, 6.0)],
+                   metal_rough=[(0.2, 0.5), (0.0, 0.7), (0.0, 0.5)], texcoords=tc, tangents=tg,
+                   textures=textures, obj_tex=obj_tex)
+
+
+def _texture_numpy(im, u, v, lut):
+    """Bilinear at level 0 with repeat addressing of the sRGB-decoded
+    texels, in FP32, operations in the restatement's order."""
+    f32 = np.float32
+    h, w = im.shape[:2]
+
+    def wrap(x):
+        with np.errstate(invalid="ignore"):
+            f = (x - np.floor(x)).astype(f32)
+        return np.where((f >= 0) & (f < 1), f, f32(0))
+
+    fx = wrap(u) * f32(w) - f32(0.5)
+    fy = wrap(v) * f32(h) - f32(0.5)
+    x0, y0 = np.floor(fx), np.floor(fy)
+    ax, ay = (fx - x0).astype(f32), (fy - y0).astype(f32)
+    i0, j0 = x0.astype(np.int64), y0.astype(np.int64)
+    i0 = np.where(i0 < 0, w - 1, i0)
+    j0 = np.where(j0 < 0, h - 1, j0)
+    i1 = np.where(i0 + 1 == w, 0, i0 + 1)
+    j1 = np.where(j0 + 1 == h, 0, j0 + 1)
+    dec = np.concatenate([lut[im[..., :3]], (im[..., 3:] / f32(255)).astype(f32)], -1).astype(f32)
+    t00, t10, t01, t11 = dec[j0, i0], dec[j0, i1], dec[j1, i0], dec[j1, i1]
+    ax, ay = ax[:, None], ay[:, None]
+    one = f32(1)
+    return ((t00 * (one - ax) + t10 * ax) * (one - ay) + (t01 * (one - ax) + t11 * ax) * ay).astype(f32)
+
+
+def test_texture_sampling():
+    """The restatement's texture(): the sRGB decode within 6 ulp of FP64 (its
+    FP32 base (c + 0.055) / 1.055 rounds once or twice and the 2.4th power
+    scales that error by 2.4), and
+    the bilinear repeat blend equal to an independent FP32 version of it,
+    including coordinates far outside [0, 1], negative, on texel centres
+    and edges, and NaN / infinite (which read the texel at 0)."""
+    lut = S.srgb_decode()
+    c = np.arange(256) / 255.0
+    ref = np.where(c <= 0.04045, c / 12.92, ((c + 0.055) / 1.055) ** 2.4)
+    ulp = np.spacing(np.maximum(ref, 1e-30).astype(np.float32)).astype(np.float64)
+    assert (np.abs(lut - ref) / ulp).max() <= 6.0
+    assert lut[0] == 0.0 and lut[255] == 1.0
+    rng = np.random.default_rng(3)
+    for h, w in ((1, 1), (1, 5), (7, 3), (16, 16)):
+        im = rng.integers(0, 256, (h, w, 4), dtype=np.uint8)
+        u = np.concatenate([rng.uniform(-3, 4, 300), (np.arange(w) + 0.5) / w, np.arange(w + 1) / w,
+                            [-1e-9, 1e-9, -0.0, 1e7, -1e7, np.nan, np.inf, -np.inf]]).astype(np.float32)
+        v = np.concatenate([rng.uniform(-3, 4, 300), rng.uniform(0, 1, w), rng.uniform(0, 1, w + 1),
+                            [0.5, 0.5, 0.5, 0.5, 0.5, 0.25, np.nan, 2.5]]).astype(np.float32)
+        got = S.texture(im, u, v)
+        want = _texture_numpy(im, u, v, lut)
+        np.testing.assert_array_equal(got.view(np.uint32), want.view(np.uint32))
+        assert np.isfinite(got).all()
+
+
+def test_textures_change_the_frame():
+    """Each texture kind reaches the image: without the albedo checker, the
+    emission texture or the normal map the frame differs."""
+    sc = textured_scene()
+    base = sc.render(CAM, integrator=S.MIS, samples=4, seed=3, use_normal_map=True)
+    assert base.max() > 0.0
+    for k in range(4):
+        tex = sc.obj_tex.copy()
+        if (tex[:, k] < 0).all():
+            continue
+        tex[:, k] = -1
+        alt = S.Scene(sc.verts, sc.normals, sc.obj, sc.albedo, sc.emissive, sc.metal_rough, texcoords=sc.texcoords,
+                      tangents=sc.tangents, textures=sc.textures, obj_tex=tex)
+        img = alt.render(CAM, integrator=S.MIS, samples=4, seed=3, use_normal_map=True)
+        assert not np.array_equal(img, base), k
+    flat = sc.render(CAM, integrator=S.MIS, samples=4, seed=3, use_normal_map=False)
+    assert not np.array_equal(flat, base)
+
+
 def test_light_pdf_integrates_to_one():
     sc = floor_and_light()
     n = 400000

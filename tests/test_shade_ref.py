@@ -126,6 +126,23 @@ def test_frames_bit_exact(scenes, name, integrator, brdf):
     assert a[0].max() > 0.0
 
 
+@pytest.mark.parametrize("integrator", [S.DIRECT, S.MATERIAL, S.MIS, S.RESTIR_DIRECT, S.RESTIR])
+@pytest.mark.parametrize("brdf", [S.BLINN_PHONG, S.GGX])
+@pytest.mark.parametrize("normal_map", [False, True])
+def test_textured_frames_bit_exact(integrator, brdf, normal_map):
+    """Textured materials (albedo, emission, metal / roughness, normal maps)
+    through the reference's own mat_info, hit_info, shade_info and
+    light_sample: the restatement's frames equal them bit for bit."""
+    import test_shade_oracle as T
+
+    sc = T.textured_scene()
+    for metal in (False, True):
+        a, b = _frame_pair(sc, T.CAM, integrator=integrator, brdf=brdf, samples=4, seed=17,
+                           use_normal_map=normal_map, use_metalness=metal)
+        _same(a, b)
+        assert a[0].max() > 0.0
+
+
 @pytest.mark.parametrize("opts", [dict(use_rr=False, max_depth=5), dict(qmc=True, frame=3, max_frame=16),
                                   dict(use_metalness=True, integrator=S.MIS), dict(frame=2, env=(0.2, 0.3, 0.4)),
                                   dict(integrator=S.RESTIR, new_samples=7, temporal_multiplier=3)])
