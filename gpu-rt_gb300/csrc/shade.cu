@@ -297,6 +297,8 @@ __device__ bool hit_bbox(v3 o, v3 d, v3 bmin, v3 bmax) {
 struct MatInfo {
     v3 albedo, emissive;
     float roughness;
+    bool use_tanspace;  // the object has a normal texture
+    v3 tn;              // its tangent-space normal at the hit
 };
 struct ShadeInfo {
     v3 wo, t, b, n;
@@ -401,6 +403,15 @@ struct ShadeArgs {
     const float* albedo;   // nobj x 3
     const float* emissive; // nobj x 3
     const float* metal_rough;  // nobj x 2
+    // textures (all NULL / 0 without): per-vertex (u, v) and tangents
+    // (xyz, w), per object the texture index of each factor, and the
+    // decoded (linear) texels of every texture
+    const float* texcoords;   // nt x 6
+    const float* tangents;    // nt x 12
+    const int32_t* obj_tex;   // nobj x 4: albedo, emissive, metal_rough, normal, or -1
+    const int32_t* tex_size;  // ntex x 2: width, height
+    const int64_t* tex_off;   // ntex + 1 texel offsets
+    const float4* texels;
     const LightRec* lights;
     uint32_t n_lights;
     cp_shade_camera cam;
@@ -448,35 +459,123 @@ __device__ bool occluded(const ShadeArgs& a, v3 pa, v3 pb, int32_t* stack) {
     return trace<K>(a, pa, divs(dir, d), kEps, d - kEps, true, stack).hit;
 }
 
+// ---- textures (rt.rgen:97-129; images RGBA8 sRGB, linear filter, repeat) ----
+
+// x mod 1 in [0, 1); NaN, the infinities and a difference that rounds up to
+// 1 give 0
+__device__ __forceinline__ float wrap01(float x) {
+    float f = x - floorf(x);
+    if (!(f >= 0.0f && f < 1.0f)) f = 0.0f;
+    return f;
+}
+// the engine's texture(): bilinear blend at level 0 of the four decoded
+// texels around (u mod 1) w - 1/2, (v mod 1) h - 1/2, neighbours wrapping
+// around the edges; the same operations in the same order as the
+// restatement
+__device__ SH_CALL float4 tex_sample(const ShadeArgs& a, int32_t tex, float u, float v) {
+    const int32_t w = a.tex_size[2 * tex], h = a.tex_size[2 * tex + 1];
+    const float4* t = a.texels + a.tex_off[tex];
+    const float fx = wrap01(u) * (float)w - 0.5f, fy = wrap01(v) * (float)h - 0.5f;
+    const float x0 = floorf(fx), y0 = floorf(fy);
+    const float ax = fx - x0, ay = fy - y0;
+    int i0 = (int)x0, j0 = (int)y0;  // in [-1, w - 1] and [-1, h - 1]
+    if (i0 < 0) i0 = w - 1;
+    if (j0 < 0) j0 = h - 1;
+    const int i1 = i0 + 1 == w ? 0 : i0 + 1, j1 = j0 + 1 == h ? 0 : j0 + 1;
+    const float4 t00 = t[(int64_t)j0 * w + i0], t10 = t[(int64_t)j0 * w + i1];
+    const float4 t01 = t[(int64_t)j1 * w + i0], t11 = t[(int64_t)j1 * w + i1];
+    const float bx = 1.0f - ax, by = 1.0f - ay;
+    float4 r;
+    r.x = (t00.x * bx + t10.x * ax) * by + (t01.x * bx + t11.x * ax) * ay;
+    r.y = (t00.y * bx + t10.y * ax) * by + (t01.y * bx + t11.y * ax) * ay;
+    r.z = (t00.z * bx + t10.z * ax) * by + (t01.z * bx + t11.z * ax) * ay;
+    r.w = (t00.w * bx + t10.w * ax) * by + (t01.w * bx + t11.w * ax) * ay;
+    return r;
+}
+__device__ __forceinline__ int32_t obj_tex(const ShadeArgs& a, int32_t o, int k) {
+    return a.obj_tex ? a.obj_tex[4 * o + k] : -1;
+}
+__device__ __forceinline__ float tcd(const ShadeArgs& a, int64_t t, int j, int k) {
+    return a.texcoords ? a.texcoords[6 * t + 2 * j + k] : 0.0f;
+}
+__device__ __forceinline__ v3 tng(const ShadeArgs& a, int64_t t, int j) {
+    if (!a.tangents) return mk(0.0f, 0.0f, 0.0f);
+    const float* q = a.tangents + 12 * t + 4 * j;
+    return scl(ld(q), q[3]);
+}
+
 struct HitInfo {
     v3 pos, normal;
+    float tc[2];           // texture coordinates (scenes with textures)
+    int32_t tri;           // for the tangent, which only a normal map reads
+    float bx, by, bz;
 };
-// interpolated world position and unit normal at a hit (rt.rgen:64-98)
+// interpolated world position, unit normal and texture coordinates at a hit
+// (rt.rgen:62-95; identity model matrices for world-space triangles); the
+// unit tangent comes from hit_tangent where a normal map needs it
 __device__ HitInfo make_hit_info(const ShadeArgs& a, const HitRec& h) {
     const float bx = 1.0f - h.u - h.v, by = h.u, bz = h.v;
     HitInfo r;
     r.normal = normalize3(comb(nrm(a, h.tri, 0), bx, nrm(a, h.tri, 1), by, nrm(a, h.tri, 2), bz));
     r.pos = comb(vert(a, h.tri, 0), bx, vert(a, h.tri, 1), by, vert(a, h.tri, 2), bz);
+    r.tc[0] = r.tc[1] = 0.0f;
+    if (a.obj_tex)
+        for (int k = 0; k < 2; ++k)
+            r.tc[k] = tcd(a, h.tri, 0, k) * bx + tcd(a, h.tri, 1, k) * by + tcd(a, h.tri, 2, k) * bz;
+    r.tri = h.tri;
+    r.bx = bx;
+    r.by = by;
+    r.bz = bz;
     return r;
 }
-// constant material of the hit object (rt.rgen:100-129, without textures)
-__device__ MatInfo make_mat_info(const ShadeArgs& a, int32_t o) {
+__device__ __forceinline__ v3 hit_tangent(const ShadeArgs& a, const HitInfo& h) {
+    return normalize3(comb(tng(a, h.tri, 0), h.bx, tng(a, h.tri, 1), h.by, tng(a, h.tri, 2), h.bz));
+}
+// material of the hit object at texture coordinates tc: each factor, or its
+// texture where the object has one (rt.rgen:97-129)
+__device__ MatInfo make_mat_info(const ShadeArgs& a, int32_t o, const float* tc) {
     MatInfo m;
     m.albedo = ld(a.albedo + 3 * o);
+    if (obj_tex(a, o, 0) >= 0) {
+        const float4 t = tex_sample(a, obj_tex(a, o, 0), tc[0], tc[1]);
+        m.albedo = mk(t.x, t.y, t.z);
+    }
     m.emissive = ld(a.emissive + 3 * o);
-    const float metal = a.metal_rough[2 * o], rough = a.metal_rough[2 * o + 1];
+    if (obj_tex(a, o, 1) >= 0) {
+        const float4 t = tex_sample(a, obj_tex(a, o, 1), tc[0], tc[1]);
+        m.emissive = mk(t.x, t.y, t.z);
+    }
+    float metal = a.metal_rough[2 * o], rough = a.metal_rough[2 * o + 1];
+    if (obj_tex(a, o, 2) >= 0) {
+        const float4 t = tex_sample(a, obj_tex(a, o, 2), tc[0], tc[1]);
+        metal = t.x;
+        rough = t.y;
+    }
     m.roughness = rough;
     if (a.p.use_metalness)  // mix(vec3(0.04), albedo, metal)
         m.albedo = mk(0.04f * (1.0f - metal) + m.albedo.x * metal, 0.04f * (1.0f - metal) + m.albedo.y * metal,
                       0.04f * (1.0f - metal) + m.albedo.z * metal);
+    m.use_tanspace = obj_tex(a, o, 3) >= 0;
+    m.tn = mk(0.0f, 0.0f, 0.0f);
+    if (m.use_tanspace) {  // texture(...).xyz * 2.0 - 1.0
+        const float4 t = tex_sample(a, obj_tex(a, o, 3), tc[0], tc[1]);
+        m.tn = mk(t.x * 2.0f - 1.0f, t.y * 2.0f - 1.0f, t.z * 2.0f - 1.0f);
+    }
     return m;
 }
-// shading frame facing the incoming ray (rt.rgen:131-148)
-__device__ ShadeInfo make_shade_info(v3 wo, v3 normal) {
+// shading frame facing the incoming ray, the normal bent by the normal map
+// when it is on (rt.rgen:131-148)
+__device__ ShadeInfo make_shade_info(const ShadeArgs& a, v3 wo, const HitInfo& hit, const MatInfo& m) {
     ShadeInfo sh;
     sh.wo = wo;
+    v3 normal = hit.normal;
     if (dot(sh.wo, normal) > 0.0f) normal = neg(normal);
     sh.n = normal;
+    if (m.use_tanspace && a.p.use_normal_map == 1) {  // N = normalize(mat3(T, B, N) * tn)
+        sh.t = hit_tangent(a, hit);
+        sh.b = cross(sh.n, sh.t);
+        sh.n = normalize3(add(add(scl(sh.t, m.tn.x), scl(sh.b, m.tn.y)), scl(sh.n, m.tn.z)));
+    }
     make_tanspace(sh.n, &sh.t, &sh.b);
     return sh;
 }
@@ -497,6 +596,14 @@ __device__ SH_CALL LightSample light_sample(const ShadeArgs& a, uint32_t* seed, 
     LightSample r;
     r.pos = comb(v0, bary.x, v1, bary.y, v2, bary.z);
     r.emissive = ld(a.emissive + 3 * L.obj);
+    if (obj_tex(a, L.obj, 1) >= 0) {
+        // the shader's coordinates: u interpolated, v vertex 1's at every
+        // corner (rt.rgen:175)
+        const float tu = tcd(a, t, 0, 0) * bary.x + tcd(a, t, 1, 0) * bary.y + tcd(a, t, 2, 0) * bary.z;
+        const float tv = tcd(a, t, 1, 1) * bary.x + tcd(a, t, 1, 1) * bary.y + tcd(a, t, 1, 1) * bary.z;
+        const float4 e = tex_sample(a, obj_tex(a, L.obj, 1), tu, tv);
+        r.emissive = mk(e.x, e.y, e.z);
+    }
     const v3 narea = cross(sub(v1, v0), sub(v2, v0));
     const float ar = 2.0f / length3(narea);
     const v3 dist = sub(r.pos, p);
@@ -542,7 +649,10 @@ template <int K>
 __device__ v3 direct_light(const ShadeArgs& a, v3 o, v3 d, int32_t* stack) {
     const HitRec h = trace<K>(a, o, d, kEps, kLargeDist, false, stack);
     if (!h.hit) return ld(a.p.env);
-    return ld(a.emissive + 3 * a.obj[h.tri]);
+    const int32_t ob = a.obj[h.tri];
+    if (obj_tex(a, ob, 1) < 0) return ld(a.emissive + 3 * ob);  // mat_info's emission, the factor
+    const HitInfo hit = make_hit_info(a, h);
+    return make_mat_info(a, ob, hit.tc).emissive;
 }
 
 // rt.rgen:301-355
@@ -877,8 +987,8 @@ __global__ void __launch_bounds__(256, 6) k_shade(ShadeArgs a) {
                 break;
             }
             const HitInfo hit = make_hit_info(a, h);
-            const MatInfo m = make_mat_info(a, a.obj[h.tri]);
-            const ShadeInfo sh = make_shade_info(tr.d, hit.normal);
+            const MatInfo m = make_mat_info(a, a.obj[h.tri], hit.tc);
+            const ShadeInfo sh = make_shade_info(a, tr.d, hit, m);
             if (smp == 0 && tr.depth == 0) {
                 g_pos = hit.pos;
                 g_norm = sh.n;
@@ -975,6 +1085,14 @@ struct cp_shade_scene {
     float* metal_rough = nullptr;
     cpq::LightRec* lights = nullptr;
     uint32_t n_lights = 0;
+    // textures (cp_shade_scene_textures)
+    float* texcoords = nullptr;
+    float* tangents = nullptr;
+    int32_t* obj_tex = nullptr;
+    int32_t* tex_size = nullptr;
+    int64_t* tex_off = nullptr;
+    float4* texels = nullptr;
+    int32_t ntex = 0;
 };
 
 namespace {
@@ -989,6 +1107,12 @@ void free_scene(cp_shade_scene* s) {
     cudaFree(s->emissive);
     cudaFree(s->metal_rough);
     cudaFree(s->lights);
+    cudaFree(s->texcoords);
+    cudaFree(s->tangents);
+    cudaFree(s->obj_tex);
+    cudaFree(s->tex_size);
+    cudaFree(s->tex_off);
+    cudaFree(s->texels);
     delete s;
 }
 
@@ -1109,6 +1233,94 @@ extern "C" CP_API cp_status cp_shade_scene_create(const float* verts, const floa
     return CP_SUCCESS;
 }
 
+namespace {
+// RGBA8 texels to linear floats: sRGB colour through the engine's pow, alpha
+// as stored / 255 (the decode of an R8G8B8A8_SRGB image; the restatement
+// decodes each texel the same way)
+__global__ void k_srgb_decode(const uint8_t* __restrict__ in, int64_t n, float4* __restrict__ out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float c[3];
+    for (int k = 0; k < 3; ++k) {
+        const float x = (float)in[4 * i + k] / 255.0f;
+        c[k] = x <= 0.04045f ? x / 12.92f : cpq::sh_pow((x + 0.055f) / 1.055f, 2.4f);
+    }
+    out[i] = make_float4(c[0], c[1], c[2], (float)in[4 * i + 3] / 255.0f);
+}
+}  // namespace
+
+extern "C" CP_API cp_status cp_shade_scene_textures(cp_shade_scene* s, const float* texcoords, const float* tangents,
+                                                    int32_t ntex, const int32_t* tex_size, const uint8_t* texels,
+                                                    const int32_t* obj_tex, cp_stream_t stream) {
+    using namespace cpq;
+    if (!s) return set_error(CP_ERROR_INVALID_VALUE, "scene is NULL");
+    if (ntex < 0) return set_error(CP_ERROR_INVALID_VALUE, "negative texture count");
+    if (ntex > 0 && (!tex_size || !texels)) return set_error(CP_ERROR_INVALID_VALUE, "texture sizes or texels are NULL");
+    // host checks first: every texture index an object names, every size
+    std::vector<int64_t> off((size_t)ntex + 1, 0);
+    for (int32_t k = 0; k < ntex; ++k) {
+        const int64_t w = tex_size[2 * k], h = tex_size[2 * k + 1];
+        if (w <= 0 || h <= 0 || w > (int64_t(1) << 20) || h > (int64_t(1) << 20))
+            return set_error(CP_ERROR_INVALID_VALUE, "texture " + std::to_string(k) + " has a size outside 1..2^20");
+        off[k + 1] = off[k] + w * h;
+    }
+    if (obj_tex)
+        for (int64_t i = 0; i < 4 * (int64_t)s->nobj; ++i)
+            if (obj_tex[i] < -1 || obj_tex[i] >= ntex)
+                return set_error(CP_ERROR_INVALID_VALUE, "object " + std::to_string(i / 4) + " names texture " +
+                                                             std::to_string(obj_tex[i]) + " of " + std::to_string(ntex));
+    cudaStream_t st = reinterpret_cast<cudaStream_t>(stream);
+    // the new arrays replace the old ones only when all are in place
+    cp_shade_scene t;
+    auto drop = [&]() {
+        cudaFree(t.texcoords);
+        cudaFree(t.tangents);
+        cudaFree(t.obj_tex);
+        cudaFree(t.tex_size);
+        cudaFree(t.tex_off);
+        cudaFree(t.texels);
+    };
+    cudaError_t e = cudaSuccess;
+    if (texcoords) e = dev_copy(&t.texcoords, texcoords, (size_t)s->nt * 6, st);
+    if (e == cudaSuccess && tangents) e = dev_copy(&t.tangents, tangents, (size_t)s->nt * 12, st);
+    if (e == cudaSuccess && obj_tex) {
+        e = cudaMalloc(reinterpret_cast<void**>(&t.obj_tex), sizeof(int32_t) * 4 * s->nobj);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(t.obj_tex, obj_tex, sizeof(int32_t) * 4 * s->nobj, cudaMemcpyHostToDevice, st);
+    }
+    if (e == cudaSuccess && ntex > 0) {
+        e = cudaMalloc(reinterpret_cast<void**>(&t.tex_size), sizeof(int32_t) * 2 * ntex);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(t.tex_size, tex_size, sizeof(int32_t) * 2 * ntex, cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&t.tex_off), sizeof(int64_t) * (ntex + 1));
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(t.tex_off, off.data(), sizeof(int64_t) * (ntex + 1), cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess) e = cudaMalloc(reinterpret_cast<void**>(&t.texels), sizeof(float4) * off[ntex]);
+        if (e == cudaSuccess) {
+            k_srgb_decode<<<(unsigned)((off[ntex] + 255) / 256), 256, 0, st>>>(texels, off[ntex], t.texels);
+            note_launch();
+            e = cudaGetLastError();
+        }
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+        drop();
+        t = cp_shade_scene();
+        return set_error(e == cudaErrorMemoryAllocation ? CP_ERROR_OUT_OF_MEMORY : CP_ERROR_CUDA,
+                         std::string("cp_shade_scene_textures: ") + cudaGetErrorString(e));
+    }
+    std::swap(s->texcoords, t.texcoords);
+    std::swap(s->tangents, t.tangents);
+    std::swap(s->obj_tex, t.obj_tex);
+    std::swap(s->tex_size, t.tex_size);
+    std::swap(s->tex_off, t.tex_off);
+    std::swap(s->texels, t.texels);
+    s->ntex = ntex;
+    drop();  // the previous arrays
+    t = cp_shade_scene();
+    return CP_SUCCESS;
+}
+
 extern "C" CP_API cp_status cp_shade_scene_destroy(cp_shade_scene* s) {
     free_scene(s);
     return CP_SUCCESS;
@@ -1155,6 +1367,12 @@ extern "C" CP_API cp_status cp_shade_render(const cp_shade_scene* s, const cp_sh
     a.albedo = s->albedo;
     a.emissive = s->emissive;
     a.metal_rough = s->metal_rough;
+    a.texcoords = s->texcoords;
+    a.tangents = s->tangents;
+    a.obj_tex = s->obj_tex;
+    a.tex_size = s->tex_size;
+    a.tex_off = s->tex_off;
+    a.texels = s->texels;
     a.lights = s->lights;
     a.n_lights = s->n_lights;
     a.cam = *cam;

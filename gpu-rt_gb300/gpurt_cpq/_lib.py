@@ -58,7 +58,7 @@ class ShadeParams(Structure):
                 ("qmc", c_int32), ("integrator", c_int32), ("brdf", c_int32), ("use_rr", c_int32),
                 ("use_metalness", c_int32), ("frame", c_int32), ("max_frame", c_int32),
                 ("new_samples", c_int32), ("temporal_multiplier", c_int32), ("use_temporal", c_int32),
-                ("debug_view", c_int32), ("seed", c_uint32)]
+                ("debug_view", c_int32), ("seed", c_uint32), ("use_normal_map", c_int32)]
 
 
 CP_TRAVERSAL_AUTO = 0
@@ -155,6 +155,8 @@ SIGNATURES = {
     "cp_shade_scene_create": (c_int32, [c_void_p, c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p,
                                         c_int32, c_void_p, POINTER(c_void_p)]),
     "cp_shade_scene_destroy": (c_int32, [c_void_p]),
+    "cp_shade_scene_textures": (c_int32, [c_void_p, c_void_p, c_void_p, c_int32, c_void_p, c_void_p, c_void_p,
+                                          c_void_p]),
     "cp_shade_scene_lights": (c_int32, [c_void_p, POINTER(c_int32)]),
     "cp_shade_render": (c_int32, [c_void_p, POINTER(ShadeCamera), POINTER(ShadeParams), c_void_p, c_void_p,
                                   c_void_p, c_void_p, c_void_p, c_void_p, c_void_p]),

@@ -99,6 +99,31 @@ class ShadeScene:
         self.num_triangles = v.shape[0]
         self.device = v.device
 
+    def set_textures(self, *, texcoords: torch.Tensor | None = None, tangents: torch.Tensor | None = None,
+                     textures=(), obj_tex=None, stream=None) -> None:
+        """cp_shade_scene_textures: device texcoords (T, 3, 2) and tangents
+        (T, 3, 4) float32, a list of RGBA8 sRGB images ((h, w, 4) uint8,
+        numpy or tensors; uploaded here) and per object the texture replacing
+        its albedo, emission, metal / roughness and its normal map
+        ((O, 4) int, -1 none)."""
+        tc = None if texcoords is None else texcoords.reshape(-1, 6).contiguous()
+        tg = None if tangents is None else tangents.reshape(-1, 12).contiguous()
+        if tc is not None:
+            _check_dev(tc, "texcoords", torch.float32, 6)
+        if tg is not None:
+            _check_dev(tg, "tangents", torch.float32, 12)
+        ims = [torch.as_tensor(np.ascontiguousarray(np.asarray(im, dtype=np.uint8))) for im in textures]
+        for im in ims:
+            if im.dim() != 3 or im.shape[2] != 4:
+                raise ValueError("each texture must be (h, w, 4) uint8")
+        size = np.asarray([[im.shape[1], im.shape[0]] for im in ims], np.int32).reshape(-1, 2)
+        texels = (torch.cat([im.reshape(-1) for im in ims]).to(self.device) if ims
+                  else torch.zeros(4, dtype=torch.uint8, device=self.device))
+        ot = None if obj_tex is None else np.ascontiguousarray(np.asarray(obj_tex, np.int32).reshape(-1, 4))
+        check(lib.cp_shade_scene_textures(self._h, _ptr(tc), _ptr(tg), len(ims), c_void_p(size.ctypes.data),
+                                          _ptr(texels), None if ot is None else c_void_p(ot.ctypes.data),
+                                          _stream(stream)), "cp_shade_scene_textures")
+
     @property
     def n_lights(self) -> int:
         n = c_int32()
@@ -120,14 +145,14 @@ class ShadeScene:
                use_rr=True, qmc=False, use_metalness=False, frame=0, max_frame=256, new_samples=4,
                temporal_multiplier=16, use_temporal=True, debug_view=0, clear=(0.3, 0.3, 0.3),
                env=(0.0, 0.0, 0.0), seed=1, image: torch.Tensor | None = None, gbuffer: bool = False,
-               temporal: TemporalState | None = None, stream=None):
+               temporal: TemporalState | None = None, use_normal_map=False, stream=None):
         """One frame; returns the image (height, width, 3) and, with `gbuffer`,
         the first-hit buffer (height, width, 9), as device tensors.  `image`
         is blended into when frame > 0.  `temporal` carries ReSTIR's state
         between frames (its out_res is written)."""
         p = ShadeParams((c_float * 3)(*clear), (c_float * 3)(*env), samples, max_depth, int(qmc), integrator,
                         brdf, int(use_rr), int(use_metalness), frame, max_frame, new_samples,
-                        temporal_multiplier, int(use_temporal), debug_view, seed)
+                        temporal_multiplier, int(use_temporal), debug_view, seed, int(use_normal_map))
         shape = (cam.height, cam.width, 3)
         img = torch.zeros(shape, dtype=torch.float32, device=self.device) if image is None else image
         if tuple(img.shape) != shape or img.dtype != torch.float32 or not img.is_contiguous():

@@ -574,12 +574,14 @@ CP_API cp_status cp_scene_ray_query(const cp_scene* scene, const float* origins,
  * (src/shaders/tonemap.frag) as CUDA kernels over this library's BVH, writing
  * a device image buffer instead of a swapchain image.  Replaces RTPipe::trace
  * (src/vk/rt.cpp:346-394) and the tonemap pass.  Scenes are world-space
- * triangles with per-vertex normals and one constant material per object (no
- * textures); an object with an emission component above zero is a light, and
- * its triangles must be contiguous.  What GLSL leaves to the implementation
- * is fixed: sin / cos / pow / exp are the library's own routines, and the
- * pixel seed is tea(pixel, seed) where the shader reads the clock
- * (rt.rgen:569).
+ * triangles with per-vertex normals and a material per object: factors,
+ * each of which a texture may replace, and an optional normal map
+ * (cp_shade_scene_textures); an object with an emission factor above zero
+ * is a light, and its triangles must be contiguous.  What GLSL leaves to the
+ * implementation is fixed: sin / cos / pow / exp are the library's own
+ * routines, texture() is the library's own bilinear blend of sRGB-decoded
+ * texels, and the pixel seed is tea(pixel, seed) where the shader reads the
+ * clock (rt.rgen:569).
  */
 typedef struct cp_shade_scene cp_shade_scene;
 
@@ -607,6 +609,7 @@ typedef struct {
     int32_t use_temporal;       /* ReSTIR: reuse the previous frame's reservoirs */
     int32_t debug_view;         /* 1, 2, 3: the previous frame's position, normal, albedo, reprojected */
     uint32_t seed;
+    int32_t use_normal_map;     /* 1: bend the shading normal by an object's normal texture */
 } cp_shade_params;
 
 /* A ReSTIR reservoir (restir.glsl:1-8), 48 bytes. */
@@ -625,6 +628,22 @@ CP_API cp_status cp_shade_scene_create(const float* verts, const float* normals,
                                        const float* albedo, const float* emissive, const float* metal_rough,
                                        int32_t nobj, cp_stream_t stream, cp_shade_scene** out);
 CP_API cp_status cp_shade_scene_destroy(cp_shade_scene* scene);
+
+/* Textures of a scene (replacing any it had): texcoords (DEVICE, nt x 3
+ * vertices x (u, v), may be NULL: all zero), tangents (DEVICE, nt x 3
+ * vertices x (xyz, w), the tangent being xyz * w, may be NULL: only normal
+ * maps use them), ntex RGBA8 images in texels (DEVICE, concatenated, row 0
+ * first, colour sRGB-encoded as in the reference's R8G8B8A8_SRGB images,
+ * rt.cpp:439), their sizes tex_size (HOST, ntex x (width, height)), and
+ * obj_tex (HOST, nobj x 4: for each object the texture that replaces its
+ * albedo, emission, metal / roughness, or gives its normal map; -1 none)
+ * (Scene_Obj's *_tex, rt.rgen:97-129).  Every index is checked on the host.
+ * Sampling is the library's texture(): the four texels around
+ * (u mod 1) w - 1/2, (v mod 1) h - 1/2 at level 0, decoded from sRGB,
+ * blended bilinearly with repeat addressing.  Synchronises `stream`. */
+CP_API cp_status cp_shade_scene_textures(cp_shade_scene* scene, const float* texcoords, const float* tangents,
+                                         int32_t ntex, const int32_t* tex_size, const uint8_t* texels,
+                                         const int32_t* obj_tex, cp_stream_t stream);
 /* Number of lights (emissive objects with triangles). */
 CP_API cp_status cp_shade_scene_lights(const cp_shade_scene* scene, int32_t* n_lights);
 

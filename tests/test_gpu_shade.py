@@ -151,6 +151,66 @@ def test_cornell_box_larger_frame_bit_exact(scenes):
         _same(g, wg, "first-hit buffer")
 
 
+def _gpu_textured(sc, cuda):
+    import torch
+
+    g = _gpu_scene(sc, cuda)
+    g.set_textures(texcoords=torch.from_numpy(sc.texcoords).to(cuda), tangents=torch.from_numpy(sc.tangents).to(cuda),
+                   textures=sc.textures, obj_tex=sc.obj_tex)
+    return g
+
+
+@pytest.mark.parametrize("integrator", [S.DIRECT, S.MATERIAL, S.MIS, S.RESTIR_DIRECT, S.RESTIR])
+@pytest.mark.parametrize("brdf", [S.BLINN_PHONG, S.GGX])
+def test_textured_frames_bit_exact(cuda, integrator, brdf):
+    """Textured albedo, emission, metal / roughness and normal maps, with the
+    normal map on and off and metalness on and off: every pixel and first
+    hit equal to the restatement."""
+    import test_shade_oracle as T
+
+    sc = T.textured_scene()
+    gs = _gpu_textured(sc, cuda)
+    for normal_map in (False, True):
+        for metal in (False, True):
+            (img, g), (wimg, wg) = _pair(sc, gs, T.CAM, integrator=integrator, brdf=brdf, samples=4, seed=17,
+                                         use_normal_map=normal_map, use_metalness=metal)
+            _same(img, wimg)
+            _same(g, wg, "first-hit buffer")
+            assert img.max() > 0.0
+
+
+def test_textured_larger_frame_and_refusals(cuda):
+    """A 48 x 36 textured frame at 8 samples per pixel through every
+    integrator option at once; then textures replaced by none give the
+    untextured frame; bad texture indices and sizes are refused."""
+    import torch
+
+    from gpurt_cpq import CpError
+
+    import test_shade_oracle as T
+
+    sc = T.textured_scene(seed=9)
+    gs = _gpu_textured(sc, cuda)
+    cam = S.camera(eye=(0.1, 0.8, 1.5), target=(0.0, 0.2, -0.3), up=(0, 1, 0), yfov=1.0, width=48, height=36)
+    for integrator in (S.MIS, S.RESTIR):
+        (img, g), (wimg, wg) = _pair(sc, gs, cam, integrator=integrator, samples=8, seed=2, use_normal_map=True)
+        _same(img, wimg)
+        _same(g, wg, "first-hit buffer")
+    plain = S.Scene(sc.verts, sc.normals, sc.obj, sc.albedo, sc.emissive, sc.metal_rough)
+    gs.set_textures()
+    _same(gs.render(_cam(cam), integrator=S.MIS, samples=2, seed=4).cpu().numpy(),
+          plain.render(cam, integrator=S.MIS, samples=2, seed=4))
+    bad = sc.obj_tex.copy()
+    bad[1, 0] = len(sc.textures)
+    with pytest.raises(CpError, match="names texture"):
+        gs.set_textures(texcoords=torch.from_numpy(sc.texcoords).to(cuda), textures=sc.textures, obj_tex=bad)
+    with pytest.raises(CpError, match="size"):
+        gs.set_textures(textures=[np.zeros((0, 4, 4), np.uint8)])
+    # the refused calls left the scene as it was (no textures)
+    _same(gs.render(_cam(cam), integrator=S.MIS, samples=2, seed=4).cpu().numpy(),
+          plain.render(cam, integrator=S.MIS, samples=2, seed=4))
+
+
 @pytest.mark.parametrize("kind", [0, 1, 2])
 def test_tonemap_bit_exact(cuda, kind):
     import torch
