@@ -3,8 +3,10 @@
 // Reads what the reference's Scene::load / Scene::parse_mesh take from
 // tinygltf (src/scene/scene.cpp:48-315, 317-391): triangle geometry
 // (POSITION + indices; strips and fans converted as parse_mesh converts
-// them), node placement, and for shading the vertex normals and material
-// factors (no textures).  Self-contained: a small JSON
+// them), node placement, and for shading the vertex normals, texture
+// coordinates and tangents, the material factors and the material's texture
+// references with each texture's image (images are not decoded).
+// Self-contained: a small JSON
 // reader, base64 "data:" URIs, external .bin buffers and .glb containers.
 // Everything is bounds-checked against the buffers it indexes; a malformed
 // file is an error, never an out-of-range read.
@@ -373,7 +375,14 @@ struct Model {
 struct Scene {
     std::vector<float> verts;
     std::vector<float> normals;    // per vertex, zeros where the primitive has no NORMAL
+    std::vector<float> texcoords;  // per vertex TEXCOORD_0, zeros where absent
+    std::vector<float> tangents;   // per vertex TANGENT (xyz, w), zeros where absent
     std::vector<float> materials;  // per primitive: base colour rgb, emission rgb, metalness, roughness
+    std::vector<int32_t> prim_tex; // per primitive: base colour, emissive, metal / rough, normal texture or -1
+    std::vector<int32_t> tex_image;    // per glTF texture: its image, or -1
+    std::vector<std::string> image_uri;  // per image: "uri", or empty
+    std::vector<const char*> image_uri_c;
+    std::vector<int32_t> image_view;   // per image: "bufferView", or -1
     std::vector<int32_t> tris;
     std::vector<int64_t> voff{0}, toff{0};
     std::vector<int32_t> mesh_first_prim, mesh_num_prim;  // per glTF mesh: its triangle primitives
@@ -409,7 +418,7 @@ void numbers(const Json& j, const char* key, size_t n, const float* dflt, float*
 
 // The factors Scene::parse_mesh copies into its Material (scene.cpp:286-299),
 // with glTF's defaults; a primitive without a material gets the default
-// material (the reference would index materials[-1]).  Textures are not read.
+// material (the reference would index materials[-1]).
 void material_factors(const Model& m, const Json& prim, float* out) {
     static const float kOne[4] = {1.0f, 1.0f, 1.0f, 1.0f}, kZero[3] = {0.0f, 0.0f, 0.0f};
     std::copy(kOne, kOne + 3, out);
@@ -429,6 +438,69 @@ void material_factors(const Model& m, const Json& prim, float* out) {
         out[7] = (float)pbr->number("roughnessFactor", 1.0);
     }
     numbers(mat, "emissiveFactor", 3, kZero, out + 3);
+}
+
+// The texture references Scene::parse_mesh copies into its Material
+// (scene.cpp:294-302): the "index" of baseColorTexture, emissiveTexture,
+// metallicRoughnessTexture and normalTexture, -1 where absent (as tinygltf
+// reports it); an index outside the file's textures is refused.
+void material_textures(const Model& m, const Json& prim, int32_t* out) {
+    for (int k = 0; k < 4; ++k) out[k] = -1;
+    const int64_t mi = prim.integer("material", -1);
+    if (mi < 0) return;
+    const auto& mats = m.doc.array("materials");
+    if (mi >= (int64_t)mats.size()) throw std::runtime_error("material index out of range");
+    const Json& mat = mats[(size_t)mi];
+    const int64_t ntex = (int64_t)m.doc.array("textures").size();
+    auto ref = [&](const Json* holder, const char* key, int32_t* slot) {
+        if (!holder) return;
+        const Json* t = holder->get(key);
+        if (!t) return;
+        const int64_t i = t->integer("index", -1);
+        if (i < 0 || i >= ntex) throw std::runtime_error(std::string(key) + " index out of range");
+        *slot = (int32_t)i;
+    };
+    const Json* pbr = mat.get("pbrMetallicRoughness");
+    ref(pbr, "baseColorTexture", out);
+    ref(&mat, "emissiveTexture", out + 1);
+    ref(pbr, "metallicRoughnessTexture", out + 2);
+    ref(&mat, "normalTexture", out + 3);
+}
+
+// n floats per vertex of an optional FLOAT attribute, paired with the
+// positions as parse_mesh pairs them: the k-th for vertex k, zeros past the
+// accessor's count or where the attribute is absent or of another type (the
+// reference reads FLOAT and skips what it does not handle, scene.cpp:188-265)
+void per_vertex(const Model& m, const Json& attrs, const char* name, int ncomp, size_t nv, std::vector<float>& out) {
+    size_t have = 0;
+    Accessor a;
+    if (const Json* j = attrs.get(name)) {
+        a = m.accessor((int64_t)j->num);
+        if (a.ctype == 5126 && a.ncomp == ncomp) have = std::min(a.count, nv);
+    }
+    for (size_t k = 0; k < nv; ++k) {
+        float v[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (k < have) std::memcpy(v, a.data + k * a.stride, sizeof(float) * ncomp);
+        out.insert(out.end(), v, v + ncomp);
+    }
+}
+
+// Each texture's image ("source") and each image's "uri" or "bufferView"
+// (scene.cpp:373-389 loads textures in this order).  Images are not decoded.
+void add_textures(const Model& m, Scene& s) {
+    const auto& images = m.doc.array("images");
+    for (const Json& t : m.doc.array("textures")) {
+        const int64_t src = t.integer("source", -1);
+        s.tex_image.push_back(src >= 0 && src < (int64_t)images.size() ? (int32_t)src : -1);
+    }
+    const int64_t nviews = (int64_t)m.doc.array("bufferViews").size();
+    for (const Json& im : images) {
+        const Json* uri = im.get("uri");
+        s.image_uri.push_back(uri && uri->kind == Json::String ? uri->str : std::string());
+        const int64_t v = im.integer("bufferView", -1);
+        s.image_view.push_back(v >= 0 && v < nviews ? (int32_t)v : -1);
+    }
+    for (const std::string& u : s.image_uri) s.image_uri_c.push_back(u.c_str());
 }
 
 void add_primitives(const Model& m, Scene& s) {
@@ -486,9 +558,14 @@ void add_primitives(const Model& m, Scene& s) {
                 if (k < nn) std::memcpy(n, na.data + k * na.stride, 12);
                 s.normals.insert(s.normals.end(), n, n + 3);
             }
+            per_vertex(m, attrs, "TEXCOORD_0", 2, nv, s.texcoords);
+            per_vertex(m, attrs, "TANGENT", 4, nv, s.tangents);
             float mat[8];
             material_factors(m, prim, mat);
             s.materials.insert(s.materials.end(), mat, mat + 8);
+            int32_t tex[4];
+            material_textures(m, prim, tex);
+            s.prim_tex.insert(s.prim_tex.end(), tex, tex + 4);
             for (uint32_t v : t) s.tris.push_back((int32_t)v);
             s.voff.push_back(s.voff.back() + (int64_t)nv);
             s.toff.push_back(s.toff.back() + (int64_t)(t.size() / 3));
@@ -622,6 +699,7 @@ CP_API cp_status cp_gltf_load(const char* path, cp_gltf** out) {
         const Model m = load_model(path);
         auto g = std::make_unique<cp_gltf>();
         add_primitives(m, g->s);
+        add_textures(m, g->s);
         const float I[16] = {1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1};
         // every scene's root nodes, depth first, as Scene::load walks them
         for (const Json& scene : m.doc.array("scenes"))
@@ -651,6 +729,22 @@ CP_API cp_status cp_gltf_shading(const cp_gltf* g, int32_t* n, const float** nor
     *n = (int32_t)(g->s.voff.size() - 1);
     if (normals) *normals = g->s.normals.data();
     if (materials) *materials = g->s.materials.data();
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_gltf_textures(const cp_gltf* g, int32_t* n, const float** texcoords, const float** tangents,
+                                  const int32_t** prim_tex, int32_t* num_textures, const int32_t** tex_image,
+                                  int32_t* num_images, const char* const** image_uri, const int32_t** image_view) {
+    if (!g || !n) return cpq::set_error(CP_ERROR_INVALID_VALUE, "scene or count is NULL");
+    *n = (int32_t)(g->s.voff.size() - 1);
+    if (texcoords) *texcoords = g->s.texcoords.data();
+    if (tangents) *tangents = g->s.tangents.data();
+    if (prim_tex) *prim_tex = g->s.prim_tex.data();
+    if (num_textures) *num_textures = (int32_t)g->s.tex_image.size();
+    if (tex_image) *tex_image = g->s.tex_image.data();
+    if (num_images) *num_images = (int32_t)g->s.image_uri.size();
+    if (image_uri) *image_uri = g->s.image_uri_c.data();
+    if (image_view) *image_view = g->s.image_view.data();
     return CP_SUCCESS;
 }
 

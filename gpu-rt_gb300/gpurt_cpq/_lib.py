@@ -112,6 +112,9 @@ SIGNATURES = {
                                      POINTER(c_void_p), POINTER(c_void_p)]),
     "cp_gltf_instances": (c_int32, [c_void_p, POINTER(c_int32), POINTER(c_void_p), POINTER(c_void_p)]),
     "cp_gltf_shading": (c_int32, [c_void_p, POINTER(c_int32), POINTER(c_void_p), POINTER(c_void_p)]),
+    "cp_gltf_textures": (c_int32, [c_void_p, POINTER(c_int32), POINTER(c_void_p), POINTER(c_void_p),
+                                   POINTER(c_void_p), POINTER(c_int32), POINTER(c_void_p), POINTER(c_int32),
+                                   POINTER(c_void_p), POINTER(c_void_p)]),
     "cp_ray_opts_default": (None, [POINTER(RayOpts)]),
     "cp_ray_workspace_size": (c_int32, [c_void_p, c_int64, POINTER(RayOpts), POINTER(c_size_t)]),
     "cp_ray_query": (c_int32, [c_void_p, c_void_p, c_void_p, c_void_p, c_int64, POINTER(RayOpts),

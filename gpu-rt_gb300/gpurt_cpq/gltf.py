@@ -1,5 +1,6 @@
 """glTF 2.0 ingest (cp_gltf_*): triangle primitives, their placement, and
-their vertex normals and material factors for shading.
+for shading their vertex normals, texture coordinates and tangents, material
+factors and texture references (images are not decoded).
 
 ``load_gltf`` copies what the library read into numpy arrays; ``world_mesh``
 flattens the instances into one world-space triangle soup for
@@ -27,6 +28,12 @@ class GltfScene:
     instance_world: np.ndarray      # (I, 4, 4) float32, row-major
     normals: np.ndarray        # (V, 3) float32, object space; zero where a primitive has none
     materials: np.ndarray      # (P, 8) float32: base colour rgb, emission rgb, metalness, roughness
+    texcoords: np.ndarray | None = None  # (V, 2) float32 TEXCOORD_0, zero where absent
+    tangents: np.ndarray | None = None   # (V, 4) float32 TANGENT (xyz, w), zero where absent
+    prim_tex: np.ndarray | None = None   # (P, 4) int32 glTF texture of base colour, emission, metal / rough, normal; -1
+    tex_image: np.ndarray | None = None  # (textures,) int32 image of each texture, -1 if none
+    image_uri: list | None = None        # per image its "uri" ("" if none)
+    image_view: np.ndarray | None = None  # (images,) int32 "bufferView" of each image, -1 if none
 
     def world_mesh(self) -> tuple[np.ndarray, np.ndarray]:
         """All instances in world space as one mesh (vertices, triangles)."""
@@ -45,26 +52,39 @@ class GltfScene:
     def world_shading(self) -> dict[str, np.ndarray]:
         """All instances in world space for shading, one object per instance
         (as Scene::load adds objects): per triangle its three vertices
-        ``verts`` (T, 3, 3) and normals ``normals`` (T, 3, 3; the instance's
-        inverse-transpose applied, not renormalised) and its object ``obj``
-        (T,); per object its primitive's ``materials`` (I, 8)."""
-        vs, ns, obj, mats = [], [], [], []
+        ``verts`` (T, 3, 3), normals ``normals`` (T, 3, 3; the instance's
+        inverse-transpose applied, not renormalised), texture coordinates
+        ``texcoords`` (T, 3, 2) and tangents ``tangents`` (T, 3, 4; xyz under
+        the inverse-transpose as the shader's modelIT, w kept) and its object
+        ``obj`` (T,); per object its primitive's ``materials`` (I, 8) and
+        glTF texture references ``obj_tex`` (I, 4)."""
+        vs, ns, tcs, tgs, obj, mats, otex = [], [], [], [], [], [], []
         for i, (p, w) in enumerate(zip(self.instance_primitive, self.instance_world)):
             lo, hi = self.vert_offsets[p], self.vert_offsets[p + 1]
             t = self.tris[self.tri_offsets[p]:self.tri_offsets[p + 1]]
             m = w[:3, :4].astype(np.float64)
             v = self.verts[lo:hi].astype(np.float64) @ m[:, :3].T + m[:, 3]
-            n = self.normals[lo:hi].astype(np.float64) @ np.linalg.inv(m[:, :3])
+            inv = np.linalg.inv(m[:, :3])
+            n = self.normals[lo:hi].astype(np.float64) @ inv
             vs.append(v[t])
             ns.append(n[t])
+            tc = self.texcoords[lo:hi] if self.texcoords is not None else np.zeros((hi - lo, 2), np.float32)
+            tg = self.tangents[lo:hi].astype(np.float64) if self.tangents is not None else np.zeros((hi - lo, 4))
+            tg = np.concatenate([tg[:, :3] @ inv, tg[:, 3:]], 1)
+            tcs.append(tc[t])
+            tgs.append(tg[t])
             obj.append(np.full(len(t), i, np.int32))
             mats.append(self.materials[p])
+            otex.append(self.prim_tex[p] if self.prim_tex is not None else np.full(4, -1, np.int32))
         if not vs:
             z = np.zeros((0, 3, 3), np.float32)
-            return {"verts": z, "normals": z.copy(), "obj": np.zeros(0, np.int32),
-                    "materials": np.zeros((0, 8), np.float32)}
+            return {"verts": z, "normals": z.copy(), "texcoords": np.zeros((0, 3, 2), np.float32),
+                    "tangents": np.zeros((0, 3, 4), np.float32), "obj": np.zeros(0, np.int32),
+                    "materials": np.zeros((0, 8), np.float32), "obj_tex": np.zeros((0, 4), np.int32)}
         return {"verts": np.concatenate(vs).astype(np.float32), "normals": np.concatenate(ns).astype(np.float32),
-                "obj": np.concatenate(obj), "materials": np.stack(mats).astype(np.float32)}
+                "texcoords": np.concatenate(tcs).astype(np.float32), "tangents": np.concatenate(tgs).astype(np.float32),
+                "obj": np.concatenate(obj), "materials": np.stack(mats).astype(np.float32),
+                "obj_tex": np.stack(otex).astype(np.int32)}
 
 
 def _array(ptr, count, dtype):
@@ -96,6 +116,18 @@ def load_gltf(path: str) -> GltfScene:
         check(lib.cp_gltf_shading(h, byref(ns), byref(pn), byref(pm)), "cp_gltf_shading")
         normals = _array(pn, int(voff[-1]) * 3, np.float32).reshape(-1, 3)
         materials = _array(pm, ns.value * 8, np.float32).reshape(-1, 8)
-        return GltfScene(verts, tris, voff, toff, prim, world, normals, materials)
+        nt_, ntex, nim = c_int32(), c_int32(), c_int32()
+        ptc, ptg, ppt, pti, puri, pview = (c_void_p() for _ in range(6))
+        check(lib.cp_gltf_textures(h, byref(nt_), byref(ptc), byref(ptg), byref(ppt), byref(ntex), byref(pti),
+                                   byref(nim), byref(puri), byref(pview)), "cp_gltf_textures")
+        texcoords = _array(ptc, int(voff[-1]) * 2, np.float32).reshape(-1, 2)
+        tangents = _array(ptg, int(voff[-1]) * 4, np.float32).reshape(-1, 4)
+        prim_tex = _array(ppt, nt_.value * 4, np.int32).reshape(-1, 4)
+        tex_image = _array(pti, ntex.value, np.int32)
+        uris = ctypes.cast(puri, ctypes.POINTER(ctypes.c_char_p)) if nim.value else None
+        image_uri = [uris[i].decode("utf-8", "replace") for i in range(nim.value)] if uris else []
+        image_view = _array(pview, nim.value, np.int32)
+        return GltfScene(verts, tris, voff, toff, prim, world, normals, materials, texcoords, tangents, prim_tex,
+                         tex_image, image_uri, image_view)
     finally:
         lib.cp_gltf_free(h)

@@ -318,7 +318,18 @@ CP_API cp_status cp_query_host_async(const cp_mesh* mesh, const float* queries, 
  * primitive 8 floats, the material factors parse_mesh copies
  * (scene.cpp:286-299): baseColorFactor rgb, emissiveFactor rgb,
  * metallicFactor, roughnessFactor, with glTF's defaults (1, 0, 1, 1) and the
- * default material for a primitive without one.  Textures are not read.
+ * default material for a primitive without one.
+ *
+ * Texture inputs (cp_gltf_textures): per vertex TEXCOORD_0 (2 floats) and
+ * TANGENT (4 floats: xyz, w), paired with the vertices as the normals are and
+ * zero where absent or not FLOAT VEC2 / VEC4 (scene.cpp:188-265, 303-310); per
+ * primitive the glTF texture index of its material's baseColorTexture,
+ * emissiveTexture, metallicRoughnessTexture and normalTexture, -1 where
+ * absent (Scene_Obj's *_tex, scene.cpp:294-302; an index past the file's
+ * textures is refused); per texture its image ("source", -1 if absent or out
+ * of range); per image its "uri" (empty if none) and "bufferView" (-1 if
+ * none).  Image files are not decoded: a caller decodes them to RGBA8 for
+ * cp_shade_scene_textures.
  *
  * Arrays returned by cp_gltf_* are owned by the handle and live until
  * cp_gltf_free.  Errors (unreadable file, malformed JSON, an accessor out of
@@ -336,6 +347,10 @@ CP_API cp_status cp_gltf_instances(const cp_gltf* scene, int32_t* num_instances,
                                    const int32_t** primitive, const float** world);
 CP_API cp_status cp_gltf_shading(const cp_gltf* scene, int32_t* num_primitives, const float** normals,
                                  const float** materials);
+CP_API cp_status cp_gltf_textures(const cp_gltf* scene, int32_t* num_primitives, const float** texcoords,
+                                  const float** tangents, const int32_t** prim_tex, int32_t* num_textures,
+                                  const int32_t** tex_image, int32_t* num_images, const char* const** image_uri,
+                                  const int32_t** image_view);
 
 /* ---- ray queries ----------------------------------------------------------- */
 

@@ -228,6 +228,80 @@ def test_shading_input_errors(cpq, tmp_path):
             cpq.load_gltf(str(_write(tmp_path, doc, data, "data")))
 
 
+def _texture_scene():
+    doc, data, qn = _shading_scene()
+    tc = np.float32([[0, 0], [1, 0], [1, 1], [0, 1]])
+    tg = np.float32([[1, 0, 0, 1], [1, 0, 0, 1], [1, 0, 0, -1], [0, 1, 0, 1]])
+    a_tc, data = _append(doc, data, tc, 5126, "VEC2")
+    a_tc_short, data = _append(doc, data, tc[:3], 5126, "VEC2")  # fewer than the fan's vertices
+    a_tc_u16, data = _append(doc, data, np.uint16([[0, 0], [65535, 0], [65535, 65535], [0, 65535]]), 5123, "VEC2")
+    a_tg, data = _append(doc, data, tg, 5126, "VEC4")
+    prims = doc["meshes"]
+    prims[0]["primitives"][0]["attributes"].update(TEXCOORD_0=a_tc, TANGENT=a_tg)
+    prims[1]["primitives"][1]["attributes"]["TEXCOORD_0"] = a_tc_short
+    prims[1]["primitives"][0]["attributes"]["TEXCOORD_0"] = a_tc_u16  # normalised shorts: not read
+    doc["materials"][0]["pbrMetallicRoughness"].update(baseColorTexture={"index": 1},
+                                                       metallicRoughnessTexture={"index": 2})
+    doc["materials"][0]["emissiveTexture"] = {"index": 0}
+    doc["materials"][0]["normalTexture"] = {"index": 1, "scale": 1.0}
+    doc["materials"][1]["normalTexture"] = {"index": 2}
+    doc["textures"] = [{"source": 0}, {"source": 1, "sampler": 0}, {"source": 7}]
+    doc["images"] = [{"uri": "albedo.jpg"}, {"bufferView": 0, "mimeType": "image/png"}]
+    return doc, data, tc, tg
+
+
+@pytest.mark.parametrize("mode", ["data", "glb"])
+def test_texture_inputs(cpq, tmp_path, mode):
+    """TEXCOORD_0 and TANGENT paired with the vertices as the normals are
+    (zero past the accessor's count, without one, or when not FLOAT VEC2 /
+    VEC4, as parse_mesh skips the types it does not read), each primitive's
+    texture references, each texture's image and each image's uri or view."""
+    doc, data, tc, tg = _texture_scene()
+    s = cpq.load_gltf(str(_write(tmp_path, doc, data, mode)))
+    assert s.texcoords.shape == (s.verts.shape[0], 2) and s.tangents.shape == (s.verts.shape[0], 4)
+    np.testing.assert_array_equal(s.texcoords[0:4], tc)
+    np.testing.assert_array_equal(s.tangents[0:4], tg)
+    np.testing.assert_array_equal(s.texcoords[4:9], np.zeros((5, 2)))   # strip: unsigned shorts, not read
+    np.testing.assert_array_equal(s.texcoords[9:12], tc[:3])            # fan: three, then zero
+    np.testing.assert_array_equal(s.texcoords[12:], np.zeros((s.verts.shape[0] - 12, 2)))
+    np.testing.assert_array_equal(s.tangents[4:], np.zeros((s.verts.shape[0] - 4, 4)))
+    np.testing.assert_array_equal(s.prim_tex, np.int32([[1, 0, 2, 1], [-1, -1, -1, 2], [-1, -1, -1, -1],
+                                                        [1, 0, 2, 1]]))
+    np.testing.assert_array_equal(s.tex_image, [0, 1, -1])
+    assert s.image_uri == ["albedo.jpg", ""]
+    np.testing.assert_array_equal(s.image_view, [-1, 0])
+    # world space: texture coordinates per triangle corner, tangents under the
+    # instance's inverse-transpose with w kept, the texture references per object
+    w = s.world_shading()
+    T = w["verts"].shape[0]
+    assert w["texcoords"].shape == (T, 3, 2) and w["tangents"].shape == (T, 3, 4)
+    assert w["obj_tex"].shape == (len(s.instance_primitive), 4)
+    i0 = int(np.nonzero(s.instance_primitive == 0)[0][0])
+    m = s.instance_world[i0][:3, :3].astype(np.float64)
+    t0 = s.tris[s.tri_offsets[0]:s.tri_offsets[1]]
+    first = int(np.nonzero(w["obj"] == i0)[0][0])
+    want = np.concatenate([tg[t0[0], :3] @ np.linalg.inv(m), tg[t0[0], 3:]], 1)
+    np.testing.assert_allclose(w["tangents"][first], want, rtol=1e-6, atol=1e-6)
+    np.testing.assert_array_equal(w["texcoords"][first], tc[t0[0]])
+    np.testing.assert_array_equal(w["obj_tex"][i0], s.prim_tex[0])
+
+
+def test_texture_input_errors(cpq, tmp_path):
+    from gpurt_cpq._lib import CpError
+
+    for change, msg in (
+        (lambda d: d["materials"][0]["pbrMetallicRoughness"].__setitem__("baseColorTexture", {"index": 3}),
+         "baseColorTexture index out of range"),
+        (lambda d: d["materials"][1].__setitem__("normalTexture", {"index": -2}), "normalTexture index out of range"),
+        (lambda d: d["accessors"][d["meshes"][0]["primitives"][0]["attributes"]["TANGENT"]].__setitem__(
+            "count", 999), "past the end"),
+    ):
+        doc, data, _, _ = _texture_scene()
+        change(doc)
+        with pytest.raises(CpError, match=msg):
+            cpq.load_gltf(str(_write(tmp_path, doc, data, "data")))
+
+
 def test_errors_are_reported(cpq, tmp_path):
     from gpurt_cpq._lib import CP_ERROR_INVALID_VALUE, CpError
 
