@@ -1264,6 +1264,15 @@ extern "C" CP_API cp_status cp_shade_scene_textures(cp_shade_scene* s, const flo
             return set_error(CP_ERROR_INVALID_VALUE, "texture " + std::to_string(k) + " has a size outside 1..2^20");
         off[k + 1] = off[k] + w * h;
     }
+    // the decode kernel reads the texels: they must be device memory
+    if (ntex > 0) {
+        cudaPointerAttributes at{};
+        if (cudaPointerGetAttributes(&at, texels) != cudaSuccess ||
+            (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged)) {
+            cudaGetLastError();
+            return set_error(CP_ERROR_INVALID_VALUE, "cp_shade_scene_textures: texels must be device memory");
+        }
+    }
     if (obj_tex)
         for (int64_t i = 0; i < 4 * (int64_t)s->nobj; ++i)
             if (obj_tex[i] < -1 || obj_tex[i] >= ntex)

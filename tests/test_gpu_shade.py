@@ -206,6 +206,15 @@ def test_textured_larger_frame_and_refusals(cuda):
         gs.set_textures(texcoords=torch.from_numpy(sc.texcoords).to(cuda), textures=sc.textures, obj_tex=bad)
     with pytest.raises(CpError, match="size"):
         gs.set_textures(textures=[np.zeros((0, 4, 4), np.uint8)])
+    # texels in host memory: refused before the decode kernel could read them
+    from ctypes import c_void_p
+
+    from gpurt_cpq._lib import lib
+    host = np.zeros(4 * 4 * 4, np.uint8)
+    size = np.int32([[4, 4]])
+    assert lib.cp_shade_scene_textures(gs._h, None, None, 1, c_void_p(size.ctypes.data), c_void_p(host.ctypes.data),
+                                       None, None) != 0
+    assert b"device memory" in lib.cp_last_error_string()
     # the refused calls left the scene as it was (no textures)
     _same(gs.render(_cam(cam), integrator=S.MIS, samples=2, seed=4).cpu().numpy(),
           plain.render(cam, integrator=S.MIS, samples=2, seed=4))
