@@ -828,6 +828,39 @@ CP_API cp_status cp_batch_destroy(cp_batch* bt) {
     return CP_SUCCESS;
 }
 
+CP_API cp_status cp_batch_save(const cp_batch* bt, const char* path) {
+    if (!bt || !path) return fail(CP_ERROR_INVALID_VALUE, "batch or path is NULL");
+    std::string why;
+    cudaError_t e = bvh_save(const_cast<cp_batch*>(bt)->bvh, path, &why);
+    if (!why.empty()) return fail(CP_ERROR_INVALID_VALUE, "cp_batch_save: " + why);
+    if (e != cudaSuccess) return cuda_fail(e, "cp_batch_save");
+    return CP_SUCCESS;
+}
+
+CP_API cp_status cp_batch_load(const char* path, cp_stream_t stream, cp_batch** out) {
+    if (!out || !path) return fail(CP_ERROR_INVALID_VALUE, "path or out is NULL");
+    *out = nullptr;
+    cp_batch* bt = new (std::nothrow) cp_batch();
+    if (!bt) return fail(CP_ERROR_OUT_OF_MEMORY, "host allocation of the handle failed");
+    std::string why;
+    bool bad = false;
+    cudaError_t e = bvh_load(bt->bvh, path, reinterpret_cast<cudaStream_t>(stream), &why, &bad);
+    if (e == cudaSuccess && !bad) {
+        if (alloc_fault()) e = cudaErrorMemoryAllocation;
+        else e = cudaMalloc(&bt->d_qoff, sizeof(int64_t) * (bt->bvh.nmeshes + 1));
+    }
+    if (bad || e != cudaSuccess) {
+        if (bt->d_qoff) cudaFree(bt->d_qoff);
+        bt->d_qoff = nullptr;
+        bvh_free(bt->bvh);
+        delete bt;
+        if (bad) return fail(CP_ERROR_INVALID_VALUE, std::string("cp_batch_load: ") + path + ": " + why);
+        return cuda_fail(e, "cp_batch_load");
+    }
+    *out = bt;
+    return CP_SUCCESS;
+}
+
 CP_API cp_status cp_batch_info(const cp_batch* bt, int32_t* nmeshes, int64_t* num_wide,
                                int64_t* num_tris, int32_t* stack_bound) {
     if (!bt) return fail(CP_ERROR_INVALID_VALUE, "batch is NULL");

@@ -129,6 +129,8 @@ SIGNATURES = {
     "cp_batch_query": (c_int32, [c_void_p, c_void_p, c_void_p, POINTER(QueryOpts), c_void_p,
                                  c_void_p, c_void_p, c_void_p, c_void_p, c_size_t, c_int32,
                                  c_void_p]),
+    "cp_batch_save": (c_int32, [c_void_p, c_char_p]),
+    "cp_batch_load": (c_int32, [c_char_p, c_void_p, POINTER(c_void_p)]),
     "cp_debug_fail_allocation": (None, [c_int64]),
     "cp_debug_order_sort": (c_int32, [c_void_p, c_int32, c_int64, c_int32, c_int32, c_void_p, c_void_p]),
     "cp_query_order": (c_int32, [c_void_p, c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),

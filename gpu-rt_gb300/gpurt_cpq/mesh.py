@@ -358,6 +358,25 @@ class Batch:
                                              _stream(stream), byref(h)), "cp_batch_create_leaves")
         self._h = h
 
+    def save(self, path) -> None:
+        """Write the built batch to a file (cp_batch_save)."""
+        check(lib.cp_batch_save(self._h, str(path).encode()), "cp_batch_save")
+
+    @classmethod
+    def load(cls, path, *, stream=None) -> "Batch":
+        """A batch read from a file cp_batch_save (or cp_mesh_save, as a batch
+        of one) wrote, without a build (cp_batch_load)."""
+        h = c_void_p()
+        check(lib.cp_batch_load(str(path).encode(), _stream(stream), byref(h)), "cp_batch_load")
+        b = cls.__new__(cls)
+        b._h = h
+        b.nmeshes = int(b.info()["nmeshes"])
+        # the build's branching, leaf size and collapse from the file's header
+        k, leaf, collapse = np.fromfile(str(path), dtype=np.int32, count=5)[2:5]
+        b.opts = build_opts(int(k), int(leaf), "sah" if collapse == CP_COLLAPSE_SAH else "count")
+        b.vert_offsets = b.tri_offsets = b.leaf_sizes = None
+        return b
+
     def close(self) -> None:
         if getattr(self, "_h", None) and self._h.value:
             lib.cp_batch_destroy(self._h)

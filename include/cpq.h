@@ -733,6 +733,14 @@ CP_API cp_status cp_batch_autotune(const float* verts, const int64_t* vert_offse
 CP_API cp_status cp_mesh_save(const cp_mesh* mesh, const char* path);
 CP_API cp_status cp_mesh_load(const char* path, cp_stream_t stream, cp_mesh** out);
 
+/* A batch (cp_batch_create*) written and read back the same way: the file
+ * holds every mesh's tree, leaf size, frame and offsets; the load checks the
+ * whole file on the host (each mesh's tree within its triangles) before
+ * anything reaches the GPU.  cp_batch_load also reads a one-mesh file as a
+ * batch of one; cp_mesh_load refuses a batch file. */
+CP_API cp_status cp_batch_save(const cp_batch* batch, const char* path);
+CP_API cp_status cp_batch_load(const char* path, cp_stream_t stream, cp_batch** out);
+
 /* Size class used by the autotuner cache: floor(log2(num_triangles)). */
 CP_API int32_t cp_size_class(int64_t num_triangles);
 

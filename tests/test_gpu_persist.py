@@ -84,6 +84,52 @@ def test_saved_mesh_answers_as_built(cpq, cuda, tmp_path, K, leaf, collapse):
     assert loaded.device_status() == 0
 
 
+@pytest.mark.gpu
+def test_saved_batch_answers_as_built(cpq, cuda, tmp_path):
+    """A batch with a leaf size per mesh, saved and read back: the same
+    answers, trees and boxes; a batch file is refused by cp_mesh_load, a
+    mesh file reads as a batch of one, and a truncated batch file is
+    refused."""
+    import torch
+
+    from gpurt_cpq import CpError
+    from gpurt_cpq import workloads as W
+
+    meshes, queries = W.batched(seed=3, nmeshes=9, tri_range=(200, 20000), q_range=(100, 8000))
+    V, voff, T, toff, Q, qoff = W.concat_batch(meshes, queries)
+    leaves = np.int32([1, 2, 4, 8, 2, 2, 4, 1, 8])
+    b = cpq.Batch(dev(V, cuda), voff, dev(T, cuda), toff, branching=4, leaf_sizes=leaves)
+    path = tmp_path / "batch.bvh"
+    b.save(path)
+    loaded = cpq.Batch.load(path)
+    assert loaded.nmeshes == 9 and loaded.opts.branching == 4
+    assert loaded.info() == b.info()
+    qd = dev(Q, cuda)
+    for opts in (cpq.query_opts(), cpq.query_opts(seed_chunk=4), cpq.query_opts(traversal="thread")):
+        a, c = b.query(qd, qoff, want_bary=True, opts=opts), loaded.query(qd, qoff, want_bary=True, opts=opts)
+        for k in ("dist", "tri", "point", "bary"):
+            assert torch.equal(getattr(a, k), getattr(c, k)), k
+    eb, lb = b.export_build(), loaded.export_build()
+    for k in eb:
+        np.testing.assert_array_equal(eb[k], lb[k], err_msg=k)
+    np.testing.assert_array_equal(b.export_wide()["boxes"].view(np.uint32),
+                                  loaded.export_wide()["boxes"].view(np.uint32))
+    with pytest.raises(CpError, match="batch of 9 meshes"):
+        cpq.Mesh.load(path)
+    data = path.read_bytes()
+    (tmp_path / "short.bvh").write_bytes(data[:-7])
+    with pytest.raises(CpError, match="cp_batch_load"):
+        cpq.Batch.load(tmp_path / "short.bvh")
+    # a mesh file as a batch of one
+    v, t = meshes[2][0], meshes[2][1]
+    m = cpq.Mesh(dev(v, cuda), dev(t, cuda), branching=4, leaf_size=4)
+    m.save(tmp_path / "mesh.bvh")
+    one = cpq.Batch.load(tmp_path / "mesh.bvh")
+    q = dev(queries[2], cuda)
+    r1, r2 = m.query(q), one.query(q, [0, q.shape[0]])
+    assert torch.equal(r1.dist, r2.dist) and torch.equal(r1.tri, r2.tri)
+
+
 def _refused(lib, path):
     from ctypes import byref, c_void_p
 
