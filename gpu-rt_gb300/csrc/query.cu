@@ -1059,7 +1059,7 @@ __device__ __forceinline__ uint32_t hilbert3_10(uint32_t x, uint32_t y, uint32_t
 template <typename KeyT>
 __global__ void k_query_keys(const float* __restrict__ q, int64_t nq, const int64_t* __restrict__ qoff,
                              int nmeshes, const float* __restrict__ frame, int qbits,
-                             KeyT* __restrict__ keys, int32_t* __restrict__ vals) {
+                             KeyT* __restrict__ keys) {
     int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= nq) return;
     const int m = nmeshes > 1 ? mesh_of(qoff, nmeshes, i) : 0;
@@ -1074,7 +1074,6 @@ __global__ void k_query_keys(const float* __restrict__ q, int64_t nq, const int6
     }
     const uint64_t h = qbits == 10 ? hilbert3_10(c[0], c[1], c[2]) : hilbert3(c[0], c[1], c[2], qbits);
     keys[i] = (KeyT)(((uint64_t)m << (3 * qbits)) | h);
-    vals[i] = (int32_t)i;
 }
 
 __device__ __forceinline__ void atomic_min_pos(float* addr, float v) {
@@ -2139,7 +2138,7 @@ cudaError_t order_points(const Bvh& b, const float* queries, int64_t nq, const i
             uint32_t* k32 = reinterpret_cast<uint32_t*>(keys);
             uint32_t* k32_alt = reinterpret_cast<uint32_t*>(keys_alt);
             k_query_keys<uint32_t><<<kgrid, 256, 0, st>>>(queries, nq, d_qoff, b.nmeshes, frame, qbits,
-                                                          k32, vals); note_launch();
+                                                          k32); note_launch();
             e = cudaGetLastError();
             if (e != cudaSuccess) return e;
             if (keys_out) {
@@ -2147,14 +2146,14 @@ cudaError_t order_points(const Bvh& b, const float* queries, int64_t nq, const i
                 if (e != cudaSuccess) return e;
             }
             e = radix_sort_pairs<uint32_t>(k32, vals, k32_alt, vals_alt, nq, begin_bit, key_bits,
-                                           w + L.sort_ws, L.sort_ws_bytes, st, &in_alt);
+                                           w + L.sort_ws, L.sort_ws_bytes, st, &in_alt, true);
         } else {
             k_query_keys<uint64_t><<<kgrid, 256, 0, st>>>(queries, nq, d_qoff, b.nmeshes, frame, qbits,
-                                                          keys, vals); note_launch();
+                                                          keys); note_launch();
             e = cudaGetLastError();
             if (e != cudaSuccess) return e;
             e = radix_sort_pairs<uint64_t>(keys, vals, keys_alt, vals_alt, nq, begin_bit, key_bits,
-                                           w + L.sort_ws, L.sort_ws_bytes, st, &in_alt);
+                                           w + L.sort_ws, L.sort_ws_bytes, st, &in_alt, true);
         }
         if (e != cudaSuccess) return e;
         perm = in_alt ? vals_alt : vals;

@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(kSortThreads) k_scatter(const KeyT* __restrict
         const int j = wbase + r * 32 + lane;
         if (j < tile_n) {
             k[r] = keys_in[base + j];
-            v[r] = vals_in[base + j];
+            v[r] = vals_in ? vals_in[base + j] : (int32_t)(base + j);  // no values: the identity
         } else {
             k[r] = 0;
             v[r] = 0;
@@ -362,7 +362,7 @@ cudaError_t sort_pass(const KeyT* ki, const int32_t* vi, KeyT* ko, int32_t* vo, 
 template <typename KeyT>
 cudaError_t radix_sort_pairs(KeyT* keys, int32_t* vals, KeyT* keys_alt, int32_t* vals_alt,
                              int64_t n, int begin_bit, int end_bit, void* workspace,
-                             size_t workspace_bytes, cudaStream_t stream, bool* in_alt) {
+                             size_t workspace_bytes, cudaStream_t stream, bool* in_alt, bool identity_vals) {
     *in_alt = false;
     if (n <= 1 || end_bit <= begin_bit) return cudaSuccess;
     if (workspace_bytes < radix_sort_workspace_bytes(n)) return cudaErrorInvalidValue;
@@ -378,11 +378,14 @@ cudaError_t radix_sort_pairs(KeyT* keys, int32_t* vals, KeyT* keys_alt, int32_t*
     KeyT *ki = keys, *ko = keys_alt;
     int32_t *vi = vals, *vo = vals_alt;
     bool alt = false;
+    bool first = true;
     for (int shift = begin_bit; shift < end_bit; shift += digit_bits) {
         const int bits = std::min(digit_bits, end_bit - shift);
+        const int32_t* vin = first && identity_vals ? nullptr : vi;  // the first pass makes the identity
+        first = false;
         cudaError_t e = digit_bits == 10
-                            ? sort_pass<KeyT, 10>(ki, vi, ko, vo, n, shift, bits, counts, scan_ws, scan_bytes, stream)
-                            : sort_pass<KeyT, 8>(ki, vi, ko, vo, n, shift, bits, counts, scan_ws, scan_bytes, stream);
+                            ? sort_pass<KeyT, 10>(ki, vin, ko, vo, n, shift, bits, counts, scan_ws, scan_bytes, stream)
+                            : sort_pass<KeyT, 8>(ki, vin, ko, vo, n, shift, bits, counts, scan_ws, scan_bytes, stream);
         if (e != cudaSuccess) return e;
         std::swap(ki, ko);
         std::swap(vi, vo);
@@ -393,8 +396,8 @@ cudaError_t radix_sort_pairs(KeyT* keys, int32_t* vals, KeyT* keys_alt, int32_t*
 }
 
 template cudaError_t radix_sort_pairs<uint32_t>(uint32_t*, int32_t*, uint32_t*, int32_t*, int64_t,
-                                                int, int, void*, size_t, cudaStream_t, bool*);
+                                                int, int, void*, size_t, cudaStream_t, bool*, bool);
 template cudaError_t radix_sort_pairs<uint64_t>(uint64_t*, int32_t*, uint64_t*, int32_t*, int64_t,
-                                                int, int, void*, size_t, cudaStream_t, bool*);
+                                                int, int, void*, size_t, cudaStream_t, bool*, bool);
 
 }  // namespace cpq

@@ -20,13 +20,15 @@ cudaError_t ensure_smem_limit(const void* kernel, size_t smem);
 size_t radix_sort_workspace_bytes(int64_t n);
 
 // Sort keys[0..n) ascending with their values, stably, on bits
-// [begin_bit, end_bit) (8 bits per pass).  keys_alt / vals_alt are buffers
-// of n elements.  On return *in_alt tells which pair of buffers holds the
-// result.  KeyT is uint32_t or uint64_t.
+// [begin_bit, end_bit) (8 or 10 bits per pass).  keys_alt / vals_alt are
+// buffers of n elements.  With identity_vals the values are 0..n-1 and vals
+// is not read (the first pass makes them).  On return *in_alt tells which
+// pair of buffers holds the result.  KeyT is uint32_t or uint64_t.
 template <typename KeyT>
 cudaError_t radix_sort_pairs(KeyT* keys, int32_t* vals, KeyT* keys_alt, int32_t* vals_alt,
                              int64_t n, int begin_bit, int end_bit, void* workspace,
-                             size_t workspace_bytes, cudaStream_t stream, bool* in_alt);
+                             size_t workspace_bytes, cudaStream_t stream, bool* in_alt,
+                             bool identity_vals = false);
 
 // Bytes of workspace exclusive_scan_u32 needs for m elements.
 size_t scan_workspace_bytes(int64_t m);
