@@ -397,6 +397,195 @@ __device__ void precise_closest(float qx, float qy, float qz, const TriRec& r, f
     ow = ff_to_float(w);
 }
 
+// q_i - s_i - t1 - t2 for exact float-float products t1, t2: one rounding of
+// the three-term sum's error parts.
+__device__ __forceinline__ ff ff_sub3(ff d, ff t1, ff t2) {
+    const ff s1 = ff_two_sum(d.hi, -t1.hi);
+    const ff s2 = ff_two_sum(s1.hi, -t2.hi);
+    const float lo = __fadd_rn(__fadd_rn(__fsub_rn(__fsub_rn(d.lo, t1.lo), t2.lo), s1.lo), s2.lo);
+    return ff_fast_two_sum(s2.hi, lo);
+}
+// alpha * e for FP32 alpha and float-float e, to float-float precision.
+__device__ __forceinline__ ff ff_scale_f(float alpha, ff e) {
+    ff t = ff_two_prod(alpha, e.hi);
+    t.lo = __fmaf_rn(alpha, e.lo, t.lo);
+    return t;
+}
+// e . r for float-float vectors, rounded once to FP32.
+__device__ __forceinline__ float ff3_dot_f(ff ex, ff ey, ff ez, ff rx, ff ry, ff rz) {
+    ff px = ff_two_prod(ex.hi, rx.hi), py = ff_two_prod(ey.hi, ry.hi), pz = ff_two_prod(ez.hi, rz.hi);
+    px.lo = __fmaf_rn(ex.hi, rx.lo, __fmaf_rn(ex.lo, rx.hi, px.lo));
+    py.lo = __fmaf_rn(ey.hi, ry.lo, __fmaf_rn(ey.lo, ry.hi, py.lo));
+    pz.lo = __fmaf_rn(ez.hi, rz.lo, __fmaf_rn(ez.lo, rz.hi, pz.lo));
+    const ff t = ff_add(ff_add(px, py), pz);
+    return __fadd_rn(t.hi, t.lo);
+}
+
+// The winner's closest point from its FP32 frame record and exact vertices,
+// at a fraction of precise_closest's float-float work; false when the lane
+// must take precise_closest instead.
+//   1. Feature: the query's in-plane coordinates (u, w) in the frame give
+//      the margins of the seven Voronoi regions (face, edges ab / ac / bc,
+//      vertices a / b / c); the largest margin picks the feature.  FP32
+//      puts (u, w) within delta = 1e-6 (|q - a|_1 + perimeter) of the exact
+//      values, so a feature picked with a smaller margin may be a neighbour
+//      of the true one, whose point lies within ~delta of the true closest
+//      point: a distance error of at most delta^2 / (2 d^2), negligible unless
+//      the query is close to the plane (then precise_closest).
+//   2. Residual: r = q - (s + alpha (P - s) + beta (R - s)) for the
+//      feature's start vertex s and FP32 parameters, in float-float on exact
+//      vertex differences, so the point lies exactly on the feature's line
+//      or plane whatever alpha and beta are.
+//   3. Two refinements, each restricted to the feature (both in-plane
+//      directions on the face, the edge's direction on an edge, none at a
+//      vertex) and applied to r as parameter changes times the exact edge
+//      vectors (exact two-products), so the point never leaves the
+//      feature's plane or line.  The first takes the move from r's FP32
+//      projection on the frame axes: well conditioned on slivers, it leaves
+//      ~2e-7 of the first step's error, so a query farther than 1e-9 of the
+//      scale from the plane gets its distance to ~1e-9 relative (closer ones
+//      take precise_closest); but the FP32 axes are ~6e-8 off the plane,
+//      which leaks ~6e-8 of r's normal part into the move.  The second
+//      removes that: r's components along the exact edge vectors
+//      (float-float dot products, no leak), solved for the parameters in
+//      FP32, which is accurate enough for a correction that small.
+//   4. |r| in FP32 from r's leading parts (a sum of squares, no cancellation):
+//      a few ulps.  The point is q - r; barycentrics follow the feature and
+//      are clamped to it.
+// Zero-area triangles take precise_closest.
+__device__ __forceinline__ bool closest_by_frame(float qx, float qy, float qz, const TriRec& r, const FastTri& f,
+                                                 float& dist, float& px, float& py, float& pz, float& ov,
+                                                 float& ow) {
+    if (__float_as_uint(r.p2.z) & kTriDegenerate) return false;
+    const float ax = r.p0.x, ay = r.p0.y, az = r.p0.z;
+    const float bxv = r.p0.w, byv = r.p1.x, bzv = r.p1.y;
+    const float cxv = r.p1.z, cyv = r.p1.w, czv = r.p2.x;
+    const float apx = qx - ax, apy = qy - ay, apz = qz - az;
+    const float u = fmaf(f.p1.x, apx, fmaf(f.p1.y, apy, f.p1.z * apz));
+    const float w = fmaf(f.p2.x, apx, fmaf(f.p2.y, apy, f.p2.z * apz));
+    const float h = fmaf(f.p3.x, apx, fmaf(f.p3.y, apy, f.p3.z * apz));
+    const float L1 = f.p0.w, x2 = f.p1.w, y2 = f.p2.w, bx = f.p3.w;
+    const float L2 = sqrtf(fmaf(x2, x2, y2 * y2)), L3 = sqrtf(fmaf(bx, bx, y2 * y2));
+    const float il2 = f.p4.x * L2, il3 = f.p4.y * L3;  // 1 / |ac|, 1 / |bc|
+    const float bu = u - L1;
+    // outside distances of the three edge lines, positions along the edges
+    const float A1 = -w, A2 = fmaf(w, x2, -u * y2) * il2, A3 = fmaf(bu, y2, -w * bx) * il3;
+    const float P1 = u, P2 = fmaf(u, x2, w * y2) * il2, P3 = fmaf(bu, bx, w * y2) * il3;
+    // margins: face, ab, ac, bc, a, b, c; the largest wins
+    float mbest = min3f(-A1, -A2, -A3);
+    int feat = 0;
+    const float m1 = min3f(A1, P1, L1 - P1), m2 = min3f(A2, P2, L2 - P2), m3 = min3f(A3, P3, L3 - P3);
+    const float m4 = fminf(-P1, -P2), m5 = fminf(P1 - L1, -P3), m6 = fminf(P2 - L2, P3 - L3);
+    if (m1 > mbest) { mbest = m1; feat = 1; }
+    if (m2 > mbest) { mbest = m2; feat = 2; }
+    if (m3 > mbest) { mbest = m3; feat = 3; }
+    if (m4 > mbest) { mbest = m4; feat = 4; }
+    if (m5 > mbest) { mbest = m5; feat = 5; }
+    if (m6 > mbest) { mbest = m6; feat = 6; }
+    const float scale = fabsf(apx) + fabsf(apy) + fabsf(apz) + L1 + L2 + L3;
+    const float delta = 1e-6f * scale, ah = fabsf(h);
+    // (a frame whose edge lengths or inverses are zero or not finite, from
+    // extreme scales, also goes to precise_closest)
+    if (!(ah >= 1e-9f * scale) || (mbest < delta && ah < 2.3e3f * delta) || !(L1 > 0.0f && y2 > 0.0f) ||
+        !(il2 < INFINITY && il3 < INFINITY && scale < INFINITY))
+        return false;
+    const float iL1 = __frcp_rn(L1), iy2 = __frcp_rn(y2);
+
+    // start vertex s and the two others (cyclic), the parameters, the
+    // refinement direction (dx, dy) in frame coordinates (face: both axes)
+    const bool from_b = feat == 3 || feat == 5, from_c = feat == 6;
+    const float sx = from_b ? bxv : (from_c ? cxv : ax), sy = from_b ? byv : (from_c ? cyv : ay),
+                sz = from_b ? bzv : (from_c ? czv : az);
+    const float Px = from_b ? cxv : (from_c ? ax : bxv), Py = from_b ? cyv : (from_c ? ay : byv),
+                Pz = from_b ? czv : (from_c ? az : bzv);
+    const float Rx = from_b ? ax : (from_c ? bxv : cxv), Ry = from_b ? ay : (from_c ? byv : cyv),
+                Rz = from_b ? az : (from_c ? bzv : czv);
+    const float wf = w * iy2, vf = (u - wf * x2) * iL1;  // face barycentrics
+    float alpha = 0.0f, beta = 0.0f, dx = 0.0f, dy = 0.0f;
+    if (feat == 0) { alpha = vf; beta = wf; }
+    else if (feat == 1) { alpha = P1 * iL1; dx = 1.0f; }
+    else if (feat == 2) { beta = P2 * il2; dx = x2 * il2; dy = y2 * il2; }
+    else if (feat == 3) { alpha = P3 * il3; dx = bx * il3; dy = y2 * il3; }
+    // exact edge vectors from s, the residual
+    const ff EPx = ff_two_sum(Px, -sx), EPy = ff_two_sum(Py, -sy), EPz = ff_two_sum(Pz, -sz);
+    const ff ERx = ff_two_sum(Rx, -sx), ERy = ff_two_sum(Ry, -sy), ERz = ff_two_sum(Rz, -sz);
+    ff rx = ff_sub3(ff_two_sum(qx, -sx), ff_scale_f(alpha, EPx), ff_scale_f(beta, ERx));
+    ff ry = ff_sub3(ff_two_sum(qy, -sy), ff_scale_f(alpha, EPy), ff_scale_f(beta, ERy));
+    ff rz = ff_sub3(ff_two_sum(qz, -sz), ff_scale_f(alpha, EPz), ff_scale_f(beta, ERz));
+    // first refinement: r's projection on the frame axes, within the feature
+    const float e1x = f.p1.x, e1y = f.p1.y, e1z = f.p1.z, e2x = f.p2.x, e2y = f.p2.y, e2z = f.p2.z;
+    const float rho1 = fmaf(e1x, rx.hi, fmaf(e1y, ry.hi, e1z * rz.hi));
+    const float rho2 = fmaf(e2x, rx.hi, fmaf(e2y, ry.hi, e2z * rz.hi));
+    const float along = fmaf(dx, rho1, dy * rho2);
+    // as parameter changes, applied along the exact edge vectors, so the
+    // point stays on the feature's plane or line
+    float da1 = 0.0f, db1 = 0.0f;
+    if (feat == 0) {
+        db1 = rho2 * iy2;
+        da1 = (rho1 - db1 * x2) * iL1;
+    } else if (feat == 1) {
+        da1 = along * iL1;
+    } else if (feat == 2) {
+        db1 = along * il2;
+    } else if (feat == 3) {
+        da1 = along * il3;
+    }
+    rx = ff_sub3(rx, ff_scale_f(da1, EPx), ff_scale_f(db1, ERx));
+    ry = ff_sub3(ry, ff_scale_f(da1, EPy), ff_scale_f(db1, ERy));
+    rz = ff_sub3(rz, ff_scale_f(da1, EPz), ff_scale_f(db1, ERz));
+    alpha += da1;
+    beta += db1;
+    // second refinement: r along the exact edge vectors, solved in FP32
+    if (feat <= 3) {
+        const float rP = ff3_dot_f(EPx, EPy, EPz, rx, ry, rz), rR = ff3_dot_f(ERx, ERy, ERz, rx, ry, rz);
+        const float gPP = fmaf(EPx.hi, EPx.hi, fmaf(EPy.hi, EPy.hi, EPz.hi * EPz.hi));
+        const float gRR = fmaf(ERx.hi, ERx.hi, fmaf(ERy.hi, ERy.hi, ERz.hi * ERz.hi));
+        const float gPR = fmaf(EPx.hi, ERx.hi, fmaf(EPy.hi, ERy.hi, EPz.hi * ERz.hi));
+        float da = 0.0f, db = 0.0f;
+        if (feat == 0) {
+            const float det = fmaf(gPP, gRR, -gPR * gPR);
+            if (det > 0.0f) {
+                const float id = __frcp_rn(det);
+                da = fmaf(gRR, rP, -gPR * rR) * id;
+                db = fmaf(gPP, rR, -gPR * rP) * id;
+            }
+        } else if (feat == 2) {
+            db = rR * __frcp_rn(gRR);
+        } else {
+            da = rP * __frcp_rn(gPP);
+        }
+        rx = ff_sub3(rx, ff_scale_f(da, EPx), ff_scale_f(db, ERx));
+        ry = ff_sub3(ry, ff_scale_f(da, EPy), ff_scale_f(db, ERy));
+        rz = ff_sub3(rz, ff_scale_f(da, EPz), ff_scale_f(db, ERz));
+        alpha += da;
+        beta += db;
+    }
+    dist = sqrtf(fmaf(rx.hi, rx.hi, fmaf(ry.hi, ry.hi, rz.hi * rz.hi)));
+    px = __fsub_rn(__fsub_rn(qx, rx.hi), rx.lo);
+    py = __fsub_rn(__fsub_rn(qy, ry.hi), ry.lo);
+    pz = __fsub_rn(__fsub_rn(qz, rz.hi), rz.lo);
+    // barycentrics (weights of b and c), clamped to the feature
+    float v = 0.0f, wb = 0.0f;
+    if (feat == 0) {
+        wb = __saturatef(beta);
+        v = fminf(__saturatef(alpha), 1.0f - wb);
+    } else if (feat == 1) {
+        v = __saturatef(alpha);
+    } else if (feat == 2) {
+        wb = __saturatef(beta);
+    } else if (feat == 3) {
+        wb = __saturatef(alpha);
+        v = 1.0f - wb;
+    } else if (feat == 5) {
+        v = 1.0f;
+    } else if (feat == 6) {
+        wb = 1.0f;
+    }
+    ov = v;
+    ow = wb;
+    return true;
+}
+
 struct TraverseArgs {
     const void* nodes;
     const TriRec* recs;   // exact vertices: the winner's re-evaluation
@@ -519,7 +708,8 @@ __global__ void __launch_bounds__(256) k_traverse(TraverseArgs a) {
             r.p0 = __ldg(rp);
             r.p1 = __ldg(rp + 1);
             r.p2 = __ldg(rp + 2);
-            precise_closest(qx, qy, qz, r, dist, px, py, pz, bv, bw);
+            if (!closest_by_frame(qx, qy, qz, r, load_fast(a.fast + best_rec), dist, px, py, pz, bv, bw))
+                precise_closest(qx, qy, qz, r, dist, px, py, pz, bv, bw);
         } else {
             atomicOr(a.status, 4u);
         }
@@ -570,7 +760,8 @@ __device__ __forceinline__ void write_result(const TraverseArgs& a, int64_t qi, 
         r.p0 = __ldg(rp);
         r.p1 = __ldg(rp + 1);
         r.p2 = __ldg(rp + 2);
-        precise_closest(qx, qy, qz, r, dist, px, py, pz, bv, bw);
+        if (!closest_by_frame(qx, qy, qz, r, load_fast(a.fast + best_rec), dist, px, py, pz, bv, bw))
+            precise_closest(qx, qy, qz, r, dist, px, py, pz, bv, bw);
     } else {
         atomicOr(a.status, 4u);
     }
