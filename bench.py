@@ -77,7 +77,7 @@ CANON_V_TRI = 44.413
 # the autotuner picks for this workload, from one ncu capture of
 # dram__bytes_read.sum + dram__bytes_write.sum on the same command; keyed by
 # leaf size so a run that picks another leaf reports null, not a stale figure
-NCU_TRAFFIC_PER_QUERY = {8: 378.3}
+NCU_TRAFFIC_PER_QUERY = {8: 378.1}
 # Adjoint per query: reads q 12 + triangle 4 + barycentrics 8 + upstream
 # gradient 4 + 3 vertex indices 12 + 3 vertices 36; writes d/dq 12 and three
 # atomic read-modify-writes of 12 B to d/dvertices (72)
