@@ -957,7 +957,7 @@ __device__ v3 camera_ray(const cp_shade_camera& cam, const cp_shade_params& p, u
 // ray walks, and it is the number of resident warps, not the spills, that
 // sets the pace — the 1920 x 1440 MIS frame took 395 ms at 2 blocks per SM
 // (128 registers), 321 ms at 4, 287 ms at 5, 281 ms at 6 and 286 ms at 8.
-template <int K>
+template <int K, int kIntegrator>
 __global__ void __launch_bounds__(256, 6) k_shade(ShadeArgs a) {
     const int x = blockIdx.x * 16 + (threadIdx.x & 15);
     const int y = blockIdx.y * 16 + (threadIdx.x >> 4);
@@ -994,13 +994,13 @@ __global__ void __launch_bounds__(256, 6) k_shade(ShadeArgs a) {
                 g_norm = sh.n;
                 g_alb = m.albedo;
             }
-            switch (p.integrator) {
-                case 0: integrate_direct<K>(a, &seed, tr, hit, m, sh, stack); break;
-                case 1: integrate_mats(a, &seed, tr, hit, m, sh); break;
-                case 2: integrate_mis<K>(a, &seed, tr, hit, m, sh, stack); break;
-                case 3: integrate_restir<K>(a, &seed, tr, hit, m, sh, true, prev, smp == 0, stack); break;
-                default: integrate_restir<K>(a, &seed, tr, hit, m, sh, false, prev, smp == 0, stack); break;
-            }
+            if constexpr (kIntegrator == 0) integrate_direct<K>(a, &seed, tr, hit, m, sh, stack);
+            else if constexpr (kIntegrator == 1) integrate_mats(a, &seed, tr, hit, m, sh);
+            else if constexpr (kIntegrator == 2) integrate_mis<K>(a, &seed, tr, hit, m, sh, stack);
+            else if constexpr (kIntegrator == 3)
+                integrate_restir<K>(a, &seed, tr, hit, m, sh, true, prev, smp == 0, stack);
+            else
+                integrate_restir<K>(a, &seed, tr, hit, m, sh, false, prev, smp == 0, stack);
             if (p.use_rr) {
                 const float pc =
                     fminf(fmaxf(tr.throughput.x, fmaxf(tr.throughput.y, tr.throughput.z)) + 0.001f, 0.95f);
@@ -1011,7 +1011,7 @@ __global__ void __launch_bounds__(256, 6) k_shade(ShadeArgs a) {
         acc = add(acc, tr.acc);
     }
     const int64_t pix = (int64_t)y * a.cam.width + x;
-    if (p.integrator >= 3 && a.out_res) res_store(prev, a.out_res[pix]);
+    if (kIntegrator >= 3 && a.out_res) res_store(prev, a.out_res[pix]);
     const v3 avg = divs(acc, (float)p.samples);
     float* out = a.image + 3 * pix;
     if (p.frame > 0) {  // mix(old, avg, 1 / (frame + 1))
@@ -1397,7 +1397,15 @@ extern "C" CP_API cp_status cp_shade_render(const cp_shade_scene* s, const cp_sh
     a.gbuf = gbuf;
     a.status = b.status;
     const dim3 grid((unsigned)((cam->width + 15) / 16), (unsigned)((cam->height + 15) / 16));
-    k_shade<4><<<grid, 256, 0, st>>>(a);
+    // one kernel per integrator: a launch's instruction stream holds only its
+    // own integrator's code
+    switch (p->integrator) {
+        case 0: k_shade<4, 0><<<grid, 256, 0, st>>>(a); break;
+        case 1: k_shade<4, 1><<<grid, 256, 0, st>>>(a); break;
+        case 2: k_shade<4, 2><<<grid, 256, 0, st>>>(a); break;
+        case 3: k_shade<4, 3><<<grid, 256, 0, st>>>(a); break;
+        default: k_shade<4, 4><<<grid, 256, 0, st>>>(a); break;
+    }
     note_launch();
     e = cudaGetLastError();
     if (e != cudaSuccess) return set_error(CP_ERROR_CUDA, std::string("cp_shade_render: ") + cudaGetErrorString(e));
