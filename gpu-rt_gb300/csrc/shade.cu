@@ -951,14 +951,19 @@ __device__ v3 camera_ray(const cp_shade_camera& cam, const cp_shade_params& p, u
     return normalize3(comb(r, sx, u, sy, f, 1.0f));
 }
 
-// rt.rgen:567-677, one thread per pixel; blocks of 16 x 16 pixels.  Six
-// blocks per SM (40 registers a thread, the rest spilled to local memory
-// that stays in L1): a warp's paths diverge across bounces, materials and
-// ray walks, and it is the number of resident warps, not the spills, that
-// sets the pace — the 1920 x 1440 MIS frame took 395 ms at 2 blocks per SM
-// (128 registers), 321 ms at 4, 287 ms at 5, 281 ms at 6 and 286 ms at 8.
+// rt.rgen:567-677, one thread per pixel; blocks of 16 x 16 pixels; one
+// kernel per integrator (kIntegrator), so a launch's instruction stream
+// holds only its own integrator's code and spills less.  Eight blocks per SM
+// (32 registers a thread, the rest spilled to local memory that stays in
+// L1): a warp's paths diverge across bounces, materials and ray walks, and
+// it is the number of resident warps, not the spills, that sets the pace.
+// The 1920 x 1440 MIS frame, one kernel for all integrators: 395 ms at 2
+// blocks per SM (128 registers), 321 ms at 4, 287 ms at 5, 281 ms at 6, 286
+// ms at 8 (239 ms at 6 with pow's exact cases); one kernel per integrator:
+// 236 ms at 4, 207 at 5, 194 at 6, 188 at 7 and 8 (ReSTIR 262, 236, 223,
+// 217, 217).
 template <int K, int kIntegrator>
-__global__ void __launch_bounds__(256, 6) k_shade(ShadeArgs a) {
+__global__ void __launch_bounds__(256, 8) k_shade(ShadeArgs a) {
     const int x = blockIdx.x * 16 + (threadIdx.x & 15);
     const int y = blockIdx.y * 16 + (threadIdx.x >> 4);
     if (x >= a.cam.width || y >= a.cam.height) return;
