@@ -34,7 +34,12 @@
  *     Vertices are float xyz triples with a byte stride >= 12 (48 reads the
  *     reference's VK::Mesh::Vertex layout, src/vk/mesh.h:16-22, directly).
  *   - Tie rule: among triangles at exactly the same computed distance, the one
- *     with the smallest index wins.
+ *     with the smallest index wins, among those the traversal reaches: a
+ *     box whose FP32 bound rounds to the best distance found so far is not
+ *     entered, so where two triangles share the closest point (an edge or a
+ *     vertex) the reported one can depend on the visiting order, which the
+ *     query options (seeding, traversal kind) change.  The distance and the
+ *     point do not.
  */
 #ifndef GPURT_CPQ_H
 #define GPURT_CPQ_H
