@@ -38,8 +38,8 @@
  *     box whose FP32 bound rounds to the best distance found so far is not
  *     entered, so where two triangles share the closest point (an edge or a
  *     vertex) the reported one can depend on the visiting order, which the
- *     query options (seeding, traversal kind) change.  The distance and the
- *     point do not.
+ *     query options (seeding, traversal kind) change; the distance and the
+ *     point agree to their rounding.
  */
 #ifndef GPURT_CPQ_H
 #define GPURT_CPQ_H
