@@ -470,6 +470,9 @@ def our_arm(args):
                 "bytes_per_query": {"io": B_IO, "trav": b_trav, "v_node": v_node, "v_tri": v_tri},
                 "hbm_gbs": hbm, "l2_gbs_measured": l2_gbs,
                 "hbm_only_frac": B_IO / t_kernel / 1e9 / hbm,
+                # the structure a launch walks: wide nodes (32 K bytes each) and
+                # the 80-byte test and 48-byte exact records per triangle
+                "structure_bytes": int(info.num_wide_nodes * 32 * info.branching + info.num_triangles * (80 + 48)),
                 "packet_counters": packet_visits}
     forms = None
     if world == 1 and not args.no_forms:
