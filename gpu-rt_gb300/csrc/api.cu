@@ -168,6 +168,11 @@ cudaError_t get_pool(cudaMemPool_t* out) {
         if (e != cudaSuccess) return e;
         uint64_t threshold = UINT64_MAX;
         cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &threshold);
+        // An allocation never waits on another stream's pending free: the pool
+        // grows instead, so calls on two streams (a double-buffered stream of
+        // host batches) keep overlapping rather than queueing behind each other.
+        int no_internal_waits = 0;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolReuseAllowInternalDependencies, &no_internal_waits);
         g_pools[dev] = pool;
     }
     *out = g_pools[dev];
