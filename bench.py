@@ -418,7 +418,7 @@ def our_arm(args):
                 "point": torch.empty((nq, 3), dtype=torch.float32).pin_memory()}
 
     hout = [host_outs(), host_outs()]
-    e2e_steps = max(1, min(args.steps, 10))
+    e2e_steps = max(1, min(args.steps, 30))
     mesh.query_host(qh, opts=qopts, out=hout[0])
     if world > 1:
         torch.distributed.barrier()
